@@ -1,0 +1,174 @@
+/*
+ * vfs_poisson.h -- C ABI of the GB300 pressure-Poisson projection for
+ * VFS-Wind's fractional-step loop.
+ *
+ * One handle owns one block (one DA) on one GPU: its device buffers are
+ * allocated at create / set-up time and reused across time steps.  All
+ * array arguments use the reference's PETSc DA natural layout on a single
+ * rank: scalars double[mz][my][mx] (i fastest), Cmpnts vectors
+ * double[mz][my][mx][3], with index 0 and m-1 the boundary layer
+ * (Source/init.c:157-161).  Every array pointer may be host memory or device
+ * memory of the handle's GPU; the library detects which and copies host
+ * arrays through the handle's stream.  Calls are synchronous on return and a
+ * handle is not thread-safe.
+ *
+ * Return codes: 0 on success, negative VFS_E* on failure; a failing call
+ * leaves the handle usable.  vfs_last_error() gives a message.
+ *
+ * Reference interfaces replaced (all in Source/ of SAFL-CFD-Lab/VFS-Wind):
+ *   FormMetrics               metrics.c:12         -> vfs_poisson_set_grid
+ *   setup_lidx2, PoissonLHSNew poisson.c:188, :977 -> vfs_poisson_set_nvert
+ *   PoissonRHS2_hypre + Remove_Nullspace_Scale
+ *                             poisson_hypre.c:265, :118 -> vfs_poisson_rhs
+ *   PoissonSolver_Hypre       poisson_hypre.c:506  -> vfs_poisson_solve
+ *   Remove_Nullspace          poisson_hypre.c:202  (inside vfs_poisson_solve)
+ *   Convert_Phi2_Phi          poisson.c:98         (inside vfs_poisson_solve)
+ *   UpdatePressure            poisson.c:3137       -> vfs_poisson_update_pressure
+ *   Projection                poisson.c:2700       -> vfs_poisson_projection
+ *   Divergence                main.c:936           -> vfs_poisson_divergence
+ *   MyRestriction / MyInterpolation / MyNvertRestriction
+ *                             poisson.c:365, :527, :1995 -> vfs_poisson_mg_*
+ */
+#ifndef VFS_POISSON_H
+#define VFS_POISSON_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define VFS_OK 0
+#define VFS_EINVAL (-1)     /* bad argument or size                    */
+#define VFS_ECUDA (-2)      /* CUDA runtime error                      */
+#define VFS_ESTATE (-3)     /* call order (e.g. solve before set_nvert) */
+#define VFS_ENOCONV (-4)    /* solver stopped above the tolerance      */
+#define VFS_ENOMEM (-5)     /* device allocation failed                */
+#define VFS_ETIMEOUT (-6)   /* a device-side watchdog gave up          */
+
+/* Grid of one block.  mx/my/mz are the DA sizes (nodes + 1, i.e. interior
+ * cells + 2).  The periodic flags are the reference's globals
+ * i/j/k_periodic (explicit ghost copy) and ii/jj/kk_periodic (periodic DA);
+ * either flag makes that direction periodic. */
+typedef struct {
+  int mx, my, mz;
+  int i_periodic, j_periodic, k_periodic;
+  int ii_periodic, jj_periodic, kk_periodic;
+  int bctype3; /* user->bctype[3]; -10 disables both null-space removals */
+} vfs_grid_desc;
+
+/* Solver options (defaults from vfs_poisson_default_opts). */
+typedef struct {
+  double rtol;        /* ||b - A phi||_2 / ||b||_2 target (poisson_tol)   */
+  int max_it;         /* outer iterations (poisson_it)                     */
+  int restart;        /* FGMRES restart length                             */
+  int precision;      /* 0: FP32 V-cycle in FP64 refinement, 1: all FP64   */
+  int nu1, nu2;       /* pre / post j-line sweeps per level                */
+  double omega;       /* line-Jacobi damping                               */
+  int use_graphs;     /* capture the V-cycle in a CUDA graph               */
+  int coarsest_max;   /* coarsest level cell budget                        */
+  int warm_start;     /* 1: start from the phi passed in (Phi2 warm start) */
+} vfs_solve_opts;
+
+typedef struct {
+  int iterations;
+  double rel_residual;   /* true FP64 residual at exit */
+  double initial_rel_residual;
+  double ms_total;       /* device time of the whole solve */
+  int levels;
+  int status;            /* 0 converged, VFS_ENOCONV otherwise */
+} vfs_solve_stats;
+
+typedef struct vfs_poisson vfs_poisson;
+
+const char *vfs_last_error(void);
+void vfs_poisson_default_opts(vfs_solve_opts *o);
+
+/* Create / destroy a handle on the current CUDA device. */
+int vfs_poisson_create(const vfs_grid_desc *g, vfs_poisson **out);
+void vfs_poisson_destroy(vfs_poisson *h);
+
+/* Grid: node coordinates (Cmpnts DA layout, node (i,j,k) at i < mx-1).
+ * Runs FormMetrics on the GPU.  If `face_metrics` is non-NULL it points to
+ * 12 Cmpnts arrays followed by 4 scalar arrays in the order
+ * icsi,ieta,izet, jcsi,jeta,jzet, kcsi,keta,kzet (Cmpnts) and iaj,jaj,kaj,aj
+ * (scalars) that replace the computed fine-level metrics, as a drop-in for
+ * an existing UserCtx. */
+int vfs_poisson_set_grid(vfs_poisson *h, const double *coor, const double *const *face_metrics);
+
+/* Immersed-boundary flags (0 fluid, 1 IB node, 3 solid; any value works
+ * with the reference's thresholds).  Numbers the dofs (setup_lidx2),
+ * assembles the FP64 operator (PoissonLHSNew) and builds the multigrid
+ * hierarchy.  Call again whenever the mask moves. */
+int vfs_poisson_set_nvert(vfs_poisson *h, const double *nvert);
+
+/* Right-hand side from Ucont: PoissonRHS2_hypre + Remove_Nullspace_Scale.
+ * coeff is time_coeff() (Source/poisson.c:23-31). */
+int vfs_poisson_rhs(vfs_poisson *h, const double *ucont, double dt, double st, double coeff);
+
+/* Solve A phi = b to opts->rtol, remove the fluid mean of phi
+ * (Remove_Nullspace) and write phi to `phi` in DA layout with periodic
+ * ghost copies (Convert_Phi2_Phi).  With opts->warm_start, `phi` is read
+ * first as the initial guess.  `phi` may be NULL to keep phi on the device. */
+int vfs_poisson_solve(vfs_poisson *h, double *phi, const vfs_solve_opts *opts, vfs_solve_stats *stats);
+
+/* PoissonSolver_Hypre in one call: rhs + solve. */
+int vfs_poisson_solver_hypre(vfs_poisson *h, const double *ucont, double dt, double st, double coeff,
+                             double *phi, const vfs_solve_opts *opts, vfs_solve_stats *stats);
+
+/* UpdatePressure: p += phi on fluid cells, p = 0 where nvert > 1.1, then
+ * periodic ghost copies of p and phi (both in/out, DA layout). */
+int vfs_poisson_update_pressure(vfs_poisson *h, double *p, double *phi);
+
+/* Projection: Ucont -= dt*st/coeff * (metric-weighted grad phi) using the
+ * handle's current phi, then the periodic face copy.  ucont in/out. */
+int vfs_poisson_projection(vfs_poisson *h, double *ucont, double dt, double st, double coeff);
+
+/* Divergence: max |div(Ucont) aj| over interior cells not next to a
+ * blanked cell (the "Maxdiv" diagnostic). */
+int vfs_poisson_divergence(vfs_poisson *h, const double *ucont, double *maxdiv);
+
+/* ---- inspection entry points (parity tests, drop-in diagnostics) ---- */
+
+/* Number of pressure dofs (reduced_p_size) and, if gid != NULL, the dof id
+ * per DA cell as int32 (-1 where none; periodic ghosts alias partners). */
+int vfs_poisson_get_numbering(vfs_poisson *h, int *ndof, int32_t *gid);
+
+/* The assembled FP64 operator: vol[mz][my][mx][19] in the slot order of
+ * Source/poisson.c:957-975 (zero where MatSetValues would not insert) and
+ * the row class per DA cell (0 none, 1 fluid, 2 identity). */
+int vfs_poisson_get_operator(vfs_poisson *h, double *vol, int32_t *rowtype);
+
+/* Metrics computed by vfs_poisson_set_grid; `which` indexes the order
+ * icsi,ieta,izet,jcsi,jeta,jzet,kcsi,keta,kzet,csi,eta,zet,cent (Cmpnts)
+ * = 0..12 and iaj,jaj,kaj,aj = 13..16 (scalars). */
+int vfs_poisson_get_metric(vfs_poisson *h, int which, double *out);
+
+/* The right-hand side b as a DA-layout array (zero where no dof). */
+int vfs_poisson_get_rhs(vfs_poisson *h, double *b);
+
+/* y = A x with the FP64 operator (x, y DA layout, interior cells used). */
+int vfs_poisson_apply(vfs_poisson *h, const double *x, double *y);
+
+/* Multigrid hierarchy: level count, then per level the interior sizes and
+ * the coarsening flags towards the next level (dims6 = nx,ny,nz,cx,cy,cz). */
+int vfs_poisson_mg_levels(vfs_poisson *h, int *nlevels);
+int vfs_poisson_mg_level_info(vfs_poisson *h, int level, int *dims6);
+/* nvert of a level (DA layout of that level), from MyNvertRestriction. */
+int vfs_poisson_mg_get_nvert(vfs_poisson *h, int level, double *nvert);
+/* MyRestriction from level `fine` to fine+1 and MyInterpolation from
+ * fine+1 to `fine`, on DA-layout FP64 arrays of those levels. */
+int vfs_poisson_mg_restrict(vfs_poisson *h, int fine, const double *xf, double *fc);
+int vfs_poisson_mg_interpolate(vfs_poisson *h, int fine, const double *xc, double *ff);
+/* One V-cycle z = M r of the chosen precision on DA-layout arrays. */
+int vfs_poisson_mg_vcycle(vfs_poisson *h, int precision, const double *r, double *z);
+
+/* Number of kernel launches issued by this library since the handle was
+ * created (graph-launched kernels included). */
+int64_t vfs_poisson_kernel_launches(vfs_poisson *h);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,303 @@
+"""ctypes front end of the CPU oracle (oracle/vfs_oracle.c, oracle/mg_solver.c).
+
+TEST INFRASTRUCTURE ONLY: used by tests/, by bench.py's cpu_baseline and
+reference arm, and by __graft_entry__.smoke() as the checker.  The product
+never imports it.  Parity unpinned: see the header of oracle/vfs_oracle.h.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
+SOURCES = [os.path.join(HERE, "vfs_oracle.c"), os.path.join(HERE, "mg_solver.c")]
+
+
+def build(force=False):
+    """Compile the oracle with IEEE source-order evaluation (no contraction)."""
+    os.makedirs(os.path.dirname(LIB_PATH), exist_ok=True)
+    newest = max(os.path.getmtime(s) for s in SOURCES + [os.path.join(HERE, "vfs_oracle.h")])
+    if not force and os.path.exists(LIB_PATH) and os.path.getmtime(LIB_PATH) >= newest:
+        return LIB_PATH
+    cmd = ["gcc", "-O3", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared", "-o", LIB_PATH,
+           *SOURCES, "-lm"]
+    subprocess.check_call(cmd)
+    return LIB_PATH
+
+
+class Dims(C.Structure):
+    _fields_ = [("mx", C.c_int), ("my", C.c_int), ("mz", C.c_int),
+                ("i_periodic", C.c_int), ("j_periodic", C.c_int), ("k_periodic", C.c_int),
+                ("ii_periodic", C.c_int), ("jj_periodic", C.c_int), ("kk_periodic", C.c_int)]
+
+
+METRIC_FIELDS = ["cent", "csi", "eta", "zet", "aj", "icsi", "ieta", "izet", "iaj",
+                 "jcsi", "jeta", "jzet", "jaj", "kcsi", "keta", "kzet", "kaj"]
+VECTOR_FIELDS = {"cent", "csi", "eta", "zet", "icsi", "ieta", "izet", "jcsi", "jeta", "jzet",
+                 "kcsi", "keta", "kzet"}
+
+
+class Metrics(C.Structure):
+    _fields_ = [(f, C.POINTER(C.c_double)) for f in METRIC_FIELDS]
+
+
+class SolveOpts(C.Structure):
+    _fields_ = [("max_it", C.c_int), ("restart", C.c_int), ("rtol", C.c_double),
+                ("nu1", C.c_int), ("nu2", C.c_int), ("omega", C.c_double),
+                ("threads", C.c_int), ("coarsest_max", C.c_int)]
+
+
+class SolveStats(C.Structure):
+    _fields_ = [("iterations", C.c_int), ("rel_residual", C.c_double),
+                ("setup_ms", C.c_double), ("solve_ms", C.c_double), ("levels", C.c_int)]
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = C.CDLL(LIB_PATH)
+        P = C.POINTER
+        dp, ip = P(C.c_double), P(C.c_int)
+        L.or_form_metrics.argtypes = [P(Dims), dp, P(Metrics)]
+        L.or_setup_lidx2.argtypes = [P(Dims), dp, ip]
+        L.or_setup_lidx2.restype = C.c_int
+        L.or_poisson_lhs.argtypes = [P(Dims), dp, P(Metrics), C.c_int, C.c_int, ip, ip, dp, ip]
+        L.or_poisson_lhs.restype = C.c_int
+        L.or_poisson_rhs2_hypre.argtypes = [P(Dims), dp, ip, dp, C.c_double, C.c_double, C.c_double, dp]
+        L.or_remove_nullspace_scale.argtypes = [P(Dims), dp, ip, dp, dp, C.c_int]
+        L.or_remove_nullspace.argtypes = [P(Dims), dp, ip, dp, C.c_int]
+        L.or_convert_phi2_phi.argtypes = [P(Dims), dp, dp, dp]
+        L.or_update_pressure.argtypes = [P(Dims), dp, dp, dp]
+        L.or_projection.argtypes = [P(Dims), dp, dp, P(Metrics), C.c_double, C.c_double, C.c_double, dp]
+        L.or_divergence.argtypes = [P(Dims), dp, dp, dp]
+        L.or_divergence.restype = C.c_double
+        L.or_my_nvert_restriction.argtypes = [P(Dims), P(Dims), C.c_int, C.c_int, C.c_int, dp, dp]
+        L.or_my_restriction.argtypes = [P(Dims), P(Dims), C.c_int, C.c_int, C.c_int, dp, dp, dp, dp]
+        L.or_my_interpolation.argtypes = [P(Dims), P(Dims), C.c_int, C.c_int, C.c_int, dp, dp, dp, dp]
+        L.or_mg_create.argtypes = [P(Dims), dp, dp, P(Metrics), P(SolveOpts)]
+        L.or_mg_create.restype = C.c_void_p
+        L.or_mg_solve.argtypes = [C.c_void_p, dp, dp, P(SolveOpts), P(SolveStats)]
+        L.or_mg_solve.restype = C.c_int
+        L.or_mg_vcycle.argtypes = [C.c_void_p, dp, dp]
+        L.or_mg_level_info.argtypes = [C.c_void_p, C.c_int, ip]
+        L.or_mg_level_info.restype = C.c_int
+        L.or_mg_destroy.argtypes = [C.c_void_p]
+        _lib = L
+    return _lib
+
+
+def _dp(a):
+    assert a.dtype == np.float64 and a.flags.c_contiguous
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def _ip(a):
+    assert a.dtype == np.int32 and a.flags.c_contiguous
+    return a.ctypes.data_as(C.POINTER(C.c_int))
+
+
+def dims(mx, my, mz, periodic):
+    return Dims(mx, my, mz, *[int(p) for p in periodic])
+
+
+def dims_of(case):
+    mx, my, mz = case.dims
+    return dims(mx, my, mz, case.periodic)
+
+
+def form_metrics(d, coor):
+    shape = (d.mz, d.my, d.mx)
+    out = {f: np.zeros(shape + ((3,) if f in VECTOR_FIELDS else ()), dtype=np.float64)
+           for f in METRIC_FIELDS}
+    m = metrics_struct(out)
+    lib().or_form_metrics(C.byref(d), _dp(np.ascontiguousarray(coor)), C.byref(m))
+    return out
+
+
+def metrics_struct(met):
+    return Metrics(*[_dp(met[f]) for f in METRIC_FIELDS])
+
+
+def poisson_lhs(d, nvert, met, scale_by_aj=False, apply_filter=True):
+    n = d.mx * d.my * d.mz
+    gid = np.zeros(n, np.int32)
+    rt = np.zeros(n, np.int32)
+    vol = np.zeros(n * 19)
+    col = np.zeros(n * 19, np.int32)
+    m = metrics_struct(met)
+    ndof = lib().or_poisson_lhs(C.byref(d), _dp(np.ascontiguousarray(nvert, np.float64)), C.byref(m),
+                                int(scale_by_aj), int(apply_filter), _ip(gid), _ip(rt), _dp(vol), _ip(col))
+    shape = (d.mz, d.my, d.mx)
+    return dict(ndof=ndof, gid=gid.reshape(shape), rowtype=rt.reshape(shape),
+                vol=vol.reshape(shape + (19,)), col=col.reshape(shape + (19,)))
+
+
+def csr(lhs):
+    """Assemble the reference's matrix (MatSetValues INSERT semantics) as CSR."""
+    import scipy.sparse as sp
+    rt = lhs["rowtype"].ravel()
+    gid = lhs["gid"].ravel()
+    vol = lhs["vol"].reshape(-1, 19)
+    col = lhs["col"].reshape(-1, 19)
+    rows, cols, vals = [], [], []
+    cells = np.nonzero(rt > 0)[0]
+    for s in range(19):
+        c = col[cells, s]
+        keep = c >= 0
+        rows.append(gid[cells][keep])
+        cols.append(c[keep])
+        vals.append(vol[cells, s][keep])
+    rows = np.concatenate(rows)
+    cols = np.concatenate(cols)
+    vals = np.concatenate(vals)
+    n = lhs["ndof"]
+    # INSERT semantics: a later slot with the same column replaces the value
+    order = np.lexsort((np.arange(len(rows)), cols, rows))
+    rows, cols, vals = rows[order], cols[order], vals[order]
+    last = np.ones(len(rows), bool)
+    last[:-1] = (rows[1:] != rows[:-1]) | (cols[1:] != cols[:-1])
+    return sp.csr_matrix((vals[last], (rows[last], cols[last])), shape=(n, n))
+
+
+def rhs(d, nvert, gid, ucont, aj, dt=1.0, st=1.0, coeff=1.0, bctype3=0):
+    n = int(gid.max()) + 1
+    b = np.zeros(max(n, 1))
+    g = np.ascontiguousarray(gid, np.int32).ravel()
+    nv = np.ascontiguousarray(nvert, np.float64)
+    lib().or_poisson_rhs2_hypre(C.byref(d), _dp(nv), _ip(g), _dp(np.ascontiguousarray(ucont)), dt, st, coeff, _dp(b))
+    lib().or_remove_nullspace_scale(C.byref(d), _dp(nv), _ip(g), _dp(np.ascontiguousarray(aj)), _dp(b), bctype3)
+    return b[:n]
+
+
+def rhs_raw(d, nvert, gid, ucont, dt=1.0, st=1.0, coeff=1.0):
+    n = int(gid.max()) + 1
+    b = np.zeros(max(n, 1))
+    g = np.ascontiguousarray(gid, np.int32).ravel()
+    lib().or_poisson_rhs2_hypre(C.byref(d), _dp(np.ascontiguousarray(nvert, np.float64)), _ip(g),
+                                _dp(np.ascontiguousarray(ucont)), dt, st, coeff, _dp(b))
+    return b[:n]
+
+
+def remove_nullspace(d, nvert, gid, phi2, bctype3=0):
+    p = np.ascontiguousarray(phi2, np.float64).copy()
+    lib().or_remove_nullspace(C.byref(d), _dp(np.ascontiguousarray(nvert, np.float64)),
+                              _ip(np.ascontiguousarray(gid, np.int32).ravel()), _dp(p), bctype3)
+    return p
+
+
+def convert_phi2_phi(d, nvert, phi2):
+    phi = np.zeros((d.mz, d.my, d.mx))
+    lib().or_convert_phi2_phi(C.byref(d), _dp(np.ascontiguousarray(nvert, np.float64)),
+                              _dp(np.ascontiguousarray(phi2, np.float64)), _dp(phi))
+    return phi
+
+
+def update_pressure(d, nvert, p, phi):
+    p = np.ascontiguousarray(p, np.float64).copy()
+    phi = np.ascontiguousarray(phi, np.float64).copy()
+    lib().or_update_pressure(C.byref(d), _dp(np.ascontiguousarray(nvert, np.float64)), _dp(p), _dp(phi))
+    return p, phi
+
+
+def projection(d, nvert, phi, met, ucont, dt=1.0, st=1.0, coeff=1.0):
+    u = np.ascontiguousarray(ucont, np.float64).copy()
+    m = metrics_struct(met)
+    lib().or_projection(C.byref(d), _dp(np.ascontiguousarray(nvert, np.float64)),
+                        _dp(np.ascontiguousarray(phi, np.float64)), C.byref(m), dt, st, coeff, _dp(u))
+    return u
+
+
+def divergence(d, nvert, ucont, aj):
+    return lib().or_divergence(C.byref(d), _dp(np.ascontiguousarray(nvert, np.float64)),
+                               _dp(np.ascontiguousarray(ucont, np.float64)), _dp(np.ascontiguousarray(aj)))
+
+
+def nvert_restriction(dh, dc, isc, jsc, ksc, nvert_h):
+    out = np.zeros((dc.mz, dc.my, dc.mx))
+    lib().or_my_nvert_restriction(C.byref(dh), C.byref(dc), isc, jsc, ksc,
+                                  _dp(np.ascontiguousarray(nvert_h, np.float64)), _dp(out))
+    return out
+
+
+def restriction(dc, df, isc, jsc, ksc, nvert_c, nvert_f, xf):
+    out = np.zeros((dc.mz, dc.my, dc.mx))
+    lib().or_my_restriction(C.byref(dc), C.byref(df), isc, jsc, ksc, _dp(np.ascontiguousarray(nvert_c)),
+                            _dp(np.ascontiguousarray(nvert_f)), _dp(np.ascontiguousarray(xf)), _dp(out))
+    return out
+
+
+def interpolation(df, dc, isc, jsc, ksc, nvert_f, nvert_c, xc):
+    out = np.zeros((df.mz, df.my, df.mx))
+    lib().or_my_interpolation(C.byref(df), C.byref(dc), isc, jsc, ksc, _dp(np.ascontiguousarray(nvert_f)),
+                              _dp(np.ascontiguousarray(nvert_c)), _dp(np.ascontiguousarray(xc)), _dp(out))
+    return out
+
+
+class MGSolver:
+    """FP64 FGMRES + geometric V-cycle on the CPU (timed CPU baseline)."""
+
+    def __init__(self, d, coor, nvert, met=None, threads=0, coarsest_max=128):
+        self.d = d
+        self.opts = SolveOpts(max_it=200, restart=30, rtol=1e-8, nu1=2, nu2=2, omega=0.8,
+                              threads=threads, coarsest_max=coarsest_max)
+        self._met = met
+        m = C.byref(metrics_struct(met)) if met is not None else None
+        self.h = lib().or_mg_create(C.byref(d), _dp(np.ascontiguousarray(coor)),
+                                    _dp(np.ascontiguousarray(nvert, np.float64)), m, C.byref(self.opts))
+
+    def levels(self):
+        v = np.zeros(7, np.int32)
+        n = lib().or_mg_level_info(self.h, 0, _ip(v))
+        out = []
+        for li in range(n):
+            lib().or_mg_level_info(self.h, li, _ip(v))
+            out.append(tuple(int(x) for x in v))
+        return out
+
+    def solve(self, b_da, x0_da=None, rtol=1e-8, max_it=200, restart=30, nu1=2, nu2=2, omega=0.8):
+        self.opts.rtol, self.opts.max_it, self.opts.restart = rtol, max_it, restart
+        self.opts.nu1, self.opts.nu2, self.opts.omega = nu1, nu2, omega
+        x = np.zeros((self.d.mz, self.d.my, self.d.mx)) if x0_da is None else np.ascontiguousarray(x0_da).copy()
+        st = SolveStats()
+        lib().or_mg_solve(self.h, _dp(np.ascontiguousarray(b_da)), _dp(x), C.byref(self.opts), C.byref(st))
+        return x, st
+
+    def vcycle(self, r_da):
+        z = np.zeros((self.d.mz, self.d.my, self.d.mx))
+        lib().or_mg_vcycle(self.h, _dp(np.ascontiguousarray(r_da)), _dp(z))
+        return z
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().or_mg_destroy(self.h)
+            self.h = None
+
+
+def to_da(d, gid, v2):
+    """Scatter a dof vector onto the DA layout (zero where there is no dof)."""
+    out = np.zeros(d.mz * d.my * d.mx)
+    g = gid.ravel()
+    inner = np.zeros((d.mz, d.my, d.mx), bool)
+    inner[1:-1, 1:-1, 1:-1] = True
+    sel = inner.ravel() & (g >= 0)
+    out[sel] = v2[g[sel]]
+    return out.reshape(d.mz, d.my, d.mx)
+
+
+def from_da(d, gid, v):
+    g = gid.ravel()
+    inner = np.zeros((d.mz, d.my, d.mx), bool)
+    inner[1:-1, 1:-1, 1:-1] = True
+    sel = inner.ravel() & (g >= 0)
+    n = int(g.max()) + 1
+    out = np.zeros(n)
+    out[g[sel]] = v.ravel()[sel]
+    return out

@@ -1,0 +1,1048 @@
+/*
+ * vfs_oracle.c -- CPU restatement of VFS-Wind's pressure-Poisson hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY (checker + timed CPU baseline).  Parity unpinned:
+ * the reference cannot be built here (it needs PETSc 3.1 / HYPRE / MPI) and
+ * ships no golden vectors for this path.  Every function cites the reference
+ * file:line it restates.  Compile with -ffp-contract=off so that every
+ * floating-point expression is evaluated in the reference's source order on
+ * both x86-64 and aarch64 hosts.
+ */
+#include "vfs_oracle.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+#define IX(d, i, j, k) ((size_t)(((size_t)(k) * (size_t)(d)->my + (size_t)(j)) * (size_t)(d)->mx + (size_t)(i)))
+
+static const double POISSON_THRESHOLD = 0.1; /* Source/main.c:124 */
+
+static inline int per_i(const or_dims *d) { return d->i_periodic || d->ii_periodic; }
+static inline int per_j(const or_dims *d) { return d->j_periodic || d->jj_periodic; }
+static inline int per_k(const or_dims *d) { return d->k_periodic || d->kk_periodic; }
+
+/* Ghost remap repeated throughout the reference (e.g. Source/poisson.c:1143-1161,
+ * :154-174, :3258-3276; Source/metrics.c:365-383).  Index 0 / m-1 of a periodic
+ * direction take the value of cell m-2 / 1.  The ii/jj/kk variants address the
+ * periodic DA's ghost index -2 / m+1, which hold exactly those cells. */
+static inline int remap(const or_dims *d, int i, int j, int k, int *a, int *b, int *c,
+                        int *fi, int *fj, int *fk)
+{
+  int ia = i, jb = j, kc = k, f1 = 0, f2 = 0, f3 = 0;
+  if (per_i(d)) {
+    if (i == 0) ia = d->mx - 2, f1 = 1;
+    else if (i == d->mx - 1) ia = 1, f1 = 1;
+  }
+  if (per_j(d)) {
+    if (j == 0) jb = d->my - 2, f2 = 1;
+    else if (j == d->my - 1) jb = 1, f2 = 1;
+  }
+  if (per_k(d)) {
+    if (k == 0) kc = d->mz - 2, f3 = 1;
+    else if (k == d->mz - 1) kc = 1, f3 = 1;
+  }
+  *a = ia; *b = jb; *c = kc;
+  if (fi) *fi = f1;
+  if (fj) *fj = f2;
+  if (fk) *fk = f3;
+  return f1 | f2 | f3;
+}
+
+/* ------------------------------------------------------------------------ */
+/* FormMetrics (Source/metrics.c:12-810, NEWMETRIC not defined for this TU). */
+/* ------------------------------------------------------------------------ */
+void or_form_metrics(const or_dims *d, const double *coor, or_metrics *m)
+{
+  const int mx = d->mx, my = d->my, mz = d->mz;
+  const size_t n = (size_t)mx * my * mz;
+#define CO(i, j, k, c) coor[IX(d, i, j, k) * 3 + (c)]
+  if (m->cent) memset(m->cent, 0, n * 3 * sizeof(double));
+  memset(m->csi, 0, n * 3 * sizeof(double));
+  memset(m->eta, 0, n * 3 * sizeof(double));
+  memset(m->zet, 0, n * 3 * sizeof(double));
+  memset(m->aj, 0, n * sizeof(double));
+  memset(m->icsi, 0, n * 3 * sizeof(double)); memset(m->ieta, 0, n * 3 * sizeof(double));
+  memset(m->izet, 0, n * 3 * sizeof(double)); memset(m->iaj, 0, n * sizeof(double));
+  memset(m->jcsi, 0, n * 3 * sizeof(double)); memset(m->jeta, 0, n * 3 * sizeof(double));
+  memset(m->jzet, 0, n * 3 * sizeof(double)); memset(m->jaj, 0, n * sizeof(double));
+  memset(m->kcsi, 0, n * 3 * sizeof(double)); memset(m->keta, 0, n * 3 * sizeof(double));
+  memset(m->kzet, 0, n * 3 * sizeof(double)); memset(m->kaj, 0, n * sizeof(double));
+
+  /* cell centres: metrics.c:103-121 */
+  if (m->cent) {
+    for (int k = 1; k < mz - 1; k++)
+      for (int j = 1; j < my - 1; j++)
+        for (int i = 1; i < mx - 1; i++)
+          for (int c = 0; c < 3; c++)
+            m->cent[IX(d, i, j, k) * 3 + c] =
+                0.125 * (CO(i, j, k, c) + CO(i, j - 1, k, c) + CO(i, j, k - 1, c) +
+                         CO(i, j - 1, k - 1, c) + CO(i - 1, j, k, c) + CO(i - 1, j - 1, k, c) +
+                         CO(i - 1, j, k - 1, c) + CO(i - 1, j - 1, k - 1, c));
+  }
+
+  /* face-normal "cell" metrics, non-NEWMETRIC path: metrics.c:128-199 */
+  for (int k = 1; k < mz - 1; k++)
+    for (int j = 1; j < my - 1; j++)
+      for (int i = 0; i < mx - 1; i++) {
+        double de[3], dz[3];
+        for (int c = 0; c < 3; c++) {
+          de[c] = 0.5 * (CO(i, j, k, c) + CO(i, j, k - 1, c) - CO(i, j - 1, k, c) - CO(i, j - 1, k - 1, c));
+          dz[c] = 0.5 * (CO(i, j - 1, k, c) + CO(i, j, k, c) - CO(i, j - 1, k - 1, c) - CO(i, j, k - 1, c));
+        }
+        double *o = &m->csi[IX(d, i, j, k) * 3];
+        o[0] = de[1] * dz[2] - de[2] * dz[1];
+        o[1] = -de[0] * dz[2] + de[2] * dz[0];
+        o[2] = de[0] * dz[1] - de[1] * dz[0];
+      }
+  for (int k = 1; k < mz - 1; k++)
+    for (int j = 0; j < my - 1; j++)
+      for (int i = 1; i < mx - 1; i++) {
+        double dc[3], dz[3];
+        for (int c = 0; c < 3; c++) {
+          dc[c] = 0.5 * (CO(i, j, k, c) + CO(i, j, k - 1, c) - CO(i - 1, j, k, c) - CO(i - 1, j, k - 1, c));
+          dz[c] = 0.5 * (CO(i, j, k, c) + CO(i - 1, j, k, c) - CO(i, j, k - 1, c) - CO(i - 1, j, k - 1, c));
+        }
+        double *o = &m->eta[IX(d, i, j, k) * 3];
+        o[0] = dz[1] * dc[2] - dz[2] * dc[1];
+        o[1] = -dz[0] * dc[2] + dz[2] * dc[0];
+        o[2] = dz[0] * dc[1] - dz[1] * dc[0];
+      }
+  for (int k = 0; k < mz - 1; k++)
+    for (int j = 1; j < my - 1; j++)
+      for (int i = 1; i < mx - 1; i++) {
+        double dc[3], de[3];
+        for (int c = 0; c < 3; c++) {
+          dc[c] = 0.5 * (CO(i, j, k, c) + CO(i, j - 1, k, c) - CO(i - 1, j, k, c) - CO(i - 1, j - 1, k, c));
+          de[c] = 0.5 * (CO(i, j, k, c) + CO(i - 1, j, k, c) - CO(i, j - 1, k, c) - CO(i - 1, j - 1, k, c));
+        }
+        double *o = &m->zet[IX(d, i, j, k) * 3];
+        o[0] = dc[1] * de[2] - dc[2] * de[1];
+        o[1] = -dc[0] * de[2] + dc[2] * de[0];
+        o[2] = dc[0] * de[1] - dc[1] * de[0];
+      }
+
+  /* Jacobian aj = 1/J of interior cells: metrics.c:202-259 */
+  for (int k = 1; k < mz - 1; k++)
+    for (int j = 1; j < my - 1; j++)
+      for (int i = 1; i < mx - 1; i++) {
+        double dc[3], de[3], dz[3];
+        for (int c = 0; c < 3; c++) {
+          dc[c] = 0.25 * (CO(i, j, k, c) + CO(i, j - 1, k, c) + CO(i, j, k - 1, c) + CO(i, j - 1, k - 1, c) -
+                          CO(i - 1, j, k, c) - CO(i - 1, j - 1, k, c) - CO(i - 1, j, k - 1, c) -
+                          CO(i - 1, j - 1, k - 1, c));
+          de[c] = 0.25 * (CO(i, j, k, c) + CO(i - 1, j, k, c) + CO(i, j, k - 1, c) + CO(i - 1, j, k - 1, c) -
+                          CO(i, j - 1, k, c) - CO(i - 1, j - 1, k, c) - CO(i, j - 1, k - 1, c) -
+                          CO(i - 1, j - 1, k - 1, c));
+          dz[c] = 0.25 * (CO(i, j, k, c) + CO(i, j - 1, k, c) + CO(i - 1, j, k, c) + CO(i - 1, j - 1, k, c) -
+                          CO(i, j, k - 1, c) - CO(i, j - 1, k - 1, c) - CO(i - 1, j, k - 1, c) -
+                          CO(i - 1, j - 1, k - 1, c));
+        }
+        double det = dc[0] * (de[1] * dz[2] - de[2] * dz[1]) - dc[1] * (de[0] * dz[2] - de[2] * dz[0]) +
+                     dc[2] * (de[0] * dz[1] - de[1] * dz[0]);
+        m->aj[IX(d, i, j, k)] = 1. / det;
+      }
+
+  /* boundary mirror: metrics.c:262-342 (csi not mirrored in i, eta not in j,
+   * zet not in k without NEWMETRIC) */
+  for (int k = 0; k < mz; k++)
+    for (int j = 0; j < my; j++) {
+      size_t a0 = IX(d, 0, j, k), a1 = IX(d, 1, j, k);
+      size_t b0 = IX(d, mx - 1, j, k), b1 = IX(d, mx - 2, j, k);
+      for (int c = 0; c < 3; c++) {
+        m->eta[a0 * 3 + c] = m->eta[a1 * 3 + c]; m->zet[a0 * 3 + c] = m->zet[a1 * 3 + c];
+      }
+      m->aj[a0] = m->aj[a1];
+      for (int c = 0; c < 3; c++) {
+        m->eta[b0 * 3 + c] = m->eta[b1 * 3 + c]; m->zet[b0 * 3 + c] = m->zet[b1 * 3 + c];
+      }
+      m->aj[b0] = m->aj[b1];
+    }
+  for (int k = 0; k < mz; k++)
+    for (int i = 0; i < mx; i++) {
+      size_t a0 = IX(d, i, 0, k), a1 = IX(d, i, 1, k);
+      size_t b0 = IX(d, i, my - 1, k), b1 = IX(d, i, my - 2, k);
+      for (int c = 0; c < 3; c++) {
+        m->csi[a0 * 3 + c] = m->csi[a1 * 3 + c]; m->zet[a0 * 3 + c] = m->zet[a1 * 3 + c];
+      }
+      m->aj[a0] = m->aj[a1];
+      for (int c = 0; c < 3; c++) {
+        m->csi[b0 * 3 + c] = m->csi[b1 * 3 + c]; m->zet[b0 * 3 + c] = m->zet[b1 * 3 + c];
+      }
+      m->aj[b0] = m->aj[b1];
+    }
+  for (int j = 0; j < my; j++)
+    for (int i = 0; i < mx; i++) {
+      size_t a0 = IX(d, i, j, 0), a1 = IX(d, i, j, 1);
+      size_t b0 = IX(d, i, j, mz - 1), b1 = IX(d, i, j, mz - 2);
+      for (int c = 0; c < 3; c++) {
+        m->eta[a0 * 3 + c] = m->eta[a1 * 3 + c]; m->csi[a0 * 3 + c] = m->csi[a1 * 3 + c];
+      }
+      m->aj[a0] = m->aj[a1];
+      for (int c = 0; c < 3; c++) {
+        m->eta[b0 * 3 + c] = m->eta[b1 * 3 + c]; m->csi[b0 * 3 + c] = m->csi[b1 * 3 + c];
+      }
+      m->aj[b0] = m->aj[b1];
+    }
+  /* periodic ghost copy of cell metrics: metrics.c:360-397 */
+  for (int k = 0; k < mz; k++)
+    for (int j = 0; j < my; j++)
+      for (int i = 0; i < mx; i++) {
+        int a, b, c;
+        if (!remap(d, i, j, k, &a, &b, &c, 0, 0, 0)) continue;
+        size_t s = IX(d, a, b, c), t = IX(d, i, j, k);
+        for (int q = 0; q < 3; q++) {
+          m->csi[t * 3 + q] = m->csi[s * 3 + q];
+          m->eta[t * 3 + q] = m->eta[s * 3 + q];
+          m->zet[t * 3 + q] = m->zet[s * 3 + q];
+        }
+        m->aj[t] = m->aj[s];
+      }
+
+  /* face metrics from face-centre differences.  i faces: metrics.c:478-574 */
+  {
+    double *cx = (double *)calloc(n * 3, sizeof(double));
+    for (int k = 1; k < mz; k++)
+      for (int j = 1; j < my; j++)
+        for (int i = 0; i < mx; i++) {
+          if (i > mx - 2 || j > my - 2 || k > mz - 2) continue; /* nodes stop at m-2 */
+          for (int c = 0; c < 3; c++)
+            cx[IX(d, i, j, k) * 3 + c] =
+                (CO(i, j, k, c) + CO(i, j, k - 1, c) + CO(i, j - 1, k, c) + CO(i, j - 1, k - 1, c)) * 0.25;
+        }
+#define CX(i, j, k, c) cx[IX(d, i, j, k) * 3 + (c)]
+    for (int k = 1; k < mz - 1; k++)
+      for (int j = 1; j < my - 1; j++)
+        for (int i = 0; i < mx - 1; i++) {
+          double dc[3], de[3], dz[3];
+          for (int c = 0; c < 3; c++) {
+            if (i == 0) dc[c] = CX(i + 1, j, k, c) - CX(i, j, k, c);
+            else if (i == mx - 2) dc[c] = CX(i, j, k, c) - CX(i - 1, j, k, c);
+            else dc[c] = (CX(i + 1, j, k, c) - CX(i - 1, j, k, c)) * 0.5;
+            if (j == 1) de[c] = CX(i, j + 1, k, c) - CX(i, j, k, c);
+            else if (j == my - 2) de[c] = CX(i, j, k, c) - CX(i, j - 1, k, c);
+            else de[c] = (CX(i, j + 1, k, c) - CX(i, j - 1, k, c)) * 0.5;
+            if (k == 1) dz[c] = (CX(i, j, k + 1, c) - CX(i, j, k, c));
+            else if (k == mz - 2) dz[c] = (CX(i, j, k, c) - CX(i, j, k - 1, c));
+            else dz[c] = (CX(i, j, k + 1, c) - CX(i, j, k - 1, c)) * 0.5;
+          }
+          size_t t = IX(d, i, j, k);
+          double *ci = &m->icsi[t * 3], *ei = &m->ieta[t * 3], *zi = &m->izet[t * 3];
+          ci[0] = de[1] * dz[2] - de[2] * dz[1];
+          ci[1] = -de[0] * dz[2] + de[2] * dz[0];
+          ci[2] = de[0] * dz[1] - de[1] * dz[0];
+          ei[0] = dz[1] * dc[2] - dz[2] * dc[1];
+          ei[1] = -dz[0] * dc[2] + dz[2] * dc[0];
+          ei[2] = dz[0] * dc[1] - dz[1] * dc[0];
+          zi[0] = dc[1] * de[2] - dc[2] * de[1];
+          zi[1] = -dc[0] * de[2] + dc[2] * de[0];
+          zi[2] = dc[0] * de[1] - dc[1] * de[0];
+          double det = dc[0] * (de[1] * dz[2] - de[2] * dz[1]) - dc[1] * (de[0] * dz[2] - de[2] * dz[0]) +
+                       dc[2] * (de[0] * dz[1] - de[1] * dz[0]);
+          m->iaj[t] = 1. / det;
+        }
+#undef CX
+    /* j faces: metrics.c:587-682 */
+    memset(cx, 0, n * 3 * sizeof(double));
+    for (int k = 1; k < mz - 1; k++)
+      for (int j = 0; j < my - 1; j++)
+        for (int i = 1; i < mx - 1; i++)
+          for (int c = 0; c < 3; c++)
+            cx[IX(d, i, j, k) * 3 + c] =
+                (CO(i, j, k, c) + CO(i, j, k - 1, c) + CO(i - 1, j, k, c) + CO(i - 1, j, k - 1, c)) * 0.25;
+#define CY(i, j, k, c) cx[IX(d, i, j, k) * 3 + (c)]
+    for (int k = 1; k < mz - 1; k++)
+      for (int j = 0; j < my - 1; j++)
+        for (int i = 1; i < mx - 1; i++) {
+          double dc[3], de[3], dz[3];
+          for (int c = 0; c < 3; c++) {
+            if (i == 1) dc[c] = CY(i + 1, j, k, c) - CY(i, j, k, c);
+            else if (i == mx - 2) dc[c] = CY(i, j, k, c) - CY(i - 1, j, k, c);
+            else dc[c] = (CY(i + 1, j, k, c) - CY(i - 1, j, k, c)) * 0.5;
+            if (j == 0) de[c] = CY(i, j + 1, k, c) - CY(i, j, k, c);
+            else if (j == my - 2) de[c] = CY(i, j, k, c) - CY(i, j - 1, k, c);
+            else de[c] = (CY(i, j + 1, k, c) - CY(i, j - 1, k, c)) * 0.5;
+            if (k == 1) dz[c] = (CY(i, j, k + 1, c) - CY(i, j, k, c));
+            else if (k == mz - 2) dz[c] = (CY(i, j, k, c) - CY(i, j, k - 1, c));
+            else dz[c] = (CY(i, j, k + 1, c) - CY(i, j, k - 1, c)) * 0.5;
+          }
+          size_t t = IX(d, i, j, k);
+          double *ci = &m->jcsi[t * 3], *ei = &m->jeta[t * 3], *zi = &m->jzet[t * 3];
+          ci[0] = de[1] * dz[2] - de[2] * dz[1];
+          ci[1] = -de[0] * dz[2] + de[2] * dz[0];
+          ci[2] = de[0] * dz[1] - de[1] * dz[0];
+          ei[0] = dz[1] * dc[2] - dz[2] * dc[1];
+          ei[1] = -dz[0] * dc[2] + dz[2] * dc[0];
+          ei[2] = dz[0] * dc[1] - dz[1] * dc[0];
+          zi[0] = dc[1] * de[2] - dc[2] * de[1];
+          zi[1] = -dc[0] * de[2] + dc[2] * de[0];
+          zi[2] = dc[0] * de[1] - dc[1] * de[0];
+          double det = dc[0] * (de[1] * dz[2] - de[2] * dz[1]) - dc[1] * (de[0] * dz[2] - de[2] * dz[0]) +
+                       dc[2] * (de[0] * dz[1] - de[1] * dz[0]);
+          m->jaj[t] = 1. / det;
+        }
+#undef CY
+    /* k faces: metrics.c:695-790 */
+    memset(cx, 0, n * 3 * sizeof(double));
+    for (int k = 0; k < mz - 1; k++)
+      for (int j = 1; j < my - 1; j++)
+        for (int i = 1; i < mx - 1; i++)
+          for (int c = 0; c < 3; c++)
+            cx[IX(d, i, j, k) * 3 + c] =
+                (CO(i, j, k, c) + CO(i, j - 1, k, c) + CO(i - 1, j, k, c) + CO(i - 1, j - 1, k, c)) * 0.25;
+#define CZ(i, j, k, c) cx[IX(d, i, j, k) * 3 + (c)]
+    for (int k = 0; k < mz - 1; k++)
+      for (int j = 1; j < my - 1; j++)
+        for (int i = 1; i < mx - 1; i++) {
+          double dc[3], de[3], dz[3];
+          for (int c = 0; c < 3; c++) {
+            if (i == 1) dc[c] = CZ(i + 1, j, k, c) - CZ(i, j, k, c);
+            else if (i == mx - 2) dc[c] = CZ(i, j, k, c) - CZ(i - 1, j, k, c);
+            else dc[c] = (CZ(i + 1, j, k, c) - CZ(i - 1, j, k, c)) * 0.5;
+            if (j == 1) de[c] = CZ(i, j + 1, k, c) - CZ(i, j, k, c);
+            else if (j == my - 2) de[c] = CZ(i, j, k, c) - CZ(i, j - 1, k, c);
+            else de[c] = (CZ(i, j + 1, k, c) - CZ(i, j - 1, k, c)) * 0.5;
+            if (k == 0) dz[c] = (CZ(i, j, k + 1, c) - CZ(i, j, k, c));
+            else if (k == mz - 2) dz[c] = (CZ(i, j, k, c) - CZ(i, j, k - 1, c));
+            else dz[c] = (CZ(i, j, k + 1, c) - CZ(i, j, k - 1, c)) * 0.5;
+          }
+          size_t t = IX(d, i, j, k);
+          double *ci = &m->kcsi[t * 3], *ei = &m->keta[t * 3], *zi = &m->kzet[t * 3];
+          ci[0] = de[1] * dz[2] - de[2] * dz[1];
+          ci[1] = -de[0] * dz[2] + de[2] * dz[0];
+          ci[2] = de[0] * dz[1] - de[1] * dz[0];
+          ei[0] = dz[1] * dc[2] - dz[2] * dc[1];
+          ei[1] = -dz[0] * dc[2] + dz[2] * dc[0];
+          ei[2] = dz[0] * dc[1] - dz[1] * dc[0];
+          zi[0] = dc[1] * de[2] - dc[2] * de[1];
+          zi[1] = -dc[0] * de[2] + dc[2] * de[0];
+          zi[2] = dc[0] * de[1] - dc[1] * de[0];
+          double det = dc[0] * (de[1] * dz[2] - de[2] * dz[1]) - dc[1] * (de[0] * dz[2] - de[2] * dz[0]) +
+                       dc[2] * (de[0] * dz[1] - de[1] * dz[0]);
+          m->kaj[t] = 1. / det;
+        }
+#undef CZ
+    free(cx);
+  }
+#undef CO
+}
+
+/* ------------------------------------------------------------------------ */
+/* setup_lidx2 (Source/poisson.c:188-335), poisson != -1 branch.            */
+/* Returns the number of pressure dofs; gid is -1 where there is no dof.    */
+/* ------------------------------------------------------------------------ */
+int or_setup_lidx2(const or_dims *d, const double *nvert, int *gid)
+{
+  const int mx = d->mx, my = d->my, mz = d->mz;
+  int n = 0;
+  for (size_t q = 0; q < (size_t)mx * my * mz; q++) gid[q] = -1;
+  for (int k = 0; k < mz; k++)
+    for (int j = 0; j < my; j++)
+      for (int i = 0; i < mx; i++) {
+        if (i == 0 || i == mx - 1 || j == 0 || j == my - 1 || k == 0 || k == mz - 1) continue;
+        if ((int)nvert[IX(d, i, j, k)] > POISSON_THRESHOLD) continue; /* poisson.c:246 */
+        gid[IX(d, i, j, k)] = n++;
+      }
+  /* periodic aliasing of ghost ids: poisson.c:299-332 */
+  for (int k = 0; k < mz; k++)
+    for (int j = 0; j < my; j++)
+      for (int i = 0; i < mx; i++) {
+        int a, b, c;
+        if (remap(d, i, j, k, &a, &b, &c, 0, 0, 0)) gid[IX(d, i, j, k)] = gid[IX(d, a, b, c)];
+      }
+  return n;
+}
+
+/* ------------------------------------------------------------------------ */
+/* PoissonLHSNew (Source/poisson.c:977-1688) without level set (r = 1).    */
+/* Writes, per DA cell, the row class, the 19 stencil values in the order  */
+/* of poisson.c:957-975 and the column (dof id) of each slot; slots that   */
+/* MatSetValues would skip (poisson.c:1610-1614) get col = -1, vol = 0.    */
+/* scale_by_aj reproduces the poisson == -1 row scaling (poisson.c:1563).  */
+/* apply_filter = 0 keeps entries with |v| <= 1e-10 (used by the V-cycle).  */
+/* ------------------------------------------------------------------------ */
+int or_poisson_lhs(const or_dims *d, const double *nvert, const or_metrics *m, int scale_by_aj,
+                   int apply_filter, int *gid, int *rowtype, double *vol, int *col)
+{
+  const int mx = d->mx, my = d->my, mz = d->mz;
+  const size_t n = (size_t)mx * my * mz;
+  const int ip = per_i(d), jp = per_j(d), kp = per_k(d);
+  const double thr = POISSON_THRESHOLD;
+  int ndof = or_setup_lidx2(d, nvert, gid);
+  double *g = (double *)malloc(n * 9 * sizeof(double));
+  /* g11..g33 with periodic source remap: poisson.c:1102-1138 */
+  for (int k = 0; k < mz; k++)
+    for (int j = 0; j < my; j++)
+      for (int i = 0; i < mx; i++) {
+        int a, b, c;
+        remap(d, i, j, k, &a, &b, &c, 0, 0, 0);
+        size_t s = IX(d, a, b, c), t = IX(d, i, j, k);
+        const double *ic = &m->icsi[s * 3], *ie = &m->ieta[s * 3], *iz = &m->izet[s * 3];
+        const double *jc = &m->jcsi[s * 3], *je = &m->jeta[s * 3], *jz = &m->jzet[s * 3];
+        const double *kc = &m->kcsi[s * 3], *ke = &m->keta[s * 3], *kz = &m->kzet[s * 3];
+        double *gg = &g[t * 9];
+        gg[0] = (ic[0] * ic[0] + ic[1] * ic[1] + ic[2] * ic[2]) * m->iaj[s];
+        gg[1] = (ie[0] * ic[0] + ie[1] * ic[1] + ie[2] * ic[2]) * m->iaj[s];
+        gg[2] = (iz[0] * ic[0] + iz[1] * ic[1] + iz[2] * ic[2]) * m->iaj[s];
+        gg[3] = (jc[0] * je[0] + jc[1] * je[1] + jc[2] * je[2]) * m->jaj[s];
+        gg[4] = (je[0] * je[0] + je[1] * je[1] + je[2] * je[2]) * m->jaj[s];
+        gg[5] = (jz[0] * je[0] + jz[1] * je[1] + jz[2] * je[2]) * m->jaj[s];
+        gg[6] = (kc[0] * kz[0] + kc[1] * kz[1] + kc[2] * kz[2]) * m->kaj[s];
+        gg[7] = (ke[0] * kz[0] + ke[1] * kz[1] + ke[2] * kz[2]) * m->kaj[s];
+        gg[8] = (kz[0] * kz[0] + kz[1] * kz[1] + kz[2] * kz[2]) * m->kaj[s];
+      }
+#define NV(i, j, k) nvert[IX(d, i, j, k)]
+#define G(q, i, j, k) g[IX(d, i, j, k) * 9 + (q)]
+  for (size_t q = 0; q < n; q++) {
+    rowtype[q] = OR_ROW_NONE;
+    for (int s = 0; s < 19; s++) { vol[q * 19 + s] = 0.; col[q * 19 + s] = -1; }
+  }
+  for (int k = 0; k < mz; k++)
+    for (int j = 0; j < my; j++)
+      for (int i = 0; i < mx; i++) {
+        size_t t = IX(d, i, j, k);
+        int row = gid[t];
+        if (i == 0 || i == mx - 1 || j == 0 || j == my - 1 || k == 0 || k == mz - 1) continue;
+        if (NV(i, j, k) > 0.1 && row >= 0) { /* poisson.c:1158-1160 */
+          rowtype[t] = OR_ROW_IDENTITY;
+          vol[t * 19 + OR_CP] = 1.0;
+          col[t * 19 + OR_CP] = row;
+          continue;
+        }
+        if (NV(i, j, k) > thr) continue;
+        double v[19];
+        for (int s = 0; s < 19; s++) v[s] = 0.;
+        const double r = 1.0;
+        /* i+1 - i: poisson.c:1167-1230 */
+        if (NV(i + 1, j, k) < thr && (i != mx - 2 || ip)) {
+          v[OR_CP] -= G(0, i, j, k) / r;
+          v[OR_EP] += G(0, i, j, k) / r;
+          if ((j == my - 2 && !jp) || NV(i, j + 1, k) + NV(i + 1, j + 1, k) > thr) {
+            if (NV(i, j - 1, k) + NV(i + 1, j - 1, k) < thr && j != 1) {
+              v[OR_CP] += G(1, i, j, k) * 0.5 / r; v[OR_EP] += G(1, i, j, k) * 0.5 / r;
+              v[OR_SP] -= G(1, i, j, k) * 0.5 / r; v[OR_SE] -= G(1, i, j, k) * 0.5 / r;
+            }
+          } else if ((j == 1 && !jp) || NV(i, j - 1, k) + NV(i + 1, j - 1, k) > thr) {
+            if (NV(i, j + 1, k) + NV(i + 1, j + 1, k) < thr) {
+              v[OR_NP] += G(1, i, j, k) * 0.5 / r; v[OR_NE] += G(1, i, j, k) * 0.5 / r;
+              v[OR_CP] -= G(1, i, j, k) * 0.5 / r; v[OR_EP] -= G(1, i, j, k) * 0.5 / r;
+            }
+          } else {
+            v[OR_NP] += G(1, i, j, k) * 0.25 / r; v[OR_NE] += G(1, i, j, k) * 0.25 / r;
+            v[OR_SP] -= G(1, i, j, k) * 0.25 / r; v[OR_SE] -= G(1, i, j, k) * 0.25 / r;
+          }
+          if ((k == mz - 2 && !kp) || NV(i, j, k + 1) + NV(i + 1, j, k + 1) > thr) {
+            if (NV(i, j, k - 1) + NV(i + 1, j, k - 1) < thr && k != 1) {
+              v[OR_CP] += G(2, i, j, k) * 0.5 / r; v[OR_EP] += G(2, i, j, k) * 0.5 / r;
+              v[OR_BP] -= G(2, i, j, k) * 0.5 / r; v[OR_BE] -= G(2, i, j, k) * 0.5 / r;
+            }
+          } else if ((k == 1 && !kp) || NV(i, j, k - 1) + NV(i + 1, j, k - 1) > thr) {
+            if (NV(i, j, k + 1) + NV(i + 1, j, k + 1) < thr) {
+              v[OR_TP] += G(2, i, j, k) * 0.5 / r; v[OR_TE] += G(2, i, j, k) * 0.5 / r;
+              v[OR_CP] -= G(2, i, j, k) * 0.5 / r; v[OR_EP] -= G(2, i, j, k) * 0.5 / r;
+            }
+          } else {
+            v[OR_TP] += G(2, i, j, k) * 0.25 / r; v[OR_TE] += G(2, i, j, k) * 0.25 / r;
+            v[OR_BP] -= G(2, i, j, k) * 0.25 / r; v[OR_BE] -= G(2, i, j, k) * 0.25 / r;
+          }
+        }
+        /* i - i-1: poisson.c:1233-1293 */
+        if (NV(i - 1, j, k) < thr && (i != 1 || ip)) {
+          v[OR_CP] -= G(0, i - 1, j, k) / r;
+          v[OR_WP] += G(0, i - 1, j, k) / r;
+          if ((j == my - 2 && !jp) || NV(i, j + 1, k) + NV(i - 1, j + 1, k) > thr) {
+            if (NV(i, j - 1, k) + NV(i - 1, j - 1, k) < thr && j != 1) {
+              v[OR_CP] -= G(1, i - 1, j, k) * 0.5 / r; v[OR_WP] -= G(1, i - 1, j, k) * 0.5 / r;
+              v[OR_SP] += G(1, i - 1, j, k) * 0.5 / r; v[OR_SW] += G(1, i - 1, j, k) * 0.5 / r;
+            }
+          } else if ((j == 1 && !jp) || NV(i, j - 1, k) + NV(i - 1, j - 1, k) > thr) {
+            if (NV(i, j + 1, k) + NV(i - 1, j + 1, k) < thr) {
+              v[OR_NP] -= G(1, i - 1, j, k) * 0.5 / r; v[OR_NW] -= G(1, i - 1, j, k) * 0.5 / r;
+              v[OR_CP] += G(1, i - 1, j, k) * 0.5 / r; v[OR_WP] += G(1, i - 1, j, k) * 0.5 / r;
+            }
+          } else {
+            v[OR_NP] -= G(1, i - 1, j, k) * 0.25 / r; v[OR_NW] -= G(1, i - 1, j, k) * 0.25 / r;
+            v[OR_SP] += G(1, i - 1, j, k) * 0.25 / r; v[OR_SW] += G(1, i - 1, j, k) * 0.25 / r;
+          }
+          if ((k == mz - 2 && !kp) || NV(i, j, k + 1) + NV(i - 1, j, k + 1) > thr) {
+            if (NV(i, j, k - 1) + NV(i - 1, j, k - 1) < thr && k != 1) {
+              v[OR_CP] -= G(2, i - 1, j, k) * 0.5 / r; v[OR_WP] -= G(2, i - 1, j, k) * 0.5 / r;
+              v[OR_BP] += G(2, i - 1, j, k) * 0.5 / r; v[OR_BW] += G(2, i - 1, j, k) * 0.5 / r;
+            }
+          } else if ((k == 1 && !kp) || NV(i, j, k - 1) + NV(i - 1, j, k - 1) > thr) {
+            if (NV(i, j, k + 1) + NV(i - 1, j, k + 1) < thr) {
+              v[OR_TP] -= G(2, i - 1, j, k) * 0.5 / r; v[OR_TW] -= G(2, i - 1, j, k) * 0.5 / r;
+              v[OR_CP] += G(2, i - 1, j, k) * 0.5 / r; v[OR_WP] += G(2, i - 1, j, k) * 0.5 / r;
+            }
+          } else {
+            v[OR_TP] -= G(2, i - 1, j, k) * 0.25 / r; v[OR_TW] -= G(2, i - 1, j, k) * 0.25 / r;
+            v[OR_BP] += G(2, i - 1, j, k) * 0.25 / r; v[OR_BW] += G(2, i - 1, j, k) * 0.25 / r;
+          }
+        }
+        /* j+1 - j: poisson.c:1296-1361 */
+        if (NV(i, j + 1, k) < thr && (j != my - 2 || jp)) {
+          if ((i == mx - 2 && !ip) || NV(i + 1, j, k) + NV(i + 1, j + 1, k) > thr) {
+            if (NV(i - 1, j, k) + NV(i - 1, j + 1, k) < thr && i != 1) {
+              v[OR_CP] += G(3, i, j, k) * 0.5 / r; v[OR_NP] += G(3, i, j, k) * 0.5 / r;
+              v[OR_WP] -= G(3, i, j, k) * 0.5 / r; v[OR_NW] -= G(3, i, j, k) * 0.5 / r;
+            }
+          } else if ((i == 1 && !ip) || NV(i - 1, j, k) + NV(i - 1, j + 1, k) > thr) {
+            if (NV(i + 1, j, k) + NV(i + 1, j + 1, k) < thr) {
+              v[OR_EP] += G(3, i, j, k) * 0.5 / r; v[OR_NE] += G(3, i, j, k) * 0.5 / r;
+              v[OR_CP] -= G(3, i, j, k) * 0.5 / r; v[OR_NP] -= G(3, i, j, k) * 0.5 / r;
+            }
+          } else {
+            v[OR_EP] += G(3, i, j, k) * 0.25 / r; v[OR_NE] += G(3, i, j, k) * 0.25 / r;
+            v[OR_WP] -= G(3, i, j, k) * 0.25 / r; v[OR_NW] -= G(3, i, j, k) * 0.25 / r;
+          }
+          v[OR_CP] -= G(4, i, j, k) / r;
+          v[OR_NP] += G(4, i, j, k) / r;
+          if ((k == mz - 2 && !kp) || NV(i, j, k + 1) + NV(i, j + 1, k + 1) > thr) {
+            if (NV(i, j, k - 1) + NV(i, j + 1, k - 1) < thr && k != 1) {
+              v[OR_CP] += G(5, i, j, k) * 0.5 / r; v[OR_NP] += G(5, i, j, k) * 0.5 / r;
+              v[OR_BP] -= G(5, i, j, k) * 0.5 / r; v[OR_BN] -= G(5, i, j, k) * 0.5 / r;
+            }
+          } else if ((k == 1 && !kp) || NV(i, j, k - 1) + NV(i, j + 1, k - 1) > thr) {
+            if (NV(i, j, k + 1) + NV(i, j + 1, k + 1) < thr) {
+              v[OR_TP] += G(5, i, j, k) * 0.5 / r; v[OR_TN] += G(5, i, j, k) * 0.5 / r;
+              v[OR_CP] -= G(5, i, j, k) * 0.5 / r; v[OR_NP] -= G(5, i, j, k) * 0.5 / r;
+            }
+          } else {
+            v[OR_TP] += G(5, i, j, k) * 0.25 / r; v[OR_TN] += G(5, i, j, k) * 0.25 / r;
+            v[OR_BP] -= G(5, i, j, k) * 0.25 / r; v[OR_BN] -= G(5, i, j, k) * 0.25 / r;
+          }
+        }
+        /* j - j-1: poisson.c:1364-1422 */
+        if (NV(i, j - 1, k) < thr && (j != 1 || jp)) {
+          if ((i == mx - 2 && !ip) || NV(i + 1, j, k) + NV(i + 1, j - 1, k) > thr) {
+            if (NV(i - 1, j, k) + NV(i - 1, j - 1, k) < thr && i != 1) {
+              v[OR_CP] -= G(3, i, j - 1, k) * 0.5 / r; v[OR_SP] -= G(3, i, j - 1, k) * 0.5 / r;
+              v[OR_WP] += G(3, i, j - 1, k) * 0.5 / r; v[OR_SW] += G(3, i, j - 1, k) * 0.5 / r;
+            }
+          } else if ((i == 1 && !ip) || NV(i - 1, j, k) + NV(i - 1, j - 1, k) > thr) {
+            if (NV(i + 1, j, k) + NV(i + 1, j - 1, k) < thr) {
+              v[OR_EP] -= G(3, i, j - 1, k) * 0.5 / r; v[OR_SE] -= G(3, i, j - 1, k) * 0.5 / r;
+              v[OR_CP] += G(3, i, j - 1, k) * 0.5 / r; v[OR_SP] += G(3, i, j - 1, k) * 0.5 / r;
+            }
+          } else {
+            v[OR_EP] -= G(3, i, j - 1, k) * 0.25 / r; v[OR_SE] -= G(3, i, j - 1, k) * 0.25 / r;
+            v[OR_WP] += G(3, i, j - 1, k) * 0.25 / r; v[OR_SW] += G(3, i, j - 1, k) * 0.25 / r;
+          }
+          v[OR_CP] -= G(4, i, j - 1, k) / r;
+          v[OR_SP] += G(4, i, j - 1, k) / r;
+          if ((k == mz - 2 && !kp) || NV(i, j, k + 1) + NV(i, j - 1, k + 1) > thr) {
+            if (NV(i, j, k - 1) + NV(i, j - 1, k - 1) < thr && k != 1) {
+              v[OR_CP] -= G(5, i, j - 1, k) * 0.5 / r; v[OR_SP] -= G(5, i, j - 1, k) * 0.5 / r;
+              v[OR_BP] += G(5, i, j - 1, k) * 0.5 / r; v[OR_BS] += G(5, i, j - 1, k) * 0.5 / r;
+            }
+          } else if ((k == 1 && !kp) || NV(i, j, k - 1) + NV(i, j - 1, k - 1) > thr) {
+            if (NV(i, j, k + 1) + NV(i, j - 1, k + 1) < thr) {
+              v[OR_TP] -= G(5, i, j - 1, k) * 0.5 / r; v[OR_TS] -= G(5, i, j - 1, k) * 0.5 / r;
+              v[OR_CP] += G(5, i, j - 1, k) * 0.5 / r; v[OR_SP] += G(5, i, j - 1, k) * 0.5 / r;
+            }
+          } else {
+            v[OR_TP] -= G(5, i, j - 1, k) * 0.25 / r; v[OR_TS] -= G(5, i, j - 1, k) * 0.25 / r;
+            v[OR_BP] += G(5, i, j - 1, k) * 0.25 / r; v[OR_BS] += G(5, i, j - 1, k) * 0.25 / r;
+          }
+        }
+        /* k+1 - k: poisson.c:1425-1491 */
+        if (NV(i, j, k + 1) < thr && (k != mz - 2 || kp)) {
+          if ((i == mx - 2 && !ip) || NV(i + 1, j, k) + NV(i + 1, j, k + 1) > thr) {
+            if (NV(i - 1, j, k) + NV(i - 1, j, k + 1) < thr && i != 1) {
+              v[OR_CP] += G(6, i, j, k) * 0.5 / r; v[OR_TP] += G(6, i, j, k) * 0.5 / r;
+              v[OR_WP] -= G(6, i, j, k) * 0.5 / r; v[OR_TW] -= G(6, i, j, k) * 0.5 / r;
+            }
+          } else if ((i == 1 && !ip) || NV(i - 1, j, k) + NV(i - 1, j, k + 1) > thr) {
+            if (NV(i + 1, j, k) + NV(i + 1, j, k + 1) < thr) {
+              v[OR_EP] += G(6, i, j, k) * 0.5 / r; v[OR_TE] += G(6, i, j, k) * 0.5 / r;
+              v[OR_CP] -= G(6, i, j, k) * 0.5 / r; v[OR_TP] -= G(6, i, j, k) * 0.5 / r;
+            }
+          } else {
+            v[OR_EP] += G(6, i, j, k) * 0.25 / r; v[OR_TE] += G(6, i, j, k) * 0.25 / r;
+            v[OR_WP] -= G(6, i, j, k) * 0.25 / r; v[OR_TW] -= G(6, i, j, k) * 0.25 / r;
+          }
+          if ((j == my - 2 && !jp) || NV(i, j + 1, k) + NV(i, j + 1, k + 1) > thr) {
+            if (NV(i, j - 1, k) + NV(i, j - 1, k + 1) < thr && j != 1) {
+              v[OR_CP] += G(7, i, j, k) * 0.5 / r; v[OR_TP] += G(7, i, j, k) * 0.5 / r;
+              v[OR_SP] -= G(7, i, j, k) * 0.5 / r; v[OR_TS] -= G(7, i, j, k) * 0.5 / r;
+            }
+          } else if ((j == 1 && !jp) || NV(i, j - 1, k) + NV(i, j - 1, k + 1) > thr) {
+            if (NV(i, j + 1, k) + NV(i, j + 1, k + 1) < thr) {
+              v[OR_NP] += G(7, i, j, k) * 0.5 / r; v[OR_TN] += G(7, i, j, k) * 0.5 / r;
+              v[OR_CP] -= G(7, i, j, k) * 0.5 / r; v[OR_TP] -= G(7, i, j, k) * 0.5 / r;
+            }
+          } else {
+            v[OR_NP] += G(7, i, j, k) * 0.25 / r; v[OR_TN] += G(7, i, j, k) * 0.25 / r;
+            v[OR_SP] -= G(7, i, j, k) * 0.25 / r; v[OR_TS] -= G(7, i, j, k) * 0.25 / r;
+          }
+          v[OR_CP] -= G(8, i, j, k) / r;
+          v[OR_TP] += G(8, i, j, k) / r;
+        }
+        /* k - k-1: poisson.c:1494-1561 */
+        if (NV(i, j, k - 1) < thr && (k != 1 || kp)) {
+          if ((i == mx - 2 && !ip) || NV(i + 1, j, k) + NV(i + 1, j, k - 1) > thr) {
+            if (NV(i - 1, j, k) + NV(i - 1, j, k - 1) < thr && i != 1) {
+              v[OR_CP] -= G(6, i, j, k - 1) * 0.5 / r; v[OR_BP] -= G(6, i, j, k - 1) * 0.5 / r;
+              v[OR_WP] += G(6, i, j, k - 1) * 0.5 / r; v[OR_BW] += G(6, i, j, k - 1) * 0.5 / r;
+            }
+          } else if ((i == 1 && !ip) || NV(i - 1, j, k) + NV(i - 1, j, k - 1) > thr) {
+            if (NV(i + 1, j, k) + NV(i + 1, j, k - 1) < thr) {
+              v[OR_EP] -= G(6, i, j, k - 1) * 0.5 / r; v[OR_BE] -= G(6, i, j, k - 1) * 0.5 / r;
+              v[OR_CP] += G(6, i, j, k - 1) * 0.5 / r; v[OR_BP] += G(6, i, j, k - 1) * 0.5 / r;
+            }
+          } else {
+            v[OR_EP] -= G(6, i, j, k - 1) * 0.25 / r; v[OR_BE] -= G(6, i, j, k - 1) * 0.25 / r;
+            v[OR_WP] += G(6, i, j, k - 1) * 0.25 / r; v[OR_BW] += G(6, i, j, k - 1) * 0.25 / r;
+          }
+          if ((j == my - 2 && !jp) || NV(i, j + 1, k) + NV(i, j + 1, k - 1) > thr) {
+            if (NV(i, j - 1, k) + NV(i, j - 1, k - 1) < thr && j != 1) {
+              v[OR_CP] -= G(7, i, j, k - 1) * 0.5 / r; v[OR_BP] -= G(7, i, j, k - 1) * 0.5 / r;
+              v[OR_SP] += G(7, i, j, k - 1) * 0.5 / r; v[OR_BS] += G(7, i, j, k - 1) * 0.5 / r;
+            }
+          } else if ((j == 1 && !jp) || NV(i, j - 1, k) + NV(i, j - 1, k - 1) > thr) {
+            if (NV(i, j + 1, k) + NV(i, j + 1, k - 1) < thr) {
+              v[OR_NP] -= G(7, i, j, k - 1) * 0.5 / r; v[OR_BN] -= G(7, i, j, k - 1) * 0.5 / r;
+              v[OR_CP] += G(7, i, j, k - 1) * 0.5 / r; v[OR_BP] += G(7, i, j, k - 1) * 0.5 / r;
+            }
+          } else {
+            v[OR_NP] -= G(7, i, j, k - 1) * 0.25 / r; v[OR_BN] -= G(7, i, j, k - 1) * 0.25 / r;
+            v[OR_SP] += G(7, i, j, k - 1) * 0.25 / r; v[OR_BS] += G(7, i, j, k - 1) * 0.25 / r;
+          }
+          v[OR_CP] -= G(8, i, j, k - 1) / r;
+          v[OR_BP] += G(8, i, j, k - 1) / r;
+        }
+        if (scale_by_aj)
+          for (int s = 0; s < 19; s++) v[s] *= m->aj[t];
+        /* column ids: poisson.c:1584-1603; entry filter: poisson.c:1610-1614 */
+        static const int off[19][3] = {{0, 0, 0},  {1, 0, 0},  {-1, 0, 0}, {0, 1, 0},  {0, -1, 0},
+                                       {0, 0, 1},  {0, 0, -1}, {1, 1, 0},  {1, -1, 0}, {-1, 1, 0},
+                                       {-1, -1, 0}, {0, 1, 1},  {0, 1, -1}, {0, -1, 1}, {0, -1, -1},
+                                       {1, 0, 1},  {1, 0, -1}, {-1, 0, 1}, {-1, 0, -1}};
+        rowtype[t] = OR_ROW_FLUID;
+        for (int s = 0; s < 19; s++) {
+          int id = gid[IX(d, i + off[s][0], j + off[s][1], k + off[s][2])];
+          int keep = (s == OR_CP) || (id >= 0 && (!apply_filter || fabs(v[s]) > 1.e-10));
+          if (keep) {
+            vol[t * 19 + s] = v[s];
+            col[t * 19 + s] = id;
+          }
+        }
+      }
+#undef NV
+#undef G
+  free(g);
+  return ndof;
+}
+
+/* ------------------------------------------------------------------------ */
+/* PoissonRHS2_hypre (Source/poisson_hypre.c:265-407) without level set.   */
+/* b has one entry per dof; entries of non-fluid dofs stay 0 (they are     */
+/* never set, poisson_hypre.c:328-331).                                    */
+/* ------------------------------------------------------------------------ */
+void or_poisson_rhs2_hypre(const or_dims *d, const double *nvert, const int *gid,
+                           const double *ucont, double dt, double st, double coeff, double *b)
+{
+  const int mx = d->mx, my = d->my, mz = d->mz;
+  const int ip = per_i(d), jp = per_j(d), kp = per_k(d);
+#define U(i, j, k, c) ucont[IX(d, i, j, k) * 3 + (c)]
+  for (int k = 1; k < mz - 1; k++)
+    for (int j = 1; j < my - 1; j++)
+      for (int i = 1; i < mx - 1; i++) {
+        size_t t = IX(d, i, j, k);
+        if (gid[t] >= 0) b[gid[t]] = 0.;
+      }
+  for (int k = 1; k < mz - 1; k++)
+    for (int j = 1; j < my - 1; j++)
+      for (int i = 1; i < mx - 1; i++) {
+        size_t t = IX(d, i, j, k);
+        if (nvert[t] >= 0.1) continue;
+        double val = 0;
+        val -= U(i, j, k, 0);
+        if (i == 1 && ip) val += U(mx - 2, j, k, 0);
+        else val += U(i - 1, j, k, 0);
+        val -= U(i, j, k, 1);
+        if (j == 1 && jp) val += U(i, my - 2, k, 1);
+        else val += U(i, j - 1, k, 1);
+        val -= U(i, j, k, 2);
+        if (k == 1 && kp) val += U(i, j, mz - 2, 2);
+        else val += U(i, j, k - 1, 2);
+        val *= -1.0 / dt * st * coeff;
+        b[gid[t]] = val;
+      }
+#undef U
+}
+
+/* Remove_Nullspace_Scale (Source/poisson_hypre.c:118-200). */
+void or_remove_nullspace_scale(const or_dims *d, const double *nvert, const int *gid,
+                               const double *aj, double *b, int bctype3)
+{
+  if (bctype3 == -10) return;
+  const int mx = d->mx, my = d->my, mz = d->mz;
+  double sum = 0, sum_aj = 0;
+  for (int k = 1; k < mz - 1; k++)
+    for (int j = 1; j < my - 1; j++)
+      for (int i = 1; i < mx - 1; i++) {
+        size_t t = IX(d, i, j, k);
+        if (nvert[t] < 0.1) { sum += b[gid[t]]; sum_aj += aj[t]; }
+      }
+  for (int k = 1; k < mz - 1; k++)
+    for (int j = 1; j < my - 1; j++)
+      for (int i = 1; i < mx - 1; i++) {
+        size_t t = IX(d, i, j, k);
+        if (nvert[t] < 0.1) {
+          double val = -sum * aj[t] / sum_aj;
+          b[gid[t]] += val;
+        }
+      }
+}
+
+/* Remove_Nullspace (Source/poisson_hypre.c:202-263). */
+void or_remove_nullspace(const or_dims *d, const double *nvert, const int *gid, double *phi2,
+                         int bctype3)
+{
+  if (bctype3 == -10) return;
+  const int mx = d->mx, my = d->my, mz = d->mz;
+  double sum = 0;
+  int count = 0;
+  for (int k = 1; k < mz - 1; k++)
+    for (int j = 1; j < my - 1; j++)
+      for (int i = 1; i < mx - 1; i++) {
+        size_t t = IX(d, i, j, k);
+        if (nvert[t] < 0.1) { sum += phi2[gid[t]]; count++; }
+      }
+  double val = -sum / (double)count;
+  for (int k = 1; k < mz - 1; k++)
+    for (int j = 1; j < my - 1; j++)
+      for (int i = 1; i < mx - 1; i++) {
+        size_t t = IX(d, i, j, k);
+        if (nvert[t] < 0.1) phi2[gid[t]] += val;
+      }
+}
+
+/* Convert_Phi2_Phi (Source/poisson.c:98-186). */
+void or_convert_phi2_phi(const or_dims *d, const double *nvert, const double *phi2, double *phi)
+{
+  const int mx = d->mx, my = d->my, mz = d->mz;
+  memset(phi, 0, sizeof(double) * (size_t)mx * my * mz);
+  int pos = 0;
+  for (int k = 1; k < mz - 1; k++)
+    for (int j = 1; j < my - 1; j++)
+      for (int i = 1; i < mx - 1; i++) {
+        size_t t = IX(d, i, j, k);
+        if ((int)nvert[t] > POISSON_THRESHOLD) phi[t] = 0;
+        else phi[t] = phi2[pos++];
+      }
+  for (int k = 0; k < mz; k++)
+    for (int j = 0; j < my; j++)
+      for (int i = 0; i < mx; i++) {
+        int a, b, c;
+        if (remap(d, i, j, k, &a, &b, &c, 0, 0, 0)) phi[IX(d, i, j, k)] = phi[IX(d, a, b, c)];
+      }
+}
+
+/* UpdatePressure (Source/poisson.c:3137-3297), non-PRIMITIVE_PRESSURE path. */
+void or_update_pressure(const or_dims *d, const double *nvert, double *p, double *phi)
+{
+  const int mx = d->mx, my = d->my, mz = d->mz;
+  for (int k = 1; k < mz - 1; k++)
+    for (int j = 1; j < my - 1; j++)
+      for (int i = 1; i < mx - 1; i++) {
+        size_t t = IX(d, i, j, k);
+        if (nvert[t] < 0.1) p[t] += phi[t];
+        if (nvert[t] > 1.1) p[t] = 0;
+      }
+  for (int k = 0; k < mz; k++)
+    for (int j = 0; j < my; j++)
+      for (int i = 0; i < mx; i++) {
+        int a, b, c;
+        if (remap(d, i, j, k, &a, &b, &c, 0, 0, 0)) {
+          p[IX(d, i, j, k)] = p[IX(d, a, b, c)];
+          phi[IX(d, i, j, k)] = phi[IX(d, a, b, c)];
+        }
+      }
+}
+
+/* Projection (Source/poisson.c:2700-3066) without level set; Contra2Cart
+ * (poisson.c:3060) is not part of this restatement. */
+void or_projection(const or_dims *d, const double *nvert, const double *phi, const or_metrics *m,
+                   double dt, double st, double coeff, double *ucont)
+{
+  const int mx = d->mx, my = d->my, mz = d->mz;
+  const int ip = per_i(d), jp = per_j(d), kp = per_k(d);
+  const double thr = POISSON_THRESHOLD;
+#define NV(i, j, k) nvert[IX(d, i, j, k)]
+#define PH(i, j, k) phi[IX(d, i, j, k)]
+#define M3(arr, i, j, k, c) m->arr[IX(d, i, j, k) * 3 + (c)]
+#define DOT(A, B, i, j, k) (M3(A, i, j, k, 0) * M3(B, i, j, k, 0) + M3(A, i, j, k, 1) * M3(B, i, j, k, 1) + M3(A, i, j, k, 2) * M3(B, i, j, k, 2))
+  for (int k = 1; k < mz - 1; k++)
+    for (int j = 1; j < my - 1; j++)
+      for (int i = 1; i < mx - 1; i++) {
+        const double r1 = 1.0, r2 = 1.0, r3 = 1.0;
+        double dpdc, dpde, dpdz;
+        size_t t = IX(d, i, j, k);
+        if (i < mx - 2 || (ip && i == mx - 2)) { /* poisson.c:2791-2834 */
+          dpdc = PH(i + 1, j, k) - PH(i, j, k);
+          if (i == mx - 2 && ip) dpdc = PH(1, j, k) - PH(i, j, k);
+          dpde = 0.; dpdz = 0.;
+          if ((j == my - 2 && !jp) || NV(i, j + 1, k) + NV(i + 1, j + 1, k) > thr) {
+            if (NV(i, j - 1, k) + NV(i + 1, j - 1, k) < thr && (j != 1))
+              dpde = (PH(i, j, k) + PH(i + 1, j, k) - PH(i, j - 1, k) - PH(i + 1, j - 1, k)) * 0.5;
+          } else if ((j == 1 && !jp) || NV(i, j - 1, k) + NV(i + 1, j - 1, k) > thr) {
+            if (NV(i, j + 1, k) + NV(i + 1, j + 1, k) < thr)
+              dpde = (PH(i, j + 1, k) + PH(i + 1, j + 1, k) - PH(i, j, k) - PH(i + 1, j, k)) * 0.5;
+          } else {
+            dpde = (PH(i, j + 1, k) + PH(i + 1, j + 1, k) - PH(i, j - 1, k) - PH(i + 1, j - 1, k)) * 0.25;
+          }
+          if ((k == mz - 2 && !kp) || NV(i, j, k + 1) + NV(i + 1, j, k + 1) > thr) {
+            if (NV(i, j, k - 1) + NV(i + 1, j, k - 1) < thr && (k != 1))
+              dpdz = (PH(i, j, k) + PH(i + 1, j, k) - PH(i, j, k - 1) - PH(i + 1, j, k - 1)) * 0.5;
+          } else if ((k == 1 && !kp) || NV(i, j, k - 1) + NV(i + 1, j, k - 1) > thr) {
+            if (NV(i, j, k + 1) + NV(i + 1, j, k + 1) < thr)
+              dpdz = (PH(i, j, k + 1) + PH(i + 1, j, k + 1) - PH(i, j, k) - PH(i + 1, j, k)) * 0.5;
+          } else {
+            dpdz = (PH(i, j, k + 1) + PH(i + 1, j, k + 1) - PH(i, j, k - 1) - PH(i + 1, j, k - 1)) * 0.25;
+          }
+          if ((NV(i, j, k) + NV(i + 1, j, k)) < thr) {
+            ucont[t * 3 + 0] -= (dpdc * DOT(icsi, icsi, i, j, k) * m->iaj[t] +
+                                 dpde * DOT(ieta, icsi, i, j, k) * m->iaj[t] +
+                                 dpdz * DOT(izet, icsi, i, j, k) * m->iaj[t]) *
+                                dt * st / coeff / r1;
+          }
+        }
+        if (j < my - 2 || (jp && j == my - 2)) { /* poisson.c:2837-2883 */
+          dpdc = 0.; dpdz = 0.;
+          if ((i == mx - 2 && !ip) || NV(i + 1, j, k) + NV(i + 1, j + 1, k) > thr) {
+            if (NV(i - 1, j, k) + NV(i - 1, j + 1, k) < thr && (i != 1))
+              dpdc = (PH(i, j, k) + PH(i, j + 1, k) - PH(i - 1, j, k) - PH(i - 1, j + 1, k)) * 0.5;
+          } else if ((i == 1 && !ip) || NV(i - 1, j, k) + NV(i - 1, j + 1, k) > thr) {
+            if (NV(i + 1, j, k) + NV(i + 1, j + 1, k) < thr)
+              dpdc = (PH(i + 1, j, k) + PH(i + 1, j + 1, k) - PH(i, j, k) - PH(i, j + 1, k)) * 0.5;
+          } else {
+            dpdc = (PH(i + 1, j, k) + PH(i + 1, j + 1, k) - PH(i - 1, j, k) - PH(i - 1, j + 1, k)) * 0.25;
+          }
+          if (j == my - 2 && jp) dpde = PH(i, 1, k) - PH(i, j, k);
+          else dpde = PH(i, j + 1, k) - PH(i, j, k);
+          if ((k == mz - 2 && !kp) || NV(i, j, k + 1) + NV(i, j + 1, k + 1) > thr) {
+            if (NV(i, j, k - 1) + NV(i, j + 1, k - 1) < thr && (k != 1))
+              dpdz = (PH(i, j, k) + PH(i, j + 1, k) - PH(i, j, k - 1) - PH(i, j + 1, k - 1)) * 0.5;
+          } else if ((k == 1 && !kp) || NV(i, j, k - 1) + NV(i, j + 1, k - 1) > thr) {
+            if (NV(i, j, k + 1) + NV(i, j + 1, k + 1) < thr)
+              dpdz = (PH(i, j, k + 1) + PH(i, j + 1, k + 1) - PH(i, j, k) - PH(i, j + 1, k)) * 0.5;
+          } else {
+            dpdz = (PH(i, j, k + 1) + PH(i, j + 1, k + 1) - PH(i, j, k - 1) - PH(i, j + 1, k - 1)) * 0.25;
+          }
+          if ((NV(i, j, k) + NV(i, j + 1, k)) < thr || (int)(NV(i, j, k) + NV(i, j + 1, k)) == 5) {
+            ucont[t * 3 + 1] -= (dpdc * DOT(jcsi, jeta, i, j, k) * m->jaj[t] +
+                                 dpde * DOT(jeta, jeta, i, j, k) * m->jaj[t] +
+                                 dpdz * DOT(jzet, jeta, i, j, k) * m->jaj[t]) *
+                                dt * st / coeff / r2;
+          }
+        }
+        if (k < mz - 2 || (kp && k == mz - 2)) { /* poisson.c:2886-2958 */
+          dpdc = 0.; dpde = 0.;
+          if ((i == mx - 2 && !ip) || NV(i + 1, j, k) + NV(i + 1, j, k + 1) > thr) {
+            if (NV(i - 1, j, k) + NV(i - 1, j, k + 1) < thr && (i != 1))
+              dpdc = (PH(i, j, k) + PH(i, j, k + 1) - PH(i - 1, j, k) - PH(i - 1, j, k + 1)) * 0.5;
+          } else if ((i == 1 && !ip) || NV(i - 1, j, k) + NV(i - 1, j, k + 1) > thr) {
+            if (NV(i + 1, j, k) + NV(i + 1, j, k + 1) < thr)
+              dpdc = (PH(i + 1, j, k) + PH(i + 1, j, k + 1) - PH(i, j, k) - PH(i, j, k + 1)) * 0.5;
+          } else {
+            dpdc = (PH(i + 1, j, k) + PH(i + 1, j, k + 1) - PH(i - 1, j, k) - PH(i - 1, j, k + 1)) * 0.25;
+          }
+          if ((j == my - 2 && !jp) || NV(i, j + 1, k) + NV(i, j + 1, k + 1) > thr) {
+            if (NV(i, j - 1, k) + NV(i, j - 1, k + 1) < thr && (j != 1))
+              dpde = (PH(i, j, k) + PH(i, j, k + 1) - PH(i, j - 1, k) - PH(i, j - 1, k + 1)) * 0.5;
+          } else if ((j == 1 && !jp) || NV(i, j - 1, k) + NV(i, j - 1, k + 1) > thr) {
+            if (NV(i, j + 1, k) + NV(i, j + 1, k + 1) < thr)
+              dpde = (PH(i, j + 1, k) + PH(i, j + 1, k + 1) - PH(i, j, k) - PH(i, j, k + 1)) * 0.5;
+          } else {
+            dpde = (PH(i, j + 1, k) + PH(i, j + 1, k + 1) - PH(i, j - 1, k) - PH(i, j - 1, k + 1)) * 0.25;
+          }
+          if (k == mz - 2 && kp) dpdz = PH(i, j, 1) - PH(i, j, k);
+          else dpdz = PH(i, j, k + 1) - PH(i, j, k);
+          if ((NV(i, j, k) + NV(i, j, k + 1)) < thr) {
+            ucont[t * 3 + 2] -= (dpdc * DOT(kcsi, kzet, i, j, k) * m->kaj[t] +
+                                 dpde * DOT(keta, kzet, i, j, k) * m->kaj[t] +
+                                 dpdz * DOT(kzet, kzet, i, j, k) * m->kaj[t]) *
+                                dt * st / coeff / r3;
+          }
+        }
+      }
+  /* periodic face copy: poisson.c:2996-3036 */
+  for (int k = 0; k < mz; k++)
+    for (int j = 0; j < my; j++)
+      for (int i = 0; i < mx; i++) {
+        int a, b, c, fi, fj, fk;
+        if (!remap(d, i, j, k, &a, &b, &c, &fi, &fj, &fk)) continue;
+        size_t s = IX(d, a, b, c), t = IX(d, i, j, k);
+        if (fi) ucont[t * 3 + 0] = ucont[s * 3 + 0];
+        if (fj) ucont[t * 3 + 1] = ucont[s * 3 + 1];
+        if (fk) ucont[t * 3 + 2] = ucont[s * 3 + 2];
+      }
+#undef NV
+#undef PH
+#undef M3
+#undef DOT
+}
+
+/* Divergence (Source/main.c:936-1074): max over interior cells of
+ * |div(Ucont) * aj|, zero next to any blanked cell. */
+double or_divergence(const or_dims *d, const double *nvert, const double *ucont, const double *aj)
+{
+  const int mx = d->mx, my = d->my, mz = d->mz;
+  double best = 0.;
+#define U(i, j, k, c) ucont[IX(d, i, j, k) * 3 + (c)]
+#define NV(i, j, k) nvert[IX(d, i, j, k)]
+  for (int k = 1; k < mz - 1; k++)
+    for (int j = 1; j < my - 1; j++)
+      for (int i = 1; i < mx - 1; i++) {
+        double v = fabs((U(i, j, k, 0) - U(i - 1, j, k, 0) + U(i, j, k, 1) - U(i, j - 1, k, 1) +
+                         U(i, j, k, 2) - U(i, j, k - 1, 2)) *
+                        aj[IX(d, i, j, k)]);
+        if (NV(i, j, k) + NV(i, j, k + 1) + NV(i, j, k - 1) + NV(i, j + 1, k) + NV(i, j - 1, k) +
+                NV(i + 1, j, k) + NV(i - 1, j, k) >
+            0.1)
+          v = 0.;
+        if (v > best) best = v;
+      }
+#undef U
+#undef NV
+  return best;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Multigrid transfer operators.                                            */
+/* ------------------------------------------------------------------------ */
+/* MyNvertRestriction (Source/poisson.c:1995-2083). */
+void or_my_nvert_restriction(const or_dims *dh, const or_dims *dc, int isc, int jsc, int ksc,
+                             const double *nvert_h, double *nvert_c)
+{
+  const int mx = dc->mx, my = dc->my, mz = dc->mz;
+  const int ia = isc ? 0 : 1, ja = jsc ? 0 : 1, ka = ksc ? 0 : 1;
+  memset(nvert_c, 0, sizeof(double) * (size_t)mx * my * mz);
+#define NH(i, j, k) nvert_h[IX(dh, i, j, k)]
+  for (int k = 1; k < mz - 1; k++)
+    for (int j = 1; j < my - 1; j++)
+      for (int i = 1; i < mx - 1; i++) {
+        int ih = isc ? i : 2 * i, jh = jsc ? j : 2 * j, kh = ksc ? k : 2 * k;
+        if (NH(ih, jh, kh) * NH(ih - ia, jh, kh) * NH(ih, jh - ja, kh) * NH(ih, jh, kh - ka) *
+                NH(ih - ia, jh - ja, kh) * NH(ih - ia, jh, kh - ka) * NH(ih, jh - ja, kh - ka) *
+                NH(ih - ia, jh - ja, kh - ka) >
+            0.1) {
+          double *o = &nvert_c[IX(dc, i, j, k)];
+          *o = (1. > *o) ? 1. : *o;
+        }
+      }
+#undef NH
+  /* isolated-cell fill, done in place in k-j-i order as the reference does;
+   * the boundary layer of the coarse array stays 0 (VecSet above) */
+  double *l = (double *)malloc(sizeof(double) * (size_t)mx * my * mz);
+  memcpy(l, nvert_c, sizeof(double) * (size_t)mx * my * mz);
+  for (int k = 1; k < mz - 1; k++)
+    for (int j = 1; j < my - 1; j++)
+      for (int i = 1; i < mx - 1; i++) {
+        size_t t = IX(dc, i, j, k);
+        if (l[t] < 0.1) {
+          if (l[IX(dc, i + 1, j, k)] + l[IX(dc, i - 1, j, k)] > 1.1 &&
+              l[IX(dc, i, j + 1, k)] + l[IX(dc, i, j - 1, k)] > 1.1 &&
+              l[IX(dc, i, j, k + 1)] + l[IX(dc, i, j, k - 1)] > 1.1)
+            l[t] = 1.;
+        }
+      }
+  memcpy(nvert_c, l, sizeof(double) * (size_t)mx * my * mz);
+  free(l);
+}
+
+/* MyRestriction (Source/poisson.c:365-472): f_c = 1/8 * sum over the
+ * children of x_f * max(0, 1 - nvert_f); zero on blanked coarse cells. */
+void or_my_restriction(const or_dims *dc, const or_dims *df, int isc, int jsc, int ksc,
+                       const double *nvert_c, const double *nvert_f, const double *xf, double *fc)
+{
+  const int mx = dc->mx, my = dc->my, mz = dc->mz;
+  const int ia = isc ? 0 : 1, ja = jsc ? 0 : 1, ka = ksc ? 0 : 1;
+#define X(i, j, k) xf[IX(df, i, j, k)]
+#define W(i, j, k) (1 - nvert_f[IX(df, i, j, k)] > 0. ? 1 - nvert_f[IX(df, i, j, k)] : 0.)
+  for (int k = 0; k < mz; k++)
+    for (int j = 0; j < my; j++)
+      for (int i = 0; i < mx; i++) {
+        size_t t = IX(dc, i, j, k);
+        if (k == 0 || k == mz - 1 || j == 0 || j == my - 1 || i == 0 || i == mx - 1) {
+          fc[t] = 0.;
+          continue;
+        }
+        int ih = isc ? i : 2 * i, jh = jsc ? j : 2 * j, kh = ksc ? k : 2 * k;
+        fc[t] = 0.125 * (X(ih, jh, kh) * W(ih, jh, kh) + X(ih - ia, jh, kh) * W(ih - ia, jh, kh) +
+                         X(ih, jh - ja, kh) * W(ih, jh - ja, kh) + X(ih, jh, kh - ka) * W(ih, jh, kh - ka) +
+                         X(ih - ia, jh - ja, kh) * W(ih - ia, jh - ja, kh) +
+                         X(ih, jh - ja, kh - ka) * W(ih, jh - ja, kh - ka) +
+                         X(ih - ia, jh, kh - ka) * W(ih - ia, jh, kh - ka) +
+                         X(ih - ia, jh - ja, kh - ka) * W(ih - ia, jh - ja, kh - ka));
+        if (nvert_c[t] > 0.1) fc[t] = 0.;
+      }
+#undef X
+#undef W
+}
+
+/* MyInterpolation (Source/poisson.c:527-670) with the GridInterpolation
+ * macro (poisson.c:474-507): trilinear (3/4, 1/4) weights, one-sided next
+ * to boundaries and blanked coarse neighbours. */
+void or_my_interpolation(const or_dims *df, const or_dims *dc, int isc, int jsc, int ksc,
+                         const double *nvert_f, const double *nvert_c, const double *xc, double *ff)
+{
+  const int mx = df->mx, my = df->my, mz = df->mz;
+#define XC(i, j, k) xc[IX(dc, i, j, k)]
+#define NC(i, j, k) nvert_c[IX(dc, i, j, k)]
+  memset(ff, 0, sizeof(double) * (size_t)mx * my * mz);
+  for (int k = 1; k < mz - 1; k++)
+    for (int j = 1; j < my - 1; j++)
+      for (int i = 1; i < mx - 1; i++) {
+        int ic, jc, kc, ia, ja, ka;
+        if (isc) { ic = i; ia = 0; }
+        else { ic = (i + 1) / 2; ia = (i - 2 * ic) == 0 ? 1 : -1; if (i == 1 || i == mx - 2) ia = 0; }
+        if (jsc) { jc = j; ja = 0; }
+        else { jc = (j + 1) / 2; ja = (j - 2 * jc) == 0 ? 1 : -1; if (j == 1 || j == my - 2) ja = 0; }
+        if (ksc) { kc = k; ka = 0; }
+        else { kc = (k + 1) / 2; ka = (k - 2 * kc) == 0 ? 1 : -1; if (k == 1 || k == mz - 2) ka = 0; }
+        if (ka == -1 && NC(ic, jc, kc - 1) > 0.1) ka = 0;
+        else if (ka == 1 && NC(ic, jc, kc + 1) > 0.1) ka = 0;
+        if (ja == -1 && NC(ic, jc - 1, kc) > 0.1) ja = 0;
+        else if (ja == 1 && NC(ic, jc + 1, kc) > 0.1) ja = 0;
+        if (ia == -1 && NC(ic - 1, jc, kc) > 0.1) ia = 0;
+        else if (ia == 1 && NC(ic + 1, jc, kc) > 0.1) ia = 0;
+        ff[IX(df, i, j, k)] = (XC(ic, jc, kc) * 9 + XC(ic, jc + ja, kc) * 3 + XC(ic + ia, jc, kc) * 3 +
+                               XC(ic + ia, jc + ja, kc)) * 3. / 64. +
+                              (XC(ic, jc, kc + ka) * 9 + XC(ic, jc + ja, kc + ka) * 3 +
+                               XC(ic + ia, jc, kc + ka) * 3 + XC(ic + ia, jc + ja, kc + ka)) / 64.;
+      }
+  for (int k = 0; k < mz; k++)
+    for (int j = 0; j < my; j++)
+      for (int i = 0; i < mx; i++) {
+        size_t t = IX(df, i, j, k);
+        if (i == 0 || i == mx - 1 || j == 0 || j == my - 1 || k == 0 || k == mz - 1) ff[t] = 0.;
+        if (nvert_f[t] > 0.1) ff[t] = 0.;
+      }
+#undef XC
+#undef NC
+}
+
+void or_stencil_apply(const or_dims *d, const int *rowtype, const double *vol, const double *x,
+                      double *y)
+{
+  /* y = A x on the DA layout; x must carry its periodic ghost copies. */
+  static const int off[19][3] = {{0, 0, 0},  {1, 0, 0},  {-1, 0, 0}, {0, 1, 0},  {0, -1, 0},
+                                 {0, 0, 1},  {0, 0, -1}, {1, 1, 0},  {1, -1, 0}, {-1, 1, 0},
+                                 {-1, -1, 0}, {0, 1, 1},  {0, 1, -1}, {0, -1, 1}, {0, -1, -1},
+                                 {1, 0, 1},  {1, 0, -1}, {-1, 0, 1}, {-1, 0, -1}};
+  const int mx = d->mx, my = d->my, mz = d->mz;
+  memset(y, 0, sizeof(double) * (size_t)mx * my * mz);
+  for (int k = 1; k < mz - 1; k++)
+    for (int j = 1; j < my - 1; j++)
+      for (int i = 1; i < mx - 1; i++) {
+        size_t t = IX(d, i, j, k);
+        if (rowtype[t] == OR_ROW_NONE) continue;
+        double s = 0;
+        for (int q = 0; q < 19; q++)
+          s += vol[t * 19 + q] * x[IX(d, i + off[q][0], j + off[q][1], k + off[q][2])];
+        y[t] = s;
+      }
+}

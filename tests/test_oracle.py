@@ -1,0 +1,136 @@
+"""CPU checks of the oracle (no GPU): the restated operator's structural
+properties, the right-hand side's consistency, the CPU baseline solver
+against an exact sparse solve, the transfer operators' algebra, and the
+committed golden fixtures.  The reference itself cannot be run here (it
+needs PETSc/HYPRE/MPI), so these pin the restatement against mathematics
+and against its own earlier outputs, not against the reference."""
+import os
+
+import numpy as np
+import pytest
+
+import oracle as O
+from vfs_poisson import configs as CF
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+
+
+@pytest.fixture(scope="module", params=["channel", "cylinder", "towers"])
+def system(request):
+    case = {"channel": lambda: CF.channel(12, 10, 12),
+            "cylinder": lambda: CF.cylinder(20, 12, 20),
+            "towers": lambda: CF.towers(24, 16, 24, radius=0.08)}[request.param]()
+    d = O.dims_of(case)
+    met = O.form_metrics(d, case.coor)
+    lhs = O.poisson_lhs(d, case.nvert, met)
+    return case, d, met, lhs
+
+
+def test_operator_is_conservative_with_constant_nullspace(system):
+    case, d, met, lhs = system
+    A = O.csr(lhs)
+    fluid = O.from_da(d, lhs["gid"], (case.nvert < 0.1).astype(float)) > 0
+    # A 1 = 0 on fluid rows (flux form) and column sums vanish (conservation)
+    assert np.abs((A @ np.ones(A.shape[0]))[fluid]).max() < 1e-14
+    assert np.abs(np.asarray(A.sum(axis=0)).ravel()[fluid]).max() < 1e-14
+    assert (A.diagonal()[fluid] < 0).all()
+
+
+def test_numbering_counts_fluid_cells(system):
+    case, d, met, lhs = system
+    inner = case.nvert[1:-1, 1:-1, 1:-1]
+    assert lhs["ndof"] == int(((inner.astype(int)) <= 0).sum())
+    gid = lhs["gid"][1:-1, 1:-1, 1:-1]
+    assert sorted(gid[gid >= 0].ravel().tolist()) == list(range(lhs["ndof"]))
+
+
+def test_rhs_is_consistent(system):
+    case, d, met, lhs = system
+    b = O.rhs(d, case.nvert, lhs["gid"], case.ucont, met["aj"])
+    assert abs(b.sum()) <= 1e-12 * np.abs(b).sum()
+
+
+def test_cpu_solver_matches_exact(system):
+    import scipy.sparse.linalg as spla
+    case, d, met, lhs = system
+    b = O.rhs(d, case.nvert, lhs["gid"], case.ucont, met["aj"])
+    A = O.csr(lhs)
+    mg = O.MGSolver(d, case.coor, case.nvert, met, threads=2)
+    x, st = mg.solve(O.to_da(d, lhs["gid"], b), rtol=1e-10)
+    x2 = O.from_da(d, lhs["gid"], x)
+    assert np.linalg.norm(b - A @ x2) / np.linalg.norm(b) <= 1e-10
+    Ap = A.tolil()
+    Ap[0, :] = 0
+    Ap[0, 0] = 1
+    bp = b.copy()
+    bp[0] = 0
+    xe = spla.spsolve(Ap.tocsr(), bp)
+    xe = O.remove_nullspace(d, case.nvert, lhs["gid"], xe)
+    x2 = O.remove_nullspace(d, case.nvert, lhs["gid"], x2)
+    assert np.linalg.norm(x2 - xe) / np.linalg.norm(xe) <= 1e-8
+
+
+def test_projection_reduces_divergence(system):
+    """Solve, update and project: the post-projection divergence of the fluid
+    cells away from the body falls to the solver tolerance level."""
+    import scipy.sparse.linalg as spla
+    case, d, met, lhs = system
+    u0 = case.ucont.copy()
+    # close the non-periodic walls so that the flux field can be made
+    # divergence-free (the synthetic Ucont is random on the wall faces too)
+    per = [case.periodic[q] or case.periodic[q + 3] for q in range(3)]
+    if not per[0]:
+        u0[:, :, 0, 0] = 0
+        u0[:, :, -2, 0] = 0
+    if not per[1]:
+        u0[:, 0, :, 1] = 0
+        u0[:, -2, :, 1] = 0
+    if not per[2]:
+        u0[0, :, :, 2] = 0
+        u0[-2, :, :, 2] = 0
+    b = O.rhs(d, case.nvert, lhs["gid"], u0, met["aj"])
+    A = O.csr(lhs).tolil()
+    A[0, :] = 0
+    A[0, 0] = 1
+    bp = b.copy()
+    bp[0] = 0
+    x2 = O.remove_nullspace(d, case.nvert, lhs["gid"], spla.spsolve(A.tocsr(), bp))
+    phi = O.convert_phi2_phi(d, case.nvert, x2)
+    div0 = O.divergence(d, case.nvert, u0, met["aj"])
+    u = O.projection(d, case.nvert, phi, met, u0)
+    div1 = O.divergence(d, case.nvert, u, met["aj"])
+    assert div1 < 1e-6 * div0
+
+
+def test_restriction_interpolation_weights():
+    """MyRestriction of a constant gives 1 on unblanked coarse cells;
+    MyInterpolation of a constant reproduces it on the fine grid."""
+    case = CF.channel(8, 8, 8)
+    d = O.dims_of(case)
+    dc = O.dims(6, 6, 6, case.periodic)
+    nvc = O.nvert_restriction(d, dc, 0, 0, 0, case.nvert)
+    one_f = np.zeros((10, 10, 10))
+    one_f[1:-1, 1:-1, 1:-1] = 1
+    rc = O.restriction(dc, d, 0, 0, 0, nvc, case.nvert, one_f)
+    np.testing.assert_allclose(rc[1:-1, 1:-1, 1:-1], 1.0)
+    one_c = np.zeros((6, 6, 6))
+    one_c[1:-1, 1:-1, 1:-1] = 1
+    f = O.interpolation(d, dc, 0, 0, 0, case.nvert, nvc, one_c)
+    np.testing.assert_allclose(f[1:-1, 1:-1, 1:-1], 1.0)
+
+
+@pytest.mark.parametrize("name", ["channel_8", "cylinder_12"])
+def test_golden_fixtures(name):
+    path = os.path.join(GOLDEN, f"{name}.npz")
+    if not os.path.exists(path):
+        pytest.skip("fixture not generated")
+    g = np.load(path)
+    case = CF.channel(8, 8, 8) if name.startswith("channel") else CF.cylinder(12, 8, 12)
+    np.testing.assert_array_equal(g["coor"], case.coor)
+    d = O.dims_of(case)
+    met = O.form_metrics(d, case.coor)
+    lhs = O.poisson_lhs(d, case.nvert, met)
+    np.testing.assert_array_equal(lhs["vol"], g["vol"])
+    b = O.rhs(d, case.nvert, lhs["gid"], case.ucont, met["aj"])
+    np.testing.assert_allclose(b, g["b"], rtol=0, atol=1e-13 * np.abs(g["b"]).max())
+    np.testing.assert_array_equal(met["iaj"], g["iaj"])

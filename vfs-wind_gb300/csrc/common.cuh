@@ -1,0 +1,129 @@
+// common.cuh -- shared device helpers of the GB300 pressure-Poisson library.
+//
+// Two layouts are used on the device:
+//   * the DA layout of the reference (Source/init.c:141-161): mx*my*mz points,
+//     i fastest, index 0 and m-1 the boundary layer; used for the arrays a
+//     caller hands over (coordinates, metrics, nvert, Ucont, phi, p);
+//   * the interior ("box") layout nx*ny*nz (nx = mx-2), used by every solver
+//     vector and operator plane so that no solver kernel touches ghost cells.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace vfs {
+
+// DA-layout grid with merged periodic flags (i_periodic || ii_periodic, ...).
+struct Grid {
+  int mx, my, mz;
+  int px, py, pz;
+  __host__ __device__ size_t n() const { return (size_t)mx * my * mz; }
+  __host__ __device__ size_t at(int i, int j, int k) const {
+    return ((size_t)k * my + j) * mx + i;
+  }
+  // Ghost remap of the reference (e.g. Source/poisson.c:1143-1161): index 0
+  // and m-1 of a periodic direction stand for cells m-2 and 1.
+  __host__ __device__ int remap(int i, int j, int k, int &a, int &b, int &c, int &fi, int &fj,
+                                int &fk) const {
+    a = i; b = j; c = k; fi = fj = fk = 0;
+    if (px) { if (i == 0) { a = mx - 2; fi = 1; } else if (i == mx - 1) { a = 1; fi = 1; } }
+    if (py) { if (j == 0) { b = my - 2; fj = 1; } else if (j == my - 1) { b = 1; fj = 1; } }
+    if (pz) { if (k == 0) { c = mz - 2; fk = 1; } else if (k == mz - 1) { c = 1; fk = 1; } }
+    return fi | fj | fk;
+  }
+};
+
+// Interior box of one multigrid level.
+struct Box {
+  int nx, ny, nz;
+  int px, py, pz;
+  __host__ __device__ size_t n() const { return (size_t)nx * ny * nz; }
+  __host__ __device__ size_t at(int i, int j, int k) const {
+    return ((size_t)k * ny + j) * nx + i;
+  }
+};
+
+// Stencil slot order of the reference's 19-point operator
+// (Source/poisson.c:957-975): offsets (di, dj, dk) per slot.
+enum { CP = 0, EP, WP, NP, SP, TP, BP, NE, SE, NW, SW, TN, BN, TS, BS, TE, BE, TW, BW, NSLOT };
+__host__ __device__ inline void slot_offset(int s, int &di, int &dj, int &dk) {
+  const int8_t o[NSLOT][3] = {{0, 0, 0},  {1, 0, 0},   {-1, 0, 0}, {0, 1, 0},  {0, -1, 0},
+                              {0, 0, 1},  {0, 0, -1},  {1, 1, 0},  {1, -1, 0}, {-1, 1, 0},
+                              {-1, -1, 0}, {0, 1, 1},  {0, 1, -1}, {0, -1, 1}, {0, -1, -1},
+                              {1, 0, 1},  {1, 0, -1},  {-1, 0, 1}, {-1, 0, -1}};
+  di = o[s][0]; dj = o[s][1]; dk = o[s][2];
+}
+
+// Neighbour coordinates in a box: periodic wrap, otherwise clamped onto the
+// cell itself (its operator coefficient is zero there by construction).
+struct Nbr {
+  int im, ip, jm, jp, km, kp;
+  __device__ Nbr(const Box &b, int i, int j, int k) {
+    im = i > 0 ? i - 1 : (b.px ? b.nx - 1 : i);
+    ip = i < b.nx - 1 ? i + 1 : (b.px ? 0 : i);
+    jm = j > 0 ? j - 1 : (b.py ? b.ny - 1 : j);
+    jp = j < b.ny - 1 ? j + 1 : (b.py ? 0 : j);
+    km = k > 0 ? k - 1 : (b.pz ? b.nz - 1 : k);
+    kp = k < b.nz - 1 ? k + 1 : (b.pz ? 0 : k);
+  }
+};
+
+// Linear indices of the 19 stencil points of (i,j,k) in slot order.
+__device__ inline void stencil_index(const Box &b, int i, int j, int k, size_t idx[NSLOT]) {
+  Nbr q(b, i, j, k);
+  idx[CP] = b.at(i, j, k);
+  idx[EP] = b.at(q.ip, j, k);     idx[WP] = b.at(q.im, j, k);
+  idx[NP] = b.at(i, q.jp, k);     idx[SP] = b.at(i, q.jm, k);
+  idx[TP] = b.at(i, j, q.kp);     idx[BP] = b.at(i, j, q.km);
+  idx[NE] = b.at(q.ip, q.jp, k);  idx[SE] = b.at(q.ip, q.jm, k);
+  idx[NW] = b.at(q.im, q.jp, k);  idx[SW] = b.at(q.im, q.jm, k);
+  idx[TN] = b.at(i, q.jp, q.kp);  idx[BN] = b.at(i, q.jp, q.km);
+  idx[TS] = b.at(i, q.jm, q.kp);  idx[BS] = b.at(i, q.jm, q.km);
+  idx[TE] = b.at(q.ip, j, q.kp);  idx[BE] = b.at(q.ip, j, q.km);
+  idx[TW] = b.at(q.im, j, q.kp);  idx[BW] = b.at(q.im, j, q.km);
+}
+
+// ---- deterministic reductions: fixed-shape block trees ----
+template <typename T>
+__device__ inline T warp_sum(T v) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  return v;
+}
+template <typename T>
+__device__ inline T warp_max(T v) {
+  for (int o = 16; o > 0; o >>= 1) { T w = __shfl_down_sync(0xffffffffu, v, o); v = w > v ? w : v; }
+  return v;
+}
+// Sum over the block; result valid in thread 0.  blockDim.x multiple of 32, <= 1024.
+template <typename T>
+__device__ inline T block_sum(T v) {
+  __shared__ T sh[32];
+  int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  v = warp_sum(v);
+  __syncthreads();
+  if (lane == 0) sh[w] = v;
+  __syncthreads();
+  T r = 0;
+  if (w == 0) {
+    r = (lane < (int)(blockDim.x >> 5)) ? sh[lane] : (T)0;
+    r = warp_sum(r);
+  }
+  return r;
+}
+template <typename T>
+__device__ inline T block_max(T v) {
+  __shared__ T sh[32];
+  int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  v = warp_max(v);
+  __syncthreads();
+  if (lane == 0) sh[w] = v;
+  __syncthreads();
+  T r = 0;
+  if (w == 0) {
+    r = (lane < (int)(blockDim.x >> 5)) ? sh[lane] : (T)0;
+    r = warp_max(r);
+  }
+  return r;
+}
+
+}  // namespace vfs

@@ -1,0 +1,83 @@
+// kernels.cuh -- kernel declarations shared by the host orchestration.
+#pragma once
+#include "common.cuh"
+
+namespace vfs {
+
+// Device pointers of the FormMetrics outputs (DA layout).
+struct MetricPtrs {
+  double *cent, *csi, *eta, *zet, *aj;
+  double *icsi, *ieta, *izet, *iaj;
+  double *jcsi, *jeta, *jzet, *jaj;
+  double *kcsi, *keta, *kzet, *kaj;
+};
+
+// setup.cu (compiled without FMA contraction)
+__global__ void k_metrics_cell(Grid g, const double *coor, MetricPtrs m);
+__global__ void k_metrics_mirror(Grid g, MetricPtrs m, int dir);
+__global__ void k_metrics_periodic(Grid g, MetricPtrs m);
+__global__ void k_metrics_face(Grid g, const double *coor, MetricPtrs m, int dir);
+__global__ void k_count_dofs(Grid g, Box b, const double *nvert, int *block_count);
+__global__ void k_scan_blocks(int *block_count, int nblocks, int *total);
+__global__ void k_number_dofs(Grid g, Box b, const double *nvert, const int *block_off, int *gid_box);
+__global__ void k_gid_da(Grid g, Box b, const int *gid_box, int *gid_da);
+__global__ void k_assemble(Grid g, Box b, const double *nvert, MetricPtrs m, int scale, int filter, double *A,
+                           uint8_t *rowtype);
+__global__ void k_projection_coef(Grid g, Box b, MetricPtrs m, double *pc);
+__global__ void k_level_masks(Grid g, Box b, const double *nvert, uint8_t *blank, double *w64, float *w32,
+                              double *aj_box, const double *aj_da);
+__global__ void k_rhs(Grid g, Box b, const double *nvert, const double *ucont, const double *aj, double dt,
+                      double st, double coeff, double *rhs, double *partial);
+__global__ void k_reduce_rows(const double *partial, int nb, int nrow, double *out);
+__global__ void k_rhs_nullspace(Grid g, Box b, const double *nvert, const double *aj, const double *sums,
+                                double *rhs);
+__global__ void k_mean_partial(Box b, const uint8_t *fluid, const double *x, double *partial);
+__global__ void k_shift_fluid(Box b, const uint8_t *fluid, const double *sums, double *x);
+__global__ void k_fluid_mask(Grid g, Box b, const double *nvert, uint8_t *fluid);
+__global__ void k_box_to_da_phi(Grid g, Box b, const double *nvert, const double *x, double *phi);
+__global__ void k_da_to_box(Grid g, Box b, const double *da, double *x);
+__global__ void k_box_to_da(Grid g, Box b, const double *x, double *da);
+__global__ void k_update_pressure(Grid g, const double *nvert, const double *phi, double *p);
+__global__ void k_periodic_copy2(Grid g, double *p, double *phi);
+__global__ void k_projection(Grid g, Box b, const double *nvert, const double *phi, const double *pc, double dt,
+                             double st, double coeff, double *ucont);
+__global__ void k_periodic_faces(Grid g, double *ucont);
+__global__ void k_divergence(Grid g, Box b, const double *nvert, const double *ucont, const double *aj,
+                             double *partial);
+__global__ void k_reduce_max(const double *partial, int nb, double *out);
+__global__ void k_coarse_nodes(Grid gf, Grid gc, int cx, int cy, int cz, const double *cf, double *cc);
+__global__ void k_nvert_restrict(Grid gh, Grid gc, int cx, int cy, int cz, const double *nh, double *nc);
+__global__ void k_nvert_fill(Grid gc, const double *src, double *dst);
+__global__ void k_restrict_f32(Box bf, Box bc, int cx, int cy, int cz, const float *rf, const float *wf,
+                               const uint8_t *blank_c, float *out);
+__global__ void k_restrict_f64(Box bf, Box bc, int cx, int cy, int cz, const double *rf, const double *wf,
+                               const uint8_t *blank_c, double *out);
+__global__ void k_prolong_f32(Box bf, Box bc, int cx, int cy, int cz, const float *xc, const uint8_t *blank_c,
+                              const uint8_t *blank_f, float *xf, int add);
+__global__ void k_prolong_f64(Box bf, Box bc, int cx, int cy, int cz, const double *xc, const uint8_t *blank_c,
+                              const uint8_t *blank_f, double *xf, int add);
+
+// solve.cu (hot loop kernels)
+#define TYPED_DECL(T, S)                                                                                 \
+  __global__ void k_residual_##S(Box b, const T *A, const T *x, const T *rhs, T *r);                     \
+  __global__ void k_line_lu_##S(Box b, const double *A64, T *inv, T *cp);                                \
+  __global__ void k_line_sweep_##S(Box b, const T *A, const T *inv, const T *cp, const T *x, const T *rhs, \
+                                   T *xo, T omega, int zero_guess);                                      \
+  __global__ void k_coarsest_##S(int nd, const int *didx, const double *dinv, const T *rhs, T *x, size_t n); \
+  __global__ void k_cast_planes_##S(const double *src, T *dst, size_t n);
+TYPED_DECL(float, f32)
+TYPED_DECL(double, f64)
+#undef TYPED_DECL
+
+__global__ void k_apply64(Box b, const double *A, const double *x, double *y);
+__global__ void k_residual64(Box b, const double *A, const double *x, const double *rhs, double *r, double *partial);
+__global__ void k_dots(size_t n, int nv, const double *const *V, const double *w, double *partial);
+__global__ void k_gs_update(size_t n, int nv, const double *const *V, const double *coef, double *w,
+                            double *partial);
+__global__ void k_axpy_multi(size_t n, int nv, const double *const *Z, const double *coef, double *x);
+__global__ void k_scale_to(size_t n, const double *v, double s, const double *scale, float *out32,
+                           double *out64);
+__global__ void k_to64(size_t n, const float *x32, const double *x64, double s, double *out);
+__global__ void k_sumsq(size_t n, const double *x, double *partial);
+
+}  // namespace vfs

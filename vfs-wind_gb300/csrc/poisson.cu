@@ -1,0 +1,1062 @@
+// poisson.cu -- host side of the GB300 pressure-Poisson library: the handle,
+// multigrid hierarchy set-up, the FGMRES(m) outer iteration in FP64 with an
+// FP32 (or FP64) V-cycle preconditioner, CUDA-graph capture of the V-cycle,
+// and the C ABI declared in include/vfs_poisson.h.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <type_traits>
+#include <vector>
+
+#include "kernels.cuh"
+#include "vfs_poisson.h"
+
+using namespace vfs;
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const std::string &msg) {
+  g_err = msg;
+  return code;
+}
+
+#define CUDA_TRY(expr)                                                                      \
+  do {                                                                                      \
+    cudaError_t e_ = (expr);                                                                \
+    if (e_ != cudaSuccess) {                                                                \
+      cudaGetLastError();                                                                   \
+      return fail(e_ == cudaErrorMemoryAllocation ? VFS_ENOMEM : VFS_ECUDA,                 \
+                  std::string(#expr) + ": " + cudaGetErrorString(e_));                      \
+    }                                                                                       \
+  } while (0)
+
+#define TRY(expr)            \
+  do {                       \
+    int rc_ = (expr);        \
+    if (rc_ != VFS_OK) return rc_; \
+  } while (0)
+
+constexpr int kMaxLevels = 24;
+constexpr int kRedBlocks = 1216;  // 8 x 152 SMs, fixed for deterministic reductions
+
+// device helper kernels that only the host orchestration needs
+__global__ void k_row_scale(size_t n, const uint8_t *rowtype, const double *aj_box, double *scale) {
+  size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= n) return;
+  scale[c] = rowtype[c] == 1 ? aj_box[c] : (rowtype[c] == 2 ? 1.0 : 0.0);
+}
+__global__ void k_mask_box(size_t n, const uint8_t *rowtype, double *x) {
+  size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c < n && rowtype[c] == 0) x[c] = 0.;
+}
+__device__ inline void atomic_max_pos(double *addr, double v) {
+  // non-negative doubles order like their bit patterns
+  atomicMax((unsigned long long *)addr, (unsigned long long)__double_as_longlong(v));
+}
+__global__ void k_max_spacing(Grid g, const double *coor, double *H) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y + 1, k = blockIdx.z + 1;
+  if (i < 1 || i >= g.mx - 1) return;
+#define CO(a, b, c, q) coor[g.at(a, b, c) * 3 + (q)]
+  double d[3] = {0, 0, 0};
+  for (int q = 0; q < 3; q++) {
+    double fp0 = 0.25 * (CO(i, j, k, q) + CO(i, j - 1, k, q) + CO(i, j, k - 1, q) + CO(i, j - 1, k - 1, q));
+    double fm0 = 0.25 * (CO(i - 1, j, k, q) + CO(i - 1, j - 1, k, q) + CO(i - 1, j, k - 1, q) + CO(i - 1, j - 1, k - 1, q));
+    double fp1 = 0.25 * (CO(i, j, k, q) + CO(i - 1, j, k, q) + CO(i, j, k - 1, q) + CO(i - 1, j, k - 1, q));
+    double fm1 = 0.25 * (CO(i, j - 1, k, q) + CO(i - 1, j - 1, k, q) + CO(i, j - 1, k - 1, q) + CO(i - 1, j - 1, k - 1, q));
+    double fp2 = 0.25 * (CO(i, j, k, q) + CO(i - 1, j, k, q) + CO(i, j - 1, k, q) + CO(i - 1, j - 1, k, q));
+    double fm2 = 0.25 * (CO(i, j, k - 1, q) + CO(i - 1, j, k - 1, q) + CO(i, j - 1, k - 1, q) + CO(i - 1, j - 1, k - 1, q));
+    d[0] += (fp0 - fm0) * (fp0 - fm0);
+    d[1] += (fp1 - fm1) * (fp1 - fm1);
+    d[2] += (fp2 - fm2) * (fp2 - fm2);
+  }
+#undef CO
+  for (int q = 0; q < 3; q++) atomic_max_pos(&H[q], sqrt(d[q]));
+}
+
+struct Level {
+  Grid g{};
+  Box b{};
+  int cx = 0, cy = 0, cz = 0;
+  double *coor = nullptr, *nvert = nullptr;
+  MetricPtrs met{};
+  bool own_met = false;
+  double *A64 = nullptr;
+  float *A32 = nullptr;
+  uint8_t *rowtype = nullptr, *blank = nullptr;
+  double *inv64 = nullptr, *cp64 = nullptr, *w64 = nullptr;
+  float *inv32 = nullptr, *cp32 = nullptr, *w32 = nullptr;
+  double *v64[4] = {};  // x, b, r, t
+  float *v32[4] = {};
+  int nd = 0;
+  int *didx = nullptr;
+  double *dinv = nullptr;
+  double *xfinal64 = nullptr;  // where x lives after a V-cycle (set at capture)
+  float *xfinal32 = nullptr;
+};
+
+}  // namespace
+
+struct vfs_poisson {
+  vfs_grid_desc desc{};
+  Grid g{};
+  Box box{};
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::vector<void *> allocs;
+  int64_t launches = 0;
+  bool capturing = false;
+  // DA-layout inputs and outputs
+  double *coor = nullptr, *nvert = nullptr, *ucont = nullptr, *phi_da = nullptr, *p_da = nullptr;
+  double *stage = nullptr;  // DA-sized staging, 3 components
+  MetricPtrs met{};
+  // fine operator and masks (box layout)
+  double *A0 = nullptr, *scale = nullptr, *pc = nullptr, *aj_box = nullptr;
+  uint8_t *rowtype0 = nullptr, *fluid = nullptr;
+  int *gid_box = nullptr, *gid_da = nullptr, *blk = nullptr, *total = nullptr;
+  int ndof = 0;
+  double *b = nullptr, *x = nullptr, *r = nullptr;
+  // Krylov basis
+  int m_alloc = 0;
+  std::vector<double *> V, Z;
+  double **dV = nullptr, **dZ = nullptr;
+  double *partial = nullptr, *red = nullptr, *coef = nullptr;
+  size_t partial_len = 0;
+  double *hbuf = nullptr;  // pinned host readback
+  std::vector<Level> L;
+  bool have_grid = false, have_nvert = false, have_rhs = false, have_phi = false;
+  // graphs of the V-cycle per precision and parameters they were built for
+  cudaGraphExec_t gexec[2] = {nullptr, nullptr};
+  int64_t gnodes[2] = {0, 0};
+  int gparams[2][3] = {{-1, -1, -1}, {-1, -1, -1}};
+  double gomega[2] = {0, 0};
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+};
+
+namespace {
+
+template <typename T>
+int dalloc(vfs_poisson *h, T **p, size_t count) {
+  void *q = nullptr;
+  size_t bytes = std::max<size_t>(count, 1) * sizeof(T);
+  cudaError_t e = cudaMalloc(&q, bytes);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return fail(VFS_ENOMEM, "cudaMalloc of " + std::to_string(bytes) + " bytes failed");
+  }
+  h->allocs.push_back(q);
+  *p = (T *)q;
+  return VFS_OK;
+}
+void dfree(vfs_poisson *h, void *p) {
+  if (!p) return;
+  auto it = std::find(h->allocs.begin(), h->allocs.end(), p);
+  if (it != h->allocs.end()) h->allocs.erase(it);
+  cudaFree(p);
+}
+
+bool is_device_ptr(const void *p) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+// copy a caller array (host or device) into a device buffer
+int upload(vfs_poisson *h, double *dst, const double *src, size_t count) {
+  CUDA_TRY(cudaMemcpyAsync(dst, src, count * sizeof(double),
+                           is_device_ptr(src) ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, h->stream));
+  return VFS_OK;
+}
+int download(vfs_poisson *h, double *dst, const double *src, size_t count) {
+  CUDA_TRY(cudaMemcpyAsync(dst, src, count * sizeof(double),
+                           is_device_ptr(dst) ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, h->stream));
+  return VFS_OK;
+}
+int sync(vfs_poisson *h) {
+  CUDA_TRY(cudaGetLastError());
+  CUDA_TRY(cudaStreamSynchronize(h->stream));
+  return VFS_OK;
+}
+
+dim3 da_grid(const Grid &g, int bx = 128) { return dim3((g.mx + bx - 1) / bx, g.my, g.mz); }
+dim3 box_grid(const Box &b, int bx = 128) { return dim3((b.nx + bx - 1) / bx, b.ny, b.nz); }
+unsigned lin_grid(size_t n, int bx = 256) { return (unsigned)((n + bx - 1) / bx); }
+
+#define LAUNCH(h, kern, grid, block, ...)                          \
+  do {                                                             \
+    kern<<<(grid), (block), 0, (h)->stream>>>(__VA_ARGS__);        \
+    (h)->launches++;                                               \
+  } while (0)
+
+int alloc_metrics(vfs_poisson *h, const Grid &g, MetricPtrs &m) {
+  size_t n = g.n();
+  double **vec[] = {&m.cent, &m.csi, &m.eta, &m.zet, &m.icsi, &m.ieta, &m.izet, &m.jcsi, &m.jeta, &m.jzet,
+                    &m.kcsi, &m.keta, &m.kzet};
+  double **sca[] = {&m.aj, &m.iaj, &m.jaj, &m.kaj};
+  for (auto p : vec) { TRY(dalloc(h, p, 3 * n)); CUDA_TRY(cudaMemsetAsync(*p, 0, 3 * n * 8, h->stream)); }
+  for (auto p : sca) { TRY(dalloc(h, p, n)); CUDA_TRY(cudaMemsetAsync(*p, 0, n * 8, h->stream)); }
+  return VFS_OK;
+}
+void free_metrics(vfs_poisson *h, MetricPtrs &m) {
+  double *all[] = {m.cent, m.csi, m.eta, m.zet, m.icsi, m.ieta, m.izet, m.jcsi, m.jeta, m.jzet,
+                   m.kcsi, m.keta, m.kzet, m.aj, m.iaj, m.jaj, m.kaj};
+  for (auto p : all) dfree(h, p);
+  m = MetricPtrs{};
+}
+
+// FormMetrics on the device, in the reference's order of passes.
+int form_metrics(vfs_poisson *h, const Grid &g, const double *coor, MetricPtrs &m) {
+  LAUNCH(h, k_metrics_cell, da_grid(g), 128, g, coor, m);
+  LAUNCH(h, k_metrics_mirror, dim3((g.my + 127) / 128, g.mz), 128, g, m, 0);
+  LAUNCH(h, k_metrics_mirror, dim3((g.mx + 127) / 128, g.mz), 128, g, m, 1);
+  LAUNCH(h, k_metrics_mirror, dim3((g.mx + 127) / 128, g.my), 128, g, m, 2);
+  LAUNCH(h, k_metrics_periodic, da_grid(g), 128, g, m);
+  for (int d = 0; d < 3; d++) LAUNCH(h, k_metrics_face, da_grid(g), 128, g, coor, m, d);
+  return VFS_OK;
+}
+
+// Coarsening choice (same rule as the CPU baseline): coarsen a direction with
+// an even count >= 4 whose largest cell extent is at most twice the smallest
+// largest-extent of the other directions; fall back to the finest direction.
+bool choose_coarsening(const double H[3], const int n[3], int c[3]) {
+  bool any = false;
+  for (int q = 0; q < 3; q++) {
+    c[q] = 0;
+    if (n[q] % 2 || n[q] < 4) continue;
+    double mn = 1e300;
+    for (int e = 0; e < 3; e++)
+      if (e != q && n[e] >= 2 && H[e] < mn) mn = H[e];
+    if (H[q] <= 2.0 * mn) { c[q] = 1; any = true; }
+  }
+  if (!any) {
+    int best = -1;
+    for (int q = 0; q < 3; q++)
+      if (n[q] % 2 == 0 && n[q] >= 4 && (best < 0 || H[q] < H[best])) best = q;
+    if (best >= 0) { c[best] = 1; any = true; }
+  }
+  return any;
+}
+
+// Dense inverse of the coarsest operator with one pinned row per connected
+// component (the singular Neumann / periodic system becomes regular).
+int build_coarsest(vfs_poisson *h, Level &l) {
+  const size_t n = l.b.n();
+  std::vector<double> A(n * NSLOT);
+  std::vector<uint8_t> rt(n);
+  CUDA_TRY(cudaMemcpyAsync(A.data(), l.A64, n * NSLOT * 8, cudaMemcpyDeviceToHost, h->stream));
+  CUDA_TRY(cudaMemcpyAsync(rt.data(), l.rowtype, n, cudaMemcpyDeviceToHost, h->stream));
+  TRY(sync(h));
+  std::vector<int> map(n, -1), idx;
+  for (size_t c = 0; c < n; c++)
+    if (rt[c]) { map[c] = (int)idx.size(); idx.push_back((int)c); }
+  const int nd = (int)idx.size();
+  if (nd > 1024) return fail(VFS_EINVAL, "coarsest level has more than 1024 dofs");
+  std::vector<double> M((size_t)nd * nd, 0.), I((size_t)nd * nd, 0.);
+  const Box &b = l.b;
+  for (int r = 0; r < nd; r++) {
+    int c = idx[r];
+    int i = c % b.nx, j = (c / b.nx) % b.ny, k = c / (b.nx * b.ny);
+    for (int s = 0; s < NSLOT; s++) {
+      int di, dj, dk;
+      slot_offset(s, di, dj, dk);
+      int a = i + di, bb = j + dj, cc = k + dk;
+      if (a < 0) { if (!b.px) continue; a += b.nx; }
+      if (a >= b.nx) { if (!b.px) continue; a -= b.nx; }
+      if (bb < 0) { if (!b.py) continue; bb += b.ny; }
+      if (bb >= b.ny) { if (!b.py) continue; bb -= b.ny; }
+      if (cc < 0) { if (!b.pz) continue; cc += b.nz; }
+      if (cc >= b.nz) { if (!b.pz) continue; cc -= b.nz; }
+      int q = map[b.at(a, bb, cc)];
+      if (q < 0) continue;
+      M[(size_t)r * nd + q] += A[(size_t)s * n + c];
+    }
+  }
+  std::vector<int> comp(nd, -1), queue(nd), first;
+  int ncomp = 0;
+  for (int r0 = 0; r0 < nd; r0++) {
+    if (comp[r0] >= 0) continue;
+    int hd = 0, tl = 0;
+    queue[tl++] = r0;
+    comp[r0] = ncomp;
+    while (hd < tl) {
+      int r = queue[hd++];
+      for (int q = 0; q < nd; q++)
+        if (comp[q] < 0 && (M[(size_t)r * nd + q] != 0. || M[(size_t)q * nd + r] != 0.)) {
+          comp[q] = ncomp;
+          queue[tl++] = q;
+        }
+    }
+    for (int q = 0; q < nd; q++) M[(size_t)r0 * nd + q] = 0.;
+    M[(size_t)r0 * nd + r0] = 1.;
+    first.push_back(r0);
+    ncomp++;
+  }
+  for (int r = 0; r < nd; r++) I[(size_t)r * nd + r] = 1.;
+  for (int c = 0; c < nd; c++) {  // Gauss-Jordan, partial pivoting
+    int p = c;
+    for (int r = c + 1; r < nd; r++)
+      if (std::fabs(M[(size_t)r * nd + c]) > std::fabs(M[(size_t)p * nd + c])) p = r;
+    if (p != c)
+      for (int q = 0; q < nd; q++) {
+        std::swap(M[(size_t)c * nd + q], M[(size_t)p * nd + q]);
+        std::swap(I[(size_t)c * nd + q], I[(size_t)p * nd + q]);
+      }
+    double piv = M[(size_t)c * nd + c];
+    double ip = piv != 0. ? 1. / piv : 0.;
+    for (int q = 0; q < nd; q++) { M[(size_t)c * nd + q] *= ip; I[(size_t)c * nd + q] *= ip; }
+    for (int r = 0; r < nd; r++) {
+      if (r == c) continue;
+      double f = M[(size_t)r * nd + c];
+      if (f == 0.) continue;
+      for (int q = 0; q < nd; q++) {
+        M[(size_t)r * nd + q] -= f * M[(size_t)c * nd + q];
+        I[(size_t)r * nd + q] -= f * I[(size_t)c * nd + q];
+      }
+    }
+  }
+  for (int r0 : first)  // pinned rows see a zero right-hand side
+    for (int r = 0; r < nd; r++) I[(size_t)r * nd + r0] = 0.;
+  l.nd = nd;
+  dfree(h, l.didx);
+  dfree(h, l.dinv);
+  TRY(dalloc(h, &l.didx, nd));
+  TRY(dalloc(h, &l.dinv, (size_t)nd * nd));
+  CUDA_TRY(cudaMemcpyAsync(l.didx, idx.data(), nd * sizeof(int), cudaMemcpyHostToDevice, h->stream));
+  CUDA_TRY(cudaMemcpyAsync(l.dinv, I.data(), (size_t)nd * nd * 8, cudaMemcpyHostToDevice, h->stream));
+  return sync(h);
+}
+
+void free_level(vfs_poisson *h, Level &l, bool level0) {
+  if (!level0) { dfree(h, l.coor); dfree(h, l.nvert); }
+  if (l.own_met) free_metrics(h, l.met);
+  dfree(h, l.A64); dfree(h, l.A32); dfree(h, l.rowtype); dfree(h, l.blank);
+  dfree(h, l.inv64); dfree(h, l.cp64); dfree(h, l.w64); dfree(h, l.inv32); dfree(h, l.cp32); dfree(h, l.w32);
+  for (int q = 0; q < 4; q++) { dfree(h, l.v64[q]); dfree(h, l.v32[q]); }
+  dfree(h, l.didx); dfree(h, l.dinv);
+  l = Level{};
+}
+
+void drop_graphs(vfs_poisson *h) {
+  for (int p = 0; p < 2; p++) {
+    if (h->gexec[p]) cudaGraphExecDestroy(h->gexec[p]);
+    h->gexec[p] = nullptr;
+    h->gparams[p][0] = -1;
+  }
+}
+
+// Operator, masks and line factors of one level (assembled from its metrics).
+int build_level_operator(vfs_poisson *h, Level &l) {
+  const size_t n = l.b.n();
+  TRY(dalloc(h, &l.A64, n * NSLOT));
+  TRY(dalloc(h, &l.A32, n * NSLOT));
+  TRY(dalloc(h, &l.rowtype, n));
+  TRY(dalloc(h, &l.blank, n));
+  TRY(dalloc(h, &l.w64, n));
+  TRY(dalloc(h, &l.w32, n));
+  TRY(dalloc(h, &l.inv64, n)); TRY(dalloc(h, &l.cp64, n));
+  TRY(dalloc(h, &l.inv32, n)); TRY(dalloc(h, &l.cp32, n));
+  for (int q = 0; q < 4; q++) { TRY(dalloc(h, &l.v64[q], n)); TRY(dalloc(h, &l.v32[q], n)); }
+  LAUNCH(h, k_assemble, box_grid(l.b), 128, l.g, l.b, l.nvert, l.met, 1, 0, l.A64, l.rowtype);
+  LAUNCH(h, k_level_masks, lin_grid(n), 256, l.g, l.b, l.nvert, l.blank, l.w64, l.w32, (double *)nullptr,
+         (const double *)nullptr);
+  LAUNCH(h, k_line_lu_f64, dim3((l.b.nx + 127) / 128, l.b.nz), 128, l.b, l.A64, l.inv64, l.cp64);
+  LAUNCH(h, k_line_lu_f32, dim3((l.b.nx + 127) / 128, l.b.nz), 128, l.b, l.A64, l.inv32, l.cp32);
+  LAUNCH(h, k_cast_planes_f32, kRedBlocks, 256, l.A64, l.A32, n * NSLOT);
+  return VFS_OK;
+}
+
+int build_hierarchy(vfs_poisson *h, int coarsest_max) {
+  for (size_t li = 0; li < h->L.size(); li++) free_level(h, h->L[li], li == 0);
+  h->L.clear();
+  drop_graphs(h);
+  Level l0;
+  l0.g = h->g;
+  l0.b = h->box;
+  l0.coor = h->coor;
+  l0.nvert = h->nvert;
+  l0.met = h->met;
+  h->L.push_back(l0);
+  double *H;
+  TRY(dalloc(h, &H, 3));
+  for (;;) {
+    Level &f = h->L.back();
+    if (f.b.n() <= (size_t)coarsest_max || (int)h->L.size() >= kMaxLevels) break;
+    double Hh[3];
+    CUDA_TRY(cudaMemsetAsync(H, 0, 3 * 8, h->stream));
+    LAUNCH(h, k_max_spacing, dim3((f.g.mx + 127) / 128, f.g.my - 2, f.g.mz - 2), 128, f.g, f.coor, H);
+    CUDA_TRY(cudaMemcpyAsync(Hh, H, 24, cudaMemcpyDeviceToHost, h->stream));
+    TRY(sync(h));
+    int n3[3] = {f.b.nx, f.b.ny, f.b.nz}, c[3];
+    if (!choose_coarsening(Hh, n3, c)) break;
+    f.cx = c[0]; f.cy = c[1]; f.cz = c[2];
+    Level q;
+    q.b = f.b;
+    q.b.nx = c[0] ? f.b.nx / 2 : f.b.nx;
+    q.b.ny = c[1] ? f.b.ny / 2 : f.b.ny;
+    q.b.nz = c[2] ? f.b.nz / 2 : f.b.nz;
+    q.g = f.g;
+    q.g.mx = q.b.nx + 2; q.g.my = q.b.ny + 2; q.g.mz = q.b.nz + 2;
+    TRY(dalloc(h, &q.coor, q.g.n() * 3));
+    TRY(dalloc(h, &q.nvert, q.g.n()));
+    double *tmp;
+    TRY(dalloc(h, &tmp, q.g.n()));
+    LAUNCH(h, k_coarse_nodes, da_grid(q.g), 128, f.g, q.g, c[0], c[1], c[2], f.coor, q.coor);
+    LAUNCH(h, k_nvert_restrict, da_grid(q.g), 128, f.g, q.g, c[0], c[1], c[2], f.nvert, tmp);
+    LAUNCH(h, k_nvert_fill, da_grid(q.g), 128, q.g, tmp, q.nvert);
+    TRY(sync(h));
+    dfree(h, tmp);
+    h->L.push_back(q);
+  }
+  dfree(h, H);
+  for (size_t li = 0; li < h->L.size(); li++) {
+    Level &l = h->L[li];
+    if (li > 0) {
+      TRY(alloc_metrics(h, l.g, l.met));
+      l.own_met = true;
+      TRY(form_metrics(h, l.g, l.coor, l.met));
+    }
+    TRY(build_level_operator(h, l));
+    TRY(sync(h));
+    if (li > 0) {  // coarse metrics are only needed for the assembly
+      free_metrics(h, l.met);
+      l.own_met = false;
+    }
+  }
+  TRY(build_coarsest(h, h->L.back()));
+  return VFS_OK;
+}
+
+// ---- V-cycle (issued on the stream; captured into a graph when enabled) ----
+template <typename T>
+struct Prec;
+template <>
+struct Prec<float> {
+  static constexpr auto sweep = k_line_sweep_f32;
+  static constexpr auto residual = k_residual_f32;
+  static constexpr auto restrict_ = k_restrict_f32;
+  static constexpr auto prolong = k_prolong_f32;
+  static constexpr auto coarsest = k_coarsest_f32;
+  static float *A(Level &l) { return l.A32; }
+  static float *inv(Level &l) { return l.inv32; }
+  static float *cp(Level &l) { return l.cp32; }
+  static float *w(Level &l) { return l.w32; }
+  static float **v(Level &l) { return l.v32; }
+  static float *&xfinal(Level &l) { return l.xfinal32; }
+};
+template <>
+struct Prec<double> {
+  static constexpr auto sweep = k_line_sweep_f64;
+  static constexpr auto residual = k_residual_f64;
+  static constexpr auto restrict_ = k_restrict_f64;
+  static constexpr auto prolong = k_prolong_f64;
+  static constexpr auto coarsest = k_coarsest_f64;
+  static double *A(Level &l) { return l.A64; }
+  static double *inv(Level &l) { return l.inv64; }
+  static double *cp(Level &l) { return l.cp64; }
+  static double *w(Level &l) { return l.w64; }
+  static double **v(Level &l) { return l.v64; }
+  static double *&xfinal(Level &l) { return l.xfinal64; }
+};
+
+template <typename T>
+void vcycle(vfs_poisson *h, int li, int nu1, int nu2, T omega) {
+  Level &l = h->L[li];
+  T **v = Prec<T>::v(l);
+  T *x = v[0], *bb = v[1], *r = v[2], *t = v[3];
+  if (li == (int)h->L.size() - 1) {
+    LAUNCH(h, Prec<T>::coarsest, 1, 256, l.nd, l.didx, l.dinv, bb, x, l.b.n());
+    Prec<T>::xfinal(l) = x;
+    return;
+  }
+  dim3 lb(32, 4), lg((l.b.nx + 31) / 32, (l.b.nz + 3) / 4);
+  if (nu1 == 0) cudaMemsetAsync(x, 0, l.b.n() * sizeof(T), h->stream);
+  for (int s = 0; s < nu1; s++) {
+    LAUNCH(h, Prec<T>::sweep, lg, lb, l.b, Prec<T>::A(l), Prec<T>::inv(l), Prec<T>::cp(l), x, bb, t, omega,
+           s == 0 ? 1 : 0);
+    std::swap(x, t);
+  }
+  LAUNCH(h, Prec<T>::residual, box_grid(l.b), 128, l.b, Prec<T>::A(l), x, bb, r);
+  Level &q = h->L[li + 1];
+  LAUNCH(h, Prec<T>::restrict_, box_grid(q.b), 128, l.b, q.b, l.cx, l.cy, l.cz, r, Prec<T>::w(l), q.blank,
+         Prec<T>::v(q)[1]);
+  vcycle<T>(h, li + 1, nu1, nu2, omega);
+  LAUNCH(h, Prec<T>::prolong, box_grid(l.b), 128, l.b, q.b, l.cx, l.cy, l.cz, (const T *)Prec<T>::xfinal(q), q.blank,
+         l.blank, x, 1);
+  for (int s = 0; s < nu2; s++) {
+    LAUNCH(h, Prec<T>::sweep, lg, lb, l.b, Prec<T>::A(l), Prec<T>::inv(l), Prec<T>::cp(l), x, bb, t, omega, 0);
+    std::swap(x, t);
+  }
+  Prec<T>::xfinal(l) = x;
+}
+
+// Run one V-cycle on level 0 (rhs already in level 0's b buffer).
+template <typename T>
+int run_vcycle(vfs_poisson *h, const vfs_solve_opts &o) {
+  const int p = std::is_same<T, float>::value ? 0 : 1;
+  if (!o.use_graphs) {
+    vcycle<T>(h, 0, o.nu1, o.nu2, (T)o.omega);
+    return VFS_OK;
+  }
+  if (!h->gexec[p] || h->gparams[p][0] != o.nu1 || h->gparams[p][1] != o.nu2 || h->gomega[p] != o.omega) {
+    if (h->gexec[p]) cudaGraphExecDestroy(h->gexec[p]);
+    h->gexec[p] = nullptr;
+    cudaGraph_t graph;
+    int64_t before = h->launches;
+    CUDA_TRY(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+    vcycle<T>(h, 0, o.nu1, o.nu2, (T)o.omega);
+    CUDA_TRY(cudaStreamEndCapture(h->stream, &graph));
+    h->gnodes[p] = h->launches - before;
+    h->launches = before;
+    cudaError_t e = cudaGraphInstantiate(&h->gexec[p], graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      h->gexec[p] = nullptr;
+      return fail(VFS_ECUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
+    }
+    h->gparams[p][0] = o.nu1;
+    h->gparams[p][1] = o.nu2;
+    h->gomega[p] = o.omega;
+  }
+  CUDA_TRY(cudaGraphLaunch(h->gexec[p], h->stream));
+  h->launches += h->gnodes[p];
+  return VFS_OK;
+}
+
+// z = M (s v): aj row scaling, one V-cycle of the chosen precision, back to FP64.
+int precondition(vfs_poisson *h, const double *v, double s, double *z, const vfs_solve_opts &o) {
+  Level &l0 = h->L[0];
+  const size_t n = h->box.n();
+  if (o.precision == 0) {
+    LAUNCH(h, k_scale_to, kRedBlocks, 256, n, v, s, h->scale, l0.v32[1], (double *)nullptr);
+    TRY(run_vcycle<float>(h, o));
+    LAUNCH(h, k_to64, kRedBlocks, 256, n, (const float *)l0.xfinal32, (const double *)nullptr, 1.0, z);
+  } else {
+    LAUNCH(h, k_scale_to, kRedBlocks, 256, n, v, s, h->scale, (float *)nullptr, l0.v64[1]);
+    TRY(run_vcycle<double>(h, o));
+    LAUNCH(h, k_to64, kRedBlocks, 256, n, (const float *)nullptr, (const double *)l0.xfinal64, 1.0, z);
+  }
+  return VFS_OK;
+}
+
+// reduce `nrow` rows of `nb` partials on the device and read them back
+int reduce_read(vfs_poisson *h, int nb, int nrow, double *out) {
+  LAUNCH(h, k_reduce_rows, 1, 1024, h->partial, nb, nrow, h->red);
+  CUDA_TRY(cudaMemcpyAsync(h->hbuf, h->red, nrow * 8, cudaMemcpyDeviceToHost, h->stream));
+  TRY(sync(h));
+  for (int q = 0; q < nrow; q++) out[q] = h->hbuf[q];
+  return VFS_OK;
+}
+
+int residual_norm(vfs_poisson *h, const double *x, double *r, double *norm) {
+  dim3 gr = box_grid(h->box);
+  LAUNCH(h, k_residual64, gr, 128, h->box, h->A0, x, h->b, r, h->partial);
+  double s;
+  TRY(reduce_read(h, (int)(gr.x * gr.y * gr.z), 1, &s));
+  *norm = std::sqrt(s);
+  return VFS_OK;
+}
+
+int ensure_krylov(vfs_poisson *h, int m) {
+  if (m <= h->m_alloc) return VFS_OK;
+  for (auto p : h->V) dfree(h, p);
+  for (auto p : h->Z) dfree(h, p);
+  h->V.assign(m + 1, nullptr);
+  h->Z.assign(m, nullptr);
+  const size_t n = h->box.n();
+  for (int q = 0; q <= m; q++) TRY(dalloc(h, &h->V[q], n));
+  for (int q = 0; q < m; q++) TRY(dalloc(h, &h->Z[q], n));
+  dfree(h, h->dV); dfree(h, h->dZ); dfree(h, h->coef);
+  TRY(dalloc(h, &h->dV, m + 1));
+  TRY(dalloc(h, &h->dZ, m));
+  TRY(dalloc(h, &h->coef, m + 1));
+  CUDA_TRY(cudaMemcpyAsync(h->dV, h->V.data(), (m + 1) * sizeof(double *), cudaMemcpyHostToDevice, h->stream));
+  CUDA_TRY(cudaMemcpyAsync(h->dZ, h->Z.data(), m * sizeof(double *), cudaMemcpyHostToDevice, h->stream));
+  if (h->hbuf) cudaFreeHost(h->hbuf);
+  CUDA_TRY(cudaMallocHost(&h->hbuf, (m + 8) * 8 * 4));
+  h->m_alloc = m;
+  return sync(h);
+}
+
+int check_opts(const vfs_solve_opts &o) {
+  if (!(o.rtol > 0) || o.max_it < 1 || o.restart < 1 || o.restart > 64 || o.nu1 < 0 || o.nu2 < 0 ||
+      o.nu1 + o.nu2 < 1 || o.nu1 > 8 || o.nu2 > 8 || !(o.omega > 0 && o.omega <= 1.5) ||
+      (o.precision != 0 && o.precision != 1))
+    return fail(VFS_EINVAL, "invalid solver options");
+  return VFS_OK;
+}
+
+// FGMRES(m) with lazily normalised basis vectors: the stored V_i times sv[i]
+// is the unit Arnoldi vector, which saves one normalisation pass per step.
+int fgmres(vfs_poisson *h, const vfs_solve_opts &o, vfs_solve_stats *st) {
+  const size_t n = h->box.n();
+  const int m = o.restart;
+  TRY(ensure_krylov(h, m));
+  const int nbd = (int)((n + 256 * 8 - 1) / (256 * 8));
+  double bn2;
+  LAUNCH(h, k_sumsq, kRedBlocks, 256, n, h->b, h->partial);
+  TRY(reduce_read(h, kRedBlocks, 1, &bn2));
+  const double bn = std::sqrt(bn2);
+  int it = 0;
+  double rel = 0., beta = 0.;
+  std::vector<double> H((size_t)(m + 1) * m, 0.), cs(m), sn(m), gv(m + 1), y(m), sv(m + 1), hc(m + 2);
+  if (bn == 0.) {
+    CUDA_TRY(cudaMemsetAsync(h->x, 0, n * 8, h->stream));
+    st->initial_rel_residual = 0.;
+    st->rel_residual = 0.;
+    st->iterations = 0;
+    return VFS_OK;
+  }
+  TRY(residual_norm(h, h->x, h->V[0], &beta));
+  rel = beta / bn;
+  st->initial_rel_residual = rel;
+  while (rel > o.rtol && it < o.max_it) {
+    sv[0] = 1.0 / beta;
+    std::fill(gv.begin(), gv.end(), 0.);
+    gv[0] = beta;
+    int jj = 0;
+    for (; jj < m && it < o.max_it; jj++) {
+      TRY(precondition(h, h->V[jj], sv[jj], h->Z[jj], o));
+      double *w = h->V[jj + 1];
+      LAUNCH(h, k_apply64, box_grid(h->box), 128, h->box, h->A0, h->Z[jj], w);
+      // classical Gram-Schmidt, one pass plus a DGKS re-orthogonalisation
+      LAUNCH(h, k_dots, nbd, 256, n, jj + 1, (const double *const *)h->dV, w, h->partial);
+      TRY(reduce_read(h, nbd, jj + 2, hc.data()));
+      double ww = hc[jj + 1], wn = 0.;
+      for (int i = 0; i <= jj; i++) { H[(size_t)i * m + jj] = hc[i] * sv[i]; hc[i] = H[(size_t)i * m + jj] * sv[i]; }
+      CUDA_TRY(cudaMemcpyAsync(h->coef, hc.data(), (jj + 1) * 8, cudaMemcpyHostToDevice, h->stream));
+      LAUNCH(h, k_gs_update, nbd, 256, n, jj + 1, (const double *const *)h->dV, h->coef, w, h->partial);
+      TRY(reduce_read(h, nbd, 1, &wn));
+      if (std::sqrt(wn) < 0.7 * std::sqrt(ww)) {
+        LAUNCH(h, k_dots, nbd, 256, n, jj + 1, (const double *const *)h->dV, w, h->partial);
+        TRY(reduce_read(h, nbd, jj + 2, hc.data()));
+        for (int i = 0; i <= jj; i++) {
+          double c2 = hc[i] * sv[i];
+          H[(size_t)i * m + jj] += c2;
+          hc[i] = c2 * sv[i];
+        }
+        CUDA_TRY(cudaMemcpyAsync(h->coef, hc.data(), (jj + 1) * 8, cudaMemcpyHostToDevice, h->stream));
+        LAUNCH(h, k_gs_update, nbd, 256, n, jj + 1, (const double *const *)h->dV, h->coef, w, h->partial);
+        TRY(reduce_read(h, nbd, 1, &wn));
+      }
+      double hn = std::sqrt(wn);
+      H[(size_t)(jj + 1) * m + jj] = hn;
+      sv[jj + 1] = hn > 0. ? 1.0 / hn : 0.;
+      for (int i = 0; i < jj; i++) {
+        double a = H[(size_t)i * m + jj], b2 = H[(size_t)(i + 1) * m + jj];
+        H[(size_t)i * m + jj] = cs[i] * a + sn[i] * b2;
+        H[(size_t)(i + 1) * m + jj] = -sn[i] * a + cs[i] * b2;
+      }
+      double a = H[(size_t)jj * m + jj], b2 = H[(size_t)(jj + 1) * m + jj];
+      double den = std::sqrt(a * a + b2 * b2);
+      cs[jj] = den != 0. ? a / den : 1.;
+      sn[jj] = den != 0. ? b2 / den : 0.;
+      H[(size_t)jj * m + jj] = den;
+      H[(size_t)(jj + 1) * m + jj] = 0.;
+      gv[jj + 1] = -sn[jj] * gv[jj];
+      gv[jj] = cs[jj] * gv[jj];
+      it++;
+      if (std::fabs(gv[jj + 1]) / bn <= o.rtol || hn == 0.) { jj++; break; }
+    }
+    for (int i = jj - 1; i >= 0; i--) {
+      double s = gv[i];
+      for (int q = i + 1; q < jj; q++) s -= H[(size_t)i * m + q] * y[q];
+      y[i] = H[(size_t)i * m + i] != 0. ? s / H[(size_t)i * m + i] : 0.;
+    }
+    CUDA_TRY(cudaMemcpyAsync(h->coef, y.data(), jj * 8, cudaMemcpyHostToDevice, h->stream));
+    LAUNCH(h, k_axpy_multi, kRedBlocks, 256, n, jj, (const double *const *)h->dZ, h->coef, h->x);
+    TRY(residual_norm(h, h->x, h->V[0], &beta));
+    rel = beta / bn;
+  }
+  st->iterations = it;
+  st->rel_residual = rel;
+  return VFS_OK;
+}
+
+}  // namespace
+
+// ============================== C ABI =====================================
+
+extern "C" {
+
+const char *vfs_last_error(void) { return g_err.c_str(); }
+
+void vfs_poisson_default_opts(vfs_solve_opts *o) {
+  o->rtol = 1e-8;
+  o->max_it = 200;
+  o->restart = 20;
+  o->precision = 0;
+  o->nu1 = 2;
+  o->nu2 = 2;
+  o->omega = 0.8;
+  o->use_graphs = 1;
+  o->coarsest_max = 128;
+  o->warm_start = 0;
+}
+
+int vfs_poisson_create(const vfs_grid_desc *gd, vfs_poisson **out) {
+  if (!gd || !out) return fail(VFS_EINVAL, "null argument");
+  *out = nullptr;
+  if (gd->mx < 3 || gd->my < 3 || gd->mz < 3) return fail(VFS_EINVAL, "grid needs at least one interior cell per direction");
+  const int nx = gd->mx - 2, ny = gd->my - 2, nz = gd->mz - 2;
+  const bool px = gd->i_periodic || gd->ii_periodic, py = gd->j_periodic || gd->jj_periodic,
+             pz = gd->k_periodic || gd->kk_periodic;
+  if ((px && nx < 3) || (py && ny < 3) || (pz && nz < 3))
+    return fail(VFS_EINVAL, "a periodic direction needs at least 3 interior cells");
+  if ((size_t)gd->mx * gd->my * gd->mz > ((size_t)1 << 31))
+    return fail(VFS_EINVAL, "grid larger than 2^31 points");
+  vfs_poisson *h = new vfs_poisson();
+  h->desc = *gd;
+  h->g = Grid{gd->mx, gd->my, gd->mz, px, py, pz};
+  h->box = Box{nx, ny, nz, px, py, pz};
+  cudaGetDevice(&h->device);
+  auto bail = [&](int rc) { vfs_poisson_destroy(h); return rc; };
+  if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    cudaGetLastError();
+    delete h;
+    return fail(VFS_ECUDA, "cudaStreamCreate failed (no usable GPU?)");
+  }
+  cudaEventCreate(&h->ev0);
+  cudaEventCreate(&h->ev1);
+  const size_t N = h->g.n(), n = h->box.n();
+  int rc;
+  if ((rc = dalloc(h, &h->coor, 3 * N)) || (rc = dalloc(h, &h->nvert, N)) || (rc = dalloc(h, &h->ucont, 3 * N)) ||
+      (rc = dalloc(h, &h->phi_da, N)) || (rc = dalloc(h, &h->p_da, N)) || (rc = dalloc(h, &h->stage, 3 * N)) ||
+      (rc = alloc_metrics(h, h->g, h->met)) || (rc = dalloc(h, &h->A0, n * NSLOT)) ||
+      (rc = dalloc(h, &h->scale, n)) || (rc = dalloc(h, &h->pc, 12 * n)) || (rc = dalloc(h, &h->aj_box, n)) ||
+      (rc = dalloc(h, &h->rowtype0, n)) || (rc = dalloc(h, &h->fluid, n)) || (rc = dalloc(h, &h->gid_box, n)) ||
+      (rc = dalloc(h, &h->gid_da, N)) || (rc = dalloc(h, &h->b, n)) || (rc = dalloc(h, &h->x, n)) ||
+      (rc = dalloc(h, &h->r, n)) || (rc = dalloc(h, &h->red, 128)) || (rc = dalloc(h, &h->total, 1)))
+    return bail(rc);
+  const int nblk = (int)((n + 1023) / 1024);
+  if ((rc = dalloc(h, &h->blk, nblk))) return bail(rc);
+  h->partial_len = std::max<size_t>(n / 16 + 65536, (size_t)70 * ((n + 2047) / 2048) + 4096);
+  if ((rc = dalloc(h, &h->partial, h->partial_len))) return bail(rc);
+  if (cudaMallocHost(&h->hbuf, 256 * 8) != cudaSuccess) { cudaGetLastError(); return bail(fail(VFS_ENOMEM, "pinned alloc")); }
+  cudaMemsetAsync(h->phi_da, 0, N * 8, h->stream);
+  cudaMemsetAsync(h->x, 0, n * 8, h->stream);
+  if ((rc = sync(h))) return bail(rc);
+  *out = h;
+  return VFS_OK;
+}
+
+void vfs_poisson_destroy(vfs_poisson *h) {
+  if (!h) return;
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  drop_graphs(h);
+  for (void *p : h->allocs) cudaFree(p);
+  h->allocs.clear();
+  if (h->hbuf) cudaFreeHost(h->hbuf);
+  if (h->ev0) cudaEventDestroy(h->ev0);
+  if (h->ev1) cudaEventDestroy(h->ev1);
+  if (h->stream) cudaStreamDestroy(h->stream);
+  cudaGetLastError();
+  delete h;
+}
+
+int vfs_poisson_set_grid(vfs_poisson *h, const double *coor, const double *const *fm) {
+  if (!h || !coor) return fail(VFS_EINVAL, "null argument");
+  const size_t N = h->g.n();
+  TRY(upload(h, h->coor, coor, 3 * N));
+  TRY(form_metrics(h, h->g, h->coor, h->met));
+  if (fm) {
+    double *vec[9] = {h->met.icsi, h->met.ieta, h->met.izet, h->met.jcsi, h->met.jeta,
+                      h->met.jzet, h->met.kcsi, h->met.keta, h->met.kzet};
+    double *sca[4] = {h->met.iaj, h->met.jaj, h->met.kaj, h->met.aj};
+    for (int q = 0; q < 9; q++) if (fm[q]) TRY(upload(h, vec[q], fm[q], 3 * N));
+    for (int q = 0; q < 4; q++) if (fm[9 + q]) TRY(upload(h, sca[q], fm[9 + q], N));
+  }
+  LAUNCH(h, k_projection_coef, box_grid(h->box), 128, h->g, h->box, h->met, h->pc);
+  TRY(sync(h));
+  h->have_grid = true;
+  h->have_nvert = false;
+  return VFS_OK;
+}
+
+int vfs_poisson_set_nvert(vfs_poisson *h, const double *nvert) {
+  if (!h || !nvert) return fail(VFS_EINVAL, "null argument");
+  if (!h->have_grid) return fail(VFS_ESTATE, "set_grid must come before set_nvert");
+  const size_t N = h->g.n(), n = h->box.n();
+  TRY(upload(h, h->nvert, nvert, N));
+  // setup_lidx2: dof numbering in k-j-i order
+  const int nblk = (int)((n + 1023) / 1024);
+  LAUNCH(h, k_count_dofs, nblk, 1024, h->g, h->box, h->nvert, h->blk);
+  LAUNCH(h, k_scan_blocks, 1, 1024, h->blk, nblk, h->total);
+  LAUNCH(h, k_number_dofs, nblk, 1024, h->g, h->box, h->nvert, h->blk, h->gid_box);
+  LAUNCH(h, k_gid_da, da_grid(h->g), 128, h->g, h->box, h->gid_box, h->gid_da);
+  LAUNCH(h, k_fluid_mask, lin_grid(n), 256, h->g, h->box, h->nvert, h->fluid);
+  // PoissonLHSNew: unscaled operator with the reference's insertion filter
+  LAUNCH(h, k_assemble, box_grid(h->box), 128, h->g, h->box, h->nvert, h->met, 0, 1, h->A0, h->rowtype0);
+  uint8_t *blank;
+  double *w64;
+  float *w32;
+  TRY(dalloc(h, &blank, n));
+  TRY(dalloc(h, &w64, n));
+  TRY(dalloc(h, &w32, n));
+  LAUNCH(h, k_level_masks, lin_grid(n), 256, h->g, h->box, h->nvert, blank, w64, w32, h->aj_box,
+         (const double *)h->met.aj);
+  LAUNCH(h, k_row_scale, lin_grid(n), 256, n, h->rowtype0, h->aj_box, h->scale);
+  int tot = 0;
+  CUDA_TRY(cudaMemcpyAsync(&tot, h->total, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+  TRY(sync(h));
+  dfree(h, blank); dfree(h, w64); dfree(h, w32);
+  h->ndof = tot;
+  vfs_solve_opts o;
+  vfs_poisson_default_opts(&o);
+  TRY(build_hierarchy(h, o.coarsest_max));
+  CUDA_TRY(cudaMemsetAsync(h->x, 0, n * 8, h->stream));
+  TRY(sync(h));
+  h->have_nvert = true;
+  h->have_rhs = false;
+  return VFS_OK;
+}
+
+int vfs_poisson_rhs(vfs_poisson *h, const double *ucont, double dt, double st, double coeff) {
+  if (!h || !ucont) return fail(VFS_EINVAL, "null argument");
+  if (!h->have_nvert) return fail(VFS_ESTATE, "set_nvert must come before rhs");
+  if (!(dt != 0.) || !(coeff != 0.)) return fail(VFS_EINVAL, "dt and coeff must be non-zero");
+  const size_t N = h->g.n();
+  TRY(upload(h, h->ucont, ucont, 3 * N));
+  LAUNCH(h, k_rhs, kRedBlocks, 256, h->g, h->box, h->nvert, h->ucont, h->met.aj, dt, st, coeff, h->b, h->partial);
+  if (h->desc.bctype3 != -10) {  // Remove_Nullspace_Scale
+    LAUNCH(h, k_reduce_rows, 1, 1024, h->partial, kRedBlocks, 2, h->red);
+    LAUNCH(h, k_rhs_nullspace, kRedBlocks, 256, h->g, h->box, h->nvert, h->met.aj, h->red, h->b);
+  }
+  TRY(sync(h));
+  h->have_rhs = true;
+  return VFS_OK;
+}
+
+int vfs_poisson_solve(vfs_poisson *h, double *phi, const vfs_solve_opts *opts, vfs_solve_stats *stats) {
+  if (!h) return fail(VFS_EINVAL, "null handle");
+  if (!h->have_rhs) return fail(VFS_ESTATE, "rhs must come before solve");
+  vfs_solve_opts o;
+  if (opts) o = *opts; else vfs_poisson_default_opts(&o);
+  TRY(check_opts(o));
+  vfs_solve_stats st{};
+  const size_t n = h->box.n();
+  CUDA_TRY(cudaEventRecord(h->ev0, h->stream));
+  if (o.warm_start && phi) {
+    TRY(upload(h, h->stage, phi, h->g.n()));
+    LAUNCH(h, k_da_to_box, lin_grid(n), 256, h->g, h->box, h->stage, h->x);
+    LAUNCH(h, k_mask_box, lin_grid(n), 256, n, h->rowtype0, h->x);
+  } else if (!o.warm_start) {
+    CUDA_TRY(cudaMemsetAsync(h->x, 0, n * 8, h->stream));
+  }
+  TRY(fgmres(h, o, &st));
+  if (h->desc.bctype3 != -10) {  // Remove_Nullspace of phi
+    LAUNCH(h, k_mean_partial, kRedBlocks, 256, h->box, h->fluid, h->x, h->partial);
+    LAUNCH(h, k_reduce_rows, 1, 1024, h->partial, kRedBlocks, 2, h->red);
+    LAUNCH(h, k_shift_fluid, kRedBlocks, 256, h->box, h->fluid, h->red, h->x);
+  }
+  LAUNCH(h, k_box_to_da_phi, da_grid(h->g), 128, h->g, h->box, h->nvert, h->x, h->phi_da);
+  if (phi) TRY(download(h, phi, h->phi_da, h->g.n()));
+  CUDA_TRY(cudaEventRecord(h->ev1, h->stream));
+  TRY(sync(h));
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, h->ev0, h->ev1);
+  st.ms_total = ms;
+  st.levels = (int)h->L.size();
+  st.status = st.rel_residual <= o.rtol ? VFS_OK : VFS_ENOCONV;
+  if (stats) *stats = st;
+  h->have_phi = true;
+  if (st.status != VFS_OK)
+    return fail(VFS_ENOCONV, "solver stopped at relative residual " + std::to_string(st.rel_residual));
+  return VFS_OK;
+}
+
+int vfs_poisson_solver_hypre(vfs_poisson *h, const double *ucont, double dt, double st, double coeff, double *phi,
+                             const vfs_solve_opts *opts, vfs_solve_stats *stats) {
+  TRY(vfs_poisson_rhs(h, ucont, dt, st, coeff));
+  return vfs_poisson_solve(h, phi, opts, stats);
+}
+
+int vfs_poisson_update_pressure(vfs_poisson *h, double *p, double *phi) {
+  if (!h || !p) return fail(VFS_EINVAL, "null argument");
+  if (!h->have_nvert) return fail(VFS_ESTATE, "set_nvert must come before update_pressure");
+  const size_t N = h->g.n();
+  TRY(upload(h, h->p_da, p, N));
+  if (phi) TRY(upload(h, h->phi_da, phi, N));
+  LAUNCH(h, k_update_pressure, da_grid(h->g), 128, h->g, h->nvert, h->phi_da, h->p_da);
+  LAUNCH(h, k_periodic_copy2, da_grid(h->g), 128, h->g, h->p_da, h->phi_da);
+  TRY(download(h, p, h->p_da, N));
+  if (phi) TRY(download(h, phi, h->phi_da, N));
+  return sync(h);
+}
+
+int vfs_poisson_projection(vfs_poisson *h, double *ucont, double dt, double st, double coeff) {
+  if (!h || !ucont) return fail(VFS_EINVAL, "null argument");
+  if (!h->have_nvert) return fail(VFS_ESTATE, "set_nvert must come before projection");
+  if (!(coeff != 0.)) return fail(VFS_EINVAL, "coeff must be non-zero");
+  const size_t N = h->g.n();
+  TRY(upload(h, h->ucont, ucont, 3 * N));
+  LAUNCH(h, k_projection, box_grid(h->box), 128, h->g, h->box, h->nvert, h->phi_da, h->pc, dt, st, coeff, h->ucont);
+  LAUNCH(h, k_periodic_faces, da_grid(h->g), 128, h->g, h->ucont);
+  TRY(download(h, ucont, h->ucont, 3 * N));
+  return sync(h);
+}
+
+int vfs_poisson_divergence(vfs_poisson *h, const double *ucont, double *maxdiv) {
+  if (!h || !ucont || !maxdiv) return fail(VFS_EINVAL, "null argument");
+  if (!h->have_nvert) return fail(VFS_ESTATE, "set_nvert must come before divergence");
+  const size_t N = h->g.n();
+  const double *u = ucont;
+  if (!is_device_ptr(ucont)) {
+    TRY(upload(h, h->stage, ucont, 3 * N));
+    u = h->stage;
+  }
+  LAUNCH(h, k_divergence, kRedBlocks, 256, h->g, h->box, h->nvert, u, h->met.aj, h->partial);
+  LAUNCH(h, k_reduce_max, 1, 1024, h->partial, kRedBlocks, h->red);
+  CUDA_TRY(cudaMemcpyAsync(h->hbuf, h->red, 8, cudaMemcpyDeviceToHost, h->stream));
+  TRY(sync(h));
+  *maxdiv = h->hbuf[0];
+  return VFS_OK;
+}
+
+int vfs_poisson_get_numbering(vfs_poisson *h, int *ndof, int32_t *gid) {
+  if (!h || !ndof) return fail(VFS_EINVAL, "null argument");
+  if (!h->have_nvert) return fail(VFS_ESTATE, "set_nvert must come first");
+  *ndof = h->ndof;
+  if (gid) {
+    CUDA_TRY(cudaMemcpyAsync(gid, h->gid_da, h->g.n() * 4,
+                             is_device_ptr(gid) ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, h->stream));
+  }
+  return sync(h);
+}
+
+int vfs_poisson_get_operator(vfs_poisson *h, double *vol, int32_t *rowtype) {
+  if (!h || !vol) return fail(VFS_EINVAL, "null argument");
+  if (!h->have_nvert) return fail(VFS_ESTATE, "set_nvert must come first");
+  const size_t n = h->box.n();
+  const Grid &g = h->g;
+  const Box &b = h->box;
+  std::vector<double> A(n * NSLOT);
+  std::vector<uint8_t> rt(n);
+  CUDA_TRY(cudaMemcpyAsync(A.data(), h->A0, n * NSLOT * 8, cudaMemcpyDeviceToHost, h->stream));
+  CUDA_TRY(cudaMemcpyAsync(rt.data(), h->rowtype0, n, cudaMemcpyDeviceToHost, h->stream));
+  TRY(sync(h));
+  std::vector<double> out(g.n() * NSLOT, 0.);
+  std::vector<int32_t> ort(g.n(), 0);
+  for (int k = 0; k < b.nz; k++)
+    for (int j = 0; j < b.ny; j++)
+      for (int i = 0; i < b.nx; i++) {
+        size_t c = b.at(i, j, k), t = g.at(i + 1, j + 1, k + 1);
+        ort[t] = rt[c];
+        for (int s = 0; s < NSLOT; s++) out[t * NSLOT + s] = A[(size_t)s * n + c];
+      }
+  bool dev = is_device_ptr(vol);
+  CUDA_TRY(cudaMemcpy(vol, out.data(), out.size() * 8, dev ? cudaMemcpyHostToDevice : cudaMemcpyHostToHost));
+  if (rowtype)
+    CUDA_TRY(cudaMemcpy(rowtype, ort.data(), ort.size() * 4,
+                        is_device_ptr(rowtype) ? cudaMemcpyHostToDevice : cudaMemcpyHostToHost));
+  return VFS_OK;
+}
+
+int vfs_poisson_get_metric(vfs_poisson *h, int which, double *out) {
+  if (!h || !out) return fail(VFS_EINVAL, "null argument");
+  if (!h->have_grid) return fail(VFS_ESTATE, "set_grid must come first");
+  double *vec[13] = {h->met.icsi, h->met.ieta, h->met.izet, h->met.jcsi, h->met.jeta, h->met.jzet, h->met.kcsi,
+                     h->met.keta, h->met.kzet, h->met.csi,  h->met.eta,  h->met.zet,  h->met.cent};
+  double *sca[4] = {h->met.iaj, h->met.jaj, h->met.kaj, h->met.aj};
+  const size_t N = h->g.n();
+  if (which >= 0 && which < 13) TRY(download(h, out, vec[which], 3 * N));
+  else if (which >= 13 && which < 17) TRY(download(h, out, sca[which - 13], N));
+  else return fail(VFS_EINVAL, "metric index out of range");
+  return sync(h);
+}
+
+int vfs_poisson_get_rhs(vfs_poisson *h, double *b) {
+  if (!h || !b) return fail(VFS_EINVAL, "null argument");
+  if (!h->have_rhs) return fail(VFS_ESTATE, "rhs must come first");
+  LAUNCH(h, k_box_to_da, da_grid(h->g), 128, h->g, h->box, h->b, h->stage);
+  TRY(download(h, b, h->stage, h->g.n()));
+  return sync(h);
+}
+
+int vfs_poisson_apply(vfs_poisson *h, const double *x, double *y) {
+  if (!h || !x || !y) return fail(VFS_EINVAL, "null argument");
+  if (!h->have_nvert) return fail(VFS_ESTATE, "set_nvert must come first");
+  const size_t n = h->box.n();
+  TRY(upload(h, h->stage, x, h->g.n()));
+  double *tmp = h->L[0].v64[3];
+  LAUNCH(h, k_da_to_box, lin_grid(n), 256, h->g, h->box, h->stage, h->r);
+  LAUNCH(h, k_apply64, box_grid(h->box), 128, h->box, h->A0, h->r, tmp);
+  LAUNCH(h, k_box_to_da, da_grid(h->g), 128, h->g, h->box, tmp, h->stage);
+  TRY(download(h, y, h->stage, h->g.n()));
+  return sync(h);
+}
+
+int vfs_poisson_mg_levels(vfs_poisson *h, int *nlevels) {
+  if (!h || !nlevels) return fail(VFS_EINVAL, "null argument");
+  if (!h->have_nvert) return fail(VFS_ESTATE, "set_nvert must come first");
+  *nlevels = (int)h->L.size();
+  return VFS_OK;
+}
+
+int vfs_poisson_mg_level_info(vfs_poisson *h, int level, int *d) {
+  if (!h || !d) return fail(VFS_EINVAL, "null argument");
+  if (level < 0 || level >= (int)h->L.size()) return fail(VFS_EINVAL, "level out of range");
+  Level &l = h->L[level];
+  d[0] = l.b.nx; d[1] = l.b.ny; d[2] = l.b.nz; d[3] = l.cx; d[4] = l.cy; d[5] = l.cz;
+  return VFS_OK;
+}
+
+int vfs_poisson_mg_get_nvert(vfs_poisson *h, int level, double *nvert) {
+  if (!h || !nvert) return fail(VFS_EINVAL, "null argument");
+  if (level < 0 || level >= (int)h->L.size()) return fail(VFS_EINVAL, "level out of range");
+  TRY(download(h, nvert, h->L[level].nvert, h->L[level].g.n()));
+  return sync(h);
+}
+
+int vfs_poisson_mg_restrict(vfs_poisson *h, int fine, const double *xf, double *fc) {
+  if (!h || !xf || !fc) return fail(VFS_EINVAL, "null argument");
+  if (fine < 0 || fine + 1 >= (int)h->L.size()) return fail(VFS_EINVAL, "level out of range");
+  Level &l = h->L[fine], &q = h->L[fine + 1];
+  TRY(upload(h, h->stage, xf, l.g.n()));
+  LAUNCH(h, k_da_to_box, lin_grid(l.b.n()), 256, l.g, l.b, h->stage, l.v64[2]);
+  LAUNCH(h, k_restrict_f64, box_grid(q.b), 128, l.b, q.b, l.cx, l.cy, l.cz, l.v64[2], l.w64, q.blank, q.v64[1]);
+  LAUNCH(h, k_box_to_da, da_grid(q.g), 128, q.g, q.b, q.v64[1], h->stage);
+  TRY(download(h, fc, h->stage, q.g.n()));
+  return sync(h);
+}
+
+int vfs_poisson_mg_interpolate(vfs_poisson *h, int fine, const double *xc, double *ff) {
+  if (!h || !xc || !ff) return fail(VFS_EINVAL, "null argument");
+  if (fine < 0 || fine + 1 >= (int)h->L.size()) return fail(VFS_EINVAL, "level out of range");
+  Level &l = h->L[fine], &q = h->L[fine + 1];
+  TRY(upload(h, h->stage, xc, q.g.n()));
+  LAUNCH(h, k_da_to_box, lin_grid(q.b.n()), 256, q.g, q.b, h->stage, q.v64[0]);
+  LAUNCH(h, k_prolong_f64, box_grid(l.b), 128, l.b, q.b, l.cx, l.cy, l.cz, (const double *)q.v64[0], q.blank,
+         l.blank, l.v64[2], 0);
+  LAUNCH(h, k_box_to_da, da_grid(l.g), 128, l.g, l.b, l.v64[2], h->stage);
+  TRY(download(h, ff, h->stage, l.g.n()));
+  return sync(h);
+}
+
+int vfs_poisson_mg_vcycle(vfs_poisson *h, int precision, const double *r, double *z) {
+  if (!h || !r || !z) return fail(VFS_EINVAL, "null argument");
+  if (!h->have_nvert) return fail(VFS_ESTATE, "set_nvert must come first");
+  vfs_solve_opts o;
+  vfs_poisson_default_opts(&o);
+  o.precision = precision ? 1 : 0;
+  const size_t n = h->box.n();
+  TRY(upload(h, h->stage, r, h->g.n()));
+  LAUNCH(h, k_da_to_box, lin_grid(n), 256, h->g, h->box, h->stage, h->r);
+  TRY(precondition(h, h->r, 1.0, h->r, o));
+  LAUNCH(h, k_box_to_da, da_grid(h->g), 128, h->g, h->box, h->r, h->stage);
+  TRY(download(h, z, h->stage, h->g.n()));
+  return sync(h);
+}
+
+int64_t vfs_poisson_kernel_launches(vfs_poisson *h) { return h ? h->launches : 0; }
+
+}  // extern "C"

@@ -1,0 +1,928 @@
+// setup.cu -- grid metrics, dof numbering, operator assembly, right-hand
+// side, pressure update, projection, divergence and the multigrid transfer
+// operators.
+//
+// This translation unit is compiled with -fmad=false: every floating-point
+// expression is rounded in the reference's source order, so these kernels
+// reproduce the reference's arithmetic (restated in the oracle) bit for bit.
+// Each kernel names the reference lines it follows.
+#include "common.cuh"
+#include "kernels.cuh"
+
+namespace vfs {
+
+static constexpr double kThr = 0.1;  // poisson_threshold, Source/main.c:124
+
+// --------------------------------------------------------------------------
+// FormMetrics (Source/metrics.c:12-810; NEWMETRIC is not defined there)
+// --------------------------------------------------------------------------
+#define CO(i, j, k, c) coor[g.at(i, j, k) * 3 + (c)]
+
+// cell centres and aj (metrics.c:103-121, :202-259) and the face-normal
+// "cell" metrics csi/eta/zet of the non-NEWMETRIC path (metrics.c:128-199).
+__global__ void k_metrics_cell(Grid g, const double *__restrict__ coor, MetricPtrs m) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y, k = blockIdx.z;
+  if (i >= g.mx) return;
+  size_t t = g.at(i, j, k);
+  const int mx = g.mx, my = g.my, mz = g.mz;
+  if (i >= 1 && i < mx - 1 && j >= 1 && j < my - 1 && k >= 1 && k < mz - 1) {
+    for (int c = 0; c < 3; c++)
+      m.cent[t * 3 + c] = 0.125 * (CO(i, j, k, c) + CO(i, j - 1, k, c) + CO(i, j, k - 1, c) +
+                                   CO(i, j - 1, k - 1, c) + CO(i - 1, j, k, c) + CO(i - 1, j - 1, k, c) +
+                                   CO(i - 1, j, k - 1, c) + CO(i - 1, j - 1, k - 1, c));
+    double dc[3], de[3], dz[3];
+    for (int c = 0; c < 3; c++) {
+      dc[c] = 0.25 * (CO(i, j, k, c) + CO(i, j - 1, k, c) + CO(i, j, k - 1, c) + CO(i, j - 1, k - 1, c) -
+                      CO(i - 1, j, k, c) - CO(i - 1, j - 1, k, c) - CO(i - 1, j, k - 1, c) -
+                      CO(i - 1, j - 1, k - 1, c));
+      de[c] = 0.25 * (CO(i, j, k, c) + CO(i - 1, j, k, c) + CO(i, j, k - 1, c) + CO(i - 1, j, k - 1, c) -
+                      CO(i, j - 1, k, c) - CO(i - 1, j - 1, k, c) - CO(i, j - 1, k - 1, c) -
+                      CO(i - 1, j - 1, k - 1, c));
+      dz[c] = 0.25 * (CO(i, j, k, c) + CO(i, j - 1, k, c) + CO(i - 1, j, k, c) + CO(i - 1, j - 1, k, c) -
+                      CO(i, j, k - 1, c) - CO(i, j - 1, k - 1, c) - CO(i - 1, j, k - 1, c) -
+                      CO(i - 1, j - 1, k - 1, c));
+    }
+    double det = dc[0] * (de[1] * dz[2] - de[2] * dz[1]) - dc[1] * (de[0] * dz[2] - de[2] * dz[0]) +
+                 dc[2] * (de[0] * dz[1] - de[1] * dz[0]);
+    m.aj[t] = 1. / det;
+  }
+  if (k >= 1 && k < mz - 1 && j >= 1 && j < my - 1 && i < mx - 1) {
+    double de[3], dz[3];
+    for (int c = 0; c < 3; c++) {
+      de[c] = 0.5 * (CO(i, j, k, c) + CO(i, j, k - 1, c) - CO(i, j - 1, k, c) - CO(i, j - 1, k - 1, c));
+      dz[c] = 0.5 * (CO(i, j - 1, k, c) + CO(i, j, k, c) - CO(i, j - 1, k - 1, c) - CO(i, j, k - 1, c));
+    }
+    double *o = &m.csi[t * 3];
+    o[0] = de[1] * dz[2] - de[2] * dz[1];
+    o[1] = -de[0] * dz[2] + de[2] * dz[0];
+    o[2] = de[0] * dz[1] - de[1] * dz[0];
+  }
+  if (k >= 1 && k < mz - 1 && j < my - 1 && i >= 1 && i < mx - 1) {
+    double dc[3], dz[3];
+    for (int c = 0; c < 3; c++) {
+      dc[c] = 0.5 * (CO(i, j, k, c) + CO(i, j, k - 1, c) - CO(i - 1, j, k, c) - CO(i - 1, j, k - 1, c));
+      dz[c] = 0.5 * (CO(i, j, k, c) + CO(i - 1, j, k, c) - CO(i, j, k - 1, c) - CO(i - 1, j, k - 1, c));
+    }
+    double *o = &m.eta[t * 3];
+    o[0] = dz[1] * dc[2] - dz[2] * dc[1];
+    o[1] = -dz[0] * dc[2] + dz[2] * dc[0];
+    o[2] = dz[0] * dc[1] - dz[1] * dc[0];
+  }
+  if (k < mz - 1 && j >= 1 && j < my - 1 && i >= 1 && i < mx - 1) {
+    double dc[3], de[3];
+    for (int c = 0; c < 3; c++) {
+      dc[c] = 0.5 * (CO(i, j, k, c) + CO(i, j - 1, k, c) - CO(i - 1, j, k, c) - CO(i - 1, j - 1, k, c));
+      de[c] = 0.5 * (CO(i, j, k, c) + CO(i - 1, j, k, c) - CO(i, j - 1, k, c) - CO(i - 1, j - 1, k, c));
+    }
+    double *o = &m.zet[t * 3];
+    o[0] = dc[1] * de[2] - dc[2] * de[1];
+    o[1] = -dc[0] * de[2] + dc[2] * de[0];
+    o[2] = dc[0] * de[1] - dc[1] * de[0];
+  }
+}
+
+// boundary mirror of the cell metrics, one direction per launch, in the
+// order x, y, z of metrics.c:262-342.
+__global__ void k_metrics_mirror(Grid g, MetricPtrs m, int dir) {
+  int u = blockIdx.x * blockDim.x + threadIdx.x, v = blockIdx.y;
+  int nu = dir == 0 ? g.my : g.mx, nv = dir == 2 ? g.my : g.mz;
+  if (u >= nu || v >= nv) return;
+  for (int side = 0; side < 2; side++) {
+    size_t t, s;
+    if (dir == 0) { int i = side ? g.mx - 1 : 0; t = g.at(i, u, v); s = g.at(side ? i - 1 : 1, u, v); }
+    else if (dir == 1) { int j = side ? g.my - 1 : 0; t = g.at(u, j, v); s = g.at(u, side ? j - 1 : 1, v); }
+    else { int k = side ? g.mz - 1 : 0; t = g.at(u, v, k); s = g.at(u, v, side ? k - 1 : 1); }
+    double *A = dir == 0 ? m.eta : m.csi;
+    double *B = dir == 2 ? m.eta : m.zet;
+    for (int c = 0; c < 3; c++) { A[t * 3 + c] = A[s * 3 + c]; B[t * 3 + c] = B[s * 3 + c]; }
+    m.aj[t] = m.aj[s];
+  }
+}
+
+// periodic ghost copy of the cell metrics (metrics.c:360-397).  A source
+// cell has every periodic coordinate inside 1..m-2, so it is never a target.
+__global__ void k_metrics_periodic(Grid g, MetricPtrs m) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y, k = blockIdx.z;
+  if (i >= g.mx) return;
+  int a, b, c, fi, fj, fk;
+  if (!g.remap(i, j, k, a, b, c, fi, fj, fk)) return;
+  size_t s = g.at(a, b, c), t = g.at(i, j, k);
+  for (int q = 0; q < 3; q++) {
+    m.csi[t * 3 + q] = m.csi[s * 3 + q];
+    m.eta[t * 3 + q] = m.eta[s * 3 + q];
+    m.zet[t * 3 + q] = m.zet[s * 3 + q];
+  }
+  m.aj[t] = m.aj[s];
+}
+
+__device__ inline void face_metric_out(const double dc[3], const double de[3], const double dz[3],
+                                       double *ci, double *ei, double *zi, double *aj) {
+  ci[0] = de[1] * dz[2] - de[2] * dz[1];
+  ci[1] = -de[0] * dz[2] + de[2] * dz[0];
+  ci[2] = de[0] * dz[1] - de[1] * dz[0];
+  ei[0] = dz[1] * dc[2] - dz[2] * dc[1];
+  ei[1] = -dz[0] * dc[2] + dz[2] * dc[0];
+  ei[2] = dz[0] * dc[1] - dz[1] * dc[0];
+  zi[0] = dc[1] * de[2] - dc[2] * de[1];
+  zi[1] = -dc[0] * de[2] + dc[2] * de[0];
+  zi[2] = dc[0] * de[1] - dc[1] * de[0];
+  double det = dc[0] * (de[1] * dz[2] - de[2] * dz[1]) - dc[1] * (de[0] * dz[2] - de[2] * dz[0]) +
+               dc[2] * (de[0] * dz[1] - de[1] * dz[0]);
+  *aj = 1. / det;
+}
+
+// face metrics of the i, j and k faces from face-centre differences
+// (metrics.c:478-574, :587-682, :695-790); the face centres are evaluated
+// on the fly in the reference's summation order.
+__global__ void k_metrics_face(Grid g, const double *__restrict__ coor, MetricPtrs m, int dir) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y, k = blockIdx.z;
+  const int mx = g.mx, my = g.my, mz = g.mz;
+  double dc[3], de[3], dz[3];
+  size_t t = g.at(i, j, k);
+  if (dir == 0) {
+    if (!(i < mx - 1 && j >= 1 && j < my - 1 && k >= 1 && k < mz - 1)) return;
+#define CX(i, j, k, c) ((CO(i, j, k, c) + CO(i, j, k - 1, c) + CO(i, j - 1, k, c) + CO(i, j - 1, k - 1, c)) * 0.25)
+    for (int c = 0; c < 3; c++) {
+      if (i == 0) dc[c] = CX(i + 1, j, k, c) - CX(i, j, k, c);
+      else if (i == mx - 2) dc[c] = CX(i, j, k, c) - CX(i - 1, j, k, c);
+      else dc[c] = (CX(i + 1, j, k, c) - CX(i - 1, j, k, c)) * 0.5;
+      if (j == 1) de[c] = CX(i, j + 1, k, c) - CX(i, j, k, c);
+      else if (j == my - 2) de[c] = CX(i, j, k, c) - CX(i, j - 1, k, c);
+      else de[c] = (CX(i, j + 1, k, c) - CX(i, j - 1, k, c)) * 0.5;
+      if (k == 1) dz[c] = (CX(i, j, k + 1, c) - CX(i, j, k, c));
+      else if (k == mz - 2) dz[c] = (CX(i, j, k, c) - CX(i, j, k - 1, c));
+      else dz[c] = (CX(i, j, k + 1, c) - CX(i, j, k - 1, c)) * 0.5;
+    }
+#undef CX
+    face_metric_out(dc, de, dz, &m.icsi[t * 3], &m.ieta[t * 3], &m.izet[t * 3], &m.iaj[t]);
+  } else if (dir == 1) {
+    if (!(i >= 1 && i < mx - 1 && j < my - 1 && k >= 1 && k < mz - 1)) return;
+#define CY(i, j, k, c) ((CO(i, j, k, c) + CO(i, j, k - 1, c) + CO(i - 1, j, k, c) + CO(i - 1, j, k - 1, c)) * 0.25)
+    for (int c = 0; c < 3; c++) {
+      if (i == 1) dc[c] = CY(i + 1, j, k, c) - CY(i, j, k, c);
+      else if (i == mx - 2) dc[c] = CY(i, j, k, c) - CY(i - 1, j, k, c);
+      else dc[c] = (CY(i + 1, j, k, c) - CY(i - 1, j, k, c)) * 0.5;
+      if (j == 0) de[c] = CY(i, j + 1, k, c) - CY(i, j, k, c);
+      else if (j == my - 2) de[c] = CY(i, j, k, c) - CY(i, j - 1, k, c);
+      else de[c] = (CY(i, j + 1, k, c) - CY(i, j - 1, k, c)) * 0.5;
+      if (k == 1) dz[c] = (CY(i, j, k + 1, c) - CY(i, j, k, c));
+      else if (k == mz - 2) dz[c] = (CY(i, j, k, c) - CY(i, j, k - 1, c));
+      else dz[c] = (CY(i, j, k + 1, c) - CY(i, j, k - 1, c)) * 0.5;
+    }
+#undef CY
+    face_metric_out(dc, de, dz, &m.jcsi[t * 3], &m.jeta[t * 3], &m.jzet[t * 3], &m.jaj[t]);
+  } else {
+    if (!(i >= 1 && i < mx - 1 && j >= 1 && j < my - 1 && k < mz - 1)) return;
+#define CZ(i, j, k, c) ((CO(i, j, k, c) + CO(i, j - 1, k, c) + CO(i - 1, j, k, c) + CO(i - 1, j - 1, k, c)) * 0.25)
+    for (int c = 0; c < 3; c++) {
+      if (i == 1) dc[c] = CZ(i + 1, j, k, c) - CZ(i, j, k, c);
+      else if (i == mx - 2) dc[c] = CZ(i, j, k, c) - CZ(i - 1, j, k, c);
+      else dc[c] = (CZ(i + 1, j, k, c) - CZ(i - 1, j, k, c)) * 0.5;
+      if (j == 1) de[c] = CZ(i, j + 1, k, c) - CZ(i, j, k, c);
+      else if (j == my - 2) de[c] = CZ(i, j, k, c) - CZ(i, j - 1, k, c);
+      else de[c] = (CZ(i, j + 1, k, c) - CZ(i, j - 1, k, c)) * 0.5;
+      if (k == 0) dz[c] = (CZ(i, j, k + 1, c) - CZ(i, j, k, c));
+      else if (k == mz - 2) dz[c] = (CZ(i, j, k, c) - CZ(i, j, k - 1, c));
+      else dz[c] = (CZ(i, j, k + 1, c) - CZ(i, j, k - 1, c)) * 0.5;
+    }
+#undef CZ
+    face_metric_out(dc, de, dz, &m.kcsi[t * 3], &m.keta[t * 3], &m.kzet[t * 3], &m.kaj[t]);
+  }
+}
+#undef CO
+
+// --------------------------------------------------------------------------
+// Dof numbering, setup_lidx2 (Source/poisson.c:188-335)
+// --------------------------------------------------------------------------
+__device__ inline bool is_dof_cell(const Grid &g, const double *nvert, int i, int j, int k) {
+  // poisson.c:244-251: interior and (int)nvert <= poisson_threshold
+  if (i <= 0 || i >= g.mx - 1 || j <= 0 || j >= g.my - 1 || k <= 0 || k >= g.mz - 1) return false;
+  return !((int)nvert[g.at(i, j, k)] > kThr);
+}
+// dof test of a possibly-ghost point, with the periodic aliasing of
+// poisson.c:299-332 (Gid of a periodic ghost is its partner's Gid).
+__device__ inline bool has_dof(const Grid &g, const double *nvert, int i, int j, int k) {
+  int a, b, c, fi, fj, fk;
+  g.remap(i, j, k, a, b, c, fi, fj, fk);
+  return is_dof_cell(g, nvert, a, b, c);
+}
+
+// per-block dof counts over the box order (k-j-i, the reference's loop order)
+__global__ void k_count_dofs(Grid g, Box b, const double *nvert, int *block_count) {
+  size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  int f = 0;
+  if (c < b.n()) {
+    int i = c % b.nx, j = (c / b.nx) % b.ny, k = c / ((size_t)b.nx * b.ny);
+    f = is_dof_cell(g, nvert, i + 1, j + 1, k + 1) ? 1 : 0;
+  }
+  int s = block_sum<int>(f);
+  if (threadIdx.x == 0) block_count[blockIdx.x] = s;
+}
+// exclusive scan of the block counts by one block (sequential per thread
+// chunk, then a scan over the 1024 chunk totals).
+__global__ void k_scan_blocks(int *block_count, int nblocks, int *total) {
+  __shared__ int part[1024];
+  int per = (nblocks + blockDim.x - 1) / blockDim.x;
+  int lo = threadIdx.x * per, hi = min(nblocks, lo + per);
+  int s = 0;
+  for (int q = lo; q < hi; q++) s += block_count[q];
+  part[threadIdx.x] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int run = 0;
+    for (int q = 0; q < (int)blockDim.x; q++) { int v = part[q]; part[q] = run; run += v; }
+    *total = run;
+  }
+  __syncthreads();
+  int run = part[threadIdx.x];
+  for (int q = lo; q < hi; q++) { int v = block_count[q]; block_count[q] = run; run += v; }
+}
+__global__ void k_number_dofs(Grid g, Box b, const double *nvert, const int *block_off, int *gid_box) {
+  __shared__ int warp_tot[32];
+  size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  int f = 0;
+  if (c < b.n()) {
+    int i = c % b.nx, j = (c / b.nx) % b.ny, k = c / ((size_t)b.nx * b.ny);
+    f = is_dof_cell(g, nvert, i + 1, j + 1, k + 1) ? 1 : 0;
+  }
+  int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  unsigned bal = __ballot_sync(0xffffffffu, f);
+  int pre = __popc(bal & ((1u << lane) - 1u));
+  if (lane == 0) warp_tot[w] = __popc(bal);
+  __syncthreads();
+  int off = 0;
+  for (int q = 0; q < w; q++) off += warp_tot[q];
+  if (c < b.n()) gid_box[c] = f ? block_off[blockIdx.x] + off + pre : -1;
+}
+// DA-layout Gid with periodic ghost aliasing.
+__global__ void k_gid_da(Grid g, Box b, const int *gid_box, int *gid_da) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y, k = blockIdx.z;
+  if (i >= g.mx) return;
+  int a, bb, c, fi, fj, fk;
+  g.remap(i, j, k, a, bb, c, fi, fj, fk);
+  int v = -1;
+  if (a >= 1 && a < g.mx - 1 && bb >= 1 && bb < g.my - 1 && c >= 1 && c < g.mz - 1)
+    v = gid_box[b.at(a - 1, bb - 1, c - 1)];
+  gid_da[g.at(i, j, k)] = v;
+}
+
+// --------------------------------------------------------------------------
+// PoissonLHSNew (Source/poisson.c:977-1688), level set off (r = 1)
+// --------------------------------------------------------------------------
+// g11..g33 at a face with the periodic source remap of poisson.c:1102-1138
+__device__ inline double gface(const Grid &g, const MetricPtrs &m, int q, int i, int j, int k) {
+  int a, b, c, fi, fj, fk;
+  g.remap(i, j, k, a, b, c, fi, fj, fk);
+  size_t s = g.at(a, b, c);
+  const double *X, *Y, *AJ;
+  switch (q) {
+    case 0: X = m.icsi; Y = m.icsi; AJ = m.iaj; break;
+    case 1: X = m.ieta; Y = m.icsi; AJ = m.iaj; break;
+    case 2: X = m.izet; Y = m.icsi; AJ = m.iaj; break;
+    case 3: X = m.jcsi; Y = m.jeta; AJ = m.jaj; break;
+    case 4: X = m.jeta; Y = m.jeta; AJ = m.jaj; break;
+    case 5: X = m.jzet; Y = m.jeta; AJ = m.jaj; break;
+    case 6: X = m.kcsi; Y = m.kzet; AJ = m.kaj; break;
+    case 7: X = m.keta; Y = m.kzet; AJ = m.kaj; break;
+    default: X = m.kzet; Y = m.kzet; AJ = m.kaj; break;
+  }
+  return (X[s * 3] * Y[s * 3] + X[s * 3 + 1] * Y[s * 3 + 1] + X[s * 3 + 2] * Y[s * 3 + 2]) * AJ[s];
+}
+
+// One row of the operator, accumulated in the reference's statement order.
+__device__ void assemble_row(const Grid &g, const double *nvert, const MetricPtrs &m, int i, int j, int k,
+                             double v[NSLOT]) {
+  const int mx = g.mx, my = g.my, mz = g.mz;
+  const bool ip = g.px, jp = g.py, kp = g.pz;
+  const double thr = kThr, r = 1.0;
+#define NV(a, b, c) nvert[g.at(a, b, c)]
+#define G(q, a, b, c) gface(g, m, q, a, b, c)
+  for (int s = 0; s < NSLOT; s++) v[s] = 0.;
+  if (NV(i + 1, j, k) < thr && (i != mx - 2 || ip)) {  // poisson.c:1167-1230
+    double g0 = G(0, i, j, k), g1 = G(1, i, j, k), g2 = G(2, i, j, k);
+    v[CP] -= g0 / r; v[EP] += g0 / r;
+    if ((j == my - 2 && !jp) || NV(i, j + 1, k) + NV(i + 1, j + 1, k) > thr) {
+      if (NV(i, j - 1, k) + NV(i + 1, j - 1, k) < thr && j != 1) {
+        v[CP] += g1 * 0.5 / r; v[EP] += g1 * 0.5 / r; v[SP] -= g1 * 0.5 / r; v[SE] -= g1 * 0.5 / r;
+      }
+    } else if ((j == 1 && !jp) || NV(i, j - 1, k) + NV(i + 1, j - 1, k) > thr) {
+      if (NV(i, j + 1, k) + NV(i + 1, j + 1, k) < thr) {
+        v[NP] += g1 * 0.5 / r; v[NE] += g1 * 0.5 / r; v[CP] -= g1 * 0.5 / r; v[EP] -= g1 * 0.5 / r;
+      }
+    } else {
+      v[NP] += g1 * 0.25 / r; v[NE] += g1 * 0.25 / r; v[SP] -= g1 * 0.25 / r; v[SE] -= g1 * 0.25 / r;
+    }
+    if ((k == mz - 2 && !kp) || NV(i, j, k + 1) + NV(i + 1, j, k + 1) > thr) {
+      if (NV(i, j, k - 1) + NV(i + 1, j, k - 1) < thr && k != 1) {
+        v[CP] += g2 * 0.5 / r; v[EP] += g2 * 0.5 / r; v[BP] -= g2 * 0.5 / r; v[BE] -= g2 * 0.5 / r;
+      }
+    } else if ((k == 1 && !kp) || NV(i, j, k - 1) + NV(i + 1, j, k - 1) > thr) {
+      if (NV(i, j, k + 1) + NV(i + 1, j, k + 1) < thr) {
+        v[TP] += g2 * 0.5 / r; v[TE] += g2 * 0.5 / r; v[CP] -= g2 * 0.5 / r; v[EP] -= g2 * 0.5 / r;
+      }
+    } else {
+      v[TP] += g2 * 0.25 / r; v[TE] += g2 * 0.25 / r; v[BP] -= g2 * 0.25 / r; v[BE] -= g2 * 0.25 / r;
+    }
+  }
+  if (NV(i - 1, j, k) < thr && (i != 1 || ip)) {  // poisson.c:1233-1293
+    double g0 = G(0, i - 1, j, k), g1 = G(1, i - 1, j, k), g2 = G(2, i - 1, j, k);
+    v[CP] -= g0 / r; v[WP] += g0 / r;
+    if ((j == my - 2 && !jp) || NV(i, j + 1, k) + NV(i - 1, j + 1, k) > thr) {
+      if (NV(i, j - 1, k) + NV(i - 1, j - 1, k) < thr && j != 1) {
+        v[CP] -= g1 * 0.5 / r; v[WP] -= g1 * 0.5 / r; v[SP] += g1 * 0.5 / r; v[SW] += g1 * 0.5 / r;
+      }
+    } else if ((j == 1 && !jp) || NV(i, j - 1, k) + NV(i - 1, j - 1, k) > thr) {
+      if (NV(i, j + 1, k) + NV(i - 1, j + 1, k) < thr) {
+        v[NP] -= g1 * 0.5 / r; v[NW] -= g1 * 0.5 / r; v[CP] += g1 * 0.5 / r; v[WP] += g1 * 0.5 / r;
+      }
+    } else {
+      v[NP] -= g1 * 0.25 / r; v[NW] -= g1 * 0.25 / r; v[SP] += g1 * 0.25 / r; v[SW] += g1 * 0.25 / r;
+    }
+    if ((k == mz - 2 && !kp) || NV(i, j, k + 1) + NV(i - 1, j, k + 1) > thr) {
+      if (NV(i, j, k - 1) + NV(i - 1, j, k - 1) < thr && k != 1) {
+        v[CP] -= g2 * 0.5 / r; v[WP] -= g2 * 0.5 / r; v[BP] += g2 * 0.5 / r; v[BW] += g2 * 0.5 / r;
+      }
+    } else if ((k == 1 && !kp) || NV(i, j, k - 1) + NV(i - 1, j, k - 1) > thr) {
+      if (NV(i, j, k + 1) + NV(i - 1, j, k + 1) < thr) {
+        v[TP] -= g2 * 0.5 / r; v[TW] -= g2 * 0.5 / r; v[CP] += g2 * 0.5 / r; v[WP] += g2 * 0.5 / r;
+      }
+    } else {
+      v[TP] -= g2 * 0.25 / r; v[TW] -= g2 * 0.25 / r; v[BP] += g2 * 0.25 / r; v[BW] += g2 * 0.25 / r;
+    }
+  }
+  if (NV(i, j + 1, k) < thr && (j != my - 2 || jp)) {  // poisson.c:1296-1361
+    double g3 = G(3, i, j, k), g4 = G(4, i, j, k), g5 = G(5, i, j, k);
+    if ((i == mx - 2 && !ip) || NV(i + 1, j, k) + NV(i + 1, j + 1, k) > thr) {
+      if (NV(i - 1, j, k) + NV(i - 1, j + 1, k) < thr && i != 1) {
+        v[CP] += g3 * 0.5 / r; v[NP] += g3 * 0.5 / r; v[WP] -= g3 * 0.5 / r; v[NW] -= g3 * 0.5 / r;
+      }
+    } else if ((i == 1 && !ip) || NV(i - 1, j, k) + NV(i - 1, j + 1, k) > thr) {
+      if (NV(i + 1, j, k) + NV(i + 1, j + 1, k) < thr) {
+        v[EP] += g3 * 0.5 / r; v[NE] += g3 * 0.5 / r; v[CP] -= g3 * 0.5 / r; v[NP] -= g3 * 0.5 / r;
+      }
+    } else {
+      v[EP] += g3 * 0.25 / r; v[NE] += g3 * 0.25 / r; v[WP] -= g3 * 0.25 / r; v[NW] -= g3 * 0.25 / r;
+    }
+    v[CP] -= g4 / r; v[NP] += g4 / r;
+    if ((k == mz - 2 && !kp) || NV(i, j, k + 1) + NV(i, j + 1, k + 1) > thr) {
+      if (NV(i, j, k - 1) + NV(i, j + 1, k - 1) < thr && k != 1) {
+        v[CP] += g5 * 0.5 / r; v[NP] += g5 * 0.5 / r; v[BP] -= g5 * 0.5 / r; v[BN] -= g5 * 0.5 / r;
+      }
+    } else if ((k == 1 && !kp) || NV(i, j, k - 1) + NV(i, j + 1, k - 1) > thr) {
+      if (NV(i, j, k + 1) + NV(i, j + 1, k + 1) < thr) {
+        v[TP] += g5 * 0.5 / r; v[TN] += g5 * 0.5 / r; v[CP] -= g5 * 0.5 / r; v[NP] -= g5 * 0.5 / r;
+      }
+    } else {
+      v[TP] += g5 * 0.25 / r; v[TN] += g5 * 0.25 / r; v[BP] -= g5 * 0.25 / r; v[BN] -= g5 * 0.25 / r;
+    }
+  }
+  if (NV(i, j - 1, k) < thr && (j != 1 || jp)) {  // poisson.c:1364-1422
+    double g3 = G(3, i, j - 1, k), g4 = G(4, i, j - 1, k), g5 = G(5, i, j - 1, k);
+    if ((i == mx - 2 && !ip) || NV(i + 1, j, k) + NV(i + 1, j - 1, k) > thr) {
+      if (NV(i - 1, j, k) + NV(i - 1, j - 1, k) < thr && i != 1) {
+        v[CP] -= g3 * 0.5 / r; v[SP] -= g3 * 0.5 / r; v[WP] += g3 * 0.5 / r; v[SW] += g3 * 0.5 / r;
+      }
+    } else if ((i == 1 && !ip) || NV(i - 1, j, k) + NV(i - 1, j - 1, k) > thr) {
+      if (NV(i + 1, j, k) + NV(i + 1, j - 1, k) < thr) {
+        v[EP] -= g3 * 0.5 / r; v[SE] -= g3 * 0.5 / r; v[CP] += g3 * 0.5 / r; v[SP] += g3 * 0.5 / r;
+      }
+    } else {
+      v[EP] -= g3 * 0.25 / r; v[SE] -= g3 * 0.25 / r; v[WP] += g3 * 0.25 / r; v[SW] += g3 * 0.25 / r;
+    }
+    v[CP] -= g4 / r; v[SP] += g4 / r;
+    if ((k == mz - 2 && !kp) || NV(i, j, k + 1) + NV(i, j - 1, k + 1) > thr) {
+      if (NV(i, j, k - 1) + NV(i, j - 1, k - 1) < thr && k != 1) {
+        v[CP] -= g5 * 0.5 / r; v[SP] -= g5 * 0.5 / r; v[BP] += g5 * 0.5 / r; v[BS] += g5 * 0.5 / r;
+      }
+    } else if ((k == 1 && !kp) || NV(i, j, k - 1) + NV(i, j - 1, k - 1) > thr) {
+      if (NV(i, j, k + 1) + NV(i, j - 1, k + 1) < thr) {
+        v[TP] -= g5 * 0.5 / r; v[TS] -= g5 * 0.5 / r; v[CP] += g5 * 0.5 / r; v[SP] += g5 * 0.5 / r;
+      }
+    } else {
+      v[TP] -= g5 * 0.25 / r; v[TS] -= g5 * 0.25 / r; v[BP] += g5 * 0.25 / r; v[BS] += g5 * 0.25 / r;
+    }
+  }
+  if (NV(i, j, k + 1) < thr && (k != mz - 2 || kp)) {  // poisson.c:1425-1491
+    double g6 = G(6, i, j, k), g7 = G(7, i, j, k), g8 = G(8, i, j, k);
+    if ((i == mx - 2 && !ip) || NV(i + 1, j, k) + NV(i + 1, j, k + 1) > thr) {
+      if (NV(i - 1, j, k) + NV(i - 1, j, k + 1) < thr && i != 1) {
+        v[CP] += g6 * 0.5 / r; v[TP] += g6 * 0.5 / r; v[WP] -= g6 * 0.5 / r; v[TW] -= g6 * 0.5 / r;
+      }
+    } else if ((i == 1 && !ip) || NV(i - 1, j, k) + NV(i - 1, j, k + 1) > thr) {
+      if (NV(i + 1, j, k) + NV(i + 1, j, k + 1) < thr) {
+        v[EP] += g6 * 0.5 / r; v[TE] += g6 * 0.5 / r; v[CP] -= g6 * 0.5 / r; v[TP] -= g6 * 0.5 / r;
+      }
+    } else {
+      v[EP] += g6 * 0.25 / r; v[TE] += g6 * 0.25 / r; v[WP] -= g6 * 0.25 / r; v[TW] -= g6 * 0.25 / r;
+    }
+    if ((j == my - 2 && !jp) || NV(i, j + 1, k) + NV(i, j + 1, k + 1) > thr) {
+      if (NV(i, j - 1, k) + NV(i, j - 1, k + 1) < thr && j != 1) {
+        v[CP] += g7 * 0.5 / r; v[TP] += g7 * 0.5 / r; v[SP] -= g7 * 0.5 / r; v[TS] -= g7 * 0.5 / r;
+      }
+    } else if ((j == 1 && !jp) || NV(i, j - 1, k) + NV(i, j - 1, k + 1) > thr) {
+      if (NV(i, j + 1, k) + NV(i, j + 1, k + 1) < thr) {
+        v[NP] += g7 * 0.5 / r; v[TN] += g7 * 0.5 / r; v[CP] -= g7 * 0.5 / r; v[TP] -= g7 * 0.5 / r;
+      }
+    } else {
+      v[NP] += g7 * 0.25 / r; v[TN] += g7 * 0.25 / r; v[SP] -= g7 * 0.25 / r; v[TS] -= g7 * 0.25 / r;
+    }
+    v[CP] -= g8 / r; v[TP] += g8 / r;
+  }
+  if (NV(i, j, k - 1) < thr && (k != 1 || kp)) {  // poisson.c:1494-1561
+    double g6 = G(6, i, j, k - 1), g7 = G(7, i, j, k - 1), g8 = G(8, i, j, k - 1);
+    if ((i == mx - 2 && !ip) || NV(i + 1, j, k) + NV(i + 1, j, k - 1) > thr) {
+      if (NV(i - 1, j, k) + NV(i - 1, j, k - 1) < thr && i != 1) {
+        v[CP] -= g6 * 0.5 / r; v[BP] -= g6 * 0.5 / r; v[WP] += g6 * 0.5 / r; v[BW] += g6 * 0.5 / r;
+      }
+    } else if ((i == 1 && !ip) || NV(i - 1, j, k) + NV(i - 1, j, k - 1) > thr) {
+      if (NV(i + 1, j, k) + NV(i + 1, j, k - 1) < thr) {
+        v[EP] -= g6 * 0.5 / r; v[BE] -= g6 * 0.5 / r; v[CP] += g6 * 0.5 / r; v[BP] += g6 * 0.5 / r;
+      }
+    } else {
+      v[EP] -= g6 * 0.25 / r; v[BE] -= g6 * 0.25 / r; v[WP] += g6 * 0.25 / r; v[BW] += g6 * 0.25 / r;
+    }
+    if ((j == my - 2 && !jp) || NV(i, j + 1, k) + NV(i, j + 1, k - 1) > thr) {
+      if (NV(i, j - 1, k) + NV(i, j - 1, k - 1) < thr && j != 1) {
+        v[CP] -= g7 * 0.5 / r; v[BP] -= g7 * 0.5 / r; v[SP] += g7 * 0.5 / r; v[BS] += g7 * 0.5 / r;
+      }
+    } else if ((j == 1 && !jp) || NV(i, j - 1, k) + NV(i, j - 1, k - 1) > thr) {
+      if (NV(i, j + 1, k) + NV(i, j + 1, k - 1) < thr) {
+        v[NP] -= g7 * 0.5 / r; v[BN] -= g7 * 0.5 / r; v[CP] += g7 * 0.5 / r; v[BP] += g7 * 0.5 / r;
+      }
+    } else {
+      v[NP] -= g7 * 0.25 / r; v[BN] -= g7 * 0.25 / r; v[SP] += g7 * 0.25 / r; v[BS] += g7 * 0.25 / r;
+    }
+    v[CP] -= g8 / r; v[BP] += g8 / r;
+  }
+#undef NV
+#undef G
+}
+
+// Assemble one level's operator into 19 box-layout planes.  filter: the
+// reference's insertion test |v| > 1e-10 (poisson.c:1610-1614); scale: the
+// aj row scaling of the poisson == -1 path (poisson.c:1563), used for the
+// multigrid levels.  Slots whose column has no dof are zero (idx < 0).
+__global__ void k_assemble(Grid g, Box b, const double *__restrict__ nvert, MetricPtrs m, int scale,
+                           int filter, double *A, uint8_t *rowtype) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y, k = blockIdx.z;
+  if (i >= b.nx) return;
+  const size_t c = b.at(i, j, k), n = b.n();
+  const int I = i + 1, J = j + 1, K = k + 1;
+  const size_t t = g.at(I, J, K);
+  const bool dof = is_dof_cell(g, nvert, I, J, K);
+  if (nvert[t] > 0.1 && dof) {  // identity row, poisson.c:1158-1160
+    for (int s = 0; s < NSLOT; s++) A[s * n + c] = s == CP ? 1.0 : 0.0;
+    rowtype[c] = 2;
+    return;
+  }
+  if (nvert[t] > kThr) {
+    for (int s = 0; s < NSLOT; s++) A[s * n + c] = 0.0;
+    rowtype[c] = 0;
+    return;
+  }
+  double v[NSLOT];
+  assemble_row(g, nvert, m, I, J, K, v);
+  if (scale) {
+    double a = m.aj[t];
+    for (int s = 0; s < NSLOT; s++) v[s] *= a;
+  }
+  for (int s = 0; s < NSLOT; s++) {
+    int di, dj, dk;
+    slot_offset(s, di, dj, dk);
+    bool keep = s == CP || (has_dof(g, nvert, I + di, J + dj, K + dk) && (!filter || fabs(v[s]) > 1.e-10));
+    A[s * n + c] = keep ? v[s] : 0.0;
+  }
+  rowtype[c] = 1;
+}
+
+// Per-face dot products S = a.b of the projection and the face aj, so that
+// Projection can form (dpdc*S)*aj exactly as poisson.c:2828-2950 does.
+__global__ void k_projection_coef(Grid g, Box b, MetricPtrs m, double *pc) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y, k = blockIdx.z;
+  if (i >= b.nx) return;
+  size_t c = b.at(i, j, k), n = b.n(), s = g.at(i + 1, j + 1, k + 1);
+#define DOT(A, B) (m.A[s * 3] * m.B[s * 3] + m.A[s * 3 + 1] * m.B[s * 3 + 1] + m.A[s * 3 + 2] * m.B[s * 3 + 2])
+  pc[0 * n + c] = DOT(icsi, icsi); pc[1 * n + c] = DOT(ieta, icsi); pc[2 * n + c] = DOT(izet, icsi);
+  pc[3 * n + c] = m.iaj[s];
+  pc[4 * n + c] = DOT(jcsi, jeta); pc[5 * n + c] = DOT(jeta, jeta); pc[6 * n + c] = DOT(jzet, jeta);
+  pc[7 * n + c] = m.jaj[s];
+  pc[8 * n + c] = DOT(kcsi, kzet); pc[9 * n + c] = DOT(keta, kzet); pc[10 * n + c] = DOT(kzet, kzet);
+  pc[11 * n + c] = m.kaj[s];
+#undef DOT
+}
+
+// Box-layout masks of a level: row-active flag from the assembly, blanking
+// (nvert > 0.1) and the restriction weight max(0, 1 - nvert)
+// (MyRestriction, poisson.c:433-441), in both precisions.
+__global__ void k_level_masks(Grid g, Box b, const double *nvert, uint8_t *blank, double *w64, float *w32,
+                              double *aj_box, const double *aj_da) {
+  size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= b.n()) return;
+  int i = c % b.nx, j = (c / b.nx) % b.ny, k = c / ((size_t)b.nx * b.ny);
+  double nv = nvert[g.at(i + 1, j + 1, k + 1)];
+  blank[c] = nv > 0.1 ? 1 : 0;
+  double w = 1 - nv > 0. ? 1 - nv : 0.;
+  w64[c] = w;
+  w32[c] = (float)w;
+  if (aj_box) aj_box[c] = aj_da[g.at(i + 1, j + 1, k + 1)];
+}
+
+// --------------------------------------------------------------------------
+// Right-hand side: PoissonRHS2_hypre (Source/poisson_hypre.c:265-407) and
+// Remove_Nullspace_Scale (:118-200)
+// --------------------------------------------------------------------------
+__global__ void k_rhs(Grid g, Box b, const double *__restrict__ nvert, const double *__restrict__ ucont,
+                      const double *__restrict__ aj, double dt, double st, double coeff, double *rhs,
+                      double *partial) {
+  double sb = 0, sa = 0;
+  const size_t n = b.n();
+  for (size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (size_t)gridDim.x * blockDim.x) {
+    int i = c % b.nx + 1, j = (c / b.nx) % b.ny + 1, k = c / ((size_t)b.nx * b.ny) + 1;
+    size_t t = g.at(i, j, k);
+    double val = 0.;
+    if (nvert[t] < 0.1) {
+#define U(a, bb, cc, q) ucont[g.at(a, bb, cc) * 3 + (q)]
+      val -= U(i, j, k, 0);
+      if (i == 1 && g.px) val += U(g.mx - 2, j, k, 0);
+      else val += U(i - 1, j, k, 0);
+      val -= U(i, j, k, 1);
+      if (j == 1 && g.py) val += U(i, g.my - 2, k, 1);
+      else val += U(i, j - 1, k, 1);
+      val -= U(i, j, k, 2);
+      if (k == 1 && g.pz) val += U(i, j, g.mz - 2, 2);
+      else val += U(i, j, k - 1, 2);
+#undef U
+      val *= -1.0 / dt * st * coeff;
+      sb += val;
+      sa += aj[t];
+    }
+    rhs[c] = val;
+  }
+  double tb = block_sum(sb);
+  double ta = block_sum(sa);
+  if (threadIdx.x == 0) { partial[blockIdx.x] = tb; partial[gridDim.x + blockIdx.x] = ta; }
+}
+
+// sums `nrow` rows of `nb` block partials each, in a fixed tree order
+__global__ void k_reduce_rows(const double *partial, int nb, int nrow, double *out) {
+  for (int r = 0; r < nrow; r++) {
+    double s = 0;
+    for (int q = threadIdx.x; q < nb; q += blockDim.x) s += partial[(size_t)r * nb + q];
+    s = block_sum(s);
+    if (threadIdx.x == 0) out[r] = s;
+    __syncthreads();
+  }
+}
+
+__global__ void k_rhs_nullspace(Grid g, Box b, const double *__restrict__ nvert, const double *__restrict__ aj,
+                                const double *sums, double *rhs) {
+  const double sum = sums[0], sum_aj = sums[1];
+  const size_t n = b.n();
+  for (size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (size_t)gridDim.x * blockDim.x) {
+    int i = c % b.nx + 1, j = (c / b.nx) % b.ny + 1, k = c / ((size_t)b.nx * b.ny) + 1;
+    size_t t = g.at(i, j, k);
+    if (nvert[t] < 0.1) {
+      double val = -sum * aj[t] / sum_aj;
+      rhs[c] += val;
+    }
+  }
+}
+
+// Remove_Nullspace (Source/poisson_hypre.c:202-263) on a box vector: sum and
+// count over nvert < 0.1
+__global__ void k_mean_partial(Box b, const uint8_t *fluid, const double *x, double *partial) {
+  double s = 0, cnt = 0;
+  const size_t n = b.n();
+  for (size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (size_t)gridDim.x * blockDim.x)
+    if (fluid[c]) { s += x[c]; cnt += 1.0; }
+  double ts = block_sum(s);
+  double tc = block_sum(cnt);
+  if (threadIdx.x == 0) { partial[blockIdx.x] = ts; partial[gridDim.x + blockIdx.x] = tc; }
+}
+__global__ void k_shift_fluid(Box b, const uint8_t *fluid, const double *sums, double *x) {
+  const double val = -sums[0] / sums[1];
+  const size_t n = b.n();
+  for (size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (size_t)gridDim.x * blockDim.x)
+    if (fluid[c]) x[c] += val;
+}
+__global__ void k_fluid_mask(Grid g, Box b, const double *nvert, uint8_t *fluid) {
+  size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= b.n()) return;
+  int i = c % b.nx + 1, j = (c / b.nx) % b.ny + 1, k = c / ((size_t)b.nx * b.ny) + 1;
+  fluid[c] = nvert[g.at(i, j, k)] < 0.1 ? 1 : 0;
+}
+
+// Convert_Phi2_Phi (Source/poisson.c:98-186): box phi -> DA phi, zero on
+// non-dof cells and non-periodic ghosts, partner values on periodic ghosts.
+__global__ void k_box_to_da_phi(Grid g, Box b, const double *nvert, const double *x, double *phi) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y, k = blockIdx.z;
+  if (i >= g.mx) return;
+  int a, bb, c, fi, fj, fk;
+  g.remap(i, j, k, a, bb, c, fi, fj, fk);
+  double v = 0.;
+  if (a >= 1 && a < g.mx - 1 && bb >= 1 && bb < g.my - 1 && c >= 1 && c < g.mz - 1)
+    if (!((int)nvert[g.at(a, bb, c)] > kThr)) v = x[b.at(a - 1, bb - 1, c - 1)];
+  phi[g.at(i, j, k)] = v;
+}
+// DA -> box copy of the interior (warm start / inspection input)
+__global__ void k_da_to_box(Grid g, Box b, const double *da, double *x) {
+  size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= b.n()) return;
+  int i = c % b.nx + 1, j = (c / b.nx) % b.ny + 1, k = c / ((size_t)b.nx * b.ny) + 1;
+  x[c] = da[g.at(i, j, k)];
+}
+__global__ void k_box_to_da(Grid g, Box b, const double *x, double *da) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y, k = blockIdx.z;
+  if (i >= g.mx) return;
+  double v = 0.;
+  if (i >= 1 && i < g.mx - 1 && j >= 1 && j < g.my - 1 && k >= 1 && k < g.mz - 1)
+    v = x[b.at(i - 1, j - 1, k - 1)];
+  da[g.at(i, j, k)] = v;
+}
+
+// UpdatePressure (Source/poisson.c:3137-3297): interior update, then the
+// periodic ghost copies of p and phi in a second launch.
+__global__ void k_update_pressure(Grid g, const double *nvert, const double *phi, double *p) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y, k = blockIdx.z;
+  if (i < 1 || i >= g.mx - 1 || j < 1 || j >= g.my - 1 || k < 1 || k >= g.mz - 1) return;
+  size_t t = g.at(i, j, k);
+  if (nvert[t] < 0.1) p[t] += phi[t];
+  if (nvert[t] > 1.1) p[t] = 0;
+}
+__global__ void k_periodic_copy2(Grid g, double *p, double *phi) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y, k = blockIdx.z;
+  if (i >= g.mx) return;
+  int a, b, c, fi, fj, fk;
+  if (!g.remap(i, j, k, a, b, c, fi, fj, fk)) return;
+  size_t s = g.at(a, b, c), t = g.at(i, j, k);
+  p[t] = p[s];
+  if (phi) phi[t] = phi[s];
+}
+
+// Projection (Source/poisson.c:2700-3066), level set off.
+__global__ void k_projection(Grid g, Box b, const double *__restrict__ nvert, const double *__restrict__ phi,
+                             const double *__restrict__ pc, double dt, double st, double coeff, double *ucont) {
+  int ii = blockIdx.x * blockDim.x + threadIdx.x, jj = blockIdx.y, kk = blockIdx.z;
+  if (ii >= b.nx) return;
+  const int i = ii + 1, j = jj + 1, k = kk + 1;
+  const int mx = g.mx, my = g.my, mz = g.mz;
+  const bool ip = g.px, jp = g.py, kp = g.pz;
+  const double thr = kThr, r1 = 1.0, r2 = 1.0, r3 = 1.0;
+  const size_t t = g.at(i, j, k), c = b.at(ii, jj, kk), n = b.n();
+#define NV(a, bb, cc) nvert[g.at(a, bb, cc)]
+#define PH(a, bb, cc) phi[g.at(a, bb, cc)]
+  double dpdc, dpde, dpdz;
+  if (i < mx - 2 || (ip && i == mx - 2)) {
+    dpdc = PH(i + 1, j, k) - PH(i, j, k);
+    if (i == mx - 2 && ip) dpdc = PH(1, j, k) - PH(i, j, k);
+    dpde = 0.; dpdz = 0.;
+    if ((j == my - 2 && !jp) || NV(i, j + 1, k) + NV(i + 1, j + 1, k) > thr) {
+      if (NV(i, j - 1, k) + NV(i + 1, j - 1, k) < thr && (j != 1))
+        dpde = (PH(i, j, k) + PH(i + 1, j, k) - PH(i, j - 1, k) - PH(i + 1, j - 1, k)) * 0.5;
+    } else if ((j == 1 && !jp) || NV(i, j - 1, k) + NV(i + 1, j - 1, k) > thr) {
+      if (NV(i, j + 1, k) + NV(i + 1, j + 1, k) < thr)
+        dpde = (PH(i, j + 1, k) + PH(i + 1, j + 1, k) - PH(i, j, k) - PH(i + 1, j, k)) * 0.5;
+    } else {
+      dpde = (PH(i, j + 1, k) + PH(i + 1, j + 1, k) - PH(i, j - 1, k) - PH(i + 1, j - 1, k)) * 0.25;
+    }
+    if ((k == mz - 2 && !kp) || NV(i, j, k + 1) + NV(i + 1, j, k + 1) > thr) {
+      if (NV(i, j, k - 1) + NV(i + 1, j, k - 1) < thr && (k != 1))
+        dpdz = (PH(i, j, k) + PH(i + 1, j, k) - PH(i, j, k - 1) - PH(i + 1, j, k - 1)) * 0.5;
+    } else if ((k == 1 && !kp) || NV(i, j, k - 1) + NV(i + 1, j, k - 1) > thr) {
+      if (NV(i, j, k + 1) + NV(i + 1, j, k + 1) < thr)
+        dpdz = (PH(i, j, k + 1) + PH(i + 1, j, k + 1) - PH(i, j, k) - PH(i + 1, j, k)) * 0.5;
+    } else {
+      dpdz = (PH(i, j, k + 1) + PH(i + 1, j, k + 1) - PH(i, j, k - 1) - PH(i + 1, j, k - 1)) * 0.25;
+    }
+    if ((NV(i, j, k) + NV(i + 1, j, k)) < thr) {
+      const double aj = pc[3 * n + c];
+      ucont[t * 3 + 0] -= (dpdc * pc[0 * n + c] * aj + dpde * pc[1 * n + c] * aj + dpdz * pc[2 * n + c] * aj) *
+                          dt * st / coeff / r1;
+    }
+  }
+  if (j < my - 2 || (jp && j == my - 2)) {
+    dpdc = 0.; dpdz = 0.;
+    if ((i == mx - 2 && !ip) || NV(i + 1, j, k) + NV(i + 1, j + 1, k) > thr) {
+      if (NV(i - 1, j, k) + NV(i - 1, j + 1, k) < thr && (i != 1))
+        dpdc = (PH(i, j, k) + PH(i, j + 1, k) - PH(i - 1, j, k) - PH(i - 1, j + 1, k)) * 0.5;
+    } else if ((i == 1 && !ip) || NV(i - 1, j, k) + NV(i - 1, j + 1, k) > thr) {
+      if (NV(i + 1, j, k) + NV(i + 1, j + 1, k) < thr)
+        dpdc = (PH(i + 1, j, k) + PH(i + 1, j + 1, k) - PH(i, j, k) - PH(i, j + 1, k)) * 0.5;
+    } else {
+      dpdc = (PH(i + 1, j, k) + PH(i + 1, j + 1, k) - PH(i - 1, j, k) - PH(i - 1, j + 1, k)) * 0.25;
+    }
+    if (j == my - 2 && jp) dpde = PH(i, 1, k) - PH(i, j, k);
+    else dpde = PH(i, j + 1, k) - PH(i, j, k);
+    if ((k == mz - 2 && !kp) || NV(i, j, k + 1) + NV(i, j + 1, k + 1) > thr) {
+      if (NV(i, j, k - 1) + NV(i, j + 1, k - 1) < thr && (k != 1))
+        dpdz = (PH(i, j, k) + PH(i, j + 1, k) - PH(i, j, k - 1) - PH(i, j + 1, k - 1)) * 0.5;
+    } else if ((k == 1 && !kp) || NV(i, j, k - 1) + NV(i, j + 1, k - 1) > thr) {
+      if (NV(i, j, k + 1) + NV(i, j + 1, k + 1) < thr)
+        dpdz = (PH(i, j, k + 1) + PH(i, j + 1, k + 1) - PH(i, j, k) - PH(i, j + 1, k)) * 0.5;
+    } else {
+      dpdz = (PH(i, j, k + 1) + PH(i, j + 1, k + 1) - PH(i, j, k - 1) - PH(i, j + 1, k - 1)) * 0.25;
+    }
+    if ((NV(i, j, k) + NV(i, j + 1, k)) < thr || (int)(NV(i, j, k) + NV(i, j + 1, k)) == 5) {
+      const double aj = pc[7 * n + c];
+      ucont[t * 3 + 1] -= (dpdc * pc[4 * n + c] * aj + dpde * pc[5 * n + c] * aj + dpdz * pc[6 * n + c] * aj) *
+                          dt * st / coeff / r2;
+    }
+  }
+  if (k < mz - 2 || (kp && k == mz - 2)) {
+    dpdc = 0.; dpde = 0.;
+    if ((i == mx - 2 && !ip) || NV(i + 1, j, k) + NV(i + 1, j, k + 1) > thr) {
+      if (NV(i - 1, j, k) + NV(i - 1, j, k + 1) < thr && (i != 1))
+        dpdc = (PH(i, j, k) + PH(i, j, k + 1) - PH(i - 1, j, k) - PH(i - 1, j, k + 1)) * 0.5;
+    } else if ((i == 1 && !ip) || NV(i - 1, j, k) + NV(i - 1, j, k + 1) > thr) {
+      if (NV(i + 1, j, k) + NV(i + 1, j, k + 1) < thr)
+        dpdc = (PH(i + 1, j, k) + PH(i + 1, j, k + 1) - PH(i, j, k) - PH(i, j, k + 1)) * 0.5;
+    } else {
+      dpdc = (PH(i + 1, j, k) + PH(i + 1, j, k + 1) - PH(i - 1, j, k) - PH(i - 1, j, k + 1)) * 0.25;
+    }
+    if ((j == my - 2 && !jp) || NV(i, j + 1, k) + NV(i, j + 1, k + 1) > thr) {
+      if (NV(i, j - 1, k) + NV(i, j - 1, k + 1) < thr && (j != 1))
+        dpde = (PH(i, j, k) + PH(i, j, k + 1) - PH(i, j - 1, k) - PH(i, j - 1, k + 1)) * 0.5;
+    } else if ((j == 1 && !jp) || NV(i, j - 1, k) + NV(i, j - 1, k + 1) > thr) {
+      if (NV(i, j + 1, k) + NV(i, j + 1, k + 1) < thr)
+        dpde = (PH(i, j + 1, k) + PH(i, j + 1, k + 1) - PH(i, j, k) - PH(i, j, k + 1)) * 0.5;
+    } else {
+      dpde = (PH(i, j + 1, k) + PH(i, j + 1, k + 1) - PH(i, j - 1, k) - PH(i, j - 1, k + 1)) * 0.25;
+    }
+    if (k == mz - 2 && kp) dpdz = PH(i, j, 1) - PH(i, j, k);
+    else dpdz = PH(i, j, k + 1) - PH(i, j, k);
+    if ((NV(i, j, k) + NV(i, j, k + 1)) < thr) {
+      const double aj = pc[11 * n + c];
+      ucont[t * 3 + 2] -= (dpdc * pc[8 * n + c] * aj + dpde * pc[9 * n + c] * aj + dpdz * pc[10 * n + c] * aj) *
+                          dt * st / coeff / r3;
+    }
+  }
+#undef NV
+#undef PH
+}
+// periodic face copy of Ucont (poisson.c:2996-3036)
+__global__ void k_periodic_faces(Grid g, double *ucont) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y, k = blockIdx.z;
+  if (i >= g.mx) return;
+  int a, b, c, fi, fj, fk;
+  if (!g.remap(i, j, k, a, b, c, fi, fj, fk)) return;
+  size_t s = g.at(a, b, c), t = g.at(i, j, k);
+  if (fi) ucont[t * 3 + 0] = ucont[s * 3 + 0];
+  if (fj) ucont[t * 3 + 1] = ucont[s * 3 + 1];
+  if (fk) ucont[t * 3 + 2] = ucont[s * 3 + 2];
+}
+
+// Divergence (Source/main.c:936-1074): block maxima of |div(Ucont) aj|.
+__global__ void k_divergence(Grid g, Box b, const double *__restrict__ nvert, const double *__restrict__ ucont,
+                             const double *__restrict__ aj, double *partial) {
+  double best = 0.;
+  const size_t n = b.n();
+  for (size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (size_t)gridDim.x * blockDim.x) {
+    int i = c % b.nx + 1, j = (c / b.nx) % b.ny + 1, k = c / ((size_t)b.nx * b.ny) + 1;
+#define U(a, bb, cc, q) ucont[g.at(a, bb, cc) * 3 + (q)]
+#define NV(a, bb, cc) nvert[g.at(a, bb, cc)]
+    double v = fabs((U(i, j, k, 0) - U(i - 1, j, k, 0) + U(i, j, k, 1) - U(i, j - 1, k, 1) + U(i, j, k, 2) -
+                     U(i, j, k - 1, 2)) *
+                    aj[g.at(i, j, k)]);
+    if (NV(i, j, k) + NV(i, j, k + 1) + NV(i, j, k - 1) + NV(i, j + 1, k) + NV(i, j - 1, k) + NV(i + 1, j, k) +
+            NV(i - 1, j, k) >
+        0.1)
+      v = 0.;
+#undef U
+#undef NV
+    best = v > best ? v : best;
+  }
+  double m = block_max(best);
+  if (threadIdx.x == 0) partial[blockIdx.x] = m;
+}
+__global__ void k_reduce_max(const double *partial, int nb, double *out) {
+  double m = 0.;
+  for (int q = threadIdx.x; q < nb; q += blockDim.x) m = partial[q] > m ? partial[q] : m;
+  m = block_max(m);
+  if (threadIdx.x == 0) *out = m;
+}
+
+// --------------------------------------------------------------------------
+// Multigrid hierarchy set-up and transfer operators
+// --------------------------------------------------------------------------
+// coarse nodes are every other fine node (Source/init.c:402-455 with
+// GridRestriction, poisson.c:337-363)
+__global__ void k_coarse_nodes(Grid gf, Grid gc, int cx, int cy, int cz, const double *cf, double *cc) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y, k = blockIdx.z;
+  if (i >= gc.mx) return;
+  size_t t = gc.at(i, j, k);
+  if (i > gc.mx - 2 || j > gc.my - 2 || k > gc.mz - 2) {
+    cc[t * 3] = cc[t * 3 + 1] = cc[t * 3 + 2] = 0.;
+    return;
+  }
+  size_t s = gf.at(cx ? 2 * i : i, cy ? 2 * j : j, cz ? 2 * k : k);
+  cc[t * 3] = cf[s * 3]; cc[t * 3 + 1] = cf[s * 3 + 1]; cc[t * 3 + 2] = cf[s * 3 + 2];
+}
+
+// MyNvertRestriction (poisson.c:1995-2083), first pass: a coarse cell is
+// blanked when the product of its children's nvert exceeds 0.1.
+__global__ void k_nvert_restrict(Grid gh, Grid gc, int cx, int cy, int cz, const double *nh, double *nc) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y, k = blockIdx.z;
+  if (i >= gc.mx) return;
+  size_t t = gc.at(i, j, k);
+  double v = 0.;
+  if (i >= 1 && i < gc.mx - 1 && j >= 1 && j < gc.my - 1 && k >= 1 && k < gc.mz - 1) {
+    const int ia = cx, ja = cy, ka = cz;
+    int ih = cx ? 2 * i : i, jh = cy ? 2 * j : j, kh = cz ? 2 * k : k;
+#define NH(a, b, c) nh[gh.at(a, b, c)]
+    if (NH(ih, jh, kh) * NH(ih - ia, jh, kh) * NH(ih, jh - ja, kh) * NH(ih, jh, kh - ka) * NH(ih - ia, jh - ja, kh) *
+            NH(ih - ia, jh, kh - ka) * NH(ih, jh - ja, kh - ka) * NH(ih - ia, jh - ja, kh - ka) >
+        0.1)
+      v = 1.;
+#undef NH
+  }
+  nc[t] = v;
+}
+// second pass, isolated-cell fill.  The reference updates in place in k-j-i
+// order; a cell is filled only when all six face neighbours are already
+// blanked, so no fluid neighbour can change its decision and a parallel
+// pass over a snapshot gives the same result.
+__global__ void k_nvert_fill(Grid gc, const double *src, double *dst) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y, k = blockIdx.z;
+  if (i >= gc.mx) return;
+  size_t t = gc.at(i, j, k);
+  double v = src[t];
+  if (i >= 1 && i < gc.mx - 1 && j >= 1 && j < gc.my - 1 && k >= 1 && k < gc.mz - 1 && v < 0.1) {
+    if (src[gc.at(i + 1, j, k)] + src[gc.at(i - 1, j, k)] > 1.1 && src[gc.at(i, j + 1, k)] + src[gc.at(i, j - 1, k)] > 1.1 &&
+        src[gc.at(i, j, k + 1)] + src[gc.at(i, j, k - 1)] > 1.1)
+      v = 1.;
+  }
+  dst[t] = v;
+}
+
+// MyRestriction (poisson.c:365-472) on box vectors: the eight weighted
+// children in the reference's order, times 1/8; zero on blanked coarse cells.
+template <typename T>
+__device__ __forceinline__ void restrict_body(Box bf, Box bc, int cx, int cy, int cz, const T *__restrict__ rf,
+                                              const T *__restrict__ wf, const uint8_t *__restrict__ blank_c,
+                                              T *bc_out) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y, k = blockIdx.z;
+  if (i >= bc.nx) return;
+  size_t cc = bc.at(i, j, k);
+  if (blank_c[cc]) { bc_out[cc] = (T)0; return; }
+  int i1 = cx ? 2 * i + 1 : i, j1 = cy ? 2 * j + 1 : j, k1 = cz ? 2 * k + 1 : k;
+  int i0 = i1 - cx, j0 = j1 - cy, k0 = k1 - cz;
+#define X(a, b, c) (rf[bf.at(a, b, c)] * wf[bf.at(a, b, c)])
+  T s = X(i1, j1, k1) + X(i0, j1, k1) + X(i1, j0, k1) + X(i1, j1, k0) + X(i0, j0, k1) + X(i1, j0, k0) +
+        X(i0, j1, k0) + X(i0, j0, k0);
+#undef X
+  bc_out[cc] = (T)0.125 * s;
+}
+
+// MyInterpolation (poisson.c:527-670, GridInterpolation macro :474-507),
+// added onto the fine vector (the V-cycle correction).  add = 0 writes.
+template <typename T>
+__device__ __forceinline__ void prolong_body(Box bf, Box bc, int cx, int cy, int cz, const T *__restrict__ xc,
+                                             const uint8_t *__restrict__ blank_c, const uint8_t *__restrict__ blank_f,
+                                             T *xf, int add) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y, k = blockIdx.z;
+  if (i >= bf.nx) return;
+  size_t c = bf.at(i, j, k);
+  if (blank_f[c]) { if (!add) xf[c] = (T)0; return; }
+  const int I = i + 1, J = j + 1, K = k + 1;
+  const int mx = bf.nx + 2, my = bf.ny + 2, mz = bf.nz + 2;
+  int ic, jc, kc, ia, ja, ka;
+  if (!cx) { ic = I; ia = 0; } else { ic = (I + 1) / 2; ia = (I - 2 * ic) == 0 ? 1 : -1; if (I == 1 || I == mx - 2) ia = 0; }
+  if (!cy) { jc = J; ja = 0; } else { jc = (J + 1) / 2; ja = (J - 2 * jc) == 0 ? 1 : -1; if (J == 1 || J == my - 2) ja = 0; }
+  if (!cz) { kc = K; ka = 0; } else { kc = (K + 1) / 2; ka = (K - 2 * kc) == 0 ? 1 : -1; if (K == 1 || K == mz - 2) ka = 0; }
+#define NC(a, b, cc) blank_c[bc.at((a)-1, (b)-1, (cc)-1)]
+#define XC(a, b, cc) xc[bc.at((a)-1, (b)-1, (cc)-1)]
+  if (ka == -1 && NC(ic, jc, kc - 1)) ka = 0;
+  else if (ka == 1 && NC(ic, jc, kc + 1)) ka = 0;
+  if (ja == -1 && NC(ic, jc - 1, kc)) ja = 0;
+  else if (ja == 1 && NC(ic, jc + 1, kc)) ja = 0;
+  if (ia == -1 && NC(ic - 1, jc, kc)) ia = 0;
+  else if (ia == 1 && NC(ic + 1, jc, kc)) ia = 0;
+  T v = (XC(ic, jc, kc) * (T)9 + XC(ic, jc + ja, kc) * (T)3 + XC(ic + ia, jc, kc) * (T)3 + XC(ic + ia, jc + ja, kc)) *
+            (T)3. / (T)64. +
+        (XC(ic, jc, kc + ka) * (T)9 + XC(ic, jc + ja, kc + ka) * (T)3 + XC(ic + ia, jc, kc + ka) * (T)3 +
+         XC(ic + ia, jc + ja, kc + ka)) /
+            (T)64.;
+#undef NC
+#undef XC
+  if (add) xf[c] += v;
+  else xf[c] = v;
+}
+
+__global__ void k_restrict_f32(Box bf, Box bc, int cx, int cy, int cz, const float *rf, const float *wf,
+                               const uint8_t *blank_c, float *out) {
+  restrict_body<float>(bf, bc, cx, cy, cz, rf, wf, blank_c, out);
+}
+__global__ void k_restrict_f64(Box bf, Box bc, int cx, int cy, int cz, const double *rf, const double *wf,
+                               const uint8_t *blank_c, double *out) {
+  restrict_body<double>(bf, bc, cx, cy, cz, rf, wf, blank_c, out);
+}
+__global__ void k_prolong_f32(Box bf, Box bc, int cx, int cy, int cz, const float *xc, const uint8_t *blank_c,
+                              const uint8_t *blank_f, float *xf, int add) {
+  prolong_body<float>(bf, bc, cx, cy, cz, xc, blank_c, blank_f, xf, add);
+}
+__global__ void k_prolong_f64(Box bf, Box bc, int cx, int cy, int cz, const double *xc, const uint8_t *blank_c,
+                              const uint8_t *blank_f, double *xf, int add) {
+  prolong_body<double>(bf, bc, cx, cy, cz, xc, blank_c, blank_f, xf, add);
+}
+
+}  // namespace vfs

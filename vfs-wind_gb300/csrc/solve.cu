@@ -1,0 +1,264 @@
+// solve.cu -- kernels of the solve loop: operator apply / residual, j-line
+// relaxation, coarsest-level solve and the FP64 Krylov vector kernels.
+//
+// All of them stream box-layout planes (i fastest) with one thread per cell
+// or per j-column, so every warp load is a contiguous 128-byte (FP32) or
+// 256-byte (FP64) segment; the 19-point neighbourhood is re-read through L1.
+#include "common.cuh"
+#include "kernels.cuh"
+
+namespace vfs {
+
+// r = rhs - A x for one level (A holds 19 box-layout planes).
+template <typename T>
+__device__ __forceinline__ void residual_body(Box b, const T *__restrict__ A, const T *__restrict__ x,
+                                                  const T *__restrict__ rhs, T *__restrict__ r) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y, k = blockIdx.z;
+  if (i >= b.nx) return;
+  size_t idx[NSLOT];
+  stencil_index(b, i, j, k, idx);
+  const size_t n = b.n(), c = idx[CP];
+  T s = (T)0;
+#pragma unroll
+  for (int q = 0; q < NSLOT; q++) s += __ldcs(&A[q * n + c]) * __ldg(&x[idx[q]]);
+  r[c] = rhs[c] - s;
+}
+
+// FP64 y = A x on the unscaled operator.
+__global__ void __launch_bounds__(256) k_apply64(Box b, const double *__restrict__ A, const double *__restrict__ x,
+                                                 double *__restrict__ y) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y, k = blockIdx.z;
+  if (i >= b.nx) return;
+  size_t idx[NSLOT];
+  stencil_index(b, i, j, k, idx);
+  const size_t n = b.n(), c = idx[CP];
+  double s = 0.;
+#pragma unroll
+  for (int q = 0; q < NSLOT; q++) s = fma(__ldcs(&A[q * n + c]), __ldg(&x[idx[q]]), s);
+  y[c] = s;
+}
+
+// FP64 r = rhs - A x with the block partial of ||r||^2.
+__global__ void __launch_bounds__(256) k_residual64(Box b, const double *__restrict__ A, const double *__restrict__ x,
+                                                    const double *__restrict__ rhs, double *__restrict__ r,
+                                                    double *partial) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y, k = blockIdx.z;
+  double rr = 0.;
+  if (i < b.nx) {
+    size_t idx[NSLOT];
+    stencil_index(b, i, j, k, idx);
+    const size_t n = b.n(), c = idx[CP];
+    double s = 0.;
+#pragma unroll
+    for (int q = 0; q < NSLOT; q++) s = fma(__ldcs(&A[q * n + c]), __ldg(&x[idx[q]]), s);
+    double v = rhs[c] - s;
+    r[c] = v;
+    rr = v * v;
+  }
+  rr = block_sum(rr);
+  if (threadIdx.x == 0) partial[blockIdx.x + (size_t)gridDim.x * (blockIdx.y + (size_t)gridDim.y * blockIdx.z)] = rr;
+}
+
+// LU factors of the tridiagonal j-line part (S, CP, N slots) of a level
+// operator, computed in FP64 and stored in T.  Rows without a dof get an
+// identity line entry.  The j-periodic wrap couplings stay off the line.
+template <typename T>
+__device__ __forceinline__ void line_lu_body(Box b, const double *__restrict__ A, T *inv, T *cp) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x, k = blockIdx.y;
+  if (i >= b.nx) return;
+  const size_t n = b.n();
+  double cprev = 0.;
+  for (int j = 0; j < b.ny; j++) {
+    size_t c = b.at(i, j, k);
+    double d = A[CP * n + c], a = 0., cc = 0.;
+    if (d != 0.) {
+      a = j > 0 ? A[SP * n + c] : 0.;
+      cc = j < b.ny - 1 ? A[NP * n + c] : 0.;
+    } else {
+      d = 1.;
+    }
+    double iv = 1.0 / (d - a * cprev);
+    inv[c] = (T)iv;
+    cp[c] = (T)(cc * iv);
+    cprev = cc * iv;
+  }
+}
+
+// One damped j-line Jacobi sweep: for each (i,k) column solve the
+// tridiagonal j-line system with the off-line neighbours taken from x, then
+// xo = x + omega (line solution - x).  zero_guess skips the x terms.
+template <typename T>
+__device__ __forceinline__ void line_sweep_body(Box b, const T *__restrict__ A, const T *__restrict__ inv,
+                                                    const T *__restrict__ cp, const T *__restrict__ x,
+                                                    const T *__restrict__ rhs, T *__restrict__ xo, T omega,
+                                                    int zero_guess) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x, k = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= b.nx || k >= b.nz) return;
+  const size_t n = b.n();
+  const int ny = b.ny;
+  const int im = i > 0 ? i - 1 : (b.px ? b.nx - 1 : i), ip = i < b.nx - 1 ? i + 1 : (b.px ? 0 : i);
+  const int km = k > 0 ? k - 1 : (b.pz ? b.nz - 1 : k), kp = k < b.nz - 1 ? k + 1 : (b.pz ? 0 : k);
+  const size_t sj = b.nx;
+  // column bases of the 9 (i,k) neighbours of the line
+  const size_t cC = b.at(i, 0, k), cE = b.at(ip, 0, k), cW = b.at(im, 0, k);
+  const size_t cT = b.at(i, 0, kp), cB = b.at(i, 0, km);
+  const size_t cTE = b.at(ip, 0, kp), cBE = b.at(ip, 0, km), cTW = b.at(im, 0, kp), cBW = b.at(im, 0, km);
+  T yprev = (T)0;
+  for (int j = 0; j < ny; j++) {
+    const size_t o = (size_t)j * sj, c = cC + o;
+    T r = rhs[c];
+    if (!zero_guess) {
+      const size_t om = (size_t)(j > 0 ? j - 1 : (b.py ? ny - 1 : j)) * sj;
+      const size_t op = (size_t)(j < ny - 1 ? j + 1 : (b.py ? 0 : j)) * sj;
+      r -= __ldcs(&A[EP * n + c]) * x[cE + o] + __ldcs(&A[WP * n + c]) * x[cW + o] +
+           __ldcs(&A[TP * n + c]) * x[cT + o] + __ldcs(&A[BP * n + c]) * x[cB + o] +
+           __ldcs(&A[NE * n + c]) * x[cE + op] + __ldcs(&A[SE * n + c]) * x[cE + om] +
+           __ldcs(&A[NW * n + c]) * x[cW + op] + __ldcs(&A[SW * n + c]) * x[cW + om] +
+           __ldcs(&A[TN * n + c]) * x[cT + op] + __ldcs(&A[BN * n + c]) * x[cB + op] +
+           __ldcs(&A[TS * n + c]) * x[cT + om] + __ldcs(&A[BS * n + c]) * x[cB + om] +
+           __ldcs(&A[TE * n + c]) * x[cTE + o] + __ldcs(&A[BE * n + c]) * x[cBE + o] +
+           __ldcs(&A[TW * n + c]) * x[cTW + o] + __ldcs(&A[BW * n + c]) * x[cBW + o];
+      if (b.py) {
+        if (j == 0) r -= A[SP * n + c] * x[cC + (size_t)(ny - 1) * sj];
+        if (j == ny - 1) r -= A[NP * n + c] * x[cC];
+      }
+    }
+    const T a = j > 0 ? __ldcs(&A[SP * n + c]) : (T)0;
+    const T y = (r - a * yprev) * __ldcs(&inv[c]);
+    xo[c] = y;
+    yprev = y;
+  }
+  T xn = (T)0;
+  for (int j = ny - 1; j >= 0; j--) {
+    const size_t c = cC + (size_t)j * sj;
+    const T v = xo[c] - (j < ny - 1 ? __ldcs(&cp[c]) * xn : (T)0);
+    xn = v;
+    const T xold = zero_guess ? (T)0 : x[c];
+    xo[c] = xold + omega * (v - xold);
+  }
+}
+
+// Coarsest level: x = dinv * rhs over the nd dof cells (one block).
+template <typename T>
+__device__ __forceinline__ void coarsest_body(int nd, const int *__restrict__ didx, const double *__restrict__ dinv,
+                           const T *__restrict__ rhs, T *x, size_t n) {
+  __shared__ double sb[1024];
+  for (size_t c = threadIdx.x; c < n; c += blockDim.x) x[c] = (T)0;
+  for (int q = threadIdx.x; q < nd; q += blockDim.x) sb[q] = (double)rhs[didx[q]];
+  __syncthreads();
+  for (int r = threadIdx.x; r < nd; r += blockDim.x) {
+    double s = 0.;
+    for (int q = 0; q < nd; q++) s += dinv[(size_t)r * nd + q] * sb[q];
+    x[didx[r]] = (T)s;
+  }
+}
+
+template <typename T>
+__device__ __forceinline__ void cast_body(const double *__restrict__ src, T *__restrict__ dst, size_t n) {
+  for (size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (size_t)gridDim.x * blockDim.x)
+    dst[c] = (T)src[c];
+}
+
+// ---- FP64 Krylov kernels (fixed grid, deterministic block partials) ----
+#define KTILE 8
+// partial[v * gridDim.x + block] = sum over the block's cells of V_v . w,
+// and row nv holds w . w.  Each thread keeps its KTILE values of w in
+// registers while the basis vectors stream past.
+__global__ void __launch_bounds__(256) k_dots(size_t n, int nv, const double *const *__restrict__ V,
+                                              const double *__restrict__ w, double *partial) {
+  const size_t base = (size_t)blockIdx.x * blockDim.x * KTILE + threadIdx.x;
+  double wr[KTILE];
+#pragma unroll
+  for (int q = 0; q < KTILE; q++) {
+    size_t c = base + (size_t)q * blockDim.x;
+    wr[q] = c < n ? w[c] : 0.;
+  }
+  for (int v = 0; v <= nv; v++) {
+    double s = 0.;
+    if (v < nv) {
+      const double *p = V[v];
+#pragma unroll
+      for (int q = 0; q < KTILE; q++) {
+        size_t c = base + (size_t)q * blockDim.x;
+        if (c < n) s = fma(wr[q], __ldcs(&p[c]), s);
+      }
+    } else {
+#pragma unroll
+      for (int q = 0; q < KTILE; q++) s = fma(wr[q], wr[q], s);
+    }
+    s = block_sum(s);
+    if (threadIdx.x == 0) partial[(size_t)v * gridDim.x + blockIdx.x] = s;
+  }
+}
+
+// w -= sum_v coef[v] V_v, with the block partial of ||w||^2.
+__global__ void __launch_bounds__(256) k_gs_update(size_t n, int nv, const double *const *__restrict__ V,
+                                                   const double *__restrict__ coef, double *__restrict__ w,
+                                                   double *partial) {
+  const size_t base = (size_t)blockIdx.x * blockDim.x * KTILE + threadIdx.x;
+  double ss = 0.;
+#pragma unroll
+  for (int q = 0; q < KTILE; q++) {
+    size_t c = base + (size_t)q * blockDim.x;
+    if (c >= n) continue;
+    double acc = w[c];
+    for (int v = 0; v < nv; v++) acc = fma(-coef[v], __ldcs(&V[v][c]), acc);
+    w[c] = acc;
+    ss = fma(acc, acc, ss);
+  }
+  ss = block_sum(ss);
+  if (threadIdx.x == 0) partial[blockIdx.x] = ss;
+}
+
+// x += sum_v coef[v] Z_v
+__global__ void __launch_bounds__(256) k_axpy_multi(size_t n, int nv, const double *const *__restrict__ Z,
+                                                    const double *__restrict__ coef, double *__restrict__ x) {
+  for (size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (size_t)gridDim.x * blockDim.x) {
+    double acc = x[c];
+    for (int v = 0; v < nv; v++) acc = fma(coef[v], __ldcs(&Z[v][c]), acc);
+    x[c] = acc;
+  }
+}
+
+// out = (s v) * scale in FP32 or FP64: the aj row scaling that turns the
+// FP64 Krylov vector into the V-cycle right-hand side.
+__global__ void k_scale_to(size_t n, const double *__restrict__ v, double s, const double *__restrict__ scale,
+                           float *out32, double *out64) {
+  for (size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (size_t)gridDim.x * blockDim.x) {
+    double t = s * v[c] * scale[c];
+    if (out32) out32[c] = (float)t;
+    else out64[c] = t;
+  }
+}
+// out = s * x (x in FP32 or FP64)
+__global__ void k_to64(size_t n, const float *__restrict__ x32, const double *__restrict__ x64, double s,
+                       double *__restrict__ out) {
+  for (size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (size_t)gridDim.x * blockDim.x)
+    out[c] = s * (x32 ? (double)x32[c] : x64[c]);
+}
+__global__ void k_sumsq(size_t n, const double *__restrict__ x, double *partial) {
+  double s = 0.;
+  for (size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (size_t)gridDim.x * blockDim.x)
+    s = fma(x[c], x[c], s);
+  s = block_sum(s);
+  if (threadIdx.x == 0) partial[blockIdx.x] = s;
+}
+
+#define TYPED(T, S)                                                                                        \
+  __global__ void __launch_bounds__(256) k_residual_##S(Box b, const T *A, const T *x, const T *rhs, T *r) {  \
+    residual_body<T>(b, A, x, rhs, r);                                                                     \
+  }                                                                                                        \
+  __global__ void k_line_lu_##S(Box b, const double *A64, T *inv, T *cp) { line_lu_body<T>(b, A64, inv, cp); } \
+  __global__ void __launch_bounds__(128) k_line_sweep_##S(Box b, const T *A, const T *inv, const T *cp,       \
+                                                          const T *x, const T *rhs, T *xo, T omega, int zg) { \
+    line_sweep_body<T>(b, A, inv, cp, x, rhs, xo, omega, zg);                                              \
+  }                                                                                                        \
+  __global__ void k_coarsest_##S(int nd, const int *didx, const double *dinv, const T *rhs, T *x, size_t n) { \
+    coarsest_body<T>(nd, didx, dinv, rhs, x, n);                                                           \
+  }                                                                                                        \
+  __global__ void k_cast_planes_##S(const double *src, T *dst, size_t n) { cast_body<T>(src, dst, n); }
+TYPED(float, f32)
+TYPED(double, f64)
+#undef TYPED
+
+}  // namespace vfs

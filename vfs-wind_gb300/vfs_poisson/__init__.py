@@ -1,0 +1,275 @@
+"""Python binding of libvfs_poisson.so (the C ABI in include/vfs_poisson.h).
+
+The class ``PoissonSolver`` mirrors the reference's per-block entry points
+(Source/poisson_hypre.c:506 PoissonSolver_Hypre, Source/poisson.c:3137
+UpdatePressure, :2700 Projection, Source/main.c:936 Divergence) on arrays in
+the reference's DA layout.  Arrays may be numpy arrays (host) or CUDA
+tensors / device pointers; the library detects which.
+
+There is no CPU fallback: loading fails loudly when the CUDA library has not
+been built, and every call fails when no GPU is present.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import configs  # noqa: F401  (synthetic inputs)
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(os.path.dirname(_HERE), "lib", "libvfs_poisson.so")
+
+VFS_OK, VFS_EINVAL, VFS_ECUDA, VFS_ESTATE, VFS_ENOCONV, VFS_ENOMEM, VFS_ETIMEOUT = 0, -1, -2, -3, -4, -5, -6
+
+# Exported symbols (every one is declared in include/vfs_poisson.h).
+EXPORTS = [
+    "vfs_last_error", "vfs_poisson_default_opts", "vfs_poisson_create", "vfs_poisson_destroy",
+    "vfs_poisson_set_grid", "vfs_poisson_set_nvert", "vfs_poisson_rhs", "vfs_poisson_solve",
+    "vfs_poisson_solver_hypre", "vfs_poisson_update_pressure", "vfs_poisson_projection",
+    "vfs_poisson_divergence", "vfs_poisson_get_numbering", "vfs_poisson_get_operator",
+    "vfs_poisson_get_metric", "vfs_poisson_get_rhs", "vfs_poisson_apply", "vfs_poisson_mg_levels",
+    "vfs_poisson_mg_level_info", "vfs_poisson_mg_get_nvert", "vfs_poisson_mg_restrict",
+    "vfs_poisson_mg_interpolate", "vfs_poisson_mg_vcycle", "vfs_poisson_kernel_launches",
+]
+
+
+class GridDesc(C.Structure):
+    _fields_ = [("mx", C.c_int), ("my", C.c_int), ("mz", C.c_int),
+                ("i_periodic", C.c_int), ("j_periodic", C.c_int), ("k_periodic", C.c_int),
+                ("ii_periodic", C.c_int), ("jj_periodic", C.c_int), ("kk_periodic", C.c_int),
+                ("bctype3", C.c_int)]
+
+
+class SolveOpts(C.Structure):
+    _fields_ = [("rtol", C.c_double), ("max_it", C.c_int), ("restart", C.c_int), ("precision", C.c_int),
+                ("nu1", C.c_int), ("nu2", C.c_int), ("omega", C.c_double), ("use_graphs", C.c_int),
+                ("coarsest_max", C.c_int), ("warm_start", C.c_int)]
+
+
+class SolveStats(C.Structure):
+    _fields_ = [("iterations", C.c_int), ("rel_residual", C.c_double), ("initial_rel_residual", C.c_double),
+                ("ms_total", C.c_double), ("levels", C.c_int), ("status", C.c_int)]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
+METRIC_INDEX = {name: q for q, name in enumerate(
+    ["icsi", "ieta", "izet", "jcsi", "jeta", "jzet", "kcsi", "keta", "kzet", "csi", "eta", "zet", "cent",
+     "iaj", "jaj", "kaj", "aj"])}
+
+_lib = None
+
+
+def load(path=LIB_PATH):
+    """Load the CUDA library (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise RuntimeError(f"{path} is missing: build it with __graft_entry__.build() "
+                           "(there is no CPU fallback)")
+    L = C.CDLL(path)
+    P, vp, dp, ip = C.POINTER, C.c_void_p, C.c_void_p, C.c_void_p
+    L.vfs_last_error.restype = C.c_char_p
+    L.vfs_poisson_default_opts.argtypes = [P(SolveOpts)]
+    L.vfs_poisson_create.argtypes = [P(GridDesc), P(vp)]
+    L.vfs_poisson_destroy.argtypes = [vp]
+    L.vfs_poisson_set_grid.argtypes = [vp, dp, vp]
+    L.vfs_poisson_set_nvert.argtypes = [vp, dp]
+    L.vfs_poisson_rhs.argtypes = [vp, dp, C.c_double, C.c_double, C.c_double]
+    L.vfs_poisson_solve.argtypes = [vp, dp, P(SolveOpts), P(SolveStats)]
+    L.vfs_poisson_solver_hypre.argtypes = [vp, dp, C.c_double, C.c_double, C.c_double, dp, P(SolveOpts),
+                                           P(SolveStats)]
+    L.vfs_poisson_update_pressure.argtypes = [vp, dp, dp]
+    L.vfs_poisson_projection.argtypes = [vp, dp, C.c_double, C.c_double, C.c_double]
+    L.vfs_poisson_divergence.argtypes = [vp, dp, P(C.c_double)]
+    L.vfs_poisson_get_numbering.argtypes = [vp, P(C.c_int), ip]
+    L.vfs_poisson_get_operator.argtypes = [vp, dp, ip]
+    L.vfs_poisson_get_metric.argtypes = [vp, C.c_int, dp]
+    L.vfs_poisson_get_rhs.argtypes = [vp, dp]
+    L.vfs_poisson_apply.argtypes = [vp, dp, dp]
+    L.vfs_poisson_mg_levels.argtypes = [vp, P(C.c_int)]
+    L.vfs_poisson_mg_level_info.argtypes = [vp, C.c_int, P(C.c_int)]
+    L.vfs_poisson_mg_get_nvert.argtypes = [vp, C.c_int, dp]
+    L.vfs_poisson_mg_restrict.argtypes = [vp, C.c_int, dp, dp]
+    L.vfs_poisson_mg_interpolate.argtypes = [vp, C.c_int, dp, dp]
+    L.vfs_poisson_mg_vcycle.argtypes = [vp, C.c_int, dp, dp]
+    L.vfs_poisson_kernel_launches.argtypes = [vp]
+    L.vfs_poisson_kernel_launches.restype = C.c_int64
+    _lib = L
+    return L
+
+
+class VfsError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"vfs_poisson error {code}: {msg}")
+        self.code = code
+
+
+def _check(rc):
+    if rc != VFS_OK:
+        raise VfsError(rc, load().vfs_last_error().decode())
+    return rc
+
+
+def _ptr(a, writable=False):
+    """Address of a numpy array (C-contiguous float64) or a CUDA tensor."""
+    if a is None:
+        return None
+    if isinstance(a, int):
+        return a
+    if hasattr(a, "data_ptr"):  # torch tensor
+        assert a.is_contiguous()
+        return a.data_ptr()
+    assert isinstance(a, np.ndarray) and a.flags.c_contiguous, "arrays must be C-contiguous"
+    if writable:
+        assert a.flags.writeable
+    return a.ctypes.data
+
+
+def default_opts(**kw):
+    o = SolveOpts()
+    load().vfs_poisson_default_opts(C.byref(o))
+    for k, v in kw.items():
+        setattr(o, k, v)
+    return o
+
+
+class PoissonSolver:
+    """One block's pressure-Poisson projection on the GPU."""
+
+    def __init__(self, mx, my, mz, periodic=(0, 0, 0, 0, 0, 0), bctype3=0):
+        L = load()
+        self.dims = (mx, my, mz)
+        g = GridDesc(mx, my, mz, *[int(p) for p in periodic], bctype3)
+        h = C.c_void_p()
+        _check(L.vfs_poisson_create(C.byref(g), C.byref(h)))
+        self.h = h
+
+    @classmethod
+    def from_case(cls, case):
+        s = cls(*case.dims, periodic=case.periodic)
+        s.set_grid(case.coor)
+        s.set_nvert(case.nvert)
+        return s
+
+    def close(self):
+        if getattr(self, "h", None):
+            load().vfs_poisson_destroy(self.h)
+            self.h = None
+
+    __del__ = close
+
+    def _shape(self, comps=0):
+        mx, my, mz = self.dims
+        return (mz, my, mx) + ((comps,) if comps else ())
+
+    # --- set-up ---
+    def set_grid(self, coor, face_metrics=None):
+        fm = None
+        if face_metrics is not None:
+            arr = (C.c_void_p * 13)(*[_ptr(a) for a in face_metrics])
+            fm = C.cast(arr, C.c_void_p)
+            self._fm_keep = (arr, face_metrics)
+        _check(load().vfs_poisson_set_grid(self.h, _ptr(coor), fm))
+
+    def set_nvert(self, nvert):
+        _check(load().vfs_poisson_set_nvert(self.h, _ptr(nvert)))
+
+    # --- per step ---
+    def rhs(self, ucont, dt=1.0, st=1.0, coeff=1.0):
+        _check(load().vfs_poisson_rhs(self.h, _ptr(ucont), dt, st, coeff))
+
+    def solve(self, phi=None, opts=None, **kw):
+        o = opts if opts is not None else default_opts(**kw)
+        st = SolveStats()
+        out = phi if phi is not None else np.zeros(self._shape())
+        rc = load().vfs_poisson_solve(self.h, _ptr(out, True), C.byref(o), C.byref(st))
+        if rc not in (VFS_OK, VFS_ENOCONV):
+            _check(rc)
+        return out, st
+
+    def solver_hypre(self, ucont, dt=1.0, st=1.0, coeff=1.0, phi=None, opts=None, **kw):
+        self.rhs(ucont, dt, st, coeff)
+        return self.solve(phi, opts, **kw)
+
+    def update_pressure(self, p, phi=None):
+        _check(load().vfs_poisson_update_pressure(self.h, _ptr(p, True), _ptr(phi, True)))
+        return p, phi
+
+    def projection(self, ucont, dt=1.0, st=1.0, coeff=1.0):
+        _check(load().vfs_poisson_projection(self.h, _ptr(ucont, True), dt, st, coeff))
+        return ucont
+
+    def divergence(self, ucont):
+        v = C.c_double()
+        _check(load().vfs_poisson_divergence(self.h, _ptr(ucont), C.byref(v)))
+        return v.value
+
+    # --- inspection ---
+    def numbering(self):
+        n = C.c_int()
+        gid = np.zeros(self._shape(), np.int32)
+        _check(load().vfs_poisson_get_numbering(self.h, C.byref(n), _ptr(gid, True)))
+        return n.value, gid
+
+    def operator(self):
+        vol = np.zeros(self._shape(19))
+        rt = np.zeros(self._shape(), np.int32)
+        _check(load().vfs_poisson_get_operator(self.h, _ptr(vol, True), _ptr(rt, True)))
+        return vol, rt
+
+    def metric(self, name):
+        q = METRIC_INDEX[name]
+        out = np.zeros(self._shape(3 if q < 13 else 0))
+        _check(load().vfs_poisson_get_metric(self.h, q, _ptr(out, True)))
+        return out
+
+    def rhs_array(self):
+        out = np.zeros(self._shape())
+        _check(load().vfs_poisson_get_rhs(self.h, _ptr(out, True)))
+        return out
+
+    def apply(self, x):
+        y = np.zeros(self._shape())
+        _check(load().vfs_poisson_apply(self.h, _ptr(np.ascontiguousarray(x, np.float64)), _ptr(y, True)))
+        return y
+
+    def mg_levels(self):
+        n = C.c_int()
+        _check(load().vfs_poisson_mg_levels(self.h, C.byref(n)))
+        out = []
+        for li in range(n.value):
+            d = (C.c_int * 6)()
+            _check(load().vfs_poisson_mg_level_info(self.h, li, d))
+            out.append(tuple(d))
+        return out
+
+    def mg_nvert(self, level):
+        nx, ny, nz = self.mg_levels()[level][:3]
+        out = np.zeros((nz + 2, ny + 2, nx + 2))
+        _check(load().vfs_poisson_mg_get_nvert(self.h, level, _ptr(out, True)))
+        return out
+
+    def mg_restrict(self, fine, xf):
+        nx, ny, nz = self.mg_levels()[fine + 1][:3]
+        out = np.zeros((nz + 2, ny + 2, nx + 2))
+        _check(load().vfs_poisson_mg_restrict(self.h, fine, _ptr(np.ascontiguousarray(xf)), _ptr(out, True)))
+        return out
+
+    def mg_interpolate(self, fine, xc):
+        nx, ny, nz = self.mg_levels()[fine][:3]
+        out = np.zeros((nz + 2, ny + 2, nx + 2))
+        _check(load().vfs_poisson_mg_interpolate(self.h, fine, _ptr(np.ascontiguousarray(xc)), _ptr(out, True)))
+        return out
+
+    def mg_vcycle(self, r, precision=0):
+        z = np.zeros(self._shape())
+        _check(load().vfs_poisson_mg_vcycle(self.h, precision, _ptr(np.ascontiguousarray(r)), _ptr(z, True)))
+        return z
+
+    def kernel_launches(self):
+        return load().vfs_poisson_kernel_launches(self.h)

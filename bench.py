@@ -1,0 +1,317 @@
+#!/usr/bin/env python3
+"""Benchmark: ms per pressure-Poisson solve to a 1e-8 relative residual.
+
+Workload: the 256x192x256 curvilinear wind-farm-like grid with a 3x2 array of
+tower cylinders (configuration 3), seeded synthetic Fourier-mode Ucont.  One
+step is one PoissonSolver_Hypre-equivalent call: right-hand side from Ucont,
+FGMRES with an FP32 multigrid V-cycle inside FP64 refinement to
+||b - A phi|| / ||b|| <= 1e-8 from a zero initial guess, fluid-mean removal and
+phi in DA layout.  The plain FP64 GPU solver (same FGMRES, FP64 V-cycle) is
+timed the same way and reported alongside.
+
+Arms:
+  default            this library on the GPU (value: inputs resident in HBM;
+                     e2e: host buffers through the C ABI)
+  --impl reference   the reference's algorithm on the host cores: the CPU
+                     port in oracle/ (the reference itself needs PETSc 3.1,
+                     HYPRE and MPI, which are not available), each step a
+                     bounded sample of the same solve scaled to a full solve.
+
+Multi-GPU: the solve does not shard in this library; under torchrun every
+rank runs an independent replica (weak scaling) and rank 0 reports.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+for _p in (os.path.join(REPO, "vfs-wind_gb300"), os.path.join(REPO, "oracle"), REPO):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "ms per Poisson solve to 1e-8 rel. residual: learned+FP32/FP64 vs plain FP64 GPU"
+WORKLOAD = "towers 256x192x256 (config 3: geometric 1.03 wall stretching, amplitude 0.02, 3x2 tower cylinders)"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--size", type=int, nargs=3, default=[256, 192, 256])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-sample-its", type=int, default=3)
+    return ap.parse_args()
+
+
+def dist_env():
+    return (int(os.environ.get("RANK", 0)), int(os.environ.get("LOCAL_RANK", 0)),
+            int(os.environ.get("WORLD_SIZE", 1)))
+
+
+def peaks():
+    try:
+        with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle-reason samples during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu):
+        self.gpu = gpu
+        self.path = tempfile.mktemp(suffix=".csv")
+        self.proc = None
+
+    def start(self):
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.close()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_port_time(case, iterations_full, sample_its, threads=0):
+    """Time the oracle's CPU port of the solve (FP64 FGMRES + geometric
+    V-cycle, OpenMP over all host threads) for `sample_its` outer
+    iterations and scale to a full solve of `iterations_full` iterations."""
+    import oracle as O
+    d = O.dims_of(case)
+    met = O.form_metrics(d, case.coor)
+    lhs = O.poisson_lhs(d, case.nvert, met)
+    b = O.rhs(d, case.nvert, lhs["gid"], case.ucont, met["aj"])
+    bda = O.to_da(d, lhs["gid"], b)
+    mg = O.MGSolver(d, case.coor, case.nvert, met, threads=threads)
+    x, st = mg.solve(bda, rtol=1e-8, max_it=sample_its, restart=20)
+    ms_it = st.solve_ms / max(st.iterations, 1)
+    del mg
+    return ms_it, st.iterations, ms_it * iterations_full
+
+
+def run_reference(args):
+    rank, local, world = dist_env()
+    if rank != 0:
+        return
+    from vfs_poisson import configs as CF
+    import oracle as O
+    O.build()
+    nx, ny, nz = args.size
+    case = CF.towers(nx, ny, nz)
+    cores = os.cpu_count()
+    d = O.dims_of(case)
+    met = O.form_metrics(d, case.coor)
+    lhs = O.poisson_lhs(d, case.nvert, met)
+    b = O.rhs(d, case.nvert, lhs["gid"], case.ucont, met["aj"])
+    bda = O.to_da(d, lhs["gid"], b)
+    mg = O.MGSolver(d, case.coor, case.nvert, met)
+    # warm-up: one full solve counts the outer iterations a full solve needs
+    _, full = mg.solve(bda, rtol=1e-8, max_it=60, restart=20)
+    its_full = full.iterations
+    for _ in range(max(0, args.warmup - 1)):
+        mg.solve(bda, rtol=1e-8, max_it=args.cpu_sample_its, restart=20)
+    ms = []
+    for _ in range(args.steps):
+        _, st = mg.solve(bda, rtol=1e-8, max_it=args.cpu_sample_its, restart=20)
+        ms.append(st.solve_ms / max(st.iterations, 1) * its_full)
+    value = statistics.mean(ms)
+    sample = (f"{args.cpu_sample_its} FGMRES iterations per step on the full {nx}x{ny}x{nz} grid, "
+              f"scaled to the {its_full} iterations of a full solve")
+    line = {"metric": METRIC, "value": value, "unit": "ms", "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": value, "higher_is_better": False, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "cells": case.cells, "solver": "FGMRES(20) + geometric V-cycle, FP64",
+                       "rtol": 1e-8, "iterations": its_full},
+            "impl": "reference",
+            "cpu_baseline": {"value": value, "unit": "ms", "cores": cores, "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": "ms", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import numpy as np
+    import torch
+
+    rank, local, world = dist_env()
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    import __graft_entry__
+    __graft_entry__.build()
+    import vfs_poisson as V
+    from vfs_poisson import configs as CF
+
+    nx, ny, nz = args.size
+    case = CF.towers(nx, ny, nz)
+    s = V.PoissonSolver.from_case(case)
+    stream = torch.cuda.current_stream()
+    s.set_stream(stream.cuda_stream)
+    shape = case.nvert.shape
+    ucont_d = torch.from_numpy(case.ucont).cuda()
+    phi_d = torch.zeros(shape, dtype=torch.float64, device="cuda")
+    mixed = V.default_opts(precision=0, rtol=1e-8)
+    plain = V.default_opts(precision=1, rtol=1e-8)
+
+    def timed(opts, steps, warmup, host=None, prof=False, clocks=None):
+        u, phi = (ucont_d, phi_d) if host is None else host
+        s.profile(prof)  # the V-cycle graph is re-captured during warm-up, not in the timed region
+        for _ in range(warmup):
+            s.solver_hypre(u, phi=phi, opts=opts)
+        torch.cuda.synchronize()
+        barrier()
+        if prof:
+            s.profile(True)  # zero the counters
+        n0 = s.kernel_launches()
+        if clocks:
+            clocks.start()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        its = []
+        for _ in range(steps):
+            _, st = s.solver_hypre(u, phi=phi, opts=opts)
+            its.append((st.iterations, st.rel_residual, st.status))
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ck = clocks.stop() if clocks else None
+        barrier()
+        ms = e0.elapsed_time(e1) / steps
+        if dist is not None:
+            t = torch.tensor([ms], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ms = float(t.item())
+        launches = s.kernel_launches() - n0
+        pr = s.profile_read() if prof else None
+        if prof:
+            s.profile(False)
+        return ms, its, launches, pr, ck
+
+    clocks = ClockSampler(local)
+    ms_mixed, its_mixed, launches, (pms, pbytes, pn), ck = timed(mixed, args.steps, args.warmup, prof=True,
+                                                                  clocks=clocks)
+    phi_mixed = phi_d.cpu().numpy().copy()
+    ms_plain, its_plain, _, _, _ = timed(plain, args.steps, max(1, args.warmup - 2))
+    # FP64 reference answer on the device: plain solver to 1e-12
+    s.solver_hypre(ucont_d, phi=phi_d, opts=V.default_opts(precision=1, rtol=1e-12, max_it=400))
+    phi_ref = phi_d.cpu().numpy()
+    fluid = case.nvert < 0.1
+    err = float(np.linalg.norm((phi_mixed - phi_ref)[fluid]) / np.linalg.norm(phi_ref[fluid]))
+    # post-projection divergence with the mixed-precision phi
+    u = case.ucont.copy()
+    p = np.zeros(shape)
+    s.update_pressure(p, phi_mixed.copy())
+    s.projection(u)
+    maxdiv_after = s.divergence(u)
+    maxdiv_before = s.divergence(case.ucont)
+    # end to end: host (pinned) buffers through the C ABI
+    u_h = torch.from_numpy(case.ucont).pin_memory()
+    phi_h = torch.zeros(shape, dtype=torch.float64).pin_memory()
+    ms_e2e, _, _, _, _ = timed(mixed, args.steps, 1, host=(u_h.numpy(), phi_h.numpy()))
+
+    hbm, peak_kind = peaks()
+    achieved = pbytes / (pms * 1e-3) / 1e9 if pms > 0 else None
+    traffic = None
+    tpath = os.path.join(REPO, "profiles", "line_sweep_traffic.json")
+    if os.path.exists(tpath):
+        try:
+            t = json.load(open(tpath))
+            traffic = t["dram_bytes_per_cell_full_sweep"] * nx * ny * nz
+        except Exception:
+            traffic = None
+    line = {
+        "metric": METRIC, "value": ms_mixed / world, "unit": "ms", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_mixed, "higher_is_better": False, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64/f32", "data": "synthetic",
+        "config": {
+            "workload": WORKLOAD, "cells": nx * ny * nz, "rtol": 1e-8,
+            "solver": "FGMRES(20) in FP64 with an FP32 geometric V-cycle (zebra j-line Gauss-Seidel over "
+                      "k-planes, 2+2 sweeps); learned initial guess not used in this line",
+            "iterations": its_mixed[-1][0], "rel_residual": its_mixed[-1][1],
+            "plain_fp64_ms": ms_plain, "plain_fp64_iterations": its_plain[-1][0],
+            "speedup_vs_plain_fp64": ms_plain / ms_mixed,
+            "phi_rel_l2_vs_fp64": err, "maxdiv_before": maxdiv_before, "maxdiv_after_projection": maxdiv_after,
+            "l2": "inputs larger than L2 (19 operator planes, 0.96 GB in FP32 on the finest level)",
+            "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
+        },
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                     "frac": (achieved / hbm) if achieved else None, "traffic": traffic,
+                     "kernel": "k_line_sweep_f32 on the finest level", "launches_timed": pn,
+                     "peak_source": peak_kind},
+        "clocks": ck,
+        "e2e": {"value": ms_e2e / world, "unit": "ms", "h2d_bytes_per_step": int(case.ucont.nbytes),
+                "d2h_bytes_per_step": int(phi_h.numel() * 8)},
+        "gpu_launches": int(launches),
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        ms_it, its_s, ms_full = cpu_port_time(case, its_plain[-1][0], args.cpu_sample_its)
+        line["cpu_baseline"] = {"value": ms_full, "unit": "ms", "cores": os.cpu_count(), "kind": "port",
+                                "sample": f"{its_s} FGMRES iterations of the FP64 CPU port on the full grid "
+                                          f"({ms_it:.0f} ms each), scaled to the {its_plain[-1][0]} iterations "
+                                          f"of a full solve"}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    s.close()
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

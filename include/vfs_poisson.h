@@ -65,10 +65,12 @@ typedef struct {
   int restart;        /* FGMRES restart length                             */
   int precision;      /* 0: FP32 V-cycle in FP64 refinement, 1: all FP64   */
   int nu1, nu2;       /* pre / post j-line sweeps per level                */
-  double omega;       /* line-Jacobi damping                               */
+  double omega;       /* relaxation weight of the line sweeps              */
   int use_graphs;     /* capture the V-cycle in a CUDA graph               */
   int coarsest_max;   /* coarsest level cell budget                        */
   int warm_start;     /* 1: start from the phi passed in (Phi2 warm start) */
+  int smoother;       /* 0 fused line Jacobi, 1 line Jacobi in correction
+                         form, 2 zebra (k-plane) line Gauss-Seidel         */
 } vfs_solve_opts;
 
 typedef struct {
@@ -167,6 +169,18 @@ int vfs_poisson_mg_vcycle(vfs_poisson *h, int precision, const double *r, double
 /* Number of kernel launches issued by this library since the handle was
  * created (graph-launched kernels included). */
 int64_t vfs_poisson_kernel_launches(vfs_poisson *h);
+
+/* Run the handle's work on a caller's CUDA stream (cudaStream_t passed as
+ * void*); NULL returns to a private stream.  No reference counterpart: the
+ * reference is CPU-only. */
+int vfs_poisson_set_stream(vfs_poisson *h, void *stream);
+
+/* Live timing of the dominant kernel (the finest-level j-line sweep): when
+ * enabled, CUDA events bracket every such launch inside the solves and
+ * vfs_poisson_profile_read returns their summed device time, their summed
+ * algorithmic bytes and their count since enabling. */
+int vfs_poisson_profile(vfs_poisson *h, int enable);
+int vfs_poisson_profile_read(vfs_poisson *h, double *ms, double *bytes, int64_t *launches);
 
 #ifdef __cplusplus
 }

@@ -439,6 +439,49 @@ static void line_sweep(const lvl_t *l, double omega, const double *x, const doub
     }
 }
 
+/* zebra j-line Gauss-Seidel: columns of colour (i + k) % 2 == 0, then 1;
+ * each colour reads the other colour's newest values (x updated in place),
+ * same-colour corner couplings see the values from before the sweep. */
+static int g_zebra = 0;
+static void zebra_sweep(const lvl_t *l, double omega, double *x, const double *b, double *tmp, int zero_guess)
+{
+  if (zero_guess) memset(x, 0, l->n * 8);
+  for (int color = 0; color < 2; color++) {
+    memcpy(tmp, x, l->n * 8);  /* snapshot: same-colour neighbours read old values */
+#pragma omp parallel for collapse(2)
+    for (int k = 0; k < l->nz; k++)
+      for (int i = 0; i < l->nx; i++) {
+        if (((i + k) & 1) != color) continue;
+        double yprev = 0;
+        double ys[1024];
+        for (int j = 0; j < l->ny; j++) {
+          size_t c = ((size_t)k * l->ny + j) * l->nx + i;
+          double rhs = 0;
+          if (l->act[c]) {
+            rhs = b[c];
+            for (int q = 1; q < NS; q++) {
+              if ((q == 3 && j < l->ny - 1) || (q == 4 && j > 0)) continue;
+              long nb = nbr(l, i, j, k, q);
+              if (nb >= 0) rhs -= l->A[q * l->n + c] * tmp[nb];
+            }
+          }
+          double a = (j > 0 && l->act[c]) ? l->A[4 * l->n + c] : 0.;
+          double y = (rhs - a * yprev) * l->inv[c];
+          ys[j] = y;
+          yprev = y;
+        }
+        double xn = 0;
+        for (int j = l->ny - 1; j >= 0; j--) {
+          size_t c = ((size_t)k * l->ny + j) * l->nx + i;
+          double v = ys[j] - ((j < l->ny - 1) ? l->cp[c] * xn : 0.);
+          xn = v;
+          double xold = tmp[c];
+          x[c] = l->act[c] ? xold + omega * (v - xold) : 0.;
+        }
+      }
+  }
+}
+
 static void vcycle(mg_t *g, int li, int nu1, int nu2, double omega)
 {
   lvl_t *l = &g->L[li];
@@ -452,6 +495,7 @@ static void vcycle(mg_t *g, int li, int nu1, int nu2, double omega)
     return;
   }
   for (int s = 0; s < nu1; s++) {
+    if (g_zebra) { zebra_sweep(l, omega, l->x, l->b, l->t, s == 0); continue; }
     line_sweep(l, omega, l->x, l->b, l->t, s == 0);
     double *tmp = l->x; l->x = l->t; l->t = tmp;
   }
@@ -522,10 +566,13 @@ static void vcycle(mg_t *g, int li, int nu1, int nu2, double omega)
         }
   }
   for (int s = 0; s < nu2; s++) {
+    if (g_zebra) { zebra_sweep(l, omega, l->x, l->b, l->t, 0); continue; }
     line_sweep(l, omega, l->x, l->b, l->t, 0);
     double *tmp = l->x; l->x = l->t; l->t = tmp;
   }
 }
+
+void or_mg_set_smoother(int zebra) { g_zebra = zebra; }
 
 static double dot(const double *a, const double *b, size_t n)
 {

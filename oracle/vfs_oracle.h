@@ -113,6 +113,9 @@ int or_mg_solve(void *h, const double *b_da, double *x_da, const or_solve_opts *
 int or_mg_vcycle(void *h, const double *r_da, double *z_da);
 int or_mg_level_info(void *h, int level, int *dims7);
 void or_mg_destroy(void *h);
+/* 1: zebra j-line Gauss-Seidel smoothing (checkerboard columns), 0: damped
+ * j-line Jacobi (default). */
+void or_mg_set_smoother(int zebra);
 
 #ifdef __cplusplus
 }

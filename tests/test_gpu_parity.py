@@ -26,8 +26,8 @@ def _cases():
     # explicit-copy periodic flags in i and j, and fractional IB values that
     # make identity rows (nvert in (0.1, 1) keeps a dof, poisson.c:1158)
     c4 = CF.cylinder(16, 12, 16, seed=7)
-    c4.periodic = (1, 1, 0, 0, 0, 0)
     c4.nvert = np.where(c4.nvert == 1.0, 0.5, c4.nvert)
+    c4.set_periodic((1, 1, 0, 0, 0, 0))
     c4.name = "cylinder_ijper_frac"
     return [c1, c2, c3, c4]
 

@@ -43,6 +43,10 @@ struct Box {
   }
 };
 
+// Cells of a j-line handled by one thread of the line smoother; a line of
+// ny cells uses ceil(ny / kLineChunk) threads (at most 24, 768 per block).
+constexpr int kLineChunk = 8;
+
 // Stencil slot order of the reference's 19-point operator
 // (Source/poisson.c:957-975): offsets (di, dj, dk) per slot.
 enum { CP = 0, EP, WP, NP, SP, TP, BP, NE, SE, NW, SW, TN, BN, TS, BS, TE, BE, TW, BW, NSLOT };
@@ -68,19 +72,23 @@ struct Nbr {
   }
 };
 
-// Linear indices of the 19 stencil points of (i,j,k) in slot order.
-__device__ inline void stencil_index(const Box &b, int i, int j, int k, size_t idx[NSLOT]) {
+// Linear indices of the 19 stencil points of (i,j,k) in slot order (32-bit:
+// the library rejects grids whose 19 operator planes reach 2^32 entries).
+__device__ inline void stencil_index(const Box &b, int i, int j, int k, uint32_t idx[NSLOT]) {
   Nbr q(b, i, j, k);
-  idx[CP] = b.at(i, j, k);
-  idx[EP] = b.at(q.ip, j, k);     idx[WP] = b.at(q.im, j, k);
-  idx[NP] = b.at(i, q.jp, k);     idx[SP] = b.at(i, q.jm, k);
-  idx[TP] = b.at(i, j, q.kp);     idx[BP] = b.at(i, j, q.km);
-  idx[NE] = b.at(q.ip, q.jp, k);  idx[SE] = b.at(q.ip, q.jm, k);
-  idx[NW] = b.at(q.im, q.jp, k);  idx[SW] = b.at(q.im, q.jm, k);
-  idx[TN] = b.at(i, q.jp, q.kp);  idx[BN] = b.at(i, q.jp, q.km);
-  idx[TS] = b.at(i, q.jm, q.kp);  idx[BS] = b.at(i, q.jm, q.km);
-  idx[TE] = b.at(q.ip, j, q.kp);  idx[BE] = b.at(q.ip, j, q.km);
-  idx[TW] = b.at(q.im, j, q.kp);  idx[BW] = b.at(q.im, j, q.km);
+  const uint32_t nx = b.nx, sl = (uint32_t)b.nx * b.ny;
+  const uint32_t r0 = (uint32_t)k * sl, rm = (uint32_t)q.km * sl, rp = (uint32_t)q.kp * sl;
+  const uint32_t j0 = (uint32_t)j * nx, jm = (uint32_t)q.jm * nx, jp = (uint32_t)q.jp * nx;
+  idx[CP] = r0 + j0 + i;
+  idx[EP] = r0 + j0 + q.ip;  idx[WP] = r0 + j0 + q.im;
+  idx[NP] = r0 + jp + i;     idx[SP] = r0 + jm + i;
+  idx[TP] = rp + j0 + i;     idx[BP] = rm + j0 + i;
+  idx[NE] = r0 + jp + q.ip;  idx[SE] = r0 + jm + q.ip;
+  idx[NW] = r0 + jp + q.im;  idx[SW] = r0 + jm + q.im;
+  idx[TN] = rp + jp + i;     idx[BN] = rm + jp + i;
+  idx[TS] = rp + jm + i;     idx[BS] = rm + jm + i;
+  idx[TE] = rp + j0 + q.ip;  idx[BE] = rm + j0 + q.ip;
+  idx[TW] = rp + j0 + q.im;  idx[BW] = rm + j0 + q.im;
 }
 
 // ---- deterministic reductions: fixed-shape block trees ----

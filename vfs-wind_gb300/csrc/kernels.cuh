@@ -59,10 +59,12 @@ __global__ void k_prolong_f64(Box bf, Box bc, int cx, int cy, int cz, const doub
 
 // solve.cu (hot loop kernels)
 #define TYPED_DECL(T, S)                                                                                 \
-  __global__ void k_residual_##S(Box b, const T *A, const T *x, const T *rhs, T *r);                     \
+  __global__ void k_residual_##S(Box b, const T *A, const T *x, const T *rhs, T *r, int color);          \
   __global__ void k_line_lu_##S(Box b, const double *A64, T *inv, T *cp);                                \
   __global__ void k_line_sweep_##S(Box b, const T *A, const T *inv, const T *cp, const T *x, const T *rhs, \
                                    T *xo, T omega, int zero_guess);                                      \
+  __global__ void k_line_tri_##S(Box b, const T *r, const T *Asp, const T *inv, const T *cp, T *x, T omega,  \
+                                 int zero_guess, int color);                                             \
   __global__ void k_coarsest_##S(int nd, const int *didx, const double *dinv, const T *rhs, T *x, size_t n); \
   __global__ void k_cast_planes_##S(const double *src, T *dst, size_t n);
 TYPED_DECL(float, f32)

@@ -62,7 +62,8 @@ __device__ inline void atomic_max_pos(double *addr, double v) {
 }
 __global__ void k_max_spacing(Grid g, const double *coor, double *H) {
   int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y + 1, k = blockIdx.z + 1;
-  if (i < 1 || i >= g.mx - 1) return;
+  const bool in = i >= 1 && i < g.mx - 1;
+  if (!in) i = 1;  // every thread joins the block reduction
 #define CO(a, b, c, q) coor[g.at(a, b, c) * 3 + (q)]
   double d[3] = {0, 0, 0};
   for (int q = 0; q < 3; q++) {
@@ -76,8 +77,23 @@ __global__ void k_max_spacing(Grid g, const double *coor, double *H) {
     d[1] += (fp1 - fm1) * (fp1 - fm1);
     d[2] += (fp2 - fm2) * (fp2 - fm2);
   }
+  if (!in) d[0] = d[1] = d[2] = 0.;
 #undef CO
-  for (int q = 0; q < 3; q++) atomic_max_pos(&H[q], sqrt(d[q]));
+  for (int q = 0; q < 3; q++) {
+    double m = block_max(sqrt(d[q]));
+    if (threadIdx.x == 0) atomic_max_pos(&H[q], m);
+  }
+}
+
+// Gram-Schmidt coefficients on the device: h_i = sv_i (V_i . w) and the
+// update coefficient h_i sv_i for the stored (unnormalised) V_i.
+__global__ void k_gs_coef(int nv, const double *dots, const double *sv, double *hcol, double *coef) {
+  int i = threadIdx.x;
+  if (i < nv) {
+    double hh = dots[i] * sv[i];
+    hcol[i] = hh;
+    coef[i] = hh * sv[i];
+  }
 }
 
 struct Level {
@@ -126,7 +142,7 @@ struct vfs_poisson {
   int m_alloc = 0;
   std::vector<double *> V, Z;
   double **dV = nullptr, **dZ = nullptr;
-  double *partial = nullptr, *red = nullptr, *coef = nullptr;
+  double *partial = nullptr, *red = nullptr, *coef = nullptr, *dsv = nullptr;
   size_t partial_len = 0;
   double *hbuf = nullptr;  // pinned host readback
   std::vector<Level> L;
@@ -134,9 +150,17 @@ struct vfs_poisson {
   // graphs of the V-cycle per precision and parameters they were built for
   cudaGraphExec_t gexec[2] = {nullptr, nullptr};
   int64_t gnodes[2] = {0, 0};
-  int gparams[2][3] = {{-1, -1, -1}, {-1, -1, -1}};
+  int gparams[2][4] = {{-1, -1, -1, -1}, {-1, -1, -1, -1}};
   double gomega[2] = {0, 0};
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  bool own_stream = true;
+  // live timing of the level-0 line sweeps (the dominant kernel)
+  bool prof = false;
+  cudaEvent_t pev[2][16] = {};
+  int pcount = 0;            // sweeps recorded in the V-cycle in flight
+  double pbytes[16] = {};    // algorithmic bytes of each recorded sweep
+  double prof_ms = 0., prof_bytes = 0.;
+  int64_t prof_launches = 0;
 };
 
 namespace {
@@ -194,6 +218,12 @@ unsigned lin_grid(size_t n, int bx = 256) { return (unsigned)((n + bx - 1) / bx)
 #define LAUNCH(h, kern, grid, block, ...)                          \
   do {                                                             \
     kern<<<(grid), (block), 0, (h)->stream>>>(__VA_ARGS__);        \
+    (h)->launches++;                                               \
+  } while (0)
+
+#define LAUNCH_SM(h, kern, grid, block, smem, ...)                 \
+  do {                                                             \
+    kern<<<(grid), (block), (smem), (h)->stream>>>(__VA_ARGS__);   \
     (h)->launches++;                                               \
   } while (0)
 
@@ -445,6 +475,7 @@ struct Prec<float> {
   static constexpr auto restrict_ = k_restrict_f32;
   static constexpr auto prolong = k_prolong_f32;
   static constexpr auto coarsest = k_coarsest_f32;
+  static constexpr auto tri = k_line_tri_f32;
   static float *A(Level &l) { return l.A32; }
   static float *inv(Level &l) { return l.inv32; }
   static float *cp(Level &l) { return l.cp32; }
@@ -459,6 +490,7 @@ struct Prec<double> {
   static constexpr auto restrict_ = k_restrict_f64;
   static constexpr auto prolong = k_prolong_f64;
   static constexpr auto coarsest = k_coarsest_f64;
+  static constexpr auto tri = k_line_tri_f64;
   static double *A(Level &l) { return l.A64; }
   static double *inv(Level &l) { return l.inv64; }
   static double *cp(Level &l) { return l.cp64; }
@@ -467,8 +499,60 @@ struct Prec<double> {
   static double *&xfinal(Level &l) { return l.xfinal64; }
 };
 
+// Event pairs around the level-0 sweeps of one V-cycle (recorded as graph
+// nodes when the V-cycle is captured); read after the next stream sync.
+// Algorithmic bytes of a sweep per cell: 16 off-line coefficients, the S
+// slot, inv and cp, the right-hand side, x and the written x (22 words),
+// or 5 words for the first sweep from a zero guess (S, inv, cp, rhs, x out).
+// For the correction-form sweeps (residual kernel + tridiagonal kernel) a
+// full sweep moves 22 + 6 words per cell (the residual's 19 coefficients,
+// x, rhs and r; then r, S slot, inv, cp, x read and written).
 template <typename T>
-void vcycle(vfs_poisson *h, int li, int nu1, int nu2, T omega) {
+void prof_begin(vfs_poisson *h, int li, bool zero_guess, int smoother) {
+  if (!h->prof || li != 0 || h->pcount >= 16) return;
+  cudaEventRecord(h->pev[0][h->pcount], h->stream);
+  const double words = zero_guess ? (smoother == 2 ? 16.5 : 5.0) : (smoother == 0 ? 22.0 : 28.0);
+  h->pbytes[h->pcount] = (double)h->box.n() * sizeof(T) * words;
+}
+void prof_end(vfs_poisson *h, int li) {
+  if (!h->prof || li != 0 || h->pcount >= 16) return;
+  cudaEventRecord(h->pev[1][h->pcount], h->stream);
+  h->pcount++;
+}
+
+// One smoothing sweep on level l.  smoother 0: fused j-line Jacobi kernel;
+// 1: j-line Jacobi in correction form (residual kernel + tridiagonal
+// kernel); 2: zebra j-line Gauss-Seidel over even then odd k-planes in
+// correction form.  x/t are swapped by the fused kernel only.
+template <typename T>
+void smooth(vfs_poisson *h, Level &l, int li, int smoother, bool zero_guess, T omega, T *&x, T *&t, T *bb, T *r) {
+  const int P = (l.b.ny + kLineChunk - 1) / kLineChunk;
+  dim3 lb(32, P), lg((l.b.nx + 31) / 32, l.b.nz);
+  const size_t lsm = 2 * 32 * P * sizeof(T);
+  T *Asp = Prec<T>::A(l) + (size_t)SP * l.b.n();
+  prof_begin<T>(h, li, zero_guess, smoother);
+  if (smoother == 0) {
+    LAUNCH_SM(h, Prec<T>::sweep, lg, lb, lsm, l.b, Prec<T>::A(l), Prec<T>::inv(l), Prec<T>::cp(l), x, bb, t, omega,
+              zero_guess ? 1 : 0);
+    std::swap(x, t);
+  } else if (smoother == 1) {
+    if (!zero_guess) LAUNCH(h, Prec<T>::residual, box_grid(l.b), 128, l.b, Prec<T>::A(l), x, bb, r, -1);
+    LAUNCH_SM(h, Prec<T>::tri, lg, lb, lsm, l.b, zero_guess ? bb : r, Asp, Prec<T>::inv(l), Prec<T>::cp(l), x,
+              omega, zero_guess ? 1 : 0, -1);
+  } else {
+    if (zero_guess) cudaMemsetAsync(x, 0, l.b.n() * sizeof(T), h->stream);
+    for (int color = 0; color < 2; color++) {
+      const bool skip_res = zero_guess && color == 0;  // x = 0: r = rhs
+      if (!skip_res) LAUNCH(h, Prec<T>::residual, box_grid(l.b), 128, l.b, Prec<T>::A(l), x, bb, r, color);
+      LAUNCH_SM(h, Prec<T>::tri, lg, lb, lsm, l.b, skip_res ? bb : r, Asp, Prec<T>::inv(l), Prec<T>::cp(l), x,
+                omega, 0, color);
+    }
+  }
+  prof_end(h, li);
+}
+
+template <typename T>
+void vcycle(vfs_poisson *h, int li, int nu1, int nu2, T omega, int smoother) {
   Level &l = h->L[li];
   T **v = Prec<T>::v(l);
   T *x = v[0], *bb = v[1], *r = v[2], *t = v[3];
@@ -477,24 +561,16 @@ void vcycle(vfs_poisson *h, int li, int nu1, int nu2, T omega) {
     Prec<T>::xfinal(l) = x;
     return;
   }
-  dim3 lb(32, 4), lg((l.b.nx + 31) / 32, (l.b.nz + 3) / 4);
   if (nu1 == 0) cudaMemsetAsync(x, 0, l.b.n() * sizeof(T), h->stream);
-  for (int s = 0; s < nu1; s++) {
-    LAUNCH(h, Prec<T>::sweep, lg, lb, l.b, Prec<T>::A(l), Prec<T>::inv(l), Prec<T>::cp(l), x, bb, t, omega,
-           s == 0 ? 1 : 0);
-    std::swap(x, t);
-  }
-  LAUNCH(h, Prec<T>::residual, box_grid(l.b), 128, l.b, Prec<T>::A(l), x, bb, r);
+  for (int s = 0; s < nu1; s++) smooth<T>(h, l, li, smoother, s == 0, omega, x, t, bb, r);
+  LAUNCH(h, Prec<T>::residual, box_grid(l.b), 128, l.b, Prec<T>::A(l), x, bb, r, -1);
   Level &q = h->L[li + 1];
   LAUNCH(h, Prec<T>::restrict_, box_grid(q.b), 128, l.b, q.b, l.cx, l.cy, l.cz, r, Prec<T>::w(l), q.blank,
          Prec<T>::v(q)[1]);
-  vcycle<T>(h, li + 1, nu1, nu2, omega);
+  vcycle<T>(h, li + 1, nu1, nu2, omega, smoother);
   LAUNCH(h, Prec<T>::prolong, box_grid(l.b), 128, l.b, q.b, l.cx, l.cy, l.cz, (const T *)Prec<T>::xfinal(q), q.blank,
          l.blank, x, 1);
-  for (int s = 0; s < nu2; s++) {
-    LAUNCH(h, Prec<T>::sweep, lg, lb, l.b, Prec<T>::A(l), Prec<T>::inv(l), Prec<T>::cp(l), x, bb, t, omega, 0);
-    std::swap(x, t);
-  }
+  for (int s = 0; s < nu2; s++) smooth<T>(h, l, li, smoother, false, omega, x, t, bb, r);
   Prec<T>::xfinal(l) = x;
 }
 
@@ -502,17 +578,20 @@ void vcycle(vfs_poisson *h, int li, int nu1, int nu2, T omega) {
 template <typename T>
 int run_vcycle(vfs_poisson *h, const vfs_solve_opts &o) {
   const int p = std::is_same<T, float>::value ? 0 : 1;
-  if (!o.use_graphs) {
-    vcycle<T>(h, 0, o.nu1, o.nu2, (T)o.omega);
+  if (!o.use_graphs || h->prof) {  // live kernel timing runs the V-cycle without a graph
+    h->pcount = 0;
+    vcycle<T>(h, 0, o.nu1, o.nu2, (T)o.omega, o.smoother);
     return VFS_OK;
   }
-  if (!h->gexec[p] || h->gparams[p][0] != o.nu1 || h->gparams[p][1] != o.nu2 || h->gomega[p] != o.omega) {
+  if (!h->gexec[p] || h->gparams[p][0] != o.nu1 || h->gparams[p][1] != o.nu2 || h->gomega[p] != o.omega ||
+      h->gparams[p][2] != (int)h->prof || h->gparams[p][3] != o.smoother) {
+    h->pcount = 0;
     if (h->gexec[p]) cudaGraphExecDestroy(h->gexec[p]);
     h->gexec[p] = nullptr;
     cudaGraph_t graph;
     int64_t before = h->launches;
     CUDA_TRY(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
-    vcycle<T>(h, 0, o.nu1, o.nu2, (T)o.omega);
+    vcycle<T>(h, 0, o.nu1, o.nu2, (T)o.omega, o.smoother);
     CUDA_TRY(cudaStreamEndCapture(h->stream, &graph));
     h->gnodes[p] = h->launches - before;
     h->launches = before;
@@ -525,6 +604,8 @@ int run_vcycle(vfs_poisson *h, const vfs_solve_opts &o) {
     }
     h->gparams[p][0] = o.nu1;
     h->gparams[p][1] = o.nu2;
+    h->gparams[p][2] = (int)h->prof;
+    h->gparams[p][3] = o.smoother;
     h->gomega[p] = o.omega;
   }
   CUDA_TRY(cudaGraphLaunch(h->gexec[p], h->stream));
@@ -548,9 +629,25 @@ int precondition(vfs_poisson *h, const double *v, double s, double *z, const vfs
   return VFS_OK;
 }
 
+// Add the level-0 sweep timings of the last V-cycle (the stream has been
+// synchronised since it ran).
+void prof_collect(vfs_poisson *h) {
+  if (!h->prof) return;
+  for (int q = 0; q < h->pcount; q++) {
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, h->pev[0][q], h->pev[1][q]) == cudaSuccess) {
+      h->prof_ms += ms;
+      h->prof_bytes += h->pbytes[q];
+      h->prof_launches++;
+    } else {
+      cudaGetLastError();
+    }
+  }
+}
+
 // reduce `nrow` rows of `nb` partials on the device and read them back
 int reduce_read(vfs_poisson *h, int nb, int nrow, double *out) {
-  LAUNCH(h, k_reduce_rows, 1, 1024, h->partial, nb, nrow, h->red);
+  LAUNCH(h, k_reduce_rows, nrow, 1024, h->partial, nb, nrow, h->red);
   CUDA_TRY(cudaMemcpyAsync(h->hbuf, h->red, nrow * 8, cudaMemcpyDeviceToHost, h->stream));
   TRY(sync(h));
   for (int q = 0; q < nrow; q++) out[q] = h->hbuf[q];
@@ -575,14 +672,15 @@ int ensure_krylov(vfs_poisson *h, int m) {
   const size_t n = h->box.n();
   for (int q = 0; q <= m; q++) TRY(dalloc(h, &h->V[q], n));
   for (int q = 0; q < m; q++) TRY(dalloc(h, &h->Z[q], n));
-  dfree(h, h->dV); dfree(h, h->dZ); dfree(h, h->coef);
+  dfree(h, h->dV); dfree(h, h->dZ); dfree(h, h->coef); dfree(h, h->dsv);
+  TRY(dalloc(h, &h->dsv, m + 1));
   TRY(dalloc(h, &h->dV, m + 1));
   TRY(dalloc(h, &h->dZ, m));
   TRY(dalloc(h, &h->coef, m + 1));
   CUDA_TRY(cudaMemcpyAsync(h->dV, h->V.data(), (m + 1) * sizeof(double *), cudaMemcpyHostToDevice, h->stream));
   CUDA_TRY(cudaMemcpyAsync(h->dZ, h->Z.data(), m * sizeof(double *), cudaMemcpyHostToDevice, h->stream));
   if (h->hbuf) cudaFreeHost(h->hbuf);
-  CUDA_TRY(cudaMallocHost(&h->hbuf, (m + 8) * 8 * 4));
+  CUDA_TRY(cudaMallocHost(&h->hbuf, 512 * 8));
   h->m_alloc = m;
   return sync(h);
 }
@@ -590,7 +688,7 @@ int ensure_krylov(vfs_poisson *h, int m) {
 int check_opts(const vfs_solve_opts &o) {
   if (!(o.rtol > 0) || o.max_it < 1 || o.restart < 1 || o.restart > 64 || o.nu1 < 0 || o.nu2 < 0 ||
       o.nu1 + o.nu2 < 1 || o.nu1 > 8 || o.nu2 > 8 || !(o.omega > 0 && o.omega <= 1.5) ||
-      (o.precision != 0 && o.precision != 1))
+      (o.precision != 0 && o.precision != 1) || o.smoother < 0 || o.smoother > 2)
     return fail(VFS_EINVAL, "invalid solver options");
   return VFS_OK;
 }
@@ -608,7 +706,7 @@ int fgmres(vfs_poisson *h, const vfs_solve_opts &o, vfs_solve_stats *st) {
   const double bn = std::sqrt(bn2);
   int it = 0;
   double rel = 0., beta = 0.;
-  std::vector<double> H((size_t)(m + 1) * m, 0.), cs(m), sn(m), gv(m + 1), y(m), sv(m + 1), hc(m + 2);
+  std::vector<double> H((size_t)(m + 1) * m, 0.), cs(m), sn(m), gv(m + 1), y(m), sv(m + 1);
   if (bn == 0.) {
     CUDA_TRY(cudaMemsetAsync(h->x, 0, n * 8, h->stream));
     st->initial_rel_residual = 0.;
@@ -621,6 +719,7 @@ int fgmres(vfs_poisson *h, const vfs_solve_opts &o, vfs_solve_stats *st) {
   st->initial_rel_residual = rel;
   while (rel > o.rtol && it < o.max_it) {
     sv[0] = 1.0 / beta;
+    CUDA_TRY(cudaMemcpyAsync(h->dsv, sv.data(), 8, cudaMemcpyHostToDevice, h->stream));
     std::fill(gv.begin(), gv.end(), 0.);
     gv[0] = beta;
     int jj = 0;
@@ -628,29 +727,30 @@ int fgmres(vfs_poisson *h, const vfs_solve_opts &o, vfs_solve_stats *st) {
       TRY(precondition(h, h->V[jj], sv[jj], h->Z[jj], o));
       double *w = h->V[jj + 1];
       LAUNCH(h, k_apply64, box_grid(h->box), 128, h->box, h->A0, h->Z[jj], w);
-      // classical Gram-Schmidt, one pass plus a DGKS re-orthogonalisation
-      LAUNCH(h, k_dots, nbd, 256, n, jj + 1, (const double *const *)h->dV, w, h->partial);
-      TRY(reduce_read(h, nbd, jj + 2, hc.data()));
-      double ww = hc[jj + 1], wn = 0.;
-      for (int i = 0; i <= jj; i++) { H[(size_t)i * m + jj] = hc[i] * sv[i]; hc[i] = H[(size_t)i * m + jj] * sv[i]; }
-      CUDA_TRY(cudaMemcpyAsync(h->coef, hc.data(), (jj + 1) * 8, cudaMemcpyHostToDevice, h->stream));
-      LAUNCH(h, k_gs_update, nbd, 256, n, jj + 1, (const double *const *)h->dV, h->coef, w, h->partial);
-      TRY(reduce_read(h, nbd, 1, &wn));
-      if (std::sqrt(wn) < 0.7 * std::sqrt(ww)) {
+      // classical Gram-Schmidt with the coefficients formed on the device and
+      // one read-back per step; a DGKS re-orthogonalisation pass runs when
+      // the update removed more than half of ||w|| (a second read-back).
+      double ww = 0., wn = 0.;
+      for (int pass = 0; pass < 2; pass++) {
+        double *dred = h->red, *dh = h->red + 128, *dwn = h->red + 256;
         LAUNCH(h, k_dots, nbd, 256, n, jj + 1, (const double *const *)h->dV, w, h->partial);
-        TRY(reduce_read(h, nbd, jj + 2, hc.data()));
-        for (int i = 0; i <= jj; i++) {
-          double c2 = hc[i] * sv[i];
-          H[(size_t)i * m + jj] += c2;
-          hc[i] = c2 * sv[i];
-        }
-        CUDA_TRY(cudaMemcpyAsync(h->coef, hc.data(), (jj + 1) * 8, cudaMemcpyHostToDevice, h->stream));
+        LAUNCH(h, k_reduce_rows, jj + 2, 1024, h->partial, nbd, jj + 2, dred);
+        LAUNCH(h, k_gs_coef, 1, 64, jj + 1, dred, h->dsv, dh, h->coef);
         LAUNCH(h, k_gs_update, nbd, 256, n, jj + 1, (const double *const *)h->dV, h->coef, w, h->partial);
-        TRY(reduce_read(h, nbd, 1, &wn));
+        LAUNCH(h, k_reduce_rows, 1, 1024, h->partial, nbd, 1, dwn);
+        CUDA_TRY(cudaMemcpyAsync(h->hbuf, h->red, 257 * 8, cudaMemcpyDeviceToHost, h->stream));
+        TRY(sync(h));
+        if (pass == 0) prof_collect(h);
+        if (pass == 0) ww = h->hbuf[jj + 1];
+        for (int i = 0; i <= jj; i++) H[(size_t)i * m + jj] = (pass ? H[(size_t)i * m + jj] : 0.) + h->hbuf[128 + i];
+        wn = h->hbuf[256];
+        if (!(std::sqrt(wn) < 0.7 * std::sqrt(ww))) break;
+        ww = wn;
       }
       double hn = std::sqrt(wn);
       H[(size_t)(jj + 1) * m + jj] = hn;
       sv[jj + 1] = hn > 0. ? 1.0 / hn : 0.;
+      CUDA_TRY(cudaMemcpyAsync(h->dsv + jj + 1, &sv[jj + 1], 8, cudaMemcpyHostToDevice, h->stream));
       for (int i = 0; i < jj; i++) {
         double a = H[(size_t)i * m + jj], b2 = H[(size_t)(i + 1) * m + jj];
         H[(size_t)i * m + jj] = cs[i] * a + sn[i] * b2;
@@ -697,10 +797,11 @@ void vfs_poisson_default_opts(vfs_solve_opts *o) {
   o->precision = 0;
   o->nu1 = 2;
   o->nu2 = 2;
-  o->omega = 0.8;
+  o->omega = 1.0;
   o->use_graphs = 1;
   o->coarsest_max = 128;
   o->warm_start = 0;
+  o->smoother = 2;
 }
 
 int vfs_poisson_create(const vfs_grid_desc *gd, vfs_poisson **out) {
@@ -712,8 +813,10 @@ int vfs_poisson_create(const vfs_grid_desc *gd, vfs_poisson **out) {
              pz = gd->k_periodic || gd->kk_periodic;
   if ((px && nx < 3) || (py && ny < 3) || (pz && nz < 3))
     return fail(VFS_EINVAL, "a periodic direction needs at least 3 interior cells");
-  if ((size_t)gd->mx * gd->my * gd->mz > ((size_t)1 << 31))
-    return fail(VFS_EINVAL, "grid larger than 2^31 points");
+  if (ny > 24 * kLineChunk)
+    return fail(VFS_EINVAL, "j-lines longer than " + std::to_string(24 * kLineChunk) + " cells are not supported");
+  if ((size_t)gd->mx * gd->my * gd->mz * NSLOT >= ((size_t)1 << 32))
+    return fail(VFS_EINVAL, "grid too large: 19 operator planes must stay below 2^32 entries");
   vfs_poisson *h = new vfs_poisson();
   h->desc = *gd;
   h->g = Grid{gd->mx, gd->my, gd->mz, px, py, pz};
@@ -727,6 +830,8 @@ int vfs_poisson_create(const vfs_grid_desc *gd, vfs_poisson **out) {
   }
   cudaEventCreate(&h->ev0);
   cudaEventCreate(&h->ev1);
+  for (int a = 0; a < 2; a++)
+    for (int q = 0; q < 16; q++) cudaEventCreate(&h->pev[a][q]);
   const size_t N = h->g.n(), n = h->box.n();
   int rc;
   if ((rc = dalloc(h, &h->coor, 3 * N)) || (rc = dalloc(h, &h->nvert, N)) || (rc = dalloc(h, &h->ucont, 3 * N)) ||
@@ -735,7 +840,7 @@ int vfs_poisson_create(const vfs_grid_desc *gd, vfs_poisson **out) {
       (rc = dalloc(h, &h->scale, n)) || (rc = dalloc(h, &h->pc, 12 * n)) || (rc = dalloc(h, &h->aj_box, n)) ||
       (rc = dalloc(h, &h->rowtype0, n)) || (rc = dalloc(h, &h->fluid, n)) || (rc = dalloc(h, &h->gid_box, n)) ||
       (rc = dalloc(h, &h->gid_da, N)) || (rc = dalloc(h, &h->b, n)) || (rc = dalloc(h, &h->x, n)) ||
-      (rc = dalloc(h, &h->r, n)) || (rc = dalloc(h, &h->red, 128)) || (rc = dalloc(h, &h->total, 1)))
+      (rc = dalloc(h, &h->r, n)) || (rc = dalloc(h, &h->red, 512)) || (rc = dalloc(h, &h->total, 1)))
     return bail(rc);
   const int nblk = (int)((n + 1023) / 1024);
   if ((rc = dalloc(h, &h->blk, nblk))) return bail(rc);
@@ -758,7 +863,10 @@ void vfs_poisson_destroy(vfs_poisson *h) {
   if (h->hbuf) cudaFreeHost(h->hbuf);
   if (h->ev0) cudaEventDestroy(h->ev0);
   if (h->ev1) cudaEventDestroy(h->ev1);
-  if (h->stream) cudaStreamDestroy(h->stream);
+  for (int a = 0; a < 2; a++)
+    for (int q = 0; q < 16; q++)
+      if (h->pev[a][q]) cudaEventDestroy(h->pev[a][q]);
+  if (h->stream && h->own_stream) cudaStreamDestroy(h->stream);
   cudaGetLastError();
   delete h;
 }
@@ -828,7 +936,7 @@ int vfs_poisson_rhs(vfs_poisson *h, const double *ucont, double dt, double st, d
   TRY(upload(h, h->ucont, ucont, 3 * N));
   LAUNCH(h, k_rhs, kRedBlocks, 256, h->g, h->box, h->nvert, h->ucont, h->met.aj, dt, st, coeff, h->b, h->partial);
   if (h->desc.bctype3 != -10) {  // Remove_Nullspace_Scale
-    LAUNCH(h, k_reduce_rows, 1, 1024, h->partial, kRedBlocks, 2, h->red);
+    LAUNCH(h, k_reduce_rows, 2, 1024, h->partial, kRedBlocks, 2, h->red);
     LAUNCH(h, k_rhs_nullspace, kRedBlocks, 256, h->g, h->box, h->nvert, h->met.aj, h->red, h->b);
   }
   TRY(sync(h));
@@ -855,7 +963,7 @@ int vfs_poisson_solve(vfs_poisson *h, double *phi, const vfs_solve_opts *opts, v
   TRY(fgmres(h, o, &st));
   if (h->desc.bctype3 != -10) {  // Remove_Nullspace of phi
     LAUNCH(h, k_mean_partial, kRedBlocks, 256, h->box, h->fluid, h->x, h->partial);
-    LAUNCH(h, k_reduce_rows, 1, 1024, h->partial, kRedBlocks, 2, h->red);
+    LAUNCH(h, k_reduce_rows, 2, 1024, h->partial, kRedBlocks, 2, h->red);
     LAUNCH(h, k_shift_fluid, kRedBlocks, 256, h->box, h->fluid, h->red, h->x);
   }
   LAUNCH(h, k_box_to_da_phi, da_grid(h->g), 128, h->g, h->box, h->nvert, h->x, h->phi_da);
@@ -1058,5 +1166,36 @@ int vfs_poisson_mg_vcycle(vfs_poisson *h, int precision, const double *r, double
 }
 
 int64_t vfs_poisson_kernel_launches(vfs_poisson *h) { return h ? h->launches : 0; }
+
+int vfs_poisson_set_stream(vfs_poisson *h, void *stream) {
+  if (!h) return fail(VFS_EINVAL, "null handle");
+  TRY(sync(h));
+  cudaStream_t st = (cudaStream_t)stream;
+  if (h->own_stream && h->stream) cudaStreamDestroy(h->stream);
+  if (st) {
+    h->stream = st;
+    h->own_stream = false;
+  } else {
+    CUDA_TRY(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+    h->own_stream = true;
+  }
+  return VFS_OK;
+}
+
+int vfs_poisson_profile(vfs_poisson *h, int enable) {
+  if (!h) return fail(VFS_EINVAL, "null handle");
+  h->prof = enable != 0;
+  h->prof_ms = h->prof_bytes = 0.;
+  h->prof_launches = 0;
+  return VFS_OK;
+}
+
+int vfs_poisson_profile_read(vfs_poisson *h, double *ms, double *bytes, int64_t *launches) {
+  if (!h || !ms || !bytes || !launches) return fail(VFS_EINVAL, "null argument");
+  *ms = h->prof_ms;
+  *bytes = h->prof_bytes;
+  *launches = h->prof_launches;
+  return VFS_OK;
+}
 
 }  // extern "C"

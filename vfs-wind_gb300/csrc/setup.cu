@@ -563,15 +563,15 @@ __global__ void k_rhs(Grid g, Box b, const double *__restrict__ nvert, const dou
   if (threadIdx.x == 0) { partial[blockIdx.x] = tb; partial[gridDim.x + blockIdx.x] = ta; }
 }
 
-// sums `nrow` rows of `nb` block partials each, in a fixed tree order
+// sums row blockIdx.x of `nb` block partials in a fixed tree order (launch
+// one block per row)
 __global__ void k_reduce_rows(const double *partial, int nb, int nrow, double *out) {
-  for (int r = 0; r < nrow; r++) {
-    double s = 0;
-    for (int q = threadIdx.x; q < nb; q += blockDim.x) s += partial[(size_t)r * nb + q];
-    s = block_sum(s);
-    if (threadIdx.x == 0) out[r] = s;
-    __syncthreads();
-  }
+  const int r = blockIdx.x;
+  if (r >= nrow) return;
+  double s = 0;
+  for (int q = threadIdx.x; q < nb; q += blockDim.x) s += partial[(size_t)r * nb + q];
+  s = block_sum(s);
+  if (threadIdx.x == 0) out[r] = s;
 }
 
 __global__ void k_rhs_nullspace(Grid g, Box b, const double *__restrict__ nvert, const double *__restrict__ aj,

@@ -10,14 +10,15 @@
 namespace vfs {
 
 // r = rhs - A x for one level (A holds 19 box-layout planes).
+// `color` >= 0 restricts the rows to the k-planes with k % 2 == color.
 template <typename T>
 __device__ __forceinline__ void residual_body(Box b, const T *__restrict__ A, const T *__restrict__ x,
-                                                  const T *__restrict__ rhs, T *__restrict__ r) {
+                                              const T *__restrict__ rhs, T *__restrict__ r, int color) {
   int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y, k = blockIdx.z;
-  if (i >= b.nx) return;
-  size_t idx[NSLOT];
+  if (i >= b.nx || (color >= 0 && (k & 1) != color)) return;
+  uint32_t idx[NSLOT];
   stencil_index(b, i, j, k, idx);
-  const size_t n = b.n(), c = idx[CP];
+  const uint32_t n = (uint32_t)b.n(), c = idx[CP];
   T s = (T)0;
 #pragma unroll
   for (int q = 0; q < NSLOT; q++) s += __ldcs(&A[q * n + c]) * __ldg(&x[idx[q]]);
@@ -29,9 +30,9 @@ __global__ void __launch_bounds__(256) k_apply64(Box b, const double *__restrict
                                                  double *__restrict__ y) {
   int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y, k = blockIdx.z;
   if (i >= b.nx) return;
-  size_t idx[NSLOT];
+  uint32_t idx[NSLOT];
   stencil_index(b, i, j, k, idx);
-  const size_t n = b.n(), c = idx[CP];
+  const uint32_t n = (uint32_t)b.n(), c = idx[CP];
   double s = 0.;
 #pragma unroll
   for (int q = 0; q < NSLOT; q++) s = fma(__ldcs(&A[q * n + c]), __ldg(&x[idx[q]]), s);
@@ -45,9 +46,9 @@ __global__ void __launch_bounds__(256) k_residual64(Box b, const double *__restr
   int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y, k = blockIdx.z;
   double rr = 0.;
   if (i < b.nx) {
-    size_t idx[NSLOT];
+    uint32_t idx[NSLOT];
     stencil_index(b, i, j, k, idx);
-    const size_t n = b.n(), c = idx[CP];
+    const uint32_t n = (uint32_t)b.n(), c = idx[CP];
     double s = 0.;
 #pragma unroll
     for (int q = 0; q < NSLOT; q++) s = fma(__ldcs(&A[q * n + c]), __ldg(&x[idx[q]]), s);
@@ -85,56 +86,228 @@ __device__ __forceinline__ void line_lu_body(Box b, const double *__restrict__ A
 }
 
 // One damped j-line Jacobi sweep: for each (i,k) column solve the
-// tridiagonal j-line system with the off-line neighbours taken from x, then
+// tridiagonal j-line system (slots S, CP, N; LU factors inv/cp of the whole
+// line) with the off-line neighbours taken from x, then
 // xo = x + omega (line solution - x).  zero_guess skips the x terms.
-template <typename T>
+//
+// The line is split into chunks of M cells, one thread per chunk, so a column
+// is worked on by P = ceil(ny/M) threads (blockDim = (32 columns, P)).  Both
+// Thomas recurrences are first-order linear recurrences, y_j = alpha_j +
+// beta_j y_{j-1} and x_j = y_j + gamma_j x_{j+1}: each chunk runs its part
+// with a zero incoming value while accumulating the product of its
+// coefficients, a P-step scan over the chunk ends in shared memory supplies
+// the true incoming values, and each chunk adds incoming * product.  This is
+// the same arithmetic as a serial Thomas sweep up to rounding, with a
+// dependent chain of about 2(M + P) steps instead of 2 ny.
+template <typename T, int M>
 __device__ __forceinline__ void line_sweep_body(Box b, const T *__restrict__ A, const T *__restrict__ inv,
-                                                    const T *__restrict__ cp, const T *__restrict__ x,
-                                                    const T *__restrict__ rhs, T *__restrict__ xo, T omega,
-                                                    int zero_guess) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x, k = blockIdx.y * blockDim.y + threadIdx.y;
-  if (i >= b.nx || k >= b.nz) return;
-  const size_t n = b.n();
-  const int ny = b.ny;
-  const int im = i > 0 ? i - 1 : (b.px ? b.nx - 1 : i), ip = i < b.nx - 1 ? i + 1 : (b.px ? 0 : i);
+                                                const T *__restrict__ cp, const T *__restrict__ x,
+                                                const T *__restrict__ rhs, T *__restrict__ xo, T omega,
+                                                int zero_guess) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int tx = threadIdx.x, ty = threadIdx.y, TI = blockDim.x, P = blockDim.y;
+  T *sA = (T *)smem_raw, *sB = sA + P * TI;
+  const int i = blockIdx.x * TI + tx, k = blockIdx.y;
+  const bool valid = i < b.nx;
+  const uint32_t n = (uint32_t)b.n();
+  const int ny = b.ny, j0 = ty * M;
+  const int cnt = valid ? max(0, min(M, ny - j0)) : 0;
+  const int ii = valid ? i : 0;
+  const int im = ii > 0 ? ii - 1 : (b.px ? b.nx - 1 : ii), ip = ii < b.nx - 1 ? ii + 1 : (b.px ? 0 : ii);
   const int km = k > 0 ? k - 1 : (b.pz ? b.nz - 1 : k), kp = k < b.nz - 1 ? k + 1 : (b.pz ? 0 : k);
-  const size_t sj = b.nx;
-  // column bases of the 9 (i,k) neighbours of the line
-  const size_t cC = b.at(i, 0, k), cE = b.at(ip, 0, k), cW = b.at(im, 0, k);
-  const size_t cT = b.at(i, 0, kp), cB = b.at(i, 0, km);
-  const size_t cTE = b.at(ip, 0, kp), cBE = b.at(ip, 0, km), cTW = b.at(im, 0, kp), cBW = b.at(im, 0, km);
-  T yprev = (T)0;
-  for (int j = 0; j < ny; j++) {
-    const size_t o = (size_t)j * sj, c = cC + o;
-    T r = rhs[c];
-    if (!zero_guess) {
-      const size_t om = (size_t)(j > 0 ? j - 1 : (b.py ? ny - 1 : j)) * sj;
-      const size_t op = (size_t)(j < ny - 1 ? j + 1 : (b.py ? 0 : j)) * sj;
-      r -= __ldcs(&A[EP * n + c]) * x[cE + o] + __ldcs(&A[WP * n + c]) * x[cW + o] +
-           __ldcs(&A[TP * n + c]) * x[cT + o] + __ldcs(&A[BP * n + c]) * x[cB + o] +
-           __ldcs(&A[NE * n + c]) * x[cE + op] + __ldcs(&A[SE * n + c]) * x[cE + om] +
-           __ldcs(&A[NW * n + c]) * x[cW + op] + __ldcs(&A[SW * n + c]) * x[cW + om] +
-           __ldcs(&A[TN * n + c]) * x[cT + op] + __ldcs(&A[BN * n + c]) * x[cB + op] +
-           __ldcs(&A[TS * n + c]) * x[cT + om] + __ldcs(&A[BS * n + c]) * x[cB + om] +
-           __ldcs(&A[TE * n + c]) * x[cTE + o] + __ldcs(&A[BE * n + c]) * x[cBE + o] +
-           __ldcs(&A[TW * n + c]) * x[cTW + o] + __ldcs(&A[BW * n + c]) * x[cBW + o];
-      if (b.py) {
-        if (j == 0) r -= A[SP * n + c] * x[cC + (size_t)(ny - 1) * sj];
-        if (j == ny - 1) r -= A[NP * n + c] * x[cC];
+  const uint32_t sj = b.nx;
+  const uint32_t cC = (uint32_t)b.at(ii, 0, k), cE = (uint32_t)b.at(ip, 0, k), cW = (uint32_t)b.at(im, 0, k);
+  const uint32_t cT = (uint32_t)b.at(ii, 0, kp), cB = (uint32_t)b.at(ii, 0, km);
+  const uint32_t cTE = (uint32_t)b.at(ip, 0, kp), cBE = (uint32_t)b.at(ip, 0, km), cTW = (uint32_t)b.at(im, 0, kp),
+                 cBW = (uint32_t)b.at(im, 0, km);
+  T r[M], g[M];
+  // right-hand sides of the chunk's cells (independent loads)
+#pragma unroll
+  for (int q = 0; q < M; q++) {
+    r[q] = (T)0;
+    if (q < cnt) {
+      const int j = j0 + q;
+      const uint32_t o = (uint32_t)j * sj, c = cC + o;
+      T v = rhs[c];
+      if (!zero_guess) {
+        const uint32_t om = (uint32_t)(j > 0 ? j - 1 : (b.py ? ny - 1 : j)) * sj;
+        const uint32_t op = (uint32_t)(j < ny - 1 ? j + 1 : (b.py ? 0 : j)) * sj;
+        v -= __ldcs(&A[EP * n + c]) * x[cE + o] + __ldcs(&A[WP * n + c]) * x[cW + o] +
+             __ldcs(&A[TP * n + c]) * x[cT + o] + __ldcs(&A[BP * n + c]) * x[cB + o] +
+             __ldcs(&A[NE * n + c]) * x[cE + op] + __ldcs(&A[SE * n + c]) * x[cE + om] +
+             __ldcs(&A[NW * n + c]) * x[cW + op] + __ldcs(&A[SW * n + c]) * x[cW + om] +
+             __ldcs(&A[TN * n + c]) * x[cT + op] + __ldcs(&A[BN * n + c]) * x[cB + op] +
+             __ldcs(&A[TS * n + c]) * x[cT + om] + __ldcs(&A[BS * n + c]) * x[cB + om] +
+             __ldcs(&A[TE * n + c]) * x[cTE + o] + __ldcs(&A[BE * n + c]) * x[cBE + o] +
+             __ldcs(&A[TW * n + c]) * x[cTW + o] + __ldcs(&A[BW * n + c]) * x[cBW + o];
+        if (b.py) {
+          if (j == 0) v -= A[SP * n + c] * x[cC + (uint32_t)(ny - 1) * sj];
+          if (j == ny - 1) v -= A[NP * n + c] * x[cC];
+        }
       }
+      r[q] = v;
     }
-    const T a = j > 0 ? __ldcs(&A[SP * n + c]) : (T)0;
-    const T y = (r - a * yprev) * __ldcs(&inv[c]);
-    xo[c] = y;
-    yprev = y;
   }
-  T xn = (T)0;
-  for (int j = ny - 1; j >= 0; j--) {
-    const size_t c = cC + (size_t)j * sj;
-    const T v = xo[c] - (j < ny - 1 ? __ldcs(&cp[c]) * xn : (T)0);
-    xn = v;
-    const T xold = zero_guess ? (T)0 : x[c];
-    xo[c] = xold + omega * (v - xold);
+  // forward recurrence y_j = (r_j - a_j y_{j-1}) inv_j with y_{j0-1} = 0,
+  // g_j = prod_{s=j0..j} (-a_s inv_s)
+  T yp = (T)0, gp = (T)1;
+#pragma unroll
+  for (int q = 0; q < M; q++) {
+    if (q < cnt) {
+      const int j = j0 + q;
+      const uint32_t c = cC + (uint32_t)j * sj;
+      const T a = j > 0 ? __ldcs(&A[SP * n + c]) : (T)0;
+      const T iv = __ldcs(&inv[c]);
+      const T y = (r[q] - a * yp) * iv;
+      gp = gp * (-a * iv);
+      r[q] = y;
+      g[q] = gp;
+      yp = y;
+    }
+  }
+  sA[ty * TI + tx] = yp;  // chunk-end y and coefficient product (0 and 1 when empty)
+  sB[ty * TI + tx] = gp;
+  __syncthreads();
+  if (ty == 0) {  // incoming y_{j0-1} of every chunk
+    T Y = (T)0;
+    for (int t = 0; t < P; t++) {
+      const T e = sA[t * TI + tx], G = sB[t * TI + tx];
+      sA[t * TI + tx] = Y;
+      Y = e + G * Y;
+    }
+  }
+  __syncthreads();
+  const T yin = sA[ty * TI + tx];
+#pragma unroll
+  for (int q = 0; q < M; q++) r[q] += g[q] * yin;
+  __syncthreads();
+  // backward recurrence x_j = y_j - cp_j x_{j+1} with x_{j0+cnt} = 0,
+  // g_j = prod_{s=j..end} (-cp_s)
+  T xn = (T)0, hp = (T)1;
+#pragma unroll
+  for (int q = M - 1; q >= 0; q--) {
+    if (q < cnt) {
+      const int j = j0 + q;
+      const uint32_t c = cC + (uint32_t)j * sj;
+      const T cv = j < ny - 1 ? __ldcs(&cp[c]) : (T)0;
+      const T v = r[q] - cv * xn;
+      hp = hp * (-cv);
+      r[q] = v;
+      g[q] = hp;
+      xn = v;
+    }
+  }
+  sA[ty * TI + tx] = xn;  // chunk-start x and coefficient product
+  sB[ty * TI + tx] = hp;
+  __syncthreads();
+  if (ty == 0) {  // incoming x_{end+1} of every chunk
+    T X = (T)0;
+    for (int t = P - 1; t >= 0; t--) {
+      const T e = sA[t * TI + tx], H = sB[t * TI + tx];
+      sA[t * TI + tx] = X;
+      X = e + H * X;
+    }
+  }
+  __syncthreads();
+  const T xin = sA[ty * TI + tx];
+#pragma unroll
+  for (int q = 0; q < M; q++) {
+    if (q < cnt) {
+      const uint32_t c = cC + (uint32_t)(j0 + q) * sj;
+      const T v = r[q] + g[q] * xin;
+      const T xold = zero_guess ? (T)0 : x[c];
+      xo[c] = xold + omega * (v - xold);
+    }
+  }
+}
+
+// Tridiagonal j-line correction of a line-relaxation sweep in correction
+// form: with r = rhs - A x already formed, solve L d = r on every (i,k)
+// column (L = the line part S, CP, N of A, factors inv/cp) and update
+// x += omega d (x = omega d when zero_guess, r then being the right-hand
+// side).  `color` >= 0 restricts the update to the k-planes with
+// k % 2 == color (zebra ordering by planes).  Same chunked recurrences and scans as
+// line_sweep_body; only 5 words per cell are streamed.
+template <typename T, int M>
+__device__ __forceinline__ void line_tri_body(Box b, const T *__restrict__ r, const T *__restrict__ Asp,
+                                              const T *__restrict__ inv, const T *__restrict__ cp, T *x, T omega,
+                                              int zero_guess, int color) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int tx = threadIdx.x, ty = threadIdx.y, TI = blockDim.x, P = blockDim.y;
+  T *sA = (T *)smem_raw, *sB = sA + P * TI;
+  const int i = blockIdx.x * TI + tx, k = blockIdx.y;
+  const bool valid = i < b.nx && (color < 0 || (k & 1) == color);
+  const int ny = b.ny, j0 = ty * M;
+  const int cnt = valid ? max(0, min(M, ny - j0)) : 0;
+  const uint32_t sj = b.nx, cC = valid ? (uint32_t)b.at(i, 0, k) : 0u;
+  T y[M], g[M];
+  T yp = (T)0, gp = (T)1;
+#pragma unroll
+  for (int q = 0; q < M; q++) {
+    y[q] = (T)0;
+    g[q] = (T)0;
+    if (q < cnt) {
+      const int j = j0 + q;
+      const uint32_t c = cC + (uint32_t)j * sj;
+      const T a = j > 0 ? __ldcs(&Asp[c]) : (T)0;
+      const T iv = __ldcs(&inv[c]);
+      const T v = (__ldcs(&r[c]) - a * yp) * iv;
+      gp = gp * (-a * iv);
+      y[q] = v;
+      g[q] = gp;
+      yp = v;
+    }
+  }
+  sA[ty * TI + tx] = yp;
+  sB[ty * TI + tx] = gp;
+  __syncthreads();
+  if (ty == 0) {
+    T Y = (T)0;
+    for (int t = 0; t < P; t++) {
+      const T e = sA[t * TI + tx], G = sB[t * TI + tx];
+      sA[t * TI + tx] = Y;
+      Y = e + G * Y;
+    }
+  }
+  __syncthreads();
+  const T yin = sA[ty * TI + tx];
+#pragma unroll
+  for (int q = 0; q < M; q++) y[q] += g[q] * yin;
+  __syncthreads();
+  T xn = (T)0, hp = (T)1;
+#pragma unroll
+  for (int q = M - 1; q >= 0; q--) {
+    if (q < cnt) {
+      const int j = j0 + q;
+      const uint32_t c = cC + (uint32_t)j * sj;
+      const T cv = j < ny - 1 ? __ldcs(&cp[c]) : (T)0;
+      const T v = y[q] - cv * xn;
+      hp = hp * (-cv);
+      y[q] = v;
+      g[q] = hp;
+      xn = v;
+    }
+  }
+  sA[ty * TI + tx] = xn;
+  sB[ty * TI + tx] = hp;
+  __syncthreads();
+  if (ty == 0) {
+    T X = (T)0;
+    for (int t = P - 1; t >= 0; t--) {
+      const T e = sA[t * TI + tx], H = sB[t * TI + tx];
+      sA[t * TI + tx] = X;
+      X = e + H * X;
+    }
+  }
+  __syncthreads();
+  const T xin = sA[ty * TI + tx];
+#pragma unroll
+  for (int q = 0; q < M; q++) {
+    if (q < cnt) {
+      const uint32_t c = cC + (uint32_t)(j0 + q) * sj;
+      const T d = y[q] + g[q] * xin;
+      x[c] = (zero_guess ? (T)0 : x[c]) + omega * d;
+    }
   }
 }
 
@@ -245,13 +418,18 @@ __global__ void k_sumsq(size_t n, const double *__restrict__ x, double *partial)
 }
 
 #define TYPED(T, S)                                                                                        \
-  __global__ void __launch_bounds__(256) k_residual_##S(Box b, const T *A, const T *x, const T *rhs, T *r) {  \
-    residual_body<T>(b, A, x, rhs, r);                                                                     \
+  __global__ void __launch_bounds__(256) k_residual_##S(Box b, const T *A, const T *x, const T *rhs, T *r,  \
+                                                        int color) {                                       \
+    residual_body<T>(b, A, x, rhs, r, color);                                                              \
   }                                                                                                        \
   __global__ void k_line_lu_##S(Box b, const double *A64, T *inv, T *cp) { line_lu_body<T>(b, A64, inv, cp); } \
-  __global__ void __launch_bounds__(128) k_line_sweep_##S(Box b, const T *A, const T *inv, const T *cp,       \
-                                                          const T *x, const T *rhs, T *xo, T omega, int zg) { \
-    line_sweep_body<T>(b, A, inv, cp, x, rhs, xo, omega, zg);                                              \
+  __global__ void __launch_bounds__(768, 1) k_line_sweep_##S(Box b, const T *A, const T *inv, const T *cp,      \
+                                                           const T *x, const T *rhs, T *xo, T omega, int zg) { \
+    line_sweep_body<T, kLineChunk>(b, A, inv, cp, x, rhs, xo, omega, zg);                                   \
+  }                                                                                                        \
+  __global__ void __launch_bounds__(768) k_line_tri_##S(Box b, const T *r, const T *Asp, const T *inv,          \
+                                                       const T *cp, T *x, T omega, int zg, int color) {        \
+    line_tri_body<T, kLineChunk>(b, r, Asp, inv, cp, x, omega, zg, color);                                    \
   }                                                                                                        \
   __global__ void k_coarsest_##S(int nd, const int *didx, const double *dinv, const T *rhs, T *x, size_t n) { \
     coarsest_body<T>(nd, didx, dinv, rhs, x, n);                                                           \

@@ -32,6 +32,7 @@ EXPORTS = [
     "vfs_poisson_get_metric", "vfs_poisson_get_rhs", "vfs_poisson_apply", "vfs_poisson_mg_levels",
     "vfs_poisson_mg_level_info", "vfs_poisson_mg_get_nvert", "vfs_poisson_mg_restrict",
     "vfs_poisson_mg_interpolate", "vfs_poisson_mg_vcycle", "vfs_poisson_kernel_launches",
+    "vfs_poisson_set_stream", "vfs_poisson_profile", "vfs_poisson_profile_read",
 ]
 
 
@@ -45,7 +46,7 @@ class GridDesc(C.Structure):
 class SolveOpts(C.Structure):
     _fields_ = [("rtol", C.c_double), ("max_it", C.c_int), ("restart", C.c_int), ("precision", C.c_int),
                 ("nu1", C.c_int), ("nu2", C.c_int), ("omega", C.c_double), ("use_graphs", C.c_int),
-                ("coarsest_max", C.c_int), ("warm_start", C.c_int)]
+                ("coarsest_max", C.c_int), ("warm_start", C.c_int), ("smoother", C.c_int)]
 
 
 class SolveStats(C.Structure):
@@ -99,6 +100,9 @@ def load(path=LIB_PATH):
     L.vfs_poisson_mg_vcycle.argtypes = [vp, C.c_int, dp, dp]
     L.vfs_poisson_kernel_launches.argtypes = [vp]
     L.vfs_poisson_kernel_launches.restype = C.c_int64
+    L.vfs_poisson_set_stream.argtypes = [vp, vp]
+    L.vfs_poisson_profile.argtypes = [vp, C.c_int]
+    L.vfs_poisson_profile_read.argtypes = [vp, P(C.c_double), P(C.c_double), P(C.c_int64)]
     _lib = L
     return L
 
@@ -273,3 +277,16 @@ class PoissonSolver:
 
     def kernel_launches(self):
         return load().vfs_poisson_kernel_launches(self.h)
+
+    def set_stream(self, stream):
+        """Run on a caller's CUDA stream (an int handle, e.g.
+        torch.cuda.current_stream().cuda_stream); None for a private one."""
+        _check(load().vfs_poisson_set_stream(self.h, stream))
+
+    def profile(self, enable=True):
+        _check(load().vfs_poisson_profile(self.h, int(enable)))
+
+    def profile_read(self):
+        ms, b, n = C.c_double(), C.c_double(), C.c_int64()
+        _check(load().vfs_poisson_profile_read(self.h, C.byref(ms), C.byref(b), C.byref(n)))
+        return ms.value, b.value, n.value

@@ -34,6 +34,14 @@ class Case:
     coeff: float = 1.0
     extra: dict = field(default_factory=dict)
 
+    def set_periodic(self, periodic):
+        """Change the periodic flags and re-sync the nvert ghost layers."""
+        self.periodic = tuple(periodic)
+        self.nvert = sync_periodic_ghosts(self.nvert, self.periodic)
+
+    def __post_init__(self):
+        self.nvert = sync_periodic_ghosts(self.nvert, self.periodic)
+
     @property
     def dims(self):
         return (self.nx + 2, self.ny + 2, self.nz + 2)
@@ -52,18 +60,25 @@ def _geometric(n, ratio):
     return (ratio ** j - 1.0) / (ratio ** n - 1.0)
 
 
-def _nodes(nx, ny, nz, yfun, amp):
-    """Node coordinates on the DA-shaped array; the last layer stays zero."""
+def _nodes(nx, ny, nz, yfun, amp, physical=False):
+    """Node coordinates on the DA-shaped array; the last layer stays zero.
+
+    x = xi + amp sin(2 pi e) sin(2 pi zeta), y = ys(eta) + amp sin(2 pi zeta)
+    sin(2 pi xi), z = zeta + amp sin(2 pi xi) sin(2 pi e), where e is the
+    computational coordinate eta, or with `physical` the stretched height
+    ys(eta) itself, so that the perturbation is smooth in physical space and
+    the wall-resolving cells stay unskewed (terrain-following grid)."""
     xi = np.arange(nx + 1) / nx
     et = np.arange(ny + 1) / ny
     ze = np.arange(nz + 1) / nz
     Z, Y, X = np.meshgrid(ze, et, xi, indexing="ij")  # [k][j][i]
     ys = yfun(Y)
+    E = ys if physical else Y
     tp = 2.0 * np.pi
     coor = np.zeros((nz + 2, ny + 2, nx + 2, 3))
-    coor[: nz + 1, : ny + 1, : nx + 1, 0] = X + amp * np.sin(tp * Y) * np.sin(tp * Z)
+    coor[: nz + 1, : ny + 1, : nx + 1, 0] = X + amp * np.sin(tp * E) * np.sin(tp * Z)
     coor[: nz + 1, : ny + 1, : nx + 1, 1] = ys + amp * np.sin(tp * Z) * np.sin(tp * X)
-    coor[: nz + 1, : ny + 1, : nx + 1, 2] = Z + amp * np.sin(tp * X) * np.sin(tp * Y)
+    coor[: nz + 1, : ny + 1, : nx + 1, 2] = Z + amp * np.sin(tp * X) * np.sin(tp * E)
     return coor
 
 
@@ -92,6 +107,26 @@ def classify(inside):
     nv[0, :, :] = nv[-1, :, :] = 0.0
     nv[:, 0, :] = nv[:, -1, :] = 0.0
     nv[:, :, 0] = nv[:, :, -1] = 0.0
+    return nv
+
+
+def sync_periodic_ghosts(nvert, periodic):
+    """Give the boundary layer of each periodic direction its partner cells'
+    values (index 0 <- m-2, m-1 <- 1), as the ghost points of a periodic DA
+    hold them.  The operator reads nvert at these ghosts
+    (Source/poisson.c:1167-1561), so this keeps blanking consistent across
+    the periodic seam."""
+    nv = nvert.copy()
+    per = [periodic[q] or periodic[q + 3] for q in range(3)]
+    if per[0]:
+        nv[:, :, 0] = nv[:, :, -2]
+        nv[:, :, -1] = nv[:, :, 1]
+    if per[1]:
+        nv[:, 0, :] = nv[:, -2, :]
+        nv[:, -1, :] = nv[:, 1, :]
+    if per[2]:
+        nv[0, :, :] = nv[-2, :, :]
+        nv[-1, :, :] = nv[1, :, :]
     return nv
 
 
@@ -167,14 +202,14 @@ def cylinder(nx=128, ny=96, nz=128, seed=1002, amp=0.05):
 
 
 def towers(nx=256, ny=192, nz=256, seed=1003, amp=0.02, ratio=1.03, array=(3, 2),
-           radius=0.02):
+           radius=0.02, physical=True):
     """Config 3: wind-farm-like grid, geometric wall stretching (ratio 1.03)
     in y, perturbation amplitude 0.02, periodic x and z, a 3x2 array of
     vertical tower cylinders (radius 0.02, 0.25 streamwise and 0.3 spanwise
     spacing); Fourier-mode Ucont plus noise."""
     rng = np.random.default_rng(seed)
     yc = _geometric(ny, ratio)
-    coor = _nodes(nx, ny, nz, lambda e: np.interp(e, np.arange(ny + 1) / ny, yc), amp)
+    coor = _nodes(nx, ny, nz, lambda e: np.interp(e, np.arange(ny + 1) / ny, yc), amp, physical=physical)
     cc = cell_centres(coor)
     inside = np.zeros(cc.shape[:3], dtype=bool)
     ax, az = array

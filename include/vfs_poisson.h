@@ -182,6 +182,23 @@ int vfs_poisson_set_stream(vfs_poisson *h, void *stream);
 int vfs_poisson_profile(vfs_poisson *h, int enable);
 int vfs_poisson_profile_read(vfs_poisson *h, double *ms, double *bytes, int64_t *launches);
 
+/* Divergence without a handle and without allocating: the same value as
+ * vfs_poisson_divergence, for callers that may not allocate device memory
+ * where they need it (inside a CUDA stream capture, or in codes whose device
+ * memory is owned by their own pool allocator).  No counterpart in the
+ * reference; it restates Divergence (Source/main.c:936-1074) like
+ * vfs_poisson_divergence.  All five arrays must be device memory of the
+ * current device (DA layout; ucont Cmpnts); the result is written to
+ * *maxdiv (device memory) on `stream` (a cudaStream_t, NULL for the default
+ * stream) and the call returns without waiting.  Its scratch is a fixed
+ * device array of 4096 doubles (32 KiB) that every GPU loading the library
+ * keeps until exit, which limits grids to 268,435,456 interior cells (larger
+ * ones return VFS_EINVAL).  The first call on a device looks up that
+ * array's address; make it before any stream capture.  Every call shares the
+ * array, so calls that overlap on the GPU race. */
+int vfs_divergence_noalloc(const vfs_grid_desc *g, const double *ucont, const double *nvert, const double *aj,
+                           double *maxdiv, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

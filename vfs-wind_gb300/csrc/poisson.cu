@@ -784,6 +784,10 @@ int fgmres(vfs_poisson *h, const vfs_solve_opts &o, vfs_solve_stats *st) {
 
 }  // namespace
 
+namespace vfs {
+void set_last_error(const std::string &msg) { g_err = msg; }
+}  // namespace vfs
+
 // ============================== C ABI =====================================
 
 extern "C" {

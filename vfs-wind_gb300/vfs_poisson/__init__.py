@@ -33,6 +33,7 @@ EXPORTS = [
     "vfs_poisson_mg_level_info", "vfs_poisson_mg_get_nvert", "vfs_poisson_mg_restrict",
     "vfs_poisson_mg_interpolate", "vfs_poisson_mg_vcycle", "vfs_poisson_kernel_launches",
     "vfs_poisson_set_stream", "vfs_poisson_profile", "vfs_poisson_profile_read",
+    "vfs_divergence_noalloc",
 ]
 
 
@@ -103,6 +104,7 @@ def load(path=LIB_PATH):
     L.vfs_poisson_set_stream.argtypes = [vp, vp]
     L.vfs_poisson_profile.argtypes = [vp, C.c_int]
     L.vfs_poisson_profile_read.argtypes = [vp, P(C.c_double), P(C.c_double), P(C.c_int64)]
+    L.vfs_divergence_noalloc.argtypes = [P(GridDesc), vp, vp, vp, vp, vp]
     _lib = L
     return L
 

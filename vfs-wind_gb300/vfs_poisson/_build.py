@@ -24,6 +24,7 @@ UNITS = {
     "setup.cu": ["-fmad=false"],
     "solve.cu": [],
     "poisson.cu": [],
+    "noalloc.cu": ["-fmad=false"],
 }
 
 

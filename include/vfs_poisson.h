@@ -28,6 +28,7 @@
  *   Divergence                main.c:936           -> vfs_poisson_divergence
  *   MyRestriction / MyInterpolation / MyNvertRestriction
  *                             poisson.c:365, :527, :1995 -> vfs_poisson_mg_*
+ *   ibm_search_advanced       ibm.c:92             -> vfs_poisson_ibm_search
  */
 #ifndef VFS_POISSON_H
 #define VFS_POISSON_H
@@ -198,6 +199,22 @@ int vfs_poisson_profile_read(vfs_poisson *h, double *ms, double *bytes, int64_t 
  * array, so calls that overlap on the GPU race. */
 int vfs_divergence_noalloc(const vfs_grid_desc *g, const double *ucont, const double *nvert, const double *aj,
                            double *maxdiv, void *stream);
+
+/* Immersed-boundary classification of one body (ibm_search_advanced,
+ * Source/ibm.c:92-594; point_cell_advanced :1075-1200): marks the cells of
+ * nvert (DA layout, in/out) whose centre lies inside the closed triangulated
+ * surface (xyz: n_v vertices x/y/z; tri: n_elmt vertex triples, 0-based) as
+ * 3 and the cells within one node of them as 1, on the cell centres of the
+ * handle's grid (set_grid first).  ibi == 0 first clears every interior
+ * value below 5 (the first body); later bodies keep the larger value.
+ * bctype (six ints or NULL): the rows next to a -1 / -2 wall become 1.
+ * Each cell casts up to 64 rays (the reference's glibc rand() directions)
+ * until one meets no doubled intersection; *n_failed (may be NULL) counts
+ * the cells that gave up, which stay 0 before the dilation.  The result is
+ * bit-identical to the reference's loops.  nvert is not installed as the
+ * solver's blanking: pass it to vfs_poisson_set_nvert. */
+int vfs_poisson_ibm_search(vfs_poisson *h, int ibi, int n_v, const double *xyz, int n_elmt, const int32_t *tri,
+                           const int *bctype, double *nvert, int *n_failed);
 
 #ifdef __cplusplus
 }

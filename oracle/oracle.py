@@ -14,7 +14,8 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
-SOURCES = [os.path.join(HERE, "vfs_oracle.c"), os.path.join(HERE, "mg_solver.c")]
+SOURCES = [os.path.join(HERE, "vfs_oracle.c"), os.path.join(HERE, "mg_solver.c"),
+           os.path.join(HERE, "ibm_oracle.c")]
 
 
 def build(force=False):
@@ -90,6 +91,12 @@ def lib():
         L.or_mg_level_info.argtypes = [C.c_void_p, C.c_int, ip]
         L.or_mg_level_info.restype = C.c_int
         L.or_mg_destroy.argtypes = [C.c_void_p]
+        L.or_mg_set_smoother.argtypes = [C.c_int]
+        L.or_glibc_rand_first.argtypes = [C.c_uint]
+        L.or_glibc_rand_first.restype = C.c_uint
+        L.or_triangle_normals.argtypes = [C.c_int, ip, dp, dp, dp, dp]
+        L.or_ibm_search.argtypes = [P(Dims), dp, C.c_int, C.c_int, dp, dp, dp, C.c_int, ip, ip, dp, C.c_int]
+        L.or_ibm_search.restype = C.c_int
         _lib = L
     return _lib
 
@@ -239,6 +246,24 @@ def interpolation(df, dc, isc, jsc, ksc, nvert_f, nvert_c, xc):
     lib().or_my_interpolation(C.byref(df), C.byref(dc), isc, jsc, ksc, _dp(np.ascontiguousarray(nvert_f)),
                               _dp(np.ascontiguousarray(nvert_c)), _dp(np.ascontiguousarray(xc)), _dp(out))
     return out
+
+
+def glibc_rand_first(seed):
+    return lib().or_glibc_rand_first(seed)
+
+
+def ibm_search(d, cent, surface, nvert=None, ibi=0, bctype=(0, 0, 0, 0, 0, 0), max_tries=64):
+    """ibm_search_advanced for one body; `surface` = (xyz[n_v,3], tris[n_elmt,3] 0-based)."""
+    xyz, tris = surface
+    x = np.ascontiguousarray(xyz[:, 0], np.float64)
+    y = np.ascontiguousarray(xyz[:, 1], np.float64)
+    z = np.ascontiguousarray(xyz[:, 2], np.float64)
+    nv = np.ascontiguousarray(tris, np.int32).ravel()
+    out = np.zeros((d.mz, d.my, d.mx)) if nvert is None else np.ascontiguousarray(nvert, np.float64).copy()
+    bc = np.ascontiguousarray(bctype, np.int32)
+    failed = lib().or_ibm_search(C.byref(d), _dp(np.ascontiguousarray(cent, np.float64)), ibi, len(x), _dp(x),
+                                 _dp(y), _dp(z), len(nv) // 3, _ip(nv), _ip(bc), _dp(out), max_tries)
+    return out, failed
 
 
 class MGSolver:

@@ -88,6 +88,14 @@ void or_my_interpolation(const or_dims *df, const or_dims *dc, int isc, int jsc,
 void or_stencil_apply(const or_dims *d, const int *rowtype, const double *vol,
                       const double *x, double *y);
 
+/* Immersed-boundary classification (oracle/ibm_oracle.c). nv holds the
+ * triangles' 0-based vertex ids, three per triangle. */
+unsigned int or_glibc_rand_first(unsigned int seed);
+void or_triangle_normals(int n_elmt, const int *nv, const double *x, const double *y, const double *z,
+                         double *nf);
+int or_ibm_search(const or_dims *d, const double *cent, int ibi, int n_v, const double *x, const double *y,
+                  const double *z, int n_elmt, const int *nv, const int *bctype, double *nvert, int max_tries);
+
 /* CPU baseline solver (oracle/mg_solver.c). */
 typedef struct {
   int max_it;       /* outer FGMRES iterations          */

@@ -134,3 +134,52 @@ def test_golden_fixtures(name):
     b = O.rhs(d, case.nvert, lhs["gid"], case.ucont, met["aj"])
     np.testing.assert_allclose(b, g["b"], rtol=0, atol=1e-13 * np.abs(g["b"]).max())
     np.testing.assert_array_equal(met["iaj"], g["iaj"])
+
+
+# --- immersed-boundary classification (ibm_search_advanced) ---
+
+def test_glibc_rand_restatement_matches_libc():
+    """The ray directions of point_cell_advanced (Source/ibm.c:1100-1110) use
+    the first rand() after srand(searchtimes); the restated generator must
+    give the C library's own values."""
+    import ctypes
+    libc = ctypes.CDLL(None)
+    libc.srand.argtypes = [ctypes.c_uint]
+    for seed in list(range(0, 130)) + [12345, 2 ** 31 - 1, 2 ** 31, 2 ** 32 - 1]:
+        libc.srand(seed)
+        assert O.glibc_rand_first(seed) == libc.rand(), seed
+
+
+def test_ibm_search_cylinder_matches_geometry():
+    c = CF.cylinder(24, 16, 24)
+    d = O.dims_of(c)
+    met = O.form_metrics(d, c.coor)
+    n = 24
+    surf = CF.rod_surface((0.5, -0.01, 0.5), (0, 1, 0), 1.02, 0.1, n, 8)
+    nv, failed = O.ibm_search(d, met["cent"], surf)
+    assert failed == 0
+    cc = met["cent"][1:-1, 1:-1, 1:-1]
+    r = np.hypot(cc[..., 0] - 0.5, cc[..., 2] - 0.5)
+    inner = nv[1:-1, 1:-1, 1:-1]
+    # inside the inscribed polygon -> solid; outside the circle -> not solid
+    assert np.all(inner[r < 0.1 * np.cos(np.pi / n) - 1e-9] == 3)
+    assert np.all(inner[r > 0.1 + 1e-9] != 3)
+    # interior agrees with the inside/dilation rule used by the generators
+    ref = CF.classify(r < 0.1)
+    np.testing.assert_array_equal(inner, ref[1:-1, 1:-1, 1:-1])
+
+
+def test_ibm_search_multibody_and_walls():
+    c = CF.towers(32, 24, 32, radius=0.05)
+    d = O.dims_of(c)
+    met = O.form_metrics(d, c.coor)
+    nv = np.zeros((d.mz, d.my, d.mx))
+    nv[5, 5, 5] = 7.0                      # >= 5 survives the first body's reset
+    bc = (0, 0, -1, 0, 0, 0)
+    for ibi, surf in enumerate(CF.tower_surfaces(radius=0.05, height=0.6)):
+        nv, failed = O.ibm_search(d, met["cent"], surf, nvert=nv, ibi=ibi, bctype=bc)
+        assert failed == 0
+    inner = nv[1:-1, 1:-1, 1:-1]
+    assert nv[5, 5, 5] == 7.0
+    assert np.all(inner[:, 0, :][inner[:, 0, :] != 7.0] == 1.0)   # j == 1 wall row
+    assert (inner == 3).sum() > 0 and set(np.unique(inner)) <= {0.0, 1.0, 3.0, 7.0}

@@ -82,4 +82,13 @@ __global__ void k_scale_to(size_t n, const double *v, double s, const double *sc
 __global__ void k_to64(size_t n, const float *x32, const double *x64, double s, double *out);
 __global__ void k_sumsq(size_t n, const double *x, double *partial);
 
+// Hand-off from a handle to the surface search (ibm.cu): its stream, grid,
+// DA-layout cell centres and launch counter.
+struct IbmContext {
+  cudaStream_t stream;
+  Grid g;
+  const double *cent;
+  int64_t *launches;
+};
+
 }  // namespace vfs

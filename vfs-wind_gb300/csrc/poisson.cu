@@ -8,6 +8,7 @@
 #include <chrono>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <type_traits>
@@ -161,6 +162,12 @@ struct vfs_poisson {
   double pbytes[16] = {};    // algorithmic bytes of each recorded sweep
   double prof_ms = 0., prof_bytes = 0.;
   int64_t prof_launches = 0;
+  // optional per-phase timing of the outer iteration (environment variable
+  // VFS_PHASE_TIMING=1): preconditioner, operator apply, Gram-Schmidt
+  bool phase = false;
+  cudaEvent_t phev[4] = {};
+  double phase_ms[3] = {0., 0., 0.};
+  double host_ms[4] = {0., 0., 0., 0.};  // enqueue V-cycle, enqueue rest, wait, host work
 };
 
 namespace {
@@ -680,7 +687,7 @@ int ensure_krylov(vfs_poisson *h, int m) {
   CUDA_TRY(cudaMemcpyAsync(h->dV, h->V.data(), (m + 1) * sizeof(double *), cudaMemcpyHostToDevice, h->stream));
   CUDA_TRY(cudaMemcpyAsync(h->dZ, h->Z.data(), m * sizeof(double *), cudaMemcpyHostToDevice, h->stream));
   if (h->hbuf) cudaFreeHost(h->hbuf);
-  CUDA_TRY(cudaMallocHost(&h->hbuf, 512 * 8));
+  CUDA_TRY(cudaMallocHost(&h->hbuf, 1024 * 8));
   h->m_alloc = m;
   return sync(h);
 }
@@ -714,33 +721,65 @@ int fgmres(vfs_poisson *h, const vfs_solve_opts &o, vfs_solve_stats *st) {
     st->iterations = 0;
     return VFS_OK;
   }
-  TRY(residual_norm(h, h->x, h->V[0], &beta));
+  if (o.warm_start) {
+    TRY(residual_norm(h, h->x, h->V[0], &beta));
+  } else {  // zero initial guess: r = b
+    CUDA_TRY(cudaMemcpyAsync(h->V[0], h->b, n * 8, cudaMemcpyDeviceToDevice, h->stream));
+    beta = bn;
+  }
   rel = beta / bn;
   st->initial_rel_residual = rel;
   while (rel > o.rtol && it < o.max_it) {
     sv[0] = 1.0 / beta;
-    CUDA_TRY(cudaMemcpyAsync(h->dsv, sv.data(), 8, cudaMemcpyHostToDevice, h->stream));
+    h->hbuf[400] = sv[0];
+    CUDA_TRY(cudaMemcpyAsync(h->dsv, h->hbuf + 400, 8, cudaMemcpyHostToDevice, h->stream));
     std::fill(gv.begin(), gv.end(), 0.);
     gv[0] = beta;
     int jj = 0;
     for (; jj < m && it < o.max_it; jj++) {
+      const auto t0 = h->phase ? std::chrono::steady_clock::now() : std::chrono::steady_clock::time_point();
+      if (h->phase) cudaEventRecord(h->phev[0], h->stream);
       TRY(precondition(h, h->V[jj], sv[jj], h->Z[jj], o));
+      const auto t1 = h->phase ? std::chrono::steady_clock::now() : t0;
+      if (h->phase) cudaEventRecord(h->phev[1], h->stream);
       double *w = h->V[jj + 1];
       LAUNCH(h, k_apply64, box_grid(h->box), 128, h->box, h->A0, h->Z[jj], w);
+      if (h->phase) cudaEventRecord(h->phev[2], h->stream);
       // classical Gram-Schmidt with the coefficients formed on the device and
       // one read-back per step; a DGKS re-orthogonalisation pass runs when
       // the update removed more than half of ||w|| (a second read-back).
       double ww = 0., wn = 0.;
       for (int pass = 0; pass < 2; pass++) {
         double *dred = h->red, *dh = h->red + 128, *dwn = h->red + 256;
-        LAUNCH(h, k_dots, nbd, 256, n, jj + 1, (const double *const *)h->dV, w, h->partial);
-        LAUNCH(h, k_reduce_rows, jj + 2, 1024, h->partial, nbd, jj + 2, dred);
+        // 8 basis vectors per pass; each pass's last row (w.w) lands where
+        // the next pass's first dot goes, and the final pass leaves w.w at
+        // dred[jj + 1]
+        for (int v0 = 0; v0 <= jj; v0 += 8) {
+          const int nv = std::min(8, jj + 1 - v0);
+          LAUNCH(h, k_dots, nbd, 256, n, nv, (const double *const *)(h->dV + v0), w, h->partial);
+          LAUNCH(h, k_reduce_rows, nv + 1, 1024, h->partial, nbd, nv + 1, dred + v0);
+        }
         LAUNCH(h, k_gs_coef, 1, 64, jj + 1, dred, h->dsv, dh, h->coef);
         LAUNCH(h, k_gs_update, nbd, 256, n, jj + 1, (const double *const *)h->dV, h->coef, w, h->partial);
         LAUNCH(h, k_reduce_rows, 1, 1024, h->partial, nbd, 1, dwn);
+        if (h->phase && pass == 0) cudaEventRecord(h->phev[3], h->stream);
         CUDA_TRY(cudaMemcpyAsync(h->hbuf, h->red, 257 * 8, cudaMemcpyDeviceToHost, h->stream));
+        const auto t2 = h->phase ? std::chrono::steady_clock::now() : t0;
         TRY(sync(h));
+        const auto t3 = h->phase ? std::chrono::steady_clock::now() : t0;
+        if (h->phase && pass == 0) {
+          h->host_ms[0] += std::chrono::duration<double, std::milli>(t1 - t0).count();
+          h->host_ms[1] += std::chrono::duration<double, std::milli>(t2 - t1).count();
+          h->host_ms[2] += std::chrono::duration<double, std::milli>(t3 - t2).count();
+        }
         if (pass == 0) prof_collect(h);
+        if (h->phase && pass == 0) {
+          float a = 0.f, b = 0.f, c = 0.f;
+          cudaEventElapsedTime(&a, h->phev[0], h->phev[1]);
+          cudaEventElapsedTime(&b, h->phev[1], h->phev[2]);
+          cudaEventElapsedTime(&c, h->phev[2], h->phev[3]);
+          h->phase_ms[0] += a; h->phase_ms[1] += b; h->phase_ms[2] += c;
+        }
         if (pass == 0) ww = h->hbuf[jj + 1];
         for (int i = 0; i <= jj; i++) H[(size_t)i * m + jj] = (pass ? H[(size_t)i * m + jj] : 0.) + h->hbuf[128 + i];
         wn = h->hbuf[256];
@@ -750,7 +789,8 @@ int fgmres(vfs_poisson *h, const vfs_solve_opts &o, vfs_solve_stats *st) {
       double hn = std::sqrt(wn);
       H[(size_t)(jj + 1) * m + jj] = hn;
       sv[jj + 1] = hn > 0. ? 1.0 / hn : 0.;
-      CUDA_TRY(cudaMemcpyAsync(h->dsv + jj + 1, &sv[jj + 1], 8, cudaMemcpyHostToDevice, h->stream));
+      h->hbuf[400 + jj + 1] = sv[jj + 1];  // pinned staging: pageable copies cost ~0.5 ms each
+      CUDA_TRY(cudaMemcpyAsync(h->dsv + jj + 1, h->hbuf + 400 + jj + 1, 8, cudaMemcpyHostToDevice, h->stream));
       for (int i = 0; i < jj; i++) {
         double a = H[(size_t)i * m + jj], b2 = H[(size_t)(i + 1) * m + jj];
         H[(size_t)i * m + jj] = cs[i] * a + sn[i] * b2;
@@ -765,6 +805,7 @@ int fgmres(vfs_poisson *h, const vfs_solve_opts &o, vfs_solve_stats *st) {
       gv[jj + 1] = -sn[jj] * gv[jj];
       gv[jj] = cs[jj] * gv[jj];
       it++;
+      if (h->phase) h->host_ms[3] += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
       if (std::fabs(gv[jj + 1]) / bn <= o.rtol || hn == 0.) { jj++; break; }
     }
     for (int i = jj - 1; i >= 0; i--) {
@@ -772,13 +813,22 @@ int fgmres(vfs_poisson *h, const vfs_solve_opts &o, vfs_solve_stats *st) {
       for (int q = i + 1; q < jj; q++) s -= H[(size_t)i * m + q] * y[q];
       y[i] = H[(size_t)i * m + i] != 0. ? s / H[(size_t)i * m + i] : 0.;
     }
-    CUDA_TRY(cudaMemcpyAsync(h->coef, y.data(), jj * 8, cudaMemcpyHostToDevice, h->stream));
+    for (int i = 0; i < jj; i++) h->hbuf[400 + 64 + i] = y[i];
+    CUDA_TRY(cudaMemcpyAsync(h->coef, h->hbuf + 464, jj * 8, cudaMemcpyHostToDevice, h->stream));
     LAUNCH(h, k_axpy_multi, kRedBlocks, 256, n, jj, (const double *const *)h->dZ, h->coef, h->x);
     TRY(residual_norm(h, h->x, h->V[0], &beta));
     rel = beta / bn;
   }
   st->iterations = it;
   st->rel_residual = rel;
+  if (h->phase) {
+    fprintf(stderr, "vfs phase ms: precondition %.3f apply %.3f gram-schmidt %.3f (iterations %d)\n",
+            h->phase_ms[0], h->phase_ms[1], h->phase_ms[2], it);
+    fprintf(stderr, "vfs host ms: enqueue-vcycle %.3f enqueue-rest %.3f wait %.3f iteration-wall %.3f\n",
+            h->host_ms[0], h->host_ms[1], h->host_ms[2], h->host_ms[3]);
+    h->phase_ms[0] = h->phase_ms[1] = h->phase_ms[2] = 0.;
+    for (double &v : h->host_ms) v = 0.;
+  }
   return VFS_OK;
 }
 
@@ -786,6 +836,16 @@ int fgmres(vfs_poisson *h, const vfs_solve_opts &o, vfs_solve_stats *st) {
 
 namespace vfs {
 void set_last_error(const std::string &msg) { g_err = msg; }
+
+int ibm_context(vfs_poisson *h, IbmContext *c) {
+  if (!h->have_grid) return fail(VFS_ESTATE, "set_grid must come before the surface search");
+  if (cudaSetDevice(h->device) != cudaSuccess) return fail(VFS_ECUDA, "cudaSetDevice failed");
+  c->stream = h->stream;
+  c->g = h->g;
+  c->cent = h->met.cent;
+  c->launches = &h->launches;
+  return VFS_OK;
+}
 }  // namespace vfs
 
 // ============================== C ABI =====================================
@@ -836,6 +896,11 @@ int vfs_poisson_create(const vfs_grid_desc *gd, vfs_poisson **out) {
   cudaEventCreate(&h->ev1);
   for (int a = 0; a < 2; a++)
     for (int q = 0; q < 16; q++) cudaEventCreate(&h->pev[a][q]);
+  for (int q = 0; q < 4; q++) cudaEventCreate(&h->phev[q]);
+  {
+    const char *e = getenv("VFS_PHASE_TIMING");
+    h->phase = e && e[0] == '1';
+  }
   const size_t N = h->g.n(), n = h->box.n();
   int rc;
   if ((rc = dalloc(h, &h->coor, 3 * N)) || (rc = dalloc(h, &h->nvert, N)) || (rc = dalloc(h, &h->ucont, 3 * N)) ||
@@ -850,7 +915,7 @@ int vfs_poisson_create(const vfs_grid_desc *gd, vfs_poisson **out) {
   if ((rc = dalloc(h, &h->blk, nblk))) return bail(rc);
   h->partial_len = std::max<size_t>(n / 16 + 65536, (size_t)70 * ((n + 2047) / 2048) + 4096);
   if ((rc = dalloc(h, &h->partial, h->partial_len))) return bail(rc);
-  if (cudaMallocHost(&h->hbuf, 256 * 8) != cudaSuccess) { cudaGetLastError(); return bail(fail(VFS_ENOMEM, "pinned alloc")); }
+  if (cudaMallocHost(&h->hbuf, 1024 * 8) != cudaSuccess) { cudaGetLastError(); return bail(fail(VFS_ENOMEM, "pinned alloc")); }
   cudaMemsetAsync(h->phi_da, 0, N * 8, h->stream);
   cudaMemsetAsync(h->x, 0, n * 8, h->stream);
   if ((rc = sync(h))) return bail(rc);
@@ -870,6 +935,8 @@ void vfs_poisson_destroy(vfs_poisson *h) {
   for (int a = 0; a < 2; a++)
     for (int q = 0; q < 16; q++)
       if (h->pev[a][q]) cudaEventDestroy(h->pev[a][q]);
+  for (int q = 0; q < 4; q++)
+    if (h->phev[q]) cudaEventDestroy(h->phev[q]);
   if (h->stream && h->own_stream) cudaStreamDestroy(h->stream);
   cudaGetLastError();
   delete h;

@@ -334,11 +334,14 @@ __device__ __forceinline__ void cast_body(const double *__restrict__ src, T *__r
 
 // ---- FP64 Krylov kernels (fixed grid, deterministic block partials) ----
 #define KTILE 8
-// partial[v * gridDim.x + block] = sum over the block's cells of V_v . w,
-// and row nv holds w . w.  Each thread keeps its KTILE values of w in
-// registers while the basis vectors stream past.
+#define KDOT 8
+// Dots of w with up to KDOT basis vectors V[v0..v0+nv) (and w.w when
+// with_ww): each thread keeps KTILE values of w in registers and one
+// accumulator per vector; the block reduces all accumulators at once.
+// partial[(v - v0) * gridDim.x + block], row nv holds w.w.
 __global__ void __launch_bounds__(256) k_dots(size_t n, int nv, const double *const *__restrict__ V,
                                               const double *__restrict__ w, double *partial) {
+  __shared__ double sh[8][KDOT + 1];
   const size_t base = (size_t)blockIdx.x * blockDim.x * KTILE + threadIdx.x;
   double wr[KTILE];
 #pragma unroll
@@ -346,38 +349,67 @@ __global__ void __launch_bounds__(256) k_dots(size_t n, int nv, const double *co
     size_t c = base + (size_t)q * blockDim.x;
     wr[q] = c < n ? w[c] : 0.;
   }
-  for (int v = 0; v <= nv; v++) {
-    double s = 0.;
+  double acc[KDOT + 1];
+#pragma unroll
+  for (int v = 0; v <= KDOT; v++) acc[v] = 0.;
+#pragma unroll
+  for (int v = 0; v < KDOT; v++) {
     if (v < nv) {
       const double *p = V[v];
 #pragma unroll
       for (int q = 0; q < KTILE; q++) {
         size_t c = base + (size_t)q * blockDim.x;
-        if (c < n) s = fma(wr[q], __ldcs(&p[c]), s);
+        if (c < n) acc[v] = fma(wr[q], __ldcs(&p[c]), acc[v]);
       }
-    } else {
-#pragma unroll
-      for (int q = 0; q < KTILE; q++) s = fma(wr[q], wr[q], s);
     }
-    s = block_sum(s);
-    if (threadIdx.x == 0) partial[(size_t)v * gridDim.x + blockIdx.x] = s;
+  }
+#pragma unroll
+  for (int q = 0; q < KTILE; q++) acc[KDOT] = fma(wr[q], wr[q], acc[KDOT]);
+  const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
+#pragma unroll
+  for (int v = 0; v <= KDOT; v++) {
+    double t = warp_sum(acc[v]);
+    if (lane == 0) sh[wp][v] = t;
+  }
+  __syncthreads();
+  if (threadIdx.x <= KDOT) {
+    const int v = threadIdx.x;
+    double t = 0.;
+    for (int q = 0; q < (int)(blockDim.x >> 5); q++) t += sh[q][v];
+    const int row = v < KDOT ? v : nv;
+    if (v < nv || v == KDOT) partial[(size_t)row * gridDim.x + blockIdx.x] = t;
   }
 }
 
-// w -= sum_v coef[v] V_v, with the block partial of ||w||^2.
+// w -= sum_v coef[v] V_v, with the block partial of ||w||^2; the w tile
+// stays in registers while each basis vector streams once.
 __global__ void __launch_bounds__(256) k_gs_update(size_t n, int nv, const double *const *__restrict__ V,
                                                    const double *__restrict__ coef, double *__restrict__ w,
                                                    double *partial) {
   const size_t base = (size_t)blockIdx.x * blockDim.x * KTILE + threadIdx.x;
+  double acc[KTILE];
+#pragma unroll
+  for (int q = 0; q < KTILE; q++) {
+    size_t c = base + (size_t)q * blockDim.x;
+    acc[q] = c < n ? w[c] : 0.;
+  }
+  for (int v = 0; v < nv; v++) {
+    const double *p = V[v];
+    const double cv = -coef[v];
+#pragma unroll
+    for (int q = 0; q < KTILE; q++) {
+      size_t c = base + (size_t)q * blockDim.x;
+      if (c < n) acc[q] = fma(cv, __ldcs(&p[c]), acc[q]);
+    }
+  }
   double ss = 0.;
 #pragma unroll
   for (int q = 0; q < KTILE; q++) {
     size_t c = base + (size_t)q * blockDim.x;
-    if (c >= n) continue;
-    double acc = w[c];
-    for (int v = 0; v < nv; v++) acc = fma(-coef[v], __ldcs(&V[v][c]), acc);
-    w[c] = acc;
-    ss = fma(acc, acc, ss);
+    if (c < n) {
+      w[c] = acc[q];
+      ss = fma(acc[q], acc[q], ss);
+    }
   }
   ss = block_sum(ss);
   if (threadIdx.x == 0) partial[blockIdx.x] = ss;

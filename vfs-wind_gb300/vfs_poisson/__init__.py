@@ -33,7 +33,7 @@ EXPORTS = [
     "vfs_poisson_mg_level_info", "vfs_poisson_mg_get_nvert", "vfs_poisson_mg_restrict",
     "vfs_poisson_mg_interpolate", "vfs_poisson_mg_vcycle", "vfs_poisson_kernel_launches",
     "vfs_poisson_set_stream", "vfs_poisson_profile", "vfs_poisson_profile_read",
-    "vfs_divergence_noalloc",
+    "vfs_divergence_noalloc", "vfs_poisson_ibm_search",
 ]
 
 
@@ -105,6 +105,7 @@ def load(path=LIB_PATH):
     L.vfs_poisson_profile.argtypes = [vp, C.c_int]
     L.vfs_poisson_profile_read.argtypes = [vp, P(C.c_double), P(C.c_double), P(C.c_int64)]
     L.vfs_divergence_noalloc.argtypes = [P(GridDesc), vp, vp, vp, vp, vp]
+    L.vfs_poisson_ibm_search.argtypes = [vp, C.c_int, C.c_int, vp, C.c_int, vp, vp, vp, P(C.c_int)]
     _lib = L
     return L
 
@@ -214,6 +215,18 @@ class PoissonSolver:
         v = C.c_double()
         _check(load().vfs_poisson_divergence(self.h, _ptr(ucont), C.byref(v)))
         return v.value
+
+    def ibm_search(self, surface, nvert=None, ibi=0, bctype=None):
+        """Classify the cells against one closed triangulated surface
+        (xyz[n_v, 3], tri[n_elmt, 3]); returns (nvert, cells that gave up)."""
+        xyz = np.ascontiguousarray(surface[0], np.float64)
+        tri = np.ascontiguousarray(surface[1], np.int32)
+        out = np.zeros(self._shape()) if nvert is None else nvert
+        bc = None if bctype is None else (C.c_int * 6)(*[int(b) for b in bctype])
+        nf = C.c_int()
+        _check(load().vfs_poisson_ibm_search(self.h, ibi, xyz.shape[0], _ptr(xyz), tri.shape[0], _ptr(tri),
+                                             bc, _ptr(out, True), C.byref(nf)))
+        return out, nf.value
 
     # --- inspection ---
     def numbering(self):

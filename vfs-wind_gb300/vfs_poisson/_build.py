@@ -1,8 +1,9 @@
 """Build the CUDA library libvfs_poisson.so for sm_103a (in-tree, no cmake).
 
-Translation units are compiled in parallel; setup.cu is compiled with
--fmad=false so that the grid, operator, right-hand-side and projection
-kernels round every operation in the reference's source order.
+Translation units are compiled in parallel; setup.cu, noalloc.cu and ibm.cu
+are compiled with -fmad=false (ibm.cu's host code also without contraction)
+so that the grid, operator, right-hand-side, projection and classification
+code rounds every operation in the reference's source order.
 """
 from __future__ import annotations
 
@@ -25,6 +26,7 @@ UNITS = {
     "solve.cu": [],
     "poisson.cu": [],
     "noalloc.cu": ["-fmad=false"],
+    "ibm.cu": ["-fmad=false", "-Xcompiler", "-ffp-contract=off"],
 }
 
 

@@ -256,6 +256,62 @@ def rotor(nx=192, ny=128, nz=192, step=0, seed=1004, amp=0.05):
                 extra={"step": step})
 
 
+def rod_surface(base, axis, length, radius, n_theta=24, n_len=8, up=(0.0, 0.0, 1.0)):
+    """Closed triangulated circular rod (the reference reads such bodies as
+    UCD surfaces, Source/ibm_io.c): rings of `n_theta` vertices at `n_len`+1
+    stations from `base` along the unit `axis`, closed by two fan caps.
+    Returns (xyz[n_v, 3], tri[n_elmt, 3]) with outward-facing windings."""
+    a = np.asarray(axis, np.float64)
+    a = a / np.linalg.norm(a)
+    u = np.cross(a, up)
+    if np.linalg.norm(u) < 1e-12:
+        u = np.cross(a, (1.0, 0.0, 0.0))
+    u /= np.linalg.norm(u)
+    w = np.cross(a, u)
+    th = 2.0 * np.pi * np.arange(n_theta) / n_theta
+    ring = radius * (np.cos(th)[:, None] * u + np.sin(th)[:, None] * w)
+    base = np.asarray(base, np.float64)
+    pts = [base + s * length * a + ring for s in np.arange(n_len + 1) / n_len]
+    xyz = np.concatenate(pts + [base[None], (base + length * a)[None]])
+    c0, c1 = len(xyz) - 2, len(xyz) - 1
+    tri = []
+    for s in range(n_len):
+        for t in range(n_theta):
+            p00, p01 = s * n_theta + t, s * n_theta + (t + 1) % n_theta
+            p10, p11 = p00 + n_theta, p01 + n_theta
+            tri += [(p00, p01, p11), (p00, p11, p10)]
+    top = n_len * n_theta
+    for t in range(n_theta):
+        tri.append((c0, (t + 1) % n_theta, t))
+        tri.append((c1, top + t, top + (t + 1) % n_theta))
+    return xyz, np.asarray(tri, np.int32)
+
+
+def tower_surfaces(array=(3, 2), radius=0.02, height=0.6, n_theta=24, n_len=12):
+    """Closed vertical tower cylinders at the positions of the towers case
+    (0.25 streamwise, 0.3 spanwise spacing about the domain centre), from
+    y = 0 to `height`: one surface per tower (body ibi)."""
+    ax, az = array
+    xs = 0.5 + 0.25 * (np.arange(ax) - (ax - 1) / 2)
+    zs = 0.5 + 0.3 * (np.arange(az) - (az - 1) / 2)
+    return [rod_surface((x0, 0.0, z0), (0.0, 1.0, 0.0), height, radius, n_theta, n_len)
+            for x0 in xs for z0 in zs]
+
+
+def rotor_surfaces(centre=(0.5, 0.5, 0.5), angle_deg=0.0, rods=3, radius=0.03, length=0.25, hub=0.04,
+                   n_theta=16, n_len=10):
+    """The rotor of the rotor case as closed surfaces, one per rod (body
+    ibi): rods of `radius` and `length` in the x-y plane starting `hub` from
+    the centre, rotated by `angle_deg` about the z axis."""
+    out = []
+    c = np.asarray(centre, np.float64)
+    for r in range(rods):
+        th = np.deg2rad(angle_deg + 360.0 * r / rods)
+        a = np.array([np.cos(th), np.sin(th), 0.0])
+        out.append(rod_surface(c + hub * a, a, length, radius, n_theta, n_len))
+    return out
+
+
 CONFIGS = {
     "c1": channel,
     "c2": cylinder,

@@ -69,7 +69,10 @@ typedef struct {
   double omega;       /* relaxation weight of the line sweeps              */
   int use_graphs;     /* capture the V-cycle in a CUDA graph               */
   int coarsest_max;   /* coarsest level cell budget                        */
-  int warm_start;     /* 1: start from the phi passed in (Phi2 warm start) */
+  int warm_start;     /* 0: zero guess; 1: start from the phi passed in (Phi2
+                         warm start; the last solution if phi is NULL);
+                         2: start from the handle's iterate as left by the
+                         last solve or by vfs_poisson_learned_guess */
   int smoother;       /* 0 fused line Jacobi, 1 line Jacobi in correction
                          form, 2 zebra (k-plane) line Gauss-Seidel         */
 } vfs_solve_opts;
@@ -112,8 +115,9 @@ int vfs_poisson_rhs(vfs_poisson *h, const double *ucont, double dt, double st, d
 
 /* Solve A phi = b to opts->rtol, remove the fluid mean of phi
  * (Remove_Nullspace) and write phi to `phi` in DA layout with periodic
- * ghost copies (Convert_Phi2_Phi).  With opts->warm_start, `phi` is read
- * first as the initial guess.  `phi` may be NULL to keep phi on the device. */
+ * ghost copies (Convert_Phi2_Phi).  With opts->warm_start == 1, `phi` is
+ * read first as the initial guess; with 2 the solve starts from the
+ * handle's iterate.  `phi` may be NULL to keep phi on the device. */
 int vfs_poisson_solve(vfs_poisson *h, double *phi, const vfs_solve_opts *opts, vfs_solve_stats *stats);
 
 /* PoissonSolver_Hypre in one call: rhs + solve. */
@@ -215,6 +219,76 @@ int vfs_divergence_noalloc(const vfs_grid_desc *g, const double *ucont, const do
  * solver's blanking: pass it to vfs_poisson_set_nvert. */
 int vfs_poisson_ibm_search(vfs_poisson *h, int ibi, int n_v, const double *xyz, int n_elmt, const int32_t *tri,
                            const int *bctype, double *nvert, int *n_failed);
+
+/* ---------------------------------------------------------------------
+ * Learned initial guess: a 3-level 3-D U-Net (channels 16/32/64, 3x3x3
+ * convolutions with ReLU, 2x2x2 average pooling, nearest upsampling with
+ * skip concatenation, 1x1 head) with BF16 weights and activations on the
+ * tensor cores and FP32 accumulation.  No counterpart in the reference.
+ *
+ * Parameters (FP32 master copy, vfs_unet_num_params floats) are laid out
+ * layer by layer, encoder e0a e0b e1a e1b e2a e2b then decoder d1a d1b d0a
+ * d0b, each as W[tap][cin][cout] (tap = 9 kz + 3 ky + kx, input channel
+ * ci of a concatenation: upsampled source first) followed by bias[cout];
+ * then the head's 16 weights and its bias.  The first layer has 16 input
+ * channels, of which the network feeds 4 (the feature planes) and zeros.
+ * --------------------------------------------------------------------- */
+typedef struct vfs_unet vfs_unet;
+
+/* A sub-box of feature planes (device memory, FP32): features
+ * [4][fz][fy][fx], target and weight [fz][fy][fx] (training only).  The
+ * network runs on the sub-box (ox..ox+nx-1, ...); nx, ny, nz multiples of 4.
+ * The loss is sum(weight * (out - target)^2) / sum(weight). */
+typedef struct {
+  const float *features;
+  const float *target;
+  const float *weight;
+  int fx, fy, fz;
+  int ox, oy, oz;
+  int nx, ny, nz;
+} vfs_unet_batch;
+
+int vfs_unet_create(unsigned int seed, vfs_unet **out);
+void vfs_unet_destroy(vfs_unet *u);
+int vfs_unet_set_stream(vfs_unet *u, void *stream);
+int64_t vfs_unet_num_params(vfs_unet *u);
+/* host or device pointers of vfs_unet_num_params floats */
+int vfs_unet_get_params(vfs_unet *u, float *out);
+int vfs_unet_set_params(vfs_unet *u, const float *in);
+/* out: [nz][ny][nx] FP32 device memory; asynchronous on the U-Net's stream */
+int vfs_unet_forward(vfs_unet *u, const vfs_unet_batch *b, float *out);
+/* loss and gradient of the batch (grad: host or device, may be NULL) */
+int vfs_unet_gradient(vfs_unet *u, const vfs_unet_batch *b, float *grad, double *loss);
+/* one Adam step (beta 0.9 / 0.999, eps 1e-8) on the batch's gradient */
+int vfs_unet_train_step(vfs_unet *u, const vfs_unet_batch *b, double lr, double *loss);
+/* Adam update from the current gradient (as left by vfs_unet_gradient or
+ * vfs_unet_set_grads) */
+int vfs_unet_adam(vfs_unet *u, double lr, double beta1, double beta2, double eps);
+int vfs_unet_set_grads(vfs_unet *u, const float *grad);
+int64_t vfs_unet_kernel_launches(vfs_unet *u);
+
+/* Learned initial guess for the current right-hand side (vfs_poisson_rhs
+ * first), from phi at steps n-1 and n-2 (DA layout, host or device).  The
+ * network sees four box-layout planes: phi_{n-1}, phi_{n-1} - phi_{n-2},
+ * aj * (b - A phi_ex) with phi_ex = 2 phi_{n-1} - phi_{n-2} (the residual
+ * of the linear extrapolation in the aj-scaled system), each divided by its
+ * RMS over the dofs, and the dof flag.  It predicts the correction
+ * phi_n - phi_ex in units of kappa * RMS(aj * (b - A phi_ex)).  The plain
+ * solver then judges the guess: the learned guess and the previous step's
+ * phi are both measured by their FP64 residual and the smaller one becomes
+ * the solver's iterate (*chosen = 1 for the learned guess, 0 for the
+ * previous step; rel_res[0..1] = their relative residuals).  Solve from it
+ * with opts.warm_start = 2.  The network runs on the handle's stream (its
+ * stream is set to it); box dims must be multiples of 4. */
+int vfs_poisson_learned_guess(vfs_poisson *h, vfs_unet *u, const double *phi_nm1, const double *phi_nm2,
+                              double kappa, int *chosen, double *rel_res);
+
+/* One training sample of the learned guess: the four feature planes of the
+ * current right-hand side (as above), the target (phi_n - phi_ex) /
+ * RMS(aj * (b - A phi_ex)) and the loss weight (dof flag), all box layout
+ * FP32 device memory (features 4 planes; target, weight 1 plane). */
+int vfs_poisson_guess_sample(vfs_poisson *h, const double *phi_n, const double *phi_nm1, const double *phi_nm2,
+                             float *features, float *target, float *weight);
 
 #ifdef __cplusplus
 }

@@ -57,6 +57,84 @@ __global__ void k_mask_box(size_t n, const uint8_t *rowtype, double *x) {
   size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (c < n && rowtype[c] == 0) x[c] = 0.;
 }
+// ---- learned initial guess: features, training target, composition ----
+// sums[0..2]: fluid sums of squares of planes 0..2, sums[3]: fluid count.
+__device__ inline void block_add(double v, double *dst) {
+  __shared__ double sh[32];
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    v = threadIdx.x < (blockDim.x >> 5) ? sh[threadIdx.x] : 0.;
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (threadIdx.x == 0) atomicAdd(dst, v);
+  }
+}
+// phi_{n-1}, phi_{n-2} (DA) -> extrapolation ex = 2 phi_{n-1} - phi_{n-2}
+// and feature planes f0 = phi_{n-1}, f1 = phi_{n-1} - phi_{n-2}, f3 = dof
+__global__ void k_guess_prep(Grid g, Box b, const uint8_t *rt, const double *p1, const double *p2, double *ex,
+                             float *f0, float *f1, float *f3, double *sums) {
+  double s0 = 0., s1 = 0., s3 = 0.;
+  for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < b.n(); c += (size_t)gridDim.x * blockDim.x) {
+    const int i = c % b.nx + 1, j = (c / b.nx) % b.ny + 1, k = c / ((size_t)b.nx * b.ny) + 1;
+    const bool d = rt[c] == 1;
+    const double a = d ? p1[g.at(i, j, k)] : 0., q = d ? p2[g.at(i, j, k)] : 0.;
+    ex[c] = 2. * a - q;
+    f0[c] = (float)a;
+    f1[c] = (float)(a - q);
+    f3[c] = d ? 1.f : 0.f;
+    s0 += a * a;
+    s1 += (a - q) * (a - q);
+    s3 += d ? 1. : 0.;
+  }
+  block_add(s0, sums);
+  block_add(s1, sums + 1);
+  block_add(s3, sums + 3);
+}
+// f2 = aj * (b - A ex): the extrapolation residual of the aj-scaled system
+__global__ void k_guess_f2(size_t n, const uint8_t *rt, const double *aj, const double *r, float *f2, double *sums) {
+  double s = 0.;
+  for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < n; c += (size_t)gridDim.x * blockDim.x) {
+    const double v = rt[c] == 1 ? aj[c] * r[c] : 0.;
+    f2[c] = (float)v;
+    s += v * v;
+  }
+  block_add(s, sums + 2);
+}
+__device__ inline double plane_rms(const double *sums, int q) {
+  const double cnt = sums[3] > 1. ? sums[3] : 1.;
+  return sqrt(sums[q] / cnt);
+}
+// planes 0..2 divided by their fluid RMS
+__global__ void k_guess_scale(size_t n, float *f, const double *sums) {
+  float inv[3];
+  for (int q = 0; q < 3; q++) {
+    const double r = plane_rms(sums, q);
+    inv[q] = r > 0. ? (float)(1. / r) : 0.f;
+  }
+  for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < n; c += (size_t)gridDim.x * blockDim.x)
+    for (int q = 0; q < 3; q++) f[q * n + c] *= inv[q];
+}
+// training target (phi_n - ex) / rms(f2) and loss weight (dof flag)
+__global__ void k_guess_target(Grid g, Box b, const uint8_t *rt, const double *phi, const double *ex,
+                               const double *sums, float *tgt, float *wt) {
+  const double s2 = plane_rms(sums, 2), inv = s2 > 0. ? 1. / s2 : 0.;
+  for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < b.n(); c += (size_t)gridDim.x * blockDim.x) {
+    const int i = c % b.nx + 1, j = (c / b.nx) % b.ny + 1, k = c / ((size_t)b.nx * b.ny) + 1;
+    const bool d = rt[c] == 1;
+    tgt[c] = d ? (float)((phi[g.at(i, j, k)] - ex[c]) * inv) : 0.f;
+    wt[c] = d ? 1.f : 0.f;
+  }
+}
+// learned guess x = ex + kappa * rms(f2) * out on dofs
+__global__ void k_guess_compose(size_t n, const uint8_t *rt, const double *ex, const float *out, double kappa,
+                                const double *sums, double *x) {
+  const double s = kappa * plane_rms(sums, 2);
+  for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < n; c += (size_t)gridDim.x * blockDim.x)
+    x[c] = rt[c] == 1 ? ex[c] + s * (double)out[c] : 0.;
+}
+
 __device__ inline void atomic_max_pos(double *addr, double v) {
   // non-negative doubles order like their bit patterns
   atomicMax((unsigned long long *)addr, (unsigned long long)__double_as_longlong(v));
@@ -146,6 +224,10 @@ struct vfs_poisson {
   double *partial = nullptr, *red = nullptr, *coef = nullptr, *dsv = nullptr;
   size_t partial_len = 0;
   double *hbuf = nullptr;  // pinned host readback
+  // learned initial guess: extrapolated phi, plane sums, feature planes and
+  // network output (box layout, allocated on first use)
+  double *gex = nullptr, *gsum = nullptr;
+  float *gfeat = nullptr, *gout = nullptr;
   std::vector<Level> L;
   bool have_grid = false, have_nvert = false, have_rhs = false, have_phi = false;
   // graphs of the V-cycle per precision and parameters they were built for
@@ -1024,7 +1106,7 @@ int vfs_poisson_solve(vfs_poisson *h, double *phi, const vfs_solve_opts *opts, v
   vfs_solve_stats st{};
   const size_t n = h->box.n();
   CUDA_TRY(cudaEventRecord(h->ev0, h->stream));
-  if (o.warm_start && phi) {
+  if (o.warm_start == 1 && phi) {
     TRY(upload(h, h->stage, phi, h->g.n()));
     LAUNCH(h, k_da_to_box, lin_grid(n), 256, h->g, h->box, h->stage, h->x);
     LAUNCH(h, k_mask_box, lin_grid(n), 256, n, h->rowtype0, h->x);
@@ -1051,6 +1133,87 @@ int vfs_poisson_solve(vfs_poisson *h, double *phi, const vfs_solve_opts *opts, v
   if (st.status != VFS_OK)
     return fail(VFS_ENOCONV, "solver stopped at relative residual " + std::to_string(st.rel_residual));
   return VFS_OK;
+}
+
+}  // extern "C"
+
+namespace {
+int guess_buffers(vfs_poisson *h) {
+  const size_t n = h->box.n();
+  if (!h->gex) {
+    TRY(dalloc(h, &h->gex, n));
+    TRY(dalloc(h, &h->gsum, 8));
+    TRY(dalloc(h, &h->gfeat, 4 * n));
+    TRY(dalloc(h, &h->gout, n));
+  }
+  return VFS_OK;
+}
+
+// feature planes of the current right-hand side into `feat` (4 planes)
+int guess_features(vfs_poisson *h, const double *phi_nm1, const double *phi_nm2, float *feat) {
+  if (!h || !phi_nm1 || !phi_nm2 || !feat) return fail(VFS_EINVAL, "null argument");
+  if (!h->have_rhs) return fail(VFS_ESTATE, "rhs must come before the guess");
+  TRY(guess_buffers(h));
+  const size_t n = h->box.n(), N = h->g.n();
+  TRY(upload(h, h->stage, phi_nm1, N));
+  TRY(upload(h, h->stage + N, phi_nm2, N));
+  CUDA_TRY(cudaMemsetAsync(h->gsum, 0, 8 * sizeof(double), h->stream));
+  LAUNCH(h, k_guess_prep, kRedBlocks, 256, h->g, h->box, h->rowtype0, h->stage, h->stage + N, h->gex, feat,
+         feat + n, feat + 3 * n, h->gsum);
+  LAUNCH(h, k_residual64, box_grid(h->box), 128, h->box, h->A0, h->gex, h->b, h->r, h->partial);
+  LAUNCH(h, k_guess_f2, kRedBlocks, 256, n, h->rowtype0, (const double *)h->aj_box, h->r, feat + 2 * n, h->gsum);
+  LAUNCH(h, k_guess_scale, kRedBlocks, 256, n, feat, h->gsum);
+  return VFS_OK;
+}
+}  // namespace
+
+extern "C" {
+
+int vfs_poisson_guess_sample(vfs_poisson *h, const double *phi_n, const double *phi_nm1, const double *phi_nm2,
+                             float *features, float *target, float *weight) {
+  if (!phi_n || !target || !weight) return fail(VFS_EINVAL, "null argument");
+  if (!is_device_ptr(features) || !is_device_ptr(target) || !is_device_ptr(weight))
+    return fail(VFS_EINVAL, "features, target and weight must be device memory");
+  TRY(guess_features(h, phi_nm1, phi_nm2, features));
+  const size_t N = h->g.n();
+  TRY(upload(h, h->stage + 2 * N, phi_n, N));
+  LAUNCH(h, k_guess_target, kRedBlocks, 256, h->g, h->box, h->rowtype0, h->stage + 2 * N, h->gex, h->gsum, target,
+         weight);
+  return sync(h);
+}
+
+int vfs_poisson_learned_guess(vfs_poisson *h, vfs_unet *u, const double *phi_nm1, const double *phi_nm2,
+                              double kappa, int *chosen, double *rel_res) {
+  if (!h || !u) return fail(VFS_EINVAL, "null argument");
+  const Box b = h->box;
+  if (b.nx % 4 || b.ny % 4 || b.nz % 4) return fail(VFS_EINVAL, "the learned guess needs box dims that are multiples of 4");
+  TRY(ensure_krylov(h, std::max(h->m_alloc, 20)));
+  TRY(guess_buffers(h));
+  TRY(guess_features(h, phi_nm1, phi_nm2, h->gfeat));
+  const size_t n = b.n();
+  vfs_unet_set_stream(u, h->stream);
+  vfs_unet_batch bt{h->gfeat, nullptr, nullptr, b.nx, b.ny, b.nz, 0, 0, 0, b.nx, b.ny, b.nz};
+  TRY(vfs_unet_forward(u, &bt, h->gout));
+  h->launches += vfs_unet_kernel_launches(u);
+  LAUNCH(h, k_guess_compose, kRedBlocks, 256, n, h->rowtype0, h->gex, h->gout, kappa, h->gsum, h->x);
+  // the plain solver judges: keep whichever of the learned guess and the
+  // previous step's phi has the smaller FP64 residual
+  LAUNCH(h, k_da_to_box, lin_grid(n), 256, h->g, h->box, h->stage, h->gex);
+  LAUNCH(h, k_mask_box, lin_grid(n), 256, n, h->rowtype0, h->gex);
+  LAUNCH(h, k_sumsq, kRedBlocks, 256, n, h->b, h->partial);
+  double nb2 = 0., r_prev = 0., r_learn = 0.;
+  TRY(reduce_read(h, kRedBlocks, 1, &nb2));
+  TRY(residual_norm(h, h->gex, h->r, &r_prev));
+  TRY(residual_norm(h, h->x, h->r, &r_learn));
+  const double nb = nb2 > 0. ? std::sqrt(nb2) : 1.;
+  const bool learned = r_learn < r_prev;
+  if (!learned) CUDA_TRY(cudaMemcpyAsync(h->x, h->gex, n * 8, cudaMemcpyDeviceToDevice, h->stream));
+  if (chosen) *chosen = learned ? 1 : 0;
+  if (rel_res) {
+    rel_res[0] = r_prev / nb;
+    rel_res[1] = r_learn / nb;
+  }
+  return sync(h);
 }
 
 int vfs_poisson_solver_hypre(vfs_poisson *h, const double *ucont, double dt, double st, double coeff, double *phi,

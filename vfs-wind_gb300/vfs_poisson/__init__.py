@@ -34,6 +34,9 @@ EXPORTS = [
     "vfs_poisson_mg_interpolate", "vfs_poisson_mg_vcycle", "vfs_poisson_kernel_launches",
     "vfs_poisson_set_stream", "vfs_poisson_profile", "vfs_poisson_profile_read",
     "vfs_divergence_noalloc", "vfs_poisson_ibm_search",
+    "vfs_unet_create", "vfs_unet_destroy", "vfs_unet_set_stream", "vfs_unet_num_params", "vfs_unet_get_params",
+    "vfs_unet_set_params", "vfs_unet_forward", "vfs_unet_gradient", "vfs_unet_train_step", "vfs_unet_adam",
+    "vfs_unet_set_grads", "vfs_unet_kernel_launches", "vfs_poisson_learned_guess", "vfs_poisson_guess_sample",
 ]
 
 
@@ -48,6 +51,12 @@ class SolveOpts(C.Structure):
     _fields_ = [("rtol", C.c_double), ("max_it", C.c_int), ("restart", C.c_int), ("precision", C.c_int),
                 ("nu1", C.c_int), ("nu2", C.c_int), ("omega", C.c_double), ("use_graphs", C.c_int),
                 ("coarsest_max", C.c_int), ("warm_start", C.c_int), ("smoother", C.c_int)]
+
+
+class UNetBatch(C.Structure):
+    _fields_ = [("features", C.c_void_p), ("target", C.c_void_p), ("weight", C.c_void_p),
+                ("fx", C.c_int), ("fy", C.c_int), ("fz", C.c_int), ("ox", C.c_int), ("oy", C.c_int),
+                ("oz", C.c_int), ("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int)]
 
 
 class SolveStats(C.Structure):
@@ -106,6 +115,23 @@ def load(path=LIB_PATH):
     L.vfs_poisson_profile_read.argtypes = [vp, P(C.c_double), P(C.c_double), P(C.c_int64)]
     L.vfs_divergence_noalloc.argtypes = [P(GridDesc), vp, vp, vp, vp, vp]
     L.vfs_poisson_ibm_search.argtypes = [vp, C.c_int, C.c_int, vp, C.c_int, vp, vp, vp, P(C.c_int)]
+    L.vfs_unet_create.argtypes = [C.c_uint, P(vp)]
+    L.vfs_unet_destroy.argtypes = [vp]
+    L.vfs_unet_destroy.restype = None
+    L.vfs_unet_set_stream.argtypes = [vp, vp]
+    L.vfs_unet_num_params.argtypes = [vp]
+    L.vfs_unet_num_params.restype = C.c_int64
+    L.vfs_unet_get_params.argtypes = [vp, vp]
+    L.vfs_unet_set_params.argtypes = [vp, vp]
+    L.vfs_unet_forward.argtypes = [vp, P(UNetBatch), vp]
+    L.vfs_unet_gradient.argtypes = [vp, P(UNetBatch), vp, P(C.c_double)]
+    L.vfs_unet_train_step.argtypes = [vp, P(UNetBatch), C.c_double, P(C.c_double)]
+    L.vfs_unet_adam.argtypes = [vp, C.c_double, C.c_double, C.c_double, C.c_double]
+    L.vfs_unet_set_grads.argtypes = [vp, vp]
+    L.vfs_unet_kernel_launches.argtypes = [vp]
+    L.vfs_unet_kernel_launches.restype = C.c_int64
+    L.vfs_poisson_learned_guess.argtypes = [vp, vp, vp, vp, C.c_double, P(C.c_int), vp]
+    L.vfs_poisson_guess_sample.argtypes = [vp, vp, vp, vp, vp, vp, vp]
     _lib = L
     return L
 
@@ -305,3 +331,88 @@ class PoissonSolver:
         ms, b, n = C.c_double(), C.c_double(), C.c_int64()
         _check(load().vfs_poisson_profile_read(self.h, C.byref(ms), C.byref(b), C.byref(n)))
         return ms.value, b.value, n.value
+
+    # --- learned initial guess ---
+    def guess_sample(self, phi_n, phi_nm1, phi_nm2, features, target, weight):
+        """Training sample for the current right-hand side: feature planes
+        [4][nz][ny][nx], target and weight [nz][ny][nx] (FP32 CUDA tensors,
+        box layout, written in place)."""
+        _check(load().vfs_poisson_guess_sample(self.h, _ptr(phi_n), _ptr(phi_nm1), _ptr(phi_nm2), _ptr(features),
+                                               _ptr(target), _ptr(weight)))
+
+    def learned_guess(self, unet, phi_nm1, phi_nm2, kappa):
+        """Install the better of the learned guess and phi_{n-1} as the
+        iterate; returns (chosen, [rel_res_prev, rel_res_learned]).  Solve
+        with warm_start=2 next."""
+        ch = C.c_int()
+        rr = (C.c_double * 2)()
+        _check(load().vfs_poisson_learned_guess(self.h, unet.u, _ptr(phi_nm1), _ptr(phi_nm2), float(kappa),
+                                                C.byref(ch), C.cast(rr, C.c_void_p)))
+        return ch.value, [rr[0], rr[1]]
+
+
+class UNet:
+    """The learned-guess network (3 levels, 16/32/64 channels, BF16 tensor
+    cores), trained and run by the library's own kernels."""
+
+    def __init__(self, seed=0):
+        L = load()
+        u = C.c_void_p()
+        _check(L.vfs_unet_create(seed, C.byref(u)))
+        self.u = u
+        self.kappa = 1.0
+
+    def close(self):
+        if getattr(self, "u", None):
+            load().vfs_unet_destroy(self.u)
+            self.u = None
+
+    __del__ = close
+
+    @property
+    def num_params(self):
+        return load().vfs_unet_num_params(self.u)
+
+    def get_params(self):
+        out = np.zeros(self.num_params, np.float32)
+        _check(load().vfs_unet_get_params(self.u, _ptr(out, True)))
+        return out
+
+    def set_params(self, p):
+        p = np.ascontiguousarray(p, np.float32) if isinstance(p, np.ndarray) else p
+        _check(load().vfs_unet_set_params(self.u, _ptr(p)))
+
+    def set_grads(self, g):
+        g = np.ascontiguousarray(g, np.float32) if isinstance(g, np.ndarray) else g
+        _check(load().vfs_unet_set_grads(self.u, _ptr(g)))
+
+    def set_stream(self, stream):
+        _check(load().vfs_unet_set_stream(self.u, stream))
+
+    @staticmethod
+    def batch(features, target=None, weight=None, origin=(0, 0, 0), size=None):
+        """features: CUDA float32 tensor [4][fz][fy][fx]; target/weight
+        [fz][fy][fx]; origin (ox, oy, oz) and size (nx, ny, nz) of the sub-box."""
+        fz, fy, fx = features.shape[1:]
+        nx, ny, nz = size if size is not None else (fx, fy, fz)
+        return UNetBatch(_ptr(features), _ptr(target), _ptr(weight), fx, fy, fz, *origin, nx, ny, nz)
+
+    def forward(self, batch, out):
+        _check(load().vfs_unet_forward(self.u, C.byref(batch), _ptr(out)))
+        return out
+
+    def gradient(self, batch, grad=None):
+        loss = C.c_double()
+        _check(load().vfs_unet_gradient(self.u, C.byref(batch), _ptr(grad), C.byref(loss)))
+        return loss.value
+
+    def train_step(self, batch, lr):
+        loss = C.c_double()
+        _check(load().vfs_unet_train_step(self.u, C.byref(batch), float(lr), C.byref(loss)))
+        return loss.value
+
+    def adam(self, lr, beta1=0.9, beta2=0.999, eps=1e-8):
+        _check(load().vfs_unet_adam(self.u, float(lr), float(beta1), float(beta2), float(eps)))
+
+    def kernel_launches(self):
+        return load().vfs_unet_kernel_launches(self.u)

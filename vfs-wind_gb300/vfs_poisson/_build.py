@@ -27,6 +27,7 @@ UNITS = {
     "poisson.cu": [],
     "noalloc.cu": ["-fmad=false"],
     "ibm.cu": ["-fmad=false", "-Xcompiler", "-ffp-contract=off"],
+    "unet.cu": [],
 }
 
 

@@ -287,14 +287,14 @@ def rod_surface(base, axis, length, radius, n_theta=24, n_len=8, up=(0.0, 0.0, 1
     return xyz, np.asarray(tri, np.int32)
 
 
-def tower_surfaces(array=(3, 2), radius=0.02, height=0.6, n_theta=24, n_len=12):
+def tower_surfaces(array=(3, 2), radius=0.02, height=0.6, n_theta=24, n_len=12, y0=0.0):
     """Closed vertical tower cylinders at the positions of the towers case
     (0.25 streamwise, 0.3 spanwise spacing about the domain centre), from
-    y = 0 to `height`: one surface per tower (body ibi)."""
+    y = `y0` to `y0 + height`: one surface per tower (body ibi)."""
     ax, az = array
     xs = 0.5 + 0.25 * (np.arange(ax) - (ax - 1) / 2)
     zs = 0.5 + 0.3 * (np.arange(az) - (az - 1) / 2)
-    return [rod_surface((x0, 0.0, z0), (0.0, 1.0, 0.0), height, radius, n_theta, n_len)
+    return [rod_surface((x0, y0, z0), (0.0, 1.0, 0.0), height, radius, n_theta, n_len)
             for x0 in xs for z0 in zs]
 
 

@@ -10,7 +10,10 @@
  * (Source/init.c:157-161).  Every array pointer may be host memory or device
  * memory of the handle's GPU; the library detects which and copies host
  * arrays through the handle's stream.  Calls are synchronous on return and a
- * handle is not thread-safe.
+ * handle is not thread-safe.  The handle's private stream is a blocking
+ * stream, so device inputs written on the legacy default stream are ready
+ * when a call starts; inputs written on another stream must be complete (or
+ * that stream passed to vfs_poisson_set_stream).
  *
  * Return codes: 0 on success, negative VFS_E* on failure; a failing call
  * leaves the handle usable.  vfs_last_error() gives a message.
@@ -176,7 +179,7 @@ int vfs_poisson_mg_vcycle(vfs_poisson *h, int precision, const double *r, double
 int64_t vfs_poisson_kernel_launches(vfs_poisson *h);
 
 /* Run the handle's work on a caller's CUDA stream (cudaStream_t passed as
- * void*); NULL returns to a private stream.  No reference counterpart: the
+ * void*); NULL returns to a private (blocking) stream.  No reference counterpart: the
  * reference is CPU-only. */
 int vfs_poisson_set_stream(vfs_poisson *h, void *stream);
 
@@ -238,7 +241,13 @@ typedef struct vfs_unet vfs_unet;
 /* A sub-box of feature planes (device memory, FP32): features
  * [4][fz][fy][fx], target and weight [fz][fy][fx] (training only).  The
  * network runs on the sub-box (ox..ox+nx-1, ...); nx, ny, nz multiples of 4.
- * The loss is sum(weight * (out - target)^2) / sum(weight). */
+ * Without `op` the loss is sum(weight * (out - target)^2) / sum(weight).
+ * With `op` (the 19 planes [19][fz][fy][fx] of the row-scaled operator, as
+ * vfs_poisson_get_operator32 gives them) the loss is
+ *   mse_weight * that  +  res_weight * sum_i w_i res_i^2 / sum_i w_i,
+ *   res = features[2] - op_scale * (A out)
+ * over the sub-box cells whose 19 neighbours lie inside it: the residual of
+ * the correction the output stands for, in the units of feature plane 2. */
 typedef struct {
   const float *features;
   const float *target;
@@ -246,6 +255,10 @@ typedef struct {
   int fx, fy, fz;
   int ox, oy, oz;
   int nx, ny, nz;
+  const float *op;
+  float op_scale;
+  float mse_weight;
+  float res_weight;
 } vfs_unet_batch;
 
 int vfs_unet_create(unsigned int seed, vfs_unet **out);
@@ -269,26 +282,35 @@ int64_t vfs_unet_kernel_launches(vfs_unet *u);
 
 /* Learned initial guess for the current right-hand side (vfs_poisson_rhs
  * first), from phi at steps n-1 and n-2 (DA layout, host or device).  The
- * network sees four box-layout planes: phi_{n-1}, phi_{n-1} - phi_{n-2},
- * aj * (b - A phi_ex) with phi_ex = 2 phi_{n-1} - phi_{n-2} (the residual
- * of the linear extrapolation in the aj-scaled system), each divided by its
- * RMS over the dofs, and the dof flag.  It predicts the correction
- * phi_n - phi_ex in units of kappa * RMS(aj * (b - A phi_ex)).  The plain
- * solver then judges the guess: the learned guess and the previous step's
- * phi are both measured by their FP64 residual and the smaller one becomes
- * the solver's iterate (*chosen = 1 for the learned guess, 0 for the
- * previous step; rel_res[0..1] = their relative residuals).  Solve from it
- * with opts.warm_start = 2.  The network runs on the handle's stream (its
- * stream is set to it); box dims must be multiples of 4. */
+ * network sees four planes on the half-resolution grid (2x2x2 averages over
+ * the dof cells): phi_{n-1}, phi_{n-1} - phi_{n-2}, aj * (b - A phi_ex)
+ * with phi_ex = 2 phi_{n-1} - phi_{n-2} (the residual of the linear
+ * extrapolation in the aj-scaled system), each divided by its RMS over the
+ * dofs, and the dof fraction.  Its output, the correction phi_n - phi_ex in
+ * units of kappa * RMS(aj * (b - A phi_ex)), is prolonged trilinearly to the
+ * cells and smoothed by two passes of the 27-point binomial filter
+ * (environment variable VFS_GUESS_SMOOTH sets the count).  The plain solver
+ * then judges the guess: the learned guess and the previous step's phi are
+ * both measured by their FP64 residual and the smaller one becomes the
+ * solver's iterate (*chosen = 1 for the learned guess, 0 for the previous
+ * step; rel_res[0..1] = their relative residuals).  Solve from it with
+ * opts.warm_start = 2.  The network runs on the handle's stream (its stream
+ * is set to it); box dims must be multiples of 8. */
 int vfs_poisson_learned_guess(vfs_poisson *h, vfs_unet *u, const double *phi_nm1, const double *phi_nm2,
                               double kappa, int *chosen, double *rel_res);
 
-/* One training sample of the learned guess: the four feature planes of the
- * current right-hand side (as above), the target (phi_n - phi_ex) /
- * RMS(aj * (b - A phi_ex)) and the loss weight (dof flag), all box layout
- * FP32 device memory (features 4 planes; target, weight 1 plane). */
+/* One training sample of the learned guess on the half-resolution grid
+ * (box dims / 2): the four feature planes of the current right-hand side
+ * (as above), the target (phi_n - phi_ex) / RMS(aj * (b - A phi_ex))
+ * averaged over the dof children, and the loss weight (dof fraction); FP32
+ * device memory (features 4 planes; target, weight 1 plane). */
 int vfs_poisson_guess_sample(vfs_poisson *h, const double *phi_n, const double *phi_nm1, const double *phi_nm2,
                              float *features, float *target, float *weight);
+
+/* The finest level's row-scaled FP32 operator (the aj-scaled PoissonLHSNew
+ * rows of the V-cycle): 19 box-layout planes in the slot order C E W N S T
+ * B NE SE NW SW TN BN TS BS TE BE TW BW (host or device memory, 19 n). */
+int vfs_poisson_get_operator32(vfs_poisson *h, float *planes);
 
 #ifdef __cplusplus
 }

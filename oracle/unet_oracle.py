@@ -88,13 +88,36 @@ def forward(params, features, bf16=True, requires_grad=False):
     return out, leaves
 
 
-def loss_and_grad(params, features, target, weight, bf16=True):
-    """Weighted MSE sum(w (out - t)^2) / sum(w) and its gradient as a flat
-    vector in the parameter layout."""
+OFFSETS = [(0, 0, 0), (1, 0, 0), (-1, 0, 0), (0, 1, 0), (0, -1, 0), (0, 0, 1), (0, 0, -1), (1, 1, 0), (1, -1, 0),
+           (-1, 1, 0), (-1, -1, 0), (0, 1, 1), (0, 1, -1), (0, -1, 1), (0, -1, -1), (1, 0, 1), (1, 0, -1),
+           (-1, 0, 1), (-1, 0, -1)]  # (di, dj, dk) of the 19 operator planes
+
+
+def residual_loss(out, f2, weight, op, scale):
+    """sum w res^2 / sum w over the cells whose 19 neighbours are inside,
+    res = f2 - scale * (A out); op: [19][nz][ny][nx] row coefficients."""
+    nz, ny, nx = out.shape
+    inner = (slice(1, nz - 1), slice(1, ny - 1), slice(1, nx - 1))
+    a = torch.zeros((nz - 2, ny - 2, nx - 2))
+    for t, (di, dj, dk) in enumerate(OFFSETS):
+        a = a + op[t][inner] * out[1 + dk:nz - 1 + dk, 1 + dj:ny - 1 + dj, 1 + di:nx - 1 + di]
+    res = f2[inner] - scale * a
+    w = weight[inner]
+    return (w * res ** 2).sum() / w.sum()
+
+
+def loss_and_grad(params, features, target, weight, bf16=True, op=None, op_scale=1.0, mse_weight=1.0,
+                  res_weight=0.0):
+    """Weighted MSE sum(w (out - t)^2) / sum(w) (times mse_weight when a
+    residual term is present) plus res_weight times the residual loss, and
+    the gradient as a flat vector in the parameter layout."""
     out, leaves = forward(params, features, bf16, requires_grad=True)
     t = torch.as_tensor(np.asarray(target, np.float32))
     w = torch.as_tensor(np.asarray(weight, np.float32))
     loss = (w * (out - t) ** 2).sum() / w.sum().clamp(min=1.0)
+    if op is not None:
+        f2 = torch.as_tensor(np.asarray(features, np.float32))[2]
+        loss = mse_weight * loss + res_weight * residual_loss(out, f2, w, torch.as_tensor(op), op_scale)
     loss.backward()
     g = []
     for q in range(0, len(leaves) - 1, 2):

@@ -133,3 +133,23 @@ def test_training_reduces_loss(cuda_lib):
         last = net.train_step(b, 2e-3)
     assert last < 0.5 * first
     net.close()
+
+
+def test_residual_loss_gradient_matches_oracle(cuda_lib):
+    """The operator-residual loss (the quantity the solver judges a guess
+    by) and its gradient, with a random 19-point operator."""
+    import torch
+    import vfs_poisson as V
+    net, p = _net()
+    dims = (16, 12, 8)
+    (f, t, w), (fd, td, wd) = _data(dims, seed=4)
+    rng = np.random.default_rng(9)
+    op = rng.normal(size=(19,) + dims[::-1]).astype(np.float32) * 0.3
+    opd = torch.from_numpy(op).cuda()
+    g = np.zeros(net.num_params, np.float32)
+    b = V.UNet.batch(fd, td, wd, op=opd, op_scale=0.7, mse_weight=0.25, res_weight=1.0)
+    loss = net.gradient(b, g)
+    lref, gref = UO.loss_and_grad(p, f, t, w, op=op, op_scale=0.7, mse_weight=0.25, res_weight=1.0)
+    assert abs(loss - lref) <= 2e-2 * abs(lref)
+    assert _rel(g, gref) < GRAD_TOL
+    net.close()

@@ -127,12 +127,123 @@ __global__ void k_guess_target(Grid g, Box b, const uint8_t *rt, const double *p
     wt[c] = d ? 1.f : 0.f;
   }
 }
-// learned guess x = ex + kappa * rms(f2) * out on dofs
-__global__ void k_guess_compose(size_t n, const uint8_t *rt, const double *ex, const float *out, double kappa,
-                                const double *sums, double *x) {
+// 2x2x2 restriction of the fine planes to the network's half-resolution
+// grid: planes 0..2 (and the target) average over the dof children, plane
+// 3 (and the loss weight) is the dof fraction.
+__global__ void k_guess_restrict(Box b, const float *ff, const float *tf, float *fc, float *tc, float *wc) {
+  const int cx = b.nx / 2, cy = b.ny / 2, cz = b.nz / 2;
+  const size_t nc = (size_t)cx * cy * cz, nf = b.n();
+  for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < nc; c += (size_t)gridDim.x * blockDim.x) {
+    const int I = c % cx, J = (c / cx) % cy, K = c / ((size_t)cx * cy);
+    float w = 0.f, s0 = 0.f, s1 = 0.f, s2 = 0.f, st = 0.f;
+    for (int q = 0; q < 8; q++) {
+      const size_t f = b.at(2 * I + (q & 1), 2 * J + ((q >> 1) & 1), 2 * K + (q >> 2));
+      const float d = ff[3 * nf + f];
+      w += d;
+      s0 += d * ff[f];
+      s1 += d * ff[nf + f];
+      s2 += d * ff[2 * nf + f];
+      if (tf) st += d * tf[f];
+    }
+    const float inv = w > 0.f ? 1.f / w : 0.f;
+    fc[c] = s0 * inv;
+    fc[nc + c] = s1 * inv;
+    fc[2 * nc + c] = s2 * inv;
+    fc[3 * nc + c] = 0.125f * w;
+    if (tc) {
+      tc[c] = st * inv;
+      wc[c] = 0.125f * w;
+    }
+  }
+}
+// cell-centred trilinear prolongation of the half-resolution output
+__global__ void k_guess_prolong(Box b, const float *oc, float *of) {
+  const int cx = b.nx / 2, cy = b.ny / 2, cz = b.nz / 2;
+  for (size_t f = blockIdx.x * (size_t)blockDim.x + threadIdx.x; f < b.n(); f += (size_t)gridDim.x * blockDim.x) {
+    const int i = f % b.nx, j = (f / b.nx) % b.ny, k = f / ((size_t)b.nx * b.ny);
+    int I[2] = {i >> 1, (i & 1) ? (i >> 1) + 1 : (i >> 1) - 1};
+    int J[2] = {j >> 1, (j & 1) ? (j >> 1) + 1 : (j >> 1) - 1};
+    int K[2] = {k >> 1, (k & 1) ? (k >> 1) + 1 : (k >> 1) - 1};
+    I[1] = min(max(I[1], 0), cx - 1);
+    J[1] = min(max(J[1], 0), cy - 1);
+    K[1] = min(max(K[1], 0), cz - 1);
+    const float w[2] = {0.75f, 0.25f};
+    float s = 0.f;
+    for (int q = 0; q < 8; q++) {
+      const int a = q & 1, bb = (q >> 1) & 1, c = q >> 2;
+      s += w[a] * w[bb] * w[c] * oc[((size_t)K[c] * cy + J[bb]) * cx + I[a]];
+    }
+    of[f] = s;
+  }
+}
+// one pass of the 27-point binomial filter (1/4, 1/2, 1/4 per direction,
+// clamped at the box faces)
+__global__ void k_guess_smooth(Box b, const float *in, float *out) {
+  for (size_t f = blockIdx.x * (size_t)blockDim.x + threadIdx.x; f < b.n(); f += (size_t)gridDim.x * blockDim.x) {
+    const int i = f % b.nx, j = (f / b.nx) % b.ny, k = f / ((size_t)b.nx * b.ny);
+    float s = 0.f;
+    for (int dk = -1; dk <= 1; dk++)
+      for (int dj = -1; dj <= 1; dj++)
+        for (int di = -1; di <= 1; di++) {
+          const int a = min(max(i + di, 0), b.nx - 1), bb = min(max(j + dj, 0), b.ny - 1),
+                    c = min(max(k + dk, 0), b.nz - 1);
+          s += (di ? 0.25f : 0.5f) * (dj ? 0.25f : 0.5f) * (dk ? 0.25f : 0.5f) * in[b.at(a, bb, c)];
+        }
+    out[f] = s;
+  }
+}
+// The learned correction enters the guess band by band: cells are grouped
+// by their index distance to the nearest non-periodic y wall (where
+// stretched grids put their thinnest cells and stiffest rows), and each
+// band gets its own weight, chosen by least squares on the FP64 residual.
+constexpr int kGuessBands = 4;
+struct BandWeights {
+  double a[kGuessBands];
+};
+__device__ inline int guess_band(const Box &b, int j) {
+  if (b.py) return kGuessBands - 1;
+  const int d = min(j, b.ny - 1 - j);
+  return d < 2 ? 0 : (d < 8 ? 1 : (d < 32 ? 2 : 3));
+}
+// y_k = A (s c [band k, dof]) per row; block partials of G_kl = <y_k, y_l>
+// (k <= l, 10 rows) and g_k = <y_k, r> (4 rows), r = b - A ex.
+__global__ void k_guess_gram(Box b, const double *__restrict__ A, const uint8_t *__restrict__ rt,
+                             const float *__restrict__ c, const double *__restrict__ r, double kappa,
+                             const double *sums, double *partial) {
+  const double sc = kappa * plane_rms(sums, 2);
+  double acc[14];
+  for (int q = 0; q < 14; q++) acc[q] = 0.;
+  const uint32_t n = (uint32_t)b.n();
+  for (size_t cell = blockIdx.x * (size_t)blockDim.x + threadIdx.x; cell < n;
+       cell += (size_t)gridDim.x * blockDim.x) {
+    const int i = cell % b.nx, j = (cell / b.nx) % b.ny, k = cell / ((size_t)b.nx * b.ny);
+    uint32_t idx[NSLOT];
+    stencil_index(b, i, j, k, idx);
+    double y[kGuessBands] = {0., 0., 0., 0.};
+    for (int t = 0; t < NSLOT; t++) {
+      const uint32_t nb = idx[t];
+      if (rt[nb] != 1) continue;
+      y[guess_band(b, (nb / b.nx) % b.ny)] += A[(size_t)t * n + cell] * (double)c[nb];
+    }
+    const double rv = r[cell];
+    int q = 0;
+    for (int u = 0; u < kGuessBands; u++) {
+      y[u] *= sc;
+      for (int v = u; v < kGuessBands; v++) acc[q++] += y[u] * y[v];
+    }
+    for (int u = 0; u < kGuessBands; u++) acc[10 + u] += y[u] * rv;
+  }
+  for (int q = 0; q < 14; q++) {
+    const double t = block_sum(acc[q]);
+    if (threadIdx.x == 0) partial[(size_t)q * gridDim.x + blockIdx.x] = t;
+  }
+}
+// learned guess x = ex + kappa * rms(f2) * alpha[band] * out on dofs
+__global__ void k_guess_compose(Box b, const uint8_t *rt, const double *ex, const float *out, double kappa,
+                                const double *sums, BandWeights w, double *x) {
   const double s = kappa * plane_rms(sums, 2);
-  for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < n; c += (size_t)gridDim.x * blockDim.x)
-    x[c] = rt[c] == 1 ? ex[c] + s * (double)out[c] : 0.;
+  for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < b.n(); c += (size_t)gridDim.x * blockDim.x)
+    x[c] = rt[c] == 1 ? ex[c] + s * w.a[guess_band(b, (c / b.nx) % b.ny)] * (double)out[c] : 0.;
 }
 
 __device__ inline void atomic_max_pos(double *addr, double v) {
@@ -227,7 +338,8 @@ struct vfs_poisson {
   // learned initial guess: extrapolated phi, plane sums, feature planes and
   // network output (box layout, allocated on first use)
   double *gex = nullptr, *gsum = nullptr;
-  float *gfeat = nullptr, *gout = nullptr;
+  float *gfeat = nullptr, *gtgt = nullptr, *gfc = nullptr, *gout = nullptr, *gof[2] = {nullptr, nullptr};
+  int gsmooth = 2;  // binomial passes over the prolonged correction
   std::vector<Level> L;
   bool have_grid = false, have_nvert = false, have_rhs = false, have_phi = false;
   // graphs of the V-cycle per precision and parameters they were built for
@@ -969,7 +1081,9 @@ int vfs_poisson_create(const vfs_grid_desc *gd, vfs_poisson **out) {
   h->box = Box{nx, ny, nz, px, py, pz};
   cudaGetDevice(&h->device);
   auto bail = [&](int rc) { vfs_poisson_destroy(h); return rc; };
-  if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) {
+  // a blocking stream: work the caller queued on the legacy default stream
+  // (e.g. filling a device input array) completes before ours starts
+  if (cudaStreamCreateWithFlags(&h->stream, cudaStreamDefault) != cudaSuccess) {
     cudaGetLastError();
     delete h;
     return fail(VFS_ECUDA, "cudaStreamCreate failed (no usable GPU?)");
@@ -1144,16 +1258,25 @@ int guess_buffers(vfs_poisson *h) {
     TRY(dalloc(h, &h->gex, n));
     TRY(dalloc(h, &h->gsum, 8));
     TRY(dalloc(h, &h->gfeat, 4 * n));
-    TRY(dalloc(h, &h->gout, n));
+    TRY(dalloc(h, &h->gtgt, n));
+    TRY(dalloc(h, &h->gfc, 4 * (n / 8 + 1)));
+    TRY(dalloc(h, &h->gout, n / 8 + 1));
+    TRY(dalloc(h, &h->gof[0], n));
+    TRY(dalloc(h, &h->gof[1], n));
+    const char *e = getenv("VFS_GUESS_SMOOTH");
+    if (e) h->gsmooth = std::max(0, std::min(8, atoi(e)));
   }
   return VFS_OK;
 }
 
-// feature planes of the current right-hand side into `feat` (4 planes)
-int guess_features(vfs_poisson *h, const double *phi_nm1, const double *phi_nm2, float *feat) {
-  if (!h || !phi_nm1 || !phi_nm2 || !feat) return fail(VFS_EINVAL, "null argument");
+// fine feature planes of the current right-hand side into h->gfeat
+int guess_features(vfs_poisson *h, const double *phi_nm1, const double *phi_nm2) {
+  if (!h || !phi_nm1 || !phi_nm2) return fail(VFS_EINVAL, "null argument");
   if (!h->have_rhs) return fail(VFS_ESTATE, "rhs must come before the guess");
+  if (h->box.nx % 8 || h->box.ny % 8 || h->box.nz % 8)
+    return fail(VFS_EINVAL, "the learned guess needs box dims that are multiples of 8");
   TRY(guess_buffers(h));
+  float *feat = h->gfeat;
   const size_t n = h->box.n(), N = h->g.n();
   TRY(upload(h, h->stage, phi_nm1, N));
   TRY(upload(h, h->stage + N, phi_nm2, N));
@@ -1174,11 +1297,20 @@ int vfs_poisson_guess_sample(vfs_poisson *h, const double *phi_n, const double *
   if (!phi_n || !target || !weight) return fail(VFS_EINVAL, "null argument");
   if (!is_device_ptr(features) || !is_device_ptr(target) || !is_device_ptr(weight))
     return fail(VFS_EINVAL, "features, target and weight must be device memory");
-  TRY(guess_features(h, phi_nm1, phi_nm2, features));
+  TRY(guess_features(h, phi_nm1, phi_nm2));
   const size_t N = h->g.n();
   TRY(upload(h, h->stage + 2 * N, phi_n, N));
-  LAUNCH(h, k_guess_target, kRedBlocks, 256, h->g, h->box, h->rowtype0, h->stage + 2 * N, h->gex, h->gsum, target,
-         weight);
+  LAUNCH(h, k_guess_target, kRedBlocks, 256, h->g, h->box, h->rowtype0, h->stage + 2 * N, h->gex, h->gsum, h->gtgt,
+         h->gof[0]);
+  LAUNCH(h, k_guess_restrict, kRedBlocks, 256, h->box, h->gfeat, h->gtgt, features, target, weight);
+  return sync(h);
+}
+
+int vfs_poisson_get_operator32(vfs_poisson *h, float *planes) {
+  if (!h || !planes) return fail(VFS_EINVAL, "null argument");
+  if (!h->have_nvert || h->L.empty() || !h->L[0].A32) return fail(VFS_ESTATE, "set_nvert must come first");
+  CUDA_TRY(cudaMemcpyAsync(planes, h->L[0].A32, (size_t)NSLOT * h->box.n() * sizeof(float), cudaMemcpyDefault,
+                           h->stream));
   return sync(h);
 }
 
@@ -1186,16 +1318,70 @@ int vfs_poisson_learned_guess(vfs_poisson *h, vfs_unet *u, const double *phi_nm1
                               double kappa, int *chosen, double *rel_res) {
   if (!h || !u) return fail(VFS_EINVAL, "null argument");
   const Box b = h->box;
-  if (b.nx % 4 || b.ny % 4 || b.nz % 4) return fail(VFS_EINVAL, "the learned guess needs box dims that are multiples of 4");
   TRY(ensure_krylov(h, std::max(h->m_alloc, 20)));
-  TRY(guess_buffers(h));
-  TRY(guess_features(h, phi_nm1, phi_nm2, h->gfeat));
+  TRY(guess_features(h, phi_nm1, phi_nm2));
   const size_t n = b.n();
+  LAUNCH(h, k_guess_restrict, kRedBlocks, 256, b, h->gfeat, nullptr, h->gfc, nullptr, nullptr);
   vfs_unet_set_stream(u, h->stream);
-  vfs_unet_batch bt{h->gfeat, nullptr, nullptr, b.nx, b.ny, b.nz, 0, 0, 0, b.nx, b.ny, b.nz};
+  const int hx = b.nx / 2, hy = b.ny / 2, hz = b.nz / 2;
+  vfs_unet_batch bt{h->gfc, nullptr, nullptr, hx, hy, hz, 0, 0, 0, hx, hy, hz, nullptr, 0.f, 0.f, 0.f};
+  const int64_t before = vfs_unet_kernel_launches(u);
   TRY(vfs_unet_forward(u, &bt, h->gout));
-  h->launches += vfs_unet_kernel_launches(u);
-  LAUNCH(h, k_guess_compose, kRedBlocks, 256, n, h->rowtype0, h->gex, h->gout, kappa, h->gsum, h->x);
+  h->launches += vfs_unet_kernel_launches(u) - before;
+  LAUNCH(h, k_guess_prolong, kRedBlocks, 256, b, h->gout, h->gof[0]);
+  int cur = 0;
+  for (int p = 0; p < h->gsmooth; p++, cur ^= 1)
+    LAUNCH(h, k_guess_smooth, kRedBlocks, 256, b, h->gof[cur], h->gof[cur ^ 1]);
+  // least-squares band weights: minimise ||r_ex - sum_k alpha_k y_k||
+  // (alpha = 0 is the plain extrapolation, so the guess is never worse)
+  LAUNCH(h, k_guess_gram, kRedBlocks, 256, b, h->A0, h->rowtype0, h->gof[cur], h->r, kappa, h->gsum, h->partial);
+  double gm[14];
+  TRY(reduce_read(h, kRedBlocks, 14, gm));
+  BandWeights bw{};
+  {
+    // the normal equations G alpha = g (symmetric positive semi-definite)
+    // by Cholesky over the bands that carry a correction
+    double G[kGuessBands][kGuessBands], g[kGuessBands];
+    int q = 0;
+    for (int u = 0; u < kGuessBands; u++)
+      for (int v = u; v < kGuessBands; v++) G[u][v] = G[v][u] = gm[q++];
+    for (int u = 0; u < kGuessBands; u++) g[u] = gm[10 + u];
+    double gmax = 0.;
+    for (int u = 0; u < kGuessBands; u++) gmax = std::max(gmax, G[u][u]);
+    int ids[kGuessBands], na = 0;
+    for (int u = 0; u < kGuessBands; u++)
+      if (gmax > 0. && G[u][u] > 1e-14 * gmax) ids[na++] = u;
+    double L[kGuessBands][kGuessBands] = {}, z[kGuessBands] = {}, al[kGuessBands] = {};
+    bool ok = na > 0;
+    for (int p = 0; p < na && ok; p++) {
+      for (int r2 = 0; r2 <= p; r2++) {
+        double v = G[ids[p]][ids[r2]] * (p == r2 ? 1. + 1e-10 : 1.);
+        for (int t = 0; t < r2; t++) v -= L[p][t] * L[r2][t];
+        if (p == r2) {
+          if (!(v > 0.)) { ok = false; break; }
+          L[p][p] = std::sqrt(v);
+        } else {
+          L[p][r2] = v / L[r2][r2];
+        }
+      }
+    }
+    if (ok) {
+      for (int p = 0; p < na; p++) {
+        double v = g[ids[p]];
+        for (int t = 0; t < p; t++) v -= L[p][t] * z[t];
+        z[p] = v / L[p][p];
+      }
+      for (int p = na - 1; p >= 0; p--) {
+        double v = z[p];
+        for (int t = p + 1; t < na; t++) v -= L[t][p] * al[t];
+        al[p] = v / L[p][p];
+      }
+      for (int p = 0; p < na; p++) bw.a[ids[p]] = al[p];
+    }
+  }
+  if (h->phase)
+    fprintf(stderr, "vfs guess band weights: %.4g %.4g %.4g %.4g\n", bw.a[0], bw.a[1], bw.a[2], bw.a[3]);
+  LAUNCH(h, k_guess_compose, kRedBlocks, 256, b, h->rowtype0, h->gex, h->gof[cur], kappa, h->gsum, bw, h->x);
   // the plain solver judges: keep whichever of the learned guess and the
   // previous step's phi has the smaller FP64 residual
   LAUNCH(h, k_da_to_box, lin_grid(n), 256, h->g, h->box, h->stage, h->gex);
@@ -1410,7 +1596,7 @@ int vfs_poisson_set_stream(vfs_poisson *h, void *stream) {
     h->stream = st;
     h->own_stream = false;
   } else {
-    CUDA_TRY(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+    CUDA_TRY(cudaStreamCreateWithFlags(&h->stream, cudaStreamDefault));
     h->own_stream = true;
   }
   return VFS_OK;

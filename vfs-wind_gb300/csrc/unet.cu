@@ -430,6 +430,113 @@ __global__ void k_head(const bf16 *d, size_t n, const float *wh, float *out, con
   if (threadIdx.x == 0) atomicAdd(loss, t);
 }
 
+// Stencil offsets of the 19-point operator planes (slot order of the
+// reference's PoissonLHSNew: C E W N S T B NE SE NW SW TN BN TS BS TE BE TW BW).
+__constant__ int8_t c_off[19][3] = {{0, 0, 0},   {1, 0, 0},   {-1, 0, 0}, {0, 1, 0},  {0, -1, 0},
+                                    {0, 0, 1},   {0, 0, -1},  {1, 1, 0},  {1, -1, 0}, {-1, 1, 0},
+                                    {-1, -1, 0}, {0, 1, 1},   {0, 1, -1}, {0, -1, 1}, {0, -1, -1},
+                                    {1, 0, 1},   {1, 0, -1},  {-1, 0, 1}, {-1, 0, -1}};
+
+struct Crop {
+  int fx, fy, fz, ox, oy, oz, nx, ny, nz;
+  __device__ size_t glob(int x, int y, int z) const {
+    return ((size_t)(z + oz) * fy + (y + oy)) * fx + (x + ox);
+  }
+  __device__ bool inner(int x, int y, int z) const {
+    return x >= 1 && y >= 1 && z >= 1 && x < nx - 1 && y < ny - 1 && z < nz - 1;
+  }
+};
+
+// Residual of the learned correction on the crop's inner cells (all 19
+// neighbours inside the crop): res = f2 - s * (A out), A the row-scaled
+// operator (19 planes over the feature grid), q = w res; acc[0] += w,
+// acc[1] += w res^2.
+__global__ void k_res_fwd(Crop cr, const float *__restrict__ op, const float *__restrict__ f2,
+                          const float *__restrict__ wt, const float *__restrict__ out, float s, float *q,
+                          float *acc) {
+  __shared__ float sh[32];
+  const size_t n = (size_t)cr.nx * cr.ny * cr.nz, plane = (size_t)cr.fx * cr.fy * cr.fz;
+  float sw = 0.f, sr = 0.f;
+  for (size_t v = blockIdx.x * (size_t)blockDim.x + threadIdx.x; v < n; v += (size_t)gridDim.x * blockDim.x) {
+    const int x = (int)(v % cr.nx), y = (int)((v / cr.nx) % cr.ny), z = (int)(v / ((size_t)cr.nx * cr.ny));
+    float qv = 0.f;
+    if (cr.inner(x, y, z)) {
+      const size_t gv = cr.glob(x, y, z);
+      const float w = wt[gv];
+      if (w > 0.f) {
+        float a = 0.f;
+        for (int t = 0; t < 19; t++)
+          a += op[t * plane + gv] * out[((size_t)(z + c_off[t][2]) * cr.ny + (y + c_off[t][1])) * cr.nx + x + c_off[t][0]];
+        const float res = f2[gv] - s * a;
+        qv = w * res;
+        sw += w;
+        sr += w * res * res;
+      }
+    }
+    q[v] = qv;
+  }
+  sw = block_sum(sw, sh);
+  if (threadIdx.x == 0) atomicAdd(acc, sw);
+  sr = block_sum(sr, sh);
+  if (threadIdx.x == 0) atomicAdd(acc + 1, sr);
+}
+
+// dLoss/dout = alpha * 2 w (out - t) / sum(w)  -  beta * 2 s A^T q / acc[0];
+// the MSE part is added to the loss.
+__global__ void k_res_bwd(Crop cr, const float *__restrict__ op, const float *__restrict__ q, const float *acc,
+                          float s, float beta, const float *__restrict__ out, const float *__restrict__ tgt,
+                          const float *__restrict__ wt, const float *wsum, float alpha, float *gout, float *loss) {
+  __shared__ float sh[32];
+  const size_t n = (size_t)cr.nx * cr.ny * cr.nz, plane = (size_t)cr.fx * cr.fy * cr.fz;
+  const float ir = acc[0] > 0.f ? 2.f * s * beta / acc[0] : 0.f;
+  const float im = alpha / fmaxf(*wsum, 1.f);
+  float lm = 0.f;
+  for (size_t v = blockIdx.x * (size_t)blockDim.x + threadIdx.x; v < n; v += (size_t)gridDim.x * blockDim.x) {
+    const int x = (int)(v % cr.nx), y = (int)((v / cr.nx) % cr.ny), z = (int)(v / ((size_t)cr.nx * cr.ny));
+    const size_t gv = cr.glob(x, y, z);
+    float g = 0.f;
+    if (alpha > 0.f) {
+      const float w = wt[gv] * im, e = out[v] - tgt[gv];
+      g += 2.f * w * e;
+      lm += w * e * e;
+    }
+    float at = 0.f;
+    for (int t = 0; t < 19; t++) {
+      const int xi = x - c_off[t][0], yi = y - c_off[t][1], zi = z - c_off[t][2];
+      if (!cr.inner(xi, yi, zi)) continue;
+      at += op[t * plane + cr.glob(xi, yi, zi)] * q[((size_t)zi * cr.ny + yi) * cr.nx + xi];
+    }
+    gout[v] = g - ir * at;
+  }
+  lm = block_sum(lm, sh);
+  if (threadIdx.x == 0) atomicAdd(loss, lm);
+}
+
+// Head backward from dLoss/dout: gd[v][c] = gout wh[c]; head gradients.
+__global__ void k_head_bwd(const bf16 *d, size_t n, const float *wh, const float *gout, float *gd, float *gwh) {
+  __shared__ float sh[32];
+  float lw[17];
+  for (int c = 0; c < 17; c++) lw[c] = 0.f;
+  for (size_t v = blockIdx.x * (size_t)blockDim.x + threadIdx.x; v < n; v += (size_t)gridDim.x * blockDim.x) {
+    const uint4 *src = reinterpret_cast<const uint4 *>(d + v * 16);
+    uint4 q0 = src[0], q1 = src[1];
+    const bf16 *h0 = reinterpret_cast<const bf16 *>(&q0), *h1 = reinterpret_cast<const bf16 *>(&q1);
+    const float go = gout[v];
+    float4 *gdst = reinterpret_cast<float4 *>(gd + v * 16);
+    for (int c = 0; c < 4; c++)
+      gdst[c] = make_float4(go * wh[4 * c], go * wh[4 * c + 1], go * wh[4 * c + 2], go * wh[4 * c + 3]);
+    for (int c = 0; c < 8; c++) {
+      lw[c] += go * __bfloat162float(h0[c]);
+      lw[c + 8] += go * __bfloat162float(h1[c]);
+    }
+    lw[16] += go;
+  }
+  for (int c = 0; c < 17; c++) {
+    const float t = block_sum(lw[c], sh);
+    if (threadIdx.x == 0) atomicAdd(&gwh[c], t);
+  }
+}
+
 // Adam (bias-corrected; c1 = 1 - beta1^t, c2 = 1 - beta2^t).
 __global__ void k_adam(float *p, const float *g, float *m, float *v, size_t n, float lr, float b1, float b2, float c1,
                        float c2, float eps) {
@@ -478,7 +585,7 @@ struct vfs_unet {
   std::vector<void *> bufs;
   bf16 *xin, *e0a, *e0b, *p0, *e1a, *e1b, *p1, *e2a, *e2b, *d1a, *d1b, *d0a, *d0b, *gpre;
   float *g_d0b, *g_d0a, *g_upd1b, *g_e0b, *g_d1b, *g_d1a, *g_upe2b, *g_e1b, *g_e2b, *g_e2a, *g_p1, *g_e1a, *g_p0,
-      *g_e0a, *scal;
+      *g_e0a, *scal, *obuf, *qbuf, *gobuf;
   int64_t launches = 0;
 };
 
@@ -538,7 +645,7 @@ int ensure_bufs(vfs_unet *u, int nx, int ny, int nz, bool train) {
   if (train) {
     A(gpre, n0 * 16) A(g_d0b, n0 * 16) A(g_d0a, n0 * 16) A(g_upd1b, n0 * 32) A(g_e0b, n0 * 16) A(g_d1b, n1 * 32)
     A(g_d1a, n1 * 32) A(g_upe2b, n1 * 64) A(g_e1b, n1 * 32) A(g_e2b, n2 * 64) A(g_e2a, n2 * 64) A(g_p1, n2 * 32)
-    A(g_e1a, n1 * 32) A(g_p0, n1 * 16) A(g_e0a, n0 * 16)
+    A(g_e1a, n1 * 32) A(g_p0, n1 * 16) A(g_e0a, n0 * 16) A(obuf, n0) A(qbuf, n0) A(gobuf, n0)
   }
 #undef A
   u->nx = nx;
@@ -743,6 +850,7 @@ int loss_grad(vfs_unet *u, const vfs_unet_batch *bt, double *loss) {
   if (bt->ox < 0 || bt->oy < 0 || bt->oz < 0 || bt->ox + bt->nx > bt->fx || bt->oy + bt->ny > bt->fy ||
       bt->oz + bt->nz > bt->fz)
     return fail(VFS_EINVAL, "sub-box outside the feature planes");
+  if (bt->op && (bt->nx < 3 || bt->ny < 3 || bt->nz < 3)) return fail(VFS_EINVAL, "residual loss needs inner cells");
   if ((rc = ensure_bufs(u, bt->nx, bt->ny, bt->nz, true))) return rc;
   if (!u->packed) pack(u);
   Box3 b{bt->features, bt->target, bt->weight, bt->fx, bt->fy, bt->fz, bt->ox, bt->oy, bt->oz};
@@ -751,16 +859,32 @@ int loss_grad(vfs_unet *u, const vfs_unet_batch *bt, double *loss) {
   cudaMemsetAsync(u->scal, 0, 64 * sizeof(float), u->stream);
   k_weight_sum<<<grid_for(n0), 256, 0, u->stream>>>(b.wt, b.fx, b.fy, b.ox, b.oy, b.oz, bt->nx, bt->ny, bt->nz,
                                                    u->scal);
-  k_head<<<grid_for(n0), 256, 0, u->stream>>>(u->d0b, n0, u->params + u->head, nullptr, b.tgt, b.wt, b.fx, b.fy,
-                                             b.ox, b.oy, b.oz, bt->nx, bt->ny, u->scal, u->g_d0b,
-                                             u->grads + u->head, u->scal + 1);
-  u->launches += 2;
+  if (!bt->op) {
+    k_head<<<grid_for(n0), 256, 0, u->stream>>>(u->d0b, n0, u->params + u->head, nullptr, b.tgt, b.wt, b.fx, b.fy,
+                                               b.ox, b.oy, b.oz, bt->nx, bt->ny, u->scal, u->g_d0b,
+                                               u->grads + u->head, u->scal + 1);
+    u->launches += 2;
+  } else {
+    // residual loss (+ optional MSE) through the row-scaled operator
+    Crop cr{b.fx, b.fy, b.fz, b.ox, b.oy, b.oz, bt->nx, bt->ny, bt->nz};
+    const size_t plane = (size_t)b.fx * b.fy * b.fz;
+    k_head<<<grid_for(n0), 256, 0, u->stream>>>(u->d0b, n0, u->params + u->head, u->obuf, nullptr, nullptr, 0, 0,
+                                               0, 0, 0, bt->nx, bt->ny, nullptr, nullptr, nullptr, nullptr);
+    k_res_fwd<<<grid_for(n0), 256, 0, u->stream>>>(cr, bt->op, b.feat + 2 * plane, b.wt, u->obuf, bt->op_scale,
+                                                  u->qbuf, u->scal + 2);
+    k_res_bwd<<<grid_for(n0), 256, 0, u->stream>>>(cr, bt->op, u->qbuf, u->scal + 2, bt->op_scale, bt->res_weight,
+                                                  u->obuf, b.tgt, b.wt, u->scal, bt->mse_weight, u->gobuf,
+                                                  u->scal + 1);
+    k_head_bwd<<<grid_for(n0), 256, 0, u->stream>>>(u->d0b, n0, u->params + u->head, u->gobuf, u->g_d0b,
+                                                   u->grads + u->head);
+    u->launches += 5;
+  }
   backward(u);
-  float l = 0.f;
-  cudaMemcpyAsync(&l, u->scal + 1, sizeof(float), cudaMemcpyDeviceToHost, u->stream);
+  float l[4] = {0.f, 0.f, 0.f, 0.f};
+  cudaMemcpyAsync(l, u->scal, 4 * sizeof(float), cudaMemcpyDeviceToHost, u->stream);
   cudaError_t e = cudaStreamSynchronize(u->stream);
   if (e != cudaSuccess) return fail(VFS_ECUDA, std::string("U-Net step: ") + cudaGetErrorString(e));
-  if (loss) *loss = l;
+  if (loss) *loss = l[1] + (bt->op && l[2] > 0.f ? bt->res_weight * l[3] / l[2] : 0.f);
   return cuda_status("U-Net step");
 }
 

@@ -37,6 +37,7 @@ EXPORTS = [
     "vfs_unet_create", "vfs_unet_destroy", "vfs_unet_set_stream", "vfs_unet_num_params", "vfs_unet_get_params",
     "vfs_unet_set_params", "vfs_unet_forward", "vfs_unet_gradient", "vfs_unet_train_step", "vfs_unet_adam",
     "vfs_unet_set_grads", "vfs_unet_kernel_launches", "vfs_poisson_learned_guess", "vfs_poisson_guess_sample",
+    "vfs_poisson_get_operator32",
 ]
 
 
@@ -56,7 +57,8 @@ class SolveOpts(C.Structure):
 class UNetBatch(C.Structure):
     _fields_ = [("features", C.c_void_p), ("target", C.c_void_p), ("weight", C.c_void_p),
                 ("fx", C.c_int), ("fy", C.c_int), ("fz", C.c_int), ("ox", C.c_int), ("oy", C.c_int),
-                ("oz", C.c_int), ("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int)]
+                ("oz", C.c_int), ("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int),
+                ("op", C.c_void_p), ("op_scale", C.c_float), ("mse_weight", C.c_float), ("res_weight", C.c_float)]
 
 
 class SolveStats(C.Structure):
@@ -132,6 +134,7 @@ def load(path=LIB_PATH):
     L.vfs_unet_kernel_launches.restype = C.c_int64
     L.vfs_poisson_learned_guess.argtypes = [vp, vp, vp, vp, C.c_double, P(C.c_int), vp]
     L.vfs_poisson_guess_sample.argtypes = [vp, vp, vp, vp, vp, vp, vp]
+    L.vfs_poisson_get_operator32.argtypes = [vp, vp]
     _lib = L
     return L
 
@@ -340,6 +343,14 @@ class PoissonSolver:
         _check(load().vfs_poisson_guess_sample(self.h, _ptr(phi_n), _ptr(phi_nm1), _ptr(phi_nm2), _ptr(features),
                                                _ptr(target), _ptr(weight)))
 
+    def operator32(self, out=None):
+        """The finest level's row-scaled FP32 operator, [19][nz][ny][nx]."""
+        if out is None:
+            mx, my, mz = self.dims
+            out = np.zeros((19, mz - 2, my - 2, mx - 2), np.float32)
+        _check(load().vfs_poisson_get_operator32(self.h, _ptr(out, True)))
+        return out
+
     def learned_guess(self, unet, phi_nm1, phi_nm2, kappa):
         """Install the better of the learned guess and phi_{n-1} as the
         iterate; returns (chosen, [rel_res_prev, rel_res_learned]).  Solve
@@ -390,12 +401,16 @@ class UNet:
         _check(load().vfs_unet_set_stream(self.u, stream))
 
     @staticmethod
-    def batch(features, target=None, weight=None, origin=(0, 0, 0), size=None):
+    def batch(features, target=None, weight=None, origin=(0, 0, 0), size=None, op=None, op_scale=1.0,
+              mse_weight=1.0, res_weight=0.0):
         """features: CUDA float32 tensor [4][fz][fy][fx]; target/weight
-        [fz][fy][fx]; origin (ox, oy, oz) and size (nx, ny, nz) of the sub-box."""
+        [fz][fy][fx]; origin (ox, oy, oz) and size (nx, ny, nz) of the
+        sub-box; op: the row-scaled operator planes [19][fz][fy][fx] for the
+        residual loss."""
         fz, fy, fx = features.shape[1:]
         nx, ny, nz = size if size is not None else (fx, fy, fz)
-        return UNetBatch(_ptr(features), _ptr(target), _ptr(weight), fx, fy, fz, *origin, nx, ny, nz)
+        return UNetBatch(_ptr(features), _ptr(target), _ptr(weight), fx, fy, fz, *origin, nx, ny, nz, _ptr(op),
+                         op_scale, mse_weight, res_weight)
 
     def forward(self, batch, out):
         _check(load().vfs_unet_forward(self.u, C.byref(batch), _ptr(out)))

@@ -36,6 +36,7 @@ class _Sequence:
     """Common part: grid, Fourier modes, per-step fluxes and face masking."""
 
     periodic = (0, 0, 0, 1, 0, 0)
+    moving = True  # the blanking changes every step
 
     def __init__(self, nx, ny, nz, coor, seed, device="cuda", noise=0.1, advect=0.5):
         import torch
@@ -128,6 +129,7 @@ class TowerSequence(_Sequence):
     per step in x."""
 
     periodic = (0, 0, 0, 1, 0, 1)
+    moving = False
 
     def __init__(self, nx=256, ny=192, nz=256, seed=1003, amp=0.02, ratio=1.03, device="cuda", n_theta=64):
         yc = CF._geometric(ny, ratio)

@@ -1,21 +1,33 @@
 #!/usr/bin/env python3
-"""Benchmark: ms per pressure-Poisson solve to a 1e-8 relative residual.
+"""Benchmark: ms per pressure-Poisson solve to a 1e-8 relative residual,
+learned guess + FP32 V-cycle in FP64 refinement vs the plain FP64 GPU solver.
 
 Workload: the 256x192x256 curvilinear wind-farm-like grid with a 3x2 array of
-tower cylinders (configuration 3), seeded synthetic Fourier-mode Ucont.  One
-step is one PoissonSolver_Hypre-equivalent call: right-hand side from Ucont,
-FGMRES with an FP32 multigrid V-cycle inside FP64 refinement to
-||b - A phi|| / ||b|| <= 1e-8 from a zero initial guess, fluid-mean removal and
-phi in DA layout.  The plain FP64 GPU solver (same FGMRES, FP64 V-cycle) is
-timed the same way and reported alongside.
+tower cylinders (configuration 3: geometric 1.03 wall stretching, amplitude
+0.02), run as a time sequence: the seeded Fourier-mode Ucont advects by 0.5
+cells per step in x, the towers (closed triangulated surfaces classified by
+the library's immersed-boundary search) stay put.  One step is one
+PoissonSolver_Hypre-equivalent call: right-hand side from Ucont, initial
+guess, FGMRES to ||b - A phi|| / ||b|| <= 1e-8 (FP64 residual), fluid-mean
+removal and phi in DA layout.
 
-Arms:
+  this arm (value)   learned initial guess (U-Net trained on the GPU on the
+                     plain solver's own solves of the first steps; the plain
+                     solver keeps it only if its FP64 residual beats the
+                     previous step's phi) + FP32 V-cycle inside FP64 FGMRES;
+                     guess time included.
+  plain FP64         the same FGMRES with an FP64 V-cycle, warm-started from
+                     the previous step's phi (the reference's Phi2 restart),
+                     timed on the same held-out steps (config.plain_fp64_ms).
+
+Arms of the driver:
   default            this library on the GPU (value: inputs resident in HBM;
                      e2e: host buffers through the C ABI)
   --impl reference   the reference's algorithm on the host cores: the CPU
                      port in oracle/ (the reference itself needs PETSc 3.1,
                      HYPRE and MPI, which are not available), each step a
-                     bounded sample of the same solve scaled to a full solve.
+                     bounded sample of the same warm-started solve scaled to
+                     a full solve.
 
 Multi-GPU: the solve does not shard in this library; under torchrun every
 rank runs an independent replica (weak scaling) and rank 0 reports.
@@ -37,7 +49,9 @@ for _p in (os.path.join(REPO, "vfs-wind_gb300"), os.path.join(REPO, "oracle"), R
         sys.path.insert(0, _p)
 
 METRIC = "ms per Poisson solve to 1e-8 rel. residual: learned+FP32/FP64 vs plain FP64 GPU"
-WORKLOAD = "towers 256x192x256 (config 3: geometric 1.03 wall stretching, amplitude 0.02, 3x2 tower cylinders)"
+def workload(nx, ny, nz):
+    return (f"towers {nx}x{ny}x{nz} sequence (config 3 grid: geometric 1.03 wall stretching, amplitude 0.02, "
+            "3x2 tower cylinders; Fourier Ucont advected 0.5 cells/step)")
 
 
 def parse():
@@ -49,6 +63,8 @@ def parse():
     ap.add_argument("--size", type=int, nargs=3, default=[256, 192, 256])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-sample-its", type=int, default=3)
+    ap.add_argument("--train-samples", type=int, default=16)
+    ap.add_argument("--train-steps", type=int, default=3000)
     return ap.parse_args()
 
 
@@ -115,60 +131,83 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def cpu_port_time(case, iterations_full, sample_its, threads=0):
-    """Time the oracle's CPU port of the solve (FP64 FGMRES + geometric
-    V-cycle, OpenMP over all host threads) for `sample_its` outer
-    iterations and scale to a full solve of `iterations_full` iterations."""
+def cpu_sequence_case(nx, ny, nz, step):
+    """The sequence's step `step` on the host: towers classified by the
+    oracle's restatement of the immersed-boundary search (identical to the
+    library's), Fourier Ucont advected like the GPU generator's."""
+    import numpy as np
     import oracle as O
-    d = O.dims_of(case)
-    met = O.form_metrics(d, case.coor)
-    lhs = O.poisson_lhs(d, case.nvert, met)
-    b = O.rhs(d, case.nvert, lhs["gid"], case.ucont, met["aj"])
-    bda = O.to_da(d, lhs["gid"], b)
-    mg = O.MGSolver(d, case.coor, case.nvert, met, threads=threads)
-    x, st = mg.solve(bda, rtol=1e-8, max_it=sample_its, restart=20)
-    ms_it = st.solve_ms / max(st.iterations, 1)
-    del mg
-    return ms_it, st.iterations, ms_it * iterations_full
+    from vfs_poisson import configs as CF, sequence as S
+    yc = CF._geometric(ny, 1.03)
+    coor = CF._nodes(nx, ny, nz, lambda e: np.interp(e, np.arange(ny + 1) / ny, yc), 0.02, physical=True)
+    periodic = S.TowerSequence.periodic
+    d = O.dims(nx + 2, ny + 2, nz + 2, periodic)
+    met = O.form_metrics(d, coor)
+    nv = None
+    for ibi, surf in enumerate(CF.tower_surfaces(radius=0.02, y0=-0.05, height=1.1, n_theta=64, n_len=4)):
+        nv, _ = O.ibm_search(d, met["cent"], surf, nvert=nv, ibi=ibi)
+    nv = CF.sync_periodic_ghosts(nv, periodic)
+    rng = np.random.default_rng(1003)
+    u = CF._mask_faces(CF._fourier_ucont(rng, nx, ny, nz, shift=0.5 * step), nv)
+    return CF.Case("towers_seq", nx, ny, nz, periodic, coor, nv, u), d, met
 
 
 def run_reference(args):
     rank, local, world = dist_env()
     if rank != 0:
         return
-    from vfs_poisson import configs as CF
+    import numpy as np
     import oracle as O
     O.build()
     nx, ny, nz = args.size
-    case = CF.towers(nx, ny, nz)
     cores = os.cpu_count()
-    d = O.dims_of(case)
-    met = O.form_metrics(d, case.coor)
-    lhs = O.poisson_lhs(d, case.nvert, met)
-    b = O.rhs(d, case.nvert, lhs["gid"], case.ucont, met["aj"])
-    bda = O.to_da(d, lhs["gid"], b)
-    mg = O.MGSolver(d, case.coor, case.nvert, met)
-    # warm-up: one full solve counts the outer iterations a full solve needs
-    _, full = mg.solve(bda, rtol=1e-8, max_it=60, restart=20)
+    case0, d, met = cpu_sequence_case(nx, ny, nz, 0)
+    case1, _, _ = cpu_sequence_case(nx, ny, nz, 1)
+    lhs = O.poisson_lhs(d, case0.nvert, met)
+    mg = O.MGSolver(d, case0.coor, case0.nvert, met)
+    b0 = O.to_da(d, lhs["gid"], O.rhs(d, case0.nvert, lhs["gid"], case0.ucont, met["aj"]))
+    b1 = O.to_da(d, lhs["gid"], O.rhs(d, case1.nvert, lhs["gid"], case1.ucont, met["aj"]))
+    # warm-up: the previous step's solution, then one full warm-started
+    # solve counts the outer iterations a full solve needs
+    phi0, _ = mg.solve(b0, rtol=1e-8, max_it=60, restart=20)
+    _, full = mg.solve(b1, rtol=1e-8, max_it=60, restart=20, x0_da=phi0)
     its_full = full.iterations
-    for _ in range(max(0, args.warmup - 1)):
-        mg.solve(bda, rtol=1e-8, max_it=args.cpu_sample_its, restart=20)
+    for _ in range(max(0, args.warmup - 2)):
+        mg.solve(b1, rtol=1e-8, max_it=args.cpu_sample_its, restart=20, x0_da=phi0)
     ms = []
     for _ in range(args.steps):
-        _, st = mg.solve(bda, rtol=1e-8, max_it=args.cpu_sample_its, restart=20)
+        _, st = mg.solve(b1, rtol=1e-8, max_it=args.cpu_sample_its, restart=20, x0_da=phi0)
         ms.append(st.solve_ms / max(st.iterations, 1) * its_full)
     value = statistics.mean(ms)
-    sample = (f"{args.cpu_sample_its} FGMRES iterations per step on the full {nx}x{ny}x{nz} grid, "
-              f"scaled to the {its_full} iterations of a full solve")
+    sample = (f"{args.cpu_sample_its} FGMRES iterations per step of the warm-started solve of sequence step 1 on "
+              f"the full {nx}x{ny}x{nz} grid, scaled to the {its_full} iterations of a full solve")
     line = {"metric": METRIC, "value": value, "unit": "ms", "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": value, "higher_is_better": False, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "cells": case.cells, "solver": "FGMRES(20) + geometric V-cycle, FP64",
+            "config": {"workload": workload(nx, ny, nz), "cells": nx * ny * nz,
+                       "solver": "FGMRES(20) + geometric V-cycle, FP64, previous-step initial guess",
                        "rtol": 1e-8, "iterations": its_full},
             "impl": "reference",
             "cpu_baseline": {"value": value, "unit": "ms", "cores": cores, "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": "ms", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+def cpu_port_time(nx, ny, nz, iterations_full, sample_its):
+    """The oracle's CPU port (FP64 FGMRES + geometric V-cycle, OpenMP over
+    all host threads) on sequence step 1 warm-started from step 0, timed for
+    `sample_its` iterations and scaled to `iterations_full`."""
+    import oracle as O
+    case0, d, met = cpu_sequence_case(nx, ny, nz, 0)
+    case1, _, _ = cpu_sequence_case(nx, ny, nz, 1)
+    lhs = O.poisson_lhs(d, case0.nvert, met)
+    mg = O.MGSolver(d, case0.coor, case0.nvert, met)
+    b0 = O.to_da(d, lhs["gid"], O.rhs(d, case0.nvert, lhs["gid"], case0.ucont, met["aj"]))
+    b1 = O.to_da(d, lhs["gid"], O.rhs(d, case1.nvert, lhs["gid"], case1.ucont, met["aj"]))
+    phi0, _ = mg.solve(b0, rtol=1e-8, max_it=sample_its, restart=20)
+    _, st = mg.solve(b1, rtol=1e-8, max_it=sample_its, restart=20, x0_da=phi0)
+    ms_it = st.solve_ms / max(st.iterations, 1)
+    return ms_it, st.iterations, ms_it * iterations_full
 
 
 def run_ours(args):
@@ -189,77 +228,134 @@ def run_ours(args):
     import __graft_entry__
     __graft_entry__.build()
     import vfs_poisson as V
-    from vfs_poisson import configs as CF
+    from vfs_poisson import learned as LG, sequence as S
 
     nx, ny, nz = args.size
-    case = CF.towers(nx, ny, nz)
-    s = V.PoissonSolver.from_case(case)
+    seq = S.TowerSequence(nx, ny, nz)
+    s = V.PoissonSolver(*seq.dims, periodic=seq.periodic)
     stream = torch.cuda.current_stream()
     s.set_stream(stream.cuda_stream)
-    shape = case.nvert.shape
-    ucont_d = torch.from_numpy(case.ucont).cuda()
-    phi_d = torch.zeros(shape, dtype=torch.float64, device="cuda")
-    mixed = V.default_opts(precision=0, rtol=1e-8)
-    plain = V.default_opts(precision=1, rtol=1e-8)
+    s.set_grid(seq.coor)
+    nv = seq.classify(s, 0)          # immersed-boundary search on the GPU
+    s.set_nvert(nv)
+    plain = V.default_opts(precision=1, rtol=1e-8, warm_start=1)
+    mixed = V.default_opts(precision=0, rtol=1e-8, warm_start=2)
 
-    def timed(opts, steps, warmup, host=None, prof=False, clocks=None):
-        u, phi = (ucont_d, phi_d) if host is None else host
-        s.profile(prof)  # the V-cycle graph is re-captured during warm-up, not in the timed region
-        for _ in range(warmup):
-            s.solver_hypre(u, phi=phi, opts=opts)
-        torch.cuda.synchronize()
-        barrier()
-        if prof:
-            s.profile(True)  # zero the counters
-        n0 = s.kernel_launches()
-        if clocks:
-            clocks.start()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    # 1. the plain solver generates the training data (steps 0 .. T+1)
+    t0 = time.time()
+    pool = LG.SamplePool((nx, ny, nz), args.train_samples)
+    hist, _ = LG.run_sequence(seq, s, args.train_samples + 2, plain, guess="prev", pool=pool)
+    t_data = time.time() - t0
+    # 2. the network is trained on the GPU by the library's own kernels
+    net = V.UNet(0)
+    t0 = time.time()
+    losses = LG.train(net, pool, args.train_steps, crop=(64, 64, 64), lr=1e-3, lr_end=2e-5)
+    torch.cuda.synchronize()
+    t_train = time.time() - t0
+    del pool
+    torch.cuda.empty_cache()
+
+    # 3. held-out steps: both arms on the same right-hand sides and history
+    def step_inputs(n):
+        return seq.mask_faces(seq.ucont(n), nv)
+
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+    def arm_plain(u, h):
+        phi = h[-1].clone()
         torch.cuda.synchronize()
         e0.record(stream)
-        its = []
-        for _ in range(steps):
-            _, st = s.solver_hypre(u, phi=phi, opts=opts)
-            its.append((st.iterations, st.rel_residual, st.status))
+        s.rhs(u)
+        _, st = s.solve(phi, opts=plain)
         e1.record(stream)
         torch.cuda.synchronize()
-        ck = clocks.stop() if clocks else None
-        barrier()
-        ms = e0.elapsed_time(e1) / steps
-        if dist is not None:
-            t = torch.tensor([ms], device="cuda")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            ms = float(t.item())
-        launches = s.kernel_launches() - n0
-        pr = s.profile_read() if prof else None
-        if prof:
-            s.profile(False)
-        return ms, its, launches, pr, ck
+        return phi, st, e0.elapsed_time(e1)
 
+    def arm_learned(u, h, host=None):
+        phi = torch.empty_like(h[-1]) if host is None else host[3]
+        torch.cuda.synchronize()
+        e0.record(stream)
+        if host is None:
+            s.rhs(u)
+            ch, rr = s.learned_guess(net, h[-1], h[-2], net.kappa)
+        else:
+            s.rhs(host[0])
+            ch, rr = s.learned_guess(net, host[1], host[2], net.kappa)
+        _, st = s.solve(phi, opts=mixed)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return phi, st, e0.elapsed_time(e1), ch, rr
+
+    n = args.train_samples + 2
+    for _ in range(args.warmup):
+        u = step_inputs(n)
+        pa, _, _ = arm_plain(u, hist)
+        arm_learned(u, hist)
+        hist = [hist[-1], pa]
+        n += 1
+    barrier()
     clocks = ClockSampler(local)
-    ms_mixed, its_mixed, launches, _, ck = timed(mixed, args.steps, args.warmup, clocks=clocks)
-    phi_mixed = phi_d.cpu().numpy().copy()
+    clocks.start()
+    ms_a, ms_b, its_a, its_b, chosen, rel_prev, rel_learned, launches = [], [], [], [], [], [], [], 0
+    for _ in range(args.steps):
+        u = step_inputs(n)
+        pa, sa, ta = arm_plain(u, hist)
+        l0 = s.kernel_launches()
+        pb, sb, tb, ch, rr = arm_learned(u, hist)
+        launches += s.kernel_launches() - l0
+        ms_a.append(ta); ms_b.append(tb); its_a.append(sa.iterations); its_b.append(sb.iterations)
+        chosen.append(ch); rel_prev.append(rr[0]); rel_learned.append(rr[1])
+        assert sa.rel_residual <= 1e-8 and sb.rel_residual <= 1e-8
+        hist = [hist[-1], pa]
+        n += 1
+    ck = clocks.stop()
+    barrier()
+    ms_b_mean = statistics.mean(ms_b)
+    ms_a_mean = statistics.mean(ms_a)
+    if dist is not None:
+        t = torch.tensor([ms_b_mean, ms_a_mean], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_b_mean, ms_a_mean = float(t[0]), float(t[1])
+
+    # accuracy and projection on the last held-out step
+    u = step_inputs(n - 1)
+    s.rhs(u)
+    phi_ref = pb.clone()
+    s.solve(phi_ref, opts=V.default_opts(precision=1, rtol=1e-12, max_it=400, warm_start=1))
+    fl = nv < 0.1
+    err = float(torch.linalg.norm((pb - phi_ref)[fl]) / torch.linalg.norm(phi_ref[fl]))
+    uu = u.clone()
+    s.update_pressure(torch.zeros_like(pb), pb.clone())
+    s.projection(uu)
+    maxdiv_after = s.divergence(uu)
+    uref = u.clone()
+    s.update_pressure(torch.zeros_like(pb), phi_ref.clone())
+    s.projection(uref)
+    maxdiv_ref = s.divergence(uref)
+    maxdiv_before = s.divergence(u)
+
     # roofline of the dominant kernel: the finest-level smoothing sweeps,
-    # bracketed by CUDA events inside the solves of a second timed pass
-    # (the V-cycle then runs without its CUDA graph)
-    _, _, _, (pms, pbytes, pn), _ = timed(mixed, max(3, args.steps // 2), 1, prof=True)
-    ms_plain, its_plain, _, _, _ = timed(plain, args.steps, max(1, args.warmup - 2))
-    # FP64 reference answer on the device: plain solver to 1e-12
-    s.solver_hypre(ucont_d, phi=phi_d, opts=V.default_opts(precision=1, rtol=1e-12, max_it=400))
-    phi_ref = phi_d.cpu().numpy()
-    fluid = case.nvert < 0.1
-    err = float(np.linalg.norm((phi_mixed - phi_ref)[fluid]) / np.linalg.norm(phi_ref[fluid]))
-    # post-projection divergence with the mixed-precision phi
-    u = case.ucont.copy()
-    p = np.zeros(shape)
-    s.update_pressure(p, phi_mixed.copy())
-    s.projection(u)
-    maxdiv_after = s.divergence(u)
-    maxdiv_before = s.divergence(case.ucont)
-    # end to end: host (pinned) buffers through the C ABI
-    u_h = torch.from_numpy(case.ucont).pin_memory()
-    phi_h = torch.zeros(shape, dtype=torch.float64).pin_memory()
-    ms_e2e, _, _, _, _ = timed(mixed, args.steps, 1, host=(u_h.numpy(), phi_h.numpy()))
+    # bracketed by CUDA events inside the solves of a separate pass (the
+    # V-cycle then runs without its CUDA graph), on the next unseen step
+    u = step_inputs(n)
+    s.profile(True)
+    for _ in range(3):
+        arm_learned(u, hist)
+    pms, pbytes, pn = s.profile_read()
+    s.profile(False)
+
+    # end to end through the C ABI with host (pinned) buffers
+    shape = tuple(nv.shape)
+    u_h = torch.empty(tuple(u.shape), dtype=torch.float64).pin_memory()
+    p1_h = torch.empty(shape, dtype=torch.float64).pin_memory()
+    p2_h = torch.empty(shape, dtype=torch.float64).pin_memory()
+    out_h = torch.empty(shape, dtype=torch.float64).pin_memory()
+    u_h.copy_(u)
+    p1_h.copy_(hist[-1])
+    p2_h.copy_(hist[-2])
+    host = (u_h.numpy(), p1_h.numpy(), p2_h.numpy(), out_h.numpy())
+    arm_learned(None, hist, host=host)
+    ms_e2e = statistics.mean([arm_learned(None, hist, host=host)[2] for _ in range(max(3, args.steps // 4))])
 
     hbm, peak_kind = peaks()
     achieved = pbytes / (pms * 1e-3) / 1e9 if pms > 0 else None
@@ -272,17 +368,24 @@ def run_ours(args):
         except Exception:
             traffic = None
     line = {
-        "metric": METRIC, "value": ms_mixed / world, "unit": "ms", "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": ms_mixed, "higher_is_better": False, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64/f32", "data": "synthetic",
+        "metric": METRIC, "value": ms_b_mean, "unit": "ms", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_b_mean, "higher_is_better": False, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64/f32/bf16", "data": "synthetic",
         "config": {
-            "workload": WORKLOAD, "cells": nx * ny * nz, "rtol": 1e-8,
-            "solver": "FGMRES(20) in FP64 with an FP32 geometric V-cycle (zebra j-line Gauss-Seidel over "
-                      "k-planes, 2+2 sweeps); learned initial guess not used in this line",
-            "iterations": its_mixed[-1][0], "rel_residual": its_mixed[-1][1],
-            "plain_fp64_ms": ms_plain, "plain_fp64_iterations": its_plain[-1][0],
-            "speedup_vs_plain_fp64": ms_plain / ms_mixed,
+            "workload": workload(nx, ny, nz), "cells": nx * ny * nz, "rtol": 1e-8,
+            "solver": "FGMRES(20), FP64 residual and Krylov; FP32 geometric V-cycle (zebra j-line Gauss-Seidel "
+                      "over k-planes, 2+2 sweeps); learned initial guess judged against the previous step",
+            "iterations": statistics.mean(its_b), "learned_guess_chosen": sum(chosen) / len(chosen),
+            "initial_rel_residual_learned": statistics.mean(rel_learned),
+            "initial_rel_residual_previous_step": statistics.mean(rel_prev),
+            "plain_fp64_ms": ms_a_mean, "plain_fp64_iterations": statistics.mean(its_a),
+            "plain_fp64_guess": "previous step's phi",
+            "speedup_vs_plain_fp64": ms_a_mean / ms_b_mean,
             "phi_rel_l2_vs_fp64": err, "maxdiv_before": maxdiv_before, "maxdiv_after_projection": maxdiv_after,
+            "maxdiv_after_projection_fp64_phi": maxdiv_ref,
+            "training": {"samples": args.train_samples, "steps": len(losses), "seconds": round(t_train, 2),
+                         "data_seconds": round(t_data, 2), "loss_first": losses[0],
+                         "loss_last50": float(np.mean(losses[-50:]))},
             "l2": "inputs larger than L2 (19 operator planes, 0.96 GB in FP32 on the finest level)",
             "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
         },
@@ -293,16 +396,18 @@ def run_ours(args):
                      "bytes_per_launch": (pbytes / pn) if pn else None,
                      "ms_per_launch": (pms / pn) if pn else None, "peak_source": peak_kind},
         "clocks": ck,
-        "e2e": {"value": ms_e2e / world, "unit": "ms", "h2d_bytes_per_step": int(case.ucont.nbytes),
-                "d2h_bytes_per_step": int(phi_h.numel() * 8)},
+        "e2e": {"value": ms_e2e, "unit": "ms",
+                "h2d_bytes_per_step": int(u_h.numel() * 8 + 2 * p1_h.numel() * 8),
+                "d2h_bytes_per_step": int(out_h.numel() * 8)},
         "gpu_launches": int(launches),
     }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        ms_it, its_s, ms_full = cpu_port_time(case, its_plain[-1][0], args.cpu_sample_its)
+        its_full = int(round(statistics.mean(its_a)))
+        ms_it, its_s, ms_full = cpu_port_time(nx, ny, nz, its_full, args.cpu_sample_its)
         line["cpu_baseline"] = {"value": ms_full, "unit": "ms", "cores": os.cpu_count(), "kind": "port",
                                 "sample": f"{its_s} FGMRES iterations of the FP64 CPU port on the full grid "
-                                          f"({ms_it:.0f} ms each), scaled to the {its_plain[-1][0]} iterations "
-                                          f"of a full solve"}
+                                          f"({ms_it:.0f} ms each, warm-started sequence step), scaled to the "
+                                          f"{its_full} iterations of the plain solver's warm-started solve"}
     if rank == 0:
         print(json.dumps(line), flush=True)
     s.close()

@@ -102,6 +102,39 @@ __global__ void k_guess_f2(size_t n, const uint8_t *rt, const double *aj, const 
   }
   block_add(s, sums + 2);
 }
+// One pass over the FP64 operator for the two candidates the solver judges:
+// ra = b - A xa (stored) and ||b - A xb||^2, plus ||ra||^2 and ||b||^2, as
+// block partials in rows 0..2 of `partial`.
+__global__ void __launch_bounds__(256) k_residual64x2(Box b, const double *__restrict__ A,
+                                                       const double *__restrict__ xa, const double *__restrict__ xb,
+                                                       const double *__restrict__ rhs, double *__restrict__ ra,
+                                                       double *partial) {
+  double s0 = 0., s1 = 0., s2 = 0.;
+  const uint32_t n = (uint32_t)b.n();
+  for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < n; c += (size_t)gridDim.x * blockDim.x) {
+    const int i = c % b.nx, j = (c / b.nx) % b.ny, k = c / ((size_t)b.nx * b.ny);
+    uint32_t idx[NSLOT];
+    stencil_index(b, i, j, k, idx);
+    double ya = 0., yb = 0.;
+#pragma unroll
+    for (int q = 0; q < NSLOT; q++) {
+      const double a = __ldcs(&A[(size_t)q * n + c]);
+      ya = fma(a, __ldg(&xa[idx[q]]), ya);
+      yb = fma(a, __ldg(&xb[idx[q]]), yb);
+    }
+    const double bv = rhs[c], va = bv - ya, vb = bv - yb;
+    ra[c] = va;
+    s0 += va * va;
+    s1 += vb * vb;
+    s2 += bv * bv;
+  }
+  const double t0 = block_sum(s0), t1 = block_sum(s1), t2 = block_sum(s2);
+  if (threadIdx.x == 0) {
+    partial[blockIdx.x] = t0;
+    partial[gridDim.x + blockIdx.x] = t1;
+    partial[2 * (size_t)gridDim.x + blockIdx.x] = t2;
+  }
+}
 __device__ inline double plane_rms(const double *sums, int q) {
   const double cnt = sums[3] > 1. ? sums[3] : 1.;
   return sqrt(sums[q] / cnt);
@@ -1269,8 +1302,10 @@ int guess_buffers(vfs_poisson *h) {
   return VFS_OK;
 }
 
-// fine feature planes of the current right-hand side into h->gfeat
-int guess_features(vfs_poisson *h, const double *phi_nm1, const double *phi_nm2) {
+// fine feature planes of the current right-hand side into h->gfeat; also
+// phi_{n-1} as a box vector in h->Z[0] and the squared norms of b - A ex,
+// b - A phi_{n-1} and b in norms[0..2]
+int guess_features(vfs_poisson *h, const double *phi_nm1, const double *phi_nm2, double *norms) {
   if (!h || !phi_nm1 || !phi_nm2) return fail(VFS_EINVAL, "null argument");
   if (!h->have_rhs) return fail(VFS_ESTATE, "rhs must come before the guess");
   if (h->box.nx % 8 || h->box.ny % 8 || h->box.nz % 8)
@@ -1283,9 +1318,16 @@ int guess_features(vfs_poisson *h, const double *phi_nm1, const double *phi_nm2)
   CUDA_TRY(cudaMemsetAsync(h->gsum, 0, 8 * sizeof(double), h->stream));
   LAUNCH(h, k_guess_prep, kRedBlocks, 256, h->g, h->box, h->rowtype0, h->stage, h->stage + N, h->gex, feat,
          feat + n, feat + 3 * n, h->gsum);
-  LAUNCH(h, k_residual64, box_grid(h->box), 128, h->box, h->A0, h->gex, h->b, h->r, h->partial);
+  TRY(ensure_krylov(h, std::max(h->m_alloc, 20)));
+  double *prev = h->Z[0];  // free until the next solve
+  LAUNCH(h, k_da_to_box, lin_grid(n), 256, h->g, h->box, h->stage, prev);
+  LAUNCH(h, k_mask_box, lin_grid(n), 256, n, h->rowtype0, prev);
+  LAUNCH(h, k_residual64x2, kRedBlocks, 256, h->box, h->A0, h->gex, prev, h->b, h->r, h->partial);
   LAUNCH(h, k_guess_f2, kRedBlocks, 256, n, h->rowtype0, (const double *)h->aj_box, h->r, feat + 2 * n, h->gsum);
   LAUNCH(h, k_guess_scale, kRedBlocks, 256, n, feat, h->gsum);
+  double nr[3];
+  TRY(reduce_read(h, kRedBlocks, 3, nr));
+  if (norms) for (int q = 0; q < 3; q++) norms[q] = nr[q];
   return VFS_OK;
 }
 }  // namespace
@@ -1297,7 +1339,7 @@ int vfs_poisson_guess_sample(vfs_poisson *h, const double *phi_n, const double *
   if (!phi_n || !target || !weight) return fail(VFS_EINVAL, "null argument");
   if (!is_device_ptr(features) || !is_device_ptr(target) || !is_device_ptr(weight))
     return fail(VFS_EINVAL, "features, target and weight must be device memory");
-  TRY(guess_features(h, phi_nm1, phi_nm2));
+  TRY(guess_features(h, phi_nm1, phi_nm2, nullptr));
   const size_t N = h->g.n();
   TRY(upload(h, h->stage + 2 * N, phi_n, N));
   LAUNCH(h, k_guess_target, kRedBlocks, 256, h->g, h->box, h->rowtype0, h->stage + 2 * N, h->gex, h->gsum, h->gtgt,
@@ -1318,9 +1360,11 @@ int vfs_poisson_learned_guess(vfs_poisson *h, vfs_unet *u, const double *phi_nm1
                               double kappa, int *chosen, double *rel_res) {
   if (!h || !u) return fail(VFS_EINVAL, "null argument");
   const Box b = h->box;
-  TRY(ensure_krylov(h, std::max(h->m_alloc, 20)));
-  TRY(guess_features(h, phi_nm1, phi_nm2));
+  if (h->phase) cudaEventRecord(h->phev[0], h->stream);
+  double nrm[3];
+  TRY(guess_features(h, phi_nm1, phi_nm2, nrm));
   const size_t n = b.n();
+  if (h->phase) cudaEventRecord(h->phev[1], h->stream);
   LAUNCH(h, k_guess_restrict, kRedBlocks, 256, b, h->gfeat, nullptr, h->gfc, nullptr, nullptr);
   vfs_unet_set_stream(u, h->stream);
   const int hx = b.nx / 2, hy = b.ny / 2, hz = b.nz / 2;
@@ -1328,6 +1372,7 @@ int vfs_poisson_learned_guess(vfs_poisson *h, vfs_unet *u, const double *phi_nm1
   const int64_t before = vfs_unet_kernel_launches(u);
   TRY(vfs_unet_forward(u, &bt, h->gout));
   h->launches += vfs_unet_kernel_launches(u) - before;
+  if (h->phase) cudaEventRecord(h->phev[2], h->stream);
   LAUNCH(h, k_guess_prolong, kRedBlocks, 256, b, h->gout, h->gof[0]);
   int cur = 0;
   for (int p = 0; p < h->gsmooth; p++, cur ^= 1)
@@ -1381,23 +1426,38 @@ int vfs_poisson_learned_guess(vfs_poisson *h, vfs_unet *u, const double *phi_nm1
   }
   if (h->phase)
     fprintf(stderr, "vfs guess band weights: %.4g %.4g %.4g %.4g\n", bw.a[0], bw.a[1], bw.a[2], bw.a[3]);
-  LAUNCH(h, k_guess_compose, kRedBlocks, 256, b, h->rowtype0, h->gex, h->gof[cur], kappa, h->gsum, bw, h->x);
   // the plain solver judges: keep whichever of the learned guess and the
-  // previous step's phi has the smaller FP64 residual
-  LAUNCH(h, k_da_to_box, lin_grid(n), 256, h->g, h->box, h->stage, h->gex);
-  LAUNCH(h, k_mask_box, lin_grid(n), 256, n, h->rowtype0, h->gex);
-  LAUNCH(h, k_sumsq, kRedBlocks, 256, n, h->b, h->partial);
-  double nb2 = 0., r_prev = 0., r_learn = 0.;
-  TRY(reduce_read(h, kRedBlocks, 1, &nb2));
-  TRY(residual_norm(h, h->gex, h->r, &r_prev));
-  TRY(residual_norm(h, h->x, h->r, &r_learn));
-  const double nb = nb2 > 0. ? std::sqrt(nb2) : 1.;
+  // previous step's phi has the smaller FP64 residual.  The learned one is
+  // r_ex - sum_k alpha_k y_k, whose squared norm follows from the sums
+  // already formed: ||r_ex||^2 - 2 alpha.g + alpha.G.alpha.
+  double r2 = nrm[0];
+  {
+    int q = 0;
+    for (int u2 = 0; u2 < kGuessBands; u2++) {
+      r2 -= 2. * bw.a[u2] * gm[10 + u2];
+      for (int v = u2; v < kGuessBands; v++, q++) r2 += (u2 == v ? 1. : 2.) * bw.a[u2] * bw.a[v] * gm[q];
+    }
+  }
+  const double r_learn = std::sqrt(std::max(r2, 0.)), r_prev = std::sqrt(nrm[1]);
+  const double nb = nrm[2] > 0. ? std::sqrt(nrm[2]) : 1.;
   const bool learned = r_learn < r_prev;
-  if (!learned) CUDA_TRY(cudaMemcpyAsync(h->x, h->gex, n * 8, cudaMemcpyDeviceToDevice, h->stream));
+  if (learned)
+    LAUNCH(h, k_guess_compose, kRedBlocks, 256, b, h->rowtype0, h->gex, h->gof[cur], kappa, h->gsum, bw, h->x);
+  else
+    CUDA_TRY(cudaMemcpyAsync(h->x, h->Z[0], n * 8, cudaMemcpyDeviceToDevice, h->stream));
   if (chosen) *chosen = learned ? 1 : 0;
   if (rel_res) {
     rel_res[0] = r_prev / nb;
     rel_res[1] = r_learn / nb;
+  }
+  if (h->phase) {
+    cudaEventRecord(h->phev[3], h->stream);
+    TRY(sync(h));
+    float a = 0.f, c = 0.f, d = 0.f;
+    cudaEventElapsedTime(&a, h->phev[0], h->phev[1]);
+    cudaEventElapsedTime(&c, h->phev[1], h->phev[2]);
+    cudaEventElapsedTime(&d, h->phev[2], h->phev[3]);
+    fprintf(stderr, "vfs guess ms: features+residuals %.3f network %.3f prolong+weights+judge %.3f\n", a, c, d);
   }
   return sync(h);
 }

@@ -68,8 +68,9 @@ typedef struct {
   int max_it;         /* outer iterations (poisson_it)                     */
   int restart;        /* FGMRES restart length                             */
   int precision;      /* 0: FP32 V-cycle in FP64 refinement, 1: all FP64   */
-  int nu1, nu2;       /* pre / post j-line sweeps per level                */
-  double omega;       /* relaxation weight of the line sweeps              */
+  int nu1, nu2;       /* pre / post j-line sweeps per level (default 1, 2) */
+  double omega;       /* relaxation weight of the line sweeps; 0 picks the
+                         smoother's own (1 for zebra, 0.8 for line Jacobi) */
   int use_graphs;     /* capture the V-cycle in a CUDA graph               */
   int coarsest_max;   /* coarsest level cell budget                        */
   int warm_start;     /* 0: zero guess; 1: start from the phi passed in (Phi2
@@ -77,7 +78,9 @@ typedef struct {
                          2: start from the handle's iterate as left by the
                          last solve or by vfs_poisson_learned_guess */
   int smoother;       /* 0 fused line Jacobi, 1 line Jacobi in correction
-                         form, 2 zebra (k-plane) line Gauss-Seidel         */
+                         form, 2 zebra line Gauss-Seidel over k-planes,
+                         3 (default) zebra line Gauss-Seidel over
+                         checkerboard (i + k parity) columns               */
 } vfs_solve_opts;
 
 typedef struct {

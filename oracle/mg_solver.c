@@ -451,7 +451,7 @@ static void zebra_sweep(const lvl_t *l, double omega, double *x, const double *b
 #pragma omp parallel for collapse(2)
     for (int k = 0; k < l->nz; k++)
       for (int i = 0; i < l->nx; i++) {
-        if (((i + k) & 1) != color) continue;
+        if ((g_zebra == 2 ? (k & 1) : ((i + k) & 1)) != color) continue;
         double yprev = 0;
         double ys[1024];
         for (int j = 0; j < l->ny; j++) {
@@ -572,6 +572,8 @@ static void vcycle(mg_t *g, int li, int nu1, int nu2, double omega)
   }
 }
 
+/* 0: line Jacobi; 1: zebra j-line Gauss-Seidel over checkerboard-coloured
+ * (i, k) columns; 2: zebra over k-planes (colour = k parity) */
 void or_mg_set_smoother(int zebra) { g_zebra = zebra; }
 
 static double dot(const double *a, const double *b, size_t n)

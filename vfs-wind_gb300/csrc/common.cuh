@@ -47,6 +47,16 @@ struct Box {
 // ny cells uses ceil(ny / kLineChunk) threads (at most 24, 768 per block).
 constexpr int kLineChunk = 8;
 
+// Parity-split row layout of the multigrid level operators and line
+// factors: within each (j, k) row the even-i cells come first, then the odd
+// ones, so that the columns of one checkerboard colour ((i + k) parity) are
+// contiguous and coalesce.  Vectors (x, b, r) keep the natural layout.
+__host__ __device__ inline int split_pos(int i, int nx) { return (i & 1) ? ((nx + 1) >> 1) + (i >> 1) : (i >> 1); }
+__host__ __device__ inline int split_cell(int p, int nx) {
+  const int nh = (nx + 1) >> 1;
+  return p < nh ? 2 * p : 2 * (p - nh) + 1;
+}
+
 // Stencil slot order of the reference's 19-point operator
 // (Source/poisson.c:957-975): offsets (di, dj, dk) per slot.
 enum { CP = 0, EP, WP, NP, SP, TP, BP, NE, SE, NW, SW, TN, BN, TS, BS, TE, BE, TW, BW, NSLOT };

@@ -21,7 +21,7 @@ __global__ void k_count_dofs(Grid g, Box b, const double *nvert, int *block_coun
 __global__ void k_scan_blocks(int *block_count, int nblocks, int *total);
 __global__ void k_number_dofs(Grid g, Box b, const double *nvert, const int *block_off, int *gid_box);
 __global__ void k_gid_da(Grid g, Box b, const int *gid_box, int *gid_da);
-__global__ void k_assemble(Grid g, Box b, const double *nvert, MetricPtrs m, int scale, int filter, double *A,
+__global__ void k_assemble(Grid g, Box b, const double *nvert, MetricPtrs m, int scale, int filter, int split, double *A,
                            uint8_t *rowtype);
 __global__ void k_projection_coef(Grid g, Box b, MetricPtrs m, double *pc);
 __global__ void k_level_masks(Grid g, Box b, const double *nvert, uint8_t *blank, double *w64, float *w32,

@@ -53,6 +53,13 @@ __global__ void k_row_scale(size_t n, const uint8_t *rowtype, const double *aj_b
   if (c >= n) return;
   scale[c] = rowtype[c] == 1 ? aj_box[c] : (rowtype[c] == 2 ? 1.0 : 0.0);
 }
+// one operator plane from the parity-split row layout to the natural one
+__global__ void k_unsplit_plane(Box b, const float *src, float *dst) {
+  size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= b.n()) return;
+  const int i = c % b.nx;
+  dst[c] = src[c - i + split_pos(i, b.nx)];
+}
 __global__ void k_mask_box(size_t n, const uint8_t *rowtype, double *x) {
   size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (c < n && rowtype[c] == 0) x[c] = 0.;
@@ -209,20 +216,27 @@ __global__ void k_guess_prolong(Box b, const float *oc, float *of) {
     of[f] = s;
   }
 }
-// one pass of the 27-point binomial filter (1/4, 1/2, 1/4 per direction,
-// clamped at the box faces)
-__global__ void k_guess_smooth(Box b, const float *in, float *out) {
+// one pass of the binomial filter (1/4, 1/2, 1/4, clamped at the box
+// faces) along direction `dir` (0 x, 1 y, 2 z; -1 copies); `mask` (may be
+// null) zeroes the output off the dofs
+__global__ void k_guess_smooth(Box b, const float *in, float *out, int dir, const uint8_t *mask) {
   for (size_t f = blockIdx.x * (size_t)blockDim.x + threadIdx.x; f < b.n(); f += (size_t)gridDim.x * blockDim.x) {
     const int i = f % b.nx, j = (f / b.nx) % b.ny, k = f / ((size_t)b.nx * b.ny);
-    float s = 0.f;
-    for (int dk = -1; dk <= 1; dk++)
-      for (int dj = -1; dj <= 1; dj++)
-        for (int di = -1; di <= 1; di++) {
-          const int a = min(max(i + di, 0), b.nx - 1), bb = min(max(j + dj, 0), b.ny - 1),
-                    c = min(max(k + dk, 0), b.nz - 1);
-          s += (di ? 0.25f : 0.5f) * (dj ? 0.25f : 0.5f) * (dk ? 0.25f : 0.5f) * in[b.at(a, bb, c)];
-        }
-    out[f] = s;
+    size_t m = f, p = f;
+    if (dir < 0) {
+    } else if (dir == 0) {
+      m = i > 0 ? f - 1 : f;
+      p = i < b.nx - 1 ? f + 1 : f;
+    } else if (dir == 1) {
+      m = j > 0 ? f - b.nx : f;
+      p = j < b.ny - 1 ? f + b.nx : f;
+    } else {
+      const size_t sl = (size_t)b.nx * b.ny;
+      m = k > 0 ? f - sl : f;
+      p = k < b.nz - 1 ? f + sl : f;
+    }
+    const float v = dir < 0 ? in[f] : 0.25f * in[m] + 0.5f * in[f] + 0.25f * in[p];
+    out[f] = (mask && mask[f] != 1) ? 0.f : v;
   }
 }
 // The learned correction enters the guess band by band: cells are grouped
@@ -238,11 +252,12 @@ __device__ inline int guess_band(const Box &b, int j) {
   const int d = min(j, b.ny - 1 - j);
   return d < 2 ? 0 : (d < 8 ? 1 : (d < 32 ? 2 : 3));
 }
-// y_k = A (s c [band k, dof]) per row; block partials of G_kl = <y_k, y_l>
-// (k <= l, 10 rows) and g_k = <y_k, r> (4 rows), r = b - A ex.
-__global__ void k_guess_gram(Box b, const double *__restrict__ A, const uint8_t *__restrict__ rt,
-                             const float *__restrict__ c, const double *__restrict__ r, double kappa,
-                             const double *sums, double *partial) {
+// y_k = A (s c [band k]) per row (c already zero off the dofs); block
+// partials of G_kl = <y_k, y_l> (k <= l, 10 rows) and g_k = <y_k, r>
+// (4 rows), r = b - A ex.  A neighbour's band follows from its j offset.
+__global__ void __launch_bounds__(256) k_guess_gram(Box b, const double *__restrict__ A,
+                                                     const float *__restrict__ c, const double *__restrict__ r,
+                                                     double kappa, const double *sums, double *partial) {
   const double sc = kappa * plane_rms(sums, 2);
   double acc[14];
   for (int q = 0; q < 14; q++) acc[q] = 0.;
@@ -252,18 +267,27 @@ __global__ void k_guess_gram(Box b, const double *__restrict__ A, const uint8_t 
     const int i = cell % b.nx, j = (cell / b.nx) % b.ny, k = cell / ((size_t)b.nx * b.ny);
     uint32_t idx[NSLOT];
     stencil_index(b, i, j, k, idx);
+    const int bm = guess_band(b, j > 0 ? j - 1 : j), b0 = guess_band(b, j),
+              bp = guess_band(b, j < b.ny - 1 ? j + 1 : j);
     double y[kGuessBands] = {0., 0., 0., 0.};
+#pragma unroll
     for (int t = 0; t < NSLOT; t++) {
-      const uint32_t nb = idx[t];
-      if (rt[nb] != 1) continue;
-      y[guess_band(b, (nb / b.nx) % b.ny)] += A[(size_t)t * n + cell] * (double)c[nb];
+      int di, dj, dk;
+      slot_offset(t, di, dj, dk);
+      const int bt = dj < 0 ? bm : (dj > 0 ? bp : b0);
+      const double term = A[(size_t)t * n + cell] * (double)__ldg(&c[idx[t]]);
+#pragma unroll
+      for (int u = 0; u < kGuessBands; u++) y[u] += bt == u ? term : 0.;
     }
     const double rv = r[cell];
     int q = 0;
+#pragma unroll
     for (int u = 0; u < kGuessBands; u++) {
       y[u] *= sc;
+#pragma unroll
       for (int v = u; v < kGuessBands; v++) acc[q++] += y[u] * y[v];
     }
+#pragma unroll
     for (int u = 0; u < kGuessBands; u++) acc[10 + u] += y[u] * rv;
   }
   for (int q = 0; q < 14; q++) {
@@ -529,6 +553,7 @@ int build_coarsest(vfs_poisson *h, Level &l) {
   for (int r = 0; r < nd; r++) {
     int c = idx[r];
     int i = c % b.nx, j = (c / b.nx) % b.ny, k = c / (b.nx * b.ny);
+    const size_t cs = b.at(split_pos(i, b.nx), j, k);  // level operators are stored split
     for (int s = 0; s < NSLOT; s++) {
       int di, dj, dk;
       slot_offset(s, di, dj, dk);
@@ -541,7 +566,7 @@ int build_coarsest(vfs_poisson *h, Level &l) {
       if (cc >= b.nz) { if (!b.pz) continue; cc -= b.nz; }
       int q = map[b.at(a, bb, cc)];
       if (q < 0) continue;
-      M[(size_t)r * nd + q] += A[(size_t)s * n + c];
+      M[(size_t)r * nd + q] += A[(size_t)s * n + cs];
     }
   }
   std::vector<int> comp(nd, -1), queue(nd), first;
@@ -629,7 +654,7 @@ int build_level_operator(vfs_poisson *h, Level &l) {
   TRY(dalloc(h, &l.inv64, n)); TRY(dalloc(h, &l.cp64, n));
   TRY(dalloc(h, &l.inv32, n)); TRY(dalloc(h, &l.cp32, n));
   for (int q = 0; q < 4; q++) { TRY(dalloc(h, &l.v64[q], n)); TRY(dalloc(h, &l.v32[q], n)); }
-  LAUNCH(h, k_assemble, box_grid(l.b), 128, l.g, l.b, l.nvert, l.met, 1, 0, l.A64, l.rowtype);
+  LAUNCH(h, k_assemble, box_grid(l.b), 128, l.g, l.b, l.nvert, l.met, 1, 0, 1, l.A64, l.rowtype);
   LAUNCH(h, k_level_masks, lin_grid(n), 256, l.g, l.b, l.nvert, l.blank, l.w64, l.w32, (double *)nullptr,
          (const double *)nullptr);
   LAUNCH(h, k_line_lu_f64, dim3((l.b.nx + 127) / 128, l.b.nz), 128, l.b, l.A64, l.inv64, l.cp64);
@@ -745,7 +770,7 @@ template <typename T>
 void prof_begin(vfs_poisson *h, int li, bool zero_guess, int smoother) {
   if (!h->prof || li != 0 || h->pcount >= 16) return;
   cudaEventRecord(h->pev[0][h->pcount], h->stream);
-  const double words = zero_guess ? (smoother == 2 ? 16.5 : 5.0) : (smoother == 0 ? 22.0 : 28.0);
+  const double words = zero_guess ? (smoother >= 2 ? 16.5 : 5.0) : (smoother == 0 ? 22.0 : 28.0);
   h->pbytes[h->pcount] = (double)h->box.n() * sizeof(T) * words;
 }
 void prof_end(vfs_poisson *h, int li) {
@@ -773,13 +798,25 @@ void smooth(vfs_poisson *h, Level &l, int li, int smoother, bool zero_guess, T o
     if (!zero_guess) LAUNCH(h, Prec<T>::residual, box_grid(l.b), 128, l.b, Prec<T>::A(l), x, bb, r, -1);
     LAUNCH_SM(h, Prec<T>::tri, lg, lb, lsm, l.b, zero_guess ? bb : r, Asp, Prec<T>::inv(l), Prec<T>::cp(l), x,
               omega, zero_guess ? 1 : 0, -1);
-  } else {
+  } else if (smoother == 2) {
     if (zero_guess) cudaMemsetAsync(x, 0, l.b.n() * sizeof(T), h->stream);
     for (int color = 0; color < 2; color++) {
       const bool skip_res = zero_guess && color == 0;  // x = 0: r = rhs
       if (!skip_res) LAUNCH(h, Prec<T>::residual, box_grid(l.b), 128, l.b, Prec<T>::A(l), x, bb, r, color);
       LAUNCH_SM(h, Prec<T>::tri, lg, lb, lsm, l.b, skip_res ? bb : r, Asp, Prec<T>::inv(l), Prec<T>::cp(l), x,
                 omega, 0, color);
+    }
+  } else {
+    // zebra by checkerboard columns: colour (i + k) % 2 == c; the colour's
+    // residuals go to split positions (r of the natural rhs when x = 0)
+    if (zero_guess) cudaMemsetAsync(x, 0, l.b.n() * sizeof(T), h->stream);
+    const int nh = (l.b.nx + 1) / 2;
+    dim3 cg((nh + 31) / 32, l.b.nz), rg((nh + 127) / 128, l.b.ny, l.b.nz);
+    for (int color = 0; color < 2; color++) {
+      const bool skip_res = zero_guess && color == 0;
+      if (!skip_res) LAUNCH(h, Prec<T>::residual, rg, 128, l.b, Prec<T>::A(l), x, bb, r, 2 + color);
+      LAUNCH_SM(h, Prec<T>::tri, cg, lb, lsm, l.b, skip_res ? bb : r, Asp, Prec<T>::inv(l), Prec<T>::cp(l), x,
+                omega, 0, (skip_res ? 4 : 2) + color);
     }
   }
   prof_end(h, li);
@@ -919,10 +956,17 @@ int ensure_krylov(vfs_poisson *h, int m) {
   return sync(h);
 }
 
+// omega 0 selects the smoother's own damping: 1 for the zebra
+// Gauss-Seidel variants, 0.8 for line Jacobi (undamped line Jacobi does not
+// converge as a smoother on the stretched curvilinear grids)
+void resolve_opts(vfs_solve_opts &o) {
+  if (o.omega == 0.) o.omega = o.smoother >= 2 ? 1.0 : 0.8;
+}
+
 int check_opts(const vfs_solve_opts &o) {
   if (!(o.rtol > 0) || o.max_it < 1 || o.restart < 1 || o.restart > 64 || o.nu1 < 0 || o.nu2 < 0 ||
       o.nu1 + o.nu2 < 1 || o.nu1 > 8 || o.nu2 > 8 || !(o.omega > 0 && o.omega <= 1.5) ||
-      (o.precision != 0 && o.precision != 1) || o.smoother < 0 || o.smoother > 2)
+      (o.precision != 0 && o.precision != 1) || o.smoother < 0 || o.smoother > 3)
     return fail(VFS_EINVAL, "invalid solver options");
   return VFS_OK;
 }
@@ -1086,13 +1130,13 @@ void vfs_poisson_default_opts(vfs_solve_opts *o) {
   o->max_it = 200;
   o->restart = 20;
   o->precision = 0;
-  o->nu1 = 2;
+  o->nu1 = 1;
   o->nu2 = 2;
-  o->omega = 1.0;
+  o->omega = 0.0;
   o->use_graphs = 1;
   o->coarsest_max = 128;
   o->warm_start = 0;
-  o->smoother = 2;
+  o->smoother = 3;
 }
 
 int vfs_poisson_create(const vfs_grid_desc *gd, vfs_poisson **out) {
@@ -1203,7 +1247,7 @@ int vfs_poisson_set_nvert(vfs_poisson *h, const double *nvert) {
   LAUNCH(h, k_gid_da, da_grid(h->g), 128, h->g, h->box, h->gid_box, h->gid_da);
   LAUNCH(h, k_fluid_mask, lin_grid(n), 256, h->g, h->box, h->nvert, h->fluid);
   // PoissonLHSNew: unscaled operator with the reference's insertion filter
-  LAUNCH(h, k_assemble, box_grid(h->box), 128, h->g, h->box, h->nvert, h->met, 0, 1, h->A0, h->rowtype0);
+  LAUNCH(h, k_assemble, box_grid(h->box), 128, h->g, h->box, h->nvert, h->met, 0, 1, 0, h->A0, h->rowtype0);
   uint8_t *blank;
   double *w64;
   float *w32;
@@ -1249,6 +1293,7 @@ int vfs_poisson_solve(vfs_poisson *h, double *phi, const vfs_solve_opts *opts, v
   if (!h->have_rhs) return fail(VFS_ESTATE, "rhs must come before solve");
   vfs_solve_opts o;
   if (opts) o = *opts; else vfs_poisson_default_opts(&o);
+  resolve_opts(o);
   TRY(check_opts(o));
   vfs_solve_stats st{};
   const size_t n = h->box.n();
@@ -1351,8 +1396,18 @@ int vfs_poisson_guess_sample(vfs_poisson *h, const double *phi_n, const double *
 int vfs_poisson_get_operator32(vfs_poisson *h, float *planes) {
   if (!h || !planes) return fail(VFS_EINVAL, "null argument");
   if (!h->have_nvert || h->L.empty() || !h->L[0].A32) return fail(VFS_ESTATE, "set_nvert must come first");
-  CUDA_TRY(cudaMemcpyAsync(planes, h->L[0].A32, (size_t)NSLOT * h->box.n() * sizeof(float), cudaMemcpyDefault,
-                           h->stream));
+  // the level operator is stored in the parity-split row layout: one plane
+  // at a time back to the natural layout (through the staging buffer when
+  // the destination is host memory)
+  const size_t n = h->box.n();
+  const bool dev = is_device_ptr(planes);
+  float *tmp = reinterpret_cast<float *>(h->stage);
+  for (int q = 0; q < NSLOT; q++) {
+    float *dst = dev ? planes + (size_t)q * n : tmp;
+    LAUNCH(h, k_unsplit_plane, lin_grid(n), 256, h->box, h->L[0].A32 + (size_t)q * n, dst);
+    if (!dev) CUDA_TRY(cudaMemcpyAsync(planes + (size_t)q * n, tmp, n * sizeof(float), cudaMemcpyDeviceToHost,
+                                       h->stream));
+  }
   return sync(h);
 }
 
@@ -1375,11 +1430,18 @@ int vfs_poisson_learned_guess(vfs_poisson *h, vfs_unet *u, const double *phi_nm1
   if (h->phase) cudaEventRecord(h->phev[2], h->stream);
   LAUNCH(h, k_guess_prolong, kRedBlocks, 256, b, h->gout, h->gof[0]);
   int cur = 0;
-  for (int p = 0; p < h->gsmooth; p++, cur ^= 1)
-    LAUNCH(h, k_guess_smooth, kRedBlocks, 256, b, h->gof[cur], h->gof[cur ^ 1]);
+  // gsmooth passes of the 27-point binomial filter, each as three 1-D passes;
+  // the last one also zeroes the correction off the dofs
+  for (int p = 0; p < std::max(h->gsmooth, 1); p++)
+    for (int dir = 0; dir < 3; dir++, cur ^= 1) {
+      const bool last = p == std::max(h->gsmooth, 1) - 1 && dir == 2;
+      if (h->gsmooth == 0 && !last) continue;
+      LAUNCH(h, k_guess_smooth, kRedBlocks, 256, b, h->gof[cur], h->gof[cur ^ 1], h->gsmooth == 0 ? -1 : dir,
+             last ? (const uint8_t *)h->rowtype0 : nullptr);
+    }
   // least-squares band weights: minimise ||r_ex - sum_k alpha_k y_k||
   // (alpha = 0 is the plain extrapolation, so the guess is never worse)
-  LAUNCH(h, k_guess_gram, kRedBlocks, 256, b, h->A0, h->rowtype0, h->gof[cur], h->r, kappa, h->gsum, h->partial);
+  LAUNCH(h, k_guess_gram, kRedBlocks, 256, b, h->A0, h->gof[cur], h->r, kappa, h->gsum, h->partial);
   double gm[14];
   TRY(reduce_read(h, kRedBlocks, 14, gm));
   BandWeights bw{};
@@ -1635,6 +1697,7 @@ int vfs_poisson_mg_vcycle(vfs_poisson *h, int precision, const double *r, double
   if (!h->have_nvert) return fail(VFS_ESTATE, "set_nvert must come first");
   vfs_solve_opts o;
   vfs_poisson_default_opts(&o);
+  resolve_opts(o);
   o.precision = precision ? 1 : 0;
   const size_t n = h->box.n();
   TRY(upload(h, h->stage, r, h->g.n()));

@@ -461,23 +461,26 @@ __device__ void assemble_row(const Grid &g, const double *nvert, const MetricPtr
 // Assemble one level's operator into 19 box-layout planes.  filter: the
 // reference's insertion test |v| > 1e-10 (poisson.c:1610-1614); scale: the
 // aj row scaling of the poisson == -1 path (poisson.c:1563), used for the
-// multigrid levels.  Slots whose column has no dof are zero (idx < 0).
+// multigrid levels; split: store rows in the parity-split row layout of the
+// multigrid levels (rowtype stays natural).  Slots whose column has no dof
+// are zero (idx < 0).
 __global__ void k_assemble(Grid g, Box b, const double *__restrict__ nvert, MetricPtrs m, int scale,
-                           int filter, double *A, uint8_t *rowtype) {
+                           int filter, int split, double *A, uint8_t *rowtype) {
   int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y, k = blockIdx.z;
   if (i >= b.nx) return;
-  const size_t c = b.at(i, j, k), n = b.n();
+  const size_t n = b.n(), c = split ? b.at(split_pos(i, b.nx), j, k) : b.at(i, j, k);
+  const size_t cr = b.at(i, j, k);
   const int I = i + 1, J = j + 1, K = k + 1;
   const size_t t = g.at(I, J, K);
   const bool dof = is_dof_cell(g, nvert, I, J, K);
   if (nvert[t] > 0.1 && dof) {  // identity row, poisson.c:1158-1160
     for (int s = 0; s < NSLOT; s++) A[s * n + c] = s == CP ? 1.0 : 0.0;
-    rowtype[c] = 2;
+    rowtype[cr] = 2;
     return;
   }
   if (nvert[t] > kThr) {
     for (int s = 0; s < NSLOT; s++) A[s * n + c] = 0.0;
-    rowtype[c] = 0;
+    rowtype[cr] = 0;
     return;
   }
   double v[NSLOT];
@@ -492,7 +495,7 @@ __global__ void k_assemble(Grid g, Box b, const double *__restrict__ nvert, Metr
     bool keep = s == CP || (has_dof(g, nvert, I + di, J + dj, K + dk) && (!filter || fabs(v[s]) > 1.e-10));
     A[s * n + c] = keep ? v[s] : 0.0;
   }
-  rowtype[c] = 1;
+  rowtype[cr] = 1;
 }
 
 // Per-face dot products S = a.b of the projection and the face aj, so that

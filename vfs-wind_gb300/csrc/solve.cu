@@ -9,20 +9,32 @@
 
 namespace vfs {
 
-// r = rhs - A x for one level (A holds 19 box-layout planes).
-// `color` >= 0 restricts the rows to the k-planes with k % 2 == color.
+// r = rhs - A x for one level (A: 19 planes in the parity-split row layout;
+// x, rhs natural).  `color`: -1 every row; 0/1 the k-planes with k % 2 ==
+// color; 2/3 the checkerboard columns with (i + k) % 2 == color - 2, whose
+// residuals are then written at their split positions (the layout the line
+// kernel reads them in).  Threads walk split positions, so operator loads
+// coalesce.
 template <typename T>
 __device__ __forceinline__ void residual_body(Box b, const T *__restrict__ A, const T *__restrict__ x,
                                               const T *__restrict__ rhs, T *__restrict__ r, int color) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y, k = blockIdx.z;
-  if (i >= b.nx || (color >= 0 && (k & 1) != color)) return;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y, k = blockIdx.z;
+  int p = t;
+  if (color >= 2) {
+    const int par = (color - 2 + k) & 1, nh = (b.nx + 1) >> 1;
+    if (t >= (par ? b.nx - nh : nh)) return;
+    p = par ? nh + t : t;
+  } else if (t >= b.nx || (color >= 0 && (k & 1) != color)) {
+    return;
+  }
+  const int i = split_cell(p, b.nx);
   uint32_t idx[NSLOT];
   stencil_index(b, i, j, k, idx);
-  const uint32_t n = (uint32_t)b.n(), c = idx[CP];
+  const uint32_t n = (uint32_t)b.n(), c = idx[CP], cs = c - i + p;
   T s = (T)0;
 #pragma unroll
-  for (int q = 0; q < NSLOT; q++) s += __ldcs(&A[q * n + c]) * __ldg(&x[idx[q]]);
-  r[c] = rhs[c] - s;
+  for (int q = 0; q < NSLOT; q++) s += __ldcs(&A[q * n + cs]) * __ldg(&x[idx[q]]);
+  r[color >= 2 ? cs : c] = rhs[c] - s;
 }
 
 // FP64 y = A x on the unscaled operator.
@@ -69,8 +81,9 @@ __device__ __forceinline__ void line_lu_body(Box b, const double *__restrict__ A
   if (i >= b.nx) return;
   const size_t n = b.n();
   double cprev = 0.;
+  const int p = split_pos(i, b.nx);
   for (int j = 0; j < b.ny; j++) {
-    size_t c = b.at(i, j, k);
+    size_t c = b.at(p, j, k);  // split position of cell i
     double d = A[CP * n + c], a = 0., cc = 0.;
     if (d != 0.) {
       a = j > 0 ? A[SP * n + c] : 0.;
@@ -107,12 +120,13 @@ __device__ __forceinline__ void line_sweep_body(Box b, const T *__restrict__ A, 
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int tx = threadIdx.x, ty = threadIdx.y, TI = blockDim.x, P = blockDim.y;
   T *sA = (T *)smem_raw, *sB = sA + P * TI;
-  const int i = blockIdx.x * TI + tx, k = blockIdx.y;
-  const bool valid = i < b.nx;
+  const int pp = blockIdx.x * TI + tx, k = blockIdx.y;  // split position of the column
+  const bool valid = pp < b.nx;
   const uint32_t n = (uint32_t)b.n();
   const int ny = b.ny, j0 = ty * M;
   const int cnt = valid ? max(0, min(M, ny - j0)) : 0;
-  const int ii = valid ? i : 0;
+  const int ii = valid ? split_cell(pp, b.nx) : 0;
+  const uint32_t sC = (uint32_t)b.at(valid ? pp : 0, 0, k);  // operator / factor index of the column
   const int im = ii > 0 ? ii - 1 : (b.px ? b.nx - 1 : ii), ip = ii < b.nx - 1 ? ii + 1 : (b.px ? 0 : ii);
   const int km = k > 0 ? k - 1 : (b.pz ? b.nz - 1 : k), kp = k < b.nz - 1 ? k + 1 : (b.pz ? 0 : k);
   const uint32_t sj = b.nx;
@@ -127,22 +141,22 @@ __device__ __forceinline__ void line_sweep_body(Box b, const T *__restrict__ A, 
     r[q] = (T)0;
     if (q < cnt) {
       const int j = j0 + q;
-      const uint32_t o = (uint32_t)j * sj, c = cC + o;
+      const uint32_t o = (uint32_t)j * sj, c = cC + o, ca = sC + o;
       T v = rhs[c];
       if (!zero_guess) {
         const uint32_t om = (uint32_t)(j > 0 ? j - 1 : (b.py ? ny - 1 : j)) * sj;
         const uint32_t op = (uint32_t)(j < ny - 1 ? j + 1 : (b.py ? 0 : j)) * sj;
-        v -= __ldcs(&A[EP * n + c]) * x[cE + o] + __ldcs(&A[WP * n + c]) * x[cW + o] +
-             __ldcs(&A[TP * n + c]) * x[cT + o] + __ldcs(&A[BP * n + c]) * x[cB + o] +
-             __ldcs(&A[NE * n + c]) * x[cE + op] + __ldcs(&A[SE * n + c]) * x[cE + om] +
-             __ldcs(&A[NW * n + c]) * x[cW + op] + __ldcs(&A[SW * n + c]) * x[cW + om] +
-             __ldcs(&A[TN * n + c]) * x[cT + op] + __ldcs(&A[BN * n + c]) * x[cB + op] +
-             __ldcs(&A[TS * n + c]) * x[cT + om] + __ldcs(&A[BS * n + c]) * x[cB + om] +
-             __ldcs(&A[TE * n + c]) * x[cTE + o] + __ldcs(&A[BE * n + c]) * x[cBE + o] +
-             __ldcs(&A[TW * n + c]) * x[cTW + o] + __ldcs(&A[BW * n + c]) * x[cBW + o];
+        v -= __ldcs(&A[EP * n + ca]) * x[cE + o] + __ldcs(&A[WP * n + ca]) * x[cW + o] +
+             __ldcs(&A[TP * n + ca]) * x[cT + o] + __ldcs(&A[BP * n + ca]) * x[cB + o] +
+             __ldcs(&A[NE * n + ca]) * x[cE + op] + __ldcs(&A[SE * n + ca]) * x[cE + om] +
+             __ldcs(&A[NW * n + ca]) * x[cW + op] + __ldcs(&A[SW * n + ca]) * x[cW + om] +
+             __ldcs(&A[TN * n + ca]) * x[cT + op] + __ldcs(&A[BN * n + ca]) * x[cB + op] +
+             __ldcs(&A[TS * n + ca]) * x[cT + om] + __ldcs(&A[BS * n + ca]) * x[cB + om] +
+             __ldcs(&A[TE * n + ca]) * x[cTE + o] + __ldcs(&A[BE * n + ca]) * x[cBE + o] +
+             __ldcs(&A[TW * n + ca]) * x[cTW + o] + __ldcs(&A[BW * n + ca]) * x[cBW + o];
         if (b.py) {
-          if (j == 0) v -= A[SP * n + c] * x[cC + (uint32_t)(ny - 1) * sj];
-          if (j == ny - 1) v -= A[NP * n + c] * x[cC];
+          if (j == 0) v -= A[SP * n + ca] * x[cC + (uint32_t)(ny - 1) * sj];
+          if (j == ny - 1) v -= A[NP * n + ca] * x[cC];
         }
       }
       r[q] = v;
@@ -155,7 +169,7 @@ __device__ __forceinline__ void line_sweep_body(Box b, const T *__restrict__ A, 
   for (int q = 0; q < M; q++) {
     if (q < cnt) {
       const int j = j0 + q;
-      const uint32_t c = cC + (uint32_t)j * sj;
+      const uint32_t c = sC + (uint32_t)j * sj;
       const T a = j > 0 ? __ldcs(&A[SP * n + c]) : (T)0;
       const T iv = __ldcs(&inv[c]);
       const T y = (r[q] - a * yp) * iv;
@@ -188,7 +202,7 @@ __device__ __forceinline__ void line_sweep_body(Box b, const T *__restrict__ A, 
   for (int q = M - 1; q >= 0; q--) {
     if (q < cnt) {
       const int j = j0 + q;
-      const uint32_t c = cC + (uint32_t)j * sj;
+      const uint32_t c = sC + (uint32_t)j * sj;
       const T cv = j < ny - 1 ? __ldcs(&cp[c]) : (T)0;
       const T v = r[q] - cv * xn;
       hp = hp * (-cv);
@@ -225,8 +239,12 @@ __device__ __forceinline__ void line_sweep_body(Box b, const T *__restrict__ A, 
 // form: with r = rhs - A x already formed, solve L d = r on every (i,k)
 // column (L = the line part S, CP, N of A, factors inv/cp) and update
 // x += omega d (x = omega d when zero_guess, r then being the right-hand
-// side).  `color` >= 0 restricts the update to the k-planes with
-// k % 2 == color (zebra ordering by planes).  Same chunked recurrences and scans as
+// side).  `color`: -1 every column; 0/1 the k-planes with k % 2 == color
+// (zebra by planes); 2/3 the checkerboard columns with (i + k) % 2 ==
+// color % 2 (zebra by columns), whose r is read at split positions; 4/5
+// the same columns with r natural (a right-hand side used as r).  A
+// column's threads walk split positions, so operator and factor loads
+// coalesce; x is natural.  Same chunked recurrences and scans as
 // line_sweep_body; only 5 words per cell are streamed.
 template <typename T, int M>
 __device__ __forceinline__ void line_tri_body(Box b, const T *__restrict__ r, const T *__restrict__ Asp,
@@ -235,11 +253,22 @@ __device__ __forceinline__ void line_tri_body(Box b, const T *__restrict__ r, co
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int tx = threadIdx.x, ty = threadIdx.y, TI = blockDim.x, P = blockDim.y;
   T *sA = (T *)smem_raw, *sB = sA + P * TI;
-  const int i = blockIdx.x * TI + tx, k = blockIdx.y;
-  const bool valid = i < b.nx && (color < 0 || (k & 1) == color);
+  const int t = blockIdx.x * TI + tx, k = blockIdx.y;
+  int pp = t;
+  bool valid;
+  if (color >= 2) {
+    const int par = (color + k) & 1, nh = (b.nx + 1) >> 1;
+    valid = t < (par ? b.nx - nh : nh);
+    pp = par ? nh + t : t;
+  } else {
+    valid = t < b.nx && (color < 0 || (k & 1) == color);
+  }
   const int ny = b.ny, j0 = ty * M;
   const int cnt = valid ? max(0, min(M, ny - j0)) : 0;
-  const uint32_t sj = b.nx, cC = valid ? (uint32_t)b.at(i, 0, k) : 0u;
+  const uint32_t sj = b.nx;
+  const uint32_t cS = valid ? (uint32_t)b.at(pp, 0, k) : 0u;                     // operator / factor index
+  const uint32_t cX = valid ? (uint32_t)b.at(split_cell(pp, b.nx), 0, k) : 0u;  // natural index
+  const uint32_t cR = (color == 2 || color == 3) ? cS : cX;
   T y[M], g[M];
   T yp = (T)0, gp = (T)1;
 #pragma unroll
@@ -248,10 +277,10 @@ __device__ __forceinline__ void line_tri_body(Box b, const T *__restrict__ r, co
     g[q] = (T)0;
     if (q < cnt) {
       const int j = j0 + q;
-      const uint32_t c = cC + (uint32_t)j * sj;
-      const T a = j > 0 ? __ldcs(&Asp[c]) : (T)0;
-      const T iv = __ldcs(&inv[c]);
-      const T v = (__ldcs(&r[c]) - a * yp) * iv;
+      const uint32_t o = (uint32_t)j * sj;
+      const T a = j > 0 ? __ldcs(&Asp[cS + o]) : (T)0;
+      const T iv = __ldcs(&inv[cS + o]);
+      const T v = (__ldcs(&r[cR + o]) - a * yp) * iv;
       gp = gp * (-a * iv);
       y[q] = v;
       g[q] = gp;
@@ -263,9 +292,9 @@ __device__ __forceinline__ void line_tri_body(Box b, const T *__restrict__ r, co
   __syncthreads();
   if (ty == 0) {
     T Y = (T)0;
-    for (int t = 0; t < P; t++) {
-      const T e = sA[t * TI + tx], G = sB[t * TI + tx];
-      sA[t * TI + tx] = Y;
+    for (int s = 0; s < P; s++) {
+      const T e = sA[s * TI + tx], G = sB[s * TI + tx];
+      sA[s * TI + tx] = Y;
       Y = e + G * Y;
     }
   }
@@ -279,8 +308,7 @@ __device__ __forceinline__ void line_tri_body(Box b, const T *__restrict__ r, co
   for (int q = M - 1; q >= 0; q--) {
     if (q < cnt) {
       const int j = j0 + q;
-      const uint32_t c = cC + (uint32_t)j * sj;
-      const T cv = j < ny - 1 ? __ldcs(&cp[c]) : (T)0;
+      const T cv = j < ny - 1 ? __ldcs(&cp[cS + (uint32_t)j * sj]) : (T)0;
       const T v = y[q] - cv * xn;
       hp = hp * (-cv);
       y[q] = v;
@@ -293,9 +321,9 @@ __device__ __forceinline__ void line_tri_body(Box b, const T *__restrict__ r, co
   __syncthreads();
   if (ty == 0) {
     T X = (T)0;
-    for (int t = P - 1; t >= 0; t--) {
-      const T e = sA[t * TI + tx], H = sB[t * TI + tx];
-      sA[t * TI + tx] = X;
+    for (int s = P - 1; s >= 0; s--) {
+      const T e = sA[s * TI + tx], H = sB[s * TI + tx];
+      sA[s * TI + tx] = X;
       X = e + H * X;
     }
   }
@@ -304,7 +332,7 @@ __device__ __forceinline__ void line_tri_body(Box b, const T *__restrict__ r, co
 #pragma unroll
   for (int q = 0; q < M; q++) {
     if (q < cnt) {
-      const uint32_t c = cC + (uint32_t)(j0 + q) * sj;
+      const uint32_t c = cX + (uint32_t)(j0 + q) * sj;
       const T d = y[q] + g[q] * xin;
       x[c] = (zero_guess ? (T)0 : x[c]) + omega * d;
     }

@@ -110,12 +110,12 @@ __global__ void k_guess_f2(size_t n, const uint8_t *rt, const double *aj, const 
   block_add(s, sums + 2);
 }
 // One pass over the FP64 operator for the two candidates the solver judges:
-// ra = b - A xa (stored) and ||b - A xb||^2, plus ||ra||^2 and ||b||^2, as
-// block partials in rows 0..2 of `partial`.
+// ra = b - A xa and rb = b - A xb (both stored), with ||ra||^2, ||rb||^2
+// and ||b||^2 as block partials in rows 0..2 of `partial`.
 __global__ void __launch_bounds__(256) k_residual64x2(Box b, const double *__restrict__ A,
                                                        const double *__restrict__ xa, const double *__restrict__ xb,
                                                        const double *__restrict__ rhs, double *__restrict__ ra,
-                                                       double *partial) {
+                                                       double *__restrict__ rb, double *partial) {
   double s0 = 0., s1 = 0., s2 = 0.;
   const uint32_t n = (uint32_t)b.n();
   for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < n; c += (size_t)gridDim.x * blockDim.x) {
@@ -131,6 +131,7 @@ __global__ void __launch_bounds__(256) k_residual64x2(Box b, const double *__res
     }
     const double bv = rhs[c], va = bv - ya, vb = bv - yb;
     ra[c] = va;
+    rb[c] = vb;
     s0 += va * va;
     s1 += vb * vb;
     s2 += bv * bv;
@@ -252,38 +253,44 @@ __device__ inline int guess_band(const Box &b, int j) {
   const int d = min(j, b.ny - 1 - j);
   return d < 2 ? 0 : (d < 8 ? 1 : (d < 32 ? 2 : 3));
 }
-// y_k = A (s c [band k]) per row (c already zero off the dofs); block
-// partials of G_kl = <y_k, y_l> (k <= l, 10 rows) and g_k = <y_k, r>
-// (4 rows), r = b - A ex.  A neighbour's band follows from its j offset.
-__global__ void __launch_bounds__(256) k_guess_gram(Box b, const double *__restrict__ A,
+// y_k = A (s c [band k]) per row (c already zero off the dofs), formed in
+// FP32 from the level-0 multigrid operator (aj-scaled rows, parity-split
+// layout) and unscaled by the row scale; block partials of
+// G_kl = <y_k, y_l> (k <= l, 10 rows) and g_k = <y_k, r> (4 rows),
+// r = b - A ex.  A neighbour's band follows from its j offset.  The fit
+// only has to be good, not exact: the candidate it produces is then
+// measured by its FP64 residual.
+__global__ void __launch_bounds__(256) k_guess_gram(Box b, const float *__restrict__ A, const double *__restrict__ scale,
                                                      const float *__restrict__ c, const double *__restrict__ r,
                                                      double kappa, const double *sums, double *partial) {
-  const double sc = kappa * plane_rms(sums, 2);
-  double acc[14];
-  for (int q = 0; q < 14; q++) acc[q] = 0.;
+  const float sc = (float)(kappa * plane_rms(sums, 2));
+  float acc[14];
+  for (int q = 0; q < 14; q++) acc[q] = 0.f;
   const uint32_t n = (uint32_t)b.n();
-  for (size_t cell = blockIdx.x * (size_t)blockDim.x + threadIdx.x; cell < n;
-       cell += (size_t)gridDim.x * blockDim.x) {
-    const int i = cell % b.nx, j = (cell / b.nx) % b.ny, k = cell / ((size_t)b.nx * b.ny);
+  for (size_t cs = blockIdx.x * (size_t)blockDim.x + threadIdx.x; cs < n; cs += (size_t)gridDim.x * blockDim.x) {
+    const int p = cs % b.nx, j = (cs / b.nx) % b.ny, k = cs / ((size_t)b.nx * b.ny);
+    const int i = split_cell(p, b.nx);
     uint32_t idx[NSLOT];
     stencil_index(b, i, j, k, idx);
+    const double sr = scale[idx[CP]];
+    if (sr == 0.) continue;
     const int bm = guess_band(b, j > 0 ? j - 1 : j), b0 = guess_band(b, j),
               bp = guess_band(b, j < b.ny - 1 ? j + 1 : j);
-    double y[kGuessBands] = {0., 0., 0., 0.};
+    float y[kGuessBands] = {0.f, 0.f, 0.f, 0.f};
 #pragma unroll
     for (int t = 0; t < NSLOT; t++) {
       int di, dj, dk;
       slot_offset(t, di, dj, dk);
       const int bt = dj < 0 ? bm : (dj > 0 ? bp : b0);
-      const double term = A[(size_t)t * n + cell] * (double)__ldg(&c[idx[t]]);
+      const float term = __ldcs(&A[(size_t)t * n + cs]) * __ldg(&c[idx[t]]);
 #pragma unroll
-      for (int u = 0; u < kGuessBands; u++) y[u] += bt == u ? term : 0.;
+      for (int u = 0; u < kGuessBands; u++) y[u] += bt == u ? term : 0.f;
     }
-    const double rv = r[cell];
+    const float inv = (float)(1. / sr), rv = (float)r[idx[CP]];
     int q = 0;
 #pragma unroll
     for (int u = 0; u < kGuessBands; u++) {
-      y[u] *= sc;
+      y[u] *= sc * inv;
 #pragma unroll
       for (int v = u; v < kGuessBands; v++) acc[q++] += y[u] * y[v];
     }
@@ -291,7 +298,7 @@ __global__ void __launch_bounds__(256) k_guess_gram(Box b, const double *__restr
     for (int u = 0; u < kGuessBands; u++) acc[10 + u] += y[u] * rv;
   }
   for (int q = 0; q < 14; q++) {
-    const double t = block_sum(acc[q]);
+    const double t = block_sum((double)acc[q]);
     if (threadIdx.x == 0) partial[(size_t)q * gridDim.x + blockIdx.x] = t;
   }
 }
@@ -397,6 +404,11 @@ struct vfs_poisson {
   double *gex = nullptr, *gsum = nullptr;
   float *gfeat = nullptr, *gtgt = nullptr, *gfc = nullptr, *gout = nullptr, *gof[2] = {nullptr, nullptr};
   int gsmooth = 2;  // binomial passes over the prolonged correction
+  // residual of the iterate installed by the learned guess, handed to the
+  // next solve (warm_start 2) so that it does not form it again
+  double *rprev = nullptr, *rlearn = nullptr, *r0 = nullptr;
+  double r0_norm = 0.;
+  bool r0_valid = false;
   std::vector<Level> L;
   bool have_grid = false, have_nvert = false, have_rhs = false, have_phi = false;
   // graphs of the V-cycle per precision and parameters they were built for
@@ -992,7 +1004,10 @@ int fgmres(vfs_poisson *h, const vfs_solve_opts &o, vfs_solve_stats *st) {
     st->iterations = 0;
     return VFS_OK;
   }
-  if (o.warm_start) {
+  if (o.warm_start == 2 && h->r0_valid) {  // residual formed by the guess
+    CUDA_TRY(cudaMemcpyAsync(h->V[0], h->r0, n * 8, cudaMemcpyDeviceToDevice, h->stream));
+    beta = h->r0_norm;
+  } else if (o.warm_start) {
     TRY(residual_norm(h, h->x, h->V[0], &beta));
   } else {  // zero initial guess: r = b
     CUDA_TRY(cudaMemcpyAsync(h->V[0], h->b, n * 8, cudaMemcpyDeviceToDevice, h->stream));
@@ -1269,6 +1284,7 @@ int vfs_poisson_set_nvert(vfs_poisson *h, const double *nvert) {
   TRY(sync(h));
   h->have_nvert = true;
   h->have_rhs = false;
+  h->r0_valid = false;
   return VFS_OK;
 }
 
@@ -1285,6 +1301,7 @@ int vfs_poisson_rhs(vfs_poisson *h, const double *ucont, double dt, double st, d
   }
   TRY(sync(h));
   h->have_rhs = true;
+  h->r0_valid = false;
   return VFS_OK;
 }
 
@@ -1322,6 +1339,7 @@ int vfs_poisson_solve(vfs_poisson *h, double *phi, const vfs_solve_opts *opts, v
   st.status = st.rel_residual <= o.rtol ? VFS_OK : VFS_ENOCONV;
   if (stats) *stats = st;
   h->have_phi = true;
+  h->r0_valid = false;
   if (st.status != VFS_OK)
     return fail(VFS_ENOCONV, "solver stopped at relative residual " + std::to_string(st.rel_residual));
   return VFS_OK;
@@ -1341,6 +1359,8 @@ int guess_buffers(vfs_poisson *h) {
     TRY(dalloc(h, &h->gout, n / 8 + 1));
     TRY(dalloc(h, &h->gof[0], n));
     TRY(dalloc(h, &h->gof[1], n));
+    TRY(dalloc(h, &h->rprev, n));
+    TRY(dalloc(h, &h->rlearn, n));
     const char *e = getenv("VFS_GUESS_SMOOTH");
     if (e) h->gsmooth = std::max(0, std::min(8, atoi(e)));
   }
@@ -1367,7 +1387,7 @@ int guess_features(vfs_poisson *h, const double *phi_nm1, const double *phi_nm2,
   double *prev = h->Z[0];  // free until the next solve
   LAUNCH(h, k_da_to_box, lin_grid(n), 256, h->g, h->box, h->stage, prev);
   LAUNCH(h, k_mask_box, lin_grid(n), 256, n, h->rowtype0, prev);
-  LAUNCH(h, k_residual64x2, kRedBlocks, 256, h->box, h->A0, h->gex, prev, h->b, h->r, h->partial);
+  LAUNCH(h, k_residual64x2, kRedBlocks, 256, h->box, h->A0, h->gex, prev, h->b, h->r, h->rprev, h->partial);
   LAUNCH(h, k_guess_f2, kRedBlocks, 256, n, h->rowtype0, (const double *)h->aj_box, h->r, feat + 2 * n, h->gsum);
   LAUNCH(h, k_guess_scale, kRedBlocks, 256, n, feat, h->gsum);
   double nr[3];
@@ -1415,6 +1435,7 @@ int vfs_poisson_learned_guess(vfs_poisson *h, vfs_unet *u, const double *phi_nm1
                               double kappa, int *chosen, double *rel_res) {
   if (!h || !u) return fail(VFS_EINVAL, "null argument");
   const Box b = h->box;
+  h->r0_valid = false;
   if (h->phase) cudaEventRecord(h->phev[0], h->stream);
   double nrm[3];
   TRY(guess_features(h, phi_nm1, phi_nm2, nrm));
@@ -1441,7 +1462,8 @@ int vfs_poisson_learned_guess(vfs_poisson *h, vfs_unet *u, const double *phi_nm1
     }
   // least-squares band weights: minimise ||r_ex - sum_k alpha_k y_k||
   // (alpha = 0 is the plain extrapolation, so the guess is never worse)
-  LAUNCH(h, k_guess_gram, kRedBlocks, 256, b, h->A0, h->gof[cur], h->r, kappa, h->gsum, h->partial);
+  LAUNCH(h, k_guess_gram, kRedBlocks, 256, b, h->L[0].A32, (const double *)h->scale, h->gof[cur], h->r, kappa,
+         h->gsum, h->partial);
   double gm[14];
   TRY(reduce_read(h, kRedBlocks, 14, gm));
   BandWeights bw{};
@@ -1489,9 +1511,10 @@ int vfs_poisson_learned_guess(vfs_poisson *h, vfs_unet *u, const double *phi_nm1
   if (h->phase)
     fprintf(stderr, "vfs guess band weights: %.4g %.4g %.4g %.4g\n", bw.a[0], bw.a[1], bw.a[2], bw.a[3]);
   // the plain solver judges: keep whichever of the learned guess and the
-  // previous step's phi has the smaller FP64 residual.  The learned one is
-  // r_ex - sum_k alpha_k y_k, whose squared norm follows from the sums
-  // already formed: ||r_ex||^2 - 2 alpha.g + alpha.G.alpha.
+  // previous step's phi has the smaller FP64 residual.  The fit predicts
+  // the learned one, ||r_ex||^2 - 2 alpha.g + alpha.G.alpha; when that is
+  // clearly above the previous step's the learned guess is not formed,
+  // otherwise it is composed and its FP64 residual decides.
   double r2 = nrm[0];
   {
     int q = 0;
@@ -1500,13 +1523,23 @@ int vfs_poisson_learned_guess(vfs_poisson *h, vfs_unet *u, const double *phi_nm1
       for (int v = u2; v < kGuessBands; v++, q++) r2 += (u2 == v ? 1. : 2.) * bw.a[u2] * bw.a[v] * gm[q];
     }
   }
-  const double r_learn = std::sqrt(std::max(r2, 0.)), r_prev = std::sqrt(nrm[1]);
+  const double r_prev = std::sqrt(nrm[1]);
   const double nb = nrm[2] > 0. ? std::sqrt(nrm[2]) : 1.;
-  const bool learned = r_learn < r_prev;
-  if (learned)
+  double r_learn = std::sqrt(std::max(r2, 0.));
+  bool learned = false;
+  if (r_learn < 1.1 * r_prev) {
     LAUNCH(h, k_guess_compose, kRedBlocks, 256, b, h->rowtype0, h->gex, h->gof[cur], kappa, h->gsum, bw, h->x);
-  else
-    CUDA_TRY(cudaMemcpyAsync(h->x, h->Z[0], n * 8, cudaMemcpyDeviceToDevice, h->stream));
+    LAUNCH(h, k_residual64, box_grid(h->box), 128, h->box, h->A0, h->x, h->b, h->rlearn, h->partial);
+    double s2 = 0.;
+    const dim3 gr = box_grid(h->box);
+    TRY(reduce_read(h, (int)(gr.x * gr.y * gr.z), 1, &s2));
+    r_learn = std::sqrt(s2);
+    learned = r_learn < r_prev;
+  }
+  if (!learned) CUDA_TRY(cudaMemcpyAsync(h->x, h->Z[0], n * 8, cudaMemcpyDeviceToDevice, h->stream));
+  h->r0 = learned ? h->rlearn : h->rprev;
+  h->r0_norm = learned ? r_learn : r_prev;
+  h->r0_valid = true;
   if (chosen) *chosen = learned ? 1 : 0;
   if (rel_res) {
     rel_res[0] = r_prev / nb;

@@ -23,6 +23,9 @@
  *   setup_lidx2, PoissonLHSNew poisson.c:188, :977 -> vfs_poisson_set_nvert
  *   PoissonRHS2_hypre + Remove_Nullspace_Scale
  *                             poisson_hypre.c:265, :118 -> vfs_poisson_rhs
+ *   PoissonRHS2               poisson.c:1780       -> vfs_poisson_rhs2
+ *   VolumeFlux (immersed)     poisson.c:3563       -> vfs_poisson_volume_flux
+ *   Contra2Cart               rhs.c:35             -> vfs_poisson_contra2cart
  *   PoissonSolver_Hypre       poisson_hypre.c:506  -> vfs_poisson_solve
  *   Remove_Nullspace          poisson_hypre.c:202  (inside vfs_poisson_solve)
  *   Convert_Phi2_Phi          poisson.c:98         (inside vfs_poisson_solve)
@@ -118,6 +121,42 @@ int vfs_poisson_set_nvert(vfs_poisson *h, const double *nvert);
 /* Right-hand side from Ucont: PoissonRHS2_hypre + Remove_Nullspace_Scale.
  * coeff is time_coeff() (Source/poisson.c:23-31). */
 int vfs_poisson_rhs(vfs_poisson *h, const double *ucont, double dt, double st, double coeff);
+
+/* PoissonRHS2 (Source/poisson.c:1780-1906), the right-hand side of the
+ * -poisson 0 (poisson = 0) and -poisson -1 (poisson = -1) paths: the same
+ * divergence as vfs_poisson_rhs on fluid cells, 0 on identity-row dofs,
+ * rows times aj for -1, then the unweighted mean over the fluid cells
+ * removed from the fluid entries (instead of Remove_Nullspace_Scale).  The
+ * solve then uses this B (poisson = 0) or B / aj on the fluid rows
+ * (poisson = -1: the same system without its row scaling; the reference's
+ * aj-scaled rows with an unweighted mean removal are not consistent, so a
+ * solve to a tight tolerance can stop at VFS_ENOCONV, as the reference's
+ * own iteration stops at its iteration limit). */
+int vfs_poisson_rhs2(vfs_poisson *h, const double *ucont, double dt, double st, double coeff, int poisson);
+
+/* VolumeFlux, the immersed == 1 variant (Source/poisson.c:3563-3903): the
+ * net flux through the faces between fluid and IB cells (0.1 < nvert <
+ * 1.1) of ucont (DA Cmpnts, in/out) is removed before the right-hand side.
+ * Faces with |U| <= 1e-8 are zeroed; flg selects the reference's
+ * correction (0: flux / area spread by face area; 1: (flux +
+ * flux_intp_sum) / area; 2: (flux + flux_intp_sum) / sum|U| spread by |U|;
+ * 3: the same with |U| / area).  *ibm_flux and *ibm_area (may be NULL) get
+ * the flux and area after the correction, as the reference returns them.
+ * The per-face arithmetic is the reference's; the three sums are reduced in
+ * a different order (their values agree to rounding). */
+int vfs_poisson_volume_flux(vfs_poisson *h, double *ucont, int flg, double flux_intp_sum, double *ibm_flux,
+                            double *ibm_area);
+
+/* Contra2Cart (Source/rhs.c:35-749), the change of basis: Cartesian
+ * velocity ucat (DA Cmpnts, in/out) at the fluid cells from the centred
+ * averages of the face fluxes ucont (periodic ghosts taken from their
+ * partners) by Cramer's rule with the cell metrics; periodic ghosts of ucat
+ * then take their partners' values; with zero_solid, cells with
+ * (int)(nvert + 0.1) == 3 are set to 0 (the reference does this when
+ * neither movefsi nor rotatefsi is set).  Other cells keep their ucat.  The
+ * reference routine's wall functions and boundary conditions belong to the
+ * momentum solver and are not part of the library. */
+int vfs_poisson_contra2cart(vfs_poisson *h, const double *ucont, double *ucat, int zero_solid);
 
 /* Solve A phi = b to opts->rtol, remove the fluid mean of phi
  * (Remove_Nullspace) and write phi to `phi` in DA layout with periodic

@@ -73,6 +73,9 @@ def lib():
         L.or_poisson_lhs.argtypes = [P(Dims), dp, P(Metrics), C.c_int, C.c_int, ip, ip, dp, ip]
         L.or_poisson_lhs.restype = C.c_int
         L.or_poisson_rhs2_hypre.argtypes = [P(Dims), dp, ip, dp, C.c_double, C.c_double, C.c_double, dp]
+        L.or_poisson_rhs2.argtypes = [P(Dims), dp, ip, dp, dp, C.c_double, C.c_double, C.c_double, C.c_int, dp]
+        L.or_volume_flux.argtypes = [P(Dims), dp, dp, dp, dp, dp, C.c_int, C.c_double, dp]
+        L.or_contra2cart.argtypes = [P(Dims), dp, dp, dp, dp, dp, dp, C.c_int]
         L.or_remove_nullspace_scale.argtypes = [P(Dims), dp, ip, dp, dp, C.c_int]
         L.or_remove_nullspace.argtypes = [P(Dims), dp, ip, dp, C.c_int]
         L.or_convert_phi2_phi.argtypes = [P(Dims), dp, dp, dp]
@@ -182,6 +185,34 @@ def rhs(d, nvert, gid, ucont, aj, dt=1.0, st=1.0, coeff=1.0, bctype3=0):
     lib().or_poisson_rhs2_hypre(C.byref(d), _dp(nv), _ip(g), _dp(np.ascontiguousarray(ucont)), dt, st, coeff, _dp(b))
     lib().or_remove_nullspace_scale(C.byref(d), _dp(nv), _ip(g), _dp(np.ascontiguousarray(aj)), _dp(b), bctype3)
     return b[:n]
+
+
+def rhs2(d, nvert, gid, ucont, aj, poisson=0, dt=1.0, st=1.0, coeff=1.0):
+    """PoissonRHS2 (the -poisson 0 / -1 right-hand side), one entry per dof."""
+    n = int(gid.max()) + 1
+    b = np.zeros(max(n, 1))
+    lib().or_poisson_rhs2(C.byref(d), _dp(np.ascontiguousarray(nvert, np.float64)),
+                          _ip(np.ascontiguousarray(gid, np.int32).ravel()), _dp(np.ascontiguousarray(ucont)),
+                          _dp(np.ascontiguousarray(aj, np.float64)), dt, st, coeff, int(poisson), _dp(b))
+    return b[:n]
+
+
+def volume_flux(d, nvert, met, ucont, flg=0, flux_intp_sum=0.0):
+    """VolumeFlux (immersed == 1); returns (corrected ucont, flux, area)."""
+    u = np.ascontiguousarray(ucont, np.float64).copy()
+    out = np.zeros(2)
+    lib().or_volume_flux(C.byref(d), _dp(np.ascontiguousarray(nvert, np.float64)), _dp(met["csi"]),
+                         _dp(met["eta"]), _dp(met["zet"]), _dp(u), int(flg), float(flux_intp_sum), _dp(out))
+    return u, out[0], out[1]
+
+
+def contra2cart(d, nvert, met, ucont, ucat=None, zero_solid=True):
+    """Contra2Cart's change of basis; returns ucat."""
+    out = np.zeros((d.mz, d.my, d.mx, 3)) if ucat is None else np.ascontiguousarray(ucat, np.float64).copy()
+    lib().or_contra2cart(C.byref(d), _dp(np.ascontiguousarray(nvert, np.float64)), _dp(met["csi"]),
+                         _dp(met["eta"]), _dp(met["zet"]), _dp(np.ascontiguousarray(ucont, np.float64)), _dp(out),
+                         int(zero_solid))
+    return out
 
 
 def rhs_raw(d, nvert, gid, ucont, dt=1.0, st=1.0, coeff=1.0):

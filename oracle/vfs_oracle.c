@@ -672,6 +672,62 @@ void or_poisson_rhs2_hypre(const or_dims *d, const double *nvert, const int *gid
 #undef U
 }
 
+/* PoissonRHS2 (Source/poisson.c:1780-1906), the -poisson 0 / -1 right-hand
+ * side: the PoissonRHS2_hypre divergence on fluid cells (nvert < 0.1), 0 on
+ * identity-row dofs (nvert >= 0.1 with a dof, :1816-1819), the aj row
+ * scaling when poisson == -1 (:1856), then the unweighted mean over the
+ * fluid cells removed from the fluid entries (:1873-1889; VecSum runs over
+ * every entry of B, the count over the fluid cells).  b has one entry per
+ * dof. */
+void or_poisson_rhs2(const or_dims *d, const double *nvert, const int *gid, const double *ucont,
+                     const double *aj, double dt, double st, double coeff, int poisson, double *b)
+{
+  const int mx = d->mx, my = d->my, mz = d->mz;
+  const int ip = per_i(d), jp = per_j(d), kp = per_k(d);
+  int count = 0;
+#define U(i, j, k, c) ucont[IX(d, i, j, k) * 3 + (c)]
+  for (int k = 1; k < mz - 1; k++)
+    for (int j = 1; j < my - 1; j++)
+      for (int i = 1; i < mx - 1; i++) {
+        size_t t = IX(d, i, j, k);
+        double val;
+        if (nvert[t] >= 0.1) {
+          if (gid[t] >= 0) val = 0;
+          else continue;
+        } else {
+          val = 0;
+          val -= U(i, j, k, 0);
+          if (i == 1 && ip) val += U(mx - 2, j, k, 0);
+          else val += U(i - 1, j, k, 0);
+          val -= U(i, j, k, 1);
+          if (j == 1 && jp) val += U(i, my - 2, k, 1);
+          else val += U(i, j - 1, k, 1);
+          val -= U(i, j, k, 2);
+          if (k == 1 && kp) val += U(i, j, mz - 2, 2);
+          else val += U(i, j, k - 1, 2);
+          val *= -1.0 / dt * st * coeff;
+          if (poisson == -1) val *= aj[t];
+          count++;
+        }
+        b[gid[t]] = val;
+      }
+#undef U
+  double sum = 0; /* every dof entry, in the grid order */
+  for (int k = 1; k < mz - 1; k++)
+    for (int j = 1; j < my - 1; j++)
+      for (int i = 1; i < mx - 1; i++) {
+        size_t t = IX(d, i, j, k);
+        if (gid[t] >= 0) sum += b[gid[t]];
+      }
+  const double val = -sum / (double)(count > 0 ? count : 1);
+  for (int k = 1; k < mz - 1; k++)
+    for (int j = 1; j < my - 1; j++)
+      for (int i = 1; i < mx - 1; i++) {
+        size_t t = IX(d, i, j, k);
+        if (nvert[t] < 0.1) b[gid[t]] += val;
+      }
+}
+
 /* Remove_Nullspace_Scale (Source/poisson_hypre.c:118-200). */
 void or_remove_nullspace_scale(const or_dims *d, const double *nvert, const int *gid,
                                const double *aj, double *b, int bctype3)
@@ -1045,4 +1101,142 @@ void or_stencil_apply(const or_dims *d, const int *rowtype, const double *vol, c
           s += vol[t * 19 + q] * x[IX(d, i + off[q][0], j + off[q][1], k + off[q][2])];
         y[t] = s;
       }
+}
+
+/* VolumeFlux, the immersed == 1 variant (Source/poisson.c:3563-3903): the
+ * net flux through the faces between fluid cells and IB cells (0.1 < nvert
+ * < 1.1) is removed.  Faces with |U| <= 1e-8 are zeroed; the correction is
+ * (flux + flux_intp_sum) / sum|U|(/|metric|) for flg 2 / 3, (flux +
+ * flux_intp_sum) / area for flg 1 and flux / area for flg 0, spread by the
+ * face area (flg 0, 1), |U| (flg 2) or |U| / area (flg 3); fluid-side
+ * faces lose it, IB-side faces gain it.  out[0..1]: the flux and area
+ * after the correction (the reference's ibm_Flux, ibm_Area). */
+void or_volume_flux(const or_dims *d, const double *nvert, const double *csi, const double *eta, const double *zet,
+                    double *ucont, int flg, double flux_intp_sum, double *out)
+{
+  const int mx = d->mx, my = d->my, mz = d->mz;
+  const double eps = 1.e-8, ibmval = 1.1;
+  const double *met[3] = {csi, eta, zet};
+  double flux = 0, flux_abs = 0, area = 0;
+  for (int pass = 0; pass < 3; pass++) {
+    double corr = 0;
+    if (pass == 1) {
+      if (area > 1.e-15) {
+        if (flg > 1) corr = (flux + flux_intp_sum) / flux_abs;
+        else if (flg) corr = (flux + flux_intp_sum) / area;
+        else corr = flux / area;
+      }
+    }
+    if (pass == 2) { flux = 0; area = 0; }
+    for (int k = 1; k < mz - 1; k++)
+      for (int j = 1; j < my - 1; j++)
+        for (int i = 1; i < mx - 1; i++) {
+          const size_t t = IX(d, i, j, k);
+          const size_t nb[3] = {IX(d, i + 1, j, k), IX(d, i, j + 1, k), IX(d, i, j, k + 1)};
+          const int inside[3] = {i < mx - 2, j < my - 2, k < mz - 2};
+          for (int s = 0; s < 2; s++) {   /* s 0: fluid cell, s 1: IB cell */
+            if (s == 0 && !(nvert[t] < 0.1)) continue;
+            if (s == 1 && !(nvert[t] > 0.1 && nvert[t] < ibmval)) continue;
+            for (int q = 0; q < 3; q++) {
+              const double nn = nvert[nb[q]];
+              const int face = s == 0 ? (nn > 0.1 && nn < ibmval) : (nn < 0.1);
+              if (!face || !inside[q]) continue;
+              double *u = &ucont[t * 3 + q];
+              const double *m = &met[q][t * 3];
+              const double a = sqrt(m[0] * m[0] + m[1] * m[1] + m[2] * m[2]);
+              if (pass == 0) {
+                if (fabs(*u) > eps) {
+                  flux += s == 0 ? *u : -*u;
+                  flux_abs += flg == 3 ? fabs(*u) / a : fabs(*u);
+                  area += a;
+                } else {
+                  *u = 0.;
+                }
+              } else if (pass == 1) {
+                if (fabs(*u) > eps) {
+                  double dlt;
+                  if (flg == 3) dlt = corr * fabs(*u) / a;
+                  else if (flg == 2) dlt = corr * fabs(*u);
+                  else dlt = a * corr;
+                  if (s == 0) *u -= dlt;
+                  else *u += dlt;
+                }
+              } else {
+                flux += s == 0 ? *u : -*u;
+                area += a;
+              }
+            }
+          }
+        }
+  }
+  out[0] = flux;
+  out[1] = area;
+}
+
+/* Contra2Cart (Source/rhs.c:35-749), its change of basis: periodic ghost
+ * values of Ucont are taken from the partner cells (:122-155); on fluid
+ * cells the centred face-flux averages q are turned into Cartesian
+ * velocity by Cramer's rule with the cell metrics csi, eta, zet (:160-240);
+ * the periodic ghosts of Ucat take their partners' values (:256-283); with
+ * zero_solid, cells with (int)(nvert + 0.1) == 3 get 0 (:304-307).  The
+ * wall-function and boundary-condition parts of the reference routine are
+ * momentum-solver physics and are not restated.  ucat in/out. */
+void or_contra2cart(const or_dims *d, const double *nvert, const double *csi, const double *eta, const double *zet,
+                    const double *ucont, double *ucat, int zero_solid)
+{
+  const int mx = d->mx, my = d->my, mz = d->mz;
+  const int ip = per_i(d), jp = per_j(d), kp = per_k(d);
+  const size_t N = (size_t)mx * my * mz;
+  double *lu = (double *)malloc(sizeof(double) * 3 * N);
+  memcpy(lu, ucont, sizeof(double) * 3 * N);
+  if (ip || jp || kp)
+    for (int k = 0; k < mz; k++)
+      for (int j = 0; j < my; j++)
+        for (int i = 0; i < mx; i++) {
+          int a = i, b = j, c = k, flag = 0;
+          if (ip && i == 0) a = mx - 2, flag = 1; else if (ip && i == mx - 1) a = 1, flag = 1;
+          if (jp && j == 0) b = my - 2, flag = 1; else if (jp && j == my - 1) b = 1, flag = 1;
+          if (kp && k == 0) c = mz - 2, flag = 1; else if (kp && k == mz - 1) c = 1, flag = 1;
+          if (flag) for (int q = 0; q < 3; q++) lu[IX(d, i, j, k) * 3 + q] = lu[IX(d, a, b, c) * 3 + q];
+        }
+  for (int k = 1; k < mz - 1; k++)
+    for (int j = 1; j < my - 1; j++)
+      for (int i = 1; i < mx - 1; i++) {
+        const size_t t = IX(d, i, j, k);
+        if (!(nvert[t] < 0.1)) continue;
+        const double *c0 = &csi[t * 3], *e0 = &eta[t * 3], *z0 = &zet[t * 3];
+        double m[3][3] = {{c0[0], c0[1], c0[2]}, {e0[0], e0[1], e0[2]}, {z0[0], z0[1], z0[2]}};
+        double q0 = 0.5 * (lu[IX(d, i - 1, j, k) * 3 + 0] + lu[t * 3 + 0]);
+        double q1 = 0.5 * (lu[IX(d, i, j - 1, k) * 3 + 1] + lu[t * 3 + 1]);
+        double q2 = 0.5 * (lu[IX(d, i, j, k - 1) * 3 + 2] + lu[t * 3 + 2]);
+        double det = m[0][0] * (m[1][1] * m[2][2] - m[1][2] * m[2][1]) -
+                     m[0][1] * (m[1][0] * m[2][2] - m[1][2] * m[2][0]) +
+                     m[0][2] * (m[1][0] * m[2][1] - m[1][1] * m[2][0]);
+        double det0 = q0 * (m[1][1] * m[2][2] - m[1][2] * m[2][1]) -
+                      q1 * (m[0][1] * m[2][2] - m[0][2] * m[2][1]) +
+                      q2 * (m[0][1] * m[1][2] - m[0][2] * m[1][1]);
+        double det1 = -q0 * (m[1][0] * m[2][2] - m[1][2] * m[2][0]) +
+                      q1 * (m[0][0] * m[2][2] - m[0][2] * m[2][0]) -
+                      q2 * (m[0][0] * m[1][2] - m[0][2] * m[1][0]);
+        double det2 = q0 * (m[1][0] * m[2][1] - m[1][1] * m[2][0]) -
+                      q1 * (m[0][0] * m[2][1] - m[0][1] * m[2][0]) +
+                      q2 * (m[0][0] * m[1][1] - m[0][1] * m[1][0]);
+        ucat[t * 3 + 0] = det0 / det;
+        ucat[t * 3 + 1] = det1 / det;
+        ucat[t * 3 + 2] = det2 / det;
+      }
+  if (ip || jp || kp)
+    for (int k = 0; k < mz; k++)
+      for (int j = 0; j < my; j++)
+        for (int i = 0; i < mx; i++) {
+          int a = i, b = j, c = k, flag = 0;
+          if (ip && i == 0) a = mx - 2, flag = 1; else if (ip && i == mx - 1) a = 1, flag = 1;
+          if (jp && j == 0) b = my - 2, flag = 1; else if (jp && j == my - 1) b = 1, flag = 1;
+          if (kp && k == 0) c = mz - 2, flag = 1; else if (kp && k == mz - 1) c = 1, flag = 1;
+          if (flag) for (int q = 0; q < 3; q++) ucat[IX(d, i, j, k) * 3 + q] = ucat[IX(d, a, b, c) * 3 + q];
+        }
+  if (zero_solid)
+    for (size_t t = 0; t < N; t++)
+      if ((int)(nvert[t] + 0.1) == 3) ucat[t * 3] = ucat[t * 3 + 1] = ucat[t * 3 + 2] = 0.;
+  free(lu);
 }

@@ -59,6 +59,12 @@ int or_poisson_lhs(const or_dims *d, const double *nvert, const or_metrics *m,
                    int scale_by_aj, int apply_filter, int *gid, int *rowtype,
                    double *vol, int *col);
 
+void or_volume_flux(const or_dims *d, const double *nvert, const double *csi, const double *eta, const double *zet,
+                    double *ucont, int flg, double flux_intp_sum, double *out);
+void or_contra2cart(const or_dims *d, const double *nvert, const double *csi, const double *eta, const double *zet,
+                    const double *ucont, double *ucat, int zero_solid);
+void or_poisson_rhs2(const or_dims *d, const double *nvert, const int *gid, const double *ucont,
+                     const double *aj, double dt, double st, double coeff, int poisson, double *b);
 void or_poisson_rhs2_hypre(const or_dims *d, const double *nvert, const int *gid,
                            const double *ucont, double dt, double st, double coeff,
                            double *b);

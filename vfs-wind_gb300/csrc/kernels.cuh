@@ -21,6 +21,16 @@ __global__ void k_count_dofs(Grid g, Box b, const double *nvert, int *block_coun
 __global__ void k_scan_blocks(int *block_count, int nblocks, int *total);
 __global__ void k_number_dofs(Grid g, Box b, const double *nvert, const int *block_off, int *gid_box);
 __global__ void k_gid_da(Grid g, Box b, const int *gid_box, int *gid_da);
+__global__ void k_rhs2(Grid g, Box b, const double *nvert, const uint8_t *rowtype, const double *ucont,
+                       const double *aj, double dt, double st, double coeff, int poisson, double *rhs, double *partial);
+__global__ void k_rhs2_shift(Grid g, Box b, const double *nvert, const double *aj, const double *sums, int poisson,
+                             double *rhs);
+__global__ void k_vflux_sum(Grid g, const double *nvert, MetricPtrs m, double *ucont, int flg, int pass,
+                            double *partial);
+__global__ void k_vflux_apply(Grid g, const double *nvert, MetricPtrs m, double *ucont, int flg, double corr);
+__global__ void k_periodic_cmpnts(Grid g, const double *src, double *dst);
+__global__ void k_contra2cart(Grid g, const double *nvert, MetricPtrs m, const double *lu, double *ucat);
+__global__ void k_zero_solid(Grid g, const double *nvert, double *ucat);
 __global__ void k_assemble(Grid g, Box b, const double *nvert, MetricPtrs m, int scale, int filter, int split, double *A,
                            uint8_t *rowtype);
 __global__ void k_projection_coef(Grid g, Box b, MetricPtrs m, double *pc);

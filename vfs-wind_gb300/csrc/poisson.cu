@@ -407,6 +407,7 @@ struct vfs_poisson {
   // residual of the iterate installed by the learned guess, handed to the
   // next solve (warm_start 2) so that it does not form it again
   double *rprev = nullptr, *rlearn = nullptr, *r0 = nullptr;
+  double *ucat = nullptr;  // Contra2Cart output staging (3 per DA point)
   double r0_norm = 0.;
   bool r0_valid = false;
   std::vector<Level> L;
@@ -1303,6 +1304,64 @@ int vfs_poisson_rhs(vfs_poisson *h, const double *ucont, double dt, double st, d
   h->have_rhs = true;
   h->r0_valid = false;
   return VFS_OK;
+}
+
+int vfs_poisson_rhs2(vfs_poisson *h, const double *ucont, double dt, double st, double coeff, int poisson) {
+  if (!h || !ucont) return fail(VFS_EINVAL, "null argument");
+  if (!h->have_nvert) return fail(VFS_ESTATE, "set_nvert must come before rhs");
+  if (!(dt != 0.) || !(coeff != 0.)) return fail(VFS_EINVAL, "dt and coeff must be non-zero");
+  if (poisson != 0 && poisson != -1) return fail(VFS_EINVAL, "poisson must be 0 or -1");
+  const size_t N = h->g.n();
+  TRY(upload(h, h->ucont, ucont, 3 * N));
+  LAUNCH(h, k_rhs2, kRedBlocks, 256, h->g, h->box, h->nvert, h->rowtype0, h->ucont, h->met.aj, dt, st, coeff,
+         poisson, h->b, h->partial);
+  LAUNCH(h, k_reduce_rows, 2, 1024, h->partial, kRedBlocks, 2, h->red);
+  LAUNCH(h, k_rhs2_shift, kRedBlocks, 256, h->g, h->box, h->nvert, h->met.aj, h->red, poisson, h->b);
+  TRY(sync(h));
+  h->have_rhs = true;
+  h->r0_valid = false;
+  return VFS_OK;
+}
+
+int vfs_poisson_volume_flux(vfs_poisson *h, double *ucont, int flg, double flux_intp_sum, double *ibm_flux,
+                            double *ibm_area) {
+  if (!h || !ucont) return fail(VFS_EINVAL, "null argument");
+  if (!h->have_nvert) return fail(VFS_ESTATE, "set_nvert must come before volume_flux");
+  if (flg < 0 || flg > 3) return fail(VFS_EINVAL, "flg must be 0..3");
+  const size_t N = h->g.n();
+  TRY(upload(h, h->ucont, ucont, 3 * N));
+  double sums[3];
+  LAUNCH(h, k_vflux_sum, kRedBlocks, 256, h->g, h->nvert, h->met, h->ucont, flg, 0, h->partial);
+  TRY(reduce_read(h, kRedBlocks, 3, sums));
+  double corr = 0.;
+  if (sums[2] > 1.e-15) {
+    if (flg > 1) corr = (sums[0] + flux_intp_sum) / sums[1];
+    else if (flg) corr = (sums[0] + flux_intp_sum) / sums[2];
+    else corr = sums[0] / sums[2];
+  }
+  LAUNCH(h, k_vflux_apply, kRedBlocks, 256, h->g, h->nvert, h->met, h->ucont, flg, corr);
+  LAUNCH(h, k_vflux_sum, kRedBlocks, 256, h->g, h->nvert, h->met, h->ucont, flg, 2, h->partial);
+  TRY(reduce_read(h, kRedBlocks, 3, sums));
+  if (ibm_flux) *ibm_flux = sums[0];
+  if (ibm_area) *ibm_area = sums[2];
+  TRY(download(h, ucont, h->ucont, 3 * N));
+  return sync(h);
+}
+
+int vfs_poisson_contra2cart(vfs_poisson *h, const double *ucont, double *ucat, int zero_solid) {
+  if (!h || !ucont || !ucat) return fail(VFS_EINVAL, "null argument");
+  if (!h->have_nvert) return fail(VFS_ESTATE, "set_nvert must come before contra2cart");
+  const size_t N = h->g.n();
+  if (!h->ucat) TRY(dalloc(h, &h->ucat, 3 * N));
+  TRY(upload(h, h->ucont, ucont, 3 * N));
+  TRY(upload(h, h->ucat, ucat, 3 * N));
+  LAUNCH(h, k_periodic_cmpnts, da_grid(h->g), 128, h->g, h->ucont, h->stage);
+  LAUNCH(h, k_contra2cart, dim3((h->g.mx - 2 + 127) / 128, h->g.my - 2, h->g.mz - 2), 128, h->g, h->nvert, h->met,
+         h->stage, h->ucat);
+  LAUNCH(h, k_periodic_cmpnts, da_grid(h->g), 128, h->g, h->ucat, h->stage);
+  if (zero_solid) LAUNCH(h, k_zero_solid, kRedBlocks, 256, h->g, h->nvert, h->stage);
+  TRY(download(h, ucat, h->stage, 3 * N));
+  return sync(h);
 }
 
 int vfs_poisson_solve(vfs_poisson *h, double *phi, const vfs_solve_opts *opts, vfs_solve_stats *stats) {

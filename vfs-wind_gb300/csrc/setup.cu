@@ -566,6 +566,58 @@ __global__ void k_rhs(Grid g, Box b, const double *__restrict__ nvert, const dou
   if (threadIdx.x == 0) { partial[blockIdx.x] = tb; partial[gridDim.x + blockIdx.x] = ta; }
 }
 
+// PoissonRHS2 (Source/poisson.c:1780-1906), the -poisson 0 / -1 variant:
+// the same divergence on fluid cells, 0 on identity-row dofs, the aj row
+// scaling for poisson == -1; block partials of the sum over every dof entry
+// and of the fluid count for the unweighted mean removal.
+__global__ void k_rhs2(Grid g, Box b, const double *__restrict__ nvert, const uint8_t *__restrict__ rowtype,
+                       const double *__restrict__ ucont, const double *__restrict__ aj, double dt, double st,
+                       double coeff, int poisson, double *rhs, double *partial) {
+  double sb = 0, cnt = 0;
+  const size_t n = b.n();
+  for (size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (size_t)gridDim.x * blockDim.x) {
+    int i = c % b.nx + 1, j = (c / b.nx) % b.ny + 1, k = c / ((size_t)b.nx * b.ny) + 1;
+    size_t t = g.at(i, j, k);
+    double val = 0.;
+    if (nvert[t] < 0.1) {
+#define U(a, bb, cc, q) ucont[g.at(a, bb, cc) * 3 + (q)]
+      val -= U(i, j, k, 0);
+      if (i == 1 && g.px) val += U(g.mx - 2, j, k, 0);
+      else val += U(i - 1, j, k, 0);
+      val -= U(i, j, k, 1);
+      if (j == 1 && g.py) val += U(i, g.my - 2, k, 1);
+      else val += U(i, j - 1, k, 1);
+      val -= U(i, j, k, 2);
+      if (k == 1 && g.pz) val += U(i, j, g.mz - 2, 2);
+      else val += U(i, j, k - 1, 2);
+#undef U
+      val *= -1.0 / dt * st * coeff;
+      if (poisson == -1) val *= aj[t];
+      cnt += 1.;
+    }
+    if (rowtype[c]) sb += val;
+    rhs[c] = val;
+  }
+  double tb = block_sum(sb);
+  double tc = block_sum(cnt);
+  if (threadIdx.x == 0) { partial[blockIdx.x] = tb; partial[gridDim.x + blockIdx.x] = tc; }
+}
+// the unweighted shift of PoissonRHS2 on fluid cells; for poisson == -1 the
+// solver's (unscaled) right-hand side is B / aj on those rows
+__global__ void k_rhs2_shift(Grid g, Box b, const double *__restrict__ nvert, const double *__restrict__ aj,
+                             const double *sums, int poisson, double *rhs) {
+  const double val = -sums[0] / (sums[1] > 0. ? sums[1] : 1.);
+  const size_t n = b.n();
+  for (size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (size_t)gridDim.x * blockDim.x) {
+    int i = c % b.nx + 1, j = (c / b.nx) % b.ny + 1, k = c / ((size_t)b.nx * b.ny) + 1;
+    size_t t = g.at(i, j, k);
+    if (nvert[t] < 0.1) {
+      rhs[c] += val;
+      if (poisson == -1) rhs[c] = rhs[c] / aj[t];
+    }
+  }
+}
+
 // sums row blockIdx.x of `nb` block partials in a fixed tree order (launch
 // one block per row)
 __global__ void k_reduce_rows(const double *partial, int nb, int nrow, double *out) {
@@ -926,6 +978,132 @@ __global__ void k_prolong_f32(Box bf, Box bc, int cx, int cy, int cz, const floa
 __global__ void k_prolong_f64(Box bf, Box bc, int cx, int cy, int cz, const double *xc, const uint8_t *blank_c,
                               const uint8_t *blank_f, double *xf, int add) {
   prolong_body<double>(bf, bc, cx, cy, cz, xc, blank_c, blank_f, xf, add);
+}
+
+}  // namespace vfs
+
+namespace vfs {
+
+// ---- VolumeFlux (Source/poisson.c:3563-3903, immersed == 1) ----
+// Faces between a fluid cell and an IB cell (0.1 < nvert < 1.1), visited
+// once each from the cell below them in i, j or k: s = 0 the cell is fluid
+// and the face's neighbour IB, s = 1 the reverse.
+struct VfluxFace {
+  double *u;
+  double a;
+  int s;
+};
+__device__ inline int vflux_faces(Grid g, const double *nvert, MetricPtrs m, double *ucont, int i, int j, int k,
+                                  VfluxFace f[6]) {
+  const size_t t = g.at(i, j, k);
+  const size_t nb[3] = {g.at(i + 1, j, k), g.at(i, j + 1, k), g.at(i, j, k + 1)};
+  const bool in[3] = {i < g.mx - 2, j < g.my - 2, k < g.mz - 2};
+  const double *met[3] = {m.csi, m.eta, m.zet};
+  int nf = 0;
+  for (int s = 0; s < 2; s++) {
+    if (s == 0 && !(nvert[t] < 0.1)) continue;
+    if (s == 1 && !(nvert[t] > 0.1 && nvert[t] < 1.1)) continue;
+    for (int q = 0; q < 3; q++) {
+      const double nn = nvert[nb[q]];
+      const bool face = s == 0 ? (nn > 0.1 && nn < 1.1) : (nn < 0.1);
+      if (!face || !in[q]) continue;
+      const double *mm = &met[q][t * 3];
+      f[nf].u = &ucont[t * 3 + q];
+      f[nf].a = sqrt(mm[0] * mm[0] + mm[1] * mm[1] + mm[2] * mm[2]);
+      f[nf].s = s;
+      nf++;
+    }
+  }
+  return nf;
+}
+
+// pass 0: zero |U| <= 1e-8 and sum flux, |U| (or |U| / area for flg 3)
+// and area; pass 2: sum flux and area after the correction
+__global__ void k_vflux_sum(Grid g, const double *__restrict__ nvert, MetricPtrs m, double *ucont, int flg, int pass,
+                            double *partial) {
+  double sf = 0, sab = 0, sa = 0;
+  const size_t n = (size_t)(g.mx - 2) * (g.my - 2) * (g.mz - 2);
+  for (size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (size_t)gridDim.x * blockDim.x) {
+    const int i = c % (g.mx - 2) + 1, j = (c / (g.mx - 2)) % (g.my - 2) + 1, k = c / ((size_t)(g.mx - 2) * (g.my - 2)) + 1;
+    VfluxFace f[6];
+    const int nf = vflux_faces(g, nvert, m, ucont, i, j, k, f);
+    for (int q = 0; q < nf; q++) {
+      const double u = *f[q].u;
+      if (pass == 0) {
+        if (fabs(u) > 1.e-8) {
+          sf += f[q].s == 0 ? u : -u;
+          sab += flg == 3 ? fabs(u) / f[q].a : fabs(u);
+          sa += f[q].a;
+        } else {
+          *f[q].u = 0.;
+        }
+      } else {
+        sf += f[q].s == 0 ? u : -u;
+        sa += f[q].a;
+      }
+    }
+  }
+  const double t0 = block_sum(sf), t1 = block_sum(sab), t2 = block_sum(sa);
+  if (threadIdx.x == 0) {
+    partial[blockIdx.x] = t0;
+    partial[gridDim.x + blockIdx.x] = t1;
+    partial[2 * gridDim.x + blockIdx.x] = t2;
+  }
+}
+
+__global__ void k_vflux_apply(Grid g, const double *__restrict__ nvert, MetricPtrs m, double *ucont, int flg,
+                              double corr) {
+  const size_t n = (size_t)(g.mx - 2) * (g.my - 2) * (g.mz - 2);
+  for (size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (size_t)gridDim.x * blockDim.x) {
+    const int i = c % (g.mx - 2) + 1, j = (c / (g.mx - 2)) % (g.my - 2) + 1, k = c / ((size_t)(g.mx - 2) * (g.my - 2)) + 1;
+    VfluxFace f[6];
+    const int nf = vflux_faces(g, nvert, m, ucont, i, j, k, f);
+    for (int q = 0; q < nf; q++) {
+      const double u = *f[q].u;
+      if (!(fabs(u) > 1.e-8)) continue;
+      double dlt;
+      if (flg == 3) dlt = corr * fabs(u) / f[q].a;
+      else if (flg == 2) dlt = corr * fabs(u);
+      else dlt = f[q].a * corr;
+      *f[q].u = f[q].s == 0 ? u - dlt : u + dlt;
+    }
+  }
+}
+
+// ---- Contra2Cart (Source/rhs.c:35-749), its change of basis ----
+// periodic ghosts of a Cmpnts DA array take their partners' values
+__global__ void k_periodic_cmpnts(Grid g, const double *src, double *dst) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y, k = blockIdx.z;
+  if (i >= g.mx) return;
+  int a, b, c, fi, fj, fk;
+  const size_t t = g.at(i, j, k);
+  const size_t s = g.remap(i, j, k, a, b, c, fi, fj, fk) ? g.at(a, b, c) : t;
+  for (int q = 0; q < 3; q++) dst[t * 3 + q] = src[s * 3 + q];
+}
+__global__ void k_contra2cart(Grid g, const double *__restrict__ nvert, MetricPtrs m, const double *__restrict__ lu,
+                              double *ucat) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x + 1, j = blockIdx.y + 1, k = blockIdx.z + 1;
+  if (i >= g.mx - 1) return;
+  const size_t t = g.at(i, j, k);
+  if (!(nvert[t] < 0.1)) return;
+  const double *c0 = &m.csi[t * 3], *e0 = &m.eta[t * 3], *z0 = &m.zet[t * 3];
+  const double m00 = c0[0], m01 = c0[1], m02 = c0[2], m10 = e0[0], m11 = e0[1], m12 = e0[2], m20 = z0[0],
+               m21 = z0[1], m22 = z0[2];
+  const double q0 = 0.5 * (lu[g.at(i - 1, j, k) * 3 + 0] + lu[t * 3 + 0]);
+  const double q1 = 0.5 * (lu[g.at(i, j - 1, k) * 3 + 1] + lu[t * 3 + 1]);
+  const double q2 = 0.5 * (lu[g.at(i, j, k - 1) * 3 + 2] + lu[t * 3 + 2]);
+  const double det = m00 * (m11 * m22 - m12 * m21) - m01 * (m10 * m22 - m12 * m20) + m02 * (m10 * m21 - m11 * m20);
+  const double det0 = q0 * (m11 * m22 - m12 * m21) - q1 * (m01 * m22 - m02 * m21) + q2 * (m01 * m12 - m02 * m11);
+  const double det1 = -q0 * (m10 * m22 - m12 * m20) + q1 * (m00 * m22 - m02 * m20) - q2 * (m00 * m12 - m02 * m10);
+  const double det2 = q0 * (m10 * m21 - m11 * m20) - q1 * (m00 * m21 - m01 * m20) + q2 * (m00 * m11 - m01 * m10);
+  ucat[t * 3 + 0] = det0 / det;
+  ucat[t * 3 + 1] = det1 / det;
+  ucat[t * 3 + 2] = det2 / det;
+}
+__global__ void k_zero_solid(Grid g, const double *nvert, double *ucat) {
+  const size_t n = g.n();
+  for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x)
+    if ((int)(nvert[t] + 0.1) == 3) ucat[t * 3] = ucat[t * 3 + 1] = ucat[t * 3 + 2] = 0.;
 }
 
 }  // namespace vfs

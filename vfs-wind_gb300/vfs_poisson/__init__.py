@@ -37,7 +37,7 @@ EXPORTS = [
     "vfs_unet_create", "vfs_unet_destroy", "vfs_unet_set_stream", "vfs_unet_num_params", "vfs_unet_get_params",
     "vfs_unet_set_params", "vfs_unet_forward", "vfs_unet_gradient", "vfs_unet_train_step", "vfs_unet_adam",
     "vfs_unet_set_grads", "vfs_unet_kernel_launches", "vfs_poisson_learned_guess", "vfs_poisson_guess_sample",
-    "vfs_poisson_get_operator32",
+    "vfs_poisson_get_operator32", "vfs_poisson_rhs2", "vfs_poisson_volume_flux", "vfs_poisson_contra2cart",
 ]
 
 
@@ -135,6 +135,9 @@ def load(path=LIB_PATH):
     L.vfs_poisson_learned_guess.argtypes = [vp, vp, vp, vp, C.c_double, P(C.c_int), vp]
     L.vfs_poisson_guess_sample.argtypes = [vp, vp, vp, vp, vp, vp, vp]
     L.vfs_poisson_get_operator32.argtypes = [vp, vp]
+    L.vfs_poisson_rhs2.argtypes = [vp, dp, C.c_double, C.c_double, C.c_double, C.c_int]
+    L.vfs_poisson_volume_flux.argtypes = [vp, dp, C.c_int, C.c_double, P(C.c_double), P(C.c_double)]
+    L.vfs_poisson_contra2cart.argtypes = [vp, dp, dp, C.c_int]
     _lib = L
     return L
 
@@ -218,6 +221,23 @@ class PoissonSolver:
     # --- per step ---
     def rhs(self, ucont, dt=1.0, st=1.0, coeff=1.0):
         _check(load().vfs_poisson_rhs(self.h, _ptr(ucont), dt, st, coeff))
+
+    def rhs2(self, ucont, poisson=0, dt=1.0, st=1.0, coeff=1.0):
+        """PoissonRHS2, the -poisson 0 / -1 right-hand side."""
+        _check(load().vfs_poisson_rhs2(self.h, _ptr(ucont), dt, st, coeff, int(poisson)))
+
+    def volume_flux(self, ucont, flg=0, flux_intp_sum=0.0):
+        """VolumeFlux (immersed): corrects ucont in place; returns (flux, area)."""
+        f, a = C.c_double(), C.c_double()
+        _check(load().vfs_poisson_volume_flux(self.h, _ptr(ucont, True), int(flg), float(flux_intp_sum),
+                                              C.byref(f), C.byref(a)))
+        return f.value, a.value
+
+    def contra2cart(self, ucont, ucat=None, zero_solid=True):
+        """Contra2Cart's change of basis; returns ucat (DA Cmpnts)."""
+        out = np.zeros(self._shape(3)) if ucat is None else ucat
+        _check(load().vfs_poisson_contra2cart(self.h, _ptr(ucont), _ptr(out, True), int(zero_solid)))
+        return out
 
     def solve(self, phi=None, opts=None, **kw):
         o = opts if opts is not None else default_opts(**kw)

@@ -354,6 +354,37 @@ int vfs_poisson_guess_sample(vfs_poisson *h, const double *phi_n, const double *
  * B NE SE NW SW TN BN TS BS TE BE TW BW (host or device memory, 19 n). */
 int vfs_poisson_get_operator32(vfs_poisson *h, float *planes);
 
+/* ---------------------------------------------------------------------
+ * The reference's input files (host code, no GPU).  Two-call pattern:
+ * with a NULL output buffer a call only reports the sizes.
+ * --------------------------------------------------------------------- */
+
+/* PETSc binary vector (VecView / VecLoadIntoVector of the restart fields
+ * vfield / pfield / nvfield, Source/main.c:376-935): big-endian class id
+ * 1211214, length, values.  On one rank a DA vector is stored in the DA
+ * natural layout, so these are the library's DA arrays (Cmpnts fields
+ * interleaved).  *n: in: buffer length; out: the vector's length. */
+int vfs_read_petsc_vec(const char *path, int64_t *n, double *values);
+int vfs_write_petsc_vec(const char *path, int64_t n, const double *values);
+
+/* Grid nodes (Source/init.c:254-366).  format 0: xyz.dat (IM JM KM, then
+ * IM rows "x y z" of which x is used, JM rows for y, KM rows for z: a
+ * tensor-product grid); 1: grid.dat as text (block count, then per block
+ * IM JM KM and the IM*JM*KM x values, then y, then z, i fastest); 2: the
+ * same in native binary.  dims[0..2] = IM, JM, KM of block `block`; coor
+ * (may be NULL) is the DA-layout node array [KM+1][JM+1][IM+1][3] (node
+ * (i,j,k) at i < IM, the last layer left as is), coordinates / cl * L_dim. */
+int vfs_read_grid(const char *path, int format, int block, double L_dim, double cl, int *dims, double *coor);
+
+/* UCD surface (ibmdata%02d, ibm_read_ucd, Source/ibm_io.c:782-1011): three
+ * header lines, "n_v n_elmt 0 0 0", n_v rows "id x y z", n_elmt rows
+ * "id mat tri n1 n2 n3" (1-based).  place (may be NULL): L_dim, CMx_c,
+ * CMy_c, CMz_c, x_r, y_r, z_r, angle_x0, angle_y0, angle_z0 - the
+ * reference's scaling, offset and initial rotations, applied in its order.
+ * xyz: n_v x 3; tri: n_elmt x 3, 0-based; *n_v / *n_elmt: in: capacities,
+ * out: counts. */
+int vfs_read_ucd(const char *path, const double *place, int *n_v, int *n_elmt, double *xyz, int32_t *tri);
+
 #ifdef __cplusplus
 }
 #endif

@@ -38,6 +38,7 @@ EXPORTS = [
     "vfs_unet_set_params", "vfs_unet_forward", "vfs_unet_gradient", "vfs_unet_train_step", "vfs_unet_adam",
     "vfs_unet_set_grads", "vfs_unet_kernel_launches", "vfs_poisson_learned_guess", "vfs_poisson_guess_sample",
     "vfs_poisson_get_operator32", "vfs_poisson_rhs2", "vfs_poisson_volume_flux", "vfs_poisson_contra2cart",
+    "vfs_read_petsc_vec", "vfs_write_petsc_vec", "vfs_read_grid", "vfs_read_ucd",
 ]
 
 
@@ -138,6 +139,10 @@ def load(path=LIB_PATH):
     L.vfs_poisson_rhs2.argtypes = [vp, dp, C.c_double, C.c_double, C.c_double, C.c_int]
     L.vfs_poisson_volume_flux.argtypes = [vp, dp, C.c_int, C.c_double, P(C.c_double), P(C.c_double)]
     L.vfs_poisson_contra2cart.argtypes = [vp, dp, dp, C.c_int]
+    L.vfs_read_petsc_vec.argtypes = [C.c_char_p, P(C.c_int64), vp]
+    L.vfs_write_petsc_vec.argtypes = [C.c_char_p, C.c_int64, vp]
+    L.vfs_read_grid.argtypes = [C.c_char_p, C.c_int, C.c_int, C.c_double, C.c_double, vp, vp]
+    L.vfs_read_ucd.argtypes = [C.c_char_p, vp, P(C.c_int), P(C.c_int), vp, vp]
     _lib = L
     return L
 
@@ -451,3 +456,46 @@ class UNet:
 
     def kernel_launches(self):
         return load().vfs_unet_kernel_launches(self.u)
+
+
+# --- the reference's input files (host) ---
+def read_petsc_vec(path):
+    """A PETSc binary vector (restart field) as a float64 array."""
+    L = load()
+    n = C.c_int64(0)
+    _check(L.vfs_read_petsc_vec(path.encode(), C.byref(n), None))
+    out = np.zeros(n.value)
+    _check(L.vfs_read_petsc_vec(path.encode(), C.byref(n), _ptr(out, True)))
+    return out
+
+
+def write_petsc_vec(path, values):
+    v = np.ascontiguousarray(values, np.float64).ravel()
+    _check(load().vfs_write_petsc_vec(path.encode(), v.size, _ptr(v)))
+
+
+GRID_XYZ, GRID_TEXT, GRID_BINARY = 0, 1, 2
+
+
+def read_grid(path, fmt=GRID_XYZ, block=0, L_dim=1.0, cl=1.0):
+    """Grid nodes as the DA-layout array [KM+1][JM+1][IM+1][3]."""
+    L = load()
+    dims = np.zeros(3, np.int32)
+    _check(L.vfs_read_grid(path.encode(), fmt, block, L_dim, cl, _ptr(dims, True), None))
+    IM, JM, KM = (int(v) for v in dims)
+    coor = np.zeros((KM + 1, JM + 1, IM + 1, 3))
+    _check(L.vfs_read_grid(path.encode(), fmt, block, L_dim, cl, _ptr(dims, True), _ptr(coor, True)))
+    return coor
+
+
+def read_ucd(path, L_dim=1.0, cm=(0.0, 0.0, 0.0), centre=(0.0, 0.0, 0.0), angles=(0.0, 0.0, 0.0)):
+    """A UCD surface as (xyz[n_v, 3], tri[n_elmt, 3] 0-based), placed like
+    the reference's ibm_read_ucd."""
+    L = load()
+    nv, ne = C.c_int(0), C.c_int(0)
+    _check(L.vfs_read_ucd(path.encode(), None, C.byref(nv), C.byref(ne), None, None))
+    xyz = np.zeros((nv.value, 3))
+    tri = np.zeros((ne.value, 3), np.int32)
+    place = np.array([L_dim, *cm, *centre, *angles], np.float64)
+    _check(L.vfs_read_ucd(path.encode(), _ptr(place), C.byref(nv), C.byref(ne), _ptr(xyz, True), _ptr(tri, True)))
+    return xyz, tri

@@ -28,6 +28,7 @@ UNITS = {
     "noalloc.cu": ["-fmad=false"],
     "ibm.cu": ["-fmad=false", "-Xcompiler", "-ffp-contract=off"],
     "unet.cu": [],
+    "io.cpp": ["-Xcompiler", "-ffp-contract=off"],
 }
 
 
@@ -38,7 +39,7 @@ def _nvcc():
 
 def _sources():
     return [os.path.join(CSRC, f) for f in os.listdir(CSRC)
-            if f.endswith((".cu", ".cuh", ".h"))] + [os.path.join(INCLUDE, f) for f in os.listdir(INCLUDE)]
+            if f.endswith((".cu", ".cuh", ".h", ".cpp"))] + [os.path.join(INCLUDE, f) for f in os.listdir(INCLUDE)]
 
 
 def build(force=False, verbose=False):
@@ -50,7 +51,7 @@ def build(force=False, verbose=False):
     objs = []
 
     def compile_one(name):
-        obj = os.path.join(OUT_DIR, name.replace(".cu", ".o"))
+        obj = os.path.join(OUT_DIR, os.path.splitext(name)[0] + ".o")
         cmd = [nvcc, *ARCH, *COMMON, *UNITS[name], "-c", os.path.join(CSRC, name), "-o", obj]
         if verbose:
             print(" ".join(cmd))

@@ -26,6 +26,7 @@
  *   PoissonRHS2               poisson.c:1780       -> vfs_poisson_rhs2
  *   VolumeFlux (immersed)     poisson.c:3563       -> vfs_poisson_volume_flux
  *   Contra2Cart               rhs.c:35             -> vfs_poisson_contra2cart
+ *   levelset operator / projection poisson.c:1171, :2738 -> vfs_poisson_set_levelset
  *   PoissonSolver_Hypre       poisson_hypre.c:506  -> vfs_poisson_solve
  *   Remove_Nullspace          poisson_hypre.c:202  (inside vfs_poisson_solve)
  *   Convert_Phi2_Phi          poisson.c:98         (inside vfs_poisson_solve)
@@ -121,6 +122,20 @@ int vfs_poisson_set_nvert(vfs_poisson *h, const double *nvert);
 /* Right-hand side from Ucont: PoissonRHS2_hypre + Remove_Nullspace_Scale.
  * coeff is time_coeff() (Source/poisson.c:23-31). */
 int vfs_poisson_rhs(vfs_poisson *h, const double *ucont, double dt, double st, double coeff);
+
+/* Level-set (two-phase) variant of the operator and the projection
+ * (levelset in Source/poisson.c:1171-1561 and :2738-2956): every face
+ * coefficient is divided by the harmonic mean of the two cells' densities
+ * (mean(), Source/level.c:2276); bctype[3] == 4 / bctype[5] == 4 make the
+ * top j / k face a zero-Dirichlet pressure face; bctype[4] == 5000 opens the
+ * bottom k face of the cells with level < 0 (density of the cell there) and
+ * bctype[4] == 5 makes it Dirichlet.  rho and level: DA-layout cell fields
+ * (level may be NULL when bctype[4] != 5000).  The multigrid levels use
+ * child averages of both fields.  With bctype[5] == 4 the right-hand side
+ * and phi keep their means, as the reference skips both null-space
+ * removals then.  Call before vfs_poisson_set_nvert (which assembles);
+ * enable = 0 turns it off. */
+int vfs_poisson_set_levelset(vfs_poisson *h, const double *rho, const double *level, const int *bctype, int enable);
 
 /* PoissonRHS2 (Source/poisson.c:1780-1906), the right-hand side of the
  * -poisson 0 (poisson = 0) and -poisson -1 (poisson = -1) paths: the same

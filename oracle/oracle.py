@@ -74,6 +74,7 @@ def lib():
         L.or_poisson_lhs.restype = C.c_int
         L.or_poisson_rhs2_hypre.argtypes = [P(Dims), dp, ip, dp, C.c_double, C.c_double, C.c_double, dp]
         L.or_poisson_rhs2.argtypes = [P(Dims), dp, ip, dp, dp, C.c_double, C.c_double, C.c_double, C.c_int, dp]
+        L.or_set_levelset.argtypes = [dp, dp, C.c_int, C.c_int, C.c_int, C.c_int]
         L.or_volume_flux.argtypes = [P(Dims), dp, dp, dp, dp, dp, C.c_int, C.c_double, dp]
         L.or_contra2cart.argtypes = [P(Dims), dp, dp, dp, dp, dp, dp, C.c_int]
         L.or_remove_nullspace_scale.argtypes = [P(Dims), dp, ip, dp, dp, C.c_int]
@@ -195,6 +196,22 @@ def rhs2(d, nvert, gid, ucont, aj, poisson=0, dt=1.0, st=1.0, coeff=1.0):
                           _ip(np.ascontiguousarray(gid, np.int32).ravel()), _dp(np.ascontiguousarray(ucont)),
                           _dp(np.ascontiguousarray(aj, np.float64)), dt, st, coeff, int(poisson), _dp(b))
     return b[:n]
+
+
+_ls_keep = None
+
+
+def set_levelset(rho=None, level=None, bctype=(0, 0, 0, 0, 0, 0)):
+    """Level-set context of poisson_lhs / projection (rho None: off)."""
+    global _ls_keep
+    if rho is None:
+        _ls_keep = None
+        lib().or_set_levelset(None, None, 0, 0, 0, 0)
+        return
+    r = np.ascontiguousarray(rho, np.float64)
+    lv = np.ascontiguousarray(level if level is not None else np.zeros_like(r), np.float64)
+    _ls_keep = (r, lv)
+    lib().or_set_levelset(_dp(r), _dp(lv), 1, int(bctype[3]), int(bctype[4]), int(bctype[5]))
 
 
 def volume_flux(d, nvert, met, ucont, flg=0, flux_intp_sum=0.0):

@@ -361,6 +361,22 @@ int or_setup_lidx2(const or_dims *d, const double *nvert, int *gid)
 /* scale_by_aj reproduces the poisson == -1 row scaling (poisson.c:1563).  */
 /* apply_filter = 0 keeps entries with |v| <= 1e-10 (used by the V-cycle).  */
 /* ------------------------------------------------------------------------ */
+/* Level-set context of PoissonLHSNew and Projection (poisson.c:1171-1561,
+ * :2738-2950): density rho and level-set field at the cells (DA layout),
+ * on = levelset, bc3 / bc4 / bc5 = user->bctype[3], [4], [5]. */
+static struct {
+  const double *rho, *level;
+  int on, bc3, bc4, bc5;
+} g_ls = {0, 0, 0, 0, 0, 0};
+
+void or_set_levelset(const double *rho, const double *level, int on, int bc3, int bc4, int bc5)
+{
+  g_ls.rho = rho; g_ls.level = level; g_ls.on = on; g_ls.bc3 = bc3; g_ls.bc4 = bc4; g_ls.bc5 = bc5;
+}
+
+/* mean (level.c:2276-2280), the harmonic mean of two densities */
+static double ls_mean(double A, double B) { return 2.0 * A * B / (A + B); }
+
 int or_poisson_lhs(const or_dims *d, const double *nvert, const or_metrics *m, int scale_by_aj,
                    int apply_filter, int *gid, int *rowtype, double *vol, int *col)
 {
@@ -393,6 +409,8 @@ int or_poisson_lhs(const or_dims *d, const double *nvert, const or_metrics *m, i
       }
 #define NV(i, j, k) nvert[IX(d, i, j, k)]
 #define G(q, i, j, k) g[IX(d, i, j, k) * 9 + (q)]
+#define RHO(i, j, k) g_ls.rho[IX(d, i, j, k)]
+#define LEV(i, j, k) g_ls.level[IX(d, i, j, k)]
   for (size_t q = 0; q < n; q++) {
     rowtype[q] = OR_ROW_NONE;
     for (int s = 0; s < 19; s++) { vol[q * 19 + s] = 0.; col[q * 19 + s] = -1; }
@@ -412,9 +430,10 @@ int or_poisson_lhs(const or_dims *d, const double *nvert, const or_metrics *m, i
         if (NV(i, j, k) > thr) continue;
         double v[19];
         for (int s = 0; s < 19; s++) v[s] = 0.;
-        const double r = 1.0;
+        double r = 1.0;
         /* i+1 - i: poisson.c:1167-1230 */
         if (NV(i + 1, j, k) < thr && (i != mx - 2 || ip)) {
+          r = g_ls.on ? ls_mean(RHO(i + 1, j, k), RHO(i, j, k)) : 1.0;
           v[OR_CP] -= G(0, i, j, k) / r;
           v[OR_EP] += G(0, i, j, k) / r;
           if ((j == my - 2 && !jp) || NV(i, j + 1, k) + NV(i + 1, j + 1, k) > thr) {
@@ -448,6 +467,7 @@ int or_poisson_lhs(const or_dims *d, const double *nvert, const or_metrics *m, i
         }
         /* i - i-1: poisson.c:1233-1293 */
         if (NV(i - 1, j, k) < thr && (i != 1 || ip)) {
+          r = g_ls.on ? ls_mean(RHO(i - 1, j, k), RHO(i, j, k)) : 1.0;
           v[OR_CP] -= G(0, i - 1, j, k) / r;
           v[OR_WP] += G(0, i - 1, j, k) / r;
           if ((j == my - 2 && !jp) || NV(i, j + 1, k) + NV(i - 1, j + 1, k) > thr) {
@@ -480,7 +500,8 @@ int or_poisson_lhs(const or_dims *d, const double *nvert, const or_metrics *m, i
           }
         }
         /* j+1 - j: poisson.c:1296-1361 */
-        if (NV(i, j + 1, k) < thr && (j != my - 2 || jp)) {
+        if (NV(i, j + 1, k) < thr && (j != my - 2 || jp || (g_ls.on && g_ls.bc3 == 4 && j == my - 2))) {
+          r = g_ls.on ? ls_mean(RHO(i, j + 1, k), RHO(i, j, k)) : 1.0;
           if ((i == mx - 2 && !ip) || NV(i + 1, j, k) + NV(i + 1, j + 1, k) > thr) {
             if (NV(i - 1, j, k) + NV(i - 1, j + 1, k) < thr && i != 1) {
               v[OR_CP] += G(3, i, j, k) * 0.5 / r; v[OR_NP] += G(3, i, j, k) * 0.5 / r;
@@ -495,8 +516,12 @@ int or_poisson_lhs(const or_dims *d, const double *nvert, const or_metrics *m, i
             v[OR_EP] += G(3, i, j, k) * 0.25 / r; v[OR_NE] += G(3, i, j, k) * 0.25 / r;
             v[OR_WP] -= G(3, i, j, k) * 0.25 / r; v[OR_NW] -= G(3, i, j, k) * 0.25 / r;
           }
-          v[OR_CP] -= G(4, i, j, k) / r;
-          v[OR_NP] += G(4, i, j, k) / r;
+          if (g_ls.on && g_ls.bc3 == 4 && j == my - 2) { /* zero Dirichlet pressure, poisson.c:1328 */
+            v[OR_CP] -= G(4, i, j, k) / 0.5 / r;
+          } else {
+            v[OR_CP] -= G(4, i, j, k) / r;
+            v[OR_NP] += G(4, i, j, k) / r;
+          }
           if ((k == mz - 2 && !kp) || NV(i, j, k + 1) + NV(i, j + 1, k + 1) > thr) {
             if (NV(i, j, k - 1) + NV(i, j + 1, k - 1) < thr && k != 1) {
               v[OR_CP] += G(5, i, j, k) * 0.5 / r; v[OR_NP] += G(5, i, j, k) * 0.5 / r;
@@ -514,6 +539,7 @@ int or_poisson_lhs(const or_dims *d, const double *nvert, const or_metrics *m, i
         }
         /* j - j-1: poisson.c:1364-1422 */
         if (NV(i, j - 1, k) < thr && (j != 1 || jp)) {
+          r = g_ls.on ? ls_mean(RHO(i, j - 1, k), RHO(i, j, k)) : 1.0;
           if ((i == mx - 2 && !ip) || NV(i + 1, j, k) + NV(i + 1, j - 1, k) > thr) {
             if (NV(i - 1, j, k) + NV(i - 1, j - 1, k) < thr && i != 1) {
               v[OR_CP] -= G(3, i, j - 1, k) * 0.5 / r; v[OR_SP] -= G(3, i, j - 1, k) * 0.5 / r;
@@ -546,7 +572,8 @@ int or_poisson_lhs(const or_dims *d, const double *nvert, const or_metrics *m, i
           }
         }
         /* k+1 - k: poisson.c:1425-1491 */
-        if (NV(i, j, k + 1) < thr && (k != mz - 2 || kp)) {
+        if (NV(i, j, k + 1) < thr && (k != mz - 2 || kp || (g_ls.on && g_ls.bc5 == 4 && k == mz - 2))) {
+          r = g_ls.on ? ls_mean(RHO(i, j, k + 1), RHO(i, j, k)) : 1.0;
           if ((i == mx - 2 && !ip) || NV(i + 1, j, k) + NV(i + 1, j, k + 1) > thr) {
             if (NV(i - 1, j, k) + NV(i - 1, j, k + 1) < thr && i != 1) {
               v[OR_CP] += G(6, i, j, k) * 0.5 / r; v[OR_TP] += G(6, i, j, k) * 0.5 / r;
@@ -575,11 +602,16 @@ int or_poisson_lhs(const or_dims *d, const double *nvert, const or_metrics *m, i
             v[OR_NP] += G(7, i, j, k) * 0.25 / r; v[OR_TN] += G(7, i, j, k) * 0.25 / r;
             v[OR_SP] -= G(7, i, j, k) * 0.25 / r; v[OR_TS] -= G(7, i, j, k) * 0.25 / r;
           }
-          v[OR_CP] -= G(8, i, j, k) / r;
-          v[OR_TP] += G(8, i, j, k) / r;
+          if (g_ls.on && g_ls.bc5 == 4 && k == mz - 2) { /* poisson.c:1482-1484 */
+            v[OR_CP] -= G(8, i, j, k) / 0.5 / r;
+          } else {
+            v[OR_CP] -= G(8, i, j, k) / r;
+            v[OR_TP] += G(8, i, j, k) / r;
+          }
         }
         /* k - k-1: poisson.c:1494-1561 */
-        if (NV(i, j, k - 1) < thr && (k != 1 || kp)) {
+        if (NV(i, j, k - 1) < thr && (k != 1 || kp || (g_ls.on && g_ls.bc4 == 5000 && k == 1 && LEV(i, j, k) < 0))) {
+          r = g_ls.on ? (k == 1 ? RHO(i, j, k) : ls_mean(RHO(i, j, k - 1), RHO(i, j, k))) : 1.0;
           if ((i == mx - 2 && !ip) || NV(i + 1, j, k) + NV(i + 1, j, k - 1) > thr) {
             if (NV(i - 1, j, k) + NV(i - 1, j, k - 1) < thr && i != 1) {
               v[OR_CP] -= G(6, i, j, k - 1) * 0.5 / r; v[OR_BP] -= G(6, i, j, k - 1) * 0.5 / r;
@@ -608,8 +640,12 @@ int or_poisson_lhs(const or_dims *d, const double *nvert, const or_metrics *m, i
             v[OR_NP] -= G(7, i, j, k - 1) * 0.25 / r; v[OR_BN] -= G(7, i, j, k - 1) * 0.25 / r;
             v[OR_SP] += G(7, i, j, k - 1) * 0.25 / r; v[OR_BS] += G(7, i, j, k - 1) * 0.25 / r;
           }
-          v[OR_CP] -= G(8, i, j, k - 1) / r;
-          v[OR_BP] += G(8, i, j, k - 1) / r;
+          if (g_ls.on && g_ls.bc4 == 5 && k == 1) { /* poisson.c:1552-1554 */
+            v[OR_CP] -= G(8, i, j, k - 1) / 0.5 / r;
+          } else {
+            v[OR_CP] -= G(8, i, j, k - 1) / r;
+            v[OR_BP] += G(8, i, j, k - 1) / r;
+          }
         }
         if (scale_by_aj)
           for (int s = 0; s < 19; s++) v[s] *= m->aj[t];
@@ -630,6 +666,8 @@ int or_poisson_lhs(const or_dims *d, const double *nvert, const or_metrics *m, i
       }
 #undef NV
 #undef G
+#undef RHO
+#undef LEV
   free(g);
   return ndof;
 }
@@ -833,7 +871,13 @@ void or_projection(const or_dims *d, const double *nvert, const double *phi, con
   for (int k = 1; k < mz - 1; k++)
     for (int j = 1; j < my - 1; j++)
       for (int i = 1; i < mx - 1; i++) {
-        const double r1 = 1.0, r2 = 1.0, r3 = 1.0;
+        double r1 = 1.0, r2 = 1.0, r3 = 1.0;
+        if (g_ls.on) { /* poisson.c:2738-2749 */
+          const double *rho = g_ls.rho;
+          r1 = i == mx - 2 ? rho[IX(d, i, j, k)] : ls_mean(rho[IX(d, i, j, k)], rho[IX(d, i + 1, j, k)]);
+          r2 = j == my - 2 ? rho[IX(d, i, j, k)] : ls_mean(rho[IX(d, i, j, k)], rho[IX(d, i, j + 1, k)]);
+          r3 = k == mz - 2 ? rho[IX(d, i, j, k)] : ls_mean(rho[IX(d, i, j, k)], rho[IX(d, i, j, k + 1)]);
+        }
         double dpdc, dpde, dpdz;
         size_t t = IX(d, i, j, k);
         if (i < mx - 2 || (ip && i == mx - 2)) { /* poisson.c:2791-2834 */
@@ -865,7 +909,7 @@ void or_projection(const or_dims *d, const double *nvert, const double *phi, con
                                 dt * st / coeff / r1;
           }
         }
-        if (j < my - 2 || (jp && j == my - 2)) { /* poisson.c:2837-2883 */
+        if (j < my - 2 || (jp && j == my - 2) || (g_ls.on && g_ls.bc3 == 4 && j == my - 2)) { /* poisson.c:2837-2883 */
           dpdc = 0.; dpdz = 0.;
           if ((i == mx - 2 && !ip) || NV(i + 1, j, k) + NV(i + 1, j + 1, k) > thr) {
             if (NV(i - 1, j, k) + NV(i - 1, j + 1, k) < thr && (i != 1))
@@ -876,7 +920,8 @@ void or_projection(const or_dims *d, const double *nvert, const double *phi, con
           } else {
             dpdc = (PH(i + 1, j, k) + PH(i + 1, j + 1, k) - PH(i - 1, j, k) - PH(i - 1, j + 1, k)) * 0.25;
           }
-          if (j == my - 2 && jp) dpde = PH(i, 1, k) - PH(i, j, k);
+          if (g_ls.on && g_ls.bc3 == 4 && j == my - 2) dpde = PH(i, j, k) - PH(i, j - 1, k);
+          else if (j == my - 2 && jp) dpde = PH(i, 1, k) - PH(i, j, k);
           else dpde = PH(i, j + 1, k) - PH(i, j, k);
           if ((k == mz - 2 && !kp) || NV(i, j, k + 1) + NV(i, j + 1, k + 1) > thr) {
             if (NV(i, j, k - 1) + NV(i, j + 1, k - 1) < thr && (k != 1))
@@ -894,7 +939,7 @@ void or_projection(const or_dims *d, const double *nvert, const double *phi, con
                                 dt * st / coeff / r2;
           }
         }
-        if (k < mz - 2 || (kp && k == mz - 2)) { /* poisson.c:2886-2958 */
+        if (k < mz - 2 || (kp && k == mz - 2) || (g_ls.on && g_ls.bc5 == 4 && k == mz - 2)) { /* poisson.c:2886-2958 */
           dpdc = 0.; dpde = 0.;
           if ((i == mx - 2 && !ip) || NV(i + 1, j, k) + NV(i + 1, j, k + 1) > thr) {
             if (NV(i - 1, j, k) + NV(i - 1, j, k + 1) < thr && (i != 1))
@@ -915,12 +960,18 @@ void or_projection(const or_dims *d, const double *nvert, const double *phi, con
             dpde = (PH(i, j + 1, k) + PH(i, j + 1, k + 1) - PH(i, j - 1, k) - PH(i, j - 1, k + 1)) * 0.25;
           }
           if (k == mz - 2 && kp) dpdz = PH(i, j, 1) - PH(i, j, k);
+          else if (k == mz - 2 && g_ls.on && g_ls.bc5 == 4) dpdz = PH(i, j, k) - PH(i, j, k - 1);
           else dpdz = PH(i, j, k + 1) - PH(i, j, k);
           if ((NV(i, j, k) + NV(i, j, k + 1)) < thr) {
             ucont[t * 3 + 2] -= (dpdc * DOT(kcsi, kzet, i, j, k) * m->kaj[t] +
                                  dpde * DOT(keta, kzet, i, j, k) * m->kaj[t] +
                                  dpdz * DOT(kzet, kzet, i, j, k) * m->kaj[t]) *
                                 dt * st / coeff / r3;
+            if (g_ls.on && k == 1 && g_ls.bc4 == 5000 && g_ls.level[IX(d, i, j, k)] < 0) { /* poisson.c:2951-2956 */
+              const size_t t0 = IX(d, i, j, 0);
+              const double r0 = g_ls.rho[IX(d, i, j, k)];
+              ucont[t0 * 3 + 2] -= (dpdz * DOT(kzet, kzet, i, j, 0) * m->kaj[t0]) * dt * st / coeff / r0;
+            }
           }
         }
       }

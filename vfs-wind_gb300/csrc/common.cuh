@@ -47,6 +47,14 @@ struct Box {
 // ny cells uses ceil(ny / kLineChunk) threads (at most 24, 768 per block).
 constexpr int kLineChunk = 8;
 
+// Level-set context of the operator and the projection (poisson.c
+// levelset branches): density and level-set field at the cells (DA layout
+// of the grid in use), on = levelset, bc3/bc4/bc5 = bctype[3], [4], [5].
+struct LevelSet {
+  const double *rho = nullptr, *level = nullptr;
+  int on = 0, bc3 = 0, bc4 = 0, bc5 = 0;
+};
+
 // Parity-split row layout of the multigrid level operators and line
 // factors: within each (j, k) row the even-i cells come first, then the odd
 // ones, so that the columns of one checkerboard colour ((i + k) parity) are

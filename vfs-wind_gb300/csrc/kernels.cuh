@@ -31,8 +31,9 @@ __global__ void k_vflux_apply(Grid g, const double *nvert, MetricPtrs m, double 
 __global__ void k_periodic_cmpnts(Grid g, const double *src, double *dst);
 __global__ void k_contra2cart(Grid g, const double *nvert, MetricPtrs m, const double *lu, double *ucat);
 __global__ void k_zero_solid(Grid g, const double *nvert, double *ucat);
+__global__ void k_cellfield_restrict(Grid gh, Grid gc, int cx, int cy, int cz, const double *fh, double *fc);
 __global__ void k_assemble(Grid g, Box b, const double *nvert, MetricPtrs m, int scale, int filter, int split, double *A,
-                           uint8_t *rowtype);
+                           uint8_t *rowtype, LevelSet ls);
 __global__ void k_projection_coef(Grid g, Box b, MetricPtrs m, double *pc);
 __global__ void k_level_masks(Grid g, Box b, const double *nvert, uint8_t *blank, double *w64, float *w32,
                               double *aj_box, const double *aj_da);
@@ -50,7 +51,7 @@ __global__ void k_box_to_da(Grid g, Box b, const double *x, double *da);
 __global__ void k_update_pressure(Grid g, const double *nvert, const double *phi, double *p);
 __global__ void k_periodic_copy2(Grid g, double *p, double *phi);
 __global__ void k_projection(Grid g, Box b, const double *nvert, const double *phi, const double *pc, double dt,
-                             double st, double coeff, double *ucont);
+                             double st, double coeff, double *ucont, MetricPtrs m, LevelSet ls);
 __global__ void k_periodic_faces(Grid g, double *ucont);
 __global__ void k_divergence(Grid g, Box b, const double *nvert, const double *ucont, const double *aj,
                              double *partial);

@@ -367,6 +367,7 @@ struct Level {
   int nd = 0;
   int *didx = nullptr;
   double *dinv = nullptr;
+  double *rho = nullptr, *level = nullptr;  // level-set fields of this level (DA layout)
   double *xfinal64 = nullptr;  // where x lives after a V-cycle (set at capture)
   float *xfinal32 = nullptr;
 };
@@ -408,6 +409,9 @@ struct vfs_poisson {
   // next solve (warm_start 2) so that it does not form it again
   double *rprev = nullptr, *rlearn = nullptr, *r0 = nullptr;
   double *ucat = nullptr;  // Contra2Cart output staging (3 per DA point)
+  // level-set variant of the operator and projection (vfs_poisson_set_levelset)
+  double *ls_rho = nullptr, *ls_level = nullptr;
+  int ls_on = 0, ls_bc3 = 0, ls_bc4 = 0, ls_bc5 = 0;
   double r0_norm = 0.;
   bool r0_valid = false;
   std::vector<Level> L;
@@ -583,23 +587,35 @@ int build_coarsest(vfs_poisson *h, Level &l) {
     }
   }
   std::vector<int> comp(nd, -1), queue(nd), first;
+  // a row whose coefficients do not sum to zero (a Dirichlet boundary of
+  // the level-set variant) makes its component regular: no pinned row there
+  std::vector<char> regular_row(nd, 0);
+  for (int r = 0; r < nd; r++) {
+    double sum = 0., dg = std::fabs(M[(size_t)r * nd + r]);
+    for (int q = 0; q < nd; q++) sum += M[(size_t)r * nd + q];
+    regular_row[r] = std::fabs(sum) > 1e-8 * dg;
+  }
   int ncomp = 0;
   for (int r0 = 0; r0 < nd; r0++) {
     if (comp[r0] >= 0) continue;
     int hd = 0, tl = 0;
     queue[tl++] = r0;
     comp[r0] = ncomp;
+    bool regular = false;
     while (hd < tl) {
       int r = queue[hd++];
+      regular = regular || regular_row[r];
       for (int q = 0; q < nd; q++)
         if (comp[q] < 0 && (M[(size_t)r * nd + q] != 0. || M[(size_t)q * nd + r] != 0.)) {
           comp[q] = ncomp;
           queue[tl++] = q;
         }
     }
-    for (int q = 0; q < nd; q++) M[(size_t)r0 * nd + q] = 0.;
-    M[(size_t)r0 * nd + r0] = 1.;
-    first.push_back(r0);
+    if (!regular) {
+      for (int q = 0; q < nd; q++) M[(size_t)r0 * nd + q] = 0.;
+      M[(size_t)r0 * nd + r0] = 1.;
+      first.push_back(r0);
+    }
     ncomp++;
   }
   for (int r = 0; r < nd; r++) I[(size_t)r * nd + r] = 1.;
@@ -638,7 +654,7 @@ int build_coarsest(vfs_poisson *h, Level &l) {
 }
 
 void free_level(vfs_poisson *h, Level &l, bool level0) {
-  if (!level0) { dfree(h, l.coor); dfree(h, l.nvert); }
+  if (!level0) { dfree(h, l.coor); dfree(h, l.nvert); dfree(h, l.rho); dfree(h, l.level); }
   if (l.own_met) free_metrics(h, l.met);
   dfree(h, l.A64); dfree(h, l.A32); dfree(h, l.rowtype); dfree(h, l.blank);
   dfree(h, l.inv64); dfree(h, l.cp64); dfree(h, l.w64); dfree(h, l.inv32); dfree(h, l.cp32); dfree(h, l.w32);
@@ -655,6 +671,19 @@ void drop_graphs(vfs_poisson *h) {
   }
 }
 
+LevelSet level_set(const vfs_poisson *h, const Level &l) {
+  LevelSet ls;
+  if (h->ls_on) {
+    ls.rho = l.rho;
+    ls.level = l.level;
+    ls.on = 1;
+    ls.bc3 = h->ls_bc3;
+    ls.bc4 = h->ls_bc4;
+    ls.bc5 = h->ls_bc5;
+  }
+  return ls;
+}
+
 // Operator, masks and line factors of one level (assembled from its metrics).
 int build_level_operator(vfs_poisson *h, Level &l) {
   const size_t n = l.b.n();
@@ -667,7 +696,7 @@ int build_level_operator(vfs_poisson *h, Level &l) {
   TRY(dalloc(h, &l.inv64, n)); TRY(dalloc(h, &l.cp64, n));
   TRY(dalloc(h, &l.inv32, n)); TRY(dalloc(h, &l.cp32, n));
   for (int q = 0; q < 4; q++) { TRY(dalloc(h, &l.v64[q], n)); TRY(dalloc(h, &l.v32[q], n)); }
-  LAUNCH(h, k_assemble, box_grid(l.b), 128, l.g, l.b, l.nvert, l.met, 1, 0, 1, l.A64, l.rowtype);
+  LAUNCH(h, k_assemble, box_grid(l.b), 128, l.g, l.b, l.nvert, l.met, 1, 0, 1, l.A64, l.rowtype, level_set(h, l));
   LAUNCH(h, k_level_masks, lin_grid(n), 256, l.g, l.b, l.nvert, l.blank, l.w64, l.w32, (double *)nullptr,
          (const double *)nullptr);
   LAUNCH(h, k_line_lu_f64, dim3((l.b.nx + 127) / 128, l.b.nz), 128, l.b, l.A64, l.inv64, l.cp64);
@@ -686,6 +715,8 @@ int build_hierarchy(vfs_poisson *h, int coarsest_max) {
   l0.coor = h->coor;
   l0.nvert = h->nvert;
   l0.met = h->met;
+  l0.rho = h->ls_rho;
+  l0.level = h->ls_level;
   h->L.push_back(l0);
   double *H;
   TRY(dalloc(h, &H, 3));
@@ -714,6 +745,12 @@ int build_hierarchy(vfs_poisson *h, int coarsest_max) {
     LAUNCH(h, k_coarse_nodes, da_grid(q.g), 128, f.g, q.g, c[0], c[1], c[2], f.coor, q.coor);
     LAUNCH(h, k_nvert_restrict, da_grid(q.g), 128, f.g, q.g, c[0], c[1], c[2], f.nvert, tmp);
     LAUNCH(h, k_nvert_fill, da_grid(q.g), 128, q.g, tmp, q.nvert);
+    if (h->ls_on) {  // level-set fields of the coarse level: child averages
+      TRY(dalloc(h, &q.rho, q.g.n()));
+      TRY(dalloc(h, &q.level, q.g.n()));
+      LAUNCH(h, k_cellfield_restrict, da_grid(q.g), 128, f.g, q.g, c[0], c[1], c[2], f.rho, q.rho);
+      LAUNCH(h, k_cellfield_restrict, da_grid(q.g), 128, f.g, q.g, c[0], c[1], c[2], f.level, q.level);
+    }
     TRY(sync(h));
     dfree(h, tmp);
     h->L.push_back(q);
@@ -1263,7 +1300,12 @@ int vfs_poisson_set_nvert(vfs_poisson *h, const double *nvert) {
   LAUNCH(h, k_gid_da, da_grid(h->g), 128, h->g, h->box, h->gid_box, h->gid_da);
   LAUNCH(h, k_fluid_mask, lin_grid(n), 256, h->g, h->box, h->nvert, h->fluid);
   // PoissonLHSNew: unscaled operator with the reference's insertion filter
-  LAUNCH(h, k_assemble, box_grid(h->box), 128, h->g, h->box, h->nvert, h->met, 0, 1, 0, h->A0, h->rowtype0);
+  LevelSet fls;
+  if (h->ls_on) {
+    fls.rho = h->ls_rho; fls.level = h->ls_level; fls.on = 1;
+    fls.bc3 = h->ls_bc3; fls.bc4 = h->ls_bc4; fls.bc5 = h->ls_bc5;
+  }
+  LAUNCH(h, k_assemble, box_grid(h->box), 128, h->g, h->box, h->nvert, h->met, 0, 1, 0, h->A0, h->rowtype0, fls);
   uint8_t *blank;
   double *w64;
   float *w32;
@@ -1296,13 +1338,40 @@ int vfs_poisson_rhs(vfs_poisson *h, const double *ucont, double dt, double st, d
   const size_t N = h->g.n();
   TRY(upload(h, h->ucont, ucont, 3 * N));
   LAUNCH(h, k_rhs, kRedBlocks, 256, h->g, h->box, h->nvert, h->ucont, h->met.aj, dt, st, coeff, h->b, h->partial);
-  if (h->desc.bctype3 != -10) {  // Remove_Nullspace_Scale
+  // Remove_Nullspace_Scale, skipped for bctype[3] == -10 and for a level
+  // set with the Dirichlet top bctype[5] == 4 (poisson_hypre.c:120, :375)
+  if (h->desc.bctype3 != -10 && !(h->ls_on && h->ls_bc5 == 4)) {
     LAUNCH(h, k_reduce_rows, 2, 1024, h->partial, kRedBlocks, 2, h->red);
     LAUNCH(h, k_rhs_nullspace, kRedBlocks, 256, h->g, h->box, h->nvert, h->met.aj, h->red, h->b);
   }
   TRY(sync(h));
   h->have_rhs = true;
   h->r0_valid = false;
+  return VFS_OK;
+}
+
+int vfs_poisson_set_levelset(vfs_poisson *h, const double *rho, const double *level, const int *bctype, int enable) {
+  if (!h) return fail(VFS_EINVAL, "null handle");
+  if (!enable) {
+    h->ls_on = 0;
+    return VFS_OK;
+  }
+  if (!rho || !bctype) return fail(VFS_EINVAL, "density and bctype are required");
+  const size_t N = h->g.n();
+  if (!h->ls_rho) {
+    TRY(dalloc(h, &h->ls_rho, N));
+    TRY(dalloc(h, &h->ls_level, N));
+  }
+  TRY(upload(h, h->ls_rho, rho, N));
+  if (level) TRY(upload(h, h->ls_level, level, N));
+  else CUDA_TRY(cudaMemsetAsync(h->ls_level, 0, N * 8, h->stream));
+  h->ls_on = 1;
+  h->ls_bc3 = bctype[3];
+  h->ls_bc4 = bctype[4];
+  h->ls_bc5 = bctype[5];
+  TRY(sync(h));
+  h->have_nvert = false;  // the operator has to be assembled again
+  h->have_rhs = false;
   return VFS_OK;
 }
 
@@ -1382,7 +1451,7 @@ int vfs_poisson_solve(vfs_poisson *h, double *phi, const vfs_solve_opts *opts, v
     CUDA_TRY(cudaMemsetAsync(h->x, 0, n * 8, h->stream));
   }
   TRY(fgmres(h, o, &st));
-  if (h->desc.bctype3 != -10) {  // Remove_Nullspace of phi
+  if (h->desc.bctype3 != -10 && !(h->ls_on && h->ls_bc5 == 4)) {  // Remove_Nullspace of phi (:604-608)
     LAUNCH(h, k_mean_partial, kRedBlocks, 256, h->box, h->fluid, h->x, h->partial);
     LAUNCH(h, k_reduce_rows, 2, 1024, h->partial, kRedBlocks, 2, h->red);
     LAUNCH(h, k_shift_fluid, kRedBlocks, 256, h->box, h->fluid, h->red, h->x);
@@ -1641,7 +1710,13 @@ int vfs_poisson_projection(vfs_poisson *h, double *ucont, double dt, double st, 
   if (!(coeff != 0.)) return fail(VFS_EINVAL, "coeff must be non-zero");
   const size_t N = h->g.n();
   TRY(upload(h, h->ucont, ucont, 3 * N));
-  LAUNCH(h, k_projection, box_grid(h->box), 128, h->g, h->box, h->nvert, h->phi_da, h->pc, dt, st, coeff, h->ucont);
+  LevelSet pls;
+  if (h->ls_on) {
+    pls.rho = h->ls_rho; pls.level = h->ls_level; pls.on = 1;
+    pls.bc3 = h->ls_bc3; pls.bc4 = h->ls_bc4; pls.bc5 = h->ls_bc5;
+  }
+  LAUNCH(h, k_projection, box_grid(h->box), 128, h->g, h->box, h->nvert, h->phi_da, h->pc, dt, st, coeff, h->ucont,
+         h->met, pls);
   LAUNCH(h, k_periodic_faces, da_grid(h->g), 128, h->g, h->ucont);
   TRY(download(h, ucont, h->ucont, 3 * N));
   return sync(h);

@@ -289,16 +289,24 @@ __device__ inline double gface(const Grid &g, const MetricPtrs &m, int q, int i,
   return (X[s * 3] * Y[s * 3] + X[s * 3 + 1] * Y[s * 3 + 1] + X[s * 3 + 2] * Y[s * 3 + 2]) * AJ[s];
 }
 
+// mean (Source/level.c:2276-2280): the harmonic mean of two densities
+__device__ inline double ls_mean(double A, double B) { return 2.0 * A * B / (A + B); }
+
 // One row of the operator, accumulated in the reference's statement order.
+// With a level set (ls.on) every face coefficient is divided by the face
+// density and the Dirichlet top / bottom rows of poisson.c:1295-1554 apply.
 __device__ void assemble_row(const Grid &g, const double *nvert, const MetricPtrs &m, int i, int j, int k,
-                             double v[NSLOT]) {
+                             double v[NSLOT], const LevelSet &ls) {
   const int mx = g.mx, my = g.my, mz = g.mz;
   const bool ip = g.px, jp = g.py, kp = g.pz;
-  const double thr = kThr, r = 1.0;
+  const double thr = kThr;
+  double r = 1.0;
+#define RHO(a, b, c) ls.rho[g.at(a, b, c)]
 #define NV(a, b, c) nvert[g.at(a, b, c)]
 #define G(q, a, b, c) gface(g, m, q, a, b, c)
   for (int s = 0; s < NSLOT; s++) v[s] = 0.;
   if (NV(i + 1, j, k) < thr && (i != mx - 2 || ip)) {  // poisson.c:1167-1230
+    r = ls.on ? ls_mean(RHO(i + 1, j, k), RHO(i, j, k)) : 1.0;
     double g0 = G(0, i, j, k), g1 = G(1, i, j, k), g2 = G(2, i, j, k);
     v[CP] -= g0 / r; v[EP] += g0 / r;
     if ((j == my - 2 && !jp) || NV(i, j + 1, k) + NV(i + 1, j + 1, k) > thr) {
@@ -325,6 +333,7 @@ __device__ void assemble_row(const Grid &g, const double *nvert, const MetricPtr
     }
   }
   if (NV(i - 1, j, k) < thr && (i != 1 || ip)) {  // poisson.c:1233-1293
+    r = ls.on ? ls_mean(RHO(i - 1, j, k), RHO(i, j, k)) : 1.0;
     double g0 = G(0, i - 1, j, k), g1 = G(1, i - 1, j, k), g2 = G(2, i - 1, j, k);
     v[CP] -= g0 / r; v[WP] += g0 / r;
     if ((j == my - 2 && !jp) || NV(i, j + 1, k) + NV(i - 1, j + 1, k) > thr) {
@@ -350,7 +359,8 @@ __device__ void assemble_row(const Grid &g, const double *nvert, const MetricPtr
       v[TP] -= g2 * 0.25 / r; v[TW] -= g2 * 0.25 / r; v[BP] += g2 * 0.25 / r; v[BW] += g2 * 0.25 / r;
     }
   }
-  if (NV(i, j + 1, k) < thr && (j != my - 2 || jp)) {  // poisson.c:1296-1361
+  if (NV(i, j + 1, k) < thr && (j != my - 2 || jp || (ls.on && ls.bc3 == 4 && j == my - 2))) {  // poisson.c:1296-1361
+    r = ls.on ? ls_mean(RHO(i, j + 1, k), RHO(i, j, k)) : 1.0;
     double g3 = G(3, i, j, k), g4 = G(4, i, j, k), g5 = G(5, i, j, k);
     if ((i == mx - 2 && !ip) || NV(i + 1, j, k) + NV(i + 1, j + 1, k) > thr) {
       if (NV(i - 1, j, k) + NV(i - 1, j + 1, k) < thr && i != 1) {
@@ -363,7 +373,8 @@ __device__ void assemble_row(const Grid &g, const double *nvert, const MetricPtr
     } else {
       v[EP] += g3 * 0.25 / r; v[NE] += g3 * 0.25 / r; v[WP] -= g3 * 0.25 / r; v[NW] -= g3 * 0.25 / r;
     }
-    v[CP] -= g4 / r; v[NP] += g4 / r;
+    if (ls.on && ls.bc3 == 4 && j == my - 2) v[CP] -= g4 / 0.5 / r;  // zero Dirichlet pressure, :1328
+    else { v[CP] -= g4 / r; v[NP] += g4 / r; }
     if ((k == mz - 2 && !kp) || NV(i, j, k + 1) + NV(i, j + 1, k + 1) > thr) {
       if (NV(i, j, k - 1) + NV(i, j + 1, k - 1) < thr && k != 1) {
         v[CP] += g5 * 0.5 / r; v[NP] += g5 * 0.5 / r; v[BP] -= g5 * 0.5 / r; v[BN] -= g5 * 0.5 / r;
@@ -377,6 +388,7 @@ __device__ void assemble_row(const Grid &g, const double *nvert, const MetricPtr
     }
   }
   if (NV(i, j - 1, k) < thr && (j != 1 || jp)) {  // poisson.c:1364-1422
+    r = ls.on ? ls_mean(RHO(i, j - 1, k), RHO(i, j, k)) : 1.0;
     double g3 = G(3, i, j - 1, k), g4 = G(4, i, j - 1, k), g5 = G(5, i, j - 1, k);
     if ((i == mx - 2 && !ip) || NV(i + 1, j, k) + NV(i + 1, j - 1, k) > thr) {
       if (NV(i - 1, j, k) + NV(i - 1, j - 1, k) < thr && i != 1) {
@@ -402,7 +414,8 @@ __device__ void assemble_row(const Grid &g, const double *nvert, const MetricPtr
       v[TP] -= g5 * 0.25 / r; v[TS] -= g5 * 0.25 / r; v[BP] += g5 * 0.25 / r; v[BS] += g5 * 0.25 / r;
     }
   }
-  if (NV(i, j, k + 1) < thr && (k != mz - 2 || kp)) {  // poisson.c:1425-1491
+  if (NV(i, j, k + 1) < thr && (k != mz - 2 || kp || (ls.on && ls.bc5 == 4 && k == mz - 2))) {  // poisson.c:1425-1491
+    r = ls.on ? ls_mean(RHO(i, j, k + 1), RHO(i, j, k)) : 1.0;
     double g6 = G(6, i, j, k), g7 = G(7, i, j, k), g8 = G(8, i, j, k);
     if ((i == mx - 2 && !ip) || NV(i + 1, j, k) + NV(i + 1, j, k + 1) > thr) {
       if (NV(i - 1, j, k) + NV(i - 1, j, k + 1) < thr && i != 1) {
@@ -426,9 +439,12 @@ __device__ void assemble_row(const Grid &g, const double *nvert, const MetricPtr
     } else {
       v[NP] += g7 * 0.25 / r; v[TN] += g7 * 0.25 / r; v[SP] -= g7 * 0.25 / r; v[TS] -= g7 * 0.25 / r;
     }
-    v[CP] -= g8 / r; v[TP] += g8 / r;
+    if (ls.on && ls.bc5 == 4 && k == mz - 2) v[CP] -= g8 / 0.5 / r;  // :1482-1484
+    else { v[CP] -= g8 / r; v[TP] += g8 / r; }
   }
-  if (NV(i, j, k - 1) < thr && (k != 1 || kp)) {  // poisson.c:1494-1561
+  if (NV(i, j, k - 1) < thr &&
+      (k != 1 || kp || (ls.on && ls.bc4 == 5000 && k == 1 && ls.level[g.at(i, j, k)] < 0))) {  // poisson.c:1494-1561
+    r = ls.on ? (k == 1 ? RHO(i, j, k) : ls_mean(RHO(i, j, k - 1), RHO(i, j, k))) : 1.0;
     double g6 = G(6, i, j, k - 1), g7 = G(7, i, j, k - 1), g8 = G(8, i, j, k - 1);
     if ((i == mx - 2 && !ip) || NV(i + 1, j, k) + NV(i + 1, j, k - 1) > thr) {
       if (NV(i - 1, j, k) + NV(i - 1, j, k - 1) < thr && i != 1) {
@@ -452,8 +468,10 @@ __device__ void assemble_row(const Grid &g, const double *nvert, const MetricPtr
     } else {
       v[NP] -= g7 * 0.25 / r; v[BN] -= g7 * 0.25 / r; v[SP] += g7 * 0.25 / r; v[BS] += g7 * 0.25 / r;
     }
-    v[CP] -= g8 / r; v[BP] += g8 / r;
+    if (ls.on && ls.bc4 == 5 && k == 1) v[CP] -= g8 / 0.5 / r;  // :1552-1554
+    else { v[CP] -= g8 / r; v[BP] += g8 / r; }
   }
+#undef RHO
 #undef NV
 #undef G
 }
@@ -465,7 +483,7 @@ __device__ void assemble_row(const Grid &g, const double *nvert, const MetricPtr
 // multigrid levels (rowtype stays natural).  Slots whose column has no dof
 // are zero (idx < 0).
 __global__ void k_assemble(Grid g, Box b, const double *__restrict__ nvert, MetricPtrs m, int scale,
-                           int filter, int split, double *A, uint8_t *rowtype) {
+                           int filter, int split, double *A, uint8_t *rowtype, LevelSet ls) {
   int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y, k = blockIdx.z;
   if (i >= b.nx) return;
   const size_t n = b.n(), c = split ? b.at(split_pos(i, b.nx), j, k) : b.at(i, j, k);
@@ -484,7 +502,7 @@ __global__ void k_assemble(Grid g, Box b, const double *__restrict__ nvert, Metr
     return;
   }
   double v[NSLOT];
-  assemble_row(g, nvert, m, I, J, K, v);
+  assemble_row(g, nvert, m, I, J, K, v, ls);
   if (scale) {
     double a = m.aj[t];
     for (int s = 0; s < NSLOT; s++) v[s] *= a;
@@ -716,14 +734,22 @@ __global__ void k_periodic_copy2(Grid g, double *p, double *phi) {
 
 // Projection (Source/poisson.c:2700-3066), level set off.
 __global__ void k_projection(Grid g, Box b, const double *__restrict__ nvert, const double *__restrict__ phi,
-                             const double *__restrict__ pc, double dt, double st, double coeff, double *ucont) {
+                             const double *__restrict__ pc, double dt, double st, double coeff, double *ucont,
+                             MetricPtrs m, LevelSet ls) {
   int ii = blockIdx.x * blockDim.x + threadIdx.x, jj = blockIdx.y, kk = blockIdx.z;
   if (ii >= b.nx) return;
   const int i = ii + 1, j = jj + 1, k = kk + 1;
   const int mx = g.mx, my = g.my, mz = g.mz;
   const bool ip = g.px, jp = g.py, kp = g.pz;
-  const double thr = kThr, r1 = 1.0, r2 = 1.0, r3 = 1.0;
+  const double thr = kThr;
   const size_t t = g.at(i, j, k), c = b.at(ii, jj, kk), n = b.n();
+  double r1 = 1.0, r2 = 1.0, r3 = 1.0;
+  if (ls.on) {  // poisson.c:2738-2749
+    const double *rho = ls.rho;
+    r1 = i == mx - 2 ? rho[t] : ls_mean(rho[t], rho[g.at(i + 1, j, k)]);
+    r2 = j == my - 2 ? rho[t] : ls_mean(rho[t], rho[g.at(i, j + 1, k)]);
+    r3 = k == mz - 2 ? rho[t] : ls_mean(rho[t], rho[g.at(i, j, k + 1)]);
+  }
 #define NV(a, bb, cc) nvert[g.at(a, bb, cc)]
 #define PH(a, bb, cc) phi[g.at(a, bb, cc)]
   double dpdc, dpde, dpdz;
@@ -755,7 +781,7 @@ __global__ void k_projection(Grid g, Box b, const double *__restrict__ nvert, co
                           dt * st / coeff / r1;
     }
   }
-  if (j < my - 2 || (jp && j == my - 2)) {
+  if (j < my - 2 || (jp && j == my - 2) || (ls.on && ls.bc3 == 4 && j == my - 2)) {
     dpdc = 0.; dpdz = 0.;
     if ((i == mx - 2 && !ip) || NV(i + 1, j, k) + NV(i + 1, j + 1, k) > thr) {
       if (NV(i - 1, j, k) + NV(i - 1, j + 1, k) < thr && (i != 1))
@@ -766,7 +792,8 @@ __global__ void k_projection(Grid g, Box b, const double *__restrict__ nvert, co
     } else {
       dpdc = (PH(i + 1, j, k) + PH(i + 1, j + 1, k) - PH(i - 1, j, k) - PH(i - 1, j + 1, k)) * 0.25;
     }
-    if (j == my - 2 && jp) dpde = PH(i, 1, k) - PH(i, j, k);
+    if (ls.on && ls.bc3 == 4 && j == my - 2) dpde = PH(i, j, k) - PH(i, j - 1, k);
+    else if (j == my - 2 && jp) dpde = PH(i, 1, k) - PH(i, j, k);
     else dpde = PH(i, j + 1, k) - PH(i, j, k);
     if ((k == mz - 2 && !kp) || NV(i, j, k + 1) + NV(i, j + 1, k + 1) > thr) {
       if (NV(i, j, k - 1) + NV(i, j + 1, k - 1) < thr && (k != 1))
@@ -783,7 +810,7 @@ __global__ void k_projection(Grid g, Box b, const double *__restrict__ nvert, co
                           dt * st / coeff / r2;
     }
   }
-  if (k < mz - 2 || (kp && k == mz - 2)) {
+  if (k < mz - 2 || (kp && k == mz - 2) || (ls.on && ls.bc5 == 4 && k == mz - 2)) {
     dpdc = 0.; dpde = 0.;
     if ((i == mx - 2 && !ip) || NV(i + 1, j, k) + NV(i + 1, j, k + 1) > thr) {
       if (NV(i - 1, j, k) + NV(i - 1, j, k + 1) < thr && (i != 1))
@@ -804,11 +831,18 @@ __global__ void k_projection(Grid g, Box b, const double *__restrict__ nvert, co
       dpde = (PH(i, j + 1, k) + PH(i, j + 1, k + 1) - PH(i, j - 1, k) - PH(i, j - 1, k + 1)) * 0.25;
     }
     if (k == mz - 2 && kp) dpdz = PH(i, j, 1) - PH(i, j, k);
+    else if (k == mz - 2 && ls.on && ls.bc5 == 4) dpdz = PH(i, j, k) - PH(i, j, k - 1);
     else dpdz = PH(i, j, k + 1) - PH(i, j, k);
     if ((NV(i, j, k) + NV(i, j, k + 1)) < thr) {
       const double aj = pc[11 * n + c];
       ucont[t * 3 + 2] -= (dpdc * pc[8 * n + c] * aj + dpde * pc[9 * n + c] * aj + dpdz * pc[10 * n + c] * aj) *
                           dt * st / coeff / r3;
+      if (ls.on && k == 1 && ls.bc4 == 5000 && ls.level[t] < 0) {  // poisson.c:2951-2956
+        const size_t t0 = g.at(i, j, 0);
+        const double *kz = &m.kzet[t0 * 3];
+        const double r0 = ls.rho[t];
+        ucont[t0 * 3 + 2] -= (dpdz * (kz[0] * kz[0] + kz[1] * kz[1] + kz[2] * kz[2]) * m.kaj[t0]) * dt * st / coeff / r0;
+      }
     }
   }
 #undef NV
@@ -1104,6 +1138,32 @@ __global__ void k_zero_solid(Grid g, const double *nvert, double *ucat) {
   const size_t n = g.n();
   for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x)
     if ((int)(nvert[t] + 0.1) == 3) ucat[t * 3] = ucat[t * 3 + 1] = ucat[t * 3 + 2] = 0.;
+}
+
+}  // namespace vfs
+
+namespace vfs {
+
+// A cell field (density, level set) on a coarse level: the average of the
+// fine cells it covers (the children of MyNvertRestriction's mapping); a
+// boundary-layer point takes the fine boundary-layer values it faces.
+__global__ void k_cellfield_restrict(Grid gh, Grid gc, int cx, int cy, int cz, const double *fh, double *fc) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y, k = blockIdx.z;
+  if (i >= gc.mx) return;
+  int ia[2], ja[2], ka[2];
+  auto kids = [](int c, int m, int mh, int coarsened, int o[2]) {
+    if (c == 0) { o[0] = o[1] = 0; return; }
+    if (c == m - 1) { o[0] = o[1] = mh - 1; return; }
+    const int h = coarsened ? 2 * c : c;
+    o[0] = h;
+    o[1] = h - coarsened;
+  };
+  kids(i, gc.mx, gh.mx, cx, ia);
+  kids(j, gc.my, gh.my, cy, ja);
+  kids(k, gc.mz, gh.mz, cz, ka);
+  double s = 0.;
+  for (int q = 0; q < 8; q++) s += fh[gh.at(ia[q & 1], ja[(q >> 1) & 1], ka[q >> 2])];
+  fc[gc.at(i, j, k)] = 0.125 * s;
 }
 
 }  // namespace vfs

@@ -38,7 +38,7 @@ EXPORTS = [
     "vfs_unet_set_params", "vfs_unet_forward", "vfs_unet_gradient", "vfs_unet_train_step", "vfs_unet_adam",
     "vfs_unet_set_grads", "vfs_unet_kernel_launches", "vfs_poisson_learned_guess", "vfs_poisson_guess_sample",
     "vfs_poisson_get_operator32", "vfs_poisson_rhs2", "vfs_poisson_volume_flux", "vfs_poisson_contra2cart",
-    "vfs_read_petsc_vec", "vfs_write_petsc_vec", "vfs_read_grid", "vfs_read_ucd",
+    "vfs_read_petsc_vec", "vfs_write_petsc_vec", "vfs_read_grid", "vfs_read_ucd", "vfs_poisson_set_levelset",
 ]
 
 
@@ -139,6 +139,7 @@ def load(path=LIB_PATH):
     L.vfs_poisson_rhs2.argtypes = [vp, dp, C.c_double, C.c_double, C.c_double, C.c_int]
     L.vfs_poisson_volume_flux.argtypes = [vp, dp, C.c_int, C.c_double, P(C.c_double), P(C.c_double)]
     L.vfs_poisson_contra2cart.argtypes = [vp, dp, dp, C.c_int]
+    L.vfs_poisson_set_levelset.argtypes = [vp, dp, dp, vp, C.c_int]
     L.vfs_read_petsc_vec.argtypes = [C.c_char_p, P(C.c_int64), vp]
     L.vfs_write_petsc_vec.argtypes = [C.c_char_p, C.c_int64, vp]
     L.vfs_read_grid.argtypes = [C.c_char_p, C.c_int, C.c_int, C.c_double, C.c_double, vp, vp]
@@ -219,6 +220,12 @@ class PoissonSolver:
             fm = C.cast(arr, C.c_void_p)
             self._fm_keep = (arr, face_metrics)
         _check(load().vfs_poisson_set_grid(self.h, _ptr(coor), fm))
+
+    def set_levelset(self, rho, level=None, bctype=(0, 0, 0, 0, 0, 0), enable=True):
+        """Level-set (two-phase) operator: densities rho, level-set field and
+        the six bctype codes; call before set_nvert."""
+        bc = np.ascontiguousarray(bctype, np.int32)
+        _check(load().vfs_poisson_set_levelset(self.h, _ptr(rho), _ptr(level), _ptr(bc), int(enable)))
 
     def set_nvert(self, nvert):
         _check(load().vfs_poisson_set_nvert(self.h, _ptr(nvert)))

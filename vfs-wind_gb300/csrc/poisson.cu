@@ -836,8 +836,9 @@ void prof_end(vfs_poisson *h, int li) {
 template <typename T>
 void smooth(vfs_poisson *h, Level &l, int li, int smoother, bool zero_guess, T omega, T *&x, T *&t, T *bb, T *r) {
   const int P = (l.b.ny + kLineChunk - 1) / kLineChunk;
-  dim3 lb(32, P), lg((l.b.nx + 31) / 32, l.b.nz);
-  const size_t lsm = 2 * 32 * P * sizeof(T);
+  constexpr int TI = 16;  // columns per block of the line kernels (k_line_tri: 384 threads at most)
+  dim3 lb(TI, P), lg((l.b.nx + TI - 1) / TI, l.b.nz);
+  const size_t lsm = 2 * TI * P * sizeof(T);
   T *Asp = Prec<T>::A(l) + (size_t)SP * l.b.n();
   prof_begin<T>(h, li, zero_guess, smoother);
   if (smoother == 0) {
@@ -861,7 +862,7 @@ void smooth(vfs_poisson *h, Level &l, int li, int smoother, bool zero_guess, T o
     // residuals go to split positions (r of the natural rhs when x = 0)
     if (zero_guess) cudaMemsetAsync(x, 0, l.b.n() * sizeof(T), h->stream);
     const int nh = (l.b.nx + 1) / 2;
-    dim3 cg((nh + 31) / 32, l.b.nz), rg((nh + 127) / 128, l.b.ny, l.b.nz);
+    dim3 cg((nh + TI - 1) / TI, l.b.nz), rg((nh + 127) / 128, l.b.ny, l.b.nz);
     for (int color = 0; color < 2; color++) {
       const bool skip_res = zero_guess && color == 0;
       if (!skip_res) LAUNCH(h, Prec<T>::residual, rg, 128, l.b, Prec<T>::A(l), x, bb, r, 2 + color);

@@ -269,19 +269,27 @@ __device__ __forceinline__ void line_tri_body(Box b, const T *__restrict__ r, co
   const uint32_t cS = valid ? (uint32_t)b.at(pp, 0, k) : 0u;                     // operator / factor index
   const uint32_t cX = valid ? (uint32_t)b.at(split_cell(pp, b.nx), 0, k) : 0u;  // natural index
   const uint32_t cR = (color == 2 || color == 3) ? cS : cX;
-  T y[M], g[M];
+  // every load of the chunk up front (one memory round trip): the line
+  // coefficients, factors, residual and the x being corrected
+  T y[M], g[M], av[M], ivv[M], cv[M], xv[M];
+#pragma unroll
+  for (int q = 0; q < M; q++) {
+    const int j = j0 + q;
+    const uint32_t o = (uint32_t)j * sj;
+    const bool in = q < cnt;
+    av[q] = in && j > 0 ? __ldcs(&Asp[cS + o]) : (T)0;
+    ivv[q] = in ? __ldcs(&inv[cS + o]) : (T)0;
+    cv[q] = in && j < ny - 1 ? __ldcs(&cp[cS + o]) : (T)0;
+    y[q] = in ? __ldcs(&r[cR + o]) : (T)0;
+    xv[q] = in && !zero_guess ? x[cX + o] : (T)0;
+  }
   T yp = (T)0, gp = (T)1;
 #pragma unroll
   for (int q = 0; q < M; q++) {
-    y[q] = (T)0;
     g[q] = (T)0;
     if (q < cnt) {
-      const int j = j0 + q;
-      const uint32_t o = (uint32_t)j * sj;
-      const T a = j > 0 ? __ldcs(&Asp[cS + o]) : (T)0;
-      const T iv = __ldcs(&inv[cS + o]);
-      const T v = (__ldcs(&r[cR + o]) - a * yp) * iv;
-      gp = gp * (-a * iv);
+      const T v = (y[q] - av[q] * yp) * ivv[q];
+      gp = gp * (-av[q] * ivv[q]);
       y[q] = v;
       g[q] = gp;
       yp = v;
@@ -307,10 +315,8 @@ __device__ __forceinline__ void line_tri_body(Box b, const T *__restrict__ r, co
 #pragma unroll
   for (int q = M - 1; q >= 0; q--) {
     if (q < cnt) {
-      const int j = j0 + q;
-      const T cv = j < ny - 1 ? __ldcs(&cp[cS + (uint32_t)j * sj]) : (T)0;
-      const T v = y[q] - cv * xn;
-      hp = hp * (-cv);
+      const T v = y[q] - cv[q] * xn;
+      hp = hp * (-cv[q]);
       y[q] = v;
       g[q] = hp;
       xn = v;
@@ -334,7 +340,7 @@ __device__ __forceinline__ void line_tri_body(Box b, const T *__restrict__ r, co
     if (q < cnt) {
       const uint32_t c = cX + (uint32_t)(j0 + q) * sj;
       const T d = y[q] + g[q] * xin;
-      x[c] = (zero_guess ? (T)0 : x[c]) + omega * d;
+      x[c] = xv[q] + omega * d;
     }
   }
 }
@@ -477,7 +483,7 @@ __global__ void k_sumsq(size_t n, const double *__restrict__ x, double *partial)
   if (threadIdx.x == 0) partial[blockIdx.x] = s;
 }
 
-#define TYPED(T, S)                                                                                        \
+#define TYPED(T, S, TRI_THREADS)                                                                           \
   __global__ void __launch_bounds__(256) k_residual_##S(Box b, const T *A, const T *x, const T *rhs, T *r,  \
                                                         int color) {                                       \
     residual_body<T>(b, A, x, rhs, r, color);                                                              \
@@ -487,7 +493,7 @@ __global__ void k_sumsq(size_t n, const double *__restrict__ x, double *partial)
                                                            const T *x, const T *rhs, T *xo, T omega, int zg) { \
     line_sweep_body<T, kLineChunk>(b, A, inv, cp, x, rhs, xo, omega, zg);                                   \
   }                                                                                                        \
-  __global__ void __launch_bounds__(768) k_line_tri_##S(Box b, const T *r, const T *Asp, const T *inv,          \
+  __global__ void __launch_bounds__(TRI_THREADS) k_line_tri_##S(Box b, const T *r, const T *Asp, const T *inv,  \
                                                        const T *cp, T *x, T omega, int zg, int color) {        \
     line_tri_body<T, kLineChunk>(b, r, Asp, inv, cp, x, omega, zg, color);                                    \
   }                                                                                                        \
@@ -495,8 +501,10 @@ __global__ void k_sumsq(size_t n, const double *__restrict__ x, double *partial)
     coarsest_body<T>(nd, didx, dinv, rhs, x, n);                                                           \
   }                                                                                                        \
   __global__ void k_cast_planes_##S(const double *src, T *dst, size_t n) { cast_body<T>(src, dst, n); }
-TYPED(float, f32)
-TYPED(double, f64)
+// the line kernel keeps a whole chunk in registers: 16 columns per block
+// (at most 24 chunks each) so that neither precision spills
+TYPED(float, f32, 384)
+TYPED(double, f64, 384)
 #undef TYPED
 
 }  // namespace vfs

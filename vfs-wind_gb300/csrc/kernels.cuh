@@ -1,5 +1,7 @@
 // kernels.cuh -- kernel declarations shared by the host orchestration.
 #pragma once
+#include <cuda_fp16.h>
+
 #include "common.cuh"
 
 namespace vfs {
@@ -82,14 +84,35 @@ TYPED_DECL(float, f32)
 TYPED_DECL(double, f64)
 #undef TYPED_DECL
 
+__global__ void k_pack16(size_t n, const double *A, __half2 *C, float *D);
+__global__ void k_residual16(Box b, const __half2 *C, const float *D, const float *x, const float *rhs, float *r,
+                             int color);
 __global__ void k_apply64(Box b, const double *A, const double *x, double *y);
 __global__ void k_residual64(Box b, const double *A, const double *x, const double *rhs, double *r, double *partial);
-__global__ void k_dots(size_t n, int nv, const double *const *V, const double *w, double *partial);
-__global__ void k_gs_update(size_t n, int nv, const double *const *V, const double *coef, double *w,
+// Gram-Schmidt rows of the reduced values (solve.cu): Q.u at 0.., Q.w at
+// kGsB.., u.u and u.w at kGsUU, r, h and 1/r at kGsR.
+// kGsTile cells per thread in k_gs_dots* and k_gs_update (256-thread blocks).
+constexpr int kGsB = 64, kGsUU = 128, kGsR = 130, kGsTile = 8;
+#define GS_DOTS_DECL(NV)                                                                             \
+  __global__ void k_gs_dots##NV(size_t n, int v0, const double *const *Q, const double *u, const double *w, \
+                                int first, double *partial);
+GS_DOTS_DECL(0)
+GS_DOTS_DECL(1)
+GS_DOTS_DECL(2)
+GS_DOTS_DECL(3)
+GS_DOTS_DECL(4)
+GS_DOTS_DECL(5)
+GS_DOTS_DECL(6)
+GS_DOTS_DECL(7)
+GS_DOTS_DECL(8)
+#undef GS_DOTS_DECL
+__global__ void k_gs_reduce(const double *partial, int nb, int nv, double *red);
+__global__ void k_gs_coef(int nv, double *red);
+__global__ void k_gs_update(size_t n, int nv, const double *const *Q, const double *red, double *u, double *w,
                             double *partial);
 __global__ void k_axpy_multi(size_t n, int nv, const double *const *Z, const double *coef, double *x);
-__global__ void k_scale_to(size_t n, const double *v, double s, const double *scale, float *out32,
-                           double *out64);
+__global__ void k_scale_to(size_t n, const double *v, double s, const double *nrm2, const double *scale,
+                           float *out32, double *out64);
 __global__ void k_to64(size_t n, const float *x32, const double *x64, double s, double *out);
 __global__ void k_sumsq(size_t n, const double *x, double *partial);
 

@@ -339,17 +339,6 @@ __global__ void k_max_spacing(Grid g, const double *coor, double *H) {
   }
 }
 
-// Gram-Schmidt coefficients on the device: h_i = sv_i (V_i . w) and the
-// update coefficient h_i sv_i for the stored (unnormalised) V_i.
-__global__ void k_gs_coef(int nv, const double *dots, const double *sv, double *hcol, double *coef) {
-  int i = threadIdx.x;
-  if (i < nv) {
-    double hh = dots[i] * sv[i];
-    hcol[i] = hh;
-    coef[i] = hh * sv[i];
-  }
-}
-
 struct Level {
   Grid g{};
   Box b{};
@@ -359,6 +348,8 @@ struct Level {
   bool own_met = false;
   double *A64 = nullptr;
   float *A32 = nullptr;
+  __half2 *C16 = nullptr;  // the FP32 V-cycle's residual operator (k_pack16)
+  float *D32 = nullptr;
   uint8_t *rowtype = nullptr, *blank = nullptr;
   double *inv64 = nullptr, *cp64 = nullptr, *w64 = nullptr;
   float *inv32 = nullptr, *cp32 = nullptr, *w32 = nullptr;
@@ -656,7 +647,7 @@ int build_coarsest(vfs_poisson *h, Level &l) {
 void free_level(vfs_poisson *h, Level &l, bool level0) {
   if (!level0) { dfree(h, l.coor); dfree(h, l.nvert); dfree(h, l.rho); dfree(h, l.level); }
   if (l.own_met) free_metrics(h, l.met);
-  dfree(h, l.A64); dfree(h, l.A32); dfree(h, l.rowtype); dfree(h, l.blank);
+  dfree(h, l.A64); dfree(h, l.A32); dfree(h, l.C16); dfree(h, l.D32); dfree(h, l.rowtype); dfree(h, l.blank);
   dfree(h, l.inv64); dfree(h, l.cp64); dfree(h, l.w64); dfree(h, l.inv32); dfree(h, l.cp32); dfree(h, l.w32);
   for (int q = 0; q < 4; q++) { dfree(h, l.v64[q]); dfree(h, l.v32[q]); }
   dfree(h, l.didx); dfree(h, l.dinv);
@@ -689,6 +680,8 @@ int build_level_operator(vfs_poisson *h, Level &l) {
   const size_t n = l.b.n();
   TRY(dalloc(h, &l.A64, n * NSLOT));
   TRY(dalloc(h, &l.A32, n * NSLOT));
+  TRY(dalloc(h, &l.C16, n * 10));
+  TRY(dalloc(h, &l.D32, n));
   TRY(dalloc(h, &l.rowtype, n));
   TRY(dalloc(h, &l.blank, n));
   TRY(dalloc(h, &l.w64, n));
@@ -702,6 +695,7 @@ int build_level_operator(vfs_poisson *h, Level &l) {
   LAUNCH(h, k_line_lu_f64, dim3((l.b.nx + 127) / 128, l.b.nz), 128, l.b, l.A64, l.inv64, l.cp64);
   LAUNCH(h, k_line_lu_f32, dim3((l.b.nx + 127) / 128, l.b.nz), 128, l.b, l.A64, l.inv32, l.cp32);
   LAUNCH(h, k_cast_planes_f32, kRedBlocks, 256, l.A64, l.A32, n * NSLOT);
+  LAUNCH(h, k_pack16, kRedBlocks, 256, n, l.A64, l.C16, l.D32);
   return VFS_OK;
 }
 
@@ -780,7 +774,9 @@ struct Prec;
 template <>
 struct Prec<float> {
   static constexpr auto sweep = k_line_sweep_f32;
-  static constexpr auto residual = k_residual_f32;
+  static void residual(vfs_poisson *h, Level &l, dim3 g, const float *x, const float *bb, float *r, int color) {
+    LAUNCH(h, k_residual16, g, 128, l.b, l.C16, l.D32, x, bb, r, color);
+  }
   static constexpr auto restrict_ = k_restrict_f32;
   static constexpr auto prolong = k_prolong_f32;
   static constexpr auto coarsest = k_coarsest_f32;
@@ -795,7 +791,9 @@ struct Prec<float> {
 template <>
 struct Prec<double> {
   static constexpr auto sweep = k_line_sweep_f64;
-  static constexpr auto residual = k_residual_f64;
+  static void residual(vfs_poisson *h, Level &l, dim3 g, const double *x, const double *bb, double *r, int color) {
+    LAUNCH(h, k_residual_f64, g, 128, l.b, l.A64, x, bb, r, color);
+  }
   static constexpr auto restrict_ = k_restrict_f64;
   static constexpr auto prolong = k_prolong_f64;
   static constexpr auto coarsest = k_coarsest_f64;
@@ -810,17 +808,22 @@ struct Prec<double> {
 
 // Event pairs around the level-0 sweeps of one V-cycle (recorded as graph
 // nodes when the V-cycle is captured); read after the next stream sync.
-// Algorithmic bytes of a sweep per cell: 16 off-line coefficients, the S
-// slot, inv and cp, the right-hand side, x and the written x (22 words),
-// or 5 words for the first sweep from a zero guess (S, inv, cp, rhs, x out).
-// For the correction-form sweeps (residual kernel + tridiagonal kernel) a
-// full sweep moves 22 + 6 words per cell (the residual's 19 coefficients,
-// x, rhs and r; then r, S slot, inv, cp, x read and written).
+// Algorithmic bytes of a sweep per cell, in words of T: the fused sweep
+// reads 16 off-line coefficients, the S slot, inv and cp, the right-hand
+// side and x and writes x (22 words), or 5 words from a zero guess (S, inv,
+// cp, rhs, x out).  The correction-form sweeps (residual kernel +
+// tridiagonal kernel) move R + 6 words per cell: the residual's operator, x,
+// rhs and r (R = 22 with 19 coefficients of T; R = 14 for the FP32 packed
+// operator, 10 half2 words and the diagonal), then r, S slot, inv, cp and x
+// read and written.  A zero-guess zebra sweep skips the first colour's
+// residual and reads rhs, S, inv, cp and writes x there.
 template <typename T>
 void prof_begin(vfs_poisson *h, int li, bool zero_guess, int smoother) {
   if (!h->prof || li != 0 || h->pcount >= 16) return;
   cudaEventRecord(h->pev[0][h->pcount], h->stream);
-  const double words = zero_guess ? (smoother >= 2 ? 16.5 : 5.0) : (smoother == 0 ? 22.0 : 28.0);
+  const double R = std::is_same<T, float>::value ? 14.0 : 22.0;
+  const double words = zero_guess ? (smoother >= 2 ? 0.5 * (5.0 + R + 6.0) : 5.0)
+                                  : (smoother == 0 ? 22.0 : R + 6.0);
   h->pbytes[h->pcount] = (double)h->box.n() * sizeof(T) * words;
 }
 void prof_end(vfs_poisson *h, int li) {
@@ -846,14 +849,14 @@ void smooth(vfs_poisson *h, Level &l, int li, int smoother, bool zero_guess, T o
               zero_guess ? 1 : 0);
     std::swap(x, t);
   } else if (smoother == 1) {
-    if (!zero_guess) LAUNCH(h, Prec<T>::residual, box_grid(l.b), 128, l.b, Prec<T>::A(l), x, bb, r, -1);
+    if (!zero_guess) Prec<T>::residual(h, l, box_grid(l.b), x, bb, r, -1);
     LAUNCH_SM(h, Prec<T>::tri, lg, lb, lsm, l.b, zero_guess ? bb : r, Asp, Prec<T>::inv(l), Prec<T>::cp(l), x,
               omega, zero_guess ? 1 : 0, -1);
   } else if (smoother == 2) {
     if (zero_guess) cudaMemsetAsync(x, 0, l.b.n() * sizeof(T), h->stream);
     for (int color = 0; color < 2; color++) {
       const bool skip_res = zero_guess && color == 0;  // x = 0: r = rhs
-      if (!skip_res) LAUNCH(h, Prec<T>::residual, box_grid(l.b), 128, l.b, Prec<T>::A(l), x, bb, r, color);
+      if (!skip_res) Prec<T>::residual(h, l, box_grid(l.b), x, bb, r, color);
       LAUNCH_SM(h, Prec<T>::tri, lg, lb, lsm, l.b, skip_res ? bb : r, Asp, Prec<T>::inv(l), Prec<T>::cp(l), x,
                 omega, 0, color);
     }
@@ -865,7 +868,7 @@ void smooth(vfs_poisson *h, Level &l, int li, int smoother, bool zero_guess, T o
     dim3 cg((nh + TI - 1) / TI, l.b.nz), rg((nh + 127) / 128, l.b.ny, l.b.nz);
     for (int color = 0; color < 2; color++) {
       const bool skip_res = zero_guess && color == 0;
-      if (!skip_res) LAUNCH(h, Prec<T>::residual, rg, 128, l.b, Prec<T>::A(l), x, bb, r, 2 + color);
+      if (!skip_res) Prec<T>::residual(h, l, rg, x, bb, r, 2 + color);
       LAUNCH_SM(h, Prec<T>::tri, cg, lb, lsm, l.b, skip_res ? bb : r, Asp, Prec<T>::inv(l), Prec<T>::cp(l), x,
                 omega, 0, (skip_res ? 4 : 2) + color);
     }
@@ -885,7 +888,7 @@ void vcycle(vfs_poisson *h, int li, int nu1, int nu2, T omega, int smoother) {
   }
   if (nu1 == 0) cudaMemsetAsync(x, 0, l.b.n() * sizeof(T), h->stream);
   for (int s = 0; s < nu1; s++) smooth<T>(h, l, li, smoother, s == 0, omega, x, t, bb, r);
-  LAUNCH(h, Prec<T>::residual, box_grid(l.b), 128, l.b, Prec<T>::A(l), x, bb, r, -1);
+  Prec<T>::residual(h, l, box_grid(l.b), x, bb, r, -1);
   Level &q = h->L[li + 1];
   LAUNCH(h, Prec<T>::restrict_, box_grid(q.b), 128, l.b, q.b, l.cx, l.cy, l.cz, r, Prec<T>::w(l), q.blank,
          Prec<T>::v(q)[1]);
@@ -935,16 +938,18 @@ int run_vcycle(vfs_poisson *h, const vfs_solve_opts &o) {
   return VFS_OK;
 }
 
-// z = M (s v): aj row scaling, one V-cycle of the chosen precision, back to FP64.
-int precondition(vfs_poisson *h, const double *v, double s, double *z, const vfs_solve_opts &o) {
+// z = M (s v): aj row scaling, one V-cycle of the chosen precision, back to
+// FP64.  With nrm2 (device) set, v is also divided by sqrt(nrm2[0]).
+int precondition(vfs_poisson *h, const double *v, double s, const double *nrm2, double *z,
+                 const vfs_solve_opts &o) {
   Level &l0 = h->L[0];
   const size_t n = h->box.n();
   if (o.precision == 0) {
-    LAUNCH(h, k_scale_to, kRedBlocks, 256, n, v, s, h->scale, l0.v32[1], (double *)nullptr);
+    LAUNCH(h, k_scale_to, kRedBlocks, 256, n, v, s, nrm2, h->scale, l0.v32[1], (double *)nullptr);
     TRY(run_vcycle<float>(h, o));
     LAUNCH(h, k_to64, kRedBlocks, 256, n, (const float *)l0.xfinal32, (const double *)nullptr, 1.0, z);
   } else {
-    LAUNCH(h, k_scale_to, kRedBlocks, 256, n, v, s, h->scale, (float *)nullptr, l0.v64[1]);
+    LAUNCH(h, k_scale_to, kRedBlocks, 256, n, v, s, nrm2, h->scale, (float *)nullptr, l0.v64[1]);
     TRY(run_vcycle<double>(h, o));
     LAUNCH(h, k_to64, kRedBlocks, 256, n, (const float *)nullptr, (const double *)l0.xfinal64, 1.0, z);
   }
@@ -1022,20 +1027,41 @@ int check_opts(const vfs_solve_opts &o) {
   return VFS_OK;
 }
 
-// FGMRES(m) with lazily normalised basis vectors: the stored V_i times sv[i]
-// is the unit Arnoldi vector, which saves one normalisation pass per step.
+// One DCGS2 dots launch over basis vectors v0 .. v0+nv-1 (nv <= 8).
+void gs_dots(vfs_poisson *h, int nv, int nb, size_t n, int v0, const double *u, const double *w, int first) {
+  const double *const *Q = (const double *const *)h->dV;
+  switch (nv) {
+#define CASE(NV) \
+  case NV: LAUNCH(h, k_gs_dots##NV, nb, 256, n, v0, Q, u, w, first, h->partial); break;
+    CASE(0) CASE(1) CASE(2) CASE(3) CASE(4) CASE(5) CASE(6) CASE(7) CASE(8)
+#undef CASE
+  }
+}
+
+// FGMRES(m) (flexible GMRES: the preconditioned vectors Z_j are kept and
+// x = x0 + Z y) with delayed classical Gram-Schmidt reorthogonalisation.
+// Step j preconditions the pending vector V_j (projected once, divided by its
+// norm reduced on the device), applies A, and one Gram-Schmidt round
+// finishes V_j (reorthogonalised, normalised) and projects A z_j into
+// V_{j+1}.  Finishing V_j = (u - Q a) / r corrects Hessenberg column j-1
+// (H[0..j-1, j-1] += a, H[j, j-1] = r) and its Givens rotation is formed
+// again; column j enters with the norm of the once-projected vector, which
+// gives the residual estimate of the convergence test.  One host read-back
+// per step.
 int fgmres(vfs_poisson *h, const vfs_solve_opts &o, vfs_solve_stats *st) {
   const size_t n = h->box.n();
   const int m = o.restart;
   TRY(ensure_krylov(h, m));
-  const int nbd = (int)((n + 256 * 8 - 1) / (256 * 8));
+  const int nbd = (int)((n + 256 * kGsTile - 1) / (256 * kGsTile));
   double bn2;
   LAUNCH(h, k_sumsq, kRedBlocks, 256, n, h->b, h->partial);
   TRY(reduce_read(h, kRedBlocks, 1, &bn2));
   const double bn = std::sqrt(bn2);
   int it = 0;
   double rel = 0., beta = 0.;
-  std::vector<double> H((size_t)(m + 1) * m, 0.), cs(m), sn(m), gv(m + 1), y(m), sv(m + 1);
+  // Hraw: Hessenberg columns as formed; R: the same after the Givens rotations
+  std::vector<double> Hraw((size_t)(m + 1) * m, 0.), R((size_t)(m + 1) * m, 0.), cs(m), sn(m), gv(m + 1),
+      gsave(m + 1), y(m);
   if (bn == 0.) {
     CUDA_TRY(cudaMemsetAsync(h->x, 0, n * 8, h->stream));
     st->initial_rel_residual = 0.;
@@ -1054,89 +1080,87 @@ int fgmres(vfs_poisson *h, const vfs_solve_opts &o, vfs_solve_stats *st) {
   }
   rel = beta / bn;
   st->initial_rel_residual = rel;
+  // rotate the formed column j by rotations 0..j-1, form rotation j and
+  // apply it to the right-hand side gv
+  auto rotate = [&](int j) {
+    for (int i = 0; i <= j + 1; i++) R[(size_t)i * m + j] = Hraw[(size_t)i * m + j];
+    for (int i = 0; i < j; i++) {
+      const double a = R[(size_t)i * m + j], b2 = R[(size_t)(i + 1) * m + j];
+      R[(size_t)i * m + j] = cs[i] * a + sn[i] * b2;
+      R[(size_t)(i + 1) * m + j] = -sn[i] * a + cs[i] * b2;
+    }
+    const double a = R[(size_t)j * m + j], b2 = R[(size_t)(j + 1) * m + j];
+    const double den = std::sqrt(a * a + b2 * b2);
+    cs[j] = den != 0. ? a / den : 1.;
+    sn[j] = den != 0. ? b2 / den : 0.;
+    R[(size_t)j * m + j] = den;
+    R[(size_t)(j + 1) * m + j] = 0.;
+    gv[j + 1] = -sn[j] * gv[j];
+    gv[j] = cs[j] * gv[j];
+  };
+  const double *const *dV = (const double *const *)h->dV;
   while (rel > o.rtol && it < o.max_it) {
-    sv[0] = 1.0 / beta;
-    h->hbuf[400] = sv[0];
+    h->hbuf[400] = beta * beta;  // pinned staging: pageable copies cost ~0.5 ms each
     CUDA_TRY(cudaMemcpyAsync(h->dsv, h->hbuf + 400, 8, cudaMemcpyHostToDevice, h->stream));
     std::fill(gv.begin(), gv.end(), 0.);
+    std::fill(Hraw.begin(), Hraw.end(), 0.);
     gv[0] = beta;
     int jj = 0;
     for (; jj < m && it < o.max_it; jj++) {
       const auto t0 = h->phase ? std::chrono::steady_clock::now() : std::chrono::steady_clock::time_point();
       if (h->phase) cudaEventRecord(h->phev[0], h->stream);
-      TRY(precondition(h, h->V[jj], sv[jj], h->Z[jj], o));
+      TRY(precondition(h, h->V[jj], 1.0, h->dsv + jj, h->Z[jj], o));
       const auto t1 = h->phase ? std::chrono::steady_clock::now() : t0;
       if (h->phase) cudaEventRecord(h->phev[1], h->stream);
       double *w = h->V[jj + 1];
       LAUNCH(h, k_apply64, box_grid(h->box), 128, h->box, h->A0, h->Z[jj], w);
       if (h->phase) cudaEventRecord(h->phev[2], h->stream);
-      // classical Gram-Schmidt with the coefficients formed on the device and
-      // one read-back per step; a DGKS re-orthogonalisation pass runs when
-      // the update removed more than half of ||w|| (a second read-back).
-      double ww = 0., wn = 0.;
-      for (int pass = 0; pass < 2; pass++) {
-        double *dred = h->red, *dh = h->red + 128, *dwn = h->red + 256;
-        // 8 basis vectors per pass; each pass's last row (w.w) lands where
-        // the next pass's first dot goes, and the final pass leaves w.w at
-        // dred[jj + 1]
-        for (int v0 = 0; v0 <= jj; v0 += 8) {
-          const int nv = std::min(8, jj + 1 - v0);
-          LAUNCH(h, k_dots, nbd, 256, n, nv, (const double *const *)(h->dV + v0), w, h->partial);
-          LAUNCH(h, k_reduce_rows, nv + 1, 1024, h->partial, nbd, nv + 1, dred + v0);
-        }
-        LAUNCH(h, k_gs_coef, 1, 64, jj + 1, dred, h->dsv, dh, h->coef);
-        LAUNCH(h, k_gs_update, nbd, 256, n, jj + 1, (const double *const *)h->dV, h->coef, w, h->partial);
-        LAUNCH(h, k_reduce_rows, 1, 1024, h->partial, nbd, 1, dwn);
-        if (h->phase && pass == 0) cudaEventRecord(h->phev[3], h->stream);
-        CUDA_TRY(cudaMemcpyAsync(h->hbuf, h->red, 257 * 8, cudaMemcpyDeviceToHost, h->stream));
-        const auto t2 = h->phase ? std::chrono::steady_clock::now() : t0;
-        TRY(sync(h));
-        const auto t3 = h->phase ? std::chrono::steady_clock::now() : t0;
-        if (h->phase && pass == 0) {
-          h->host_ms[0] += std::chrono::duration<double, std::milli>(t1 - t0).count();
-          h->host_ms[1] += std::chrono::duration<double, std::milli>(t2 - t1).count();
-          h->host_ms[2] += std::chrono::duration<double, std::milli>(t3 - t2).count();
-        }
-        if (pass == 0) prof_collect(h);
-        if (h->phase && pass == 0) {
-          float a = 0.f, b = 0.f, c = 0.f;
-          cudaEventElapsedTime(&a, h->phev[0], h->phev[1]);
-          cudaEventElapsedTime(&b, h->phev[1], h->phev[2]);
-          cudaEventElapsedTime(&c, h->phev[2], h->phev[3]);
-          h->phase_ms[0] += a; h->phase_ms[1] += b; h->phase_ms[2] += c;
-        }
-        if (pass == 0) ww = h->hbuf[jj + 1];
-        for (int i = 0; i <= jj; i++) H[(size_t)i * m + jj] = (pass ? H[(size_t)i * m + jj] : 0.) + h->hbuf[128 + i];
-        wn = h->hbuf[256];
-        if (!(std::sqrt(wn) < 0.7 * std::sqrt(ww))) break;
-        ww = wn;
+      for (int v0 = 0; v0 == 0 || v0 < jj; v0 += 8) gs_dots(h, std::min(8, jj - v0), nbd, n, v0, h->V[jj], w, v0 == 0);
+      LAUNCH(h, k_gs_reduce, 2 * jj + 2, 1024, h->partial, nbd, jj, h->red);
+      LAUNCH(h, k_gs_coef, 1, 32, jj, h->red);
+      LAUNCH(h, k_gs_update, nbd, 256, n, jj, dV, h->red, h->V[jj], w, h->partial);
+      LAUNCH(h, k_reduce_rows, 1, 1024, h->partial, nbd, 1, h->dsv + jj + 1);
+      if (h->phase) cudaEventRecord(h->phev[3], h->stream);
+      CUDA_TRY(cudaMemcpyAsync(h->hbuf, h->red, (kGsR + 3) * 8, cudaMemcpyDeviceToHost, h->stream));
+      CUDA_TRY(cudaMemcpyAsync(h->hbuf + kGsR + 3, h->dsv + jj + 1, 8, cudaMemcpyDeviceToHost, h->stream));
+      const auto t2 = h->phase ? std::chrono::steady_clock::now() : t0;
+      TRY(sync(h));
+      const auto t3 = h->phase ? std::chrono::steady_clock::now() : t0;
+      if (h->phase) {
+        h->host_ms[0] += std::chrono::duration<double, std::milli>(t1 - t0).count();
+        h->host_ms[1] += std::chrono::duration<double, std::milli>(t2 - t1).count();
+        h->host_ms[2] += std::chrono::duration<double, std::milli>(t3 - t2).count();
+        float a = 0.f, b = 0.f, c = 0.f;
+        cudaEventElapsedTime(&a, h->phev[0], h->phev[1]);
+        cudaEventElapsedTime(&b, h->phev[1], h->phev[2]);
+        cudaEventElapsedTime(&c, h->phev[2], h->phev[3]);
+        h->phase_ms[0] += a; h->phase_ms[1] += b; h->phase_ms[2] += c;
       }
-      double hn = std::sqrt(wn);
-      H[(size_t)(jj + 1) * m + jj] = hn;
-      sv[jj + 1] = hn > 0. ? 1.0 / hn : 0.;
-      h->hbuf[400 + jj + 1] = sv[jj + 1];  // pinned staging: pageable copies cost ~0.5 ms each
-      CUDA_TRY(cudaMemcpyAsync(h->dsv + jj + 1, h->hbuf + 400 + jj + 1, 8, cudaMemcpyHostToDevice, h->stream));
-      for (int i = 0; i < jj; i++) {
-        double a = H[(size_t)i * m + jj], b2 = H[(size_t)(i + 1) * m + jj];
-        H[(size_t)i * m + jj] = cs[i] * a + sn[i] * b2;
-        H[(size_t)(i + 1) * m + jj] = -sn[i] * a + cs[i] * b2;
-      }
-      double a = H[(size_t)jj * m + jj], b2 = H[(size_t)(jj + 1) * m + jj];
-      double den = std::sqrt(a * a + b2 * b2);
-      cs[jj] = den != 0. ? a / den : 1.;
-      sn[jj] = den != 0. ? b2 / den : 0.;
-      H[(size_t)jj * m + jj] = den;
-      H[(size_t)(jj + 1) * m + jj] = 0.;
-      gv[jj + 1] = -sn[jj] * gv[jj];
-      gv[jj] = cs[jj] * gv[jj];
+      prof_collect(h);
       it++;
+      const double r = h->hbuf[kGsR], hj = h->hbuf[kGsR + 1];
+      const double wn = std::sqrt(std::max(h->hbuf[kGsR + 3], 0.));
+      if (jj > 0) {
+        // V_jj lies in the span of the finished vectors: column jj-1 was a
+        // breakdown; the cycle ends with the columns before this step
+        if (!(r > 0.)) break;
+        for (int i = 0; i < jj; i++) Hraw[(size_t)i * m + jj - 1] += h->hbuf[i];
+        Hraw[(size_t)jj * m + jj - 1] = r;
+        gv = gsave;
+        rotate(jj - 1);
+      }
+      for (int i = 0; i < jj; i++) Hraw[(size_t)i * m + jj] = h->hbuf[kGsB + i];
+      Hraw[(size_t)jj * m + jj] = hj;
+      Hraw[(size_t)(jj + 1) * m + jj] = wn;
+      gsave = gv;
+      rotate(jj);
       if (h->phase) h->host_ms[3] += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
-      if (std::fabs(gv[jj + 1]) / bn <= o.rtol || hn == 0.) { jj++; break; }
+      if (std::fabs(gv[jj + 1]) / bn <= o.rtol || wn == 0.) { jj++; break; }
     }
     for (int i = jj - 1; i >= 0; i--) {
       double s = gv[i];
-      for (int q = i + 1; q < jj; q++) s -= H[(size_t)i * m + q] * y[q];
-      y[i] = H[(size_t)i * m + i] != 0. ? s / H[(size_t)i * m + i] : 0.;
+      for (int q = i + 1; q < jj; q++) s -= R[(size_t)i * m + q] * y[q];
+      y[i] = R[(size_t)i * m + i] != 0. ? s / R[(size_t)i * m + i] : 0.;
     }
     for (int i = 0; i < jj; i++) h->hbuf[400 + 64 + i] = y[i];
     CUDA_TRY(cudaMemcpyAsync(h->coef, h->hbuf + 464, jj * 8, cudaMemcpyHostToDevice, h->stream));
@@ -1240,7 +1264,7 @@ int vfs_poisson_create(const vfs_grid_desc *gd, vfs_poisson **out) {
     return bail(rc);
   const int nblk = (int)((n + 1023) / 1024);
   if ((rc = dalloc(h, &h->blk, nblk))) return bail(rc);
-  h->partial_len = std::max<size_t>(n / 16 + 65536, (size_t)70 * ((n + 2047) / 2048) + 4096);
+  h->partial_len = std::max<size_t>(n / 16 + 65536, (size_t)(kGsUU + 2) * ((n + 2047) / 2048) + 4096);
   if ((rc = dalloc(h, &h->partial, h->partial_len))) return bail(rc);
   if (cudaMallocHost(&h->hbuf, 1024 * 8) != cudaSuccess) { cudaGetLastError(); return bail(fail(VFS_ENOMEM, "pinned alloc")); }
   cudaMemsetAsync(h->phi_da, 0, N * 8, h->stream);
@@ -1656,7 +1680,18 @@ int vfs_poisson_learned_guess(vfs_poisson *h, vfs_unet *u, const double *phi_nm1
   const double nb = nrm[2] > 0. ? std::sqrt(nrm[2]) : 1.;
   double r_learn = std::sqrt(std::max(r2, 0.));
   bool learned = false;
-  if (r_learn < 1.1 * r_prev) {
+  bool weighted = false;
+  for (int u2 = 0; u2 < kGuessBands; u2++) weighted = weighted || bw.a[u2] != 0.;
+  if (!weighted) {
+    // all band weights 0: the learned guess is the extrapolation, whose
+    // residual the features step already formed
+    r_learn = std::sqrt(nrm[0]);
+    learned = r_learn < r_prev;
+    if (learned) {
+      CUDA_TRY(cudaMemcpyAsync(h->x, h->gex, n * 8, cudaMemcpyDeviceToDevice, h->stream));
+      CUDA_TRY(cudaMemcpyAsync(h->rlearn, h->r, n * 8, cudaMemcpyDeviceToDevice, h->stream));
+    }
+  } else if (r_learn < 1.1 * r_prev) {
     LAUNCH(h, k_guess_compose, kRedBlocks, 256, b, h->rowtype0, h->gex, h->gof[cur], kappa, h->gsum, bw, h->x);
     LAUNCH(h, k_residual64, box_grid(h->box), 128, h->box, h->A0, h->x, h->b, h->rlearn, h->partial);
     double s2 = 0.;
@@ -1870,7 +1905,7 @@ int vfs_poisson_mg_vcycle(vfs_poisson *h, int precision, const double *r, double
   const size_t n = h->box.n();
   TRY(upload(h, h->stage, r, h->g.n()));
   LAUNCH(h, k_da_to_box, lin_grid(n), 256, h->g, h->box, h->stage, h->r);
-  TRY(precondition(h, h->r, 1.0, h->r, o));
+  TRY(precondition(h, h->r, 1.0, nullptr, h->r, o));
   LAUNCH(h, k_box_to_da, da_grid(h->g), 128, h->g, h->box, h->r, h->stage);
   TRY(download(h, z, h->stage, h->g.n()));
   return sync(h);

@@ -4,6 +4,8 @@
 // All of them stream box-layout planes (i fastest) with one thread per cell
 // or per j-column, so every warp load is a contiguous 128-byte (FP32) or
 // 256-byte (FP64) segment; the 19-point neighbourhood is re-read through L1.
+#include <cuda_fp16.h>
+
 #include "common.cuh"
 #include "kernels.cuh"
 
@@ -15,18 +17,26 @@ namespace vfs {
 // residuals are then written at their split positions (the layout the line
 // kernel reads them in).  Threads walk split positions, so operator loads
 // coalesce.
+//
+// The row a thread takes: its split position p (false when the thread has no
+// row of the colour).
+__device__ __forceinline__ bool colour_row(const Box &b, int color, int t, int k, int &p) {
+  p = t;
+  if (color >= 2) {
+    const int par = (color - 2 + k) & 1, nh = (b.nx + 1) >> 1;
+    if (t >= (par ? b.nx - nh : nh)) return false;
+    p = par ? nh + t : t;
+    return true;
+  }
+  return t < b.nx && (color < 0 || (k & 1) == color);
+}
+
 template <typename T>
 __device__ __forceinline__ void residual_body(Box b, const T *__restrict__ A, const T *__restrict__ x,
                                               const T *__restrict__ rhs, T *__restrict__ r, int color) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y, k = blockIdx.z;
-  int p = t;
-  if (color >= 2) {
-    const int par = (color - 2 + k) & 1, nh = (b.nx + 1) >> 1;
-    if (t >= (par ? b.nx - nh : nh)) return;
-    p = par ? nh + t : t;
-  } else if (t >= b.nx || (color >= 0 && (k & 1) != color)) {
-    return;
-  }
+  int p;
+  if (!colour_row(b, color, t, k, p)) return;
   const int i = split_cell(p, b.nx);
   uint32_t idx[NSLOT];
   stencil_index(b, i, j, k, idx);
@@ -35,6 +45,51 @@ __device__ __forceinline__ void residual_body(Box b, const T *__restrict__ A, co
 #pragma unroll
   for (int q = 0; q < NSLOT; q++) s += __ldcs(&A[q * n + cs]) * __ldg(&x[idx[q]]);
   r[color >= 2 ? cs : c] = rhs[c] - s;
+}
+
+// The FP32 V-cycle's copy of a level operator (split layout): D = the
+// diagonal; half2 plane m < 9 holds the couplings of slots 2m+1 and 2m+2
+// divided by D, plane 9 the row sum divided by D (0 for the Neumann rows).
+// Rows without a dof get D = 0 and zero couplings.
+__global__ void k_pack16(size_t n, const double *__restrict__ A, __half2 *__restrict__ C, float *__restrict__ D) {
+  for (size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (size_t)gridDim.x * blockDim.x) {
+    const double d = A[CP * n + c];
+    const double inv = d != 0. ? 1. / d : 0.;
+    double sum = d;
+    for (int q = 1; q < NSLOT; q++) sum += A[q * n + c];
+    for (int m = 0; m < 9; m++)
+      C[m * n + c] = __halves2half2(__double2half(A[(2 * m + 1) * n + c] * inv), __double2half(A[(2 * m + 2) * n + c] * inv));
+    C[9 * n + c] = __halves2half2(__double2half(sum * inv), __double2half(0.));
+    D[c] = (float)d;
+  }
+}
+
+// FP32 r = rhs - A x from the packed operator in difference form,
+// r = rhs - D (s x_c + sum_q c_q (x_q - x_c)): rounding the couplings to half
+// perturbs each one by at most 2^-11 relative and leaves the row sums (the
+// constant null space of the Neumann rows) exact.  44 operator bytes per row
+// instead of 76.  Colours and layouts as in residual_body.
+__global__ void __launch_bounds__(128) k_residual16(Box b, const __half2 *__restrict__ C,
+                                                    const float *__restrict__ D, const float *__restrict__ x,
+                                                    const float *__restrict__ rhs, float *__restrict__ r, int color) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y, k = blockIdx.z;
+  int p;
+  if (!colour_row(b, color, t, k, p)) return;
+  const int i = split_cell(p, b.nx);
+  uint32_t idx[NSLOT];
+  stencil_index(b, i, j, k, idx);
+  const uint32_t n = (uint32_t)b.n(), c = idx[CP], cs = c - i + p;
+  const float xc = __ldg(&x[c]);
+  float s = 0.f;
+#pragma unroll
+  for (int m = 0; m < 9; m++) {
+    const float2 f = __half22float2(__ldcs(&C[m * n + cs]));
+    s = fmaf(f.x, __ldg(&x[idx[2 * m + 1]]) - xc, s);
+    s = fmaf(f.y, __ldg(&x[idx[2 * m + 2]]) - xc, s);
+  }
+  const float2 f = __half22float2(__ldcs(&C[9 * n + cs]));
+  s = fmaf(f.x, xc, s);
+  r[color >= 2 ? cs : c] = rhs[c] - __ldcs(&D[cs]) * s;
 }
 
 // FP64 y = A x on the unscaled operator.
@@ -367,82 +422,145 @@ __device__ __forceinline__ void cast_body(const double *__restrict__ src, T *__r
 }
 
 // ---- FP64 Krylov kernels (fixed grid, deterministic block partials) ----
-#define KTILE 8
-#define KDOT 8
-// Dots of w with up to KDOT basis vectors V[v0..v0+nv) (and w.w when
-// with_ww): each thread keeps KTILE values of w in registers and one
-// accumulator per vector; the block reduces all accumulators at once.
-// partial[(v - v0) * gridDim.x + block], row nv holds w.w.
-__global__ void __launch_bounds__(256) k_dots(size_t n, int nv, const double *const *__restrict__ V,
-                                              const double *__restrict__ w, double *partial) {
-  __shared__ double sh[8][KDOT + 1];
-  const size_t base = (size_t)blockIdx.x * blockDim.x * KTILE + threadIdx.x;
-  double wr[KTILE];
+// Delayed classical Gram-Schmidt with reorthogonalisation (DCGS2: Bielich,
+// Langou, Thomas, Swirydowicz, Yamazaki, Boman, "Low-synch Gram-Schmidt with
+// delayed reorthogonalization for Krylov solvers", Parallel Computing 2022).
+// Arnoldi step j holds the finished orthonormal vectors Q_0..Q_{j-1}, the
+// pending vector u (step j-1's projected vector, projected once) and the new
+// vector w = A z_j.  One pass forms Q.u, Q.w, u.u and u.w; one more pass
+// reorthogonalises and normalises u into Q_j and projects w against
+// Q_0..Q_j.  Two passes over the basis and one host read-back per step.
+//
+// Rows of the block partials (and of the reduced values): Q_v.u at v,
+// Q_v.w at kGsB + v, u.u at kGsUU, u.w at kGsUU + 1.
+template <int NV>
+__device__ __forceinline__ void gs_dots_body(size_t n, int v0, const double *const *__restrict__ Q,
+                                             const double *__restrict__ u, const double *__restrict__ w, int first,
+                                             double *__restrict__ partial) {
+  constexpr int NA = 2 * NV + 2;
+  __shared__ double sh[8][NA];
+  double acc[NA];
 #pragma unroll
-  for (int q = 0; q < KTILE; q++) {
-    size_t c = base + (size_t)q * blockDim.x;
-    wr[q] = c < n ? w[c] : 0.;
+  for (int a = 0; a < NA; a++) acc[a] = 0.;
+  const double *q[NV > 0 ? NV : 1];
+#pragma unroll
+  for (int v = 0; v < NV; v++) q[v] = Q[v0 + v];
+  const size_t base = (size_t)blockIdx.x * blockDim.x * kGsTile + threadIdx.x;
+#pragma unroll 2
+  for (int t = 0; t < kGsTile; t++) {
+    const size_t c = base + (size_t)t * blockDim.x;
+    if (c < n) {
+      const double uc = u[c], wc = w[c];
+#pragma unroll
+      for (int v = 0; v < NV; v++) {
+        const double qv = __ldcs(q[v] + c);
+        acc[v] = fma(qv, uc, acc[v]);
+        acc[NV + v] = fma(qv, wc, acc[NV + v]);
+      }
+      acc[2 * NV] = fma(uc, uc, acc[2 * NV]);
+      acc[2 * NV + 1] = fma(uc, wc, acc[2 * NV + 1]);
+    }
   }
-  double acc[KDOT + 1];
+  const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
 #pragma unroll
-  for (int v = 0; v <= KDOT; v++) acc[v] = 0.;
+  for (int a = 0; a < NA; a++) {
+    const double s = warp_sum(acc[a]);
+    if (lane == 0) sh[wp][a] = s;
+  }
+  __syncthreads();
+  if (threadIdx.x < NA) {
+    const int a = threadIdx.x;
+    double s = 0.;
+    for (int k = 0; k < (int)(blockDim.x >> 5); k++) s += sh[k][a];
+    const int row = a < NV ? v0 + a : a < 2 * NV ? kGsB + v0 + a - NV : kGsUU + a - 2 * NV;
+    if (a < 2 * NV || first) partial[(size_t)row * gridDim.x + blockIdx.x] = s;
+  }
+}
+#define GS_DOTS(NV)                                                                                            \
+  __global__ void __launch_bounds__(256) k_gs_dots##NV(size_t n, int v0, const double *const *Q,               \
+                                                       const double *u, const double *w, int first,            \
+                                                       double *partial) {                                      \
+    gs_dots_body<NV>(n, v0, Q, u, w, first, partial);                                                         \
+  }
+GS_DOTS(0)
+GS_DOTS(1)
+GS_DOTS(2)
+GS_DOTS(3)
+GS_DOTS(4)
+GS_DOTS(5)
+GS_DOTS(6)
+GS_DOTS(7)
+GS_DOTS(8)
+#undef GS_DOTS
+
+// Sums the used partial rows (one block per row: Q.u rows 0..nv-1, Q.w rows
+// kGsB.., then u.u and u.w) in a fixed order into red at the same row index.
+__global__ void k_gs_reduce(const double *__restrict__ partial, int nb, int nv, double *red) {
+  const int r = blockIdx.x;
+  const int row = r < nv ? r : r < 2 * nv ? kGsB + r - nv : kGsUU + r - 2 * nv;
+  double s = 0.;
+  for (int q = threadIdx.x; q < nb; q += blockDim.x) s += partial[(size_t)row * nb + q];
+  s = block_sum(s);
+  if (threadIdx.x == 0) red[row] = s;
+}
+
+// Step coefficients from the reduced dots: r = ||u - Q a|| by Pythagoras
+// (the reorthogonalisation coefficients a = Q.u are small next to ||u||),
+// h = Q_j.w for the finished Q_j = (u - Q a) / r.  red[kGsR] = r,
+// red[kGsR + 1] = h, red[kGsR + 2] = 1 / r (0 when r is 0).
+__global__ void k_gs_coef(int nv, double *red) {
+  if (threadIdx.x != 0) return;
+  double aa = 0., ab = 0.;
+  for (int v = 0; v < nv; v++) {
+    aa = fma(red[v], red[v], aa);
+    ab = fma(red[v], red[kGsB + v], ab);
+  }
+  const double r2 = red[kGsUU] - aa;
+  const double r = r2 > 0. ? sqrt(r2) : 0.;
+  const double rinv = r > 0. ? 1. / r : 0.;
+  red[kGsR] = r;
+  red[kGsR + 1] = (red[kGsUU + 1] - ab) * rinv;
+  red[kGsR + 2] = rinv;
+}
+
+// Q_j = (u - sum_v a_v Q_v) / r written over u; w -= sum_v b_v Q_v + h Q_j;
+// block partials of ||w||^2.  Each basis vector streams once; the u and w
+// tiles stay in registers.
+__global__ void __launch_bounds__(256) k_gs_update(size_t n, int nv, const double *const *__restrict__ Q,
+                                                   const double *__restrict__ red, double *__restrict__ u,
+                                                   double *__restrict__ w, double *partial) {
+  const size_t base = (size_t)blockIdx.x * blockDim.x * kGsTile + threadIdx.x;
+  double au[kGsTile], aw[kGsTile];
 #pragma unroll
-  for (int v = 0; v < KDOT; v++) {
-    if (v < nv) {
-      const double *p = V[v];
+  for (int t = 0; t < kGsTile; t++) {
+    const size_t c = base + (size_t)t * blockDim.x;
+    au[t] = c < n ? u[c] : 0.;
+    aw[t] = c < n ? w[c] : 0.;
+  }
+  for (int v = 0; v < nv; v++) {
+    const double *p = Q[v];
+    const double ca = -red[v], cb = -red[kGsB + v];
 #pragma unroll
-      for (int q = 0; q < KTILE; q++) {
-        size_t c = base + (size_t)q * blockDim.x;
-        if (c < n) acc[v] = fma(wr[q], __ldcs(&p[c]), acc[v]);
+    for (int t = 0; t < kGsTile; t++) {
+      const size_t c = base + (size_t)t * blockDim.x;
+      if (c < n) {
+        const double qv = __ldcs(&p[c]);
+        au[t] = fma(ca, qv, au[t]);
+        aw[t] = fma(cb, qv, aw[t]);
       }
     }
   }
-#pragma unroll
-  for (int q = 0; q < KTILE; q++) acc[KDOT] = fma(wr[q], wr[q], acc[KDOT]);
-  const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
-#pragma unroll
-  for (int v = 0; v <= KDOT; v++) {
-    double t = warp_sum(acc[v]);
-    if (lane == 0) sh[wp][v] = t;
-  }
-  __syncthreads();
-  if (threadIdx.x <= KDOT) {
-    const int v = threadIdx.x;
-    double t = 0.;
-    for (int q = 0; q < (int)(blockDim.x >> 5); q++) t += sh[q][v];
-    const int row = v < KDOT ? v : nv;
-    if (v < nv || v == KDOT) partial[(size_t)row * gridDim.x + blockIdx.x] = t;
-  }
-}
-
-// w -= sum_v coef[v] V_v, with the block partial of ||w||^2; the w tile
-// stays in registers while each basis vector streams once.
-__global__ void __launch_bounds__(256) k_gs_update(size_t n, int nv, const double *const *__restrict__ V,
-                                                   const double *__restrict__ coef, double *__restrict__ w,
-                                                   double *partial) {
-  const size_t base = (size_t)blockIdx.x * blockDim.x * KTILE + threadIdx.x;
-  double acc[KTILE];
-#pragma unroll
-  for (int q = 0; q < KTILE; q++) {
-    size_t c = base + (size_t)q * blockDim.x;
-    acc[q] = c < n ? w[c] : 0.;
-  }
-  for (int v = 0; v < nv; v++) {
-    const double *p = V[v];
-    const double cv = -coef[v];
-#pragma unroll
-    for (int q = 0; q < KTILE; q++) {
-      size_t c = base + (size_t)q * blockDim.x;
-      if (c < n) acc[q] = fma(cv, __ldcs(&p[c]), acc[q]);
-    }
-  }
+  const double rinv = red[kGsR + 2], hj = -red[kGsR + 1];
   double ss = 0.;
 #pragma unroll
-  for (int q = 0; q < KTILE; q++) {
-    size_t c = base + (size_t)q * blockDim.x;
+  for (int t = 0; t < kGsTile; t++) {
+    const size_t c = base + (size_t)t * blockDim.x;
     if (c < n) {
-      w[c] = acc[q];
-      ss = fma(acc[q], acc[q], ss);
+      const double qj = au[t] * rinv;
+      const double wn = fma(hj, qj, aw[t]);
+      u[c] = qj;
+      w[c] = wn;
+      ss = fma(wn, wn, ss);
     }
   }
   ss = block_sum(ss);
@@ -460,9 +578,11 @@ __global__ void __launch_bounds__(256) k_axpy_multi(size_t n, int nv, const doub
 }
 
 // out = (s v) * scale in FP32 or FP64: the aj row scaling that turns the
-// FP64 Krylov vector into the V-cycle right-hand side.
-__global__ void k_scale_to(size_t n, const double *__restrict__ v, double s, const double *__restrict__ scale,
-                           float *out32, double *out64) {
+// FP64 Krylov vector into the V-cycle right-hand side.  With nrm2 set, s is
+// divided by sqrt(nrm2[0]) (the norm of v, reduced on the device).
+__global__ void k_scale_to(size_t n, const double *__restrict__ v, double s, const double *__restrict__ nrm2,
+                           const double *__restrict__ scale, float *out32, double *out64) {
+  if (nrm2) s = nrm2[0] > 0. ? s / sqrt(nrm2[0]) : 0.;
   for (size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (size_t)gridDim.x * blockDim.x) {
     double t = s * v[c] * scale[c];
     if (out32) out32[c] = (float)t;
@@ -483,7 +603,7 @@ __global__ void k_sumsq(size_t n, const double *__restrict__ x, double *partial)
   if (threadIdx.x == 0) partial[blockIdx.x] = s;
 }
 
-#define TYPED(T, S, TRI_THREADS)                                                                           \
+#define TYPED(T, S, TRI_THREADS, TRI_MINB)                                                                         \
   __global__ void __launch_bounds__(256) k_residual_##S(Box b, const T *A, const T *x, const T *rhs, T *r,  \
                                                         int color) {                                       \
     residual_body<T>(b, A, x, rhs, r, color);                                                              \
@@ -493,7 +613,7 @@ __global__ void k_sumsq(size_t n, const double *__restrict__ x, double *partial)
                                                            const T *x, const T *rhs, T *xo, T omega, int zg) { \
     line_sweep_body<T, kLineChunk>(b, A, inv, cp, x, rhs, xo, omega, zg);                                   \
   }                                                                                                        \
-  __global__ void __launch_bounds__(TRI_THREADS) k_line_tri_##S(Box b, const T *r, const T *Asp, const T *inv,  \
+  __global__ void __launch_bounds__(TRI_THREADS, TRI_MINB) k_line_tri_##S(Box b, const T *r, const T *Asp, const T *inv,  \
                                                        const T *cp, T *x, T omega, int zg, int color) {        \
     line_tri_body<T, kLineChunk>(b, r, Asp, inv, cp, x, omega, zg, color);                                    \
   }                                                                                                        \
@@ -503,8 +623,8 @@ __global__ void k_sumsq(size_t n, const double *__restrict__ x, double *partial)
   __global__ void k_cast_planes_##S(const double *src, T *dst, size_t n) { cast_body<T>(src, dst, n); }
 // the line kernel keeps a whole chunk in registers: 16 columns per block
 // (at most 24 chunks each) so that neither precision spills
-TYPED(float, f32, 384)
-TYPED(double, f64, 384)
+TYPED(float, f32, 384, 3)
+TYPED(double, f64, 384, 1)
 #undef TYPED
 
 }  // namespace vfs

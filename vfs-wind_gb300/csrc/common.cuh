@@ -43,6 +43,16 @@ struct Box {
   }
 };
 
+// (i, j, k) of box-layout cell c, in 32-bit arithmetic (a box holds fewer
+// than 2^32 cells; 64-bit integer division costs a software routine).
+__device__ __forceinline__ void box_ijk(const Box &b, size_t c, int &i, int &j, int &k) {
+  const uint32_t u = (uint32_t)c, nx = (uint32_t)b.nx, ny = (uint32_t)b.ny;
+  const uint32_t row = u / nx, kk = row / ny;
+  i = (int)(u - row * nx);
+  j = (int)(row - kk * ny);
+  k = (int)kk;
+}
+
 // Cells of a j-line handled by one thread of the line smoother; a line of
 // ny cells uses ceil(ny / kLineChunk) threads (at most 24, 768 per block).
 constexpr int kLineChunk = 8;

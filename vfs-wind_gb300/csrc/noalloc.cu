@@ -78,7 +78,9 @@ __global__ void __launch_bounds__(kThreads) k_div_partial_noalloc(Grid g, Box b,
   const size_t hi = lo + kCellsPerBlock < n ? lo + kCellsPerBlock : n;
   double best = 0.;
   for (size_t c = lo + threadIdx.x; c < hi; c += kThreads) {
-    int i = c % b.nx + 1, j = (c / b.nx) % b.ny + 1, k = c / ((size_t)b.nx * b.ny) + 1;
+    int i, j, k;
+    box_ijk(b, c, i, j, k);
+    i++; j++; k++;
     double v = cell_div(g, nvert, ucont, aj, i, j, k);
     best = v > best ? v : best;
   }

@@ -57,7 +57,7 @@ __global__ void k_row_scale(size_t n, const uint8_t *rowtype, const double *aj_b
 __global__ void k_unsplit_plane(Box b, const float *src, float *dst) {
   size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= b.n()) return;
-  const int i = c % b.nx;
+  const int i = (int)((uint32_t)c % (uint32_t)b.nx);
   dst[c] = src[c - i + split_pos(i, b.nx)];
 }
 __global__ void k_mask_box(size_t n, const uint8_t *rowtype, double *x) {
@@ -79,14 +79,20 @@ __device__ inline void block_add(double v, double *dst) {
   }
 }
 // phi_{n-1}, phi_{n-2} (DA) -> extrapolation ex = 2 phi_{n-1} - phi_{n-2}
-// and feature planes f0 = phi_{n-1}, f1 = phi_{n-1} - phi_{n-2}, f3 = dof
+// and feature planes f0 = phi_{n-1}, f1 = phi_{n-1} - phi_{n-2}, f3 = dof;
+// prev = phi_{n-1} in box layout, zero on the rows without an equation
 __global__ void k_guess_prep(Grid g, Box b, const uint8_t *rt, const double *p1, const double *p2, double *ex,
-                             float *f0, float *f1, float *f3, double *sums) {
+                             double *prev, float *f0, float *f1, float *f3, double *sums) {
   double s0 = 0., s1 = 0., s3 = 0.;
   for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < b.n(); c += (size_t)gridDim.x * blockDim.x) {
-    const int i = c % b.nx + 1, j = (c / b.nx) % b.ny + 1, k = c / ((size_t)b.nx * b.ny) + 1;
-    const bool d = rt[c] == 1;
-    const double a = d ? p1[g.at(i, j, k)] : 0., q = d ? p2[g.at(i, j, k)] : 0.;
+    int i, j, k;
+    box_ijk(b, c, i, j, k);
+    i++; j++; k++;
+    const uint8_t t = rt[c];
+    const bool d = t == 1;
+    const double p = t ? p1[g.at(i, j, k)] : 0.;
+    const double a = d ? p : 0., q = d ? p2[g.at(i, j, k)] : 0.;
+    prev[c] = p;
     ex[c] = 2. * a - q;
     f0[c] = (float)a;
     f1[c] = (float)(a - q);
@@ -111,17 +117,21 @@ __global__ void k_guess_f2(size_t n, const uint8_t *rt, const double *aj, const 
 }
 // One pass over the FP64 operator for the two candidates the solver judges:
 // ra = b - A xa and rb = b - A xb (both stored), with ||ra||^2, ||rb||^2
-// and ||b||^2 as block partials in rows 0..2 of `partial`.
-__global__ void __launch_bounds__(256) k_residual64x2(Box b, const double *__restrict__ A,
+// and ||b||^2 as block partials in rows 0..2 of `partial` (grid
+// guess_grid: a thread takes kGuessRows j-rows of one column, one partial
+// per block).
+constexpr int kGuessRows = 8;
+__global__ void __launch_bounds__(128) k_residual64x2(Box b, const double *__restrict__ A,
                                                        const double *__restrict__ xa, const double *__restrict__ xb,
                                                        const double *__restrict__ rhs, double *__restrict__ ra,
                                                        double *__restrict__ rb, double *partial) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x, k = blockIdx.z;
   double s0 = 0., s1 = 0., s2 = 0.;
   const uint32_t n = (uint32_t)b.n();
-  for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < n; c += (size_t)gridDim.x * blockDim.x) {
-    const int i = c % b.nx, j = (c / b.nx) % b.ny, k = c / ((size_t)b.nx * b.ny);
+  for (int j = blockIdx.y * kGuessRows; i < b.nx && j < min(b.ny, (int)(blockIdx.y + 1) * kGuessRows); j++) {
     uint32_t idx[NSLOT];
     stencil_index(b, i, j, k, idx);
+    const uint32_t c = idx[CP];
     double ya = 0., yb = 0.;
 #pragma unroll
     for (int q = 0; q < NSLOT; q++) {
@@ -138,9 +148,11 @@ __global__ void __launch_bounds__(256) k_residual64x2(Box b, const double *__res
   }
   const double t0 = block_sum(s0), t1 = block_sum(s1), t2 = block_sum(s2);
   if (threadIdx.x == 0) {
-    partial[blockIdx.x] = t0;
-    partial[gridDim.x + blockIdx.x] = t1;
-    partial[2 * (size_t)gridDim.x + blockIdx.x] = t2;
+    const size_t nb = (size_t)gridDim.x * gridDim.y * gridDim.z;
+    const size_t blk = blockIdx.x + (size_t)gridDim.x * (blockIdx.y + (size_t)gridDim.y * blockIdx.z);
+    partial[blk] = t0;
+    partial[nb + blk] = t1;
+    partial[2 * nb + blk] = t2;
   }
 }
 __device__ inline double plane_rms(const double *sums, int q) {
@@ -162,7 +174,9 @@ __global__ void k_guess_target(Grid g, Box b, const uint8_t *rt, const double *p
                                const double *sums, float *tgt, float *wt) {
   const double s2 = plane_rms(sums, 2), inv = s2 > 0. ? 1. / s2 : 0.;
   for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < b.n(); c += (size_t)gridDim.x * blockDim.x) {
-    const int i = c % b.nx + 1, j = (c / b.nx) % b.ny + 1, k = c / ((size_t)b.nx * b.ny) + 1;
+    int i, j, k;
+    box_ijk(b, c, i, j, k);
+    i++; j++; k++;
     const bool d = rt[c] == 1;
     tgt[c] = d ? (float)((phi[g.at(i, j, k)] - ex[c]) * inv) : 0.f;
     wt[c] = d ? 1.f : 0.f;
@@ -175,7 +189,8 @@ __global__ void k_guess_restrict(Box b, const float *ff, const float *tf, float 
   const int cx = b.nx / 2, cy = b.ny / 2, cz = b.nz / 2;
   const size_t nc = (size_t)cx * cy * cz, nf = b.n();
   for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < nc; c += (size_t)gridDim.x * blockDim.x) {
-    const int I = c % cx, J = (c / cx) % cy, K = c / ((size_t)cx * cy);
+    const uint32_t row = (uint32_t)c / (uint32_t)cx;
+    const int I = (int)((uint32_t)c - row * (uint32_t)cx), J = (int)(row % (uint32_t)cy), K = (int)(row / (uint32_t)cy);
     float w = 0.f, s0 = 0.f, s1 = 0.f, s2 = 0.f, st = 0.f;
     for (int q = 0; q < 8; q++) {
       const size_t f = b.at(2 * I + (q & 1), 2 * J + ((q >> 1) & 1), 2 * K + (q >> 2));
@@ -201,7 +216,8 @@ __global__ void k_guess_restrict(Box b, const float *ff, const float *tf, float 
 __global__ void k_guess_prolong(Box b, const float *oc, float *of) {
   const int cx = b.nx / 2, cy = b.ny / 2, cz = b.nz / 2;
   for (size_t f = blockIdx.x * (size_t)blockDim.x + threadIdx.x; f < b.n(); f += (size_t)gridDim.x * blockDim.x) {
-    const int i = f % b.nx, j = (f / b.nx) % b.ny, k = f / ((size_t)b.nx * b.ny);
+    int i, j, k;
+    box_ijk(b, f, i, j, k);
     int I[2] = {i >> 1, (i & 1) ? (i >> 1) + 1 : (i >> 1) - 1};
     int J[2] = {j >> 1, (j & 1) ? (j >> 1) + 1 : (j >> 1) - 1};
     int K[2] = {k >> 1, (k & 1) ? (k >> 1) + 1 : (k >> 1) - 1};
@@ -222,7 +238,8 @@ __global__ void k_guess_prolong(Box b, const float *oc, float *of) {
 // null) zeroes the output off the dofs
 __global__ void k_guess_smooth(Box b, const float *in, float *out, int dir, const uint8_t *mask) {
   for (size_t f = blockIdx.x * (size_t)blockDim.x + threadIdx.x; f < b.n(); f += (size_t)gridDim.x * blockDim.x) {
-    const int i = f % b.nx, j = (f / b.nx) % b.ny, k = f / ((size_t)b.nx * b.ny);
+    int i, j, k;
+    box_ijk(b, f, i, j, k);
     size_t m = f, p = f;
     if (dir < 0) {
     } else if (dir == 0) {
@@ -239,6 +256,31 @@ __global__ void k_guess_smooth(Box b, const float *in, float *out, int dir, cons
     const float v = dir < 0 ? in[f] : 0.25f * in[m] + 0.5f * in[f] + 0.25f * in[p];
     out[f] = (mask && mask[f] != 1) ? 0.f : v;
   }
+}
+// One pass of the 27-point binomial filter (the tensor product of
+// (1/4, 1/2, 1/4) along x, y and z, clamped at the box faces); `mask` (may
+// be null) zeroes the output off the dofs.
+__global__ void __launch_bounds__(128) k_guess_smooth3(Box b, const float *__restrict__ in, float *__restrict__ out,
+                                                        const uint8_t *__restrict__ mask) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y, k = blockIdx.z;
+  if (i >= b.nx) return;
+  const int xs[3] = {max(i - 1, 0), i, min(i + 1, b.nx - 1)};
+  const int ys[3] = {max(j - 1, 0), j, min(j + 1, b.ny - 1)};
+  const int zs[3] = {max(k - 1, 0), k, min(k + 1, b.nz - 1)};
+  const float w[3] = {0.25f, 0.5f, 0.25f};
+  float s = 0.f;
+#pragma unroll
+  for (int c = 0; c < 3; c++) {
+    float sy = 0.f;
+#pragma unroll
+    for (int bb = 0; bb < 3; bb++) {
+      const float *row = in + ((size_t)zs[c] * b.ny + ys[bb]) * b.nx;
+      sy += w[bb] * (0.25f * __ldg(&row[xs[0]]) + 0.5f * __ldg(&row[xs[1]]) + 0.25f * __ldg(&row[xs[2]]));
+    }
+    s += w[c] * sy;
+  }
+  const size_t f = ((size_t)k * b.ny + j) * b.nx + i;
+  out[f] = (mask && mask[f] != 1) ? 0.f : s;
 }
 // The learned correction enters the guess band by band: cells are grouped
 // by their index distance to the nearest non-periodic y wall (where
@@ -260,46 +302,50 @@ __device__ inline int guess_band(const Box &b, int j) {
 // r = b - A ex.  A neighbour's band follows from its j offset.  The fit
 // only has to be good, not exact: the candidate it produces is then
 // measured by its FP64 residual.
-__global__ void __launch_bounds__(256) k_guess_gram(Box b, const float *__restrict__ A, const double *__restrict__ scale,
+__global__ void __launch_bounds__(128) k_guess_gram(Box b, const float *__restrict__ A, const double *__restrict__ scale,
                                                      const float *__restrict__ c, const double *__restrict__ r,
                                                      double kappa, const double *sums, double *partial) {
   const float sc = (float)(kappa * plane_rms(sums, 2));
   float acc[14];
   for (int q = 0; q < 14; q++) acc[q] = 0.f;
+  const int p = blockIdx.x * blockDim.x + threadIdx.x, k = blockIdx.z;
   const uint32_t n = (uint32_t)b.n();
-  for (size_t cs = blockIdx.x * (size_t)blockDim.x + threadIdx.x; cs < n; cs += (size_t)gridDim.x * blockDim.x) {
-    const int p = cs % b.nx, j = (cs / b.nx) % b.ny, k = cs / ((size_t)b.nx * b.ny);
+  for (int j = blockIdx.y * kGuessRows; p < b.nx && j < min(b.ny, (int)(blockIdx.y + 1) * kGuessRows); j++) {
     const int i = split_cell(p, b.nx);
     uint32_t idx[NSLOT];
     stencil_index(b, i, j, k, idx);
+    const uint32_t cs = idx[CP] - i + p;
     const double sr = scale[idx[CP]];
-    if (sr == 0.) continue;
-    const int bm = guess_band(b, j > 0 ? j - 1 : j), b0 = guess_band(b, j),
-              bp = guess_band(b, j < b.ny - 1 ? j + 1 : j);
-    float y[kGuessBands] = {0.f, 0.f, 0.f, 0.f};
+    if (sr != 0.) {
+      const int bm = guess_band(b, j > 0 ? j - 1 : j), b0 = guess_band(b, j),
+                bp = guess_band(b, j < b.ny - 1 ? j + 1 : j);
+      float y[kGuessBands] = {0.f, 0.f, 0.f, 0.f};
 #pragma unroll
-    for (int t = 0; t < NSLOT; t++) {
-      int di, dj, dk;
-      slot_offset(t, di, dj, dk);
-      const int bt = dj < 0 ? bm : (dj > 0 ? bp : b0);
-      const float term = __ldcs(&A[(size_t)t * n + cs]) * __ldg(&c[idx[t]]);
+      for (int t = 0; t < NSLOT; t++) {
+        int di, dj, dk;
+        slot_offset(t, di, dj, dk);
+        const int bt = dj < 0 ? bm : (dj > 0 ? bp : b0);
+        const float term = __ldcs(&A[(size_t)t * n + cs]) * __ldg(&c[idx[t]]);
 #pragma unroll
-      for (int u = 0; u < kGuessBands; u++) y[u] += bt == u ? term : 0.f;
+        for (int u = 0; u < kGuessBands; u++) y[u] += bt == u ? term : 0.f;
+      }
+      const float inv = (float)(1. / sr), rv = (float)r[idx[CP]];
+      int q = 0;
+#pragma unroll
+      for (int u = 0; u < kGuessBands; u++) {
+        y[u] *= sc * inv;
+#pragma unroll
+        for (int v = u; v < kGuessBands; v++) acc[q++] += y[u] * y[v];
+      }
+#pragma unroll
+      for (int u = 0; u < kGuessBands; u++) acc[10 + u] += y[u] * rv;
     }
-    const float inv = (float)(1. / sr), rv = (float)r[idx[CP]];
-    int q = 0;
-#pragma unroll
-    for (int u = 0; u < kGuessBands; u++) {
-      y[u] *= sc * inv;
-#pragma unroll
-      for (int v = u; v < kGuessBands; v++) acc[q++] += y[u] * y[v];
-    }
-#pragma unroll
-    for (int u = 0; u < kGuessBands; u++) acc[10 + u] += y[u] * rv;
   }
+  const size_t nb = (size_t)gridDim.x * gridDim.y * gridDim.z;
+  const size_t blk = blockIdx.x + (size_t)gridDim.x * (blockIdx.y + (size_t)gridDim.y * blockIdx.z);
   for (int q = 0; q < 14; q++) {
     const double t = block_sum((double)acc[q]);
-    if (threadIdx.x == 0) partial[(size_t)q * gridDim.x + blockIdx.x] = t;
+    if (threadIdx.x == 0) partial[(size_t)q * nb + blk] = t;
   }
 }
 // learned guess x = ex + kappa * rms(f2) * alpha[band] * out on dofs
@@ -307,7 +353,7 @@ __global__ void k_guess_compose(Box b, const uint8_t *rt, const double *ex, cons
                                 const double *sums, BandWeights w, double *x) {
   const double s = kappa * plane_rms(sums, 2);
   for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < b.n(); c += (size_t)gridDim.x * blockDim.x)
-    x[c] = rt[c] == 1 ? ex[c] + s * w.a[guess_band(b, (c / b.nx) % b.ny)] * (double)out[c] : 0.;
+    x[c] = rt[c] == 1 ? ex[c] + s * w.a[guess_band(b, (int)(((uint32_t)c / (uint32_t)b.nx) % (uint32_t)b.ny))] * (double)out[c] : 0.;
 }
 
 __device__ inline void atomic_max_pos(double *addr, double v) {
@@ -466,6 +512,15 @@ int upload(vfs_poisson *h, double *dst, const double *src, size_t count) {
                            is_device_ptr(src) ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, h->stream));
   return VFS_OK;
 }
+// device memory is read where it lies; host memory is staged
+int device_view(vfs_poisson *h, const double *src, double *stage, size_t count, const double **out) {
+  if (is_device_ptr(src)) {
+    *out = src;
+    return VFS_OK;
+  }
+  *out = stage;
+  return upload(h, stage, src, count);
+}
 int download(vfs_poisson *h, double *dst, const double *src, size_t count) {
   CUDA_TRY(cudaMemcpyAsync(dst, src, count * sizeof(double),
                            is_device_ptr(dst) ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, h->stream));
@@ -480,6 +535,8 @@ int sync(vfs_poisson *h) {
 dim3 da_grid(const Grid &g, int bx = 128) { return dim3((g.mx + bx - 1) / bx, g.my, g.mz); }
 dim3 box_grid(const Box &b, int bx = 128) { return dim3((b.nx + bx - 1) / bx, b.ny, b.nz); }
 unsigned lin_grid(size_t n, int bx = 256) { return (unsigned)((n + bx - 1) / bx); }
+// grid of the guess's reduction kernels: 128 columns x kGuessRows j-rows
+dim3 guess_grid(const Box &b) { return dim3((b.nx + 127) / 128, (b.ny + kGuessRows - 1) / kGuessRows, b.nz); }
 
 #define LAUNCH(h, kern, grid, block, ...)                          \
   do {                                                             \
@@ -1264,7 +1321,11 @@ int vfs_poisson_create(const vfs_grid_desc *gd, vfs_poisson **out) {
     return bail(rc);
   const int nblk = (int)((n + 1023) / 1024);
   if ((rc = dalloc(h, &h->blk, nblk))) return bail(rc);
-  h->partial_len = std::max<size_t>(n / 16 + 65536, (size_t)(kGsUU + 2) * ((n + 2047) / 2048) + 4096);
+  {
+    const dim3 gb = guess_grid(h->box);  // 14 rows of per-block partials (k_guess_gram)
+    h->partial_len = std::max<size_t>({n / 16 + 65536, (size_t)(kGsUU + 2) * ((n + 2047) / 2048) + 4096,
+                                       (size_t)16 * gb.x * gb.y * gb.z + 4096});
+  }
   if ((rc = dalloc(h, &h->partial, h->partial_len))) return bail(rc);
   if (cudaMallocHost(&h->hbuf, 1024 * 8) != cudaSuccess) { cudaGetLastError(); return bail(fail(VFS_ENOMEM, "pinned alloc")); }
   cudaMemsetAsync(h->phi_da, 0, N * 8, h->stream);
@@ -1531,20 +1592,21 @@ int guess_features(vfs_poisson *h, const double *phi_nm1, const double *phi_nm2,
   TRY(guess_buffers(h));
   float *feat = h->gfeat;
   const size_t n = h->box.n(), N = h->g.n();
-  TRY(upload(h, h->stage, phi_nm1, N));
-  TRY(upload(h, h->stage + N, phi_nm2, N));
+  const double *p1, *p2;
+  TRY(device_view(h, phi_nm1, h->stage, N, &p1));
+  TRY(device_view(h, phi_nm2, h->stage + N, N, &p2));
   CUDA_TRY(cudaMemsetAsync(h->gsum, 0, 8 * sizeof(double), h->stream));
-  LAUNCH(h, k_guess_prep, kRedBlocks, 256, h->g, h->box, h->rowtype0, h->stage, h->stage + N, h->gex, feat,
-         feat + n, feat + 3 * n, h->gsum);
   TRY(ensure_krylov(h, std::max(h->m_alloc, 20)));
   double *prev = h->Z[0];  // free until the next solve
-  LAUNCH(h, k_da_to_box, lin_grid(n), 256, h->g, h->box, h->stage, prev);
-  LAUNCH(h, k_mask_box, lin_grid(n), 256, n, h->rowtype0, prev);
-  LAUNCH(h, k_residual64x2, kRedBlocks, 256, h->box, h->A0, h->gex, prev, h->b, h->r, h->rprev, h->partial);
+  LAUNCH(h, k_guess_prep, kRedBlocks, 256, h->g, h->box, h->rowtype0, p1, p2, h->gex, prev, feat, feat + n,
+         feat + 3 * n, h->gsum);
+  const dim3 gr = guess_grid(h->box);
+  const int nbox = (int)(gr.x * gr.y * gr.z);
+  LAUNCH(h, k_residual64x2, gr, 128, h->box, h->A0, h->gex, prev, h->b, h->r, h->rprev, h->partial);
   LAUNCH(h, k_guess_f2, kRedBlocks, 256, n, h->rowtype0, (const double *)h->aj_box, h->r, feat + 2 * n, h->gsum);
   LAUNCH(h, k_guess_scale, kRedBlocks, 256, n, feat, h->gsum);
   double nr[3];
-  TRY(reduce_read(h, kRedBlocks, 3, nr));
+  TRY(reduce_read(h, nbox, 3, nr));
   if (norms) for (int q = 0; q < 3; q++) norms[q] = nr[q];
   return VFS_OK;
 }
@@ -1604,21 +1666,22 @@ int vfs_poisson_learned_guess(vfs_poisson *h, vfs_unet *u, const double *phi_nm1
   if (h->phase) cudaEventRecord(h->phev[2], h->stream);
   LAUNCH(h, k_guess_prolong, kRedBlocks, 256, b, h->gout, h->gof[0]);
   int cur = 0;
-  // gsmooth passes of the 27-point binomial filter, each as three 1-D passes;
-  // the last one also zeroes the correction off the dofs
-  for (int p = 0; p < std::max(h->gsmooth, 1); p++)
-    for (int dir = 0; dir < 3; dir++, cur ^= 1) {
-      const bool last = p == std::max(h->gsmooth, 1) - 1 && dir == 2;
-      if (h->gsmooth == 0 && !last) continue;
-      LAUNCH(h, k_guess_smooth, kRedBlocks, 256, b, h->gof[cur], h->gof[cur ^ 1], h->gsmooth == 0 ? -1 : dir,
-             last ? (const uint8_t *)h->rowtype0 : nullptr);
-    }
+  // gsmooth passes of the 27-point binomial filter; the last one also
+  // zeroes the correction off the dofs (gsmooth 0: only the masking)
+  if (h->gsmooth == 0) {
+    LAUNCH(h, k_guess_smooth, kRedBlocks, 256, b, h->gof[cur], h->gof[cur ^ 1], -1, (const uint8_t *)h->rowtype0);
+    cur ^= 1;
+  }
+  for (int p = 0; p < h->gsmooth; p++, cur ^= 1)
+    LAUNCH(h, k_guess_smooth3, box_grid(b), 128, b, h->gof[cur], h->gof[cur ^ 1],
+           p == h->gsmooth - 1 ? (const uint8_t *)h->rowtype0 : nullptr);
   // least-squares band weights: minimise ||r_ex - sum_k alpha_k y_k||
   // (alpha = 0 is the plain extrapolation, so the guess is never worse)
-  LAUNCH(h, k_guess_gram, kRedBlocks, 256, b, h->L[0].A32, (const double *)h->scale, h->gof[cur], h->r, kappa,
-         h->gsum, h->partial);
+  const dim3 gg = guess_grid(b);
+  LAUNCH(h, k_guess_gram, gg, 128, b, h->L[0].A32, (const double *)h->scale, h->gof[cur], h->r, kappa, h->gsum,
+         h->partial);
   double gm[14];
-  TRY(reduce_read(h, kRedBlocks, 14, gm));
+  TRY(reduce_read(h, (int)(gg.x * gg.y * gg.z), 14, gm));
   BandWeights bw{};
   {
     // the normal equations G alpha = g (symmetric positive semi-definite)

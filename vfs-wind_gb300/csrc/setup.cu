@@ -212,7 +212,8 @@ __global__ void k_count_dofs(Grid g, Box b, const double *nvert, int *block_coun
   size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   int f = 0;
   if (c < b.n()) {
-    int i = c % b.nx, j = (c / b.nx) % b.ny, k = c / ((size_t)b.nx * b.ny);
+    int i, j, k;
+    box_ijk(b, c, i, j, k);
     f = is_dof_cell(g, nvert, i + 1, j + 1, k + 1) ? 1 : 0;
   }
   int s = block_sum<int>(f);
@@ -242,7 +243,8 @@ __global__ void k_number_dofs(Grid g, Box b, const double *nvert, const int *blo
   size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   int f = 0;
   if (c < b.n()) {
-    int i = c % b.nx, j = (c / b.nx) % b.ny, k = c / ((size_t)b.nx * b.ny);
+    int i, j, k;
+    box_ijk(b, c, i, j, k);
     f = is_dof_cell(g, nvert, i + 1, j + 1, k + 1) ? 1 : 0;
   }
   int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -539,7 +541,8 @@ __global__ void k_level_masks(Grid g, Box b, const double *nvert, uint8_t *blank
                               double *aj_box, const double *aj_da) {
   size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= b.n()) return;
-  int i = c % b.nx, j = (c / b.nx) % b.ny, k = c / ((size_t)b.nx * b.ny);
+  int i, j, k;
+  box_ijk(b, c, i, j, k);
   double nv = nvert[g.at(i + 1, j + 1, k + 1)];
   blank[c] = nv > 0.1 ? 1 : 0;
   double w = 1 - nv > 0. ? 1 - nv : 0.;
@@ -558,7 +561,9 @@ __global__ void k_rhs(Grid g, Box b, const double *__restrict__ nvert, const dou
   double sb = 0, sa = 0;
   const size_t n = b.n();
   for (size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (size_t)gridDim.x * blockDim.x) {
-    int i = c % b.nx + 1, j = (c / b.nx) % b.ny + 1, k = c / ((size_t)b.nx * b.ny) + 1;
+    int i, j, k;
+    box_ijk(b, c, i, j, k);
+    i++; j++; k++;
     size_t t = g.at(i, j, k);
     double val = 0.;
     if (nvert[t] < 0.1) {
@@ -594,7 +599,9 @@ __global__ void k_rhs2(Grid g, Box b, const double *__restrict__ nvert, const ui
   double sb = 0, cnt = 0;
   const size_t n = b.n();
   for (size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (size_t)gridDim.x * blockDim.x) {
-    int i = c % b.nx + 1, j = (c / b.nx) % b.ny + 1, k = c / ((size_t)b.nx * b.ny) + 1;
+    int i, j, k;
+    box_ijk(b, c, i, j, k);
+    i++; j++; k++;
     size_t t = g.at(i, j, k);
     double val = 0.;
     if (nvert[t] < 0.1) {
@@ -627,7 +634,9 @@ __global__ void k_rhs2_shift(Grid g, Box b, const double *__restrict__ nvert, co
   const double val = -sums[0] / (sums[1] > 0. ? sums[1] : 1.);
   const size_t n = b.n();
   for (size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (size_t)gridDim.x * blockDim.x) {
-    int i = c % b.nx + 1, j = (c / b.nx) % b.ny + 1, k = c / ((size_t)b.nx * b.ny) + 1;
+    int i, j, k;
+    box_ijk(b, c, i, j, k);
+    i++; j++; k++;
     size_t t = g.at(i, j, k);
     if (nvert[t] < 0.1) {
       rhs[c] += val;
@@ -652,7 +661,9 @@ __global__ void k_rhs_nullspace(Grid g, Box b, const double *__restrict__ nvert,
   const double sum = sums[0], sum_aj = sums[1];
   const size_t n = b.n();
   for (size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (size_t)gridDim.x * blockDim.x) {
-    int i = c % b.nx + 1, j = (c / b.nx) % b.ny + 1, k = c / ((size_t)b.nx * b.ny) + 1;
+    int i, j, k;
+    box_ijk(b, c, i, j, k);
+    i++; j++; k++;
     size_t t = g.at(i, j, k);
     if (nvert[t] < 0.1) {
       double val = -sum * aj[t] / sum_aj;
@@ -681,7 +692,9 @@ __global__ void k_shift_fluid(Box b, const uint8_t *fluid, const double *sums, d
 __global__ void k_fluid_mask(Grid g, Box b, const double *nvert, uint8_t *fluid) {
   size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= b.n()) return;
-  int i = c % b.nx + 1, j = (c / b.nx) % b.ny + 1, k = c / ((size_t)b.nx * b.ny) + 1;
+  int i, j, k;
+  box_ijk(b, c, i, j, k);
+  i++; j++; k++;
   fluid[c] = nvert[g.at(i, j, k)] < 0.1 ? 1 : 0;
 }
 
@@ -701,7 +714,9 @@ __global__ void k_box_to_da_phi(Grid g, Box b, const double *nvert, const double
 __global__ void k_da_to_box(Grid g, Box b, const double *da, double *x) {
   size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= b.n()) return;
-  int i = c % b.nx + 1, j = (c / b.nx) % b.ny + 1, k = c / ((size_t)b.nx * b.ny) + 1;
+  int i, j, k;
+  box_ijk(b, c, i, j, k);
+  i++; j++; k++;
   x[c] = da[g.at(i, j, k)];
 }
 __global__ void k_box_to_da(Grid g, Box b, const double *x, double *da) {
@@ -866,7 +881,9 @@ __global__ void k_divergence(Grid g, Box b, const double *__restrict__ nvert, co
   double best = 0.;
   const size_t n = b.n();
   for (size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (size_t)gridDim.x * blockDim.x) {
-    int i = c % b.nx + 1, j = (c / b.nx) % b.ny + 1, k = c / ((size_t)b.nx * b.ny) + 1;
+    int i, j, k;
+    box_ijk(b, c, i, j, k);
+    i++; j++; k++;
 #define U(a, bb, cc, q) ucont[g.at(a, bb, cc) * 3 + (q)]
 #define NV(a, bb, cc) nvert[g.at(a, bb, cc)]
     double v = fabs((U(i, j, k, 0) - U(i - 1, j, k, 0) + U(i, j, k, 1) - U(i, j - 1, k, 1) + U(i, j, k, 2) -

@@ -623,7 +623,7 @@ __global__ void k_sumsq(size_t n, const double *__restrict__ x, double *partial)
   __global__ void k_cast_planes_##S(const double *src, T *dst, size_t n) { cast_body<T>(src, dst, n); }
 // the line kernel keeps a whole chunk in registers: 16 columns per block
 // (at most 24 chunks each) so that neither precision spills
-TYPED(float, f32, 384, 3)
+TYPED(float, f32, 384, 1)
 TYPED(double, f64, 384, 1)
 #undef TYPED
 

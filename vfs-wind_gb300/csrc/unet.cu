@@ -282,7 +282,8 @@ __global__ void k_input(const float *feat, int fx, int fy, int fz, int ox, int o
   const size_t n = (size_t)nx * ny * nz;
   const size_t plane = (size_t)fx * fy * fz;
   for (size_t v = blockIdx.x * (size_t)blockDim.x + threadIdx.x; v < n; v += (size_t)gridDim.x * blockDim.x) {
-    const int x = (int)(v % nx), y = (int)((v / nx) % ny), z = (int)(v / ((size_t)nx * ny));
+    const uint32_t vr = (uint32_t)v / (uint32_t)nx;  // < 2^32 voxels
+    const int x = (int)((uint32_t)v - vr * (uint32_t)nx), y = (int)(vr % (uint32_t)ny), z = (int)(vr / (uint32_t)ny);
     const size_t s = ((size_t)(z + oz) * fy + (y + oy)) * fx + (x + ox);
     __align__(16) bf16 row[16];
     for (int c = 0; c < 16; c++) row[c] = __float2bfloat16_rn(c < 4 ? feat[c * plane + s] : 0.f);
@@ -316,7 +317,8 @@ __global__ void k_pool_bwd(const float *gc, int nx, int ny, int nz, int C, float
   for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
     const int c = (int)(e % C);
     const size_t v = e / C;
-    const int x = (int)(v % nx), y = (int)((v / nx) % ny), z = (int)(v / ((size_t)nx * ny));
+    const uint32_t vr = (uint32_t)v / (uint32_t)nx;  // < 2^32 voxels
+    const int x = (int)((uint32_t)v - vr * (uint32_t)nx), y = (int)(vr % (uint32_t)ny), z = (int)(vr / (uint32_t)ny);
     gf[e] += 0.125f * gc[(((size_t)(z >> 1) * cy + (y >> 1)) * cx + (x >> 1)) * C + c];
   }
 }
@@ -378,7 +380,8 @@ __global__ void k_weight_sum(const float *wt, int fx, int fy, int ox, int oy, in
   const size_t n = (size_t)nx * ny * nz;
   float s = 0.f;
   for (size_t v = blockIdx.x * (size_t)blockDim.x + threadIdx.x; v < n; v += (size_t)gridDim.x * blockDim.x) {
-    const int x = (int)(v % nx), y = (int)((v / nx) % ny), z = (int)(v / ((size_t)nx * ny));
+    const uint32_t vr = (uint32_t)v / (uint32_t)nx;  // < 2^32 voxels
+    const int x = (int)((uint32_t)v - vr * (uint32_t)nx), y = (int)(vr % (uint32_t)ny), z = (int)(vr / (uint32_t)ny);
     s += wt[((size_t)(z + oz) * fy + (y + oy)) * fx + (x + ox)];
   }
   s = block_sum(s, sh);
@@ -409,7 +412,8 @@ __global__ void k_head(const bf16 *d, size_t n, const float *wh, float *out, con
     for (int c = 0; c < 16; c++) o += dv[c] * wh[c];
     if (out) out[v] = o;
     if (tgt) {
-      const int x = (int)(v % nx), y = (int)((v / nx) % ny), z = (int)(v / ((size_t)nx * ny));
+      const uint32_t vr = (uint32_t)v / (uint32_t)nx;  // < 2^32 voxels
+      const int x = (int)((uint32_t)v - vr * (uint32_t)nx), y = (int)(vr % (uint32_t)ny), z = (int)(vr / (uint32_t)ny);
       const size_t s = ((size_t)(z + oz) * fy + (y + oy)) * fx + (x + ox);
       const float w = wt[s] * inv, e = o - tgt[s];
       ls += w * e * e;

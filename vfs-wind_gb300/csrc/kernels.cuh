@@ -111,9 +111,11 @@ __global__ void k_gs_coef(int nv, double *red);
 __global__ void k_gs_update(size_t n, int nv, const double *const *Q, const double *red, double *u, double *w,
                             double *partial);
 __global__ void k_axpy_multi(size_t n, int nv, const double *const *Z, const double *coef, double *x);
-__global__ void k_scale_to(size_t n, const double *v, double s, const double *nrm2, const double *scale,
-                           float *out32, double *out64);
-__global__ void k_to64(size_t n, const float *x32, const double *x64, double s, double *out);
+__global__ void k_scale_to(size_t n, const double *v, double s, const double *sinv, const double *scale,
+                           double *out);
+__global__ void k_scale_to32(size_t n, const double *v, float s, const float *sinv, const float *scale, float *out);
+__global__ void k_reduce_norm(const double *partial, int nb, double *out, float *out32);
+__global__ void k_to64(size_t n, const float *x32, const double *x64, double *out);
 __global__ void k_sumsq(size_t n, const double *x, double *partial);
 
 // Hand-off from a handle to the surface search (ibm.cu): its stream, grid,

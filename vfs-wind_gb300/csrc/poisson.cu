@@ -80,10 +80,13 @@ __device__ inline void block_add(double v, double *dst) {
 }
 // phi_{n-1}, phi_{n-2} (DA) -> extrapolation ex = 2 phi_{n-1} - phi_{n-2}
 // and feature planes f0 = phi_{n-1}, f1 = phi_{n-1} - phi_{n-2}, f3 = dof;
-// prev = phi_{n-1} in box layout, zero on the rows without an equation
+// prev = phi_{n-1} in box layout (and in FP32), zero on the rows without an
+// equation
 __global__ void k_guess_prep(Grid g, Box b, const uint8_t *rt, const double *p1, const double *p2, double *ex,
-                             double *prev, float *f0, float *f1, float *f3, double *sums) {
-  double s0 = 0., s1 = 0., s3 = 0.;
+                             double *prev, float *prev32, float *f0, float *f1, float *f3, double *sums) {
+  // the plane sums only set the feature scales: FP32 per thread
+  float s0 = 0.f, s1 = 0.f;
+  int s3 = 0;
   for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < b.n(); c += (size_t)gridDim.x * blockDim.x) {
     int i, j, k;
     box_ijk(b, c, i, j, k);
@@ -92,18 +95,20 @@ __global__ void k_guess_prep(Grid g, Box b, const uint8_t *rt, const double *p1,
     const bool d = t == 1;
     const double p = t ? p1[g.at(i, j, k)] : 0.;
     const double a = d ? p : 0., q = d ? p2[g.at(i, j, k)] : 0.;
+    const float pf = (float)p, af = d ? pf : 0.f, df = (float)(a - q);
     prev[c] = p;
+    prev32[c] = pf;
     ex[c] = 2. * a - q;
-    f0[c] = (float)a;
-    f1[c] = (float)(a - q);
+    f0[c] = af;
+    f1[c] = df;
     f3[c] = d ? 1.f : 0.f;
-    s0 += a * a;
-    s1 += (a - q) * (a - q);
-    s3 += d ? 1. : 0.;
+    s0 = fmaf(af, af, s0);
+    s1 = fmaf(df, df, s1);
+    s3 += d ? 1 : 0;
   }
-  block_add(s0, sums);
-  block_add(s1, sums + 1);
-  block_add(s3, sums + 3);
+  block_add((double)s0, sums);
+  block_add((double)s1, sums + 1);
+  block_add((double)s3, sums + 3);
 }
 // f2 = aj * (b - A ex): the extrapolation residual of the aj-scaled system
 __global__ void k_guess_f2(size_t n, const uint8_t *rt, const double *aj, const double *r, float *f2, double *sums) {
@@ -115,38 +120,49 @@ __global__ void k_guess_f2(size_t n, const uint8_t *rt, const double *aj, const 
   }
   block_add(s, sums + 2);
 }
-// One pass over the FP64 operator for the two candidates the solver judges:
-// ra = b - A xa and rb = b - A xb (both stored), with ||ra||^2, ||rb||^2
-// and ||b||^2 as block partials in rows 0..2 of `partial` (grid
-// guess_grid: a thread takes kGuessRows j-rows of one column, one partial
-// per block).
+// The two candidates the solver judges: ra = b - A xa in FP64 (stored: the
+// residual FGMRES starts from when xa is chosen) and the norm of
+// rb = b - A xb estimated in FP32 from the packed level-0 operator (its rows
+// are the aj-scaled ones, so each is divided by its row scale) with xb in
+// FP32 -- FP64 arithmetic is the scarce pipe and a judgement needs a few
+// digits.  ||ra||^2, the estimate of ||rb||^2 and ||b||^2 go to rows 0..2
+// of `partial` (grid guess_grid: a thread takes kGuessRows j-rows of one
+// column, one partial per block).
 constexpr int kGuessRows = 8;
-__global__ void __launch_bounds__(128) k_residual64x2(Box b, const double *__restrict__ A,
-                                                       const double *__restrict__ xa, const double *__restrict__ xb,
-                                                       const double *__restrict__ rhs, double *__restrict__ ra,
-                                                       double *__restrict__ rb, double *partial) {
+__global__ void __launch_bounds__(128) k_guess_residuals(Box b, const double *__restrict__ A,
+                                                          const __half2 *__restrict__ C, const float *__restrict__ D,
+                                                          const float *__restrict__ scale, const double *__restrict__ xa,
+                                                          const float *__restrict__ xb, const double *__restrict__ rhs,
+                                                          double *__restrict__ ra, double *partial) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x, k = blockIdx.z;
-  double s0 = 0., s1 = 0., s2 = 0.;
+  double s0 = 0., s2 = 0.;
+  float s1 = 0.f;
   const uint32_t n = (uint32_t)b.n();
   for (int j = blockIdx.y * kGuessRows; i < b.nx && j < min(b.ny, (int)(blockIdx.y + 1) * kGuessRows); j++) {
     uint32_t idx[NSLOT];
     stencil_index(b, i, j, k, idx);
-    const uint32_t c = idx[CP];
-    double ya = 0., yb = 0.;
+    const uint32_t c = idx[CP], cs = c - i + split_pos(i, b.nx);
+    double ya = 0.;
 #pragma unroll
-    for (int q = 0; q < NSLOT; q++) {
-      const double a = __ldcs(&A[(size_t)q * n + c]);
-      ya = fma(a, __ldg(&xa[idx[q]]), ya);
-      yb = fma(a, __ldg(&xb[idx[q]]), yb);
+    for (int q = 0; q < NSLOT; q++) ya = fma(__ldcs(&A[(size_t)q * n + c]), __ldg(&xa[idx[q]]), ya);
+    const float xc = __ldg(&xb[c]);
+    float t = 0.f;
+#pragma unroll
+    for (int m = 0; m < 9; m++) {
+      const float2 f = __half22float2(__ldcs(&C[(size_t)m * n + cs]));
+      t = fmaf(f.x, __ldg(&xb[idx[2 * m + 1]]) - xc, t);
+      t = fmaf(f.y, __ldg(&xb[idx[2 * m + 2]]) - xc, t);
     }
-    const double bv = rhs[c], va = bv - ya, vb = bv - yb;
+    t = fmaf(__half22float2(__ldcs(&C[(size_t)9 * n + cs])).x, xc, t);
+    const double bv = rhs[c], va = bv - ya;
+    const float sc = scale[c];
+    const float vb = sc != 0.f ? (float)bv - __ldcs(&D[cs]) * t / sc : (float)bv;
     ra[c] = va;
-    rb[c] = vb;
     s0 += va * va;
-    s1 += vb * vb;
+    s1 = fmaf(vb, vb, s1);
     s2 += bv * bv;
   }
-  const double t0 = block_sum(s0), t1 = block_sum(s1), t2 = block_sum(s2);
+  const double t0 = block_sum(s0), t1 = block_sum((double)s1), t2 = block_sum(s2);
   if (threadIdx.x == 0) {
     const size_t nb = (size_t)gridDim.x * gridDim.y * gridDim.z;
     const size_t blk = blockIdx.x + (size_t)gridDim.x * (blockIdx.y + (size_t)gridDim.y * blockIdx.z);
@@ -302,7 +318,7 @@ __device__ inline int guess_band(const Box &b, int j) {
 // r = b - A ex.  A neighbour's band follows from its j offset.  The fit
 // only has to be good, not exact: the candidate it produces is then
 // measured by its FP64 residual.
-__global__ void __launch_bounds__(128) k_guess_gram(Box b, const float *__restrict__ A, const double *__restrict__ scale,
+__global__ void __launch_bounds__(128) k_guess_gram(Box b, const float *__restrict__ A, const float *__restrict__ scale,
                                                      const float *__restrict__ c, const double *__restrict__ r,
                                                      double kappa, const double *sums, double *partial) {
   const float sc = (float)(kappa * plane_rms(sums, 2));
@@ -315,8 +331,8 @@ __global__ void __launch_bounds__(128) k_guess_gram(Box b, const float *__restri
     uint32_t idx[NSLOT];
     stencil_index(b, i, j, k, idx);
     const uint32_t cs = idx[CP] - i + p;
-    const double sr = scale[idx[CP]];
-    if (sr != 0.) {
+    const float sr = scale[idx[CP]];
+    if (sr != 0.f) {
       const int bm = guess_band(b, j > 0 ? j - 1 : j), b0 = guess_band(b, j),
                 bp = guess_band(b, j < b.ny - 1 ? j + 1 : j);
       float y[kGuessBands] = {0.f, 0.f, 0.f, 0.f};
@@ -329,7 +345,7 @@ __global__ void __launch_bounds__(128) k_guess_gram(Box b, const float *__restri
 #pragma unroll
         for (int u = 0; u < kGuessBands; u++) y[u] += bt == u ? term : 0.f;
       }
-      const float inv = (float)(1. / sr), rv = (float)r[idx[CP]];
+      const float inv = 1.f / sr, rv = (float)r[idx[CP]];
       int q = 0;
 #pragma unroll
       for (int u = 0; u < kGuessBands; u++) {
@@ -426,6 +442,7 @@ struct vfs_poisson {
   MetricPtrs met{};
   // fine operator and masks (box layout)
   double *A0 = nullptr, *scale = nullptr, *pc = nullptr, *aj_box = nullptr;
+  float *scale32 = nullptr;  // the row scale in FP32 (the FP32 V-cycle's right-hand side)
   uint8_t *rowtype0 = nullptr, *fluid = nullptr;
   int *gid_box = nullptr, *gid_da = nullptr, *blk = nullptr, *total = nullptr;
   int ndof = 0;
@@ -434,7 +451,9 @@ struct vfs_poisson {
   int m_alloc = 0;
   std::vector<double *> V, Z;
   double **dV = nullptr, **dZ = nullptr;
+  // dsv[2q] = ||V_q||^2 and dsv[2q+1] = 1 / ||V_q||; dsv32[q] the latter in FP32
   double *partial = nullptr, *red = nullptr, *coef = nullptr, *dsv = nullptr;
+  float *dsv32 = nullptr;
   size_t partial_len = 0;
   double *hbuf = nullptr;  // pinned host readback
   // learned initial guess: extrapolated phi, plane sums, feature planes and
@@ -445,6 +464,7 @@ struct vfs_poisson {
   // residual of the iterate installed by the learned guess, handed to the
   // next solve (warm_start 2) so that it does not form it again
   double *rprev = nullptr, *rlearn = nullptr, *r0 = nullptr;
+  float *prev32 = nullptr;
   double *ucat = nullptr;  // Contra2Cart output staging (3 per DA point)
   // level-set variant of the operator and projection (vfs_poisson_set_levelset)
   double *ls_rho = nullptr, *ls_level = nullptr;
@@ -996,19 +1016,20 @@ int run_vcycle(vfs_poisson *h, const vfs_solve_opts &o) {
 }
 
 // z = M (s v): aj row scaling, one V-cycle of the chosen precision, back to
-// FP64.  With nrm2 (device) set, v is also divided by sqrt(nrm2[0]).
-int precondition(vfs_poisson *h, const double *v, double s, const double *nrm2, double *z,
+// FP64.  With sinv64 / sinv32 (device) set, v is also multiplied by
+// sinv64[0] (FP64 V-cycle) or sinv32[0] (FP32 V-cycle).
+int precondition(vfs_poisson *h, const double *v, double s, const double *sinv64, const float *sinv32, double *z,
                  const vfs_solve_opts &o) {
   Level &l0 = h->L[0];
   const size_t n = h->box.n();
   if (o.precision == 0) {
-    LAUNCH(h, k_scale_to, kRedBlocks, 256, n, v, s, nrm2, h->scale, l0.v32[1], (double *)nullptr);
+    LAUNCH(h, k_scale_to32, lin_grid(n), 256, n, v, (float)s, sinv32, h->scale32, l0.v32[1]);
     TRY(run_vcycle<float>(h, o));
-    LAUNCH(h, k_to64, kRedBlocks, 256, n, (const float *)l0.xfinal32, (const double *)nullptr, 1.0, z);
+    LAUNCH(h, k_to64, lin_grid(n), 256, n, (const float *)l0.xfinal32, (const double *)nullptr, z);
   } else {
-    LAUNCH(h, k_scale_to, kRedBlocks, 256, n, v, s, nrm2, h->scale, (float *)nullptr, l0.v64[1]);
+    LAUNCH(h, k_scale_to, kRedBlocks, 256, n, v, s, sinv64, h->scale, l0.v64[1]);
     TRY(run_vcycle<double>(h, o));
-    LAUNCH(h, k_to64, kRedBlocks, 256, n, (const float *)nullptr, (const double *)l0.xfinal64, 1.0, z);
+    LAUNCH(h, k_to64, lin_grid(n), 256, n, (const float *)nullptr, (const double *)l0.xfinal64, z);
   }
   return VFS_OK;
 }
@@ -1056,8 +1077,9 @@ int ensure_krylov(vfs_poisson *h, int m) {
   const size_t n = h->box.n();
   for (int q = 0; q <= m; q++) TRY(dalloc(h, &h->V[q], n));
   for (int q = 0; q < m; q++) TRY(dalloc(h, &h->Z[q], n));
-  dfree(h, h->dV); dfree(h, h->dZ); dfree(h, h->coef); dfree(h, h->dsv);
-  TRY(dalloc(h, &h->dsv, m + 1));
+  dfree(h, h->dV); dfree(h, h->dZ); dfree(h, h->coef); dfree(h, h->dsv); dfree(h, h->dsv32);
+  TRY(dalloc(h, &h->dsv, 2 * (m + 1)));
+  TRY(dalloc(h, &h->dsv32, m + 1));
   TRY(dalloc(h, &h->dV, m + 1));
   TRY(dalloc(h, &h->dZ, m));
   TRY(dalloc(h, &h->coef, m + 1));
@@ -1158,7 +1180,10 @@ int fgmres(vfs_poisson *h, const vfs_solve_opts &o, vfs_solve_stats *st) {
   const double *const *dV = (const double *const *)h->dV;
   while (rel > o.rtol && it < o.max_it) {
     h->hbuf[400] = beta * beta;  // pinned staging: pageable copies cost ~0.5 ms each
-    CUDA_TRY(cudaMemcpyAsync(h->dsv, h->hbuf + 400, 8, cudaMemcpyHostToDevice, h->stream));
+    h->hbuf[401] = 1.0 / beta;
+    reinterpret_cast<float *>(h->hbuf + 402)[0] = (float)(1.0 / beta);
+    CUDA_TRY(cudaMemcpyAsync(h->dsv, h->hbuf + 400, 16, cudaMemcpyHostToDevice, h->stream));
+    CUDA_TRY(cudaMemcpyAsync(h->dsv32, h->hbuf + 402, 4, cudaMemcpyHostToDevice, h->stream));
     std::fill(gv.begin(), gv.end(), 0.);
     std::fill(Hraw.begin(), Hraw.end(), 0.);
     gv[0] = beta;
@@ -1166,7 +1191,7 @@ int fgmres(vfs_poisson *h, const vfs_solve_opts &o, vfs_solve_stats *st) {
     for (; jj < m && it < o.max_it; jj++) {
       const auto t0 = h->phase ? std::chrono::steady_clock::now() : std::chrono::steady_clock::time_point();
       if (h->phase) cudaEventRecord(h->phev[0], h->stream);
-      TRY(precondition(h, h->V[jj], 1.0, h->dsv + jj, h->Z[jj], o));
+      TRY(precondition(h, h->V[jj], 1.0, h->dsv + 2 * jj + 1, h->dsv32 + jj, h->Z[jj], o));
       const auto t1 = h->phase ? std::chrono::steady_clock::now() : t0;
       if (h->phase) cudaEventRecord(h->phev[1], h->stream);
       double *w = h->V[jj + 1];
@@ -1176,10 +1201,10 @@ int fgmres(vfs_poisson *h, const vfs_solve_opts &o, vfs_solve_stats *st) {
       LAUNCH(h, k_gs_reduce, 2 * jj + 2, 1024, h->partial, nbd, jj, h->red);
       LAUNCH(h, k_gs_coef, 1, 32, jj, h->red);
       LAUNCH(h, k_gs_update, nbd, 256, n, jj, dV, h->red, h->V[jj], w, h->partial);
-      LAUNCH(h, k_reduce_rows, 1, 1024, h->partial, nbd, 1, h->dsv + jj + 1);
+      LAUNCH(h, k_reduce_norm, 1, 1024, h->partial, nbd, h->dsv + 2 * (jj + 1), h->dsv32 + jj + 1);
       if (h->phase) cudaEventRecord(h->phev[3], h->stream);
       CUDA_TRY(cudaMemcpyAsync(h->hbuf, h->red, (kGsR + 3) * 8, cudaMemcpyDeviceToHost, h->stream));
-      CUDA_TRY(cudaMemcpyAsync(h->hbuf + kGsR + 3, h->dsv + jj + 1, 8, cudaMemcpyDeviceToHost, h->stream));
+      CUDA_TRY(cudaMemcpyAsync(h->hbuf + kGsR + 3, h->dsv + 2 * (jj + 1), 8, cudaMemcpyDeviceToHost, h->stream));
       const auto t2 = h->phase ? std::chrono::steady_clock::now() : t0;
       TRY(sync(h));
       const auto t3 = h->phase ? std::chrono::steady_clock::now() : t0;
@@ -1314,7 +1339,8 @@ int vfs_poisson_create(const vfs_grid_desc *gd, vfs_poisson **out) {
   if ((rc = dalloc(h, &h->coor, 3 * N)) || (rc = dalloc(h, &h->nvert, N)) || (rc = dalloc(h, &h->ucont, 3 * N)) ||
       (rc = dalloc(h, &h->phi_da, N)) || (rc = dalloc(h, &h->p_da, N)) || (rc = dalloc(h, &h->stage, 3 * N)) ||
       (rc = alloc_metrics(h, h->g, h->met)) || (rc = dalloc(h, &h->A0, n * NSLOT)) ||
-      (rc = dalloc(h, &h->scale, n)) || (rc = dalloc(h, &h->pc, 12 * n)) || (rc = dalloc(h, &h->aj_box, n)) ||
+      (rc = dalloc(h, &h->scale, n)) || (rc = dalloc(h, &h->scale32, n)) || (rc = dalloc(h, &h->pc, 12 * n)) ||
+      (rc = dalloc(h, &h->aj_box, n)) ||
       (rc = dalloc(h, &h->rowtype0, n)) || (rc = dalloc(h, &h->fluid, n)) || (rc = dalloc(h, &h->gid_box, n)) ||
       (rc = dalloc(h, &h->gid_da, N)) || (rc = dalloc(h, &h->b, n)) || (rc = dalloc(h, &h->x, n)) ||
       (rc = dalloc(h, &h->r, n)) || (rc = dalloc(h, &h->red, 512)) || (rc = dalloc(h, &h->total, 1)))
@@ -1401,6 +1427,7 @@ int vfs_poisson_set_nvert(vfs_poisson *h, const double *nvert) {
   LAUNCH(h, k_level_masks, lin_grid(n), 256, h->g, h->box, h->nvert, blank, w64, w32, h->aj_box,
          (const double *)h->met.aj);
   LAUNCH(h, k_row_scale, lin_grid(n), 256, n, h->rowtype0, h->aj_box, h->scale);
+  LAUNCH(h, k_cast_planes_f32, kRedBlocks, 256, h->scale, h->scale32, n);
   int tot = 0;
   CUDA_TRY(cudaMemcpyAsync(&tot, h->total, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
   TRY(sync(h));
@@ -1575,6 +1602,7 @@ int guess_buffers(vfs_poisson *h) {
     TRY(dalloc(h, &h->gof[1], n));
     TRY(dalloc(h, &h->rprev, n));
     TRY(dalloc(h, &h->rlearn, n));
+    TRY(dalloc(h, &h->prev32, n));
     const char *e = getenv("VFS_GUESS_SMOOTH");
     if (e) h->gsmooth = std::max(0, std::min(8, atoi(e)));
   }
@@ -1583,7 +1611,7 @@ int guess_buffers(vfs_poisson *h) {
 
 // fine feature planes of the current right-hand side into h->gfeat; also
 // phi_{n-1} as a box vector in h->Z[0] and the squared norms of b - A ex,
-// b - A phi_{n-1} and b in norms[0..2]
+// b - A phi_{n-1} (an FP32 estimate) and b in norms[0..2]
 int guess_features(vfs_poisson *h, const double *phi_nm1, const double *phi_nm2, double *norms) {
   if (!h || !phi_nm1 || !phi_nm2) return fail(VFS_EINVAL, "null argument");
   if (!h->have_rhs) return fail(VFS_ESTATE, "rhs must come before the guess");
@@ -1598,11 +1626,12 @@ int guess_features(vfs_poisson *h, const double *phi_nm1, const double *phi_nm2,
   CUDA_TRY(cudaMemsetAsync(h->gsum, 0, 8 * sizeof(double), h->stream));
   TRY(ensure_krylov(h, std::max(h->m_alloc, 20)));
   double *prev = h->Z[0];  // free until the next solve
-  LAUNCH(h, k_guess_prep, kRedBlocks, 256, h->g, h->box, h->rowtype0, p1, p2, h->gex, prev, feat, feat + n,
-         feat + 3 * n, h->gsum);
+  LAUNCH(h, k_guess_prep, kRedBlocks, 256, h->g, h->box, h->rowtype0, p1, p2, h->gex, prev, h->prev32, feat,
+         feat + n, feat + 3 * n, h->gsum);
   const dim3 gr = guess_grid(h->box);
   const int nbox = (int)(gr.x * gr.y * gr.z);
-  LAUNCH(h, k_residual64x2, gr, 128, h->box, h->A0, h->gex, prev, h->b, h->r, h->rprev, h->partial);
+  LAUNCH(h, k_guess_residuals, gr, 128, h->box, h->A0, h->L[0].C16, h->L[0].D32, h->scale32, h->gex, h->prev32,
+         h->b, h->r, h->partial);
   LAUNCH(h, k_guess_f2, kRedBlocks, 256, n, h->rowtype0, (const double *)h->aj_box, h->r, feat + 2 * n, h->gsum);
   LAUNCH(h, k_guess_scale, kRedBlocks, 256, n, feat, h->gsum);
   double nr[3];
@@ -1678,7 +1707,7 @@ int vfs_poisson_learned_guess(vfs_poisson *h, vfs_unet *u, const double *phi_nm1
   // least-squares band weights: minimise ||r_ex - sum_k alpha_k y_k||
   // (alpha = 0 is the plain extrapolation, so the guess is never worse)
   const dim3 gg = guess_grid(b);
-  LAUNCH(h, k_guess_gram, gg, 128, b, h->L[0].A32, (const double *)h->scale, h->gof[cur], h->r, kappa, h->gsum,
+  LAUNCH(h, k_guess_gram, gg, 128, b, h->L[0].A32, (const float *)h->scale32, h->gof[cur], h->r, kappa, h->gsum,
          h->partial);
   double gm[14];
   TRY(reduce_read(h, (int)(gg.x * gg.y * gg.z), 14, gm));
@@ -1763,13 +1792,22 @@ int vfs_poisson_learned_guess(vfs_poisson *h, vfs_unet *u, const double *phi_nm1
     r_learn = std::sqrt(s2);
     learned = r_learn < r_prev;
   }
-  if (!learned) CUDA_TRY(cudaMemcpyAsync(h->x, h->Z[0], n * 8, cudaMemcpyDeviceToDevice, h->stream));
+  double r_prev64 = r_prev;
+  if (!learned) {
+    // the previous step's phi stays: its FP64 residual is FGMRES's start
+    CUDA_TRY(cudaMemcpyAsync(h->x, h->Z[0], n * 8, cudaMemcpyDeviceToDevice, h->stream));
+    const dim3 gr = box_grid(h->box);
+    LAUNCH(h, k_residual64, gr, 128, h->box, h->A0, h->x, h->b, h->rprev, h->partial);
+    double s2 = 0.;
+    TRY(reduce_read(h, (int)(gr.x * gr.y * gr.z), 1, &s2));
+    r_prev64 = std::sqrt(s2);
+  }
   h->r0 = learned ? h->rlearn : h->rprev;
-  h->r0_norm = learned ? r_learn : r_prev;
+  h->r0_norm = learned ? r_learn : r_prev64;
   h->r0_valid = true;
   if (chosen) *chosen = learned ? 1 : 0;
   if (rel_res) {
-    rel_res[0] = r_prev / nb;
+    rel_res[0] = r_prev64 / nb;
     rel_res[1] = r_learn / nb;
   }
   if (h->phase) {
@@ -1968,7 +2006,7 @@ int vfs_poisson_mg_vcycle(vfs_poisson *h, int precision, const double *r, double
   const size_t n = h->box.n();
   TRY(upload(h, h->stage, r, h->g.n()));
   LAUNCH(h, k_da_to_box, lin_grid(n), 256, h->g, h->box, h->stage, h->r);
-  TRY(precondition(h, h->r, 1.0, nullptr, h->r, o));
+  TRY(precondition(h, h->r, 1.0, nullptr, nullptr, h->r, o));
   LAUNCH(h, k_box_to_da, da_grid(h->g), 128, h->g, h->box, h->r, h->stage);
   TRY(download(h, z, h->stage, h->g.n()));
   return sync(h);

@@ -577,23 +577,42 @@ __global__ void __launch_bounds__(256) k_axpy_multi(size_t n, int nv, const doub
   }
 }
 
-// out = (s v) * scale in FP32 or FP64: the aj row scaling that turns the
-// FP64 Krylov vector into the V-cycle right-hand side.  With nrm2 set, s is
-// divided by sqrt(nrm2[0]) (the norm of v, reduced on the device).
-__global__ void k_scale_to(size_t n, const double *__restrict__ v, double s, const double *__restrict__ nrm2,
-                           const double *__restrict__ scale, float *out32, double *out64) {
-  if (nrm2) s = nrm2[0] > 0. ? s / sqrt(nrm2[0]) : 0.;
-  for (size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (size_t)gridDim.x * blockDim.x) {
-    double t = s * v[c] * scale[c];
-    if (out32) out32[c] = (float)t;
-    else out64[c] = t;
+// out = (s v) * scale in FP64: the aj row scaling that turns the FP64
+// Krylov vector into the FP64 V-cycle's right-hand side; with sinv set, s is
+// multiplied by sinv[0] (the inverse norm of v, formed on the device).
+__global__ void k_scale_to(size_t n, const double *__restrict__ v, double s, const double *__restrict__ sinv,
+                           const double *__restrict__ scale, double *__restrict__ out) {
+  if (sinv) s *= sinv[0];
+  for (size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (size_t)gridDim.x * blockDim.x)
+    out[c] = s * v[c] * scale[c];
+}
+// The same into the FP32 V-cycle's right-hand side, with the products in
+// FP32 (the result is rounded to FP32 anyway and FP64 arithmetic is the
+// scarce pipe), one element per thread.
+__global__ void __launch_bounds__(256) k_scale_to32(size_t n, const double *__restrict__ v, float s,
+                                                    const float *__restrict__ sinv, const float *__restrict__ scale,
+                                                    float *__restrict__ out) {
+  const size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c < n) out[c] = (float)v[c] * ((sinv ? s * sinv[0] : s) * scale[c]);
+}
+// ||V||^2 from the block partials into out[0], 1/||V|| into out[1] and
+// out32[0] (0 for a zero vector); one block
+__global__ void k_reduce_norm(const double *partial, int nb, double *out, float *out32) {
+  double s = 0.;
+  for (int q = threadIdx.x; q < nb; q += blockDim.x) s += partial[q];
+  s = block_sum(s);
+  if (threadIdx.x == 0) {
+    const double inv = s > 0. ? 1. / sqrt(s) : 0.;
+    out[0] = s;
+    out[1] = inv;
+    out32[0] = (float)inv;
   }
 }
-// out = s * x (x in FP32 or FP64)
-__global__ void k_to64(size_t n, const float *__restrict__ x32, const double *__restrict__ x64, double s,
-                       double *__restrict__ out) {
-  for (size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (size_t)gridDim.x * blockDim.x)
-    out[c] = s * (x32 ? (double)x32[c] : x64[c]);
+// out = x (the V-cycle's result in FP32 or FP64, widened), one element per thread
+__global__ void __launch_bounds__(256) k_to64(size_t n, const float *__restrict__ x32,
+                                              const double *__restrict__ x64, double *__restrict__ out) {
+  const size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c < n) out[c] = x32 ? (double)x32[c] : x64[c];
 }
 __global__ void k_sumsq(size_t n, const double *__restrict__ x, double *partial) {
   double s = 0.;

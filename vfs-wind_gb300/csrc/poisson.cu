@@ -317,14 +317,15 @@ __device__ inline int guess_band(const Box &b, int j) {
 // G_kl = <y_k, y_l> (k <= l, 10 rows) and g_k = <y_k, r> (4 rows),
 // r = b - A ex.  A neighbour's band follows from its j offset.  The fit
 // only has to be good, not exact: the candidate it produces is then
-// measured by its FP64 residual.
+// measured by its FP64 residual.  The sums run over every kstride-th
+// k-plane (each plane holds every band, which depend on j only).
 __global__ void __launch_bounds__(128) k_guess_gram(Box b, const float *__restrict__ A, const float *__restrict__ scale,
                                                      const float *__restrict__ c, const double *__restrict__ r,
-                                                     double kappa, const double *sums, double *partial) {
+                                                     double kappa, const double *sums, int kstride, double *partial) {
   const float sc = (float)(kappa * plane_rms(sums, 2));
   float acc[14];
   for (int q = 0; q < 14; q++) acc[q] = 0.f;
-  const int p = blockIdx.x * blockDim.x + threadIdx.x, k = blockIdx.z;
+  const int p = blockIdx.x * blockDim.x + threadIdx.x, k = blockIdx.z * kstride;
   const uint32_t n = (uint32_t)b.n();
   for (int j = blockIdx.y * kGuessRows; p < b.nx && j < min(b.ny, (int)(blockIdx.y + 1) * kGuessRows); j++) {
     const int i = split_cell(p, b.nx);
@@ -1706,11 +1707,16 @@ int vfs_poisson_learned_guess(vfs_poisson *h, vfs_unet *u, const double *phi_nm1
            p == h->gsmooth - 1 ? (const uint8_t *)h->rowtype0 : nullptr);
   // least-squares band weights: minimise ||r_ex - sum_k alpha_k y_k||
   // (alpha = 0 is the plain extrapolation, so the guess is never worse)
-  const dim3 gg = guess_grid(b);
+  // the normal equations from every kGramStride-th k-plane, scaled to the
+  // whole box (the fit predicts the full ||r||^2 below)
+  constexpr int kGramStride = 4;
+  dim3 gg = guess_grid(b);
+  gg.z = (b.nz + kGramStride - 1) / kGramStride;
   LAUNCH(h, k_guess_gram, gg, 128, b, h->L[0].A32, (const float *)h->scale32, h->gof[cur], h->r, kappa, h->gsum,
-         h->partial);
+         kGramStride, h->partial);
   double gm[14];
   TRY(reduce_read(h, (int)(gg.x * gg.y * gg.z), 14, gm));
+  for (double &v : gm) v *= (double)b.nz / gg.z;
   BandWeights bw{};
   {
     // the normal equations G alpha = g (symmetric positive semi-definite)

@@ -36,6 +36,9 @@
  *   MyRestriction / MyInterpolation / MyNvertRestriction
  *                             poisson.c:365, :527, :1995 -> vfs_poisson_mg_*
  *   ibm_search_advanced       ibm.c:92             -> vfs_poisson_ibm_search
+ *   IB interpolation records  ibm.c:373-508        -> vfs_poisson_ibm_search_nodes
+ *   ibm_interpolation_advanced ibm.c:3301          -> vfs_poisson_ibm_interpolate
+ *   IB_BC                     momentum.c:2016      -> vfs_poisson_ib_bc
  */
 #ifndef VFS_POISSON_H
 #define VFS_POISSON_H
@@ -279,6 +282,69 @@ int vfs_divergence_noalloc(const vfs_grid_desc *g, const double *ucont, const do
  * solver's blanking: pass it to vfs_poisson_set_nvert. */
 int vfs_poisson_ibm_search(vfs_poisson *h, int ibi, int n_v, const double *xyz, int n_elmt, const int32_t *tri,
                            const int *bctype, double *nvert, int *n_failed);
+
+/* One IB node's interpolation record (the reference's IBMInfo, built in
+ * ibm_search_advanced, Source/ibm.c:373-508): the node (DA indices), its
+ * nearest surface element (nearestcell1, :1373-1518) with the nearest point
+ * pmin, the distance d_s and the point's weights cs on the element's
+ * vertices; the three cell centres (ip, jp, kp) where the ray from pmin
+ * through the node leaves the node's neighbourhood (InterceptionPoint,
+ * :1766-2258), their weights cr and the distance d_i; imode, the triangle of
+ * the 3x3 patch that ray crosses (-100: none); status 0 = found, 1 = the
+ * reference's fallback next to a domain boundary (one k or j neighbour,
+ * :423-505), 2 = the reference's search failure (it keeps the previous
+ * node's values; here the node itself with zero weights). */
+typedef struct {
+  int i, j, k;
+  int cell;
+  double pmin[3];
+  double d_s;
+  double cs[3];
+  int ip[3], jp[3], kp[3];
+  double cr[3];
+  double d_i;
+  int imode;
+  int status;
+} vfs_ibm_node;
+
+/* vfs_poisson_ibm_search plus the interpolation records of the body's IB
+ * nodes (the cells the dilation marks for this body, in k, j, i order),
+ * kept in the handle for vfs_poisson_ibm_interpolate.  *n_nodes (may be
+ * NULL) receives their number. */
+int vfs_poisson_ibm_search_nodes(vfs_poisson *h, int ibi, int n_v, const double *xyz, int n_elmt,
+                                 const int32_t *tri, const int *bctype, double *nvert, int *n_failed,
+                                 int *n_nodes);
+
+/* Copy up to max_nodes of body ibi's IB node records to nodes (host). */
+int vfs_poisson_ibm_nodes(vfs_poisson *h, int ibi, vfs_ibm_node *nodes, int max_nodes, int *n_nodes);
+
+/* ibm_interpolation_advanced (Source/ibm.c:3301-3640) for body ibi with
+ * the no-slip reconstruction (Source/wallfunction.c:140-156): at every IB
+ * node ucat = Ua + d_s/(d_s + d_i) (Uc - Ua), Ua the surface velocity at
+ * pmin (u_surf: n_v x 3 vertex velocities, or NULL for a body at rest),
+ * Uc the weighted ucat of the three interception cells -- 0 when any of
+ * those is not fluid or the node has nvert > 2.9 -- and p the weighted p of
+ * the three cells; then the face fluxes ucont of every cell with
+ * (int)(nvert + 0.5) == 1 and of the faces it shares with its -i/-j/-k
+ * neighbours from the new ucat (times 0 with immersed == 3; the faces of
+ * the -1/-2 walls in bctype set to 0), and Contra2Cart (with the solid
+ * zeroing) from the new ucont.  ucat, p, ucont: DA arrays, in/out, host or
+ * device; the handle's nvert (set_nvert) is the blanking.  The averaging,
+ * level-set, moving-body, inviscid and wall-function branches of the
+ * reference routine are momentum-solver options and are not restated. */
+int vfs_poisson_ibm_interpolate(vfs_poisson *h, int ibi, const double *u_surf, int immersed, const int *bctype,
+                                double *ucat, double *p, double *ucont);
+
+/* IB_BC (Source/momentum.c:2016-2220) with immersed set: the periodic ghost
+ * cells of ucat take their partners' values, the face fluxes of the cells
+ * with (int)nvert == 1 and of the faces they share with their -i/-j/-k
+ * neighbours are formed from ucat (0 with immersed == 3, where the faces
+ * between cells whose nvert sum exceeds 1.1 are also zeroed), the faces of
+ * the -1/-2 walls in i and j and of the slip (10) walls are set to 0 and
+ * the periodic faces take their partners' fluxes.  ucat, ucont: DA arrays,
+ * in/out.  The first-step wall marking of nvert (immersed == 0) and the
+ * air-flow level-set faces are not restated. */
+int vfs_poisson_ib_bc(vfs_poisson *h, int immersed, const int *bctype, double *ucat, double *ucont);
 
 /* ---------------------------------------------------------------------
  * Learned initial guess: a 3-level 3-D U-Net (channels 16/32/64, 3x3x3

@@ -182,8 +182,8 @@ static int point_cell(const double p[3], int ip, int jp, int kp, const hashgrid 
  * interpolation-stencil parts).  cent: cell centres (DA layout, Cmpnts);
  * nvert: in/out; bctype: the six boundary codes.  Returns the number of
  * cells whose ray search gave up (0 normally). */
-int or_ibm_search(const or_dims *d, const double *cent, int ibi, int n_v, const double *x, const double *y,
-                  const double *z, int n_elmt, const int *nv, const int *bctype, double *nvert, int max_tries)
+int or_ibm_mark(const or_dims *d, const double *cent, int ibi, int n_v, const double *x, const double *y,
+                const double *z, int n_elmt, const int *nv, double *nvert, int max_tries)
 {
   const int mx = d->mx, my = d->my, mz = d->mz;
   hashgrid H;
@@ -224,7 +224,14 @@ int or_ibm_search(const or_dims *d, const double *cent, int ibi, int n_v, const 
                 if ((int)(nvert[IX(d, ii, jj, kk)] + 0.5) == 4) nvert[t] = nvert[t] > 2 ? nvert[t] : 2;
         }
       }
-  /* back to 3 / 1 and the wall rows (ibm.c:514-543) */
+  free(H.head); free(H.next); free(H.tri); free(nf); free(seen);
+  return failed;
+}
+
+/* back to 3 / 1 and the wall rows (ibm.c:514-543) */
+void or_ibm_finish(const or_dims *d, const int *bctype, double *nvert)
+{
+  const int mx = d->mx, my = d->my, mz = d->mz;
   for (int k = 1; k < mz - 1; k++)
     for (int j = 1; j < my - 1; j++)
       for (int i = 1; i < mx - 1; i++) {
@@ -243,6 +250,14 @@ int or_ibm_search(const or_dims *d, const double *cent, int ibi, int n_v, const 
           }
         }
       }
-  free(H.head); free(H.next); free(H.tri); free(nf); free(seen);
+}
+
+/* ibm_search_advanced for one body: the marking (classification and
+ * dilation, 4 = inside, 2 = IB node) then the finish (3 / 1 and walls). */
+int or_ibm_search(const or_dims *d, const double *cent, int ibi, int n_v, const double *x, const double *y,
+                  const double *z, int n_elmt, const int *nv, const int *bctype, double *nvert, int max_tries)
+{
+  int failed = or_ibm_mark(d, cent, ibi, n_v, x, y, z, n_elmt, nv, nvert, max_tries);
+  or_ibm_finish(d, bctype, nvert);
   return failed;
 }

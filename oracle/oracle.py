@@ -15,7 +15,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
 SOURCES = [os.path.join(HERE, "vfs_oracle.c"), os.path.join(HERE, "mg_solver.c"),
-           os.path.join(HERE, "ibm_oracle.c")]
+           os.path.join(HERE, "ibm_oracle.c"), os.path.join(HERE, "ibm_interp_oracle.c")]
 
 
 def build(force=False):
@@ -55,6 +55,14 @@ class SolveOpts(C.Structure):
 class SolveStats(C.Structure):
     _fields_ = [("iterations", C.c_int), ("rel_residual", C.c_double),
                 ("setup_ms", C.c_double), ("solve_ms", C.c_double), ("levels", C.c_int)]
+
+
+class IbmNode(C.Structure):
+    """One IB node's interpolation record (or_ibm_node)."""
+    _fields_ = [("i", C.c_int), ("j", C.c_int), ("k", C.c_int), ("cell", C.c_int),
+                ("pmin", C.c_double * 3), ("d_s", C.c_double), ("cs", C.c_double * 3),
+                ("ip", C.c_int * 3), ("jp", C.c_int * 3), ("kp", C.c_int * 3),
+                ("cr", C.c_double * 3), ("d_i", C.c_double), ("imode", C.c_int), ("status", C.c_int)]
 
 
 _lib = None
@@ -101,6 +109,15 @@ def lib():
         L.or_triangle_normals.argtypes = [C.c_int, ip, dp, dp, dp, dp]
         L.or_ibm_search.argtypes = [P(Dims), dp, C.c_int, C.c_int, dp, dp, dp, C.c_int, ip, ip, dp, C.c_int]
         L.or_ibm_search.restype = C.c_int
+        L.or_ibm_mark.argtypes = [P(Dims), dp, C.c_int, C.c_int, dp, dp, dp, C.c_int, ip, dp, C.c_int]
+        L.or_ibm_mark.restype = C.c_int
+        L.or_ibm_finish.argtypes = [P(Dims), ip, dp]
+        L.or_bounding_sphere.argtypes = [C.c_int, ip, dp, dp, dp, dp, dp]
+        L.or_ibm_nodes.argtypes = [P(Dims), dp, dp, C.c_int, dp, dp, dp, C.c_int, ip, P(IbmNode), C.c_int]
+        L.or_ibm_nodes.restype = C.c_int
+        L.or_ibm_interpolate.argtypes = [P(Dims), dp, P(IbmNode), C.c_int, ip, dp, dp, dp, dp, dp, dp, dp, ip,
+                                         C.c_int, dp, dp, dp]
+        L.or_ib_bc.argtypes = [P(Dims), dp, dp, dp, dp, ip, C.c_int, dp, dp]
         _lib = L
     return _lib
 
@@ -374,3 +391,73 @@ def from_da(d, gid, v):
     out = np.zeros(n)
     out[g[sel]] = v.ravel()[sel]
     return out
+
+
+def _surface_arrays(surface):
+    xyz, tris = surface
+    x = np.ascontiguousarray(xyz[:, 0], np.float64)
+    y = np.ascontiguousarray(xyz[:, 1], np.float64)
+    z = np.ascontiguousarray(xyz[:, 2], np.float64)
+    nv = np.ascontiguousarray(tris, np.int32).ravel()
+    return x, y, z, nv
+
+
+def ibm_mark(d, cent, surface, nvert=None, ibi=0, max_tries=64):
+    """Classification and dilation of one body (4 inside, 2 IB node)."""
+    x, y, z, nv = _surface_arrays(surface)
+    out = np.zeros((d.mz, d.my, d.mx)) if nvert is None else np.ascontiguousarray(nvert, np.float64).copy()
+    failed = lib().or_ibm_mark(C.byref(d), _dp(np.ascontiguousarray(cent, np.float64)), ibi, len(x), _dp(x),
+                               _dp(y), _dp(z), len(nv) // 3, _ip(nv), _dp(out), max_tries)
+    return out, failed
+
+
+def ibm_finish(d, nvert, bctype=(0, 0, 0, 0, 0, 0)):
+    out = np.ascontiguousarray(nvert, np.float64).copy()
+    lib().or_ibm_finish(C.byref(d), _ip(np.ascontiguousarray(bctype, np.int32)), _dp(out))
+    return out
+
+
+def bounding_sphere(surface):
+    x, y, z, nv = _surface_arrays(surface)
+    ne = len(nv) // 3
+    q = np.zeros((ne, 3))
+    r = np.zeros(ne)
+    lib().or_bounding_sphere(ne, _ip(nv), _dp(x), _dp(y), _dp(z), _dp(q), _dp(r))
+    return q, r
+
+
+def ibm_nodes(d, cent, nvert_marked, surface):
+    """The IB nodes (cells marked 2) of one body with their records."""
+    x, y, z, nv = _surface_arrays(surface)
+    marked = np.ascontiguousarray(nvert_marked, np.float64)
+    c = np.ascontiguousarray(cent, np.float64)
+    n = lib().or_ibm_nodes(C.byref(d), _dp(c), _dp(marked), len(x), _dp(x), _dp(y), _dp(z), len(nv) // 3, _ip(nv),
+                           None, 0)
+    arr = (IbmNode * max(n, 1))()
+    lib().or_ibm_nodes(C.byref(d), _dp(c), _dp(marked), len(x), _dp(x), _dp(y), _dp(z), len(nv) // 3, _ip(nv),
+                       arr, n)
+    return arr, n
+
+
+def ibm_interpolate(d, nvert, nodes, n_nodes, surface, met, ucat, p, ucont, u_surf=None,
+                    bctype=(0, 0, 0, 0, 0, 0), immersed=1):
+    """ibm_interpolation_advanced + noslip for one body; returns (ucat, p, ucont)."""
+    _, _, _, nv = _surface_arrays(surface)
+    uc = np.ascontiguousarray(ucat, np.float64).copy()
+    pp = np.ascontiguousarray(p, np.float64).copy()
+    uo = np.ascontiguousarray(ucont, np.float64).copy()
+    us = None if u_surf is None else _dp(np.ascontiguousarray(u_surf, np.float64))
+    lib().or_ibm_interpolate(C.byref(d), _dp(np.ascontiguousarray(nvert, np.float64)), nodes, n_nodes, _ip(nv), us,
+                             _dp(met["icsi"]), _dp(met["jeta"]), _dp(met["kzet"]), _dp(met["csi"]),
+                             _dp(met["eta"]), _dp(met["zet"]), _ip(np.ascontiguousarray(bctype, np.int32)),
+                             int(immersed), _dp(uc), _dp(pp), _dp(uo))
+    return uc, pp, uo
+
+
+def ib_bc(d, nvert, met, ucat, ucont, bctype=(0, 0, 0, 0, 0, 0), immersed=1):
+    """IB_BC's face fluxes and boundary faces; returns (ucat, ucont)."""
+    uc = np.ascontiguousarray(ucat, np.float64).copy()
+    uo = np.ascontiguousarray(ucont, np.float64).copy()
+    lib().or_ib_bc(C.byref(d), _dp(np.ascontiguousarray(nvert, np.float64)), _dp(met["icsi"]), _dp(met["jeta"]),
+                   _dp(met["kzet"]), _ip(np.ascontiguousarray(bctype, np.int32)), int(immersed), _dp(uc), _dp(uo))
+    return uc, uo

@@ -102,6 +102,34 @@ void or_triangle_normals(int n_elmt, const int *nv, const double *x, const doubl
                          double *nf);
 int or_ibm_search(const or_dims *d, const double *cent, int ibi, int n_v, const double *x, const double *y,
                   const double *z, int n_elmt, const int *nv, const int *bctype, double *nvert, int max_tries);
+int or_ibm_mark(const or_dims *d, const double *cent, int ibi, int n_v, const double *x, const double *y,
+                const double *z, int n_elmt, const int *nv, double *nvert, int max_tries);
+void or_ibm_finish(const or_dims *d, const int *bctype, double *nvert);
+
+/* One IB node's interpolation record (ibm_interp_oracle.c; the reference's
+ * IBMInfo): the node, its nearest surface element and point, the distance
+ * d_s and the point's weights on the element's vertices, the three cell
+ * centres the normal ray meets with their weights and distance d_i, the
+ * patch triangle (imode) and a status (0: found, 1: the reference's
+ * boundary fallback, 2: the reference's search failure). */
+typedef struct {
+  int i, j, k;
+  int cell;
+  double pmin[3], d_s, cs[3];
+  int ip[3], jp[3], kp[3];
+  double cr[3], d_i;
+  int imode, status;
+} or_ibm_node;
+void or_bounding_sphere(int n_elmt, const int *nv, const double *x, const double *y, const double *z, double *q,
+                        double *rad);
+int or_ibm_nodes(const or_dims *d, const double *cent, const double *nvert_marked, int n_v, const double *x,
+                 const double *y, const double *z, int n_elmt, const int *nv, or_ibm_node *nodes, int max_nodes);
+void or_ibm_interpolate(const or_dims *d, const double *nvert, const or_ibm_node *nodes, int n_nodes,
+                        const int *nv, const double *u_surf, const double *icsi, const double *jeta,
+                        const double *kzet, const double *csi, const double *eta, const double *zet,
+                        const int *bctype, int immersed, double *ucat, double *p, double *ucont);
+void or_ib_bc(const or_dims *d, const double *nvert, const double *icsi, const double *jeta, const double *kzet,
+              const int *bctype, int immersed, double *ucat, double *ucont);
 
 /* CPU baseline solver (oracle/mg_solver.c). */
 typedef struct {

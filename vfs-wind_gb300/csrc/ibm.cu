@@ -185,6 +185,236 @@ __global__ void k_ibm_finish(Grid g, int b0, int b1, int b2, int b3, int b4, int
   nvert[t] = v;
 }
 
+// ---- IB interpolation records (ibm.c:373-508) ----
+// One thread per IB node: the nearest surface element (nearestcell1,
+// :1373-1518), the interception of the normal ray with the 3x3 patches of
+// neighbouring cell centres (InterceptionPoint, :1766-2258, ICP :1666-1764)
+// and the boundary fallback (:423-505), in the reference's operation order
+// (compiled without FMA contraction).
+struct V3 {
+  double x, y, z;
+};
+struct V2 {
+  double x, y;
+};
+__device__ inline V3 vload(const double *a, size_t t) { return V3{a[3 * t], a[3 * t + 1], a[3 * t + 2]}; }
+__device__ inline double vdist(V3 a, V3 b) {
+  return sqrt((a.x - b.x) * (a.x - b.x) + (a.y - b.y) * (a.y - b.y) + (a.z - b.z) * (a.z - b.z));
+}
+// ISSameSide2D (compgeom.c:62-114)
+__device__ inline int same_side(V2 p, V2 p1, V2 p2, V2 p3) {
+  const double t1 = (p.x - p1.x) * (p2.y - p1.y) - (p.y - p1.y) * (p2.x - p1.x);
+  const double t2 = (p3.x - p1.x) * (p2.y - p1.y) - (p3.y - p1.y) * (p2.x - p1.x);
+  const double lt = sqrt((p1.x - p2.x) * (p1.x - p2.x) + (p1.y - p2.y) * (p1.y - p2.y));
+  if (fabs(t1 / lt) < 1.e-10) return 1;
+  if (t1 > 0) return t2 > 0 ? 1 : -1;
+  return t2 < 0 ? 1 : -1;
+}
+// ISInsideTriangle2D / ISPointInTriangle (compgeom.c:116-166)
+__device__ inline int point_in_triangle(V3 p, V3 p1, V3 p2, V3 p3, double nx, double ny, double nz) {
+  V2 a, b, c, e;
+  if (fabs(nz) >= fabs(nx) && fabs(nz) >= fabs(ny)) {
+    a = {p.x, p.y}; b = {p1.x, p1.y}; c = {p2.x, p2.y}; e = {p3.x, p3.y};
+  } else if (fabs(nx) >= fabs(ny) && fabs(nx) >= fabs(nz)) {
+    a = {p.z, p.y}; b = {p1.z, p1.y}; c = {p2.z, p2.y}; e = {p3.z, p3.y};
+  } else {
+    a = {p.x, p.z}; b = {p1.x, p1.z}; c = {p2.x, p2.z}; e = {p3.x, p3.z};
+  }
+  int ls = same_side(a, b, c, e);
+  if (ls < 0) return ls;
+  ls = same_side(a, c, e, b);
+  if (ls < 0) return ls;
+  return same_side(a, e, b, c);
+}
+// Dis_P_Line (compgeom.c:168-194)
+__device__ inline void dist_point_line(V3 p, V3 p1, V3 p2, V3 &po, double &d) {
+  const double dx21 = p2.x - p1.x, dy21 = p2.y - p1.y, dz21 = p2.z - p1.z;
+  const double dx31 = p.x - p1.x, dy31 = p.y - p1.y, dz31 = p.z - p1.z;
+  const double t = (dx31 * dx21 + dy31 * dy21 + dz31 * dz21) / (dx21 * dx21 + dy21 * dy21 + dz21 * dz21);
+  if (t < 0) {
+    po = p1;
+    d = sqrt(dx31 * dx31 + dy31 * dy31 + dz31 * dz31);
+  } else if (t > 1) {
+    po = p2;
+    d = sqrt((p.x - po.x) * (p.x - po.x) + (p.y - po.y) * (p.y - po.y) + (p.z - po.z) * (p.z - po.z));
+  } else {
+    po = V3{p1.x + t * dx21, p1.y + t * dy21, p1.z + t * dz21};
+    d = sqrt((p.x - po.x) * (p.x - po.x) + (p.y - po.y) * (p.y - po.y) + (p.z - po.z) * (p.z - po.z));
+  }
+}
+// triangle_intp / triangle_intp2 (compgeom.c:196-230) on the plane the
+// dominant normal component picks
+__device__ inline void project_bary(V3 p, V3 p1, V3 p2, V3 p3, double nx, double ny, double nz, double w[3]) {
+  V2 a, b, c, e;
+  if (fabs(nx) >= fabs(ny) && fabs(nx) >= fabs(nz)) {
+    a = {p.y, p.z}; b = {p1.y, p1.z}; c = {p2.y, p2.z}; e = {p3.y, p3.z};
+  } else if (fabs(ny) >= fabs(nx) && fabs(ny) >= fabs(nz)) {
+    a = {p.x, p.z}; b = {p1.x, p1.z}; c = {p2.x, p2.z}; e = {p3.x, p3.z};
+  } else if (fabs(nz) >= fabs(ny) && fabs(nz) >= fabs(nx)) {
+    a = {p.y, p.x}; b = {p1.y, p1.x}; c = {p2.y, p2.x}; e = {p3.y, p3.x};
+  } else {
+    return;
+  }
+  const double x13 = b.x - e.x, y13 = b.y - e.y, x23 = c.x - e.x, y23 = c.y - e.y;
+  const double xp3 = a.x - e.x, yp3 = a.y - e.y;
+  const double det = x13 * y23 - x23 * y13;
+  w[0] = (y23 * xp3 - x23 * yp3) / det;
+  w[1] = (-y13 * xp3 + x13 * yp3) / det;
+  w[2] = 1. - w[0] - w[1];
+}
+__constant__ int kPatchTri[8][3] = {{0, 1, 4}, {1, 2, 4}, {2, 4, 5}, {4, 5, 8}, {4, 7, 8}, {4, 6, 7}, {3, 4, 6}, {3, 4, 0}};
+
+// the cells of one body marked 2 (IB node) after the dilation, interior
+// only: per 256-cell block, their count ...
+__global__ void k_ibm_mark_count(Grid g, const double *nvert, int *bcount) {
+  const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  bool mark = false;
+  if (t < g.n()) {
+    const int i = (int)(t % g.mx), j = (int)((t / g.mx) % g.my), k = (int)(t / ((size_t)g.mx * g.my));
+    mark = i >= 1 && i < g.mx - 1 && j >= 1 && j < g.my - 1 && k >= 1 && k < g.mz - 1 &&
+           (int)(nvert[t] + 0.5) == 2;
+  }
+  const int c = __syncthreads_count(mark);
+  if (threadIdx.x == 0) bcount[blockIdx.x] = c;
+}
+// ... and their DA indices in order, from the blocks' exclusive offsets
+__global__ void k_ibm_mark_scatter(Grid g, const double *nvert, const int *boff, int *list) {
+  __shared__ int wsum[8];
+  const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  bool mark = false;
+  if (t < g.n()) {
+    const int i = (int)(t % g.mx), j = (int)((t / g.mx) % g.my), k = (int)(t / ((size_t)g.mx * g.my));
+    mark = i >= 1 && i < g.mx - 1 && j >= 1 && j < g.my - 1 && k >= 1 && k < g.mz - 1 &&
+           (int)(nvert[t] + 0.5) == 2;
+  }
+  const unsigned ball = __ballot_sync(0xffffffffu, mark);
+  const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
+  if (lane == 0) wsum[wp] = __popc(ball);
+  __syncthreads();
+  int base = boff[blockIdx.x];
+  for (int q = 0; q < wp; q++) base += wsum[q];
+  if (mark) list[base + __popc(ball & ((1u << lane) - 1u))] = (int)t;
+}
+
+__global__ void k_ibm_nodes(Grid g, const double *__restrict__ cent, const int *__restrict__ list, int n_nodes,
+                            int n_elmt, const double *__restrict__ tv, const double *__restrict__ nf,
+                            const double *__restrict__ qv, const double *__restrict__ rad, vfs_ibm_node *out) {
+  const int n = blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= n_nodes) return;
+  const size_t t = (size_t)list[n];
+  const int i = (int)(t % g.mx), j = (int)((t / g.mx) % g.my), k = (int)(t / ((size_t)g.mx * g.my));
+  vfs_ibm_node nd;
+  nd.i = i; nd.j = j; nd.k = k;
+  const V3 p = vload(cent, t);
+  // nearestcell1
+  double dmin = 1.e20;
+  int cell_min = -100;
+  V3 pmin{0., 0., 0.};
+  for (int e = 0; e < n_elmt; e++) {
+    const V3 qe{qv[3 * e], qv[3 * e + 1], qv[3 * e + 2]};
+    const double d_center = vdist(p, qe);
+    if (!(d_center - rad[e] < dmin)) continue;
+    const double *v = &tv[(size_t)e * 9];
+    const V3 p1{v[0], v[1], v[2]}, p2{v[3], v[4], v[5]}, p3{v[6], v[7], v[8]};
+    const double nfx = nf[3 * e], nfy = nf[3 * e + 1], nfz = nf[3 * e + 2];
+    double tf = (p.x - p1.x) * nfx + (p.y - p1.y) * nfy + (p.z - p1.z) * nfz;
+    if (fabs(tf) < 1.e-10) tf = 1.e-10;
+    if (!(tf >= 0)) continue;
+    const V3 pj{p.x - tf * nfx, p.y - tf * nfy, p.z - tf * nfz};
+    if (point_in_triangle(pj, p1, p2, p3, nfx, nfy, nfz) == 1) {
+      if (tf < dmin) { dmin = tf; pmin = pj; cell_min = e; }
+    } else {
+      V3 po;
+      double d;
+      dist_point_line(p, p1, p2, po, d);
+      if (d < dmin) { dmin = d; pmin = po; cell_min = e; }
+      dist_point_line(p, p2, p3, po, d);
+      if (d < dmin) { dmin = d; pmin = po; cell_min = e; }
+      dist_point_line(p, p3, p1, po, d);
+      if (d < dmin) { dmin = d; pmin = po; cell_min = e; }
+    }
+  }
+  nd.cell = cell_min;
+  nd.pmin[0] = pmin.x; nd.pmin[1] = pmin.y; nd.pmin[2] = pmin.z;
+  nd.d_s = dmin;
+  nd.cs[0] = nd.cs[1] = nd.cs[2] = 0.;
+  if (cell_min >= 0) {
+    const double *v = &tv[(size_t)cell_min * 9];
+    project_bary(pmin, V3{v[0], v[1], v[2]}, V3{v[3], v[4], v[5]}, V3{v[6], v[7], v[8]}, nf[3 * cell_min],
+                 nf[3 * cell_min + 1], nf[3 * cell_min + 2], nd.cs);
+  }
+  // InterceptionPoint: the patches at i-1, i+1, j-1, j+1, k-1, k+1
+  double nfx = p.x - pmin.x, nfy = p.y - pmin.y, nfz = p.z - pmin.z;
+  const double dr = sqrt(nfx * nfx + nfy * nfy + nfz * nfz);
+  nfx /= dr; nfy /= dr; nfz /= dr;
+  nd.imode = -100;
+  for (int s = 0; s < 3; s++) { nd.ip[s] = i; nd.jp[s] = j; nd.kp[s] = k; nd.cr[s] = 0.; }
+  nd.d_i = 0.;
+  for (int face = 0; face < 6 && nd.imode < 0; face++) {
+    int ip[9], jp[9], kp[9];
+    V3 pc[9];
+    for (int s = 0; s < 9; s++) {
+      const int a = s % 3 - 1, b = s / 3 - 1;
+      switch (face) {
+        case 0: ip[s] = i - 1; jp[s] = j + a; kp[s] = k + b; break;
+        case 1: ip[s] = i + 1; jp[s] = j + a; kp[s] = k + b; break;
+        case 2: ip[s] = i + a; jp[s] = j - 1; kp[s] = k + b; break;
+        case 3: ip[s] = i + a; jp[s] = j + 1; kp[s] = k + b; break;
+        case 4: ip[s] = i + a; jp[s] = j + b; kp[s] = k - 1; break;
+        default: ip[s] = i + a; jp[s] = j + b; kp[s] = k + 1; break;
+      }
+      pc[s] = vload(cent, g.at(ip[s], jp[s], kp[s]));
+    }
+    for (int tr = 0; tr < 8; tr++) {  // ICP
+      const V3 p1 = pc[kPatchTri[tr][0]], p2 = pc[kPatchTri[tr][1]], p3 = pc[kPatchTri[tr][2]];
+      const double dx1 = p.x - p1.x, dy1 = p.y - p1.y, dz1 = p.z - p1.z;
+      const double dx2 = p2.x - p1.x, dy2 = p2.y - p1.y, dz2 = p2.z - p1.z;
+      const double dx3 = p3.x - p1.x, dy3 = p3.y - p1.y, dz3 = p3.z - p1.z;
+      double d = (nfx * (dy2 * dz3 - dz2 * dy3) - nfy * (dx2 * dz3 - dz2 * dx3) + nfz * (dx2 * dy3 - dy2 * dx3));
+      if (!(fabs(d) > 1.e-10)) continue;
+      d = -(dx1 * (dy2 * dz3 - dz2 * dy3) - dy1 * (dx2 * dz3 - dz2 * dx3) + dz1 * (dx2 * dy3 - dy2 * dx3)) / d;
+      if (!(d > 0)) continue;
+      const V3 pint{p.x + d * nfx, p.y + d * nfy, p.z + d * nfz};
+      const double rx1 = p2.x - p1.x, ry1 = p2.y - p1.y, rz1 = p2.z - p1.z;
+      const double rx2 = p3.x - p1.x, ry2 = p3.y - p1.y, rz2 = p3.z - p1.z;
+      const double nfxt = ry1 * rz2 - rz1 * ry2, nfyt = -rx1 * rz2 + rz1 * rx2, nfzt = rx1 * ry2 - ry1 * rx2;
+      if (point_in_triangle(pint, p1, p2, p3, nfxt, nfyt, nfzt) >= 0) {
+        double w[3] = {0., 0., 0.};
+        project_bary(pint, p1, p2, p3, nfxt, nfyt, nfzt, w);
+        nd.d_i = sqrt((pint.x - p.x) * (pint.x - p.x) + (pint.y - p.y) * (pint.y - p.y) +
+                      (pint.z - p.z) * (pint.z - p.z));
+        nd.imode = tr;
+        for (int q = 0; q < 3; q++) {
+          const int s = kPatchTri[tr][q];
+          nd.ip[q] = ip[s]; nd.jp[q] = jp[s]; nd.kp[q] = kp[s];
+          nd.cr[q] = w[q];
+        }
+        break;
+      }
+    }
+  }
+  nd.status = 0;
+  if (nd.imode < 0) {
+    int di = 0, dj = 0, dk = 0;
+    if (i == 1 || i == g.mx - 2 || j == 1 || j == g.my - 2) {
+      dk = (cell_min >= 0 && nf[3 * cell_min + 2] > 0) ? 1 : -1;
+      nd.status = 1;
+    } else if (k == 1 || k == g.mz - 2) {
+      dj = 1;
+      nd.status = 1;
+    } else {
+      nd.status = 2;
+    }
+    if (nd.status == 1) {
+      const V3 c0 = p, c1 = vload(cent, g.at(i + di, j + dj, k + dk));
+      nd.d_i = sqrt((c0.x - c1.x) * (c0.x - c1.x) + (c0.y - c1.y) * (c0.y - c1.y) + (c0.z - c1.z) * (c0.z - c1.z));
+      nd.cr[0] = 1.; nd.cr[1] = 0.; nd.cr[2] = 0.;
+      for (int q = 0; q < 3; q++) { nd.ip[q] = i + di; nd.jp[q] = j + dj; nd.kp[q] = k + dk; }
+    }
+  }
+  out[n] = nd;
+}
+
 int fail(int code, const std::string &m) {
   set_last_error(m);
   return code;
@@ -201,9 +431,48 @@ bool on_device(const void *p) {
 
 }  // namespace
 
-extern "C" int vfs_poisson_ibm_search(vfs_poisson *h, int ibi, int n_v, const double *xyz, int n_elmt,
-                                      const int32_t *tri, const int *bctype, double *nvert, int *n_failed) {
+namespace {
+
+// BoundingSphere (ibm.c:1282-1370): per element, a sphere through the
+// longest edge's end points centred on the circumcentre side
+void bounding_sphere(int n_elmt, const int32_t *tri, const std::vector<double> &x, const std::vector<double> &y,
+                     const std::vector<double> &z, std::vector<double> &q, std::vector<double> &rad) {
+  struct P { double x, y, z; };
+  auto dist = [](P a, P b) {
+    return std::sqrt((a.x - b.x) * (a.x - b.x) + (a.y - b.y) * (a.y - b.y) + (a.z - b.z) * (a.z - b.z));
+  };
+  const P p0{0., 0., 0.};
+  q.assign((size_t)n_elmt * 3, 0.);
+  rad.assign(n_elmt, 0.);
+  for (int e = 0; e < n_elmt; e++) {
+    const int n1 = tri[3 * e], n2 = tri[3 * e + 1], n3 = tri[3 * e + 2];
+    const P p1{x[n1], y[n1], z[n1]}, p2{x[n2], y[n2], z[n2]}, p3{x[n3], y[n3], z[n3]};
+    const double l12 = dist(p1, p2), l23 = dist(p2, p3), l31 = dist(p3, p1);
+    P pa, pb, pc;
+    if (l12 > l23) {
+      if (l12 > l31) { pa = p1; pb = p2; pc = p3; } else { pa = p3; pb = p1; pc = p2; }
+    } else {
+      if (l31 < l23) { pa = p2; pb = p3; pc = p1; } else { pa = p3; pb = p1; pc = p2; }
+    }
+    const P pf{0.5 * (pa.x + pb.x), 0.5 * (pa.y + pb.y), 0.5 * (pa.z + pb.z)};
+    const P pu{pa.x - pf.x, pa.y - pf.y, pa.z - pf.z}, pv{pc.x - pf.x, pc.y - pf.y, pc.z - pf.z};
+    const P pt{pu.y * pv.z - pu.z * pv.y, pu.z * pv.x - pu.x * pv.z, pu.x * pv.y - pu.y * pv.x};
+    const P pd{pt.y * pu.z - pt.z * pu.y, pt.z * pu.x - pt.x * pu.z, pt.x * pu.y - pt.y * pu.x};
+    double gama = -(dist(pu, p0) * dist(pu, p0) - dist(pv, p0) * dist(pv, p0));
+    const P pw{pv.x - pu.x, pv.y - pu.y, pv.z - pu.z};
+    double lamda = 2 * (pd.x * pw.x + pd.y * pw.y + pd.z * pw.z);
+    gama /= lamda;
+    lamda = gama < 0 ? 0 : gama;
+    const P qq{pf.x + lamda * pd.x, pf.y + lamda * pd.y, pf.z + lamda * pd.z};
+    q[3 * e] = qq.x; q[3 * e + 1] = qq.y; q[3 * e + 2] = qq.z;
+    rad[e] = dist(qq, pa);
+  }
+}
+
+int ibm_search_impl(vfs_poisson *h, int ibi, int n_v, const double *xyz, int n_elmt, const int32_t *tri,
+                    const int *bctype, double *nvert, int *n_failed, bool want_nodes, int *n_nodes) {
   if (!h || !xyz || !tri || !nvert || n_v < 3 || n_elmt < 1) return fail(VFS_EINVAL, "bad surface arguments");
+  if (want_nodes && (ibi < 0 || ibi > 1023)) return fail(VFS_EINVAL, "body index out of range");
   IbmContext cx;
   int rc = ibm_context(h, &cx);
   if (rc != VFS_OK) return rc;
@@ -293,6 +562,63 @@ extern "C" int vfs_poisson_ibm_search(vfs_poisson *h, int ibi, int n_v, const do
   k_ibm_classify<<<gi, 128, 0, st>>>(g, cx.cent, ibi, H, (int *)buf[0], (int *)buf[1], (int *)buf[2],
                                      (double *)buf[3], (double *)buf[4], (double *)buf[5], dnv, dfail);
   k_ibm_dilate<<<gd, 128, 0, st>>>(g, dnv, dtmp);
+  int nodes_found = 0;
+  if (want_nodes) {  // the IB nodes (marked 2) and their interpolation records
+    const int nb = (int)((N + 255) / 256);
+    std::vector<double> q, rad;
+    bounding_sphere(n_elmt, tri, x, y, z, q, rad);
+    std::vector<int> bcount(nb), boff(nb + 1, 0);
+    int *dcount = nullptr, *dlist = nullptr;
+    double *dq = nullptr, *drad = nullptr;
+    bool ok = cudaMalloc(&dcount, (size_t)nb * 4) == cudaSuccess;
+    if (ok) {
+      k_ibm_mark_count<<<nb, 256, 0, st>>>(g, dtmp, dcount);
+      ok = cudaMemcpyAsync(bcount.data(), dcount, (size_t)nb * 4, cudaMemcpyDeviceToHost, st) == cudaSuccess &&
+           cudaStreamSynchronize(st) == cudaSuccess;
+    }
+    if (ok) {
+      for (int q2 = 0; q2 < nb; q2++) boff[q2 + 1] = boff[q2] + bcount[q2];
+      nodes_found = boff[nb];
+      ok = cudaMemcpyAsync(dcount, boff.data(), (size_t)nb * 4, cudaMemcpyHostToDevice, st) == cudaSuccess &&
+           cudaMalloc(&dlist, (size_t)std::max(nodes_found, 1) * 4) == cudaSuccess &&
+           cudaMalloc(&dq, q.size() * 8) == cudaSuccess && cudaMalloc(&drad, rad.size() * 8) == cudaSuccess;
+    }
+    IbmBody body;
+    body.n_nodes = nodes_found;
+    body.n_elmt = n_elmt;
+    body.n_v = n_v;
+    if (ok)
+      ok = cudaMalloc(&body.nodes, (size_t)std::max(nodes_found, 1) * sizeof(vfs_ibm_node)) == cudaSuccess &&
+           cudaMalloc(&body.tri, (size_t)n_elmt * 3 * 4) == cudaSuccess;
+    if (ok) {
+      cudaMemcpyAsync(dq, q.data(), q.size() * 8, cudaMemcpyHostToDevice, st);
+      cudaMemcpyAsync(drad, rad.data(), rad.size() * 8, cudaMemcpyHostToDevice, st);
+      cudaMemcpyAsync(body.tri, tri, (size_t)n_elmt * 3 * 4, cudaMemcpyHostToDevice, st);
+      k_ibm_mark_scatter<<<nb, 256, 0, st>>>(g, dtmp, dcount, dlist);
+      if (nodes_found > 0)
+        k_ibm_nodes<<<(nodes_found + 127) / 128, 128, 0, st>>>(g, cx.cent, dlist, nodes_found, n_elmt,
+                                                               (const double *)buf[3], (const double *)buf[4], dq,
+                                                               drad, body.nodes);
+      *cx.launches += 3;
+      ok = cudaStreamSynchronize(st) == cudaSuccess;
+    }
+    if (dcount) cudaFree(dcount);
+    if (dlist) cudaFree(dlist);
+    if (dq) cudaFree(dq);
+    if (drad) cudaFree(drad);
+    if (!ok) {
+      cudaGetLastError();
+      if (body.nodes) cudaFree(body.nodes);
+      if (body.tri) cudaFree(body.tri);
+      cleanup();
+      return fail(VFS_ECUDA, "IB node records: allocation or launch failed");
+    }
+    auto &B = *cx.bodies;
+    if ((int)B.size() <= ibi) B.resize(ibi + 1);
+    if (B[ibi].nodes) cudaFree(B[ibi].nodes);
+    if (B[ibi].tri) cudaFree(B[ibi].tri);
+    B[ibi] = body;
+  }
   int b[6] = {0, 0, 0, 0, 0, 0};
   if (bctype)
     for (int q = 0; q < 6; q++) b[q] = bctype[q];
@@ -308,5 +634,189 @@ extern "C" int vfs_poisson_ibm_search(vfs_poisson *h, int ibi, int n_v, const do
     return fail(VFS_ECUDA, std::string("surface search: ") + cudaGetErrorString(e));
   }
   if (n_failed) *n_failed = nfail;
+  if (n_nodes) *n_nodes = nodes_found;
   return VFS_OK;
 }
+
+}  // namespace
+
+extern "C" int vfs_poisson_ibm_search(vfs_poisson *h, int ibi, int n_v, const double *xyz, int n_elmt,
+                                      const int32_t *tri, const int *bctype, double *nvert, int *n_failed) {
+  return ibm_search_impl(h, ibi, n_v, xyz, n_elmt, tri, bctype, nvert, n_failed, false, nullptr);
+}
+
+extern "C" int vfs_poisson_ibm_search_nodes(vfs_poisson *h, int ibi, int n_v, const double *xyz, int n_elmt,
+                                            const int32_t *tri, const int *bctype, double *nvert, int *n_failed,
+                                            int *n_nodes) {
+  return ibm_search_impl(h, ibi, n_v, xyz, n_elmt, tri, bctype, nvert, n_failed, true, n_nodes);
+}
+
+extern "C" int vfs_poisson_ibm_nodes(vfs_poisson *h, int ibi, vfs_ibm_node *nodes, int max_nodes, int *n_nodes) {
+  if (!h || max_nodes < 0 || (max_nodes > 0 && !nodes)) return fail(VFS_EINVAL, "bad arguments");
+  IbmContext cx;
+  int rc = ibm_context(h, &cx);
+  if (rc != VFS_OK) return rc;
+  const auto &B = *cx.bodies;
+  if (ibi < 0 || ibi >= (int)B.size() || !B[ibi].nodes) return fail(VFS_ESTATE, "no IB nodes for this body");
+  const int n = B[ibi].n_nodes;
+  if (n_nodes) *n_nodes = n;
+  const int c = std::min(n, max_nodes);
+  if (c > 0 && cudaMemcpy(nodes, B[ibi].nodes, (size_t)c * sizeof(vfs_ibm_node), cudaMemcpyDeviceToHost) !=
+                   cudaSuccess) {
+    cudaGetLastError();
+    return fail(VFS_ECUDA, "copy of the IB node records failed");
+  }
+  return VFS_OK;
+}
+
+// ---- ibm_interpolation_advanced and IB_BC (launched by poisson.cu) ----
+namespace vfs {
+
+// noslip velocity and interpolated pressure at every IB node of one body
+// (ibm.c:3405-3560, wallfunction.c:140-156); lucat / lp are the inputs as
+// read (the reference's local copies), ucat / p are written at the nodes.
+__global__ void k_ibm_apply(Grid g, const vfs_ibm_node *nodes, int n_nodes, const int *tri, const double *u_surf,
+                            const double *nvert, const double *lucat, const double *lp, double *ucat, double *p) {
+  const int n = blockIdx.x * blockDim.x + threadIdx.x;
+  if (n >= n_nodes) return;
+  const vfs_ibm_node nd = nodes[n];
+  const size_t t = g.at(nd.i, nd.j, nd.k);
+  const size_t t1 = g.at(nd.ip[0], nd.jp[0], nd.kp[0]), t2 = g.at(nd.ip[1], nd.jp[1], nd.kp[1]),
+               t3 = g.at(nd.ip[2], nd.jp[2], nd.kp[2]);
+  const double sb = nd.d_s, sc = sb + nd.d_i;
+  const double sk1 = nd.cr[0], sk2 = nd.cr[1], sk3 = nd.cr[2];
+  double ua[3] = {0., 0., 0.};
+  if (nd.cell >= 0 && u_surf) {
+    const int v1 = tri[3 * nd.cell], v2 = tri[3 * nd.cell + 1], v3 = tri[3 * nd.cell + 2];
+    for (int q = 0; q < 3; q++)
+      ua[q] = u_surf[3 * v1 + q] * nd.cs[0] + u_surf[3 * v2 + q] * nd.cs[1] + u_surf[3 * v3 + q] * nd.cs[2];
+  }
+  if (nvert[t1] + nvert[t2] + nvert[t3] > 0.1 || nvert[t] > 2.9) {
+    for (int q = 0; q < 3; q++) ucat[t * 3 + q] = 0.;
+  } else {
+    for (int q = 0; q < 3; q++) {
+      const double uc = (lucat[t1 * 3 + q] * sk1 + lucat[t2 * 3 + q] * sk2 + lucat[t3 * 3 + q] * sk3);
+      const double uq = uc - ua[q];
+      double v = sb / sc * uq;
+      v += ua[q];
+      ucat[t * 3 + q] = v;
+    }
+  }
+  p[t] = (lp[t1] * sk1 + lp[t2] * sk2 + lp[t3] * sk3);
+}
+
+__device__ inline double face_flux(const double *lu, size_t a, size_t b, const double *m) {
+  const double ucx = (lu[a * 3] + lu[b * 3]) * 0.5;
+  const double ucy = (lu[a * 3 + 1] + lu[b * 3 + 1]) * 0.5;
+  const double ucz = (lu[a * 3 + 2] + lu[b * 3 + 2]) * 0.5;
+  return ucx * m[0] + ucy * m[1] + ucz * m[2];
+}
+
+// the face fluxes around the IB nodes (ibm.c:3577-3630): every interior
+// cell writes only its own three faces, so cells are independent
+__global__ void k_ibm_faces(Grid g, const double *nvert, const double *lu, const double *icsi, const double *jeta,
+                            const double *kzet, double f, int b0, int b1, int b2, int b3, int b4, int b5,
+                            double *ucont) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x + 1, j = blockIdx.y + 1, k = blockIdx.z + 1;
+  if (i >= g.mx - 1) return;
+  const size_t t = g.at(i, j, k), te = g.at(i + 1, j, k), tn = g.at(i, j + 1, k), tt = g.at(i, j, k + 1);
+  const bool wi0 = b0 == -1 || b0 == -2, wi1 = b1 == -1 || b1 == -2, wj0 = b2 == -1 || b2 == -2,
+             wj1 = b3 == -1 || b3 == -2, wk0 = b4 == -1 || b4 == -2, wk1 = b5 == -1 || b5 == -2;
+  if ((int)(nvert[t] + 0.5) == 1) {
+    ucont[t * 3] = face_flux(lu, t, te, &icsi[t * 3]) * f;
+    ucont[t * 3 + 1] = face_flux(lu, tn, t, &jeta[t * 3]) * f;
+    ucont[t * 3 + 2] = face_flux(lu, tt, t, &kzet[t * 3]) * f;
+    if (wi0 && i == 1) ucont[t * 3] = 0;
+    if (wj0 && j == 1) ucont[t * 3 + 1] = 0;
+    if (wk0 && k == 1) ucont[t * 3 + 2] = 0;
+  }
+  if ((int)(nvert[te] + 0.5) == 1) {
+    ucont[t * 3] = face_flux(lu, t, te, &icsi[t * 3]) * f;
+    if (wi1 && i == g.mx - 3) ucont[t * 3] = 0;
+  }
+  if ((int)(nvert[tn] + 0.5) == 1) {
+    ucont[t * 3 + 1] = face_flux(lu, tn, t, &jeta[t * 3]) * f;
+    if (wj1 && j == g.my - 3) ucont[t * 3 + 1] = 0;
+  }
+  if ((int)(nvert[tt] + 0.5) == 1) {
+    ucont[t * 3 + 2] = face_flux(lu, tt, t, &kzet[t * 3]) * f;
+    if (wk1 && k == g.mz - 3) ucont[t * 3 + 2] = 0;
+  }
+}
+
+// IB_BC's interior loop (momentum.c:2114-2178): the IB faces from ucat
+// ((int)nvert == 1), the immersed == 3 zeroing and the -1/-2 walls in i and
+// j (the i == 1 / j == 1 rows write the face below them, which no other cell
+// of this loop writes)
+__global__ void k_ib_bc_faces(Grid g, const double *nvert, const double *lu, const double *icsi,
+                              const double *jeta, const double *kzet, int immersed, int b0, int b1, int b2, int b3,
+                              double *ucont) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x + 1, j = blockIdx.y + 1, k = blockIdx.z + 1;
+  if (i >= g.mx - 1) return;
+  const size_t t = g.at(i, j, k), te = g.at(i + 1, j, k), tn = g.at(i, j + 1, k), tt = g.at(i, j, k + 1);
+  if (immersed) {
+    const double f = immersed == 3 ? 0. : 1.;
+    if ((int)nvert[t] == 1) {
+      ucont[t * 3] = face_flux(lu, t, te, &icsi[t * 3]) * f;
+      ucont[t * 3 + 1] = face_flux(lu, tn, t, &jeta[t * 3]) * f;
+      ucont[t * 3 + 2] = face_flux(lu, tt, t, &kzet[t * 3]) * f;
+    }
+    if ((int)(nvert[te]) == 1) ucont[t * 3] = face_flux(lu, t, te, &icsi[t * 3]) * f;
+    if ((int)(nvert[tn]) == 1) ucont[t * 3 + 1] = face_flux(lu, tn, t, &jeta[t * 3]) * f;
+    if ((int)(nvert[tt]) == 1) ucont[t * 3 + 2] = face_flux(lu, tt, t, &kzet[t * 3]) * f;
+    if (immersed == 3) {
+      if ((nvert[te] + nvert[t]) > 1.1) ucont[t * 3] = 0;
+      if ((nvert[tn] + nvert[t]) > 1.1) ucont[t * 3 + 1] = 0;
+      if ((nvert[tt] + nvert[t]) > 1.1) ucont[t * 3 + 2] = 0;
+    }
+  }
+  const bool wi0 = b0 == -1 || b0 == -2, wi1 = b1 == -1 || b1 == -2, wj0 = b2 == -1 || b2 == -2,
+             wj1 = b3 == -1 || b3 == -2;
+  if ((wi0 && i == 1) || (wi1 && i == g.mx - 2)) {
+    if (i == 1) ucont[g.at(i - 1, j, k) * 3] = 0;
+    else ucont[t * 3] = 0;
+  }
+  if ((wj0 && j == 1) || (wj1 && j == g.my - 2)) {
+    if (j == 1) ucont[g.at(i, j - 1, k) * 3 + 1] = 0;
+    else ucont[t * 3 + 1] = 0;
+  }
+}
+
+// IB_BC's closing loop over every DA point (momentum.c:2180-2210): the slip
+// (10) walls and the periodic faces.  The reference runs it in place in
+// k, j, i order; a periodic copy there reads its partner before a slip rule
+// of the same row could zero it, so every value follows from the values
+// before the loop (uold).
+__global__ void k_ib_bc_edges(Grid g, const double *uold, int b0, int b1, int b2, int b3, int b4, int b5,
+                              double *ucont) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y, k = blockIdx.z;
+  if (i >= g.mx) return;
+  const size_t t = g.at(i, j, k);
+  double vx = uold[t * 3], vy = uold[t * 3 + 1], vz = uold[t * 3 + 2];
+  if (i == 0) {
+    if (g.px) vx = uold[g.at(g.mx - 2, j, k) * 3];
+    if (b0 == 10) vx = 0;
+  } else if (i == g.mx - 1) {
+    if (g.px) vx = uold[g.at(1, j, k) * 3];
+  }
+  if (i == g.mx - 2 && b1 == 10) vx = 0;
+  if (j == 0) {
+    if (g.py) vy = uold[g.at(i, g.my - 2, k) * 3 + 1];
+    if (b2 == 10) vy = 0;
+  } else if (j == g.my - 1) {
+    if (g.py) vy = uold[g.at(i, 1, k) * 3 + 1];
+  }
+  if (j == g.my - 2 && b3 == 10) vy = 0;
+  if (k == 0) {
+    if (g.pz) vz = uold[g.at(i, j, g.mz - 2) * 3 + 2];
+    if (b4 == 10) vz = 0;
+  } else if (k == g.mz - 1) {
+    if (g.pz) vz = uold[g.at(i, j, 1) * 3 + 2];
+  }
+  if (k == g.mz - 2 && b5 == 10) vz = 0;
+  ucont[t * 3] = vx;
+  ucont[t * 3 + 1] = vy;
+  ucont[t * 3 + 2] = vz;
+}
+
+}  // namespace vfs

@@ -2,7 +2,10 @@
 #pragma once
 #include <cuda_fp16.h>
 
+#include <vector>
+
 #include "common.cuh"
+#include "vfs_poisson.h"
 
 namespace vfs {
 
@@ -120,11 +123,31 @@ __global__ void k_sumsq(size_t n, const double *x, double *partial);
 
 // Hand-off from a handle to the surface search (ibm.cu): its stream, grid,
 // DA-layout cell centres and launch counter.
+// One body's IB node records in device memory (built by the surface
+// search in ibm.cu, applied by vfs_poisson_ibm_interpolate; the handle owns
+// and frees them).
+struct IbmBody {
+  int n_nodes = 0, n_elmt = 0, n_v = 0;
+  vfs_ibm_node *nodes = nullptr;
+  int *tri = nullptr;
+};
 struct IbmContext {
   cudaStream_t stream;
   Grid g;
   const double *cent;
   int64_t *launches;
+  std::vector<IbmBody> *bodies;
 };
+// ibm.cu: the IB interpolation and IB_BC kernels (launched by poisson.cu)
+__global__ void k_ibm_apply(Grid g, const vfs_ibm_node *nodes, int n_nodes, const int *tri, const double *u_surf,
+                            const double *nvert, const double *lucat, const double *lp, double *ucat, double *p);
+__global__ void k_ibm_faces(Grid g, const double *nvert, const double *lu, const double *icsi, const double *jeta,
+                            const double *kzet, double f, int b0, int b1, int b2, int b3, int b4, int b5,
+                            double *ucont);
+__global__ void k_ib_bc_faces(Grid g, const double *nvert, const double *lu, const double *icsi,
+                              const double *jeta, const double *kzet, int immersed, int b0, int b1, int b2, int b3,
+                              double *ucont);
+__global__ void k_ib_bc_edges(Grid g, const double *uold, int b0, int b1, int b2, int b3, int b4, int b5,
+                              double *ucont);
 
 }  // namespace vfs

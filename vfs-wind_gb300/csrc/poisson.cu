@@ -462,6 +462,9 @@ struct vfs_poisson {
   double *gex = nullptr, *gsum = nullptr;
   float *gfeat = nullptr, *gtgt = nullptr, *gfc = nullptr, *gout = nullptr, *gof[2] = {nullptr, nullptr};
   int gsmooth = 2;  // binomial passes over the prolonged correction
+  std::vector<IbmBody> ibm_bodies;  // IB node records per body (ibm.cu)
+  double *ibm_work = nullptr;        // 5 N words + the surface velocities (allocated on first use)
+  size_t ibm_work_len = 0;
   // residual of the iterate installed by the learned guess, handed to the
   // next solve (warm_start 2) so that it does not form it again
   double *rprev = nullptr, *rlearn = nullptr, *r0 = nullptr;
@@ -1276,6 +1279,7 @@ int ibm_context(vfs_poisson *h, IbmContext *c) {
   c->g = h->g;
   c->cent = h->met.cent;
   c->launches = &h->launches;
+  c->bodies = &h->ibm_bodies;
   return VFS_OK;
 }
 }  // namespace vfs
@@ -1368,6 +1372,10 @@ void vfs_poisson_destroy(vfs_poisson *h) {
   drop_graphs(h);
   for (void *p : h->allocs) cudaFree(p);
   h->allocs.clear();
+  for (auto &b : h->ibm_bodies) {
+    if (b.nodes) cudaFree(b.nodes);
+    if (b.tri) cudaFree(b.tri);
+  }
   if (h->hbuf) cudaFreeHost(h->hbuf);
   if (h->ev0) cudaEventDestroy(h->ev0);
   if (h->ev1) cudaEventDestroy(h->ev1);
@@ -1544,6 +1552,92 @@ int vfs_poisson_contra2cart(vfs_poisson *h, const double *ucont, double *ucat, i
   LAUNCH(h, k_periodic_cmpnts, da_grid(h->g), 128, h->g, h->ucat, h->stage);
   if (zero_solid) LAUNCH(h, k_zero_solid, kRedBlocks, 256, h->g, h->nvert, h->stage);
   TRY(download(h, ucat, h->stage, 3 * N));
+  return sync(h);
+}
+
+int vfs_poisson_ibm_interpolate(vfs_poisson *h, int ibi, const double *u_surf, int immersed, const int *bctype,
+                                double *ucat, double *p, double *ucont) {
+  if (!h || !ucat || !p || !ucont) return fail(VFS_EINVAL, "null argument");
+  if (!h->have_nvert) return fail(VFS_ESTATE, "set_nvert must come before the IB interpolation");
+  if (ibi < 0 || ibi >= (int)h->ibm_bodies.size() || !h->ibm_bodies[ibi].nodes)
+    return fail(VFS_ESTATE, "vfs_poisson_ibm_search_nodes must run for this body first");
+  const IbmBody &B = h->ibm_bodies[ibi];
+  const size_t N = h->g.n();
+  if (!h->ucat) TRY(dalloc(h, &h->ucat, 3 * N));
+  // device work space: ucat (h->ucat) and ucont (h->ucont); the copies of
+  // the inputs as read, p and the surface velocities in ibm_work
+  const size_t need = 5 * N + (size_t)B.n_v * 3;
+  if (h->ibm_work_len < need) {
+    if (h->ibm_work) dfree(h, h->ibm_work);
+    h->ibm_work = nullptr;
+    h->ibm_work_len = 0;
+    TRY(dalloc(h, &h->ibm_work, need));
+    h->ibm_work_len = need;
+  }
+  double *lucat = h->ibm_work, *lpr = h->ibm_work + 3 * N, *pd = h->ibm_work + 4 * N, *us = nullptr;
+  TRY(upload(h, h->ucat, ucat, 3 * N));
+  TRY(upload(h, pd, p, N));
+  TRY(upload(h, h->ucont, ucont, 3 * N));
+  CUDA_TRY(cudaMemcpyAsync(lucat, h->ucat, 3 * N * 8, cudaMemcpyDeviceToDevice, h->stream));
+  CUDA_TRY(cudaMemcpyAsync(lpr, pd, N * 8, cudaMemcpyDeviceToDevice, h->stream));
+  if (u_surf) {
+    if (is_device_ptr(u_surf)) {
+      us = const_cast<double *>(u_surf);
+    } else {
+      us = h->ibm_work + 5 * N;
+      CUDA_TRY(cudaMemcpyAsync(us, u_surf, (size_t)B.n_v * 3 * 8, cudaMemcpyHostToDevice, h->stream));
+    }
+  }
+  if (B.n_nodes > 0)
+    LAUNCH(h, k_ibm_apply, (B.n_nodes + 127) / 128, 128, h->g, B.nodes, B.n_nodes, B.tri, us, h->nvert, lucat, lpr,
+           h->ucat, pd);
+  // the new ucat with periodic ghosts (the local copy the flux loop reads)
+  LAUNCH(h, k_periodic_cmpnts, da_grid(h->g), 128, h->g, h->ucat, h->stage);
+  int b[6] = {0, 0, 0, 0, 0, 0};
+  if (bctype)
+    for (int q = 0; q < 6; q++) b[q] = bctype[q];
+  LAUNCH(h, k_ibm_faces, dim3((h->g.mx - 2 + 127) / 128, h->g.my - 2, h->g.mz - 2), 128, h->g, h->nvert, h->stage,
+         h->met.icsi, h->met.jeta, h->met.kzet, immersed == 3 ? 0. : 1., b[0], b[1], b[2], b[3], b[4], b[5],
+         h->ucont);
+  // Contra2Cart with the solid zeroing
+  LAUNCH(h, k_periodic_cmpnts, da_grid(h->g), 128, h->g, h->ucont, h->stage);
+  LAUNCH(h, k_contra2cart, dim3((h->g.mx - 2 + 127) / 128, h->g.my - 2, h->g.mz - 2), 128, h->g, h->nvert, h->met,
+         h->stage, h->ucat);
+  LAUNCH(h, k_periodic_cmpnts, da_grid(h->g), 128, h->g, h->ucat, h->stage);
+  LAUNCH(h, k_zero_solid, kRedBlocks, 256, h->g, h->nvert, h->stage);
+  TRY(download(h, ucat, h->stage, 3 * N));
+  TRY(download(h, p, pd, N));
+  TRY(download(h, ucont, h->ucont, 3 * N));
+  return sync(h);
+}
+
+int vfs_poisson_ib_bc(vfs_poisson *h, int immersed, const int *bctype, double *ucat, double *ucont) {
+  if (!h || !ucat || !ucont) return fail(VFS_EINVAL, "null argument");
+  if (!h->have_nvert) return fail(VFS_ESTATE, "set_nvert must come before IB_BC");
+  const size_t N = h->g.n();
+  if (!h->ucat) TRY(dalloc(h, &h->ucat, 3 * N));
+  TRY(upload(h, h->ucat, ucat, 3 * N));
+  TRY(upload(h, h->ucont, ucont, 3 * N));
+  int b[6] = {0, 0, 0, 0, 0, 0};
+  if (bctype)
+    for (int q = 0; q < 6; q++) b[q] = bctype[q];
+  // periodic ghosts of ucat from their partners (written back: the
+  // reference writes them into lUcat)
+  LAUNCH(h, k_periodic_cmpnts, da_grid(h->g), 128, h->g, h->ucat, h->stage);
+  LAUNCH(h, k_ib_bc_faces, dim3((h->g.mx - 2 + 127) / 128, h->g.my - 2, h->g.mz - 2), 128, h->g, h->nvert,
+         h->stage, h->met.icsi, h->met.jeta, h->met.kzet, immersed, b[0], b[1], b[2], b[3], h->ucont);
+  if (h->ibm_work_len < 3 * N) {
+    if (h->ibm_work) dfree(h, h->ibm_work);
+    h->ibm_work = nullptr;
+    h->ibm_work_len = 0;
+    TRY(dalloc(h, &h->ibm_work, 3 * N));
+    h->ibm_work_len = 3 * N;
+  }
+  double *uold = h->ibm_work;
+  CUDA_TRY(cudaMemcpyAsync(uold, h->ucont, 3 * N * 8, cudaMemcpyDeviceToDevice, h->stream));
+  LAUNCH(h, k_ib_bc_edges, da_grid(h->g), 128, h->g, uold, b[0], b[1], b[2], b[3], b[4], b[5], h->ucont);
+  TRY(download(h, ucat, h->stage, 3 * N));
+  TRY(download(h, ucont, h->ucont, 3 * N));
   return sync(h);
 }
 

@@ -39,7 +39,16 @@ EXPORTS = [
     "vfs_unet_set_grads", "vfs_unet_kernel_launches", "vfs_poisson_learned_guess", "vfs_poisson_guess_sample",
     "vfs_poisson_get_operator32", "vfs_poisson_rhs2", "vfs_poisson_volume_flux", "vfs_poisson_contra2cart",
     "vfs_read_petsc_vec", "vfs_write_petsc_vec", "vfs_read_grid", "vfs_read_ucd", "vfs_poisson_set_levelset",
+    "vfs_poisson_ibm_search_nodes", "vfs_poisson_ibm_nodes", "vfs_poisson_ibm_interpolate", "vfs_poisson_ib_bc",
 ]
+
+
+class IbmNode(C.Structure):
+    """One IB node's interpolation record (vfs_ibm_node)."""
+    _fields_ = [("i", C.c_int), ("j", C.c_int), ("k", C.c_int), ("cell", C.c_int),
+                ("pmin", C.c_double * 3), ("d_s", C.c_double), ("cs", C.c_double * 3),
+                ("ip", C.c_int * 3), ("jp", C.c_int * 3), ("kp", C.c_int * 3),
+                ("cr", C.c_double * 3), ("d_i", C.c_double), ("imode", C.c_int), ("status", C.c_int)]
 
 
 class GridDesc(C.Structure):
@@ -118,6 +127,11 @@ def load(path=LIB_PATH):
     L.vfs_poisson_profile_read.argtypes = [vp, P(C.c_double), P(C.c_double), P(C.c_int64)]
     L.vfs_divergence_noalloc.argtypes = [P(GridDesc), vp, vp, vp, vp, vp]
     L.vfs_poisson_ibm_search.argtypes = [vp, C.c_int, C.c_int, vp, C.c_int, vp, vp, vp, P(C.c_int)]
+    L.vfs_poisson_ibm_search_nodes.argtypes = [vp, C.c_int, C.c_int, vp, C.c_int, vp, vp, vp, P(C.c_int),
+                                               P(C.c_int)]
+    L.vfs_poisson_ibm_nodes.argtypes = [vp, C.c_int, vp, C.c_int, P(C.c_int)]
+    L.vfs_poisson_ibm_interpolate.argtypes = [vp, C.c_int, vp, C.c_int, vp, vp, vp, vp]
+    L.vfs_poisson_ib_bc.argtypes = [vp, C.c_int, vp, vp, vp]
     L.vfs_unet_create.argtypes = [C.c_uint, P(vp)]
     L.vfs_unet_destroy.argtypes = [vp]
     L.vfs_unet_destroy.restype = None
@@ -288,6 +302,42 @@ class PoissonSolver:
         _check(load().vfs_poisson_ibm_search(self.h, ibi, xyz.shape[0], _ptr(xyz), tri.shape[0], _ptr(tri),
                                              bc, _ptr(out, True), C.byref(nf)))
         return out, nf.value
+
+    def ibm_search_nodes(self, surface, nvert=None, ibi=0, bctype=None):
+        """ibm_search plus the interpolation records of the body's IB nodes
+        (kept in the handle); returns (nvert, cells that gave up, nodes)."""
+        xyz = np.ascontiguousarray(surface[0], np.float64)
+        tri = np.ascontiguousarray(surface[1], np.int32)
+        out = np.zeros(self._shape()) if nvert is None else nvert
+        bc = None if bctype is None else (C.c_int * 6)(*[int(b) for b in bctype])
+        nf, nn = C.c_int(), C.c_int()
+        _check(load().vfs_poisson_ibm_search_nodes(self.h, ibi, xyz.shape[0], _ptr(xyz), tri.shape[0], _ptr(tri),
+                                                   bc, _ptr(out, True), C.byref(nf), C.byref(nn)))
+        return out, nf.value, nn.value
+
+    def ibm_nodes(self, ibi=0):
+        """The IB node records of body ibi (a ctypes array of IbmNode)."""
+        n = C.c_int()
+        _check(load().vfs_poisson_ibm_nodes(self.h, ibi, None, 0, C.byref(n)))
+        arr = (IbmNode * max(n.value, 1))()
+        _check(load().vfs_poisson_ibm_nodes(self.h, ibi, C.cast(arr, C.c_void_p), n.value, C.byref(n)))
+        return arr, n.value
+
+    def ibm_interpolate(self, ucat, p, ucont, ibi=0, u_surf=None, immersed=1, bctype=None):
+        """ibm_interpolation_advanced with no-slip for body ibi; ucat, p,
+        ucont in/out (DA layout)."""
+        bc = None if bctype is None else (C.c_int * 6)(*[int(b) for b in bctype])
+        us = None if u_surf is None else np.ascontiguousarray(u_surf, np.float64)
+        _check(load().vfs_poisson_ibm_interpolate(self.h, ibi, _ptr(us), int(immersed), bc, _ptr(ucat, True),
+                                                  _ptr(p, True), _ptr(ucont, True)))
+        return ucat, p, ucont
+
+    def ib_bc(self, ucat, ucont, immersed=1, bctype=None):
+        """IB_BC: face fluxes around the IB nodes and the wall / slip /
+        periodic faces; ucat (periodic ghosts) and ucont in/out."""
+        bc = None if bctype is None else (C.c_int * 6)(*[int(b) for b in bctype])
+        _check(load().vfs_poisson_ib_bc(self.h, int(immersed), bc, _ptr(ucat, True), _ptr(ucont, True)))
+        return ucat, ucont
 
     # --- inspection ---
     def numbering(self):

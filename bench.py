@@ -73,6 +73,17 @@ def dist_env():
             int(os.environ.get("WORLD_SIZE", 1)))
 
 
+def replica_max(values, dist=None, device="cpu"):
+    """The solve does not shard: every rank runs a replica, and the job's
+    time per step is the slowest rank's (max over ranks of each value)."""
+    if dist is None:
+        return [float(v) for v in values]
+    import torch
+    t = torch.tensor([float(v) for v in values], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(v) for v in t.tolist()]
+
+
 def peaks():
     try:
         with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as f:
@@ -315,10 +326,7 @@ def run_ours(args):
     barrier()
     ms_b_mean = statistics.mean(ms_b)
     ms_a_mean = statistics.mean(ms_a)
-    if dist is not None:
-        t = torch.tensor([ms_b_mean, ms_a_mean], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms_b_mean, ms_a_mean = float(t[0]), float(t[1])
+    ms_b_mean, ms_a_mean = replica_max([ms_b_mean, ms_a_mean], dist, "cuda")
 
     # accuracy and projection on the last held-out step
     u = step_inputs(n - 1)

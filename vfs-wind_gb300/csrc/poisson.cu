@@ -969,7 +969,15 @@ void vcycle(vfs_poisson *h, int li, int nu1, int nu2, T omega, int smoother) {
   }
   if (nu1 == 0) cudaMemsetAsync(x, 0, l.b.n() * sizeof(T), h->stream);
   for (int s = 0; s < nu1; s++) smooth<T>(h, l, li, smoother, s == 0, omega, x, t, bb, r);
-  Prec<T>::residual(h, l, box_grid(l.b), x, bb, r, -1);
+  if (smoother == 3 && nu1 > 0 && omega == (T)1) {
+    // the second colour's lines were just solved exactly (omega 1), so its
+    // residual is zero up to rounding: form the first colour's only
+    const int nh = (l.b.nx + 1) / 2;
+    cudaMemsetAsync(r, 0, l.b.n() * sizeof(T), h->stream);
+    Prec<T>::residual(h, l, dim3((nh + 127) / 128, l.b.ny, l.b.nz), x, bb, r, 6);
+  } else {
+    Prec<T>::residual(h, l, box_grid(l.b), x, bb, r, -1);
+  }
   Level &q = h->L[li + 1];
   LAUNCH(h, Prec<T>::restrict_, box_grid(q.b), 128, l.b, q.b, l.cx, l.cy, l.cz, r, Prec<T>::w(l), q.blank,
          Prec<T>::v(q)[1]);

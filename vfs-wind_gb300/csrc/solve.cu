@@ -15,15 +15,16 @@ namespace vfs {
 // x, rhs natural).  `color`: -1 every row; 0/1 the k-planes with k % 2 ==
 // color; 2/3 the checkerboard columns with (i + k) % 2 == color - 2, whose
 // residuals are then written at their split positions (the layout the line
-// kernel reads them in).  Threads walk split positions, so operator loads
-// coalesce.
+// kernel reads them in); 6/7 the same columns with (i + k) % 2 == color - 6
+// written at their natural positions.  Threads walk split positions, so
+// operator loads coalesce.
 //
 // The row a thread takes: its split position p (false when the thread has no
 // row of the colour).
 __device__ __forceinline__ bool colour_row(const Box &b, int color, int t, int k, int &p) {
   p = t;
   if (color >= 2) {
-    const int par = (color - 2 + k) & 1, nh = (b.nx + 1) >> 1;
+    const int par = ((color >= 6 ? color - 6 : color - 2) + k) & 1, nh = (b.nx + 1) >> 1;
     if (t >= (par ? b.nx - nh : nh)) return false;
     p = par ? nh + t : t;
     return true;
@@ -44,7 +45,7 @@ __device__ __forceinline__ void residual_body(Box b, const T *__restrict__ A, co
   T s = (T)0;
 #pragma unroll
   for (int q = 0; q < NSLOT; q++) s += __ldcs(&A[q * n + cs]) * __ldg(&x[idx[q]]);
-  r[color >= 2 ? cs : c] = rhs[c] - s;
+  r[color == 2 || color == 3 ? cs : c] = rhs[c] - s;
 }
 
 // The FP32 V-cycle's copy of a level operator (split layout): D = the
@@ -89,7 +90,7 @@ __global__ void __launch_bounds__(128) k_residual16(Box b, const __half2 *__rest
   }
   const float2 f = __half22float2(__ldcs(&C[9 * n + cs]));
   s = fmaf(f.x, xc, s);
-  r[color >= 2 ? cs : c] = rhs[c] - __ldcs(&D[cs]) * s;
+  r[color == 2 || color == 3 ? cs : c] = rhs[c] - __ldcs(&D[cs]) * s;
 }
 
 // FP64 y = A x on the unscaled operator.

@@ -982,7 +982,8 @@ void vcycle(vfs_poisson *h, int li, int nu1, int nu2, T omega, int smoother) {
   LAUNCH(h, Prec<T>::restrict_, box_grid(q.b), 128, l.b, q.b, l.cx, l.cy, l.cz, r, Prec<T>::w(l), q.blank,
          Prec<T>::v(q)[1]);
   vcycle<T>(h, li + 1, nu1, nu2, omega, smoother);
-  LAUNCH(h, Prec<T>::prolong, box_grid(l.b), 128, l.b, q.b, l.cx, l.cy, l.cz, (const T *)Prec<T>::xfinal(q), q.blank,
+  LAUNCH(h, Prec<T>::prolong, dim3((l.b.nx + 127) / 128, (l.b.ny + 1) / 2, l.b.nz), 128, l.b, q.b, l.cx, l.cy,
+         l.cz, (const T *)Prec<T>::xfinal(q), q.blank,
          l.blank, x, 1);
   for (int s = 0; s < nu2; s++) smooth<T>(h, l, li, smoother, false, omega, x, t, bb, r);
   Prec<T>::xfinal(l) = x;

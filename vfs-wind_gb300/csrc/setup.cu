@@ -985,48 +985,69 @@ template <typename T>
 __device__ __forceinline__ void prolong_body(Box bf, Box bc, int cx, int cy, int cz, const T *__restrict__ xc,
                                              const uint8_t *__restrict__ blank_c, const uint8_t *__restrict__ blank_f,
                                              T *xf, int add) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y, k = blockIdx.z;
+  // a thread takes rows j = blockIdx.y and blockIdx.y + gridDim.y of column
+  // i (when inside the box): all the loads of both cells first, then both
+  // results
+  const int i = blockIdx.x * blockDim.x + threadIdx.x, k = blockIdx.z;
   if (i >= bf.nx) return;
-  const size_t c = bf.at(i, j, k);
-  const int I = i + 1, J = j + 1, K = k + 1;
   const int mx = bf.nx + 2, my = bf.ny + 2, mz = bf.nz + 2;
-  int ic, jc, kc, ia, ja, ka;
+  const int I = i + 1, K = k + 1;
+  int ic, kc, ia, ka;
   if (!cx) { ic = I; ia = 0; } else { ic = (I + 1) / 2; ia = (I - 2 * ic) == 0 ? 1 : -1; if (I == 1 || I == mx - 2) ia = 0; }
-  if (!cy) { jc = J; ja = 0; } else { jc = (J + 1) / 2; ja = (J - 2 * jc) == 0 ? 1 : -1; if (J == 1 || J == my - 2) ja = 0; }
   if (!cz) { kc = K; ka = 0; } else { kc = (K + 1) / 2; ka = (K - 2 * kc) == 0 ? 1 : -1; if (K == 1 || K == mz - 2) ka = 0; }
-  // every load in one round trip: the fine blank flag, the three coarse
-  // neighbours' blank flags and the 8 coarse values at the unblanked
-  // offsets (all inside the coarse box); a blanked neighbour then selects
-  // the centre-side value, exactly the stencil the offsets would give
-  // 32-bit offsets into the coarse box (fewer than 2^31 cells)
-  const int base = ((kc - 1) * bc.ny + (jc - 1)) * bc.nx + (ic - 1);
-  const int oi = ia, oj = ja * bc.nx, ok = ka * bc.nx * bc.ny;
-  const uint8_t bf0 = blank_f[c];
-  const uint8_t nk = blank_c[base + ok], nj = blank_c[base + oj], ni = blank_c[base + oi];
-  T X[2][2][2];  // [i side][j side][k side]
+  size_t c[2];
+  bool valid[2];
+  int ja[2];
+  uint8_t bf0[2], ni[2], nj[2], nk[2];
+  T X[2][2][2][2], xold[2];  // [row][i side][j side][k side]
 #pragma unroll
-  for (int q = 0; q < 8; q++) {
-    const int a = q & 1, bb = (q >> 1) & 1, cc = q >> 2;
-    X[a][bb][cc] = xc[base + a * oi + bb * oj + cc * ok];
+  for (int r = 0; r < 2; r++) {
+    const int j = blockIdx.y + r * gridDim.y;
+    valid[r] = j < bf.ny;
+    if (!valid[r]) continue;
+    c[r] = bf.at(i, j, k);
+    const int J = j + 1;
+    int jc;
+    if (!cy) { jc = J; ja[r] = 0; } else { jc = (J + 1) / 2; ja[r] = (J - 2 * jc) == 0 ? 1 : -1; if (J == 1 || J == my - 2) ja[r] = 0; }
+    // every load in one round trip: the fine blank flag, the three coarse
+    // neighbours' blank flags and the 8 coarse values at the unblanked
+    // offsets (all inside the coarse box); a blanked neighbour then
+    // selects the centre-side value, exactly the stencil the offsets
+    // would give; 32-bit offsets into the coarse box (fewer than 2^31 cells)
+    const int base = ((kc - 1) * bc.ny + (jc - 1)) * bc.nx + (ic - 1);
+    const int oi = ia, oj = ja[r] * bc.nx, ok = ka * bc.nx * bc.ny;
+    bf0[r] = blank_f[c[r]];
+    nk[r] = blank_c[base + ok];
+    nj[r] = blank_c[base + oj];
+    ni[r] = blank_c[base + oi];
+#pragma unroll
+    for (int q = 0; q < 8; q++) {
+      const int a = q & 1, bb = (q >> 1) & 1, cc = q >> 2;
+      X[r][a][bb][cc] = xc[base + a * oi + bb * oj + cc * ok];
+    }
+    xold[r] = add ? xf[c[r]] : (T)0;
   }
-  const T xold = add ? xf[c] : (T)0;
-  if (bf0) { if (!add) xf[c] = (T)0; return; }
-  // the reference zeroes an offset whose coarse neighbour is blank; an
-  // offset already 0 reads the centre (its test reads the centre cell, which
-  // an unblanked fine cell's parent is not)
-  const bool zk = ka != 0 && nk, zj = ja != 0 && nj, zi = ia != 0 && ni;
-  // collapse the zeroed offsets one axis after the other (constant indices
-  // keep X in registers)
 #pragma unroll
-  for (int q = 0; q < 4; q++) X[1][q & 1][q >> 1] = zi ? X[0][q & 1][q >> 1] : X[1][q & 1][q >> 1];
+  for (int r = 0; r < 2; r++) {
+    if (!valid[r]) continue;
+    if (bf0[r]) { if (!add) xf[c[r]] = (T)0; continue; }
+    // the reference zeroes an offset whose coarse neighbour is blank; an
+    // offset already 0 reads the centre (its test reads the centre cell,
+    // which an unblanked fine cell's parent is not).  Collapse the zeroed
+    // offsets one axis after the other (constant indices keep X in
+    // registers).
+    const bool zk = ka != 0 && nk[r], zj = ja[r] != 0 && nj[r], zi = ia != 0 && ni[r];
 #pragma unroll
-  for (int q = 0; q < 4; q++) X[q & 1][1][q >> 1] = zj ? X[q & 1][0][q >> 1] : X[q & 1][1][q >> 1];
+    for (int q = 0; q < 4; q++) X[r][1][q & 1][q >> 1] = zi ? X[r][0][q & 1][q >> 1] : X[r][1][q & 1][q >> 1];
 #pragma unroll
-  for (int q = 0; q < 4; q++) X[q & 1][q >> 1][1] = zk ? X[q & 1][q >> 1][0] : X[q & 1][q >> 1][1];
-  T v = (X[0][0][0] * (T)9 + X[0][1][0] * (T)3 + X[1][0][0] * (T)3 + X[1][1][0]) * (T)3. / (T)64. +
-        (X[0][0][1] * (T)9 + X[0][1][1] * (T)3 + X[1][0][1] * (T)3 + X[1][1][1]) / (T)64.;
-  if (add) xf[c] = xold + v;
-  else xf[c] = v;
+    for (int q = 0; q < 4; q++) X[r][q & 1][1][q >> 1] = zj ? X[r][q & 1][0][q >> 1] : X[r][q & 1][1][q >> 1];
+#pragma unroll
+    for (int q = 0; q < 4; q++) X[r][q & 1][q >> 1][1] = zk ? X[r][q & 1][q >> 1][0] : X[r][q & 1][q >> 1][1];
+    T v = (X[r][0][0][0] * (T)9 + X[r][0][1][0] * (T)3 + X[r][1][0][0] * (T)3 + X[r][1][1][0]) * (T)3. / (T)64. +
+          (X[r][0][0][1] * (T)9 + X[r][0][1][1] * (T)3 + X[r][1][0][1] * (T)3 + X[r][1][1][1]) / (T)64.;
+    if (add) xf[c[r]] = xold[r] + v;
+    else xf[c[r]] = v;
+  }
 }
 
 __global__ void k_restrict_f32(Box bf, Box bc, int cx, int cy, int cz, const float *rf, const float *wf,

@@ -382,7 +382,7 @@ def run_ours(args):
         "vs_baseline": None, "dtype": "f64/f32/bf16", "data": "synthetic",
         "config": {
             "workload": workload(nx, ny, nz), "cells": nx * ny * nz, "rtol": 1e-8,
-            "solver": "FGMRES(20) with delayed CGS2, FP64 residual, operator apply and Krylov; FP32 geometric "
+            "solver": "FGMRES(20) with one-pass classical Gram-Schmidt, FP64 residual, operator apply and Krylov; FP32 geometric "
                       "V-cycle (zebra j-line Gauss-Seidel over checkerboard columns, 1+2 sweeps; residual couplings "
                       "stored in half precision, difference form); learned initial guess judged against the "
                       "previous step",

@@ -88,6 +88,10 @@ typedef struct {
                          form, 2 zebra line Gauss-Seidel over k-planes,
                          3 (default) zebra line Gauss-Seidel over
                          checkerboard (i + k parity) columns               */
+  int orth;           /* Arnoldi orthogonalisation: 0 (default) classical
+                         Gram-Schmidt in one pass (PETSc GMRES's default
+                         refinement "never"), 1 classical Gram-Schmidt
+                         with delayed reorthogonalisation (DCGS2)          */
 } vfs_solve_opts;
 
 typedef struct {

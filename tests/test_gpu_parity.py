@@ -124,11 +124,12 @@ def _exact(case, d, lhs, b2):
     return O.remove_nullspace(d, case.nvert, lhs["gid"], xe)
 
 
+@pytest.mark.parametrize("orth", [0, 1], ids=["cgs", "dcgs2"])
 @pytest.mark.parametrize("precision", [0, 1], ids=["fp32mg", "fp64mg"])
-def test_solve_matches_exact(pair, precision):
+def test_solve_matches_exact(pair, precision, orth):
     case, s, d, met, lhs = pair
     s.rhs(case.ucont)
-    phi, st = s.solve(precision=precision, rtol=1e-8)
+    phi, st = s.solve(precision=precision, rtol=1e-8, orth=orth)
     assert st.status == 0 and st.rel_residual <= 1e-8, st.as_dict()
     b2 = O.rhs(d, case.nvert, lhs["gid"], case.ucont, met["aj"])
     A = O.csr(lhs)
@@ -181,6 +182,26 @@ def test_mg_transfers_bitexact(pair):
         np.testing.assert_array_equal(s.mg_interpolate(li, xc),
                                       O.interpolation(df, dc, 1 - cx, 1 - cy, 1 - cz, nv_f, nv_c, xc))
         nv_f, df = nv_c, dc
+
+
+@pytest.mark.parametrize("restart", [6, 20])
+def test_orthogonalisation_variants(pair, restart):
+    """One-pass classical Gram-Schmidt and DCGS2 reach the same tolerance in
+    (nearly) the same iterations.  Line Jacobi with one sweep each way keeps
+    a cycle past eight basis vectors (two dots launches per step)."""
+    case, s, d, met, lhs = pair
+    s.rhs(case.ucont)
+    rtol = 1e-9 if restart == 6 else 1e-11
+    res = {}
+    for orth in (0, 1):
+        phi, st = s.solve(rtol=rtol, orth=orth, restart=restart, smoother=0, nu1=1, nu2=1, max_it=400)
+        assert st.status == 0 and st.rel_residual <= rtol, (orth, st.as_dict())
+        res[orth] = (st.iterations, phi)
+    print(case.name, restart, res[0][0], res[1][0])
+    assert abs(res[0][0] - res[1][0]) <= max(1, res[1][0] // 10)
+    fl = case.nvert < 0.1
+    a, b = res[0][1][fl], res[1][1][fl]
+    assert np.linalg.norm(a - b) <= 1e-6 * np.linalg.norm(b)
 
 
 def test_warm_start_and_launch_count(pair):

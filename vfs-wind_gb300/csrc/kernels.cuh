@@ -109,6 +109,20 @@ GS_DOTS_DECL(6)
 GS_DOTS_DECL(7)
 GS_DOTS_DECL(8)
 #undef GS_DOTS_DECL
+#define CGS_DOTS_DECL(NV) \
+  __global__ void k_cgs_dots##NV(size_t n, int v0, const double *const *Q, const double *w, double *partial);
+CGS_DOTS_DECL(1)
+CGS_DOTS_DECL(2)
+CGS_DOTS_DECL(3)
+CGS_DOTS_DECL(4)
+CGS_DOTS_DECL(5)
+CGS_DOTS_DECL(6)
+CGS_DOTS_DECL(7)
+CGS_DOTS_DECL(8)
+#undef CGS_DOTS_DECL
+__global__ void k_cgs_reduce(const double *partial, int nb, const double *dsv, double *red);
+__global__ void k_cgs_update(size_t n, int nv, const double *const *Q, const double *red, double *w,
+                             double *partial);
 __global__ void k_gs_reduce(const double *partial, int nb, int nv, double *red);
 __global__ void k_gs_coef(int nv, double *red);
 __global__ void k_gs_update(size_t n, int nv, const double *const *Q, const double *red, double *u, double *w,

@@ -1114,7 +1114,7 @@ void resolve_opts(vfs_solve_opts &o) {
 int check_opts(const vfs_solve_opts &o) {
   if (!(o.rtol > 0) || o.max_it < 1 || o.restart < 1 || o.restart > 64 || o.nu1 < 0 || o.nu2 < 0 ||
       o.nu1 + o.nu2 < 1 || o.nu1 > 8 || o.nu2 > 8 || !(o.omega > 0 && o.omega <= 1.5) ||
-      (o.precision != 0 && o.precision != 1) || o.smoother < 0 || o.smoother > 3)
+      (o.precision != 0 && o.precision != 1) || o.smoother < 0 || o.smoother > 3 || (o.orth != 0 && o.orth != 1))
     return fail(VFS_EINVAL, "invalid solver options");
   return VFS_OK;
 }
@@ -1130,9 +1130,28 @@ void gs_dots(vfs_poisson *h, int nv, int nb, size_t n, int v0, const double *u, 
   }
 }
 
+// One classical Gram-Schmidt dots launch over basis vectors v0 .. v0+nv-1
+// (1 <= nv <= 8).
+void cgs_dots(vfs_poisson *h, int nv, int nb, size_t n, int v0, const double *w) {
+  const double *const *Q = (const double *const *)h->dV;
+  switch (nv) {
+#define CASE(NV) \
+  case NV: LAUNCH(h, k_cgs_dots##NV, nb, 256, n, v0, Q, w, h->partial); break;
+    CASE(1) CASE(2) CASE(3) CASE(4) CASE(5) CASE(6) CASE(7) CASE(8)
+#undef CASE
+  }
+}
+
 // FGMRES(m) (flexible GMRES: the preconditioned vectors Z_j are kept and
-// x = x0 + Z y) with delayed classical Gram-Schmidt reorthogonalisation.
-// Step j preconditions the pending vector V_j (projected once, divided by its
+// x = x0 + Z y).  The basis vectors stay unnormalised in memory; their
+// norms and inverse norms are reduced on the device (dsv) and every use
+// scales by them.
+// orth 0, classical Gram-Schmidt in one pass: step j preconditions
+// V_j / ||V_j||, applies A, forms h_i = Q_i.w / ||Q_i|| for i <= j in one
+// pass and w - sum h_i Q_i / ||Q_i|| with its norm in another; column j is
+// final at once.
+// orth 1, delayed reorthogonalisation (DCGS2):
+// step j preconditions the pending vector V_j (projected once, divided by its
 // norm reduced on the device), applies A, and one Gram-Schmidt round
 // finishes V_j (reorthogonalised, normalised) and projects A z_j into
 // V_{j+1}.  Finishing V_j = (u - Q a) / r corrects Hessenberg column j-1
@@ -1210,13 +1229,21 @@ int fgmres(vfs_poisson *h, const vfs_solve_opts &o, vfs_solve_stats *st) {
       double *w = h->V[jj + 1];
       LAUNCH(h, k_apply64, box_grid(h->box), 128, h->box, h->A0, h->Z[jj], w);
       if (h->phase) cudaEventRecord(h->phev[2], h->stream);
-      for (int v0 = 0; v0 == 0 || v0 < jj; v0 += 8) gs_dots(h, std::min(8, jj - v0), nbd, n, v0, h->V[jj], w, v0 == 0);
-      LAUNCH(h, k_gs_reduce, 2 * jj + 2, 1024, h->partial, nbd, jj, h->red);
-      LAUNCH(h, k_gs_coef, 1, 32, jj, h->red);
-      LAUNCH(h, k_gs_update, nbd, 256, n, jj, dV, h->red, h->V[jj], w, h->partial);
+      if (o.orth == 0) {
+        for (int v0 = 0; v0 <= jj; v0 += 8) cgs_dots(h, std::min(8, jj + 1 - v0), nbd, n, v0, w);
+        LAUNCH(h, k_cgs_reduce, jj + 1, 1024, h->partial, nbd, h->dsv, h->red);
+        LAUNCH(h, k_cgs_update, nbd, 256, n, jj + 1, dV, h->red, w, h->partial);
+      } else {
+        for (int v0 = 0; v0 == 0 || v0 < jj; v0 += 8)
+          gs_dots(h, std::min(8, jj - v0), nbd, n, v0, h->V[jj], w, v0 == 0);
+        LAUNCH(h, k_gs_reduce, 2 * jj + 2, 1024, h->partial, nbd, jj, h->red);
+        LAUNCH(h, k_gs_coef, 1, 32, jj, h->red);
+        LAUNCH(h, k_gs_update, nbd, 256, n, jj, dV, h->red, h->V[jj], w, h->partial);
+      }
       LAUNCH(h, k_reduce_norm, 1, 1024, h->partial, nbd, h->dsv + 2 * (jj + 1), h->dsv32 + jj + 1);
       if (h->phase) cudaEventRecord(h->phev[3], h->stream);
-      CUDA_TRY(cudaMemcpyAsync(h->hbuf, h->red, (kGsR + 3) * 8, cudaMemcpyDeviceToHost, h->stream));
+      CUDA_TRY(cudaMemcpyAsync(h->hbuf, h->red, (o.orth == 0 ? jj + 1 : kGsR + 3) * 8, cudaMemcpyDeviceToHost,
+                               h->stream));
       CUDA_TRY(cudaMemcpyAsync(h->hbuf + kGsR + 3, h->dsv + 2 * (jj + 1), 8, cudaMemcpyDeviceToHost, h->stream));
       const auto t2 = h->phase ? std::chrono::steady_clock::now() : t0;
       TRY(sync(h));
@@ -1233,21 +1260,25 @@ int fgmres(vfs_poisson *h, const vfs_solve_opts &o, vfs_solve_stats *st) {
       }
       prof_collect(h);
       it++;
-      const double r = h->hbuf[kGsR], hj = h->hbuf[kGsR + 1];
       const double wn = std::sqrt(std::max(h->hbuf[kGsR + 3], 0.));
-      if (jj > 0) {
-        // V_jj lies in the span of the finished vectors: column jj-1 was a
-        // breakdown; the cycle ends with the columns before this step
-        if (!(r > 0.)) break;
-        for (int i = 0; i < jj; i++) Hraw[(size_t)i * m + jj - 1] += h->hbuf[i];
-        Hraw[(size_t)jj * m + jj - 1] = r;
-        gv = gsave;
-        rotate(jj - 1);
+      if (o.orth == 0) {  // column jj is final: H[i, jj] = Q_i.w / ||Q_i||
+        for (int i = 0; i <= jj; i++) Hraw[(size_t)i * m + jj] = h->hbuf[i];
+      } else {
+        const double r = h->hbuf[kGsR], hj = h->hbuf[kGsR + 1];
+        if (jj > 0) {
+          // V_jj lies in the span of the finished vectors: column jj-1 was a
+          // breakdown; the cycle ends with the columns before this step
+          if (!(r > 0.)) break;
+          for (int i = 0; i < jj; i++) Hraw[(size_t)i * m + jj - 1] += h->hbuf[i];
+          Hraw[(size_t)jj * m + jj - 1] = r;
+          gv = gsave;
+          rotate(jj - 1);
+        }
+        for (int i = 0; i < jj; i++) Hraw[(size_t)i * m + jj] = h->hbuf[kGsB + i];
+        Hraw[(size_t)jj * m + jj] = hj;
+        gsave = gv;
       }
-      for (int i = 0; i < jj; i++) Hraw[(size_t)i * m + jj] = h->hbuf[kGsB + i];
-      Hraw[(size_t)jj * m + jj] = hj;
       Hraw[(size_t)(jj + 1) * m + jj] = wn;
-      gsave = gv;
       rotate(jj);
       if (h->phase) h->host_ms[3] += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
       if (std::fabs(gv[jj + 1]) / bn <= o.rtol || wn == 0.) { jj++; break; }
@@ -1311,6 +1342,7 @@ void vfs_poisson_default_opts(vfs_solve_opts *o) {
   o->coarsest_max = 128;
   o->warm_start = 0;
   o->smoother = 3;
+  o->orth = 0;
 }
 
 int vfs_poisson_create(const vfs_grid_desc *gd, vfs_poisson **out) {

@@ -477,6 +477,107 @@ __device__ __forceinline__ void gs_dots_body(size_t n, int v0, const double *con
     if (a < 2 * NV || first) partial[(size_t)row * gridDim.x + blockIdx.x] = s;
   }
 }
+// Classical Gram-Schmidt in one pass (the orthogonalisation of PETSc's
+// GMRES with its default refinement "never"): rows kGsB + v0 + v of the
+// block partials hold Q_{v0+v}.w, the basis vectors kept unnormalised.
+template <int NV>
+__device__ __forceinline__ void cgs_dots_body(size_t n, int v0, const double *const *__restrict__ Q,
+                                              const double *__restrict__ w, double *__restrict__ partial) {
+  __shared__ double sh[8][NV];
+  double acc[NV];
+  const double *q[NV];
+#pragma unroll
+  for (int v = 0; v < NV; v++) {
+    acc[v] = 0.;
+    q[v] = Q[v0 + v];
+  }
+  const size_t base = (size_t)blockIdx.x * blockDim.x * kGsTile + threadIdx.x;
+#pragma unroll 2
+  for (int t = 0; t < kGsTile; t++) {
+    const size_t c = base + (size_t)t * blockDim.x;
+    if (c < n) {
+      const double wc = __ldg(&w[c]);
+#pragma unroll
+      for (int v = 0; v < NV; v++) acc[v] = fma(__ldcs(q[v] + c), wc, acc[v]);
+    }
+  }
+  const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
+#pragma unroll
+  for (int v = 0; v < NV; v++) {
+    const double s = warp_sum(acc[v]);
+    if (lane == 0) sh[wp][v] = s;
+  }
+  __syncthreads();
+  if (threadIdx.x < NV) {
+    double s = 0.;
+    for (int k = 0; k < (int)(blockDim.x >> 5); k++) s += sh[k][threadIdx.x];
+    partial[(size_t)(kGsB + v0 + threadIdx.x) * gridDim.x + blockIdx.x] = s;
+  }
+}
+#define CGS_DOTS(NV)                                                                                            \
+  __global__ void __launch_bounds__(256) k_cgs_dots##NV(size_t n, int v0, const double *const *Q,               \
+                                                        const double *w, double *partial) {                     \
+    cgs_dots_body<NV>(n, v0, Q, w, partial);                                                                   \
+  }
+CGS_DOTS(1)
+CGS_DOTS(2)
+CGS_DOTS(3)
+CGS_DOTS(4)
+CGS_DOTS(5)
+CGS_DOTS(6)
+CGS_DOTS(7)
+CGS_DOTS(8)
+#undef CGS_DOTS
+
+// One block per basis vector v: d = Q_v.w summed in a fixed order, then
+// h_v = d / ||Q_v|| (the Hessenberg entry, red[v]) and the update
+// coefficient h_v / ||Q_v|| (red[kGsB + v]); dsv[2v+1] = 1 / ||Q_v||.
+__global__ void k_cgs_reduce(const double *__restrict__ partial, int nb, const double *__restrict__ dsv,
+                             double *red) {
+  const int v = blockIdx.x;
+  double s = 0.;
+  for (int q = threadIdx.x; q < nb; q += blockDim.x) s += partial[(size_t)(kGsB + v) * nb + q];
+  s = block_sum(s);
+  if (threadIdx.x == 0) {
+    const double sinv = dsv[2 * v + 1], hv = s * sinv;
+    red[v] = hv;
+    red[kGsB + v] = hv * sinv;
+  }
+}
+
+// w -= sum_v red[kGsB + v] Q_v; block partials of ||w||^2.
+__global__ void __launch_bounds__(256) k_cgs_update(size_t n, int nv, const double *const *__restrict__ Q,
+                                                    const double *__restrict__ red, double *__restrict__ w,
+                                                    double *partial) {
+  const size_t base = (size_t)blockIdx.x * blockDim.x * kGsTile + threadIdx.x;
+  double aw[kGsTile];
+#pragma unroll
+  for (int t = 0; t < kGsTile; t++) {
+    const size_t c = base + (size_t)t * blockDim.x;
+    aw[t] = c < n ? w[c] : 0.;
+  }
+  for (int v = 0; v < nv; v++) {
+    const double *p = Q[v];
+    const double cb = -red[kGsB + v];
+#pragma unroll
+    for (int t = 0; t < kGsTile; t++) {
+      const size_t c = base + (size_t)t * blockDim.x;
+      if (c < n) aw[t] = fma(cb, __ldcs(&p[c]), aw[t]);
+    }
+  }
+  double ss = 0.;
+#pragma unroll
+  for (int t = 0; t < kGsTile; t++) {
+    const size_t c = base + (size_t)t * blockDim.x;
+    if (c < n) {
+      w[c] = aw[t];
+      ss = fma(aw[t], aw[t], ss);
+    }
+  }
+  ss = block_sum(ss);
+  if (threadIdx.x == 0) partial[blockIdx.x] = ss;
+}
+
 #define GS_DOTS(NV)                                                                                            \
   __global__ void __launch_bounds__(256) k_gs_dots##NV(size_t n, int v0, const double *const *Q,               \
                                                        const double *u, const double *w, int first,            \

@@ -61,7 +61,7 @@ class GridDesc(C.Structure):
 class SolveOpts(C.Structure):
     _fields_ = [("rtol", C.c_double), ("max_it", C.c_int), ("restart", C.c_int), ("precision", C.c_int),
                 ("nu1", C.c_int), ("nu2", C.c_int), ("omega", C.c_double), ("use_graphs", C.c_int),
-                ("coarsest_max", C.c_int), ("warm_start", C.c_int), ("smoother", C.c_int)]
+                ("coarsest_max", C.c_int), ("warm_start", C.c_int), ("smoother", C.c_int), ("orth", C.c_int)]
 
 
 class UNetBatch(C.Structure):
@@ -193,6 +193,8 @@ def default_opts(**kw):
     o = SolveOpts()
     load().vfs_poisson_default_opts(C.byref(o))
     for k, v in kw.items():
+        if not any(k == f for f, _ in SolveOpts._fields_):
+            raise TypeError(f"unknown solver option {k!r}")
         setattr(o, k, v)
     return o
 

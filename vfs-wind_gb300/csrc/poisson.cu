@@ -1952,6 +1952,8 @@ int vfs_poisson_learned_guess(vfs_poisson *h, vfs_unet *u, const double *phi_nm1
     rel_res[1] = r_learn / nb;
   }
   if (h->phase) {
+    fprintf(stderr, "vfs guess rel residuals: extrapolation %.4e fit %.4e learned %.4e previous %.4e\n",
+            std::sqrt(nrm[0]) / nb, std::sqrt(std::max(r2, 0.)) / nb, r_learn / nb, r_prev64 / nb);
     cudaEventRecord(h->phev[3], h->stream);
     TRY(sync(h));
     float a = 0.f, c = 0.f, d = 0.f;

@@ -86,8 +86,12 @@ typedef struct {
                          last solve or by vfs_poisson_learned_guess */
   int smoother;       /* 0 fused line Jacobi, 1 line Jacobi in correction
                          form, 2 zebra line Gauss-Seidel over k-planes,
-                         3 (default) zebra line Gauss-Seidel over
-                         checkerboard (i + k parity) columns               */
+                         3 zebra line Gauss-Seidel over checkerboard
+                         (i + k parity) columns, 4 (default) the same
+                         sweep, bit-identical to 3, with each colour's
+                         residual formed inside the line kernel on the
+                         FP32 levels of at most 2^20 cells (3's kernels
+                         elsewhere)                                        */
   int orth;           /* Arnoldi orthogonalisation: 0 (default) classical
                          Gram-Schmidt in one pass (PETSc GMRES's default
                          refinement "never"), 1 classical Gram-Schmidt

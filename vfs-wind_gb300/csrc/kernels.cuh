@@ -90,6 +90,16 @@ TYPED_DECL(double, f64)
 __global__ void k_pack16(size_t n, const double *A, __half2 *C, float *D);
 __global__ void k_residual16(Box b, const __half2 *C, const float *D, const float *x, const float *rhs, float *r,
                              int color);
+// Checkerboard zebra colour with the residual formed in the line kernel:
+// _oz counts the launch's colour as zero (its loads are masked), _z every x
+// (r = rhs).
+#define LINE_FUSED_DECL(NAME)                                                                                   \
+  __global__ void NAME(Box b, const __half2 *C, const float *D, const float *xo, const float *xn, const float *rhs, \
+                       const float *Asp, const float *inv, const float *cp, float *xd, float omega, int color);
+LINE_FUSED_DECL(k_line_fused16)
+LINE_FUSED_DECL(k_line_fused16_oz)
+LINE_FUSED_DECL(k_line_fused16_z)
+#undef LINE_FUSED_DECL
 __global__ void k_apply64(Box b, const double *A, const double *x, double *y);
 __global__ void k_residual64(Box b, const double *A, const double *x, const double *rhs, double *r, double *partial);
 // Gram-Schmidt rows of the reduced values (solve.cu): Q.u at 0.., Q.w at

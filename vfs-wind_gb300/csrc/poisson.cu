@@ -862,6 +862,12 @@ struct Prec<float> {
   static constexpr auto prolong = k_prolong_f32;
   static constexpr auto coarsest = k_coarsest_f32;
   static constexpr auto tri = k_line_tri_f32;
+  static void fused(vfs_poisson *h, Level &l, dim3 g, dim3 blk, size_t sm, const float *xo, const float *xn,
+                    const float *bb, float *xd, float omega, bool own_zero, bool both_zero, int color) {
+    const auto kern = both_zero ? k_line_fused16_z : own_zero ? k_line_fused16_oz : k_line_fused16;
+    LAUNCH_SM(h, kern, g, blk, sm, l.b, l.C16, l.D32, xo, xn, bb, l.A32 + (size_t)SP * l.b.n(), l.inv32, l.cp32, xd,
+              omega, color);
+  }
   static float *A(Level &l) { return l.A32; }
   static float *inv(Level &l) { return l.inv32; }
   static float *cp(Level &l) { return l.cp32; }
@@ -879,6 +885,9 @@ struct Prec<double> {
   static constexpr auto prolong = k_prolong_f64;
   static constexpr auto coarsest = k_coarsest_f64;
   static constexpr auto tri = k_line_tri_f64;
+  // no FP64 variant of the fused sweep (smoother 4 runs smoother 3's kernels)
+  static void fused(vfs_poisson *, Level &, dim3, dim3, size_t, const double *, const double *, const double *,
+                    double *, double, bool, bool, int) {}
   static double *A(Level &l) { return l.A64; }
   static double *inv(Level &l) { return l.inv64; }
   static double *cp(Level &l) { return l.cp64; }
@@ -898,13 +907,29 @@ struct Prec<double> {
 // operator, 10 half2 words and the diagonal), then r, S slot, inv, cp and x
 // read and written.  A zero-guess zebra sweep skips the first colour's
 // residual and reads rhs, S, inv, cp and writes x there.
+// Smoother 4 forms the residual inside the line kernel on levels of at most
+// kFusedMaxCells cells (FP32).  Finer levels run smoother 3's kernels: they
+// are bandwidth-bound, and there the separate residual kernel (high
+// occupancy) and line kernel move their larger byte count faster than the
+// fused kernel (one 168-register block per SM) moves its smaller one.  The
+// coarse levels are latency-bound and gain from half the launches.
+constexpr size_t kFusedMaxCells = size_t(1) << 20;
+template <typename T>
+bool fused_level(const Level &l, int smoother) {
+  return smoother == 4 && std::is_same<T, float>::value && l.b.n() <= kFusedMaxCells;
+}
+
 template <typename T>
 void prof_begin(vfs_poisson *h, int li, bool zero_guess, int smoother) {
   if (!h->prof || li != 0 || h->pcount >= 16) return;
   cudaEventRecord(h->pev[0][h->pcount], h->stream);
   const double R = std::is_same<T, float>::value ? 14.0 : 22.0;
-  const double words = zero_guess ? (smoother >= 2 ? 0.5 * (5.0 + R + 6.0) : 5.0)
-                                  : (smoother == 0 ? 22.0 : R + 6.0);
+  double words = zero_guess ? (smoother >= 2 ? 0.5 * (5.0 + R + 6.0) : 5.0)
+                            : (smoother == 0 ? 22.0 : R + 6.0);
+  // residual formed in the line kernel (FP32): 10 half2 words and the
+  // diagonal, x, rhs, S slot, inv, cp and x written; from a zero guess the
+  // first colour streams rhs, S, inv, cp and x written
+  if (fused_level<T>(h->L[li], smoother)) words = zero_guess ? 0.5 * (5.0 + 17.0) : 17.0;
   h->pbytes[h->pcount] = (double)h->box.n() * sizeof(T) * words;
 }
 void prof_end(vfs_poisson *h, int li) {
@@ -916,7 +941,10 @@ void prof_end(vfs_poisson *h, int li) {
 // One smoothing sweep on level l.  smoother 0: fused j-line Jacobi kernel;
 // 1: j-line Jacobi in correction form (residual kernel + tridiagonal
 // kernel); 2: zebra j-line Gauss-Seidel over even then odd k-planes in
-// correction form.  x/t are swapped by the fused kernel only.
+// correction form; 3: zebra over checkerboard columns in correction form;
+// 4: the same sweep with each colour's residual formed in the line kernel
+// on the levels fused_level selects (3 elsewhere).  x/t are swapped by the
+// sweeps that write t (0 and the fused 4).
 template <typename T>
 void smooth(vfs_poisson *h, Level &l, int li, int smoother, bool zero_guess, T omega, T *&x, T *&t, T *bb, T *r) {
   const int P = (l.b.ny + kLineChunk - 1) / kLineChunk;
@@ -941,6 +969,15 @@ void smooth(vfs_poisson *h, Level &l, int li, int smoother, bool zero_guess, T o
       LAUNCH_SM(h, Prec<T>::tri, lg, lb, lsm, l.b, skip_res ? bb : r, Asp, Prec<T>::inv(l), Prec<T>::cp(l), x,
                 omega, 0, color);
     }
+  } else if (fused_level<T>(l, smoother)) {
+    // checkerboard zebra, residual in the line kernel: the first colour reads
+    // x and writes its columns to t, the second reads its own colour from x
+    // and the first colour from t and writes its columns to t
+    const int nh = (l.b.nx + 1) / 2;
+    dim3 cg((nh + TI - 1) / TI, l.b.nz);
+    Prec<T>::fused(h, l, cg, lb, lsm, x, x, bb, t, omega, zero_guess, zero_guess, 2);
+    Prec<T>::fused(h, l, cg, lb, lsm, x, t, bb, t, omega, zero_guess, false, 3);
+    std::swap(x, t);
   } else {
     // zebra by checkerboard columns: colour (i + k) % 2 == c; the colour's
     // residuals go to split positions (r of the natural rhs when x = 0)
@@ -969,7 +1006,7 @@ void vcycle(vfs_poisson *h, int li, int nu1, int nu2, T omega, int smoother) {
   }
   if (nu1 == 0) cudaMemsetAsync(x, 0, l.b.n() * sizeof(T), h->stream);
   for (int s = 0; s < nu1; s++) smooth<T>(h, l, li, smoother, s == 0, omega, x, t, bb, r);
-  if (smoother == 3 && nu1 > 0 && omega == (T)1) {
+  if ((smoother == 3 || smoother == 4) && nu1 > 0 && omega == (T)1) {
     // the second colour's lines were just solved exactly (omega 1), so its
     // residual is zero up to rounding: form the first colour's only
     const int nh = (l.b.nx + 1) / 2;
@@ -1114,7 +1151,7 @@ void resolve_opts(vfs_solve_opts &o) {
 int check_opts(const vfs_solve_opts &o) {
   if (!(o.rtol > 0) || o.max_it < 1 || o.restart < 1 || o.restart > 64 || o.nu1 < 0 || o.nu2 < 0 ||
       o.nu1 + o.nu2 < 1 || o.nu1 > 8 || o.nu2 > 8 || !(o.omega > 0 && o.omega <= 1.5) ||
-      (o.precision != 0 && o.precision != 1) || o.smoother < 0 || o.smoother > 3 || (o.orth != 0 && o.orth != 1))
+      (o.precision != 0 && o.precision != 1) || o.smoother < 0 || o.smoother > 4 || (o.orth != 0 && o.orth != 1))
     return fail(VFS_EINVAL, "invalid solver options");
   return VFS_OK;
 }
@@ -1341,7 +1378,7 @@ void vfs_poisson_default_opts(vfs_solve_opts *o) {
   o->use_graphs = 1;
   o->coarsest_max = 128;
   o->warm_start = 0;
-  o->smoother = 3;
+  o->smoother = 4;
   o->orth = 0;
 }
 

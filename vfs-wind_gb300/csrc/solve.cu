@@ -291,54 +291,16 @@ __device__ __forceinline__ void line_sweep_body(Box b, const T *__restrict__ A, 
   }
 }
 
-// Tridiagonal j-line correction of a line-relaxation sweep in correction
-// form: with r = rhs - A x already formed, solve L d = r on every (i,k)
-// column (L = the line part S, CP, N of A, factors inv/cp) and update
-// x += omega d (x = omega d when zero_guess, r then being the right-hand
-// side).  `color`: -1 every column; 0/1 the k-planes with k % 2 == color
-// (zebra by planes); 2/3 the checkerboard columns with (i + k) % 2 ==
-// color % 2 (zebra by columns), whose r is read at split positions; 4/5
-// the same columns with r natural (a right-hand side used as r).  A
-// column's threads walk split positions, so operator and factor loads
-// coalesce; x is natural.  Same chunked recurrences and scans as
-// line_sweep_body; only 5 words per cell are streamed.
+// The chunked tridiagonal solve of one j-line: on entry y holds the
+// chunk's right-hand side (rows j0 .. j0+cnt-1), av/ivv/cv its line
+// coefficients and factors; on exit y holds the solution on the chunk.
+// Chunk boundaries are joined by scans over the P chunks of the column in
+// shared memory (sA, sB: P x TI words each).
 template <typename T, int M>
-__device__ __forceinline__ void line_tri_body(Box b, const T *__restrict__ r, const T *__restrict__ Asp,
-                                              const T *__restrict__ inv, const T *__restrict__ cp, T *x, T omega,
-                                              int zero_guess, int color) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
+__device__ __forceinline__ void line_tri_solve(T (&y)[M], const T (&av)[M], const T (&ivv)[M], const T (&cv)[M],
+                                               int cnt, T *sA, T *sB) {
   const int tx = threadIdx.x, ty = threadIdx.y, TI = blockDim.x, P = blockDim.y;
-  T *sA = (T *)smem_raw, *sB = sA + P * TI;
-  const int t = blockIdx.x * TI + tx, k = blockIdx.y;
-  int pp = t;
-  bool valid;
-  if (color >= 2) {
-    const int par = (color + k) & 1, nh = (b.nx + 1) >> 1;
-    valid = t < (par ? b.nx - nh : nh);
-    pp = par ? nh + t : t;
-  } else {
-    valid = t < b.nx && (color < 0 || (k & 1) == color);
-  }
-  const int ny = b.ny, j0 = ty * M;
-  const int cnt = valid ? max(0, min(M, ny - j0)) : 0;
-  const uint32_t sj = b.nx;
-  const uint32_t cS = valid ? (uint32_t)b.at(pp, 0, k) : 0u;                     // operator / factor index
-  const uint32_t cX = valid ? (uint32_t)b.at(split_cell(pp, b.nx), 0, k) : 0u;  // natural index
-  const uint32_t cR = (color == 2 || color == 3) ? cS : cX;
-  // every load of the chunk up front (one memory round trip): the line
-  // coefficients, factors, residual and the x being corrected
-  T y[M], g[M], av[M], ivv[M], cv[M], xv[M];
-#pragma unroll
-  for (int q = 0; q < M; q++) {
-    const int j = j0 + q;
-    const uint32_t o = (uint32_t)j * sj;
-    const bool in = q < cnt;
-    av[q] = in && j > 0 ? __ldcs(&Asp[cS + o]) : (T)0;
-    ivv[q] = in ? __ldcs(&inv[cS + o]) : (T)0;
-    cv[q] = in && j < ny - 1 ? __ldcs(&cp[cS + o]) : (T)0;
-    y[q] = in ? __ldcs(&r[cR + o]) : (T)0;
-    xv[q] = in && !zero_guess ? x[cX + o] : (T)0;
-  }
+  T g[M];
   T yp = (T)0, gp = (T)1;
 #pragma unroll
   for (int q = 0; q < M; q++) {
@@ -392,14 +354,193 @@ __device__ __forceinline__ void line_tri_body(Box b, const T *__restrict__ r, co
   __syncthreads();
   const T xin = sA[ty * TI + tx];
 #pragma unroll
+  for (int q = 0; q < M; q++) y[q] += g[q] * xin;
+}
+
+// Column of a line kernel thread: split position pp of column t of the
+// launch's colour (2/3 and 4/5: checkerboard columns (i + k) % 2 == color %
+// 2; 0/1: k-planes with k % 2 == color; -1: every column).
+__device__ __forceinline__ bool line_column(const Box &b, int color, int t, int k, int &pp) {
+  pp = t;
+  if (color >= 2) {
+    const int par = (color + k) & 1, nh = (b.nx + 1) >> 1;
+    pp = par ? nh + t : t;
+    return t < (par ? b.nx - nh : nh);
+  }
+  return t < b.nx && (color < 0 || (k & 1) == color);
+}
+
+// Tridiagonal j-line correction of a line-relaxation sweep in correction
+// form: with r = rhs - A x already formed, solve L d = r on every (i,k)
+// column (L = the line part S, CP, N of A, factors inv/cp) and update
+// x += omega d (x = omega d when zero_guess, r then being the right-hand
+// side).  `color`: -1 every column; 0/1 the k-planes with k % 2 == color
+// (zebra by planes); 2/3 the checkerboard columns with (i + k) % 2 ==
+// color % 2 (zebra by columns), whose r is read at split positions; 4/5
+// the same columns with r natural (a right-hand side used as r).  A
+// column's threads walk split positions, so operator and factor loads
+// coalesce; x is natural.  Same chunked recurrences and scans as
+// line_sweep_body; only 5 words per cell are streamed.
+template <typename T, int M>
+__device__ __forceinline__ void line_tri_body(Box b, const T *__restrict__ r, const T *__restrict__ Asp,
+                                              const T *__restrict__ inv, const T *__restrict__ cp, T *x, T omega,
+                                              int zero_guess, int color) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int tx = threadIdx.x, ty = threadIdx.y, TI = blockDim.x, P = blockDim.y;
+  T *sA = (T *)smem_raw, *sB = sA + P * TI;
+  const int t = blockIdx.x * TI + tx, k = blockIdx.y;
+  int pp;
+  const bool valid = line_column(b, color, t, k, pp);
+  const int ny = b.ny, j0 = ty * M;
+  const int cnt = valid ? max(0, min(M, ny - j0)) : 0;
+  const uint32_t sj = b.nx;
+  const uint32_t cS = valid ? (uint32_t)b.at(pp, 0, k) : 0u;                     // operator / factor index
+  const uint32_t cX = valid ? (uint32_t)b.at(split_cell(pp, b.nx), 0, k) : 0u;  // natural index
+  const uint32_t cR = (color == 2 || color == 3) ? cS : cX;
+  // every load of the chunk up front (one memory round trip): the line
+  // coefficients, factors, residual and the x being corrected
+  T y[M], av[M], ivv[M], cv[M], xv[M];
+#pragma unroll
+  for (int q = 0; q < M; q++) {
+    const int j = j0 + q;
+    const uint32_t o = (uint32_t)j * sj;
+    const bool in = q < cnt;
+    av[q] = in && j > 0 ? __ldcs(&Asp[cS + o]) : (T)0;
+    ivv[q] = in ? __ldcs(&inv[cS + o]) : (T)0;
+    cv[q] = in && j < ny - 1 ? __ldcs(&cp[cS + o]) : (T)0;
+    y[q] = in ? __ldcs(&r[cR + o]) : (T)0;
+    xv[q] = in && !zero_guess ? x[cX + o] : (T)0;
+  }
+  line_tri_solve<T, M>(y, av, ivv, cv, cnt, sA, sB);
+#pragma unroll
   for (int q = 0; q < M; q++) {
     if (q < cnt) {
       const uint32_t c = cX + (uint32_t)(j0 + q) * sj;
-      const T d = y[q] + g[q] * xin;
-      x[c] = xv[q] + omega * d;
+      x[c] = xv[q] + omega * y[q];
     }
   }
 }
+
+// One colour of the checkerboard zebra sweep with the residual formed in
+// the line kernel (FP32 V-cycle, packed operator): for the columns with
+// (i + k) % 2 == color % 2 (color 2/3),
+//   r = rhs - A x   (difference form over the packed couplings, in the
+//                    order of k_residual16),
+//   x_new = x + omega L^-1 r   on every j-line (L, inv, cp as line_tri_body).
+// x is read from two buffers and written to a third, so that no block reads
+// a value another block of the same launch writes: a cell of the launch's
+// colour (the columns' own cells and the same-colour diagonal columns
+// i +- 1, k +- 1, or any wrap neighbour that has that parity) is read from
+// xo, a cell of the other colour from xn, and the new values of the
+// launch's columns go to xd.  Within one sweep the first colour runs with
+// xo = xn = x and xd = t, the second with xo = x, xn = xd = t, which
+// reproduces the in-place two-kernel sweep bit for bit.  own_zero: the
+// launch's colour is zero (first sweep from a zero guess, xo not read);
+// both_zero: every x is zero (r = rhs; xo and xn not read).
+template <int M, bool OWN_ZERO, bool BOTH_ZERO>
+__device__ __forceinline__ void line_fused16_body(Box b, const __half2 *__restrict__ C, const float *__restrict__ D,
+                                                  const float *xo, const float *xn, const float *__restrict__ rhs,
+                                                  const float *__restrict__ Asp, const float *__restrict__ inv,
+                                                  const float *__restrict__ cp, float *xd, float omega, int color) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int tx = threadIdx.x, ty = threadIdx.y, TI = blockDim.x, P = blockDim.y;
+  float *sA = (float *)smem_raw, *sB = sA + P * TI;
+  const int t = blockIdx.x * TI + tx, k = blockIdx.y;
+  int pp;
+  const bool valid = line_column(b, color, t, k, pp);
+  const int ny = b.ny, j0 = ty * M;
+  const int cnt = valid ? max(0, min(M, ny - j0)) : 0;
+  const uint32_t sj = b.nx, n = (uint32_t)b.n();
+  const int i = valid ? split_cell(pp, b.nx) : 0;
+  const uint32_t cS = valid ? (uint32_t)b.at(pp, 0, k) : 0u;
+  const uint32_t cX = valid ? (uint32_t)b.at(i, 0, k) : 0u;
+  // slots holding a cell of the launch's colour (read from xo): decided by
+  // the neighbour column's own (i + k) parity, wraps included
+  uint32_t own = 0;
+  {
+    const Nbr q(b, i, 0, k);
+    const int par = (i + k) & 1;
+#pragma unroll
+    for (int m = 1; m < NSLOT; m++) {
+      int di, dj, dk;
+      slot_offset(m, di, dj, dk);
+      const int ii = di < 0 ? q.im : (di > 0 ? q.ip : i), kk = dk < 0 ? q.km : (dk > 0 ? q.kp : k);
+      if (((ii + kk) & 1) == par) own |= 1u << m;
+    }
+  }
+  float y[M], av[M], ivv[M], cv[M], xv[M];
+#pragma unroll
+  for (int q = 0; q < M; q++) {
+    const int j = j0 + q;
+    const uint32_t o = (uint32_t)j * sj;
+    const bool in = q < cnt;
+    av[q] = in && j > 0 ? __ldcs(&Asp[cS + o]) : 0.f;
+    ivv[q] = in ? __ldcs(&inv[cS + o]) : 0.f;
+    cv[q] = in && j < ny - 1 ? __ldcs(&cp[cS + o]) : 0.f;
+  }
+#pragma unroll
+  for (int q = 0; q < M; q++) {
+    // rows past the line end recompute the last row (in bounds, unused)
+    const int j = j0 + min(q, max(cnt - 1, 0));
+    const uint32_t o = (uint32_t)j * sj;
+    if (BOTH_ZERO) {
+      y[q] = __ldcs(&rhs[cX + o]);
+      xv[q] = 0.f;
+      continue;
+    }
+    uint32_t idx[NSLOT];
+    stencil_index(b, i, j, k, idx);
+    const uint32_t cs = cS + o;
+    // every load unconditional (addresses selected, values masked after)
+    float xs[NSLOT];
+#pragma unroll
+    for (int m = 0; m < NSLOT; m++) {
+      const float *src = ((own >> m) & 1) || m == CP ? xo : xn;
+      xs[m] = __ldg(&src[idx[m]]);
+    }
+    float2 f[10];
+#pragma unroll
+    for (int m = 0; m < 10; m++) f[m] = __half22float2(__ldcs(&C[m * n + cs]));
+    const float rv = __ldg(&rhs[idx[CP]]), dv = __ldcs(&D[cs]);
+    if (OWN_ZERO) {
+#pragma unroll
+      for (int m = 0; m < NSLOT; m++)
+        if (((own >> m) & 1) || m == CP) xs[m] = 0.f;
+    }
+    const float xc = xs[CP];
+    float sum = 0.f;
+#pragma unroll
+    for (int m = 0; m < 9; m++) {
+      sum = fmaf(f[m].x, xs[2 * m + 1] - xc, sum);
+      sum = fmaf(f[m].y, xs[2 * m + 2] - xc, sum);
+    }
+    sum = fmaf(f[9].x, xc, sum);
+    y[q] = rv - dv * sum;
+    xv[q] = xc;
+  }
+  line_tri_solve<float, M>(y, av, ivv, cv, cnt, sA, sB);
+#pragma unroll
+  for (int q = 0; q < M; q++) {
+    if (q < cnt) {
+      const uint32_t c = cX + (uint32_t)(j0 + q) * sj;
+      xd[c] = xv[q] + omega * y[q];
+    }
+  }
+}
+#define LINE_FUSED(NAME, OZ, BZ, MINB)                                                                             \
+  __global__ void __launch_bounds__(384, MINB) NAME(Box b, const __half2 *C, const float *D, const float *xo,         \
+                                                 const float *xn, const float *rhs, const float *Asp,             \
+                                                 const float *inv, const float *cp, float *xd, float omega,       \
+                                                 int color) {                                                     \
+    line_fused16_body<kLineChunk, OZ, BZ>(b, C, D, xo, xn, rhs, Asp, inv, cp, xd, omega, color);                 \
+  }
+// one 384-thread block per SM: the compiler keeps several cells' loads in
+// flight (168 registers); capped at two blocks it spills and runs at half
+// the speed
+LINE_FUSED(k_line_fused16, false, false, 1)
+LINE_FUSED(k_line_fused16_oz, true, false, 1)
+LINE_FUSED(k_line_fused16_z, true, true, 1)
+#undef LINE_FUSED
 
 // Coarsest level: x = dinv * rhs over the nd dof cells (one block).
 template <typename T>

@@ -79,7 +79,9 @@ typedef struct {
   double omega;       /* relaxation weight of the line sweeps; 0 picks the
                          smoother's own (1 for zebra, 0.8 for line Jacobi) */
   int use_graphs;     /* capture the V-cycle in a CUDA graph               */
-  int coarsest_max;   /* coarsest level cell budget                        */
+  int coarsest_max;   /* coarsest level cell budget (default 256; the
+                         hierarchy is built with the default at
+                         vfs_poisson_set_nvert)                            */
   int warm_start;     /* 0: zero guess; 1: start from the phi passed in (Phi2
                          warm start; the last solution if phi is NULL);
                          2: start from the handle's iterate as left by the

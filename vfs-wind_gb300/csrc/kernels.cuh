@@ -81,7 +81,8 @@ __global__ void k_prolong_f64(Box bf, Box bc, int cx, int cy, int cz, const doub
                                    T *xo, T omega, int zero_guess);                                      \
   __global__ void k_line_tri_##S(Box b, const T *r, const T *Asp, const T *inv, const T *cp, T *x, T omega,  \
                                  int zero_guess, int color);                                             \
-  __global__ void k_coarsest_##S(int nd, const int *didx, const double *dinv, const T *rhs, T *x, size_t n); \
+  __global__ void k_coarsest_##S(int nd, const int *dmap, const int *didx, const double *dinv, const T *rhs, T *x, \
+                                 int n);                                                                     \
   __global__ void k_cast_planes_##S(const double *src, T *dst, size_t n);
 TYPED_DECL(float, f32)
 TYPED_DECL(double, f64)

@@ -419,7 +419,7 @@ struct Level {
   double *v64[4] = {};  // x, b, r, t
   float *v32[4] = {};
   int nd = 0;
-  int *didx = nullptr;
+  int *didx = nullptr, *dmap = nullptr;
   double *dinv = nullptr;
   double *rho = nullptr, *level = nullptr;  // level-set fields of this level (DA layout)
   double *xfinal64 = nullptr;  // where x lives after a V-cycle (set at capture)
@@ -668,6 +668,8 @@ int build_coarsest(vfs_poisson *h, Level &l) {
     regular_row[r] = std::fabs(sum) > 1e-8 * dg;
   }
   int ncomp = 0;
+  std::vector<int> pin_comp;                  // component of each pinned row
+  std::vector<std::vector<double>> pin_row;   // its equation before pinning
   for (int r0 = 0; r0 < nd; r0++) {
     if (comp[r0] >= 0) continue;
     int hd = 0, tl = 0;
@@ -684,6 +686,8 @@ int build_coarsest(vfs_poisson *h, Level &l) {
         }
     }
     if (!regular) {
+      pin_comp.push_back(ncomp);
+      pin_row.emplace_back(M.begin() + (size_t)r0 * nd, M.begin() + (size_t)(r0 + 1) * nd);
       for (int q = 0; q < nd; q++) M[(size_t)r0 * nd + q] = 0.;
       M[(size_t)r0 * nd + r0] = 1.;
       first.push_back(r0);
@@ -713,14 +717,52 @@ int build_coarsest(vfs_poisson *h, Level &l) {
       }
     }
   }
+  // Left null vector w of each singular component (w^T M = 0 on it): with
+  // M_p the matrix with row r0 pinned to e_r0 and I = M_p^-1, M_p 1 = e_r0
+  // (the rows sum to zero), and w^T = e_r0^T I - m_r0^T I has w_r0 = 1.
+  std::vector<std::vector<double>> wv;
+  for (size_t t = 0; t < first.size(); t++) {
+    const int r0 = first[t];
+    std::vector<double> w(I.begin() + (size_t)r0 * nd, I.begin() + (size_t)(r0 + 1) * nd);
+    for (int p = 0; p < nd; p++) {
+      const double m = pin_row[t][p];
+      if (m == 0.) continue;
+      for (int q = 0; q < nd; q++) w[q] -= m * I[(size_t)p * nd + q];
+    }
+    wv.push_back(std::move(w));
+  }
   for (int r0 : first)  // pinned rows see a zero right-hand side
     for (int r = 0; r < nd; r++) I[(size_t)r * nd + r0] = 0.;
+  // A restricted right-hand side need not be consistent (w^T b != 0 on a
+  // singular component); pinning alone would put the whole inconsistency
+  // into the pinned cell's equation.  The solve projects it out evenly
+  // first: dinv = I_z (1 - 1_c w^T / w^T 1_c) on every such component c.
+  for (size_t t = 0; t < first.size(); t++) {
+    const int cid = pin_comp[t];
+    const std::vector<double> &w = wv[t];
+    double s1 = 0.;
+    for (int q = 0; q < nd; q++)
+      if (comp[q] == cid) s1 += w[q];
+    if (!(std::fabs(s1) > 0.)) continue;
+    for (int r = 0; r < nd; r++) {
+      double rs = 0.;
+      for (int p = 0; p < nd; p++)
+        if (comp[p] == cid) rs += I[(size_t)r * nd + p];
+      if (rs == 0.) continue;
+      const double f = rs / s1;
+      for (int q = 0; q < nd; q++)
+        if (comp[q] == cid) I[(size_t)r * nd + q] -= f * w[q];
+    }
+  }
   l.nd = nd;
   dfree(h, l.didx);
+  dfree(h, l.dmap);
   dfree(h, l.dinv);
   TRY(dalloc(h, &l.didx, nd));
+  TRY(dalloc(h, &l.dmap, n));
   TRY(dalloc(h, &l.dinv, (size_t)nd * nd));
   CUDA_TRY(cudaMemcpyAsync(l.didx, idx.data(), nd * sizeof(int), cudaMemcpyHostToDevice, h->stream));
+  CUDA_TRY(cudaMemcpyAsync(l.dmap, map.data(), n * sizeof(int), cudaMemcpyHostToDevice, h->stream));
   CUDA_TRY(cudaMemcpyAsync(l.dinv, I.data(), (size_t)nd * nd * 8, cudaMemcpyHostToDevice, h->stream));
   return sync(h);
 }
@@ -731,7 +773,7 @@ void free_level(vfs_poisson *h, Level &l, bool level0) {
   dfree(h, l.A64); dfree(h, l.A32); dfree(h, l.C16); dfree(h, l.D32); dfree(h, l.rowtype); dfree(h, l.blank);
   dfree(h, l.inv64); dfree(h, l.cp64); dfree(h, l.w64); dfree(h, l.inv32); dfree(h, l.cp32); dfree(h, l.w32);
   for (int q = 0; q < 4; q++) { dfree(h, l.v64[q]); dfree(h, l.v32[q]); }
-  dfree(h, l.didx); dfree(h, l.dinv);
+  dfree(h, l.didx); dfree(h, l.dmap); dfree(h, l.dinv);
   l = Level{};
 }
 
@@ -1000,7 +1042,7 @@ void vcycle(vfs_poisson *h, int li, int nu1, int nu2, T omega, int smoother) {
   T **v = Prec<T>::v(l);
   T *x = v[0], *bb = v[1], *r = v[2], *t = v[3];
   if (li == (int)h->L.size() - 1) {
-    LAUNCH(h, Prec<T>::coarsest, 1, 256, l.nd, l.didx, l.dinv, bb, x, l.b.n());
+    LAUNCH(h, Prec<T>::coarsest, (int)((l.b.n() + 7) / 8), 256, l.nd, l.dmap, l.didx, l.dinv, bb, x, (int)l.b.n());
     Prec<T>::xfinal(l) = x;
     return;
   }
@@ -1376,7 +1418,7 @@ void vfs_poisson_default_opts(vfs_solve_opts *o) {
   o->nu2 = 2;
   o->omega = 0.0;
   o->use_graphs = 1;
-  o->coarsest_max = 128;
+  o->coarsest_max = 256;
   o->warm_start = 0;
   o->smoother = 4;
   o->orth = 0;

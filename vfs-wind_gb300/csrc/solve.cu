@@ -542,19 +542,26 @@ LINE_FUSED(k_line_fused16_oz, true, false, 1)
 LINE_FUSED(k_line_fused16_z, true, true, 1)
 #undef LINE_FUSED
 
-// Coarsest level: x = dinv * rhs over the nd dof cells (one block).
+// Coarsest level: x = dinv * rhs over the nd dof cells, 0 elsewhere.  One
+// warp per cell (8 per block): every block gathers the nd right-hand-side
+// values into shared memory, and a warp forms its cell's row of dinv times
+// them in FP64 (lane-strided sums, then a fixed shuffle tree).  dmap: the
+// row of a cell, -1 off the dofs.
 template <typename T>
-__device__ __forceinline__ void coarsest_body(int nd, const int *__restrict__ didx, const double *__restrict__ dinv,
-                           const T *__restrict__ rhs, T *x, size_t n) {
+__device__ __forceinline__ void coarsest_body(int nd, const int *__restrict__ dmap, const int *__restrict__ didx,
+                                              const double *__restrict__ dinv, const T *__restrict__ rhs, T *x,
+                                              int n) {
   __shared__ double sb[1024];
-  for (size_t c = threadIdx.x; c < n; c += blockDim.x) x[c] = (T)0;
   for (int q = threadIdx.x; q < nd; q += blockDim.x) sb[q] = (double)rhs[didx[q]];
   __syncthreads();
-  for (int r = threadIdx.x; r < nd; r += blockDim.x) {
-    double s = 0.;
-    for (int q = 0; q < nd; q++) s += dinv[(size_t)r * nd + q] * sb[q];
-    x[didx[r]] = (T)s;
-  }
+  const int c = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+  if (c >= n) return;
+  const int r = dmap[c];
+  double s = 0.;
+  if (r >= 0)
+    for (int q = lane; q < nd; q += 32) s = fma(dinv[(size_t)r * nd + q], sb[q], s);
+  s = warp_sum(s);
+  if (lane == 0) x[c] = (T)s;
 }
 
 template <typename T>
@@ -879,8 +886,9 @@ __global__ void k_sumsq(size_t n, const double *__restrict__ x, double *partial)
                                                        const T *cp, T *x, T omega, int zg, int color) {        \
     line_tri_body<T, kLineChunk>(b, r, Asp, inv, cp, x, omega, zg, color);                                    \
   }                                                                                                        \
-  __global__ void k_coarsest_##S(int nd, const int *didx, const double *dinv, const T *rhs, T *x, size_t n) { \
-    coarsest_body<T>(nd, didx, dinv, rhs, x, n);                                                           \
+  __global__ void __launch_bounds__(256) k_coarsest_##S(int nd, const int *dmap, const int *didx,             \
+                                                        const double *dinv, const T *rhs, T *x, int n) {     \
+    coarsest_body<T>(nd, dmap, didx, dinv, rhs, x, n);                                                     \
   }                                                                                                        \
   __global__ void k_cast_planes_##S(const double *src, T *dst, size_t n) { cast_body<T>(src, dst, n); }
 // the line kernel keeps a whole chunk in registers: 16 columns per block

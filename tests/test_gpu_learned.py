@@ -47,3 +47,42 @@ def test_learned_guess_on_sequence(cuda_lib):
     s.close()
     net.close()
     fresh.close()
+
+
+def test_speculative_first_step_bitexact(cuda_lib, monkeypatch):
+    """A learned guess that expects the plain extrapolation to win runs the
+    next solve's first Arnoldi step on the handle's stream while the network
+    runs on a side stream.  Solves that resume from it match solves that
+    form every step themselves bit for bit, step after step; and a solve
+    whose options differ from the step's forms its own first step."""
+    import torch
+    import vfs_poisson as V
+    from vfs_poisson import learned as LG, sequence as S
+    seq = S.TowerSequence(nx=64, ny=48, nz=64, n_theta=24)
+    o64 = V.default_opts(precision=1)
+    o32 = V.default_opts(precision=0)
+    runs = {}
+    for spec in ("1", "0"):
+        monkeypatch.setenv("VFS_GUESS_SPECULATE", spec)
+        s = V.PoissonSolver(*seq.dims, periodic=seq.periodic)
+        s.set_grid(seq.coor)
+        hist, _ = LG.run_sequence(seq, s, 4, o64, guess="prev")
+        net = V.UNet(0)
+        net.kappa = 1e-4
+        hist2, recs = LG.run_sequence(seq, s, 3, o32, guess="learned", net=net, start=4, history=hist)
+        # a solve with other options after a speculative guess
+        u = seq.mask_faces(seq.ucont(7), seq.classify(s, 7))
+        s.rhs(u)
+        s.learned_guess(net, hist2[-1], hist2[-2], net.kappa)
+        phi = torch.empty_like(hist2[-1])
+        _, st = s.solve(phi, opts=V.default_opts(precision=0, warm_start=2, nu2=3))
+        runs[spec] = ([r["iterations"] for r in recs], [h.clone() for h in hist2], st.iterations, phi.clone())
+        assert all(r["rel"] <= 1e-8 for r in recs) and st.rel_residual <= 1e-8
+        assert all(r["chosen"] == 1 for r in recs)
+        s.close()
+        net.close()
+    a, b = runs["1"], runs["0"]
+    assert a[0] == b[0] and a[2] == b[2]
+    for x, y in zip(a[1], b[1]):
+        assert torch.equal(x, y)
+    assert torch.equal(a[3], b[3])

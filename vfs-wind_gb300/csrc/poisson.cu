@@ -475,6 +475,18 @@ struct vfs_poisson {
   int ls_on = 0, ls_bc3 = 0, ls_bc4 = 0, ls_bc5 = 0;
   double r0_norm = 0.;
   bool r0_valid = false;
+  // Speculative first Arnoldi step: a learned guess that expects the plain
+  // extrapolation to win (the previous guess did, with every band weight 0)
+  // enqueues step 0 of the next solve on the handle's stream while the
+  // network and the band fit run on a side stream.  The solve resumes at
+  // step 1 when the guess installs that extrapolation and the solve's
+  // options are the ones the step used; otherwise the step is dropped.
+  cudaStream_t side = nullptr;
+  cudaEvent_t ev_feat = nullptr;
+  double *spartial = nullptr, *sred = nullptr;  // side-stream reductions
+  bool spec_enable = true;                      // VFS_GUESS_SPECULATE=0 turns it off
+  bool spec_next = false, spec_valid = false;
+  vfs_solve_opts spec_opts{};
   std::vector<Level> L;
   bool have_grid = false, have_nvert = false, have_rhs = false, have_phi = false;
   // graphs of the V-cycle per precision and parameters they were built for
@@ -496,7 +508,7 @@ struct vfs_poisson {
   bool phase = false;
   cudaEvent_t phev[4] = {};
   double phase_ms[3] = {0., 0., 0.};
-  double host_ms[4] = {0., 0., 0., 0.};  // enqueue V-cycle, enqueue rest, wait, host work
+  double host_ms[4] = {0., 0., 0., 0.};  // enqueue, (unused), wait, host work
 };
 
 namespace {
@@ -1221,6 +1233,47 @@ void cgs_dots(vfs_poisson *h, int nv, int nb, size_t n, int v0, const double *w)
   }
 }
 
+// hbuf offsets: the read-back of the speculative step 0 and its staging of
+// the first basis norm (apart from the rows reduce_read and FGMRES use)
+constexpr int kSpecHb = 620, kSpecStage = 610;
+
+// Enqueue Arnoldi step jj of FGMRES: precondition V_jj, apply A, orthogonalise
+// (orth 0 or DCGS2), reduce the new vector's norm and copy the Hessenberg
+// data to hbuf + hb (orth 0: h at hb + 0..jj; the norm^2 at hb + kGsR + 3).
+int arnoldi_enqueue(vfs_poisson *h, int jj, int nbd, const vfs_solve_opts &o, int hb) {
+  const size_t n = h->box.n();
+  const double *const *dV = (const double *const *)h->dV;
+  TRY(precondition(h, h->V[jj], 1.0, h->dsv + 2 * jj + 1, h->dsv32 + jj, h->Z[jj], o));
+  if (h->phase && hb == 0) cudaEventRecord(h->phev[1], h->stream);
+  double *w = h->V[jj + 1];
+  LAUNCH(h, k_apply64, box_grid(h->box), 128, h->box, h->A0, h->Z[jj], w);
+  if (h->phase && hb == 0) cudaEventRecord(h->phev[2], h->stream);
+  if (o.orth == 0) {
+    for (int v0 = 0; v0 <= jj; v0 += 8) cgs_dots(h, std::min(8, jj + 1 - v0), nbd, n, v0, w);
+    LAUNCH(h, k_cgs_reduce, jj + 1, 1024, h->partial, nbd, h->dsv, h->red);
+    LAUNCH(h, k_cgs_update, nbd, 256, n, jj + 1, dV, h->red, w, h->partial);
+  } else {
+    for (int v0 = 0; v0 == 0 || v0 < jj; v0 += 8)
+      gs_dots(h, std::min(8, jj - v0), nbd, n, v0, h->V[jj], w, v0 == 0);
+    LAUNCH(h, k_gs_reduce, 2 * jj + 2, 1024, h->partial, nbd, jj, h->red);
+    LAUNCH(h, k_gs_coef, 1, 32, jj, h->red);
+    LAUNCH(h, k_gs_update, nbd, 256, n, jj, dV, h->red, h->V[jj], w, h->partial);
+  }
+  LAUNCH(h, k_reduce_norm, 1, 1024, h->partial, nbd, h->dsv + 2 * (jj + 1), h->dsv32 + jj + 1);
+  if (h->phase && hb == 0) cudaEventRecord(h->phev[3], h->stream);
+  CUDA_TRY(cudaMemcpyAsync(h->hbuf + hb, h->red, (o.orth == 0 ? jj + 1 : kGsR + 3) * 8, cudaMemcpyDeviceToHost,
+                           h->stream));
+  CUDA_TRY(cudaMemcpyAsync(h->hbuf + hb + kGsR + 3, h->dsv + 2 * (jj + 1), 8, cudaMemcpyDeviceToHost, h->stream));
+  return VFS_OK;
+}
+
+// The options of a solve that may resume from the speculative step 0: the
+// same preconditioner and orthogonalisation.
+bool spec_matches(const vfs_solve_opts &a, const vfs_solve_opts &b) {
+  return a.precision == b.precision && a.nu1 == b.nu1 && a.nu2 == b.nu2 && a.omega == b.omega &&
+         a.smoother == b.smoother && a.orth == b.orth && a.restart >= 1 && a.max_it >= 1;
+}
+
 // FGMRES(m) (flexible GMRES: the preconditioned vectors Z_j are kept and
 // x = x0 + Z y).  The basis vectors stay unnormalised in memory; their
 // norms and inverse norms are reduced on the device (dsv) and every use
@@ -1259,7 +1312,12 @@ int fgmres(vfs_poisson *h, const vfs_solve_opts &o, vfs_solve_stats *st) {
     st->iterations = 0;
     return VFS_OK;
   }
-  if (o.warm_start == 2 && h->r0_valid) {  // residual formed by the guess
+  // step 0 enqueued by the learned guess (V_0 = the guess's residual)
+  const bool resume = o.warm_start == 2 && h->r0_valid && h->spec_valid && spec_matches(o, h->spec_opts);
+  h->spec_valid = false;
+  if (resume) {
+    beta = h->r0_norm;
+  } else if (o.warm_start == 2 && h->r0_valid) {  // residual formed by the guess
     CUDA_TRY(cudaMemcpyAsync(h->V[0], h->r0, n * 8, cudaMemcpyDeviceToDevice, h->stream));
     beta = h->r0_norm;
   } else if (o.warm_start) {
@@ -1288,7 +1346,6 @@ int fgmres(vfs_poisson *h, const vfs_solve_opts &o, vfs_solve_stats *st) {
     gv[j + 1] = -sn[j] * gv[j];
     gv[j] = cs[j] * gv[j];
   };
-  const double *const *dV = (const double *const *)h->dV;
   while (rel > o.rtol && it < o.max_it) {
     h->hbuf[400] = beta * beta;  // pinned staging: pageable copies cost ~0.5 ms each
     h->hbuf[401] = 1.0 / beta;
@@ -1302,34 +1359,14 @@ int fgmres(vfs_poisson *h, const vfs_solve_opts &o, vfs_solve_stats *st) {
     for (; jj < m && it < o.max_it; jj++) {
       const auto t0 = h->phase ? std::chrono::steady_clock::now() : std::chrono::steady_clock::time_point();
       if (h->phase) cudaEventRecord(h->phev[0], h->stream);
-      TRY(precondition(h, h->V[jj], 1.0, h->dsv + 2 * jj + 1, h->dsv32 + jj, h->Z[jj], o));
-      const auto t1 = h->phase ? std::chrono::steady_clock::now() : t0;
-      if (h->phase) cudaEventRecord(h->phev[1], h->stream);
-      double *w = h->V[jj + 1];
-      LAUNCH(h, k_apply64, box_grid(h->box), 128, h->box, h->A0, h->Z[jj], w);
-      if (h->phase) cudaEventRecord(h->phev[2], h->stream);
-      if (o.orth == 0) {
-        for (int v0 = 0; v0 <= jj; v0 += 8) cgs_dots(h, std::min(8, jj + 1 - v0), nbd, n, v0, w);
-        LAUNCH(h, k_cgs_reduce, jj + 1, 1024, h->partial, nbd, h->dsv, h->red);
-        LAUNCH(h, k_cgs_update, nbd, 256, n, jj + 1, dV, h->red, w, h->partial);
-      } else {
-        for (int v0 = 0; v0 == 0 || v0 < jj; v0 += 8)
-          gs_dots(h, std::min(8, jj - v0), nbd, n, v0, h->V[jj], w, v0 == 0);
-        LAUNCH(h, k_gs_reduce, 2 * jj + 2, 1024, h->partial, nbd, jj, h->red);
-        LAUNCH(h, k_gs_coef, 1, 32, jj, h->red);
-        LAUNCH(h, k_gs_update, nbd, 256, n, jj, dV, h->red, h->V[jj], w, h->partial);
-      }
-      LAUNCH(h, k_reduce_norm, 1, 1024, h->partial, nbd, h->dsv + 2 * (jj + 1), h->dsv32 + jj + 1);
-      if (h->phase) cudaEventRecord(h->phev[3], h->stream);
-      CUDA_TRY(cudaMemcpyAsync(h->hbuf, h->red, (o.orth == 0 ? jj + 1 : kGsR + 3) * 8, cudaMemcpyDeviceToHost,
-                               h->stream));
-      CUDA_TRY(cudaMemcpyAsync(h->hbuf + kGsR + 3, h->dsv + 2 * (jj + 1), 8, cudaMemcpyDeviceToHost, h->stream));
+      const bool pre = resume && it == 0 && jj == 0;  // enqueued by the guess
+      const int hb = pre ? kSpecHb : 0;
+      if (!pre) TRY(arnoldi_enqueue(h, jj, nbd, o, 0));
       const auto t2 = h->phase ? std::chrono::steady_clock::now() : t0;
       TRY(sync(h));
       const auto t3 = h->phase ? std::chrono::steady_clock::now() : t0;
-      if (h->phase) {
-        h->host_ms[0] += std::chrono::duration<double, std::milli>(t1 - t0).count();
-        h->host_ms[1] += std::chrono::duration<double, std::milli>(t2 - t1).count();
+      if (h->phase && !pre) {
+        h->host_ms[0] += std::chrono::duration<double, std::milli>(t2 - t0).count();
         h->host_ms[2] += std::chrono::duration<double, std::milli>(t3 - t2).count();
         float a = 0.f, b = 0.f, c = 0.f;
         cudaEventElapsedTime(&a, h->phev[0], h->phev[1]);
@@ -1339,9 +1376,10 @@ int fgmres(vfs_poisson *h, const vfs_solve_opts &o, vfs_solve_stats *st) {
       }
       prof_collect(h);
       it++;
-      const double wn = std::sqrt(std::max(h->hbuf[kGsR + 3], 0.));
+      const double *rb = h->hbuf + hb;
+      const double wn = std::sqrt(std::max(rb[kGsR + 3], 0.));
       if (o.orth == 0) {  // column jj is final: H[i, jj] = Q_i.w / ||Q_i||
-        for (int i = 0; i <= jj; i++) Hraw[(size_t)i * m + jj] = h->hbuf[i];
+        for (int i = 0; i <= jj; i++) Hraw[(size_t)i * m + jj] = rb[i];
       } else {
         const double r = h->hbuf[kGsR], hj = h->hbuf[kGsR + 1];
         if (jj > 0) {
@@ -1378,8 +1416,8 @@ int fgmres(vfs_poisson *h, const vfs_solve_opts &o, vfs_solve_stats *st) {
   if (h->phase) {
     fprintf(stderr, "vfs phase ms: precondition %.3f apply %.3f gram-schmidt %.3f (iterations %d)\n",
             h->phase_ms[0], h->phase_ms[1], h->phase_ms[2], it);
-    fprintf(stderr, "vfs host ms: enqueue-vcycle %.3f enqueue-rest %.3f wait %.3f iteration-wall %.3f\n",
-            h->host_ms[0], h->host_ms[1], h->host_ms[2], h->host_ms[3]);
+    fprintf(stderr, "vfs host ms: enqueue %.3f wait %.3f iteration-wall %.3f\n", h->host_ms[0], h->host_ms[2],
+            h->host_ms[3]);
     h->phase_ms[0] = h->phase_ms[1] = h->phase_ms[2] = 0.;
     for (double &v : h->host_ms) v = 0.;
   }
@@ -1458,6 +1496,8 @@ int vfs_poisson_create(const vfs_grid_desc *gd, vfs_poisson **out) {
   {
     const char *e = getenv("VFS_PHASE_TIMING");
     h->phase = e && e[0] == '1';
+    const char *sp = getenv("VFS_GUESS_SPECULATE");
+    h->spec_enable = !(sp && sp[0] == '0');
   }
   const size_t N = h->g.n(), n = h->box.n();
   int rc;
@@ -1504,6 +1544,8 @@ void vfs_poisson_destroy(vfs_poisson *h) {
       if (h->pev[a][q]) cudaEventDestroy(h->pev[a][q]);
   for (int q = 0; q < 4; q++)
     if (h->phev[q]) cudaEventDestroy(h->phev[q]);
+  if (h->ev_feat) cudaEventDestroy(h->ev_feat);
+  if (h->side) cudaStreamDestroy(h->side);
   if (h->stream && h->own_stream) cudaStreamDestroy(h->stream);
   cudaGetLastError();
   delete h;
@@ -1825,7 +1867,7 @@ int guess_buffers(vfs_poisson *h) {
 }
 
 // fine feature planes of the current right-hand side into h->gfeat; also
-// phi_{n-1} as a box vector in h->Z[0] and the squared norms of b - A ex,
+// phi_{n-1} as a box vector in the last Z and the squared norms of b - A ex,
 // b - A phi_{n-1} (an FP32 estimate) and b in norms[0..2]
 int guess_features(vfs_poisson *h, const double *phi_nm1, const double *phi_nm2, double *norms) {
   if (!h || !phi_nm1 || !phi_nm2) return fail(VFS_EINVAL, "null argument");
@@ -1840,7 +1882,9 @@ int guess_features(vfs_poisson *h, const double *phi_nm1, const double *phi_nm2,
   TRY(device_view(h, phi_nm2, h->stage + N, N, &p2));
   CUDA_TRY(cudaMemsetAsync(h->gsum, 0, 8 * sizeof(double), h->stream));
   TRY(ensure_krylov(h, std::max(h->m_alloc, 20)));
-  double *prev = h->Z[0];  // free until the next solve
+  // phi_{n-1} (box layout) in the last preconditioned vector, free until the
+  // next solve (the speculative step 0 writes Z_0)
+  double *prev = h->Z[h->m_alloc - 1];
   LAUNCH(h, k_guess_prep, kRedBlocks, 256, h->g, h->box, h->rowtype0, p1, p2, h->gex, prev, h->prev32, feat,
          feat + n, feat + 3 * n, h->gsum);
   const dim3 gr = guess_grid(h->box);
@@ -1895,10 +1939,61 @@ int vfs_poisson_learned_guess(vfs_poisson *h, vfs_unet *u, const double *phi_nm1
   if (!h || !u) return fail(VFS_EINVAL, "null argument");
   const Box b = h->box;
   h->r0_valid = false;
+  h->spec_valid = false;
   if (h->phase) cudaEventRecord(h->phev[0], h->stream);
   double nrm[3];
   TRY(guess_features(h, phi_nm1, phi_nm2, nrm));
   const size_t n = b.n();
+  // speculative step 0 of the next solve on the handle's stream; the network
+  // and the band fit then run on the side stream with their own reduction
+  // buffers (the step's V-cycle, apply and Gram-Schmidt use V_0, V_1, Z_0,
+  // dsv, partial, red and the level buffers; the guess reads r and writes
+  // its own planes)
+  const bool spec = h->spec_enable && h->spec_next && !h->phase && !h->prof && nrm[0] > 0.;
+  // puts the handle's stream and reduction buffers back on every exit
+  struct SideScope {
+    vfs_poisson *h;
+    vfs_unet *u;
+    cudaStream_t main;
+    bool on = false;
+    void leave() {
+      if (!on) return;
+      h->stream = main;
+      std::swap(h->partial, h->spartial);
+      std::swap(h->red, h->sred);
+      vfs_unet_set_stream(u, main);
+      on = false;
+    }
+    ~SideScope() { leave(); }
+  } side_scope{h, u, h->stream};
+  if (spec) {
+    if (!h->side) {
+      CUDA_TRY(cudaStreamCreateWithFlags(&h->side, cudaStreamNonBlocking));
+      CUDA_TRY(cudaEventCreateWithFlags(&h->ev_feat, cudaEventDisableTiming));
+      const dim3 gb = guess_grid(h->box);
+      TRY(dalloc(h, &h->spartial, (size_t)16 * gb.x * gb.y * gb.z + 4096));
+      TRY(dalloc(h, &h->sred, 32));
+    }
+    vfs_solve_opts so;
+    vfs_poisson_default_opts(&so);
+    resolve_opts(so);
+    h->spec_opts = so;
+    const double beta = std::sqrt(nrm[0]);
+    CUDA_TRY(cudaEventRecord(h->ev_feat, h->stream));
+    CUDA_TRY(cudaMemcpyAsync(h->V[0], h->r, n * 8, cudaMemcpyDeviceToDevice, h->stream));
+    h->hbuf[kSpecStage] = beta * beta;
+    h->hbuf[kSpecStage + 1] = 1.0 / beta;
+    reinterpret_cast<float *>(h->hbuf + kSpecStage + 2)[0] = (float)(1.0 / beta);
+    CUDA_TRY(cudaMemcpyAsync(h->dsv, h->hbuf + kSpecStage, 16, cudaMemcpyHostToDevice, h->stream));
+    CUDA_TRY(cudaMemcpyAsync(h->dsv32, h->hbuf + kSpecStage + 2, 4, cudaMemcpyHostToDevice, h->stream));
+    const int nbd = (int)((n + 256 * kGsTile - 1) / (256 * kGsTile));
+    TRY(arnoldi_enqueue(h, 0, nbd, so, kSpecHb));
+    CUDA_TRY(cudaStreamWaitEvent(h->side, h->ev_feat, 0));
+    h->stream = h->side;
+    std::swap(h->partial, h->spartial);
+    std::swap(h->red, h->sred);
+    side_scope.on = true;
+  }
   if (h->phase) cudaEventRecord(h->phev[1], h->stream);
   LAUNCH(h, k_guess_restrict, kRedBlocks, 256, b, h->gfeat, nullptr, h->gfc, nullptr, nullptr);
   vfs_unet_set_stream(u, h->stream);
@@ -1929,7 +2024,9 @@ int vfs_poisson_learned_guess(vfs_poisson *h, vfs_unet *u, const double *phi_nm1
   LAUNCH(h, k_guess_gram, gg, 128, b, h->L[0].A32, (const float *)h->scale32, h->gof[cur], h->r, kappa, h->gsum,
          kGramStride, h->partial);
   double gm[14];
-  TRY(reduce_read(h, (int)(gg.x * gg.y * gg.z), 14, gm));
+  const int grc = reduce_read(h, (int)(gg.x * gg.y * gg.z), 14, gm);
+  side_scope.leave();  // back to the handle's stream and buffers
+  TRY(grc);
   for (double &v : gm) v *= (double)b.nz / gg.z;
   BandWeights bw{};
   {
@@ -2015,7 +2112,7 @@ int vfs_poisson_learned_guess(vfs_poisson *h, vfs_unet *u, const double *phi_nm1
   double r_prev64 = r_prev;
   if (!learned) {
     // the previous step's phi stays: its FP64 residual is FGMRES's start
-    CUDA_TRY(cudaMemcpyAsync(h->x, h->Z[0], n * 8, cudaMemcpyDeviceToDevice, h->stream));
+    CUDA_TRY(cudaMemcpyAsync(h->x, h->Z[h->m_alloc - 1], n * 8, cudaMemcpyDeviceToDevice, h->stream));
     const dim3 gr = box_grid(h->box);
     LAUNCH(h, k_residual64, gr, 128, h->box, h->A0, h->x, h->b, h->rprev, h->partial);
     double s2 = 0.;
@@ -2025,6 +2122,10 @@ int vfs_poisson_learned_guess(vfs_poisson *h, vfs_unet *u, const double *phi_nm1
   h->r0 = learned ? h->rlearn : h->rprev;
   h->r0_norm = learned ? r_learn : r_prev64;
   h->r0_valid = true;
+  // the speculative step holds when the installed iterate is the plain
+  // extrapolation (its residual and norm are the step's V_0 and beta)
+  h->spec_valid = spec && learned && !weighted;
+  h->spec_next = learned && !weighted;
   if (chosen) *chosen = learned ? 1 : 0;
   if (rel_res) {
     rel_res[0] = r_prev64 / nb;

@@ -2097,7 +2097,9 @@ int vfs_poisson_learned_guess(vfs_poisson *h, vfs_unet *u, const double *phi_nm1
     r_learn = std::sqrt(nrm[0]);
     learned = r_learn < r_prev;
     if (learned) {
-      CUDA_TRY(cudaMemcpyAsync(h->x, h->gex, n * 8, cudaMemcpyDeviceToDevice, h->stream));
+      // the extrapolation becomes the iterate: the two box vectors trade
+      // places (no queued work reads or writes either here)
+      std::swap(h->x, h->gex);
       CUDA_TRY(cudaMemcpyAsync(h->rlearn, h->r, n * 8, cudaMemcpyDeviceToDevice, h->stream));
     }
   } else if (r_learn < 1.1 * r_prev) {

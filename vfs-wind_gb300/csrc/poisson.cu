@@ -1002,7 +1002,10 @@ void prof_end(vfs_poisson *h, int li) {
 template <typename T>
 void smooth(vfs_poisson *h, Level &l, int li, int smoother, bool zero_guess, T omega, T *&x, T *&t, T *bb, T *r) {
   const int P = (l.b.ny + kLineChunk - 1) / kLineChunk;
-  constexpr int TI = 16;  // columns per block of the line kernels (k_line_tri: 384 threads at most)
+  // columns per block of the line kernels (at most 384 threads): 16 in FP32;
+  // 4 in FP64, where more, smaller blocks per SM measured faster (warm FP64
+  // solve 31.5 -> 30.3 ms on the 256x192x256 towers grid; FP32 unchanged)
+  const int TI = std::is_same<T, double>::value ? 4 : 16;
   dim3 lb(TI, P), lg((l.b.nx + TI - 1) / TI, l.b.nz);
   const size_t lsm = 2 * TI * P * sizeof(T);
   T *Asp = Prec<T>::A(l) + (size_t)SP * l.b.n();

@@ -384,8 +384,9 @@ def run_ours(args):
             "workload": workload(nx, ny, nz), "cells": nx * ny * nz, "rtol": 1e-8,
             "solver": "FGMRES(20) with one-pass classical Gram-Schmidt, FP64 residual, operator apply and Krylov; FP32 geometric "
                       "V-cycle (zebra j-line Gauss-Seidel over checkerboard columns, 1+2 sweeps; residual couplings "
-                      "stored in half precision, difference form); learned initial guess judged against the "
-                      "previous step",
+                      "stored in half precision, difference form, formed inside the line kernel on the levels of at "
+                      "most 2^20 cells; dense projected solve on a 192-cell coarsest level); learned initial guess "
+                      "judged against the previous step, the solve's first Arnoldi step overlapping the network",
             "iterations": statistics.mean(its_b), "learned_guess_chosen": sum(chosen) / len(chosen),
             "initial_rel_residual_learned": statistics.mean(rel_learned),
             "initial_rel_residual_previous_step": statistics.mean(rel_prev),

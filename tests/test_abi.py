@@ -38,3 +38,36 @@ def test_no_cpu_fallback_without_gpu(cuda_lib):
         assert e.code in (vfs_poisson.VFS_ECUDA, vfs_poisson.VFS_ENOMEM)
     else:
         raise AssertionError("the library must fail loudly without a GPU")
+
+
+def test_python_structs_match_the_header(tmp_path):
+    """Every ctypes mirror of a struct in include/vfs_poisson.h has the C
+    layout: a small C program built with gcc against the header prints each
+    field's offset and each struct's size."""
+    import shutil
+    import subprocess
+    import pytest
+    import vfs_poisson as V
+    gcc = shutil.which("gcc")
+    if gcc is None:
+        pytest.skip("gcc not available")
+    mirrors = {"vfs_grid_desc": V.GridDesc, "vfs_solve_opts": V.SolveOpts, "vfs_solve_stats": V.SolveStats,
+               "vfs_ibm_node": V.IbmNode, "vfs_unet_batch": V.UNetBatch}
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "vfs_poisson.h"', "int main(void) {"]
+    for cname, py in mirrors.items():
+        lines.append(f'  printf("{cname} size %zu\\n", sizeof({cname}));')
+        for f, _ in py._fields_:
+            lines.append(f'  printf("{cname} {f} %zu\\n", offsetof({cname}, {f}));')
+    lines += ["  return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    subprocess.run([gcc, "-std=c99", "-I", os.path.join(REPO, "include"), str(src), "-o", str(exe)], check=True)
+    got = {}
+    for ln in subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.splitlines():
+        cname, field, val = ln.split()
+        got[(cname, field)] = int(val)
+    for cname, py in mirrors.items():
+        assert got[(cname, "size")] == ctypes.sizeof(py), cname
+        for f, _ in py._fields_:
+            assert got[(cname, f)] == getattr(py, f).offset, (cname, f)

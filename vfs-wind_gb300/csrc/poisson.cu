@@ -2100,10 +2100,11 @@ int vfs_poisson_learned_guess(vfs_poisson *h, vfs_unet *u, const double *phi_nm1
     r_learn = std::sqrt(nrm[0]);
     learned = r_learn < r_prev;
     if (learned) {
-      // the extrapolation becomes the iterate: the two box vectors trade
-      // places (no queued work reads or writes either here)
+      // the extrapolation becomes the iterate and its residual the learned
+      // candidate's: the box vectors trade places (queued work holds the
+      // pointers it was launched with; none writes these buffers later)
       std::swap(h->x, h->gex);
-      CUDA_TRY(cudaMemcpyAsync(h->rlearn, h->r, n * 8, cudaMemcpyDeviceToDevice, h->stream));
+      std::swap(h->r, h->rlearn);
     }
   } else if (r_learn < 1.1 * r_prev) {
     LAUNCH(h, k_guess_compose, kRedBlocks, 256, b, h->rowtype0, h->gex, h->gof[cur], kappa, h->gsum, bw, h->x);

@@ -54,7 +54,8 @@ def test_speculative_first_step_bitexact(cuda_lib, monkeypatch):
     next solve's first Arnoldi step on the handle's stream while the network
     runs on a side stream.  Solves that resume from it match solves that
     form every step themselves bit for bit, step after step; and a solve
-    whose options differ from the step's forms its own first step."""
+    whose options differ from the step's, or that needs a larger Krylov
+    basis, forms its own first step."""
     import torch
     import vfs_poisson as V
     from vfs_poisson import learned as LG, sequence as S
@@ -76,8 +77,13 @@ def test_speculative_first_step_bitexact(cuda_lib, monkeypatch):
         s.learned_guess(net, hist2[-1], hist2[-2], net.kappa)
         phi = torch.empty_like(hist2[-1])
         _, st = s.solve(phi, opts=V.default_opts(precision=0, warm_start=2, nu2=3))
-        runs[spec] = ([r["iterations"] for r in recs], [h.clone() for h in hist2], st.iterations, phi.clone())
-        assert all(r["rel"] <= 1e-8 for r in recs) and st.rel_residual <= 1e-8
+        # and one whose restart length needs a larger basis than the step's
+        s.learned_guess(net, hist2[-1], hist2[-2], net.kappa)
+        phi2 = torch.empty_like(hist2[-1])
+        _, st2 = s.solve(phi2, opts=V.default_opts(precision=0, warm_start=2, restart=30))
+        runs[spec] = ([r["iterations"] for r in recs], [h.clone() for h in hist2], st.iterations, phi.clone(),
+                      st2.iterations, phi2.clone())
+        assert all(r["rel"] <= 1e-8 for r in recs) and st.rel_residual <= 1e-8 and st2.rel_residual <= 1e-8
         assert all(r["chosen"] == 1 for r in recs)
         s.close()
         net.close()
@@ -86,3 +92,4 @@ def test_speculative_first_step_bitexact(cuda_lib, monkeypatch):
     for x, y in zip(a[1], b[1]):
         assert torch.equal(x, y)
     assert torch.equal(a[3], b[3])
+    assert a[4] == b[4] and torch.equal(a[5], b[5])

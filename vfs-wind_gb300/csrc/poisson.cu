@@ -1297,6 +1297,8 @@ bool spec_matches(const vfs_solve_opts &a, const vfs_solve_opts &b) {
 int fgmres(vfs_poisson *h, const vfs_solve_opts &o, vfs_solve_stats *st) {
   const size_t n = h->box.n();
   const int m = o.restart;
+  // a larger basis is allocated afresh: the speculative step's vectors go
+  if (m > h->m_alloc) h->spec_valid = false;
   TRY(ensure_krylov(h, m));
   const int nbd = (int)((n + 256 * kGsTile - 1) / (256 * kGsTile));
   double bn2;

@@ -103,6 +103,7 @@ LINE_FUSED_DECL(k_line_fused16_z)
 #undef LINE_FUSED_DECL
 __global__ void k_apply64(Box b, const double *A, const double *x, double *y);
 __global__ void k_residual64(Box b, const double *A, const double *x, const double *rhs, double *r, double *partial);
+__global__ void k_residual64r(Box b, const double *A, const double *x, const double *rhs, double *r);
 // Gram-Schmidt rows of the reduced values (solve.cu): Q.u at 0.., Q.w at
 // kGsB.., u.u and u.w at kGsUU, r, h and 1/r at kGsR.
 // kGsTile cells per thread in k_gs_dots* and k_gs_update (256-thread blocks).

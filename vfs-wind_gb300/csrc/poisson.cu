@@ -1166,11 +1166,14 @@ int reduce_read(vfs_poisson *h, int nb, int nrow, double *out) {
   return VFS_OK;
 }
 
+// r = b - A x in FP64 and ||r||: the residual kernel without a reduction,
+// then the fixed-shape sum of squares (faster than block partials formed in
+// the stencil kernel, whose barriers hold its loads back)
 int residual_norm(vfs_poisson *h, const double *x, double *r, double *norm) {
-  dim3 gr = box_grid(h->box);
-  LAUNCH(h, k_residual64, gr, 128, h->box, h->A0, x, h->b, r, h->partial);
+  LAUNCH(h, k_residual64r, box_grid(h->box), 128, h->box, h->A0, x, h->b, r);
+  LAUNCH(h, k_sumsq, kRedBlocks, 256, h->box.n(), r, h->partial);
   double s;
-  TRY(reduce_read(h, (int)(gr.x * gr.y * gr.z), 1, &s));
+  TRY(reduce_read(h, kRedBlocks, 1, &s));
   *norm = std::sqrt(s);
   return VFS_OK;
 }

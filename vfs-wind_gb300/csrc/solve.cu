@@ -107,6 +107,23 @@ __global__ void __launch_bounds__(256) k_apply64(Box b, const double *__restrict
   y[c] = s;
 }
 
+// FP64 r = rhs - A x (the same products and order as k_residual64; its
+// norm comes from k_sumsq over fixed blocks, so no block barrier holds the
+// stencil's loads back).
+__global__ void __launch_bounds__(256) k_residual64r(Box b, const double *__restrict__ A,
+                                                     const double *__restrict__ x, const double *__restrict__ rhs,
+                                                     double *__restrict__ r) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y, k = blockIdx.z;
+  if (i >= b.nx) return;
+  uint32_t idx[NSLOT];
+  stencil_index(b, i, j, k, idx);
+  const uint32_t n = (uint32_t)b.n(), c = idx[CP];
+  double s = 0.;
+#pragma unroll
+  for (int q = 0; q < NSLOT; q++) s = fma(__ldcs(&A[q * n + c]), __ldg(&x[idx[q]]), s);
+  r[c] = rhs[c] - s;
+}
+
 // FP64 r = rhs - A x with the block partial of ||r||^2.
 __global__ void __launch_bounds__(256) k_residual64(Box b, const double *__restrict__ A, const double *__restrict__ x,
                                                     const double *__restrict__ rhs, double *__restrict__ r,

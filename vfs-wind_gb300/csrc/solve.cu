@@ -908,8 +908,9 @@ __global__ void k_sumsq(size_t n, const double *__restrict__ x, double *partial)
     coarsest_body<T>(nd, dmap, didx, dinv, rhs, x, n);                                                     \
   }                                                                                                        \
   __global__ void k_cast_planes_##S(const double *src, T *dst, size_t n) { cast_body<T>(src, dst, n); }
-// the line kernel keeps a whole chunk in registers: 16 columns per block
-// (at most 24 chunks each) so that neither precision spills
+// the line kernel keeps a whole chunk in registers: at most 384 threads per
+// block (16 columns of up to 24 chunks in FP32, 4 columns in FP64) so that
+// neither precision spills
 TYPED(float, f32, 384, 1)
 TYPED(double, f64, 384, 1)
 #undef TYPED

@@ -245,3 +245,42 @@ def test_contra2cart_recovers_uniform_velocity():
     ucat = O.contra2cart(d, c.nvert, met, ucont)
     inner = ucat[1:-1, 1:-1, 1:-1]
     np.testing.assert_allclose(inner, np.broadcast_to(vel, inner.shape), rtol=0, atol=1e-12)
+
+
+@pytest.mark.parametrize("density", [1.0, 3.0])
+def test_levelset_operator_with_uniform_density(system, density):
+    """The level-set branch of the restated operator with a uniform density
+    and no Dirichlet faces is the plain operator divided by that density
+    (harmonic face means of equal densities)."""
+    case, d, met, lhs = system
+    rho = np.full(case.nvert.shape, density)
+    try:
+        O.set_levelset(rho, np.zeros_like(rho), (0, 0, 0, 0, 0, 0))
+        ls = O.poisson_lhs(d, case.nvert, met)
+    finally:
+        O.set_levelset(None)
+    assert ls["ndof"] == lhs["ndof"]
+    np.testing.assert_array_equal(ls["col"], lhs["col"])
+    np.testing.assert_allclose(ls["vol"], lhs["vol"] / density, rtol=1e-13, atol=1e-13 * np.abs(lhs["vol"]).max())
+
+
+def test_levelset_dirichlet_top_makes_rows_regular():
+    """With bctype[3] == 4 (zero-Dirichlet j-top faces) the rows next to the
+    top face lose their zero row sum and the others keep it."""
+    case = CF.channel(12, 10, 12)
+    d = O.dims_of(case)
+    met = O.form_metrics(d, case.coor)
+    rho = np.where(np.arange(case.nvert.shape[1])[None, :, None] < 6, 1000.0, 1.2) * np.ones(case.nvert.shape)
+    try:
+        O.set_levelset(rho, np.zeros_like(rho), (0, 0, 0, 4, 0, 0))
+        lhs = O.poisson_lhs(d, case.nvert, met)
+    finally:
+        O.set_levelset(None)
+    A = O.csr(lhs)
+    rs = np.abs(A @ np.ones(A.shape[0]))
+    gid = lhs["gid"]
+    top = gid[1:-1, -2, 1:-1]
+    rest = gid[1:-1, 1:-2, 1:-1]
+    scale = np.abs(A.diagonal()).max()
+    assert (rs[top[top >= 0]] > 1e-8 * scale).all()
+    assert rs[rest[rest >= 0]].max() < 1e-12 * scale

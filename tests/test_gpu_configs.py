@@ -1,0 +1,142 @@
+"""Solves at the stated configuration sizes and on long j-lines, against the
+oracle (marked gpu).
+
+  * configuration 1 (64x64x64 channel) and configuration 2 (128x96x128
+    curvilinear grid with the cylinder), both precisions of the V-cycle:
+    the true FP64 relative residual of the returned phi is <= 1e-8 (the
+    oracle's operator and right-hand side), phi is within 1e-6 relative L2
+    of the oracle's CPU solve to 1e-12 (both with the fluid mean removed,
+    Source/poisson_hypre.c:202-263), and the max divergence after
+    UpdatePressure + Projection is within 10 % of the one the oracle's
+    projection of its own phi leaves (Source/main.c:936-1074);
+  * j-lines longer than 192 cells (the 256- and 512-cell-high grids of the
+    larger configurations) run on narrower line-kernel blocks: the block
+    width changes no bit of a solve, and a 256-cell-high stretched grid
+    with towers solves to the oracle's phi.
+"""
+import os
+
+import numpy as np
+import pytest
+
+import oracle as O
+from vfs_poisson import configs as CF
+
+pytestmark = pytest.mark.gpu
+
+
+def _oracle(case, rtol=1e-12):
+    d = O.dims_of(case)
+    met = O.form_metrics(d, case.coor)
+    lhs = O.poisson_lhs(d, case.nvert, met)
+    b2 = O.rhs(d, case.nvert, lhs["gid"], case.ucont, met["aj"])
+    mg = O.MGSolver(d, case.coor, case.nvert, met)
+    x, st = mg.solve(O.to_da(d, lhs["gid"], b2), rtol=rtol, max_it=400)
+    assert st.rel_residual <= rtol * 1.01, (st.iterations, st.rel_residual)
+    x2 = O.remove_nullspace(d, case.nvert, lhs["gid"], O.from_da(d, lhs["gid"], x))
+    phi = O.convert_phi2_phi(d, case.nvert, x2)
+    u = O.projection(d, case.nvert, phi, met, case.ucont)
+    return d, met, lhs, b2, x2, O.divergence(d, case.nvert, u, met["aj"])
+
+
+def _check_solve(case, s, ref, precision):
+    d, met, lhs, b2, x2, maxdiv_o = ref
+    s.rhs(case.ucont)
+    phi, st = s.solve(precision=precision, rtol=1e-8, max_it=100)
+    assert st.status == 0 and st.rel_residual <= 1e-8, st.as_dict()
+    A = O.csr(lhs)
+    phi2 = O.from_da(d, lhs["gid"], phi)
+    assert np.linalg.norm(b2 - A @ phi2) / np.linalg.norm(b2) <= 1.2e-8
+    fl = O.from_da(d, lhs["gid"], (case.nvert < 0.1).astype(np.float64)) > 0
+    err = np.linalg.norm((phi2 - x2)[fl]) / np.linalg.norm(x2[fl])
+    assert err <= 1e-6, err
+    u = case.ucont.copy()
+    s.update_pressure(np.zeros_like(phi), phi.copy())
+    s.projection(u)
+    maxdiv = s.divergence(u)
+    assert abs(maxdiv - maxdiv_o) <= 0.1 * maxdiv_o, (maxdiv, maxdiv_o)
+    return st
+
+
+FULL = {
+    "c1_channel_64x64x64": lambda: CF.channel(64, 64, 64),
+    "c2_cylinder_128x96x128": lambda: CF.cylinder(128, 96, 128),
+}
+
+
+@pytest.fixture(scope="module", params=list(FULL), ids=list(FULL))
+def full(request, cuda_lib):
+    import vfs_poisson as V
+    case = FULL[request.param]()
+    ref = _oracle(case)
+    s = V.PoissonSolver.from_case(case)
+    yield case, s, ref
+    s.close()
+
+
+@pytest.mark.parametrize("precision", [0, 1], ids=["fp32mg", "fp64mg"])
+def test_stated_configuration_vs_oracle(full, precision):
+    case, s, ref = full
+    _check_solve(case, s, ref, precision)
+
+
+def _tall(ny, nx=24, nz=24):
+    # towers on a 1.02 geometric wall stretching (the largest configuration's
+    # ratio), radius large enough to cover a few cells of the coarse grid
+    return CF.towers(nx, ny, nz, ratio=1.02, radius=0.1, array=(2, 1))
+
+
+def _solver_with_columns(case, cap):
+    import vfs_poisson as V
+    old = os.environ.get("VFS_LINE_COLUMNS")
+    try:
+        if cap:
+            os.environ["VFS_LINE_COLUMNS"] = str(cap)
+        else:
+            os.environ.pop("VFS_LINE_COLUMNS", None)
+        return V.PoissonSolver.from_case(case)
+    finally:
+        if old is None:
+            os.environ.pop("VFS_LINE_COLUMNS", None)
+        else:
+            os.environ["VFS_LINE_COLUMNS"] = old
+
+
+@pytest.mark.parametrize("precision", [0, 1], ids=["fp32mg", "fp64mg"])
+def test_line_block_width_changes_no_bit(cuda_lib, precision):
+    """192-cell j-lines: the default blocks (16 columns in FP32, 4 in FP64)
+    and blocks capped at 8 / 2 columns give bit-identical solves."""
+    case = _tall(192, 32, 32)
+    outs = []
+    for cap in (0, 8 if precision == 0 else 2):
+        s = _solver_with_columns(case, cap)
+        try:
+            s.rhs(case.ucont)
+            phi, st = s.solve(precision=precision, rtol=1e-10, max_it=60)
+            outs.append((phi, st.iterations, st.rel_residual))
+        finally:
+            s.close()
+    assert outs[0][1] == outs[1][1]
+    assert outs[0][2] == outs[1][2]
+    np.testing.assert_array_equal(outs[0][0], outs[1][0])
+
+
+@pytest.mark.parametrize("precision", [0, 1], ids=["fp32mg", "fp64mg"])
+def test_long_lines_vs_oracle(cuda_lib, precision):
+    """A 24x256x24 grid (256-cell j-lines: 8-column blocks in FP32) solves
+    to 1e-8 and to the oracle's phi."""
+    import vfs_poisson as V
+    case = _tall(256)
+    ref = _oracle(case)
+    s = V.PoissonSolver.from_case(case)
+    try:
+        _check_solve(case, s, ref, precision)
+    finally:
+        s.close()
+
+
+def test_too_long_lines_rejected(cuda_lib):
+    import vfs_poisson as V
+    with pytest.raises(V.VfsError) as e:
+        V.PoissonSolver(6, 3075, 6)
+    assert e.value.code == V.VFS_EINVAL

@@ -100,3 +100,30 @@ def test_solve(lspair):
         if np.linalg.norm(a1) > 0:
             r = r - (r @ a1) / (a1 @ a1) * a1
     assert np.linalg.norm(r) / np.linalg.norm(b_g) <= 1.2e-8
+
+
+def test_disable_requires_new_operator(cuda_lib):
+    """Turning level-set mode off invalidates the density-weighted operator:
+    the next right-hand side without a new set_nvert is refused, and after
+    set_nvert the operator is the plain one again."""
+    import vfs_poisson as V
+    c, rho, level = _case("density")
+    s = V.PoissonSolver(*c.dims, periodic=c.periodic)
+    try:
+        s.set_grid(c.coor)
+        s.set_levelset(rho, level, VARIANTS["density"])
+        s.set_nvert(c.nvert)
+        s.rhs(c.ucont)
+        s.set_levelset(None, enable=False)
+        with pytest.raises(V.VfsError) as e:
+            s.rhs(c.ucont)
+        assert e.value.code == V.VFS_ESTATE
+        s.set_nvert(c.nvert)
+        d = O.dims_of(c)
+        met = O.form_metrics(d, c.coor)
+        O.set_levelset(None)
+        lhs = O.poisson_lhs(d, c.nvert, met)
+        vol, _ = s.operator()
+        np.testing.assert_array_equal(vol, lhs["vol"])
+    finally:
+        s.close()

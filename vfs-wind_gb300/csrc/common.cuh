@@ -53,9 +53,34 @@ __device__ __forceinline__ void box_ijk(const Box &b, size_t c, int &i, int &j, 
   k = (int)kk;
 }
 
+// |div(Ucont) aj| of DA cell (i, j, k), zero when the cell or one of its six
+// face neighbours is blanked (nvert sum > 0.1), exactly as Divergence
+// computes it (Source/main.c:956-958).  Shared by the handle's divergence
+// kernel and the no-allocation entry point; both translation units are
+// compiled without FMA contraction.
+__device__ __forceinline__ double divergence_cell(const Grid &g, const double *__restrict__ nvert,
+                                                  const double *__restrict__ ucont, const double *__restrict__ aj,
+                                                  int i, int j, int k) {
+#define VFS_U(a, b, c, q) ucont[g.at(a, b, c) * 3 + (q)]
+#define VFS_NV(a, b, c) nvert[g.at(a, b, c)]
+  double v = fabs((VFS_U(i, j, k, 0) - VFS_U(i - 1, j, k, 0) + VFS_U(i, j, k, 1) - VFS_U(i, j - 1, k, 1) +
+                   VFS_U(i, j, k, 2) - VFS_U(i, j, k - 1, 2)) *
+                  aj[g.at(i, j, k)]);
+  if (VFS_NV(i, j, k) + VFS_NV(i, j, k + 1) + VFS_NV(i, j, k - 1) + VFS_NV(i, j + 1, k) + VFS_NV(i, j - 1, k) +
+          VFS_NV(i + 1, j, k) + VFS_NV(i - 1, j, k) >
+      0.1)
+    v = 0.;
+#undef VFS_U
+#undef VFS_NV
+  return v;
+}
+
 // Cells of a j-line handled by one thread of the line smoother; a line of
-// ny cells uses ceil(ny / kLineChunk) threads (at most 24, 768 per block).
+// ny cells uses ceil(ny / kLineChunk) threads per column.
 constexpr int kLineChunk = 8;
+// Threads per block the line kernels are compiled for (launch bounds): a
+// block holds TI columns of ceil(ny / kLineChunk) chunks each.
+constexpr int kLineMaxThreads = 384;
 
 // Level-set context of the operator and the projection (poisson.c
 // levelset branches): density and level-set field at the cells (DA layout

@@ -50,23 +50,6 @@ void *g_scratch_addr[kMaxDevices] = {};
 std::mutex g_scratch_mu;
 
 
-// Divergence of one cell exactly as Source/main.c:956-958 computes it.
-__device__ inline double cell_div(const Grid &g, const double *nvert, const double *ucont, const double *aj, int i,
-                                  int j, int k) {
-#define U(a, b, c, q) ucont[g.at(a, b, c) * 3 + (q)]
-#define NV(a, b, c) nvert[g.at(a, b, c)]
-  double v = fabs((U(i, j, k, 0) - U(i - 1, j, k, 0) + U(i, j, k, 1) - U(i, j - 1, k, 1) + U(i, j, k, 2) -
-                   U(i, j, k - 1, 2)) *
-                  aj[g.at(i, j, k)]);
-  if (NV(i, j, k) + NV(i, j, k + 1) + NV(i, j, k - 1) + NV(i, j + 1, k) + NV(i, j - 1, k) + NV(i + 1, j, k) +
-          NV(i - 1, j, k) >
-      0.1)
-    v = 0.;
-#undef U
-#undef NV
-  return v;
-}
-
 // Block b reduces interior cells [b*kCellsPerBlock, (b+1)*kCellsPerBlock)
 // into scratch[b].  Every launched block writes its own slot before the
 // final kernel reads it, so nothing in the scratch has to start at zero.
@@ -81,7 +64,7 @@ __global__ void __launch_bounds__(kThreads) k_div_partial_noalloc(Grid g, Box b,
     int i, j, k;
     box_ijk(b, c, i, j, k);
     i++; j++; k++;
-    double v = cell_div(g, nvert, ucont, aj, i, j, k);
+    const double v = divergence_cell(g, nvert, ucont, aj, i, j, k);
     best = v > best ? v : best;
   }
   best = block_max(best);
@@ -95,13 +78,17 @@ __global__ void k_div_final_noalloc(const double *scratch, int nb, double *out) 
   if (threadIdx.x == 0) *out = m;
 }
 
-bool on_device(const void *p) {
+// True for memory that kernels on device `dev` may read: device memory of
+// that device, or managed memory.  Device memory of another GPU is refused
+// (without peer access a kernel would fault on it).
+bool on_device(const void *p, int dev) {
   cudaPointerAttributes a;
   if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
     cudaGetLastError();
     return false;
   }
-  return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+  if (a.type == cudaMemoryTypeManaged) return true;
+  return a.type == cudaMemoryTypeDevice && a.device == dev;
 }
 
 int fail(int code, const std::string &m) {
@@ -126,13 +113,13 @@ int vfs_divergence_noalloc(const vfs_grid_desc *gd, const double *ucont, const d
   if (nb > (size_t)kMaxBlocks)
     return fail(VFS_EINVAL, "grid has " + std::to_string(n) + " interior cells; vfs_divergence_noalloc handles at most " +
                                 std::to_string((size_t)kMaxBlocks * kCellsPerBlock));
-  if (!on_device(ucont) || !on_device(nvert) || !on_device(aj) || !on_device(maxdiv))
-    return fail(VFS_EINVAL, "vfs_divergence_noalloc takes device pointers only");
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
     cudaGetLastError();
     return fail(VFS_ECUDA, "no current CUDA device");
   }
+  if (!on_device(ucont, dev) || !on_device(nvert, dev) || !on_device(aj, dev) || !on_device(maxdiv, dev))
+    return fail(VFS_EINVAL, "vfs_divergence_noalloc takes device pointers of the current device only");
   void *scratch = nullptr;
   {
     std::lock_guard<std::mutex> lk(g_scratch_mu);

@@ -473,6 +473,7 @@ struct vfs_poisson {
   // level-set variant of the operator and projection (vfs_poisson_set_levelset)
   double *ls_rho = nullptr, *ls_level = nullptr;
   int ls_on = 0, ls_bc3 = 0, ls_bc4 = 0, ls_bc5 = 0;
+  int line_cols_cap = 0;  // cap on the line kernels' columns per block (0: none)
   double r0_norm = 0.;
   bool r0_valid = false;
   // Speculative first Arnoldi step: a learned guess that expects the plain
@@ -992,6 +993,21 @@ void prof_end(vfs_poisson *h, int li) {
   h->pcount++;
 }
 
+// Columns per block of the line kernels for lines of P chunks.  The
+// kernels are compiled for at most kLineMaxThreads threads per block (a
+// whole chunk stays in registers): 16 columns in FP32 and 4 in FP64, where
+// more, smaller blocks per SM measured faster (warm FP64 solve 31.5 -> 30.3
+// ms on the 256x192x256 towers grid; FP32 unchanged), halved while the block
+// would exceed the limit (8 columns for j-lines of 193..384 cells in FP32).
+// Every column is solved independently, so the width changes no result bit.
+// VFS_LINE_COLUMNS caps the width (read at create).
+int line_columns(const vfs_poisson *h, int P, bool fp64) {
+  int ti = fp64 ? 4 : 16;
+  if (h->line_cols_cap > 0 && ti > h->line_cols_cap) ti = h->line_cols_cap;
+  while (ti > 1 && ti * P > kLineMaxThreads) ti >>= 1;
+  return ti;
+}
+
 // One smoothing sweep on level l.  smoother 0: fused j-line Jacobi kernel;
 // 1: j-line Jacobi in correction form (residual kernel + tridiagonal
 // kernel); 2: zebra j-line Gauss-Seidel over even then odd k-planes in
@@ -1002,10 +1018,7 @@ void prof_end(vfs_poisson *h, int li) {
 template <typename T>
 void smooth(vfs_poisson *h, Level &l, int li, int smoother, bool zero_guess, T omega, T *&x, T *&t, T *bb, T *r) {
   const int P = (l.b.ny + kLineChunk - 1) / kLineChunk;
-  // columns per block of the line kernels (at most 384 threads): 16 in FP32;
-  // 4 in FP64, where more, smaller blocks per SM measured faster (warm FP64
-  // solve 31.5 -> 30.3 ms on the 256x192x256 towers grid; FP32 unchanged)
-  const int TI = std::is_same<T, double>::value ? 4 : 16;
+  const int TI = line_columns(h, P, std::is_same<T, double>::value);
   dim3 lb(TI, P), lg((l.b.nx + TI - 1) / TI, l.b.nz);
   const size_t lsm = 2 * TI * P * sizeof(T);
   T *Asp = Prec<T>::A(l) + (size_t)SP * l.b.n();
@@ -1479,8 +1492,9 @@ int vfs_poisson_create(const vfs_grid_desc *gd, vfs_poisson **out) {
              pz = gd->k_periodic || gd->kk_periodic;
   if ((px && nx < 3) || (py && ny < 3) || (pz && nz < 3))
     return fail(VFS_EINVAL, "a periodic direction needs at least 3 interior cells");
-  if (ny > 24 * kLineChunk)
-    return fail(VFS_EINVAL, "j-lines longer than " + std::to_string(24 * kLineChunk) + " cells are not supported");
+  if (ny > kLineMaxThreads * kLineChunk)
+    return fail(VFS_EINVAL, "j-lines longer than " + std::to_string(kLineMaxThreads * kLineChunk) +
+                                " cells are not supported");
   if ((size_t)gd->mx * gd->my * gd->mz * NSLOT >= ((size_t)1 << 32))
     return fail(VFS_EINVAL, "grid too large: 19 operator planes must stay below 2^32 entries");
   vfs_poisson *h = new vfs_poisson();
@@ -1506,6 +1520,8 @@ int vfs_poisson_create(const vfs_grid_desc *gd, vfs_poisson **out) {
     h->phase = e && e[0] == '1';
     const char *sp = getenv("VFS_GUESS_SPECULATE");
     h->spec_enable = !(sp && sp[0] == '0');
+    const char *lc = getenv("VFS_LINE_COLUMNS");
+    h->line_cols_cap = lc ? atoi(lc) : 0;
   }
   const size_t N = h->g.n(), n = h->box.n();
   int rc;
@@ -1645,6 +1661,13 @@ int vfs_poisson_rhs(vfs_poisson *h, const double *ucont, double dt, double st, d
 int vfs_poisson_set_levelset(vfs_poisson *h, const double *rho, const double *level, const int *bctype, int enable) {
   if (!h) return fail(VFS_EINVAL, "null handle");
   if (!enable) {
+    if (h->ls_on) {
+      // the assembled operator and right-hand side carry the density
+      // weights: both have to be formed again without them
+      h->have_nvert = false;
+      h->have_rhs = false;
+      h->r0_valid = false;
+    }
     h->ls_on = 0;
     return VFS_OK;
   }

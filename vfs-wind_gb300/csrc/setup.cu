@@ -884,17 +884,7 @@ __global__ void k_divergence(Grid g, Box b, const double *__restrict__ nvert, co
     int i, j, k;
     box_ijk(b, c, i, j, k);
     i++; j++; k++;
-#define U(a, bb, cc, q) ucont[g.at(a, bb, cc) * 3 + (q)]
-#define NV(a, bb, cc) nvert[g.at(a, bb, cc)]
-    double v = fabs((U(i, j, k, 0) - U(i - 1, j, k, 0) + U(i, j, k, 1) - U(i, j - 1, k, 1) + U(i, j, k, 2) -
-                     U(i, j, k - 1, 2)) *
-                    aj[g.at(i, j, k)]);
-    if (NV(i, j, k) + NV(i, j, k + 1) + NV(i, j, k - 1) + NV(i, j + 1, k) + NV(i, j - 1, k) + NV(i + 1, j, k) +
-            NV(i - 1, j, k) >
-        0.1)
-      v = 0.;
-#undef U
-#undef NV
+    const double v = divergence_cell(g, nvert, ucont, aj, i, j, k);
     best = v > best ? v : best;
   }
   double m = block_max(best);

@@ -545,7 +545,7 @@ __device__ __forceinline__ void line_fused16_body(Box b, const __half2 *__restri
   }
 }
 #define LINE_FUSED(NAME, OZ, BZ, MINB)                                                                             \
-  __global__ void __launch_bounds__(384, MINB) NAME(Box b, const __half2 *C, const float *D, const float *xo,         \
+  __global__ void __launch_bounds__(kLineMaxThreads, MINB) NAME(Box b, const __half2 *C, const float *D, const float *xo,         \
                                                  const float *xn, const float *rhs, const float *Asp,             \
                                                  const float *inv, const float *cp, float *xd, float omega,       \
                                                  int color) {                                                     \
@@ -911,8 +911,8 @@ __global__ void k_sumsq(size_t n, const double *__restrict__ x, double *partial)
 // the line kernel keeps a whole chunk in registers: at most 384 threads per
 // block (16 columns of up to 24 chunks in FP32, 4 columns in FP64) so that
 // neither precision spills
-TYPED(float, f32, 384, 1)
-TYPED(double, f64, 384, 1)
+TYPED(float, f32, kLineMaxThreads, 1)
+TYPED(double, f64, kLineMaxThreads, 1)
 #undef TYPED
 
 }  // namespace vfs

@@ -25,6 +25,7 @@
  *                             poisson_hypre.c:265, :118 -> vfs_poisson_rhs
  *   PoissonRHS2               poisson.c:1780       -> vfs_poisson_rhs2
  *   VolumeFlux (immersed)     poisson.c:3563       -> vfs_poisson_volume_flux
+ *   VolumeFlux (immersed!=1)  poisson.c:3299       -> vfs_poisson_volume_flux0
  *   Contra2Cart               rhs.c:35             -> vfs_poisson_contra2cart
  *   levelset operator / projection poisson.c:1171, :2738 -> vfs_poisson_set_levelset
  *   PoissonSolver_Hypre       poisson_hypre.c:506  -> vfs_poisson_solve
@@ -174,6 +175,18 @@ int vfs_poisson_rhs2(vfs_poisson *h, const double *ucont, double dt, double st, 
  * a different order (their values agree to rounding). */
 int vfs_poisson_volume_flux(vfs_poisson *h, double *ucont, int flg, double flux_intp_sum, double *ibm_flux,
                             double *ibm_area);
+
+/* VolumeFlux, the overload PoissonSolver_Hypre calls when immersed is not
+ * 1 or 2 (Source/poisson.c:3299-3493, called at poisson_hypre.c:561): the
+ * faces between a fluid cell (nvert < 0.1) and a blanked one (nvert > 0.1)
+ * of ucont (DA Cmpnts, in/out) carry the net flux; the correction flux /
+ * area (area: the norms of the adjacent cell's metric) is taken off the
+ * fluid side and added to the blanked side, and for immersed 0 or 3 those
+ * faces are then zeroed (immersed 2 changes nothing).  *flux and *area (may
+ * be NULL) get the sums formed afterwards, as the reference reports them.
+ * Per-face arithmetic is the reference's; the two sums are reduced in a
+ * different order (their values agree to rounding). */
+int vfs_poisson_volume_flux0(vfs_poisson *h, double *ucont, int immersed, double *flux, double *area);
 
 /* Contra2Cart (Source/rhs.c:35-749), the change of basis: Cartesian
  * velocity ucat (DA Cmpnts, in/out) at the fluid cells from the centred

@@ -19,14 +19,18 @@ SOURCES = [os.path.join(HERE, "vfs_oracle.c"), os.path.join(HERE, "mg_solver.c")
 
 
 def build(force=False):
-    """Compile the oracle with IEEE source-order evaluation (no contraction)."""
+    """Compile the oracle with IEEE source-order evaluation (no contraction),
+    and, where the reference's sources are present, the reference's own
+    pressure-Poisson units against the PETSc/HYPRE/MPI stand-in
+    (oracle/_ref, the oracle's pin; see reference.py)."""
     os.makedirs(os.path.dirname(LIB_PATH), exist_ok=True)
     newest = max(os.path.getmtime(s) for s in SOURCES + [os.path.join(HERE, "vfs_oracle.h")])
-    if not force and os.path.exists(LIB_PATH) and os.path.getmtime(LIB_PATH) >= newest:
-        return LIB_PATH
-    cmd = ["gcc", "-O3", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared", "-o", LIB_PATH,
-           *SOURCES, "-lm"]
-    subprocess.check_call(cmd)
+    if force or not os.path.exists(LIB_PATH) or os.path.getmtime(LIB_PATH) < newest:
+        cmd = ["gcc", "-O3", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared", "-o", LIB_PATH,
+               *SOURCES, "-lm"]
+        subprocess.check_call(cmd)
+    import reference
+    reference.build(force=force)
     return LIB_PATH
 
 
@@ -84,6 +88,7 @@ def lib():
         L.or_poisson_rhs2.argtypes = [P(Dims), dp, ip, dp, dp, C.c_double, C.c_double, C.c_double, C.c_int, dp]
         L.or_set_levelset.argtypes = [dp, dp, C.c_int, C.c_int, C.c_int, C.c_int]
         L.or_volume_flux.argtypes = [P(Dims), dp, dp, dp, dp, dp, C.c_int, C.c_double, dp]
+        L.or_volume_flux0.argtypes = [P(Dims), dp, dp, dp, dp, dp, C.c_int, dp]
         L.or_contra2cart.argtypes = [P(Dims), dp, dp, dp, dp, dp, dp, C.c_int]
         L.or_remove_nullspace_scale.argtypes = [P(Dims), dp, ip, dp, dp, C.c_int]
         L.or_remove_nullspace.argtypes = [P(Dims), dp, ip, dp, C.c_int]
@@ -237,6 +242,15 @@ def volume_flux(d, nvert, met, ucont, flg=0, flux_intp_sum=0.0):
     out = np.zeros(2)
     lib().or_volume_flux(C.byref(d), _dp(np.ascontiguousarray(nvert, np.float64)), _dp(met["csi"]),
                          _dp(met["eta"]), _dp(met["zet"]), _dp(u), int(flg), float(flux_intp_sum), _dp(out))
+    return u, out[0], out[1]
+
+
+def volume_flux0(d, nvert, met, ucont, immersed=0):
+    """VolumeFlux, the overload for immersed != 1, 2; returns (ucont, flux, area)."""
+    u = np.ascontiguousarray(ucont, np.float64).copy()
+    out = np.zeros(2)
+    lib().or_volume_flux0(C.byref(d), _dp(np.ascontiguousarray(nvert, np.float64)), _dp(met["csi"]),
+                          _dp(met["eta"]), _dp(met["zet"]), _dp(u), int(immersed), _dp(out))
     return u, out[0], out[1]
 
 

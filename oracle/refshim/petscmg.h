@@ -1,0 +1,2 @@
+// Forwards to the single-rank PETSc/HYPRE/MPI stand-in.
+#include "petsc_shim.h"

@@ -50,8 +50,42 @@ static inline int remap(const or_dims *d, int i, int j, int k, int *a, int *b, i
 }
 
 /* ------------------------------------------------------------------------ */
-/* FormMetrics (Source/metrics.c:12-810, NEWMETRIC not defined for this TU). */
+/* FormMetrics (Source/metrics.c:12-1355; metrics.c:10 defines NEWMETRIC).   */
 /* ------------------------------------------------------------------------ */
+/* Cell metrics csi/eta/zet and aj = 1/J of every interior cell come from the
+ * 8-node differences (metrics.c:194-256); the boundary layer mirrors its
+ * neighbour, i planes first, then j, then k (metrics.c:262-342); periodic
+ * directions take their partner cells (metrics.c:360-397).  The face metrics
+ * are NEWMETRIC averages of the two adjacent cells: arithmetic for the
+ * vectors (AxByC, Source/momentum.c:40-45) and harmonic for aj
+ * (metrics.c:588-592, :696-700, :804-808), over i faces i = 0..mx-2 of the
+ * interior j, k; j faces j = 0..my-2; k faces k = 0..mz-2.  Faces outside
+ * those ranges stay 0, and the periodic boundary layers finally take their
+ * partners' values for every array (metrics.c:1227-1262). */
+static void avg_face(const double *a, const double *b, double *o)
+{
+  for (int c = 0; c < 3; c++) o[c] = 0.5 * a[c] + 0.5 * b[c];
+}
+
+static void periodic_copy16(const or_dims *d, or_metrics *m, int faces)
+{
+  const int mx = d->mx, my = d->my, mz = d->mz;
+  double *v3[12] = {m->csi, m->eta, m->zet, m->icsi, m->ieta, m->izet,
+                    m->jcsi, m->jeta, m->jzet, m->kcsi, m->keta, m->kzet};
+  double *v1[4] = {m->aj, m->iaj, m->jaj, m->kaj};
+  const int n3 = faces ? 12 : 3, n1 = faces ? 4 : 1;
+  for (int k = 0; k < mz; k++)
+    for (int j = 0; j < my; j++)
+      for (int i = 0; i < mx; i++) {
+        int a, b, c;
+        if (!remap(d, i, j, k, &a, &b, &c, 0, 0, 0)) continue;
+        size_t s = IX(d, a, b, c), t = IX(d, i, j, k);
+        for (int q = 0; q < n3; q++)
+          for (int e = 0; e < 3; e++) v3[q][t * 3 + e] = v3[q][s * 3 + e];
+        for (int q = 0; q < n1; q++) v1[q][t] = v1[q][s];
+      }
+}
+
 void or_form_metrics(const or_dims *d, const double *coor, or_metrics *m)
 {
   const int mx = d->mx, my = d->my, mz = d->mz;
@@ -69,7 +103,7 @@ void or_form_metrics(const or_dims *d, const double *coor, or_metrics *m)
   memset(m->kcsi, 0, n * 3 * sizeof(double)); memset(m->keta, 0, n * 3 * sizeof(double));
   memset(m->kzet, 0, n * 3 * sizeof(double)); memset(m->kaj, 0, n * sizeof(double));
 
-  /* cell centres: metrics.c:103-121 */
+  /* cell centres: metrics.c:89-108 */
   if (m->cent) {
     for (int k = 1; k < mz - 1; k++)
       for (int j = 1; j < my - 1; j++)
@@ -81,48 +115,7 @@ void or_form_metrics(const or_dims *d, const double *coor, or_metrics *m)
                          CO(i - 1, j, k - 1, c) + CO(i - 1, j - 1, k - 1, c));
   }
 
-  /* face-normal "cell" metrics, non-NEWMETRIC path: metrics.c:128-199 */
-  for (int k = 1; k < mz - 1; k++)
-    for (int j = 1; j < my - 1; j++)
-      for (int i = 0; i < mx - 1; i++) {
-        double de[3], dz[3];
-        for (int c = 0; c < 3; c++) {
-          de[c] = 0.5 * (CO(i, j, k, c) + CO(i, j, k - 1, c) - CO(i, j - 1, k, c) - CO(i, j - 1, k - 1, c));
-          dz[c] = 0.5 * (CO(i, j - 1, k, c) + CO(i, j, k, c) - CO(i, j - 1, k - 1, c) - CO(i, j, k - 1, c));
-        }
-        double *o = &m->csi[IX(d, i, j, k) * 3];
-        o[0] = de[1] * dz[2] - de[2] * dz[1];
-        o[1] = -de[0] * dz[2] + de[2] * dz[0];
-        o[2] = de[0] * dz[1] - de[1] * dz[0];
-      }
-  for (int k = 1; k < mz - 1; k++)
-    for (int j = 0; j < my - 1; j++)
-      for (int i = 1; i < mx - 1; i++) {
-        double dc[3], dz[3];
-        for (int c = 0; c < 3; c++) {
-          dc[c] = 0.5 * (CO(i, j, k, c) + CO(i, j, k - 1, c) - CO(i - 1, j, k, c) - CO(i - 1, j, k - 1, c));
-          dz[c] = 0.5 * (CO(i, j, k, c) + CO(i - 1, j, k, c) - CO(i, j, k - 1, c) - CO(i - 1, j, k - 1, c));
-        }
-        double *o = &m->eta[IX(d, i, j, k) * 3];
-        o[0] = dz[1] * dc[2] - dz[2] * dc[1];
-        o[1] = -dz[0] * dc[2] + dz[2] * dc[0];
-        o[2] = dz[0] * dc[1] - dz[1] * dc[0];
-      }
-  for (int k = 0; k < mz - 1; k++)
-    for (int j = 1; j < my - 1; j++)
-      for (int i = 1; i < mx - 1; i++) {
-        double dc[3], de[3];
-        for (int c = 0; c < 3; c++) {
-          dc[c] = 0.5 * (CO(i, j, k, c) + CO(i, j - 1, k, c) - CO(i - 1, j, k, c) - CO(i - 1, j - 1, k, c));
-          de[c] = 0.5 * (CO(i, j, k, c) + CO(i - 1, j, k, c) - CO(i, j - 1, k, c) - CO(i - 1, j - 1, k, c));
-        }
-        double *o = &m->zet[IX(d, i, j, k) * 3];
-        o[0] = dc[1] * de[2] - dc[2] * de[1];
-        o[1] = -dc[0] * de[2] + dc[2] * de[0];
-        o[2] = dc[0] * de[1] - dc[1] * de[0];
-      }
-
-  /* Jacobian aj = 1/J of interior cells: metrics.c:202-259 */
+  /* aj and the cell metrics of interior cells: metrics.c:194-256 */
   for (int k = 1; k < mz - 1; k++)
     for (int j = 1; j < my - 1; j++)
       for (int i = 1; i < mx - 1; i++) {
@@ -138,192 +131,73 @@ void or_form_metrics(const or_dims *d, const double *coor, or_metrics *m)
                           CO(i, j, k - 1, c) - CO(i, j - 1, k - 1, c) - CO(i - 1, j, k - 1, c) -
                           CO(i - 1, j - 1, k - 1, c));
         }
+        const size_t t = IX(d, i, j, k);
         double det = dc[0] * (de[1] * dz[2] - de[2] * dz[1]) - dc[1] * (de[0] * dz[2] - de[2] * dz[0]) +
                      dc[2] * (de[0] * dz[1] - de[1] * dz[0]);
-        m->aj[IX(d, i, j, k)] = 1. / det;
+        m->aj[t] = 1. / det;
+        double *cs = &m->csi[t * 3], *et = &m->eta[t * 3], *ze = &m->zet[t * 3];
+        cs[0] = de[1] * dz[2] - de[2] * dz[1];
+        cs[1] = -de[0] * dz[2] + de[2] * dz[0];
+        cs[2] = de[0] * dz[1] - de[1] * dz[0];
+        et[0] = dz[1] * dc[2] - dz[2] * dc[1];
+        et[1] = -dz[0] * dc[2] + dz[2] * dc[0];
+        et[2] = dz[0] * dc[1] - dz[1] * dc[0];
+        ze[0] = dc[1] * de[2] - dc[2] * de[1];
+        ze[1] = -dc[0] * de[2] + dc[2] * de[0];
+        ze[2] = dc[0] * de[1] - dc[1] * de[0];
       }
 
-  /* boundary mirror: metrics.c:262-342 (csi not mirrored in i, eta not in j,
-   * zet not in k without NEWMETRIC) */
-  for (int k = 0; k < mz; k++)
-    for (int j = 0; j < my; j++) {
-      size_t a0 = IX(d, 0, j, k), a1 = IX(d, 1, j, k);
-      size_t b0 = IX(d, mx - 1, j, k), b1 = IX(d, mx - 2, j, k);
-      for (int c = 0; c < 3; c++) {
-        m->eta[a0 * 3 + c] = m->eta[a1 * 3 + c]; m->zet[a0 * 3 + c] = m->zet[a1 * 3 + c];
-      }
-      m->aj[a0] = m->aj[a1];
-      for (int c = 0; c < 3; c++) {
-        m->eta[b0 * 3 + c] = m->eta[b1 * 3 + c]; m->zet[b0 * 3 + c] = m->zet[b1 * 3 + c];
-      }
-      m->aj[b0] = m->aj[b1];
-    }
-  for (int k = 0; k < mz; k++)
-    for (int i = 0; i < mx; i++) {
-      size_t a0 = IX(d, i, 0, k), a1 = IX(d, i, 1, k);
-      size_t b0 = IX(d, i, my - 1, k), b1 = IX(d, i, my - 2, k);
-      for (int c = 0; c < 3; c++) {
-        m->csi[a0 * 3 + c] = m->csi[a1 * 3 + c]; m->zet[a0 * 3 + c] = m->zet[a1 * 3 + c];
-      }
-      m->aj[a0] = m->aj[a1];
-      for (int c = 0; c < 3; c++) {
-        m->csi[b0 * 3 + c] = m->csi[b1 * 3 + c]; m->zet[b0 * 3 + c] = m->zet[b1 * 3 + c];
-      }
-      m->aj[b0] = m->aj[b1];
-    }
-  for (int j = 0; j < my; j++)
-    for (int i = 0; i < mx; i++) {
-      size_t a0 = IX(d, i, j, 0), a1 = IX(d, i, j, 1);
-      size_t b0 = IX(d, i, j, mz - 1), b1 = IX(d, i, j, mz - 2);
-      for (int c = 0; c < 3; c++) {
-        m->eta[a0 * 3 + c] = m->eta[a1 * 3 + c]; m->csi[a0 * 3 + c] = m->csi[a1 * 3 + c];
-      }
-      m->aj[a0] = m->aj[a1];
-      for (int c = 0; c < 3; c++) {
-        m->eta[b0 * 3 + c] = m->eta[b1 * 3 + c]; m->csi[b0 * 3 + c] = m->csi[b1 * 3 + c];
-      }
-      m->aj[b0] = m->aj[b1];
-    }
-  /* periodic ghost copy of cell metrics: metrics.c:360-397 */
-  for (int k = 0; k < mz; k++)
-    for (int j = 0; j < my; j++)
-      for (int i = 0; i < mx; i++) {
-        int a, b, c;
-        if (!remap(d, i, j, k, &a, &b, &c, 0, 0, 0)) continue;
-        size_t s = IX(d, a, b, c), t = IX(d, i, j, k);
-        for (int q = 0; q < 3; q++) {
-          m->csi[t * 3 + q] = m->csi[s * 3 + q];
-          m->eta[t * 3 + q] = m->eta[s * 3 + q];
-          m->zet[t * 3 + q] = m->zet[s * 3 + q];
-        }
-        m->aj[t] = m->aj[s];
-      }
-
-  /* face metrics from face-centre differences.  i faces: metrics.c:478-574 */
+  /* boundary mirror of all four cell arrays: metrics.c:262-342 */
   {
-    double *cx = (double *)calloc(n * 3, sizeof(double));
-    for (int k = 1; k < mz; k++)
-      for (int j = 1; j < my; j++)
-        for (int i = 0; i < mx; i++) {
-          if (i > mx - 2 || j > my - 2 || k > mz - 2) continue; /* nodes stop at m-2 */
-          for (int c = 0; c < 3; c++)
-            cx[IX(d, i, j, k) * 3 + c] =
-                (CO(i, j, k, c) + CO(i, j, k - 1, c) + CO(i, j - 1, k, c) + CO(i, j - 1, k - 1, c)) * 0.25;
-        }
-#define CX(i, j, k, c) cx[IX(d, i, j, k) * 3 + (c)]
-    for (int k = 1; k < mz - 1; k++)
-      for (int j = 1; j < my - 1; j++)
-        for (int i = 0; i < mx - 1; i++) {
-          double dc[3], de[3], dz[3];
-          for (int c = 0; c < 3; c++) {
-            if (i == 0) dc[c] = CX(i + 1, j, k, c) - CX(i, j, k, c);
-            else if (i == mx - 2) dc[c] = CX(i, j, k, c) - CX(i - 1, j, k, c);
-            else dc[c] = (CX(i + 1, j, k, c) - CX(i - 1, j, k, c)) * 0.5;
-            if (j == 1) de[c] = CX(i, j + 1, k, c) - CX(i, j, k, c);
-            else if (j == my - 2) de[c] = CX(i, j, k, c) - CX(i, j - 1, k, c);
-            else de[c] = (CX(i, j + 1, k, c) - CX(i, j - 1, k, c)) * 0.5;
-            if (k == 1) dz[c] = (CX(i, j, k + 1, c) - CX(i, j, k, c));
-            else if (k == mz - 2) dz[c] = (CX(i, j, k, c) - CX(i, j, k - 1, c));
-            else dz[c] = (CX(i, j, k + 1, c) - CX(i, j, k - 1, c)) * 0.5;
+    double *v3[3] = {m->csi, m->eta, m->zet};
+    for (int dir = 0; dir < 3; dir++) {
+      const int nu = dir == 0 ? my : mx, nv = dir == 2 ? my : mz;
+      for (int side = 0; side < 2; side++)
+        for (int v = 0; v < nv; v++)
+          for (int u = 0; u < nu; u++) {
+            size_t t, s;
+            if (dir == 0) { int i = side ? mx - 1 : 0; t = IX(d, i, u, v); s = IX(d, side ? i - 1 : 1, u, v); }
+            else if (dir == 1) { int j = side ? my - 1 : 0; t = IX(d, u, j, v); s = IX(d, u, side ? j - 1 : 1, v); }
+            else { int k = side ? mz - 1 : 0; t = IX(d, u, v, k); s = IX(d, u, v, side ? k - 1 : 1); }
+            for (int q = 0; q < 3; q++)
+              for (int c = 0; c < 3; c++) v3[q][t * 3 + c] = v3[q][s * 3 + c];
+            m->aj[t] = m->aj[s];
           }
-          size_t t = IX(d, i, j, k);
-          double *ci = &m->icsi[t * 3], *ei = &m->ieta[t * 3], *zi = &m->izet[t * 3];
-          ci[0] = de[1] * dz[2] - de[2] * dz[1];
-          ci[1] = -de[0] * dz[2] + de[2] * dz[0];
-          ci[2] = de[0] * dz[1] - de[1] * dz[0];
-          ei[0] = dz[1] * dc[2] - dz[2] * dc[1];
-          ei[1] = -dz[0] * dc[2] + dz[2] * dc[0];
-          ei[2] = dz[0] * dc[1] - dz[1] * dc[0];
-          zi[0] = dc[1] * de[2] - dc[2] * de[1];
-          zi[1] = -dc[0] * de[2] + dc[2] * de[0];
-          zi[2] = dc[0] * de[1] - dc[1] * de[0];
-          double det = dc[0] * (de[1] * dz[2] - de[2] * dz[1]) - dc[1] * (de[0] * dz[2] - de[2] * dz[0]) +
-                       dc[2] * (de[0] * dz[1] - de[1] * dz[0]);
-          m->iaj[t] = 1. / det;
-        }
-#undef CX
-    /* j faces: metrics.c:587-682 */
-    memset(cx, 0, n * 3 * sizeof(double));
-    for (int k = 1; k < mz - 1; k++)
-      for (int j = 0; j < my - 1; j++)
-        for (int i = 1; i < mx - 1; i++)
-          for (int c = 0; c < 3; c++)
-            cx[IX(d, i, j, k) * 3 + c] =
-                (CO(i, j, k, c) + CO(i, j, k - 1, c) + CO(i - 1, j, k, c) + CO(i - 1, j, k - 1, c)) * 0.25;
-#define CY(i, j, k, c) cx[IX(d, i, j, k) * 3 + (c)]
-    for (int k = 1; k < mz - 1; k++)
-      for (int j = 0; j < my - 1; j++)
-        for (int i = 1; i < mx - 1; i++) {
-          double dc[3], de[3], dz[3];
-          for (int c = 0; c < 3; c++) {
-            if (i == 1) dc[c] = CY(i + 1, j, k, c) - CY(i, j, k, c);
-            else if (i == mx - 2) dc[c] = CY(i, j, k, c) - CY(i - 1, j, k, c);
-            else dc[c] = (CY(i + 1, j, k, c) - CY(i - 1, j, k, c)) * 0.5;
-            if (j == 0) de[c] = CY(i, j + 1, k, c) - CY(i, j, k, c);
-            else if (j == my - 2) de[c] = CY(i, j, k, c) - CY(i, j - 1, k, c);
-            else de[c] = (CY(i, j + 1, k, c) - CY(i, j - 1, k, c)) * 0.5;
-            if (k == 1) dz[c] = (CY(i, j, k + 1, c) - CY(i, j, k, c));
-            else if (k == mz - 2) dz[c] = (CY(i, j, k, c) - CY(i, j, k - 1, c));
-            else dz[c] = (CY(i, j, k + 1, c) - CY(i, j, k - 1, c)) * 0.5;
-          }
-          size_t t = IX(d, i, j, k);
-          double *ci = &m->jcsi[t * 3], *ei = &m->jeta[t * 3], *zi = &m->jzet[t * 3];
-          ci[0] = de[1] * dz[2] - de[2] * dz[1];
-          ci[1] = -de[0] * dz[2] + de[2] * dz[0];
-          ci[2] = de[0] * dz[1] - de[1] * dz[0];
-          ei[0] = dz[1] * dc[2] - dz[2] * dc[1];
-          ei[1] = -dz[0] * dc[2] + dz[2] * dc[0];
-          ei[2] = dz[0] * dc[1] - dz[1] * dc[0];
-          zi[0] = dc[1] * de[2] - dc[2] * de[1];
-          zi[1] = -dc[0] * de[2] + dc[2] * de[0];
-          zi[2] = dc[0] * de[1] - dc[1] * de[0];
-          double det = dc[0] * (de[1] * dz[2] - de[2] * dz[1]) - dc[1] * (de[0] * dz[2] - de[2] * dz[0]) +
-                       dc[2] * (de[0] * dz[1] - de[1] * dz[0]);
-          m->jaj[t] = 1. / det;
-        }
-#undef CY
-    /* k faces: metrics.c:695-790 */
-    memset(cx, 0, n * 3 * sizeof(double));
-    for (int k = 0; k < mz - 1; k++)
-      for (int j = 1; j < my - 1; j++)
-        for (int i = 1; i < mx - 1; i++)
-          for (int c = 0; c < 3; c++)
-            cx[IX(d, i, j, k) * 3 + c] =
-                (CO(i, j, k, c) + CO(i, j - 1, k, c) + CO(i - 1, j, k, c) + CO(i - 1, j - 1, k, c)) * 0.25;
-#define CZ(i, j, k, c) cx[IX(d, i, j, k) * 3 + (c)]
-    for (int k = 0; k < mz - 1; k++)
-      for (int j = 1; j < my - 1; j++)
-        for (int i = 1; i < mx - 1; i++) {
-          double dc[3], de[3], dz[3];
-          for (int c = 0; c < 3; c++) {
-            if (i == 1) dc[c] = CZ(i + 1, j, k, c) - CZ(i, j, k, c);
-            else if (i == mx - 2) dc[c] = CZ(i, j, k, c) - CZ(i - 1, j, k, c);
-            else dc[c] = (CZ(i + 1, j, k, c) - CZ(i - 1, j, k, c)) * 0.5;
-            if (j == 1) de[c] = CZ(i, j + 1, k, c) - CZ(i, j, k, c);
-            else if (j == my - 2) de[c] = CZ(i, j, k, c) - CZ(i, j - 1, k, c);
-            else de[c] = (CZ(i, j + 1, k, c) - CZ(i, j - 1, k, c)) * 0.5;
-            if (k == 0) dz[c] = (CZ(i, j, k + 1, c) - CZ(i, j, k, c));
-            else if (k == mz - 2) dz[c] = (CZ(i, j, k, c) - CZ(i, j, k - 1, c));
-            else dz[c] = (CZ(i, j, k + 1, c) - CZ(i, j, k - 1, c)) * 0.5;
-          }
-          size_t t = IX(d, i, j, k);
-          double *ci = &m->kcsi[t * 3], *ei = &m->keta[t * 3], *zi = &m->kzet[t * 3];
-          ci[0] = de[1] * dz[2] - de[2] * dz[1];
-          ci[1] = -de[0] * dz[2] + de[2] * dz[0];
-          ci[2] = de[0] * dz[1] - de[1] * dz[0];
-          ei[0] = dz[1] * dc[2] - dz[2] * dc[1];
-          ei[1] = -dz[0] * dc[2] + dz[2] * dc[0];
-          ei[2] = dz[0] * dc[1] - dz[1] * dc[0];
-          zi[0] = dc[1] * de[2] - dc[2] * de[1];
-          zi[1] = -dc[0] * de[2] + dc[2] * de[0];
-          zi[2] = dc[0] * de[1] - dc[1] * de[0];
-          double det = dc[0] * (de[1] * dz[2] - de[2] * dz[1]) - dc[1] * (de[0] * dz[2] - de[2] * dz[0]) +
-                       dc[2] * (de[0] * dz[1] - de[1] * dz[0]);
-          m->kaj[t] = 1. / det;
-        }
-#undef CZ
-    free(cx);
+    }
   }
+  /* periodic ghost copy of the cell metrics: metrics.c:360-397 */
+  periodic_copy16(d, m, 0);
+
+  /* face metrics, NEWMETRIC averages: metrics.c:588-592, :696-700, :804-808 */
+  for (int k = 1; k < mz - 1; k++)
+    for (int j = 1; j < my - 1; j++)
+      for (int i = 0; i < mx - 1; i++) {
+        const size_t t = IX(d, i, j, k), u = IX(d, i + 1, j, k);
+        avg_face(&m->csi[t * 3], &m->csi[u * 3], &m->icsi[t * 3]);
+        avg_face(&m->eta[t * 3], &m->eta[u * 3], &m->ieta[t * 3]);
+        avg_face(&m->zet[t * 3], &m->zet[u * 3], &m->izet[t * 3]);
+        m->iaj[t] = 2. / (1. / m->aj[t] + 1. / m->aj[u]);
+      }
+  for (int k = 1; k < mz - 1; k++)
+    for (int j = 0; j < my - 1; j++)
+      for (int i = 1; i < mx - 1; i++) {
+        const size_t t = IX(d, i, j, k), u = IX(d, i, j + 1, k);
+        avg_face(&m->csi[t * 3], &m->csi[u * 3], &m->jcsi[t * 3]);
+        avg_face(&m->eta[t * 3], &m->eta[u * 3], &m->jeta[t * 3]);
+        avg_face(&m->zet[t * 3], &m->zet[u * 3], &m->jzet[t * 3]);
+        m->jaj[t] = 2. / (1. / m->aj[t] + 1. / m->aj[u]);
+      }
+  for (int k = 0; k < mz - 1; k++)
+    for (int j = 1; j < my - 1; j++)
+      for (int i = 1; i < mx - 1; i++) {
+        const size_t t = IX(d, i, j, k), u = IX(d, i, j, k + 1);
+        avg_face(&m->csi[t * 3], &m->csi[u * 3], &m->kcsi[t * 3]);
+        avg_face(&m->eta[t * 3], &m->eta[u * 3], &m->keta[t * 3]);
+        avg_face(&m->zet[t * 3], &m->zet[u * 3], &m->kzet[t * 3]);
+        m->kaj[t] = 2. / (1. / m->aj[t] + 1. / m->aj[u]);
+      }
+  /* periodic boundary layers of every array: metrics.c:1227-1262 */
+  periodic_copy16(d, m, 1);
 #undef CO
 }
 
@@ -1214,6 +1088,60 @@ void or_volume_flux(const or_dims *d, const double *nvert, const double *csi, co
                 }
               } else {
                 flux += s == 0 ? *u : -*u;
+                area += a;
+              }
+            }
+          }
+        }
+  }
+  out[0] = flux;
+  out[1] = area;
+}
+
+/* VolumeFlux, the overload PoissonSolver_Hypre calls when immersed is not 1
+ * or 2 (Source/poisson.c:3299-3493, called at poisson_hypre.c:561 with the
+ * global Ucont): over the interior cells in k, j, i order, the faces between
+ * a fluid cell (nvert < 0.1) and a blanked one (nvert > 0.1), in either
+ * order, add +-U to the flux and |csi|, |eta| or |zet| of the cell (the
+ * cell metric) to the area; the correction flux / area (0 if the area is at
+ * most 1e-15) is taken off the fluid side and added to the blanked side,
+ * and with immersed 0 or 3 those faces are then zeroed; immersed 2 applies
+ * nothing.  out[0..1]: the sums formed again afterwards. */
+void or_volume_flux0(const or_dims *d, const double *nvert, const double *csi, const double *eta,
+                     const double *zet, double *ucont, int immersed, double *out)
+{
+  const int mx = d->mx, my = d->my, mz = d->mz;
+  const double thr = 0.1;
+  const double *met[3] = {csi, eta, zet};
+  double flux = 0, area = 0;
+  for (int pass = 0; pass < 3; pass++) {
+    double corr = 0;
+    if (pass == 1) {
+      if (area > 1.e-15) corr = flux / area;
+      if (immersed == 2) continue;
+    }
+    if (pass == 2) { flux = 0; area = 0; }
+    for (int k = 1; k < mz - 1; k++)
+      for (int j = 1; j < my - 1; j++)
+        for (int i = 1; i < mx - 1; i++) {
+          const size_t t = IX(d, i, j, k);
+          const size_t nb[3] = {IX(d, i + 1, j, k), IX(d, i, j + 1, k), IX(d, i, j, k + 1)};
+          for (int s = 0; s < 2; s++) {  /* s 0: fluid cell, s 1: blanked cell */
+            if (s == 0 && !(nvert[t] < thr)) continue;
+            if (s == 1 && !(nvert[t] > thr)) continue;
+            for (int q = 0; q < 3; q++) {
+              const double nn = nvert[nb[q]];
+              if (s == 0 ? !(nn > thr) : !(nn < thr)) continue;
+              double *u = &ucont[t * 3 + q];
+              const double *m = &met[q][t * 3];
+              const double a = sqrt(m[0] * m[0] + m[1] * m[1] + m[2] * m[2]);
+              if (pass == 1) {
+                if (s == 0) *u -= a * corr;
+                else *u += a * corr;
+                if (immersed == 3 || !immersed) *u = 0;
+              } else {
+                if (s == 0) flux += *u;
+                else flux -= *u;
                 area += a;
               }
             }

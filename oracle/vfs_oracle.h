@@ -62,6 +62,8 @@ int or_poisson_lhs(const or_dims *d, const double *nvert, const or_metrics *m,
 void or_set_levelset(const double *rho, const double *level, int on, int bc3, int bc4, int bc5);
 void or_volume_flux(const or_dims *d, const double *nvert, const double *csi, const double *eta, const double *zet,
                     double *ucont, int flg, double flux_intp_sum, double *out);
+void or_volume_flux0(const or_dims *d, const double *nvert, const double *csi, const double *eta,
+                     const double *zet, double *ucont, int immersed, double *out);
 void or_contra2cart(const or_dims *d, const double *nvert, const double *csi, const double *eta, const double *zet,
                     const double *ucont, double *ucat, int zero_solid);
 void or_poisson_rhs2(const or_dims *d, const double *nvert, const int *gid, const double *ucont,

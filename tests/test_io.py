@@ -8,7 +8,17 @@ import os
 import numpy as np
 import pytest
 
-REF_CASES = "/root/reference/Instructional_Cases"
+
+
+def _reference_cases():
+    """Instructional_Cases of the reference tree: VFS_REFERENCE_DIR, else the
+    tree the reference pin was built from (oracle/_ref), else none."""
+    import reference
+    root = os.environ.get("VFS_REFERENCE_DIR") or reference.reference_dir()
+    return os.path.join(root, "Instructional_Cases") if root else ""
+
+
+REF_CASES = _reference_cases()
 
 
 @pytest.fixture(scope="module")

@@ -1,18 +1,19 @@
-"""CPU checks of the oracle (no GPU): the restated operator's structural
-properties, the right-hand side's consistency, the CPU baseline solver
-against an exact sparse solve, the transfer operators' algebra, and the
-committed golden fixtures.  The reference itself cannot be run here (it
-needs PETSc/HYPRE/MPI), so these pin the restatement against mathematics
-and against its own earlier outputs, not against the reference."""
+"""CPU checks of the oracle (no GPU): every stage of the restatement against
+the golden fixtures that the reference's own functions produced
+(tests/golden/, written by tests/golden/make_golden.py from the reference's
+sources compiled against a single-rank PETSc/HYPRE/MPI stand-in), plus the
+restated operator's structural properties, the right-hand side's
+consistency, the CPU baseline solver against an exact sparse solve and the
+transfer operators' algebra."""
 import os
 
 import numpy as np
 import pytest
 
+import golden_io
 import oracle as O
 from vfs_poisson import configs as CF
 
-GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
 
 
 @pytest.fixture(scope="module", params=["channel", "cylinder", "towers"])
@@ -119,21 +120,15 @@ def test_restriction_interpolation_weights():
     np.testing.assert_allclose(f[1:-1, 1:-1, 1:-1], 1.0)
 
 
-@pytest.mark.parametrize("name", ["channel_8", "cylinder_12"])
+@pytest.mark.parametrize("name", golden_io.names())
 def test_golden_fixtures(name):
-    path = os.path.join(GOLDEN, f"{name}.npz")
-    if not os.path.exists(path):
-        pytest.skip("fixture not generated")
-    g = np.load(path)
-    case = CF.channel(8, 8, 8) if name.startswith("channel") else CF.cylinder(12, 8, 12)
-    np.testing.assert_array_equal(g["coor"], case.coor)
-    d = O.dims_of(case)
-    met = O.form_metrics(d, case.coor)
-    lhs = O.poisson_lhs(d, case.nvert, met)
-    np.testing.assert_array_equal(lhs["vol"], g["vol"])
-    b = O.rhs(d, case.nvert, lhs["gid"], case.ucont, met["aj"])
-    np.testing.assert_allclose(b, g["b"], rtol=0, atol=1e-13 * np.abs(g["b"]).max())
-    np.testing.assert_array_equal(met["iaj"], g["iaj"])
+    """The oracle reproduces the reference's outputs bit for bit: FormMetrics,
+    the dof numbering, the assembled operator, PoissonRHS2 (-poisson 0 and
+    -1), the right-hand side PoissonSolver_Hypre hands to HYPRE,
+    Remove_Nullspace + Convert_Phi2_Phi of the same inner solution,
+    UpdatePressure, Projection, Divergence and both VolumeFlux variants."""
+    case, g = golden_io.load(name)
+    golden_io.check_oracle(case, g)
 
 
 # --- immersed-boundary classification (ibm_search_advanced) ---

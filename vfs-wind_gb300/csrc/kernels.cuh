@@ -20,8 +20,8 @@ struct MetricPtrs {
 // setup.cu (compiled without FMA contraction)
 __global__ void k_metrics_cell(Grid g, const double *coor, MetricPtrs m);
 __global__ void k_metrics_mirror(Grid g, MetricPtrs m, int dir);
-__global__ void k_metrics_periodic(Grid g, MetricPtrs m);
-__global__ void k_metrics_face(Grid g, const double *coor, MetricPtrs m, int dir);
+__global__ void k_metrics_periodic(Grid g, MetricPtrs m, int faces);
+__global__ void k_metrics_face(Grid g, MetricPtrs m, int dir);
 __global__ void k_count_dofs(Grid g, Box b, const double *nvert, int *block_count);
 __global__ void k_scan_blocks(int *block_count, int nblocks, int *total);
 __global__ void k_number_dofs(Grid g, Box b, const double *nvert, const int *block_off, int *gid_box);
@@ -33,6 +33,8 @@ __global__ void k_rhs2_shift(Grid g, Box b, const double *nvert, const double *a
 __global__ void k_vflux_sum(Grid g, const double *nvert, MetricPtrs m, double *ucont, int flg, int pass,
                             double *partial);
 __global__ void k_vflux_apply(Grid g, const double *nvert, MetricPtrs m, double *ucont, int flg, double corr);
+__global__ void k_vflux0_sum(Grid g, const double *nvert, MetricPtrs m, double *ucont, double *partial);
+__global__ void k_vflux0_apply(Grid g, const double *nvert, MetricPtrs m, double *ucont, double corr, int zero);
 __global__ void k_periodic_cmpnts(Grid g, const double *src, double *dst);
 __global__ void k_contra2cart(Grid g, const double *nvert, MetricPtrs m, const double *lu, double *ucat);
 __global__ void k_zero_solid(Grid g, const double *nvert, double *ucat);

@@ -609,8 +609,9 @@ int form_metrics(vfs_poisson *h, const Grid &g, const double *coor, MetricPtrs &
   LAUNCH(h, k_metrics_mirror, dim3((g.my + 127) / 128, g.mz), 128, g, m, 0);
   LAUNCH(h, k_metrics_mirror, dim3((g.mx + 127) / 128, g.mz), 128, g, m, 1);
   LAUNCH(h, k_metrics_mirror, dim3((g.mx + 127) / 128, g.my), 128, g, m, 2);
-  LAUNCH(h, k_metrics_periodic, da_grid(g), 128, g, m);
-  for (int d = 0; d < 3; d++) LAUNCH(h, k_metrics_face, da_grid(g), 128, g, coor, m, d);
+  LAUNCH(h, k_metrics_periodic, da_grid(g), 128, g, m, 0);
+  for (int d = 0; d < 3; d++) LAUNCH(h, k_metrics_face, da_grid(g), 128, g, m, d);
+  LAUNCH(h, k_metrics_periodic, da_grid(g), 128, g, m, 1);
   return VFS_OK;
 }
 
@@ -1728,6 +1729,28 @@ int vfs_poisson_volume_flux(vfs_poisson *h, double *ucont, int flg, double flux_
   TRY(reduce_read(h, kRedBlocks, 3, sums));
   if (ibm_flux) *ibm_flux = sums[0];
   if (ibm_area) *ibm_area = sums[2];
+  TRY(download(h, ucont, h->ucont, 3 * N));
+  return sync(h);
+}
+
+int vfs_poisson_volume_flux0(vfs_poisson *h, double *ucont, int immersed, double *flux, double *area) {
+  if (!h || !ucont) return fail(VFS_EINVAL, "null argument");
+  if (!h->have_nvert) return fail(VFS_ESTATE, "set_nvert must come before volume_flux0");
+  if (immersed == 1) return fail(VFS_EINVAL, "immersed 1 takes the other VolumeFlux (vfs_poisson_volume_flux)");
+  const size_t N = h->g.n();
+  TRY(upload(h, h->ucont, ucont, 3 * N));
+  double sums[2];
+  LAUNCH(h, k_vflux0_sum, kRedBlocks, 256, h->g, h->nvert, h->met, h->ucont, h->partial);
+  TRY(reduce_read(h, kRedBlocks, 2, sums));
+  if (immersed != 2) {
+    const double corr = sums[1] > 1.e-15 ? sums[0] / sums[1] : 0.;
+    LAUNCH(h, k_vflux0_apply, kRedBlocks, 256, h->g, h->nvert, h->met, h->ucont, corr,
+           (immersed == 0 || immersed == 3) ? 1 : 0);
+  }
+  LAUNCH(h, k_vflux0_sum, kRedBlocks, 256, h->g, h->nvert, h->met, h->ucont, h->partial);
+  TRY(reduce_read(h, kRedBlocks, 2, sums));
+  if (flux) *flux = sums[0];
+  if (area) *area = sums[1];
   TRY(download(h, ucont, h->ucont, 3 * N));
   return sync(h);
 }

@@ -14,74 +14,48 @@ namespace vfs {
 static constexpr double kThr = 0.1;  // poisson_threshold, Source/main.c:124
 
 // --------------------------------------------------------------------------
-// FormMetrics (Source/metrics.c:12-810; NEWMETRIC is not defined there)
+// FormMetrics (Source/metrics.c:12-1355; metrics.c:10 defines NEWMETRIC)
 // --------------------------------------------------------------------------
 #define CO(i, j, k, c) coor[g.at(i, j, k) * 3 + (c)]
 
-// cell centres and aj (metrics.c:103-121, :202-259) and the face-normal
-// "cell" metrics csi/eta/zet of the non-NEWMETRIC path (metrics.c:128-199).
+// cell centres (metrics.c:89-108) and, for every interior cell, aj = 1/J and
+// the cell metrics csi/eta/zet from the 8-node differences
+// (metrics.c:194-256, the NEWMETRIC branch)
 __global__ void k_metrics_cell(Grid g, const double *__restrict__ coor, MetricPtrs m) {
   int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y, k = blockIdx.z;
   if (i >= g.mx) return;
   size_t t = g.at(i, j, k);
   const int mx = g.mx, my = g.my, mz = g.mz;
-  if (i >= 1 && i < mx - 1 && j >= 1 && j < my - 1 && k >= 1 && k < mz - 1) {
-    for (int c = 0; c < 3; c++)
-      m.cent[t * 3 + c] = 0.125 * (CO(i, j, k, c) + CO(i, j - 1, k, c) + CO(i, j, k - 1, c) +
-                                   CO(i, j - 1, k - 1, c) + CO(i - 1, j, k, c) + CO(i - 1, j - 1, k, c) +
-                                   CO(i - 1, j, k - 1, c) + CO(i - 1, j - 1, k - 1, c));
-    double dc[3], de[3], dz[3];
-    for (int c = 0; c < 3; c++) {
-      dc[c] = 0.25 * (CO(i, j, k, c) + CO(i, j - 1, k, c) + CO(i, j, k - 1, c) + CO(i, j - 1, k - 1, c) -
-                      CO(i - 1, j, k, c) - CO(i - 1, j - 1, k, c) - CO(i - 1, j, k - 1, c) -
-                      CO(i - 1, j - 1, k - 1, c));
-      de[c] = 0.25 * (CO(i, j, k, c) + CO(i - 1, j, k, c) + CO(i, j, k - 1, c) + CO(i - 1, j, k - 1, c) -
-                      CO(i, j - 1, k, c) - CO(i - 1, j - 1, k, c) - CO(i, j - 1, k - 1, c) -
-                      CO(i - 1, j - 1, k - 1, c));
-      dz[c] = 0.25 * (CO(i, j, k, c) + CO(i, j - 1, k, c) + CO(i - 1, j, k, c) + CO(i - 1, j - 1, k, c) -
-                      CO(i, j, k - 1, c) - CO(i, j - 1, k - 1, c) - CO(i - 1, j, k - 1, c) -
-                      CO(i - 1, j - 1, k - 1, c));
-    }
-    double det = dc[0] * (de[1] * dz[2] - de[2] * dz[1]) - dc[1] * (de[0] * dz[2] - de[2] * dz[0]) +
-                 dc[2] * (de[0] * dz[1] - de[1] * dz[0]);
-    m.aj[t] = 1. / det;
+  if (!(i >= 1 && i < mx - 1 && j >= 1 && j < my - 1 && k >= 1 && k < mz - 1)) return;
+  for (int c = 0; c < 3; c++)
+    m.cent[t * 3 + c] = 0.125 * (CO(i, j, k, c) + CO(i, j - 1, k, c) + CO(i, j, k - 1, c) + CO(i, j - 1, k - 1, c) +
+                                 CO(i - 1, j, k, c) + CO(i - 1, j - 1, k, c) + CO(i - 1, j, k - 1, c) +
+                                 CO(i - 1, j - 1, k - 1, c));
+  double dc[3], de[3], dz[3];
+  for (int c = 0; c < 3; c++) {
+    dc[c] = 0.25 * (CO(i, j, k, c) + CO(i, j - 1, k, c) + CO(i, j, k - 1, c) + CO(i, j - 1, k - 1, c) -
+                    CO(i - 1, j, k, c) - CO(i - 1, j - 1, k, c) - CO(i - 1, j, k - 1, c) - CO(i - 1, j - 1, k - 1, c));
+    de[c] = 0.25 * (CO(i, j, k, c) + CO(i - 1, j, k, c) + CO(i, j, k - 1, c) + CO(i - 1, j, k - 1, c) -
+                    CO(i, j - 1, k, c) - CO(i - 1, j - 1, k, c) - CO(i, j - 1, k - 1, c) - CO(i - 1, j - 1, k - 1, c));
+    dz[c] = 0.25 * (CO(i, j, k, c) + CO(i, j - 1, k, c) + CO(i - 1, j, k, c) + CO(i - 1, j - 1, k, c) -
+                    CO(i, j, k - 1, c) - CO(i, j - 1, k - 1, c) - CO(i - 1, j, k - 1, c) - CO(i - 1, j - 1, k - 1, c));
   }
-  if (k >= 1 && k < mz - 1 && j >= 1 && j < my - 1 && i < mx - 1) {
-    double de[3], dz[3];
-    for (int c = 0; c < 3; c++) {
-      de[c] = 0.5 * (CO(i, j, k, c) + CO(i, j, k - 1, c) - CO(i, j - 1, k, c) - CO(i, j - 1, k - 1, c));
-      dz[c] = 0.5 * (CO(i, j - 1, k, c) + CO(i, j, k, c) - CO(i, j - 1, k - 1, c) - CO(i, j, k - 1, c));
-    }
-    double *o = &m.csi[t * 3];
-    o[0] = de[1] * dz[2] - de[2] * dz[1];
-    o[1] = -de[0] * dz[2] + de[2] * dz[0];
-    o[2] = de[0] * dz[1] - de[1] * dz[0];
-  }
-  if (k >= 1 && k < mz - 1 && j < my - 1 && i >= 1 && i < mx - 1) {
-    double dc[3], dz[3];
-    for (int c = 0; c < 3; c++) {
-      dc[c] = 0.5 * (CO(i, j, k, c) + CO(i, j, k - 1, c) - CO(i - 1, j, k, c) - CO(i - 1, j, k - 1, c));
-      dz[c] = 0.5 * (CO(i, j, k, c) + CO(i - 1, j, k, c) - CO(i, j, k - 1, c) - CO(i - 1, j, k - 1, c));
-    }
-    double *o = &m.eta[t * 3];
-    o[0] = dz[1] * dc[2] - dz[2] * dc[1];
-    o[1] = -dz[0] * dc[2] + dz[2] * dc[0];
-    o[2] = dz[0] * dc[1] - dz[1] * dc[0];
-  }
-  if (k < mz - 1 && j >= 1 && j < my - 1 && i >= 1 && i < mx - 1) {
-    double dc[3], de[3];
-    for (int c = 0; c < 3; c++) {
-      dc[c] = 0.5 * (CO(i, j, k, c) + CO(i, j - 1, k, c) - CO(i - 1, j, k, c) - CO(i - 1, j - 1, k, c));
-      de[c] = 0.5 * (CO(i, j, k, c) + CO(i - 1, j, k, c) - CO(i, j - 1, k, c) - CO(i - 1, j - 1, k, c));
-    }
-    double *o = &m.zet[t * 3];
-    o[0] = dc[1] * de[2] - dc[2] * de[1];
-    o[1] = -dc[0] * de[2] + dc[2] * de[0];
-    o[2] = dc[0] * de[1] - dc[1] * de[0];
-  }
+  double det = dc[0] * (de[1] * dz[2] - de[2] * dz[1]) - dc[1] * (de[0] * dz[2] - de[2] * dz[0]) +
+               dc[2] * (de[0] * dz[1] - de[1] * dz[0]);
+  m.aj[t] = 1. / det;
+  double *cs = &m.csi[t * 3], *et = &m.eta[t * 3], *ze = &m.zet[t * 3];
+  cs[0] = de[1] * dz[2] - de[2] * dz[1];
+  cs[1] = -de[0] * dz[2] + de[2] * dz[0];
+  cs[2] = de[0] * dz[1] - de[1] * dz[0];
+  et[0] = dz[1] * dc[2] - dz[2] * dc[1];
+  et[1] = -dz[0] * dc[2] + dz[2] * dc[0];
+  et[2] = dz[0] * dc[1] - dz[1] * dc[0];
+  ze[0] = dc[1] * de[2] - dc[2] * de[1];
+  ze[1] = -dc[0] * de[2] + dc[2] * de[0];
+  ze[2] = dc[0] * de[1] - dc[1] * de[0];
 }
 
-// boundary mirror of the cell metrics, one direction per launch, in the
+// boundary mirror of csi, eta, zet and aj, one direction per launch, in the
 // order x, y, z of metrics.c:262-342.
 __global__ void k_metrics_mirror(Grid g, MetricPtrs m, int dir) {
   int u = blockIdx.x * blockDim.x + threadIdx.x, v = blockIdx.y;
@@ -92,102 +66,57 @@ __global__ void k_metrics_mirror(Grid g, MetricPtrs m, int dir) {
     if (dir == 0) { int i = side ? g.mx - 1 : 0; t = g.at(i, u, v); s = g.at(side ? i - 1 : 1, u, v); }
     else if (dir == 1) { int j = side ? g.my - 1 : 0; t = g.at(u, j, v); s = g.at(u, side ? j - 1 : 1, v); }
     else { int k = side ? g.mz - 1 : 0; t = g.at(u, v, k); s = g.at(u, v, side ? k - 1 : 1); }
-    double *A = dir == 0 ? m.eta : m.csi;
-    double *B = dir == 2 ? m.eta : m.zet;
-    for (int c = 0; c < 3; c++) { A[t * 3 + c] = A[s * 3 + c]; B[t * 3 + c] = B[s * 3 + c]; }
+    for (int c = 0; c < 3; c++) {
+      m.csi[t * 3 + c] = m.csi[s * 3 + c];
+      m.eta[t * 3 + c] = m.eta[s * 3 + c];
+      m.zet[t * 3 + c] = m.zet[s * 3 + c];
+    }
     m.aj[t] = m.aj[s];
   }
 }
 
-// periodic ghost copy of the cell metrics (metrics.c:360-397).  A source
-// cell has every periodic coordinate inside 1..m-2, so it is never a target.
-__global__ void k_metrics_periodic(Grid g, MetricPtrs m) {
+// periodic ghost copy: of the cell metrics before the face averages
+// (metrics.c:360-397), of all sixteen arrays at the end (metrics.c:1227-1262).
+// A source cell has every periodic coordinate inside 1..m-2, so it is never
+// a target.
+__global__ void k_metrics_periodic(Grid g, MetricPtrs m, int faces) {
   int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y, k = blockIdx.z;
   if (i >= g.mx) return;
   int a, b, c, fi, fj, fk;
   if (!g.remap(i, j, k, a, b, c, fi, fj, fk)) return;
   size_t s = g.at(a, b, c), t = g.at(i, j, k);
-  for (int q = 0; q < 3; q++) {
-    m.csi[t * 3 + q] = m.csi[s * 3 + q];
-    m.eta[t * 3 + q] = m.eta[s * 3 + q];
-    m.zet[t * 3 + q] = m.zet[s * 3 + q];
-  }
-  m.aj[t] = m.aj[s];
+  double *v3[12] = {m.csi, m.eta, m.zet, m.icsi, m.ieta, m.izet, m.jcsi, m.jeta, m.jzet, m.kcsi, m.keta, m.kzet};
+  double *v1[4] = {m.aj, m.iaj, m.jaj, m.kaj};
+  const int n3 = faces ? 12 : 3, n1 = faces ? 4 : 1;
+  for (int q = 0; q < n3; q++)
+    for (int e = 0; e < 3; e++) v3[q][t * 3 + e] = v3[q][s * 3 + e];
+  for (int q = 0; q < n1; q++) v1[q][t] = v1[q][s];
 }
 
-__device__ inline void face_metric_out(const double dc[3], const double de[3], const double dz[3],
-                                       double *ci, double *ei, double *zi, double *aj) {
-  ci[0] = de[1] * dz[2] - de[2] * dz[1];
-  ci[1] = -de[0] * dz[2] + de[2] * dz[0];
-  ci[2] = de[0] * dz[1] - de[1] * dz[0];
-  ei[0] = dz[1] * dc[2] - dz[2] * dc[1];
-  ei[1] = -dz[0] * dc[2] + dz[2] * dc[0];
-  ei[2] = dz[0] * dc[1] - dz[1] * dc[0];
-  zi[0] = dc[1] * de[2] - dc[2] * de[1];
-  zi[1] = -dc[0] * de[2] + dc[2] * de[0];
-  zi[2] = dc[0] * de[1] - dc[1] * de[0];
-  double det = dc[0] * (de[1] * dz[2] - de[2] * dz[1]) - dc[1] * (de[0] * dz[2] - de[2] * dz[0]) +
-               dc[2] * (de[0] * dz[1] - de[1] * dz[0]);
-  *aj = 1. / det;
-}
-
-// face metrics of the i, j and k faces from face-centre differences
-// (metrics.c:478-574, :587-682, :695-790); the face centres are evaluated
-// on the fly in the reference's summation order.
-__global__ void k_metrics_face(Grid g, const double *__restrict__ coor, MetricPtrs m, int dir) {
+// NEWMETRIC face metrics (metrics.c:588-592, :696-700, :804-808): the
+// arithmetic mean of the two adjacent cells' csi/eta/zet (AxByC,
+// Source/momentum.c:40-45) and the harmonic mean of their aj; i faces
+// i = 0..mx-2 of the interior j, k; j faces j = 0..my-2; k faces k = 0..mz-2.
+__global__ void k_metrics_face(Grid g, MetricPtrs m, int dir) {
   int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y, k = blockIdx.z;
   const int mx = g.mx, my = g.my, mz = g.mz;
-  double dc[3], de[3], dz[3];
-  size_t t = g.at(i, j, k);
-  if (dir == 0) {
-    if (!(i < mx - 1 && j >= 1 && j < my - 1 && k >= 1 && k < mz - 1)) return;
-#define CX(i, j, k, c) ((CO(i, j, k, c) + CO(i, j, k - 1, c) + CO(i, j - 1, k, c) + CO(i, j - 1, k - 1, c)) * 0.25)
-    for (int c = 0; c < 3; c++) {
-      if (i == 0) dc[c] = CX(i + 1, j, k, c) - CX(i, j, k, c);
-      else if (i == mx - 2) dc[c] = CX(i, j, k, c) - CX(i - 1, j, k, c);
-      else dc[c] = (CX(i + 1, j, k, c) - CX(i - 1, j, k, c)) * 0.5;
-      if (j == 1) de[c] = CX(i, j + 1, k, c) - CX(i, j, k, c);
-      else if (j == my - 2) de[c] = CX(i, j, k, c) - CX(i, j - 1, k, c);
-      else de[c] = (CX(i, j + 1, k, c) - CX(i, j - 1, k, c)) * 0.5;
-      if (k == 1) dz[c] = (CX(i, j, k + 1, c) - CX(i, j, k, c));
-      else if (k == mz - 2) dz[c] = (CX(i, j, k, c) - CX(i, j, k - 1, c));
-      else dz[c] = (CX(i, j, k + 1, c) - CX(i, j, k - 1, c)) * 0.5;
-    }
-#undef CX
-    face_metric_out(dc, de, dz, &m.icsi[t * 3], &m.ieta[t * 3], &m.izet[t * 3], &m.iaj[t]);
-  } else if (dir == 1) {
-    if (!(i >= 1 && i < mx - 1 && j < my - 1 && k >= 1 && k < mz - 1)) return;
-#define CY(i, j, k, c) ((CO(i, j, k, c) + CO(i, j, k - 1, c) + CO(i - 1, j, k, c) + CO(i - 1, j, k - 1, c)) * 0.25)
-    for (int c = 0; c < 3; c++) {
-      if (i == 1) dc[c] = CY(i + 1, j, k, c) - CY(i, j, k, c);
-      else if (i == mx - 2) dc[c] = CY(i, j, k, c) - CY(i - 1, j, k, c);
-      else dc[c] = (CY(i + 1, j, k, c) - CY(i - 1, j, k, c)) * 0.5;
-      if (j == 0) de[c] = CY(i, j + 1, k, c) - CY(i, j, k, c);
-      else if (j == my - 2) de[c] = CY(i, j, k, c) - CY(i, j - 1, k, c);
-      else de[c] = (CY(i, j + 1, k, c) - CY(i, j - 1, k, c)) * 0.5;
-      if (k == 1) dz[c] = (CY(i, j, k + 1, c) - CY(i, j, k, c));
-      else if (k == mz - 2) dz[c] = (CY(i, j, k, c) - CY(i, j, k - 1, c));
-      else dz[c] = (CY(i, j, k + 1, c) - CY(i, j, k - 1, c)) * 0.5;
-    }
-#undef CY
-    face_metric_out(dc, de, dz, &m.jcsi[t * 3], &m.jeta[t * 3], &m.jzet[t * 3], &m.jaj[t]);
-  } else {
-    if (!(i >= 1 && i < mx - 1 && j >= 1 && j < my - 1 && k < mz - 1)) return;
-#define CZ(i, j, k, c) ((CO(i, j, k, c) + CO(i, j - 1, k, c) + CO(i - 1, j, k, c) + CO(i - 1, j - 1, k, c)) * 0.25)
-    for (int c = 0; c < 3; c++) {
-      if (i == 1) dc[c] = CZ(i + 1, j, k, c) - CZ(i, j, k, c);
-      else if (i == mx - 2) dc[c] = CZ(i, j, k, c) - CZ(i - 1, j, k, c);
-      else dc[c] = (CZ(i + 1, j, k, c) - CZ(i - 1, j, k, c)) * 0.5;
-      if (j == 1) de[c] = CZ(i, j + 1, k, c) - CZ(i, j, k, c);
-      else if (j == my - 2) de[c] = CZ(i, j, k, c) - CZ(i, j - 1, k, c);
-      else de[c] = (CZ(i, j + 1, k, c) - CZ(i, j - 1, k, c)) * 0.5;
-      if (k == 0) dz[c] = (CZ(i, j, k + 1, c) - CZ(i, j, k, c));
-      else if (k == mz - 2) dz[c] = (CZ(i, j, k, c) - CZ(i, j, k - 1, c));
-      else dz[c] = (CZ(i, j, k + 1, c) - CZ(i, j, k - 1, c)) * 0.5;
-    }
-#undef CZ
-    face_metric_out(dc, de, dz, &m.kcsi[t * 3], &m.keta[t * 3], &m.kzet[t * 3], &m.kaj[t]);
+  bool in;
+  if (dir == 0) in = i < mx - 1 && j >= 1 && j < my - 1 && k >= 1 && k < mz - 1;
+  else if (dir == 1) in = i >= 1 && i < mx - 1 && j < my - 1 && k >= 1 && k < mz - 1;
+  else in = i >= 1 && i < mx - 1 && j >= 1 && j < my - 1 && k < mz - 1;
+  if (!in) return;
+  const size_t t = g.at(i, j, k);
+  const size_t u = dir == 0 ? g.at(i + 1, j, k) : dir == 1 ? g.at(i, j + 1, k) : g.at(i, j, k + 1);
+  double *fc = dir == 0 ? m.icsi : dir == 1 ? m.jcsi : m.kcsi;
+  double *fe = dir == 0 ? m.ieta : dir == 1 ? m.jeta : m.keta;
+  double *fz = dir == 0 ? m.izet : dir == 1 ? m.jzet : m.kzet;
+  double *fa = dir == 0 ? m.iaj : dir == 1 ? m.jaj : m.kaj;
+  for (int c = 0; c < 3; c++) {
+    fc[t * 3 + c] = 0.5 * m.csi[t * 3 + c] + 0.5 * m.csi[u * 3 + c];
+    fe[t * 3 + c] = 0.5 * m.eta[t * 3 + c] + 0.5 * m.eta[u * 3 + c];
+    fz[t * 3 + c] = 0.5 * m.zet[t * 3 + c] + 0.5 * m.zet[u * 3 + c];
   }
+  fa[t] = 2. / (1. / m.aj[t] + 1. / m.aj[u]);
 }
 #undef CO
 
@@ -1143,6 +1072,71 @@ __global__ void k_vflux_apply(Grid g, const double *__restrict__ nvert, MetricPt
       else if (flg == 2) dlt = corr * fabs(u);
       else dlt = f[q].a * corr;
       *f[q].u = f[q].s == 0 ? u - dlt : u + dlt;
+    }
+  }
+}
+
+// ---- VolumeFlux, the overload for immersed != 1, 2 (Source/poisson.c:3299-3493) ----
+// Faces between a fluid cell (nvert < 0.1) and a blanked one (nvert > 0.1),
+// visited from the cell below them; the area term is the cell metric's norm.
+__device__ inline int vflux0_faces(Grid g, const double *nvert, MetricPtrs m, double *ucont, int i, int j, int k,
+                                   VfluxFace f[6]) {
+  const size_t t = g.at(i, j, k);
+  const size_t nb[3] = {g.at(i + 1, j, k), g.at(i, j + 1, k), g.at(i, j, k + 1)};
+  const double *met[3] = {m.csi, m.eta, m.zet};
+  int nf = 0;
+  for (int s = 0; s < 2; s++) {
+    if (s == 0 && !(nvert[t] < 0.1)) continue;
+    if (s == 1 && !(nvert[t] > 0.1)) continue;
+    for (int q = 0; q < 3; q++) {
+      const double nn = nvert[nb[q]];
+      if (s == 0 ? !(nn > 0.1) : !(nn < 0.1)) continue;
+      const double *mm = &met[q][t * 3];
+      f[nf].u = &ucont[t * 3 + q];
+      f[nf].a = sqrt(mm[0] * mm[0] + mm[1] * mm[1] + mm[2] * mm[2]);
+      f[nf].s = s;
+      nf++;
+    }
+  }
+  return nf;
+}
+
+// block partials of the flux (+U on the fluid side, -U on the blanked side)
+// and of the area
+__global__ void k_vflux0_sum(Grid g, const double *__restrict__ nvert, MetricPtrs m, double *ucont,
+                             double *partial) {
+  double sf = 0, sa = 0;
+  const size_t n = (size_t)(g.mx - 2) * (g.my - 2) * (g.mz - 2);
+  for (size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (size_t)gridDim.x * blockDim.x) {
+    const int i = c % (g.mx - 2) + 1, j = (c / (g.mx - 2)) % (g.my - 2) + 1, k = c / ((size_t)(g.mx - 2) * (g.my - 2)) + 1;
+    VfluxFace f[6];
+    const int nf = vflux0_faces(g, nvert, m, ucont, i, j, k, f);
+    for (int q = 0; q < nf; q++) {
+      const double u = *f[q].u;
+      sf += f[q].s == 0 ? u : -u;
+      sa += f[q].a;
+    }
+  }
+  const double t0 = block_sum(sf), t1 = block_sum(sa);
+  if (threadIdx.x == 0) {
+    partial[blockIdx.x] = t0;
+    partial[gridDim.x + blockIdx.x] = t1;
+  }
+}
+
+// the correction: off the fluid side, onto the blanked side; then the face
+// is zeroed when `zero` (immersed 0 or 3)
+__global__ void k_vflux0_apply(Grid g, const double *__restrict__ nvert, MetricPtrs m, double *ucont, double corr,
+                               int zero) {
+  const size_t n = (size_t)(g.mx - 2) * (g.my - 2) * (g.mz - 2);
+  for (size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (size_t)gridDim.x * blockDim.x) {
+    const int i = c % (g.mx - 2) + 1, j = (c / (g.mx - 2)) % (g.my - 2) + 1, k = c / ((size_t)(g.mx - 2) * (g.my - 2)) + 1;
+    VfluxFace f[6];
+    const int nf = vflux0_faces(g, nvert, m, ucont, i, j, k, f);
+    for (int q = 0; q < nf; q++) {
+      const double u = *f[q].u;
+      const double dlt = f[q].a * corr;
+      *f[q].u = zero ? 0. : (f[q].s == 0 ? u - dlt : u + dlt);
     }
   }
 }

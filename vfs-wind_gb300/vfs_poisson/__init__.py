@@ -37,7 +37,7 @@ EXPORTS = [
     "vfs_unet_create", "vfs_unet_destroy", "vfs_unet_set_stream", "vfs_unet_num_params", "vfs_unet_get_params",
     "vfs_unet_set_params", "vfs_unet_forward", "vfs_unet_gradient", "vfs_unet_train_step", "vfs_unet_adam",
     "vfs_unet_set_grads", "vfs_unet_kernel_launches", "vfs_poisson_learned_guess", "vfs_poisson_guess_sample",
-    "vfs_poisson_get_operator32", "vfs_poisson_rhs2", "vfs_poisson_volume_flux", "vfs_poisson_contra2cart",
+    "vfs_poisson_get_operator32", "vfs_poisson_rhs2", "vfs_poisson_volume_flux", "vfs_poisson_volume_flux0", "vfs_poisson_contra2cart",
     "vfs_read_petsc_vec", "vfs_write_petsc_vec", "vfs_read_grid", "vfs_read_ucd", "vfs_poisson_set_levelset",
     "vfs_poisson_ibm_search_nodes", "vfs_poisson_ibm_nodes", "vfs_poisson_ibm_interpolate", "vfs_poisson_ib_bc",
 ]
@@ -152,6 +152,7 @@ def load(path=LIB_PATH):
     L.vfs_poisson_get_operator32.argtypes = [vp, vp]
     L.vfs_poisson_rhs2.argtypes = [vp, dp, C.c_double, C.c_double, C.c_double, C.c_int]
     L.vfs_poisson_volume_flux.argtypes = [vp, dp, C.c_int, C.c_double, P(C.c_double), P(C.c_double)]
+    L.vfs_poisson_volume_flux0.argtypes = [vp, dp, C.c_int, P(C.c_double), P(C.c_double)]
     L.vfs_poisson_contra2cart.argtypes = [vp, dp, dp, C.c_int]
     L.vfs_poisson_set_levelset.argtypes = [vp, dp, dp, vp, C.c_int]
     L.vfs_read_petsc_vec.argtypes = [C.c_char_p, P(C.c_int64), vp]
@@ -259,6 +260,14 @@ class PoissonSolver:
         f, a = C.c_double(), C.c_double()
         _check(load().vfs_poisson_volume_flux(self.h, _ptr(ucont, True), int(flg), float(flux_intp_sum),
                                               C.byref(f), C.byref(a)))
+        return f.value, a.value
+
+    def volume_flux0(self, ucont, immersed=0):
+        """VolumeFlux, the overload for immersed != 1: corrects (immersed 3,
+        other) or zeroes (immersed 0, 3) the fluid/blanked faces of ucont in
+        place; returns (flux, area) formed afterwards."""
+        f, a = C.c_double(), C.c_double()
+        _check(load().vfs_poisson_volume_flux0(self.h, _ptr(ucont, True), int(immersed), C.byref(f), C.byref(a)))
         return f.value, a.value
 
     def contra2cart(self, ucont, ucat=None, zero_solid=True):

@@ -61,6 +61,7 @@ int MPI_Recv(void *, int, MPI_Datatype, int, int, MPI_Comm, MPI_Status *);
 int MPI_Gather(void *, int, MPI_Datatype, void *, int, MPI_Datatype, int, MPI_Comm);
 int MPI_Allgather(void *, int, MPI_Datatype, void *, int, MPI_Datatype, MPI_Comm);
 double MPI_Wtime(void);
+int MPI_Abort(MPI_Comm, int);
 
 // -------------------------------------------------------------- PETSc ----
 typedef int PetscErrorCode;

@@ -5,6 +5,7 @@
 #include "petsc_shim.h"
 
 #include <execinfo.h>
+#include <unistd.h>
 
 #include <chrono>
 #include <map>
@@ -157,6 +158,11 @@ int MPI_Gather(void *a, int n, MPI_Datatype t, void *b, int, MPI_Datatype, int, 
 int MPI_Allgather(void *a, int n, MPI_Datatype t, void *b, int, MPI_Datatype, MPI_Comm) {
   memmove(b, a, n * type_size(t));
   return 0;
+}
+int MPI_Abort(MPI_Comm, int code) {
+  fflush(stdout);
+  fflush(stderr);
+  _exit(code ? code : 1);
 }
 double MPI_Wtime(void) {
   return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();

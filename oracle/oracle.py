@@ -345,6 +345,12 @@ def ibm_search(d, cent, surface, nvert=None, ibi=0, bctype=(0, 0, 0, 0, 0, 0), m
     return out, failed
 
 
+def set_smoother(zebra):
+    """CPU solver smoother: 1 zebra j-line Gauss-Seidel over checkerboard
+    columns (the GPU V-cycle's), 2 over k-planes, 0 damped line Jacobi."""
+    lib().or_mg_set_smoother(int(zebra))
+
+
 class MGSolver:
     """FP64 FGMRES + geometric V-cycle on the CPU (timed CPU baseline)."""
 

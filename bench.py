@@ -64,6 +64,9 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--train-samples", type=int, default=16)
     ap.add_argument("--train-steps", type=int, default=3000)
+    ap.add_argument("--history", type=int, default=6, help="solutions kept for the history projection (0: off)")
+    ap.add_argument("--network-period", type=int, default=8,
+                    help="while its candidate loses, the network runs on every n-th guess")
     return ap.parse_args()
 
 
@@ -310,7 +313,11 @@ def run_ours(args):
     del pool
     torch.cuda.empty_cache()
 
-    # 3. held-out steps: both arms on the same right-hand sides and history
+    # 3. held-out steps: every arm on the same right-hand sides and history;
+    # only the learned arm's solves enter the solution history
+    s.set_history(args.history)
+    s.set_network_period(args.network_period)
+
     def step_inputs(n):
         return seq.mask_faces(seq.ucont(n), nv)
 
@@ -318,13 +325,33 @@ def run_ours(args):
 
     def arm_plain(u, h):
         phi = h[-1].clone()
+        s.history_record(False)
         torch.cuda.synchronize()
         e0.record(stream)
         s.rhs(u)
         _, st = s.solve(phi, opts=plain)
         e1.record(stream)
         torch.cuda.synchronize()
+        s.history_record(True)
         return phi, st, e0.elapsed_time(e1)
+
+    def arm_split(u, h, precision, guess):
+        """The other combinations, for the record: the plain or mixed solve
+        from phi_{n-1} ("prev") or from the history projection ("hist")."""
+        phi = h[-1].clone()
+        s.history_record(False)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        s.rhs(u)
+        if guess == "hist" and args.history:
+            s.history_guess()
+            _, st = s.solve(phi, opts=V.default_opts(precision=precision, rtol=1e-8, warm_start=2))
+        else:
+            _, st = s.solve(phi, opts=V.default_opts(precision=precision, rtol=1e-8, warm_start=1))
+        e1.record(stream)
+        torch.cuda.synchronize()
+        s.history_record(True)
+        return st, e0.elapsed_time(e1)
 
     def arm_learned(u, h, host=None):
         phi = torch.empty_like(h[-1]) if host is None else host[3]
@@ -352,9 +379,15 @@ def run_ours(args):
     clocks = ClockSampler(local)
     clocks.start()
     ms_a, ms_b, its_a, its_b, chosen, rel_prev, rel_learned, launches = [], [], [], [], [], [], [], 0
+    split = {k: ([], []) for k in ("mixed_prev", "mixed_hist", "plain_hist")}
     for _ in range(args.steps):
         u = step_inputs(n)
         pa, sa, ta = arm_plain(u, hist)
+        for key, prec, g in (("mixed_prev", 0, "prev"), ("mixed_hist", 0, "hist"), ("plain_hist", 1, "hist")):
+            st_x, t_x = arm_split(u, hist, prec, g)
+            assert st_x.rel_residual <= 1e-8
+            split[key][0].append(t_x)
+            split[key][1].append(st_x.iterations)
         l0 = s.kernel_launches()
         pb, sb, tb, ch, rr = arm_learned(u, hist)
         launches += s.kernel_launches() - l0
@@ -431,11 +464,18 @@ def run_ours(args):
             "solver": "FGMRES(20) with one-pass classical Gram-Schmidt, FP64 residual, operator apply and Krylov; FP32 geometric "
                       "V-cycle (zebra j-line Gauss-Seidel over checkerboard columns, 1+2 sweeps; residual couplings "
                       "stored in half precision, difference form, formed inside the line kernel on the levels of at "
-                      "most 2^20 cells; dense projected solve on a 192-cell coarsest level); learned initial guess "
-                      "judged against the previous step, the solve's first Arnoldi step overlapping the network",
+                      "most 2^20 cells; dense projected solve on a 192-cell coarsest level); initial guess: the history "
+                      "projection (least squares over the last solutions' images) with the learned network's "
+                      "correction judged against it (the network run on every n-th step while it loses)",
             "iterations": statistics.mean(its_b), "learned_guess_chosen": sum(chosen) / len(chosen),
-            "initial_rel_residual_learned": statistics.mean(rel_learned),
-            "initial_rel_residual_previous_step": statistics.mean(rel_prev),
+            "network_evaluations": sum(1 for r in rel_learned if r >= 0),
+            "initial_rel_residual_learned": (statistics.mean([r for r in rel_learned if r >= 0])
+                                             if any(r >= 0 for r in rel_learned) else None),
+            "initial_rel_residual_base": statistics.mean(rel_prev),
+            "base_guess": (f"history projection over the last {args.history} solutions" if args.history
+                           else "previous step's phi"),
+            "other_arms": {k: {"ms": statistics.mean(v[0]), "iterations": statistics.mean(v[1])}
+                           for k, v in split.items()},
             "plain_fp64_ms": ms_a_mean, "plain_fp64_iterations": statistics.mean(its_a),
             "plain_fp64_guess": "previous step's phi",
             "speedup_vs_plain_fp64": ms_a_mean / ms_b_mean,

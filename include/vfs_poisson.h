@@ -426,6 +426,31 @@ int vfs_unet_adam(vfs_unet *u, double lr, double beta1, double beta2, double eps
 int vfs_unet_set_grads(vfs_unet *u, const float *grad);
 int64_t vfs_unet_kernel_launches(vfs_unet *u);
 
+/* History projection of the initial guess (no counterpart in the
+ * reference, which restarts from the previous step's Phi2,
+ * poisson_hypre.c:577; Fischer's projection for successive right-hand
+ * sides, CMAME 163 (1998) 193-204).  The handle keeps the last k converged
+ * solutions X_j (1 <= k <= 8; 0 turns it off) and their images A X_j (b - r
+ * of the solves that produced them; recomputed with the FP64 operator after
+ * vfs_poisson_set_nvert).  vfs_poisson_history_guess, after
+ * vfs_poisson_rhs, installs x = sum_j c_j X_j with c minimising
+ * ||b - sum_j c_j A X_j||_2 as the iterate for the next solve
+ * (opts.warm_start = 2), with its exact FP64 residual; the newest solution is
+ * in the span, so the guess is never worse than the previous step's phi.
+ * rel_res gets ||b - A x|| / ||b||.  Each converged solve appends its
+ * solution.  Memory: 2 k box-sized FP64 vectors. */
+int vfs_poisson_set_history(vfs_poisson *h, int k);
+int vfs_poisson_history_guess(vfs_poisson *h, double *rel_res);
+/* Whether converged solves append to the history (default 1): 0 lets a
+ * second solver sequence share the handle without entering it. */
+int vfs_poisson_history_record(vfs_poisson *h, int on);
+
+/* With a history, vfs_poisson_learned_guess judges its candidate against the
+ * history projection instead of phi_{n-1}; while the network's candidate
+ * keeps losing, the network runs on every `period`-th call only (the others
+ * install the projection directly and report rel_res[1] = -1).  Default 1. */
+int vfs_poisson_set_network_period(vfs_poisson *h, int period);
+
 /* Learned initial guess for the current right-hand side (vfs_poisson_rhs
  * first), from phi at steps n-1 and n-2 (DA layout, host or device).  The
  * network sees four planes on the half-resolution grid (2x2x2 averages over

@@ -148,6 +148,15 @@ __global__ void k_scale_to32(size_t n, const double *v, float s, const float *si
 __global__ void k_reduce_norm(const double *partial, int nb, double *out, float *out32);
 __global__ void k_to64(size_t n, const float *x32, const double *x64, double *out);
 __global__ void k_sumsq(size_t n, const double *x, double *partial);
+// history projection of the initial guess (at most kHistMax solutions)
+constexpr int kHistMax = 8;
+struct HistPtrs {
+  const double *p[kHistMax];
+};
+__global__ void k_hist_dots(size_t n, HistPtrs Y, int k, const double *v, double *partial);
+__global__ void k_hist_combine(size_t n, HistPtrs X, HistPtrs Y, int k, const double *c, const double *b, double *x,
+                               double *r, double *partial);
+__global__ void k_hist_push(size_t n, const double *x, const double *b, const double *r, double *Xs, double *Ys);
 
 // Hand-off from a handle to the surface search (ibm.cu): its stream, grid,
 // DA-layout cell centres and launch counter.

@@ -474,6 +474,20 @@ struct vfs_poisson {
   double *ls_rho = nullptr, *ls_level = nullptr;
   int ls_on = 0, ls_bc3 = 0, ls_bc4 = 0, ls_bc5 = 0;
   int line_cols_cap = 0;  // cap on the line kernels' columns per block (0: none)
+  // history projection of the initial guess: the last hist_cap solutions X_j
+  // (FGMRES iterates before the mean removal) and their images Y_j = A X_j
+  // (b - r of the solves that produced them), a ring with the newest at
+  // hist_head - 1, and their Gram matrix G_ij = Y_i . Y_j (host)
+  int hist_cap = 0, hist_cnt = 0, hist_head = 0;
+  double *hist_X[kHistMax] = {}, *hist_Y[kHistMax] = {};
+  double hist_G[kHistMax][kHistMax] = {};
+  double *hist_x = nullptr, *hist_r = nullptr;  // the projection and its residual
+  uint64_t op_version = 0, hist_op_version = 0;  // operator assemblies seen
+  // the learned guess runs its network on every net_period-th call while
+  // its candidate keeps losing to the history projection (net_wait: calls
+  // left to skip)
+  int net_period = 1, net_wait = 0;
+  bool hist_record = true;  // converged solves append to the history
   double r0_norm = 0.;
   bool r0_valid = false;
   // Speculative first Arnoldi step: a learned guess that expects the plain
@@ -1192,6 +1206,102 @@ int residual_norm(vfs_poisson *h, const double *x, double *r, double *norm) {
   return VFS_OK;
 }
 
+// ---- history projection of the initial guess (Fischer's projection for
+// successive right-hand sides, CMAME 163 (1998) 193-204) ----
+HistPtrs hist_ptrs(double *const *a, int k) {
+  HistPtrs p{};
+  for (int j = 0; j < k; j++) p.p[j] = a[j];
+  return p;
+}
+
+// row and column s of the Gram matrix: Y_s . Y_j for the stored slots
+int hist_gram_row(vfs_poisson *h, int s) {
+  const int k = h->hist_cnt;
+  LAUNCH(h, k_hist_dots, kRedBlocks, 256, h->box.n(), hist_ptrs(h->hist_Y, k), k, (const double *)h->hist_Y[s],
+         h->partial);
+  double d[kHistMax + 1];
+  TRY(reduce_read(h, kRedBlocks, k + 1, d));
+  for (int j = 0; j < k; j++) h->hist_G[s][j] = h->hist_G[j][s] = d[j];
+  h->hist_G[s][s] = d[k];
+  return VFS_OK;
+}
+
+// after a new operator assembly: the stored solutions' images under it
+int hist_refresh(vfs_poisson *h) {
+  if (h->hist_op_version == h->op_version) return VFS_OK;
+  for (int j = 0; j < h->hist_cnt; j++)
+    LAUNCH(h, k_apply64, box_grid(h->box), 128, h->box, h->A0, (const double *)h->hist_X[j], h->hist_Y[j]);
+  for (int j = 0; j < h->hist_cnt; j++) TRY(hist_gram_row(h, j));
+  h->hist_op_version = h->op_version;
+  return VFS_OK;
+}
+
+// store a converged solve: the iterate x and its image b - r (V_0 holds the
+// solve's final FP64 residual r = b - A x)
+int hist_push(vfs_poisson *h) {
+  if (!h->hist_cap) return VFS_OK;
+  TRY(hist_refresh(h));
+  const int s = h->hist_head;
+  LAUNCH(h, k_hist_push, kRedBlocks, 256, h->box.n(), (const double *)h->x, (const double *)h->b,
+         (const double *)h->V[0], h->hist_X[s], h->hist_Y[s]);
+  h->hist_head = (s + 1) % h->hist_cap;
+  if (h->hist_cnt < h->hist_cap) h->hist_cnt++;
+  return hist_gram_row(h, s);
+}
+
+// the projection x = X c, r = b - Y c minimising ||b - Y c|| over the
+// stored images: normal equations G c = Y^T b by a Cholesky factorisation
+// taken newest first, where a vector whose pivot falls below 1e-13 of its
+// Gram diagonal adds nothing new and keeps the coefficient 0 (the images
+// of successive solutions are nearly parallel).  The newest solution alone
+// is in the span, so the result is never worse than the previous step's phi.
+int hist_project(vfs_poisson *h, double *rnorm, double *bnorm) {
+  TRY(hist_refresh(h));
+  const int k = h->hist_cnt;
+  const size_t n = h->box.n();
+  LAUNCH(h, k_hist_dots, kRedBlocks, 256, n, hist_ptrs(h->hist_Y, k), k, (const double *)h->b, h->partial);
+  double g[kHistMax + 1];
+  TRY(reduce_read(h, kRedBlocks, k + 1, g));
+  int ord[kHistMax], na = 0;
+  double L[kHistMax][kHistMax] = {};
+  for (int i = 0; i < k; i++) {
+    const int sl = ((h->hist_head - 1 - i) % h->hist_cap + h->hist_cap) % h->hist_cap;
+    double row[kHistMax];
+    for (int q = 0; q < na; q++) {
+      double v = h->hist_G[sl][ord[q]];
+      for (int t = 0; t < q; t++) v -= row[t] * L[q][t];
+      row[q] = v / L[q][q];
+    }
+    double piv = h->hist_G[sl][sl];
+    for (int t = 0; t < na; t++) piv -= row[t] * row[t];
+    if (!(piv > 1e-13 * h->hist_G[sl][sl])) continue;
+    for (int t = 0; t < na; t++) L[na][t] = row[t];
+    L[na][na] = std::sqrt(piv);
+    ord[na++] = sl;
+  }
+  double z[kHistMax], cc[kHistMax] = {}, c[kHistMax] = {};
+  for (int p = 0; p < na; p++) {
+    double v = g[ord[p]];
+    for (int t = 0; t < p; t++) v -= L[p][t] * z[t];
+    z[p] = v / L[p][p];
+  }
+  for (int p = na - 1; p >= 0; p--) {
+    double v = z[p];
+    for (int t = p + 1; t < na; t++) v -= L[t][p] * cc[t];
+    cc[p] = v / L[p][p];
+  }
+  for (int p = 0; p < na; p++) c[ord[p]] = cc[p];
+  for (int j = 0; j < k; j++) h->hbuf[464 + j] = c[j];
+  CUDA_TRY(cudaMemcpyAsync(h->coef, h->hbuf + 464, k * 8, cudaMemcpyHostToDevice, h->stream));
+  LAUNCH(h, k_hist_combine, kRedBlocks, 256, n, hist_ptrs(h->hist_X, k), hist_ptrs(h->hist_Y, k), k,
+         (const double *)h->coef, (const double *)h->b, h->hist_x, h->hist_r, h->partial);
+  double rr;
+  TRY(reduce_read(h, kRedBlocks, 1, &rr));
+  *rnorm = std::sqrt(std::max(rr, 0.));
+  *bnorm = std::sqrt(std::max(g[k], 0.));
+  return VFS_OK;
+}
+
 int ensure_krylov(vfs_poisson *h, int m) {
   if (m <= h->m_alloc) return VFS_OK;
   for (auto p : h->V) dfree(h, p);
@@ -1637,6 +1747,7 @@ int vfs_poisson_set_nvert(vfs_poisson *h, const double *nvert) {
   h->have_nvert = true;
   h->have_rhs = false;
   h->r0_valid = false;
+  h->op_version++;  // stored history images belong to the previous operator
   return VFS_OK;
 }
 
@@ -1875,6 +1986,8 @@ int vfs_poisson_solve(vfs_poisson *h, double *phi, const vfs_solve_opts *opts, v
     CUDA_TRY(cudaMemsetAsync(h->x, 0, n * 8, h->stream));
   }
   TRY(fgmres(h, o, &st));
+  if (h->hist_cap && h->hist_record && st.initial_rel_residual > 0. && st.rel_residual <= o.rtol)
+    TRY(hist_push(h));
   if (h->desc.bctype3 != -10 && !(h->ls_on && h->ls_bc5 == 4)) {  // Remove_Nullspace of phi (:604-608)
     LAUNCH(h, k_mean_partial, kRedBlocks, 256, h->box, h->fluid, h->x, h->partial);
     LAUNCH(h, k_reduce_rows, 2, 1024, h->partial, kRedBlocks, 2, h->red);
@@ -1988,6 +2101,64 @@ int vfs_poisson_get_operator32(vfs_poisson *h, float *planes) {
   return sync(h);
 }
 
+int vfs_poisson_set_history(vfs_poisson *h, int k) {
+  if (!h) return fail(VFS_EINVAL, "null handle");
+  if (k < 0 || k > kHistMax) return fail(VFS_EINVAL, "history length must be 0.." + std::to_string(kHistMax));
+  TRY(sync(h));
+  for (int j = 0; j < kHistMax; j++) {
+    dfree(h, h->hist_X[j]);
+    dfree(h, h->hist_Y[j]);
+    h->hist_X[j] = h->hist_Y[j] = nullptr;
+  }
+  if (h->r0 == h->hist_r) h->r0_valid = false;
+  dfree(h, h->hist_x);
+  dfree(h, h->hist_r);
+  h->hist_x = h->hist_r = nullptr;
+  h->hist_cap = h->hist_cnt = h->hist_head = 0;
+  const size_t n = h->box.n();
+  for (int j = 0; j < k; j++) {
+    TRY(dalloc(h, &h->hist_X[j], n));
+    TRY(dalloc(h, &h->hist_Y[j], n));
+  }
+  if (k) {
+    TRY(dalloc(h, &h->hist_x, n));
+    TRY(dalloc(h, &h->hist_r, n));
+  }
+  h->hist_cap = k;
+  h->hist_op_version = h->op_version;
+  return VFS_OK;
+}
+
+int vfs_poisson_history_record(vfs_poisson *h, int on) {
+  if (!h) return fail(VFS_EINVAL, "null handle");
+  h->hist_record = on != 0;
+  return VFS_OK;
+}
+
+int vfs_poisson_set_network_period(vfs_poisson *h, int period) {
+  if (!h) return fail(VFS_EINVAL, "null handle");
+  if (period < 1) return fail(VFS_EINVAL, "period must be at least 1");
+  h->net_period = period;
+  h->net_wait = 0;
+  return VFS_OK;
+}
+
+int vfs_poisson_history_guess(vfs_poisson *h, double *rel_res) {
+  if (!h) return fail(VFS_EINVAL, "null handle");
+  if (!h->have_rhs) return fail(VFS_ESTATE, "rhs must come before the guess");
+  if (!h->hist_cnt) return fail(VFS_ESTATE, "no stored solution (vfs_poisson_set_history, then a solve)");
+  double rn, bn;
+  TRY(hist_project(h, &rn, &bn));
+  std::swap(h->x, h->hist_x);
+  h->r0 = h->hist_r;
+  h->r0_norm = rn;
+  h->r0_valid = true;
+  h->spec_valid = false;
+  h->spec_next = false;
+  if (rel_res) *rel_res = bn > 0. ? rn / bn : 0.;
+  return sync(h);
+}
+
 int vfs_poisson_learned_guess(vfs_poisson *h, vfs_unet *u, const double *phi_nm1, const double *phi_nm2,
                               double kappa, int *chosen, double *rel_res) {
   if (!h || !u) return fail(VFS_EINVAL, "null argument");
@@ -1995,6 +2166,25 @@ int vfs_poisson_learned_guess(vfs_poisson *h, vfs_unet *u, const double *phi_nm1
   h->r0_valid = false;
   h->spec_valid = false;
   if (h->phase) cudaEventRecord(h->phev[0], h->stream);
+  // with a solution history the candidate the network must beat is its
+  // projection (never worse than the previous step's phi), not phi_{n-1}
+  const bool use_hist = h->hist_cnt > 0;
+  double r_hist = 0., b_hist = 0.;
+  if (use_hist) TRY(hist_project(h, &r_hist, &b_hist));
+  if (use_hist && h->net_wait > 0) {  // the network sits this call out
+    h->net_wait--;
+    std::swap(h->x, h->hist_x);
+    h->r0 = h->hist_r;
+    h->r0_norm = r_hist;
+    h->r0_valid = true;
+    h->spec_next = false;
+    if (chosen) *chosen = 0;
+    if (rel_res) {
+      rel_res[0] = b_hist > 0. ? r_hist / b_hist : 0.;
+      rel_res[1] = -1.;
+    }
+    return sync(h);
+  }
   double nrm[3];
   TRY(guess_features(h, phi_nm1, phi_nm2, nrm));
   const size_t n = b.n();
@@ -2139,7 +2329,7 @@ int vfs_poisson_learned_guess(vfs_poisson *h, vfs_unet *u, const double *phi_nm1
       for (int v = u2; v < kGuessBands; v++, q++) r2 += (u2 == v ? 1. : 2.) * bw.a[u2] * bw.a[v] * gm[q];
     }
   }
-  const double r_prev = std::sqrt(nrm[1]);
+  const double r_prev = use_hist ? r_hist : std::sqrt(nrm[1]);
   const double nb = nrm[2] > 0. ? std::sqrt(nrm[2]) : 1.;
   double r_learn = std::sqrt(std::max(r2, 0.));
   bool learned = false;
@@ -2167,7 +2357,10 @@ int vfs_poisson_learned_guess(vfs_poisson *h, vfs_unet *u, const double *phi_nm1
     learned = r_learn < r_prev;
   }
   double r_prev64 = r_prev;
-  if (!learned) {
+  if (!learned && use_hist) {
+    // the projection stays: its residual is exact already
+    std::swap(h->x, h->hist_x);
+  } else if (!learned) {
     // the previous step's phi stays: its FP64 residual is FGMRES's start
     CUDA_TRY(cudaMemcpyAsync(h->x, h->Z[h->m_alloc - 1], n * 8, cudaMemcpyDeviceToDevice, h->stream));
     const dim3 gr = box_grid(h->box);
@@ -2176,7 +2369,8 @@ int vfs_poisson_learned_guess(vfs_poisson *h, vfs_unet *u, const double *phi_nm1
     TRY(reduce_read(h, (int)(gr.x * gr.y * gr.z), 1, &s2));
     r_prev64 = std::sqrt(s2);
   }
-  h->r0 = learned ? h->rlearn : h->rprev;
+  h->r0 = learned ? h->rlearn : (use_hist ? h->hist_r : h->rprev);
+  if (use_hist) h->net_wait = learned ? 0 : h->net_period - 1;
   h->r0_norm = learned ? r_learn : r_prev64;
   h->r0_valid = true;
   // the speculative step holds when the installed iterate is the plain

@@ -889,6 +889,66 @@ __global__ void k_sumsq(size_t n, const double *__restrict__ x, double *partial)
   if (threadIdx.x == 0) partial[blockIdx.x] = s;
 }
 
+// ---- history projection of the initial guess ----
+// Block partials (grid-stride, fixed block count: deterministic) of the dot
+// products v . Y_j for j < k and of v . v: row j of `partial` holds v . Y_j,
+// row k holds v . v.
+__global__ void __launch_bounds__(256) k_hist_dots(size_t n, HistPtrs Y, int k, const double *__restrict__ v,
+                                                   double *partial) {
+  double s[kHistMax + 1];
+#pragma unroll
+  for (int j = 0; j <= kHistMax; j++) s[j] = 0.;
+  for (size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (size_t)gridDim.x * blockDim.x) {
+    const double vc = v[c];
+#pragma unroll
+    for (int j = 0; j < kHistMax; j++)
+      if (j < k) s[j] = fma(vc, __ldg(&Y.p[j][c]), s[j]);
+    s[kHistMax] = fma(vc, vc, s[kHistMax]);
+  }
+  for (int j = 0; j <= k; j++) {
+    const double t = block_sum(j < k ? s[j] : s[kHistMax]);
+    if (threadIdx.x == 0) partial[(size_t)j * gridDim.x + blockIdx.x] = t;
+  }
+}
+
+// x = sum_j c_j X_j and r = b - sum_j c_j Y_j (Y_j = A X_j), with the block
+// partials of ||r||^2.  coefficients in `c` (device, k values).
+__global__ void __launch_bounds__(256) k_hist_combine(size_t n, HistPtrs X, HistPtrs Y, int k,
+                                                      const double *__restrict__ c, const double *__restrict__ b,
+                                                      double *__restrict__ x, double *__restrict__ r,
+                                                      double *partial) {
+  double cj[kHistMax];
+#pragma unroll
+  for (int j = 0; j < kHistMax; j++) cj[j] = j < k ? c[j] : 0.;
+  double s = 0.;
+  for (size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (size_t)gridDim.x * blockDim.x) {
+    double xv = 0., yv = 0.;
+#pragma unroll
+    for (int j = 0; j < kHistMax; j++)
+      if (j < k) {
+        xv = fma(cj[j], __ldg(&X.p[j][q]), xv);
+        yv = fma(cj[j], __ldg(&Y.p[j][q]), yv);
+      }
+    const double rv = b[q] - yv;
+    x[q] = xv;
+    r[q] = rv;
+    s = fma(rv, rv, s);
+  }
+  s = block_sum(s);
+  if (threadIdx.x == 0) partial[blockIdx.x] = s;
+}
+
+// a solve's iterate and its image into a history slot: Xs = x, Ys = b - r
+// (r = b - A x, the solve's final FP64 residual)
+__global__ void __launch_bounds__(256) k_hist_push(size_t n, const double *__restrict__ x,
+                                                   const double *__restrict__ b, const double *__restrict__ r,
+                                                   double *__restrict__ Xs, double *__restrict__ Ys) {
+  for (size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (size_t)gridDim.x * blockDim.x) {
+    Xs[q] = x[q];
+    Ys[q] = b[q] - r[q];
+  }
+}
+
 #define TYPED(T, S, TRI_THREADS, TRI_MINB)                                                                         \
   __global__ void __launch_bounds__(256) k_residual_##S(Box b, const T *A, const T *x, const T *rhs, T *r,  \
                                                         int color) {                                       \

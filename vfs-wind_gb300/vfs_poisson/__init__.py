@@ -40,6 +40,8 @@ EXPORTS = [
     "vfs_poisson_get_operator32", "vfs_poisson_rhs2", "vfs_poisson_volume_flux", "vfs_poisson_volume_flux0", "vfs_poisson_contra2cart",
     "vfs_read_petsc_vec", "vfs_write_petsc_vec", "vfs_read_grid", "vfs_read_ucd", "vfs_poisson_set_levelset",
     "vfs_poisson_ibm_search_nodes", "vfs_poisson_ibm_nodes", "vfs_poisson_ibm_interpolate", "vfs_poisson_ib_bc",
+    "vfs_poisson_set_history", "vfs_poisson_history_guess", "vfs_poisson_set_network_period",
+    "vfs_poisson_history_record",
 ]
 
 
@@ -153,6 +155,10 @@ def load(path=LIB_PATH):
     L.vfs_poisson_rhs2.argtypes = [vp, dp, C.c_double, C.c_double, C.c_double, C.c_int]
     L.vfs_poisson_volume_flux.argtypes = [vp, dp, C.c_int, C.c_double, P(C.c_double), P(C.c_double)]
     L.vfs_poisson_volume_flux0.argtypes = [vp, dp, C.c_int, P(C.c_double), P(C.c_double)]
+    L.vfs_poisson_set_history.argtypes = [vp, C.c_int]
+    L.vfs_poisson_history_guess.argtypes = [vp, P(C.c_double)]
+    L.vfs_poisson_set_network_period.argtypes = [vp, C.c_int]
+    L.vfs_poisson_history_record.argtypes = [vp, C.c_int]
     L.vfs_poisson_contra2cart.argtypes = [vp, dp, dp, C.c_int]
     L.vfs_poisson_set_levelset.argtypes = [vp, dp, dp, vp, C.c_int]
     L.vfs_read_petsc_vec.argtypes = [C.c_char_p, P(C.c_int64), vp]
@@ -443,6 +449,25 @@ class PoissonSolver:
             out = np.zeros((19, mz - 2, my - 2, mx - 2), np.float32)
         _check(load().vfs_poisson_get_operator32(self.h, _ptr(out, True)))
         return out
+
+    def set_history(self, k):
+        """Keep the last k converged solutions for the history projection of
+        the initial guess (0 turns it off)."""
+        _check(load().vfs_poisson_set_history(self.h, int(k)))
+
+    def history_guess(self):
+        """Install the history projection as the iterate (solve with
+        warm_start=2 next); returns its relative residual."""
+        r = C.c_double()
+        _check(load().vfs_poisson_history_guess(self.h, C.byref(r)))
+        return r.value
+
+    def history_record(self, on=True):
+        """Whether converged solves append to the history."""
+        _check(load().vfs_poisson_history_record(self.h, int(bool(on))))
+
+    def set_network_period(self, period):
+        _check(load().vfs_poisson_set_network_period(self.h, int(period)))
 
     def learned_guess(self, unet, phi_nm1, phi_nm2, kappa):
         """Install the better of the learned guess and phi_{n-1} as the

@@ -139,3 +139,35 @@ class TowerSequence(_Sequence):
 
     def bodies(self, step):
         return CF.tower_surfaces(radius=0.02, y0=-0.05, height=1.1, n_theta=self.n_theta, n_len=4)
+
+
+class FarmSequence(_Sequence):
+    """Configuration 5: 512x256x512, geometric 1.02 wall stretching,
+    amplitude 0.02, periodic x and z; a 4x3 array of towers (the towers
+    case's radius 0.02 and 0.25 streamwise spacing, 0.3 spanwise, filling the
+    domain) from below the wall to the hub height 0.5, each carrying a 3-rod
+    rotor (rod radius 3 cells, length 0.08) at its top that rotates 2 degrees
+    per step about the z axis, as the rotor case's does; Fourier fluxes
+    advected 0.5 cells per step in x."""
+
+    periodic = (0, 0, 0, 1, 0, 1)
+    moving = True
+    XS = (0.125, 0.375, 0.625, 0.875)
+    ZS = (0.2, 0.5, 0.8)
+    HUB = 0.5
+
+    def __init__(self, nx=512, ny=256, nz=512, seed=1005, amp=0.02, ratio=1.02, device="cuda", n_theta=32):
+        yc = CF._geometric(ny, ratio)
+        coor = CF._nodes(nx, ny, nz, lambda e: np.interp(e, np.arange(ny + 1) / ny, yc), amp, physical=True)
+        super().__init__(nx, ny, nz, coor, seed, device)
+        self.n_theta = n_theta
+        self.h = 1.0 / nx
+
+    def bodies(self, step):
+        out = []
+        for x0 in self.XS:
+            for z0 in self.ZS:
+                out.append(CF.rod_surface((x0, -0.05, z0), (0.0, 1.0, 0.0), self.HUB + 0.05, 0.02, self.n_theta, 4))
+                out += CF.rotor_surfaces(centre=(x0, self.HUB, z0), angle_deg=2.0 * step, rods=3,
+                                         radius=3 * self.h, length=0.08, hub=0.0, n_theta=16, n_len=12)
+        return out

@@ -677,6 +677,18 @@ __global__ void k_periodic_copy2(Grid g, double *p, double *phi) {
 }
 
 // Projection (Source/poisson.c:2700-3066), level set off.
+// v * dt * st / coeff / r in the reference's left-to-right order.  A
+// division by exactly 1 returns its dividend unchanged in IEEE arithmetic,
+// so the divisions by coeff == 1 (time_coeff() without level set or RANS)
+// and r == 1 (no density weighting) are skipped: the same bits, without the
+// FP64 division sequence that dominates this kernel's FP64 pipe.
+__device__ __forceinline__ double proj_scale(double v, double dt, double st, double coeff, double r) {
+  v = v * dt * st;
+  if (coeff != 1.0) v = v / coeff;
+  if (r != 1.0) v = v / r;
+  return v;
+}
+
 __global__ void k_projection(Grid g, Box b, const double *__restrict__ nvert, const double *__restrict__ phi,
                              const double *__restrict__ pc, double dt, double st, double coeff, double *ucont,
                              MetricPtrs m, LevelSet ls) {
@@ -721,8 +733,7 @@ __global__ void k_projection(Grid g, Box b, const double *__restrict__ nvert, co
     }
     if ((NV(i, j, k) + NV(i + 1, j, k)) < thr) {
       const double aj = pc[3 * n + c];
-      ucont[t * 3 + 0] -= (dpdc * pc[0 * n + c] * aj + dpde * pc[1 * n + c] * aj + dpdz * pc[2 * n + c] * aj) *
-                          dt * st / coeff / r1;
+      ucont[t * 3 + 0] -= proj_scale(dpdc * pc[0 * n + c] * aj + dpde * pc[1 * n + c] * aj + dpdz * pc[2 * n + c] * aj, dt, st, coeff, r1);
     }
   }
   if (j < my - 2 || (jp && j == my - 2) || (ls.on && ls.bc3 == 4 && j == my - 2)) {
@@ -750,8 +761,7 @@ __global__ void k_projection(Grid g, Box b, const double *__restrict__ nvert, co
     }
     if ((NV(i, j, k) + NV(i, j + 1, k)) < thr || (int)(NV(i, j, k) + NV(i, j + 1, k)) == 5) {
       const double aj = pc[7 * n + c];
-      ucont[t * 3 + 1] -= (dpdc * pc[4 * n + c] * aj + dpde * pc[5 * n + c] * aj + dpdz * pc[6 * n + c] * aj) *
-                          dt * st / coeff / r2;
+      ucont[t * 3 + 1] -= proj_scale(dpdc * pc[4 * n + c] * aj + dpde * pc[5 * n + c] * aj + dpdz * pc[6 * n + c] * aj, dt, st, coeff, r2);
     }
   }
   if (k < mz - 2 || (kp && k == mz - 2) || (ls.on && ls.bc5 == 4 && k == mz - 2)) {
@@ -779,13 +789,12 @@ __global__ void k_projection(Grid g, Box b, const double *__restrict__ nvert, co
     else dpdz = PH(i, j, k + 1) - PH(i, j, k);
     if ((NV(i, j, k) + NV(i, j, k + 1)) < thr) {
       const double aj = pc[11 * n + c];
-      ucont[t * 3 + 2] -= (dpdc * pc[8 * n + c] * aj + dpde * pc[9 * n + c] * aj + dpdz * pc[10 * n + c] * aj) *
-                          dt * st / coeff / r3;
+      ucont[t * 3 + 2] -= proj_scale(dpdc * pc[8 * n + c] * aj + dpde * pc[9 * n + c] * aj + dpdz * pc[10 * n + c] * aj, dt, st, coeff, r3);
       if (ls.on && k == 1 && ls.bc4 == 5000 && ls.level[t] < 0) {  // poisson.c:2951-2956
         const size_t t0 = g.at(i, j, 0);
         const double *kz = &m.kzet[t0 * 3];
         const double r0 = ls.rho[t];
-        ucont[t0 * 3 + 2] -= (dpdz * (kz[0] * kz[0] + kz[1] * kz[1] + kz[2] * kz[2]) * m.kaj[t0]) * dt * st / coeff / r0;
+        ucont[t0 * 3 + 2] -= proj_scale(dpdz * (kz[0] * kz[0] + kz[1] * kz[1] + kz[2] * kz[2]) * m.kaj[t0], dt, st, coeff, r0);
       }
     }
   }

@@ -11,23 +11,26 @@ PoissonSolver_Hypre-equivalent call: right-hand side from Ucont, initial
 guess, FGMRES to ||b - A phi|| / ||b|| <= 1e-8 (FP64 residual), fluid-mean
 removal and phi in DA layout.
 
-  this arm (value)   learned initial guess (U-Net trained on the GPU on the
-                     plain solver's own solves of the first steps; the plain
-                     solver keeps it only if its FP64 residual beats the
-                     previous step's phi) + FP32 V-cycle inside FP64 FGMRES;
-                     guess time included.
+  this arm (value)   initial guess from the history projection (least squares
+                     over the last solutions' images), with the U-Net
+                     correction (trained on the GPU on the plain solver's own
+                     solves of the first steps) judged against it by exact
+                     FP64 residual, + FP32 V-cycle inside FP64 FGMRES; guess
+                     time included.
   plain FP64         the same FGMRES with an FP64 V-cycle, warm-started from
                      the previous step's phi (the reference's Phi2 restart),
                      timed on the same held-out steps (config.plain_fp64_ms).
+  other arms         the FP32 or FP64 V-cycle from phi_{n-1}, from the linear
+                     extrapolation and from the projection alone
+                     (config.other_arms), so that each part's gain shows.
 
 Arms of the driver:
   default            this library on the GPU (value: inputs resident in HBM;
                      e2e: host buffers through the C ABI)
   --impl reference   the reference's algorithm on the host cores: the CPU
-                     port in oracle/ (the reference itself needs PETSc 3.1,
-                     HYPRE and MPI, which are not available), each step a
-                     bounded sample of the same warm-started solve scaled to
-                     a full solve.
+                     port in oracle/ (the reference's own solve needs PETSc
+                     3.1, HYPRE and MPI, which are not available), each step a
+                     complete warm-started solve of the same workload.
 
 Multi-GPU: the solve does not shard in this library; under torchrun every
 rank runs an independent replica (weak scaling) and rank 0 reports.
@@ -421,7 +424,9 @@ def run_ours(args):
             split[key][0].append(t_x)
             split[key][1].append(st_x.iterations)
         l0 = s.kernel_launches()
+        torch.cuda.nvtx.range_push("held_out_step")   # lets ncu --nvtx-include select this arm's launches
         pb, sb, tb, ch, rr = arm_learned(u, hist)
+        torch.cuda.nvtx.range_pop()
         launches += s.kernel_launches() - l0
         ms_a.append(ta); ms_b.append(tb); its_a.append(sa.iterations); its_b.append(sb.iterations)
         chosen.append(ch); rel_prev.append(rr[0]); rel_learned.append(rr[1])

@@ -609,12 +609,12 @@ static void int_to_da(const lvl_t *l, const double *v, double *da)
         da[(((size_t)(k + 1) * l->d.my) + j + 1) * l->d.mx + i + 1] = v[((size_t)k * l->ny + j) * l->nx + i];
 }
 
-int or_mg_vcycle(void *h, const double *r_da, double *z_da)
+int or_mg_vcycle(void *h, const double *r_da, double *z_da, int nu1, int nu2, double omega)
 {
   mg_t *g = (mg_t *)h;
   lvl_t *l = &g->L[0];
   or_solve_opts o = {0};
-  o.nu1 = 2; o.nu2 = 2; o.omega = 0.8;
+  o.nu1 = nu1; o.nu2 = nu2; o.omega = omega;
   double *v = (double *)malloc(l->n * 8), *z = (double *)malloc(l->n * 8);
   da_to_int(l, r_da, v);
   precond(g, v, z, &o);

@@ -104,7 +104,7 @@ def lib():
         L.or_mg_create.restype = C.c_void_p
         L.or_mg_solve.argtypes = [C.c_void_p, dp, dp, P(SolveOpts), P(SolveStats)]
         L.or_mg_solve.restype = C.c_int
-        L.or_mg_vcycle.argtypes = [C.c_void_p, dp, dp]
+        L.or_mg_vcycle.argtypes = [C.c_void_p, dp, dp, C.c_int, C.c_int, C.c_double]
         L.or_mg_level_info.argtypes = [C.c_void_p, C.c_int, ip]
         L.or_mg_level_info.restype = C.c_int
         L.or_mg_destroy.argtypes = [C.c_void_p]
@@ -380,9 +380,9 @@ class MGSolver:
         lib().or_mg_solve(self.h, _dp(np.ascontiguousarray(b_da)), _dp(x), C.byref(self.opts), C.byref(st))
         return x, st
 
-    def vcycle(self, r_da):
+    def vcycle(self, r_da, nu1=2, nu2=2, omega=0.8):
         z = np.zeros((self.d.mz, self.d.my, self.d.mx))
-        lib().or_mg_vcycle(self.h, _dp(np.ascontiguousarray(r_da)), _dp(z))
+        lib().or_mg_vcycle(self.h, _dp(np.ascontiguousarray(r_da)), _dp(z), nu1, nu2, omega)
         return z
 
     def __del__(self):

@@ -155,7 +155,7 @@ void *or_mg_create(const or_dims *d, const double *coor, const double *nvert,
                    const or_metrics *fine_metrics, const or_solve_opts *o);
 int or_mg_solve(void *h, const double *b_da, double *x_da, const or_solve_opts *o,
                 or_solve_stats *st);
-int or_mg_vcycle(void *h, const double *r_da, double *z_da);
+int or_mg_vcycle(void *h, const double *r_da, double *z_da, int nu1, int nu2, double omega);
 int or_mg_level_info(void *h, int level, int *dims7);
 void or_mg_destroy(void *h);
 /* 1: zebra j-line Gauss-Seidel smoothing (checkerboard columns), 0: damped

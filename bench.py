@@ -415,6 +415,7 @@ def run_ours(args):
     arms = (("mixed_prev", 0, "prev"), ("mixed_extrap", 0, "extrap"), ("mixed_hist", 0, "hist"),
             ("plain_hist", 1, "hist"))
     split = {k: ([], []) for k, _, _ in arms}
+    reports = []
     for _ in range(args.steps):
         u = step_inputs(n)
         pa, sa, ta = arm_plain(u, hist)
@@ -428,6 +429,7 @@ def run_ours(args):
         pb, sb, tb, ch, rr = arm_learned(u, hist)
         torch.cuda.nvtx.range_pop()
         launches += s.kernel_launches() - l0
+        reports.append(s.guess_report())
         ms_a.append(ta); ms_b.append(tb); its_a.append(sa.iterations); its_b.append(sb.iterations)
         chosen.append(ch); rel_prev.append(rr[0]); rel_learned.append(rr[1])
         assert sa.rel_residual <= 1e-8 and sb.rel_residual <= 1e-8
@@ -516,16 +518,21 @@ def run_ours(args):
             "solver": "FGMRES(20) with one-pass classical Gram-Schmidt, FP64 residual, operator apply and Krylov; FP32 geometric "
                       "V-cycle (zebra j-line Gauss-Seidel over checkerboard columns, 1+2 sweeps; residual couplings "
                       "stored in half precision, difference form, formed inside the line kernel on the levels of at "
-                      "most 2^20 cells; dense projected solve on a 192-cell coarsest level); initial guess: the history "
-                      "projection (least squares over the last solutions' images) with the learned network's "
-                      "correction judged against it (the network run on every n-th step while it loses)",
-            "iterations": statistics.mean(its_b), "learned_guess_chosen": sum(chosen) / len(chosen),
+                      "most 2^20 cells; dense projected solve on a 192-cell coarsest level); initial guess: candidates "
+                      "from the solution history (least-squares projection over the solutions of the current operator, "
+                      "extrapolation of the newest two) and the learned network's correction of the extrapolation "
+                      "(run on every n-th step while it loses), chosen by estimated error (one V-cycle of each "
+                      "residual within 32x of the smallest, fluid mean removed; the winner's V-cycle starts FGMRES)",
+            "iterations": statistics.mean(its_b),
+            "guess_chosen": {name: sum(1 for r in reports if r[0] == code)
+                             for code, name in ((0, "projection"), (1, "network"), (2, "extrapolation"))},
             "network_evaluations": sum(1 for r in rel_learned if r >= 0),
             "initial_rel_residual_learned": (statistics.mean([r for r in rel_learned if r >= 0])
                                              if any(r >= 0 for r in rel_learned) else None),
-            "initial_rel_residual_base": statistics.mean(rel_prev),
-            "base_guess": (f"history projection over the last {args.history} solutions" if args.history
-                           else "previous step's phi"),
+            "initial_rel_residual_base": (statistics.mean([r for r in rel_prev if r >= 0])
+                                          if any(r >= 0 for r in rel_prev) else None),
+            "initial_rel_residual_chosen": statistics.mean(r[1][r[0]] for r in reports),
+            "base_guess": (f"solution history of {args.history}" if args.history else "previous step's phi"),
             "other_arms": {k: {"ms": statistics.mean(v[0]), "iterations": statistics.mean(v[1])}
                            for k, v in split.items()},
             "plain_fp64_ms": ms_a_mean, "plain_fp64_iterations": statistics.mean(its_a),

@@ -426,30 +426,57 @@ int vfs_unet_adam(vfs_unet *u, double lr, double beta1, double beta2, double eps
 int vfs_unet_set_grads(vfs_unet *u, const float *grad);
 int64_t vfs_unet_kernel_launches(vfs_unet *u);
 
-/* History projection of the initial guess (no counterpart in the
+/* Initial guess from a history of solutions (no counterpart in the
  * reference, which restarts from the previous step's Phi2,
- * poisson_hypre.c:577; Fischer's projection for successive right-hand
- * sides, CMAME 163 (1998) 193-204).  The handle keeps the last k converged
- * solutions X_j (1 <= k <= 8; 0 turns it off) and their images A X_j (b - r
- * of the solves that produced them; recomputed with the FP64 operator after
- * vfs_poisson_set_nvert).  vfs_poisson_history_guess, after
- * vfs_poisson_rhs, installs x = sum_j c_j X_j with c minimising
- * ||b - sum_j c_j A X_j||_2 as the iterate for the next solve
- * (opts.warm_start = 2), with its exact FP64 residual; the newest solution is
- * in the span, so the guess is never worse than the previous step's phi.
- * rel_res gets ||b - A x|| / ||b||.  Each converged solve appends its
- * solution.  Memory: 2 k box-sized FP64 vectors. */
+ * poisson_hypre.c:577).  The handle keeps the last k converged solutions
+ * X_j (1 <= k <= 8; 0 turns it off) and their images A X_j (b - r of the
+ * solves that produced them) under the operator assembly current when each
+ * was stored.  vfs_poisson_history_guess, after vfs_poisson_rhs, forms two
+ * candidates:
+ *   - the projection x = sum_j c_j X_j over the solutions of the current
+ *     assembly, with c minimising ||b - sum_j c_j A X_j||_2 (Fischer's
+ *     projection for successive right-hand sides, CMAME 163 (1998) 193-204);
+ *     never above the previous step's phi in residual;
+ *   - the extrapolation 2 X_0 - X_1 of the newest two solutions (its
+ *     residual from the stored images, or by an operator apply when a moving
+ *     mask made them stale);
+ * and installs the one the judge prefers as the iterate for the next solve
+ * (opts.warm_start = 2), with its exact FP64 residual.  The judge: a
+ * candidate whose residual exceeds 32x the other's loses outright (the
+ * extrapolation is not even formed when the Gram matrix predicts that);
+ * otherwise each is rated by its estimated error, the 2-norm of one V-cycle
+ * of its residual with the fluid mean removed, and the smaller wins.  A
+ * least-squares fit of the residual can leave a smooth error of small
+ * residual that the iteration removes slowly (after a mask moves, the
+ * projection's error is often several times the extrapolation's); that
+ * V-cycle then becomes the solve's first preconditioned vector, so the
+ * judging costs one V-cycle per losing candidate.  rel_res gets
+ * ||b - A x|| / ||b|| of the installed guess.  Each converged solve appends
+ * its solution.  Memory: 2 k + 4 box-sized FP64 vectors. */
 int vfs_poisson_set_history(vfs_poisson *h, int k);
 int vfs_poisson_history_guess(vfs_poisson *h, double *rel_res);
 /* Whether converged solves append to the history (default 1): 0 lets a
  * second solver sequence share the handle without entering it. */
 int vfs_poisson_history_record(vfs_poisson *h, int on);
 
-/* With a history, vfs_poisson_learned_guess judges its candidate against the
- * history projection instead of phi_{n-1}; while the network's candidate
- * keeps losing, the network runs on every `period`-th call only (the others
- * install the projection directly and report rel_res[1] = -1).  Default 1. */
+/* With a history, vfs_poisson_learned_guess puts the network's candidate
+ * before the same judge as the history's projection and the extrapolation;
+ * while the network's candidate keeps losing, the network runs on every
+ * `period`-th call only (the others judge the history's candidates alone and
+ * report rel_res[1] = -1).  Default 1.  The network is not run either when
+ * the projection's residual is below the extrapolation's by more than
+ * 1024x. */
 int vfs_poisson_set_network_period(vfs_poisson *h, int period);
+
+/* What the last vfs_poisson_history_guess / vfs_poisson_learned_guess
+ * installed (no counterpart in the reference).  *chosen: 0 the projection
+ * (or the previous step's phi when no history is kept), 1 the network's
+ * candidate, 2 the extrapolation.  rel_res[3] and est[3] (either may be
+ * NULL), indexed by those codes: each candidate's ||b - A x|| / ||b|| and
+ * its estimated error (2-norm of one V-cycle of its residual, fluid mean
+ * removed, in units of phi); -1 where the candidate was not formed or not
+ * rated. */
+int vfs_poisson_guess_report(vfs_poisson *h, int *chosen, double *rel_res, double *est);
 
 /* Learned initial guess for the current right-hand side (vfs_poisson_rhs
  * first), from phi at steps n-1 and n-2 (DA layout, host or device).  The
@@ -460,13 +487,16 @@ int vfs_poisson_set_network_period(vfs_poisson *h, int period);
  * dofs, and the dof fraction.  Its output, the correction phi_n - phi_ex in
  * units of kappa * RMS(aj * (b - A phi_ex)), is prolonged trilinearly to the
  * cells and smoothed by two passes of the 27-point binomial filter
- * (environment variable VFS_GUESS_SMOOTH sets the count).  The plain solver
- * then judges the guess: the learned guess and the previous step's phi are
- * both measured by their FP64 residual and the smaller one becomes the
- * solver's iterate (*chosen = 1 for the learned guess, 0 for the previous
- * step; rel_res[0..1] = their relative residuals).  Solve from it with
- * opts.warm_start = 2.  The network runs on the handle's stream (its stream
- * is set to it); box dims must be multiples of 8. */
+ * (environment variable VFS_GUESS_SMOOTH sets the count), and enters in 4
+ * wall-distance bands whose weights minimise the residual.  The judge of
+ * vfs_poisson_history_guess then chooses among the base (the history's
+ * projection; the previous step's phi without a history), the extrapolation
+ * phi_ex and the network's guess (formed only when its predicted residual is
+ * within 32x of the best).  *chosen: 0 base, 1 network, 2 extrapolation;
+ * rel_res[0] = the base's relative residual (-1 without one), rel_res[1] =
+ * the network guess's (the extrapolation's when every band weight is 0).
+ * Solve from it with opts.warm_start = 2.  The network runs on the handle's
+ * stream (its stream is set to it); box dims must be multiples of 8. */
 int vfs_poisson_learned_guess(vfs_poisson *h, vfs_unet *u, const double *phi_nm1, const double *phi_nm2,
                               double kappa, int *chosen, double *rel_res);
 

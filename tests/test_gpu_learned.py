@@ -2,12 +2,12 @@
 (marked gpu): samples from the plain solver, training by the library's own
 kernels, then held-out steps where the plain solver judges the guess.
 
-What the test pins: the guess is never worse than the linear
-extrapolation it corrects (its band weights are a least-squares fit on the
-FP64 residual, and zero weights give the extrapolation back), it beats the
-previous-step warm start (the reference's Phi2 restart, the fallback), and
-the solve from it converges in fewer iterations than from the previous
-step.
+What the test pins: the network's guess is never worse in residual than
+the linear extrapolation it corrects (its band weights are a least-squares
+fit on the FP64 residual, and zero weights give the extrapolation back);
+the judge installs the network's guess or the extrapolation rather than the
+previous-step warm start (the reference's Phi2 restart), and the solve from
+it converges in fewer iterations than from the previous step.
 """
 import numpy as np
 import pytest
@@ -42,7 +42,7 @@ def test_learned_guess_on_sequence(cuda_lib):
     for a, u, p in zip(learned, untrained, prev):
         assert a["rel"] <= 1e-8
         assert a["rel_learned"] <= u["rel_learned"] * (1 + 1e-6)   # never worse than the extrapolation
-        assert a["chosen"] == 1 and a["rel_learned"] < a["rel_prev"]
+        assert a["chosen"] in (1, 2) and a["rel_learned"] < a["rel_prev"]
         assert a["iterations"] < p["iterations"]
     s.close()
     net.close()
@@ -84,7 +84,7 @@ def test_speculative_first_step_bitexact(cuda_lib, monkeypatch):
         runs[spec] = ([r["iterations"] for r in recs], [h.clone() for h in hist2], st.iterations, phi.clone(),
                       st2.iterations, phi2.clone())
         assert all(r["rel"] <= 1e-8 for r in recs) and st.rel_residual <= 1e-8 and st2.rel_residual <= 1e-8
-        assert all(r["chosen"] == 1 for r in recs)
+        assert all(r["chosen"] == 2 for r in recs)   # the extrapolation (band weights 0)
         s.close()
         net.close()
     a, b = runs["1"], runs["0"]

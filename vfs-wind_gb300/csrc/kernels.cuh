@@ -157,6 +157,8 @@ __global__ void k_hist_dots(size_t n, HistPtrs Y, int k, const double *v, double
 __global__ void k_hist_combine(size_t n, HistPtrs X, HistPtrs Y, int k, const double *c, const double *b, double *x,
                                double *r, double *partial);
 __global__ void k_hist_push(size_t n, const double *x, const double *b, const double *r, double *Xs, double *Ys);
+__global__ void k_fluid_moments(size_t n, const uint8_t *fluid, const double *z, double mean, int pass,
+                                double *partial);
 
 // Hand-off from a handle to the surface search (ibm.cu): its stream, grid,
 // DA-layout cell centres and launch counter.

@@ -459,7 +459,7 @@ struct vfs_poisson {
   double *hbuf = nullptr;  // pinned host readback
   // learned initial guess: extrapolated phi, plane sums, feature planes and
   // network output (box layout, allocated on first use)
-  double *gex = nullptr, *gsum = nullptr;
+  double *gex = nullptr, *gsum = nullptr, *gnet = nullptr;  // gnet: the network's guess
   float *gfeat = nullptr, *gtgt = nullptr, *gfc = nullptr, *gout = nullptr, *gof[2] = {nullptr, nullptr};
   int gsmooth = 2;  // binomial passes over the prolonged correction
   std::vector<IbmBody> ibm_bodies;  // IB node records per body (ibm.cu)
@@ -474,22 +474,33 @@ struct vfs_poisson {
   double *ls_rho = nullptr, *ls_level = nullptr;
   int ls_on = 0, ls_bc3 = 0, ls_bc4 = 0, ls_bc5 = 0;
   int line_cols_cap = 0;  // cap on the line kernels' columns per block (0: none)
-  // history projection of the initial guess: the last hist_cap solutions X_j
-  // (FGMRES iterates before the mean removal) and their images Y_j = A X_j
-  // (b - r of the solves that produced them), a ring with the newest at
-  // hist_head - 1, and their Gram matrix G_ij = Y_i . Y_j (host)
+  // history of converged solutions for the initial guess: the last hist_cap
+  // solutions X_j (FGMRES iterates before the mean removal) and their images
+  // Y_j = A X_j (b - r of the solves that produced them) under the operator
+  // assembly hist_ver[j], a ring with the newest at hist_head - 1, and the
+  // Gram matrix G_ij = Y_i . Y_j (host).  The projection uses the slots of
+  // the current assembly only; the extrapolation uses the newest two.
   int hist_cap = 0, hist_cnt = 0, hist_head = 0;
   double *hist_X[kHistMax] = {}, *hist_Y[kHistMax] = {};
+  uint64_t hist_ver[kHistMax] = {};
   double hist_G[kHistMax][kHistMax] = {};
-  double *hist_x = nullptr, *hist_r = nullptr;  // the projection and its residual
-  uint64_t op_version = 0, hist_op_version = 0;  // operator assemblies seen
+  double *hist_x = nullptr, *hist_r = nullptr;    // the projection and its residual
+  double *hist_ex = nullptr, *hist_er = nullptr;  // the extrapolation and its residual
+  double *hist_coef = nullptr;                    // combination coefficients (device)
+  uint64_t op_version = 0;                        // operator assemblies seen
   // the learned guess runs its network on every net_period-th call while
-  // its candidate keeps losing to the history projection (net_wait: calls
-  // left to skip)
+  // its candidate keeps losing (net_wait: calls left to skip)
   int net_period = 1, net_wait = 0;
   bool hist_record = true;  // converged solves append to the history
   double r0_norm = 0.;
   bool r0_valid = false;
+  // Z_0 of the next solve formed by the guess's judge: one V-cycle of the
+  // installed residual divided by its norm, under the options z0_opts
+  bool z0_valid = false;
+  vfs_solve_opts z0_opts{};
+  // what the last guess installed (vfs_poisson_guess_report)
+  int guess_chosen = -1;
+  double guess_rel[3] = {-1., -1., -1.}, guess_est[3] = {-1., -1., -1.};
   // Speculative first Arnoldi step: a learned guess that expects the plain
   // extrapolation to win (the previous guess did, with every band weight 0)
   // enqueues step 0 of the next solve on the handle's stream while the
@@ -1206,6 +1217,11 @@ int residual_norm(vfs_poisson *h, const double *x, double *r, double *norm) {
   return VFS_OK;
 }
 
+int ensure_krylov(vfs_poisson *h, int m);
+void resolve_opts(vfs_solve_opts &o);
+// hbuf offset of the history combinations' coefficients (kHistMax + 2)
+constexpr int kHistStage = 960;
+
 // ---- history projection of the initial guess (Fischer's projection for
 // successive right-hand sides, CMAME 163 (1998) 193-204) ----
 HistPtrs hist_ptrs(double *const *a, int k) {
@@ -1226,58 +1242,73 @@ int hist_gram_row(vfs_poisson *h, int s) {
   return VFS_OK;
 }
 
-// after a new operator assembly: the stored solutions' images under it
-int hist_refresh(vfs_poisson *h) {
-  if (h->hist_op_version == h->op_version) return VFS_OK;
-  for (int j = 0; j < h->hist_cnt; j++)
-    LAUNCH(h, k_apply64, box_grid(h->box), 128, h->box, h->A0, (const double *)h->hist_X[j], h->hist_Y[j]);
-  for (int j = 0; j < h->hist_cnt; j++) TRY(hist_gram_row(h, j));
-  h->hist_op_version = h->op_version;
-  return VFS_OK;
+// slot of the i-th newest stored solution
+int hist_slot(const vfs_poisson *h, int i) {
+  return ((h->hist_head - 1 - i) % h->hist_cap + h->hist_cap) % h->hist_cap;
+}
+
+// the slots stored under the current operator assembly, newest first (a
+// moving mask makes the older images stale: they are not recomputed)
+int hist_fresh(const vfs_poisson *h, int *sl) {
+  int nf = 0;
+  for (int i = 0; i < h->hist_cnt; i++) {
+    const int q = hist_slot(h, i);
+    if (h->hist_ver[q] == h->op_version) sl[nf++] = q;
+  }
+  return nf;
 }
 
 // store a converged solve: the iterate x and its image b - r (V_0 holds the
-// solve's final FP64 residual r = b - A x)
+// solve's final FP64 residual r = b - A x) under the current assembly
 int hist_push(vfs_poisson *h) {
   if (!h->hist_cap) return VFS_OK;
-  TRY(hist_refresh(h));
   const int s = h->hist_head;
   LAUNCH(h, k_hist_push, kRedBlocks, 256, h->box.n(), (const double *)h->x, (const double *)h->b,
          (const double *)h->V[0], h->hist_X[s], h->hist_Y[s]);
+  h->hist_ver[s] = h->op_version;
   h->hist_head = (s + 1) % h->hist_cap;
   if (h->hist_cnt < h->hist_cap) h->hist_cnt++;
   return hist_gram_row(h, s);
 }
 
 // the projection x = X c, r = b - Y c minimising ||b - Y c|| over the
-// stored images: normal equations G c = Y^T b by a Cholesky factorisation
-// taken newest first, where a vector whose pivot falls below 1e-13 of its
-// Gram diagonal adds nothing new and keeps the coefficient 0 (the images
-// of successive solutions are nearly parallel).  The newest solution alone
-// is in the span, so the result is never worse than the previous step's phi.
-int hist_project(vfs_poisson *h, double *rnorm, double *bnorm) {
-  TRY(hist_refresh(h));
-  const int k = h->hist_cnt;
+// stored images of the current assembly: normal equations G c = Y^T b by a
+// Cholesky factorisation taken newest first, where a vector whose pivot
+// falls below 1e-13 of its Gram diagonal adds nothing new and keeps the
+// coefficient 0 (the images of successive solutions are nearly parallel).
+// The newest solution alone is in the span, so the result's residual is
+// never above the previous step's phi's.  *rext receives the residual norm
+// of the extrapolation 2 X_0 - X_1 of the newest two solutions, predicted
+// from the Gram matrix when both are of the current assembly (else -1).
+int hist_project(vfs_poisson *h, double *rnorm, double *bnorm, double *rext) {
+  int sl[kHistMax];
+  const int k = hist_fresh(h, sl);
+  *rext = -1.;
+  if (k == 0) return fail(VFS_ESTATE, "no stored solution of the current operator");
   const size_t n = h->box.n();
-  LAUNCH(h, k_hist_dots, kRedBlocks, 256, n, hist_ptrs(h->hist_Y, k), k, (const double *)h->b, h->partial);
+  double *Xp[kHistMax], *Yp[kHistMax];
+  for (int i = 0; i < k; i++) {
+    Xp[i] = h->hist_X[sl[i]];
+    Yp[i] = h->hist_Y[sl[i]];
+  }
+  LAUNCH(h, k_hist_dots, kRedBlocks, 256, n, hist_ptrs(Yp, k), k, (const double *)h->b, h->partial);
   double g[kHistMax + 1];
   TRY(reduce_read(h, kRedBlocks, k + 1, g));
   int ord[kHistMax], na = 0;
   double L[kHistMax][kHistMax] = {};
   for (int i = 0; i < k; i++) {
-    const int sl = ((h->hist_head - 1 - i) % h->hist_cap + h->hist_cap) % h->hist_cap;
     double row[kHistMax];
     for (int q = 0; q < na; q++) {
-      double v = h->hist_G[sl][ord[q]];
+      double v = h->hist_G[sl[i]][sl[ord[q]]];
       for (int t = 0; t < q; t++) v -= row[t] * L[q][t];
       row[q] = v / L[q][q];
     }
-    double piv = h->hist_G[sl][sl];
+    double piv = h->hist_G[sl[i]][sl[i]];
     for (int t = 0; t < na; t++) piv -= row[t] * row[t];
-    if (!(piv > 1e-13 * h->hist_G[sl][sl])) continue;
+    if (!(piv > 1e-13 * h->hist_G[sl[i]][sl[i]])) continue;
     for (int t = 0; t < na; t++) L[na][t] = row[t];
     L[na][na] = std::sqrt(piv);
-    ord[na++] = sl;
+    ord[na++] = i;
   }
   double z[kHistMax], cc[kHistMax] = {}, c[kHistMax] = {};
   for (int p = 0; p < na; p++) {
@@ -1291,15 +1322,179 @@ int hist_project(vfs_poisson *h, double *rnorm, double *bnorm) {
     cc[p] = v / L[p][p];
   }
   for (int p = 0; p < na; p++) c[ord[p]] = cc[p];
-  for (int j = 0; j < k; j++) h->hbuf[464 + j] = c[j];
-  CUDA_TRY(cudaMemcpyAsync(h->coef, h->hbuf + 464, k * 8, cudaMemcpyHostToDevice, h->stream));
-  LAUNCH(h, k_hist_combine, kRedBlocks, 256, n, hist_ptrs(h->hist_X, k), hist_ptrs(h->hist_Y, k), k,
-         (const double *)h->coef, (const double *)h->b, h->hist_x, h->hist_r, h->partial);
+  for (int j = 0; j < k; j++) h->hbuf[kHistStage + j] = c[j];
+  CUDA_TRY(cudaMemcpyAsync(h->hist_coef, h->hbuf + kHistStage, k * 8, cudaMemcpyHostToDevice, h->stream));
+  LAUNCH(h, k_hist_combine, kRedBlocks, 256, n, hist_ptrs(Xp, k), hist_ptrs(Yp, k), k,
+         (const double *)h->hist_coef, (const double *)h->b, h->hist_x, h->hist_r, h->partial);
   double rr;
   TRY(reduce_read(h, kRedBlocks, 1, &rr));
   *rnorm = std::sqrt(std::max(rr, 0.));
   *bnorm = std::sqrt(std::max(g[k], 0.));
+  if (k >= 2 && sl[0] == hist_slot(h, 0) && sl[1] == hist_slot(h, 1)) {
+    const double G00 = h->hist_G[sl[0]][sl[0]], G01 = h->hist_G[sl[0]][sl[1]], G11 = h->hist_G[sl[1]][sl[1]];
+    const double e2 = g[k] - 2. * (2. * g[0] - g[1]) + 4. * G00 - 4. * G01 + G11;
+    *rext = std::sqrt(std::max(e2, 0.));
+  }
   return VFS_OK;
+}
+
+// the extrapolation 2 X_0 - X_1 of the newest two stored solutions (X_0
+// alone when one is stored) into hist_ex, and its FP64 residual into
+// hist_er: from the stored images when both belong to the current
+// assembly, otherwise by an operator apply
+int hist_extrap(vfs_poisson *h, double *rnorm) {
+  const int k = std::min(h->hist_cnt, 2);
+  if (k == 0) return fail(VFS_ESTATE, "no stored solution");
+  const size_t n = h->box.n();
+  const int s0 = hist_slot(h, 0), s1 = hist_slot(h, k - 1);
+  double *Xp[2] = {h->hist_X[s0], h->hist_X[s1]}, *Yp[2] = {h->hist_Y[s0], h->hist_Y[s1]};
+  const bool fresh = h->hist_ver[s0] == h->op_version && h->hist_ver[s1] == h->op_version;
+  h->hbuf[kHistStage + kHistMax] = k > 1 ? 2. : 1.;
+  h->hbuf[kHistStage + kHistMax + 1] = -1.;
+  CUDA_TRY(cudaMemcpyAsync(h->hist_coef + kHistMax, h->hbuf + kHistStage + kHistMax, 2 * 8, cudaMemcpyHostToDevice,
+                           h->stream));
+  // (with stale images the combination's residual is formed again below)
+  LAUNCH(h, k_hist_combine, kRedBlocks, 256, n, hist_ptrs(Xp, k), hist_ptrs(Yp, k), k,
+         (const double *)(h->hist_coef + kHistMax), (const double *)h->b, h->hist_ex, h->hist_er, h->partial);
+  if (fresh) {
+    double rr;
+    TRY(reduce_read(h, kRedBlocks, 1, &rr));
+    *rnorm = std::sqrt(std::max(rr, 0.));
+    return VFS_OK;
+  }
+  return residual_norm(h, h->hist_ex, h->hist_er, rnorm);
+}
+
+// A candidate initial guess: its iterate, its FP64 residual and norm, the
+// code reported for it (0 projection or previous phi, 1 network, 2
+// extrapolation), and a V-cycle of its residual already formed (or null).
+struct GuessCand {
+  double *x, *r;
+  double beta;
+  int code;
+  const double *zready;
+  double est;
+};
+
+// The judge among candidate guesses.  Their FP64 residuals alone mislead:
+// a least-squares fit of the residual can leave a large smooth error that
+// has a small residual and that the preconditioned iteration removes
+// slowly, while an extrapolation's larger residual can sit in components
+// the first V-cycle removes.  Each candidate within kJudgeGate of the
+// smallest residual is therefore rated by its estimated error: one V-cycle
+// of its residual (the solver's default preconditioner), the fluid mean
+// removed (the operator's constant null space), 2-norm.  The winner's
+// V-cycle, divided by its residual norm, is Z_0 of the next solve.
+constexpr double kJudgeGate = 32.;
+int judge(vfs_poisson *h, GuessCand *c, int nc, int *win) {
+  double bmin = c[0].beta;
+  for (int i = 1; i < nc; i++) bmin = std::min(bmin, c[i].beta);
+  int live[4], nl = 0;
+  for (int i = 0; i < nc; i++) {
+    c[i].est = -1.;
+    if (c[i].beta <= kJudgeGate * bmin) live[nl++] = i;
+  }
+  h->z0_valid = false;
+  if (nl == 1 || bmin == 0.) {
+    int b = 0;
+    for (int i = 1; i < nc; i++) if (c[i].beta < c[b].beta) b = i;
+    *win = b;
+    return VFS_OK;
+  }
+  vfs_solve_opts so;
+  vfs_poisson_default_opts(&so);
+  resolve_opts(so);
+  TRY(ensure_krylov(h, std::max(h->m_alloc, 20)));
+  const size_t n = h->box.n();
+  int best = -1;
+  const double *zbest = nullptr;
+  for (int q = 0; q < nl; q++) {
+    GuessCand &cd = c[live[q]];
+    const double *z = cd.zready;
+    if (!z) {
+      TRY(precondition(h, cd.r, 1.0 / cd.beta, nullptr, nullptr, h->Z[1 + q], so));
+      z = h->Z[1 + q];
+    }
+    LAUNCH(h, k_fluid_moments, kRedBlocks, 256, n, (const uint8_t *)h->fluid, z, 0., 0, h->partial);
+    double m[2];
+    TRY(reduce_read(h, kRedBlocks, 2, m));
+    LAUNCH(h, k_fluid_moments, kRedBlocks, 256, n, (const uint8_t *)h->fluid, z, m[1] > 0. ? m[0] / m[1] : 0., 1,
+           h->partial);
+    double d;
+    TRY(reduce_read(h, kRedBlocks, 1, &d));
+    cd.est = cd.beta * std::sqrt(std::max(d, 0.));
+    if (best < 0 || cd.est < c[best].est) {
+      best = live[q];
+      zbest = z;
+    }
+  }
+  if (zbest != h->Z[0]) CUDA_TRY(cudaMemcpyAsync(h->Z[0], zbest, n * 8, cudaMemcpyDeviceToDevice, h->stream));
+  h->z0_valid = true;
+  h->z0_opts = so;
+  *win = best;
+  return VFS_OK;
+}
+
+// make candidate c the solver's iterate (warm_start 2): its buffer trades
+// places with x (queued work holds the pointers it was launched with; none
+// writes these buffers later) and its residual becomes FGMRES's start
+void install_guess(vfs_poisson *h, GuessCand &c) {
+  if (c.x != h->x) {
+    double *old = h->x;
+    h->x = c.x;
+    if (h->gex == c.x) h->gex = old;
+    else if (h->gnet == c.x) h->gnet = old;
+    else if (h->hist_x == c.x) h->hist_x = old;
+    else if (h->hist_ex == c.x) h->hist_ex = old;
+  }
+  h->r0 = c.r;
+  h->r0_norm = c.beta;
+  h->r0_valid = true;
+}
+
+// The history's candidates for the next solve's guess: the projection over
+// the slots of the current assembly (code 0) and the extrapolation of the
+// newest two solutions (code 2).  The extrapolation is formed only when it
+// can pass the judge's gate: its residual, predicted from the Gram matrix
+// when both solutions are of the current assembly, within kJudgeGate of the
+// projection's.  *far: the prediction exceeds the projection's residual by
+// more than kNetGate.  *bnorm: ||b||.
+constexpr double kNetGate = 1024.;
+int history_candidates(vfs_poisson *h, GuessCand *c, int *nc, double *bnorm, bool *far) {
+  int sl[kHistMax];
+  const int nf = hist_fresh(h, sl);
+  *nc = 0;
+  *far = false;
+  if (nf) {
+    double rp, re;
+    TRY(hist_project(h, &rp, bnorm, &re));
+    c[(*nc)++] = GuessCand{h->hist_x, h->hist_r, rp, 0, nullptr, -1.};
+    if (h->hist_cnt < 2) return VFS_OK;  // the extrapolation would be the projection's vector
+    if (re >= 0.) {
+      *far = re > kNetGate * rp;
+      if (re > kJudgeGate * rp) return VFS_OK;
+    }
+  } else {
+    LAUNCH(h, k_sumsq, kRedBlocks, 256, h->box.n(), h->b, h->partial);
+    double bb;
+    TRY(reduce_read(h, kRedBlocks, 1, &bb));
+    *bnorm = std::sqrt(std::max(bb, 0.));
+  }
+  double rex;
+  TRY(hist_extrap(h, &rex));
+  c[(*nc)++] = GuessCand{h->hist_ex, h->hist_er, rex, 2, nullptr, -1.};
+  return VFS_OK;
+}
+
+// what the guess installed, for vfs_poisson_guess_report: per candidate
+// code its residual relative to ||b|| and its estimated error
+void guess_report(vfs_poisson *h, const GuessCand *c, int nc, int w, double bnorm) {
+  for (int q = 0; q < 3; q++) h->guess_rel[q] = h->guess_est[q] = -1.;
+  for (int i = 0; i < nc; i++) {
+    h->guess_rel[c[i].code] = bnorm > 0. ? c[i].beta / bnorm : 0.;
+    h->guess_est[c[i].code] = c[i].est;
+  }
+  h->guess_chosen = c[w].code;
 }
 
 int ensure_krylov(vfs_poisson *h, int m) {
@@ -1367,13 +1562,14 @@ void cgs_dots(vfs_poisson *h, int nv, int nb, size_t n, int v0, const double *w)
 // the first basis norm (apart from the rows reduce_read and FGMRES use)
 constexpr int kSpecHb = 620, kSpecStage = 610;
 
-// Enqueue Arnoldi step jj of FGMRES: precondition V_jj, apply A, orthogonalise
-// (orth 0 or DCGS2), reduce the new vector's norm and copy the Hessenberg
-// data to hbuf + hb (orth 0: h at hb + 0..jj; the norm^2 at hb + kGsR + 3).
-int arnoldi_enqueue(vfs_poisson *h, int jj, int nbd, const vfs_solve_opts &o, int hb) {
+// Enqueue Arnoldi step jj of FGMRES: precondition V_jj (unless Z_jj holds it
+// already: have_z), apply A, orthogonalise (orth 0 or DCGS2), reduce the new
+// vector's norm and copy the Hessenberg data to hbuf + hb (orth 0: h at
+// hb + 0..jj; the norm^2 at hb + kGsR + 3).
+int arnoldi_enqueue(vfs_poisson *h, int jj, int nbd, const vfs_solve_opts &o, int hb, bool have_z = false) {
   const size_t n = h->box.n();
   const double *const *dV = (const double *const *)h->dV;
-  TRY(precondition(h, h->V[jj], 1.0, h->dsv + 2 * jj + 1, h->dsv32 + jj, h->Z[jj], o));
+  if (!have_z) TRY(precondition(h, h->V[jj], 1.0, h->dsv + 2 * jj + 1, h->dsv32 + jj, h->Z[jj], o));
   if (h->phase && hb == 0) cudaEventRecord(h->phev[1], h->stream);
   double *w = h->V[jj + 1];
   LAUNCH(h, k_apply64, box_grid(h->box), 128, h->box, h->A0, h->Z[jj], w);
@@ -1425,7 +1621,7 @@ int fgmres(vfs_poisson *h, const vfs_solve_opts &o, vfs_solve_stats *st) {
   const size_t n = h->box.n();
   const int m = o.restart;
   // a larger basis is allocated afresh: the speculative step's vectors go
-  if (m > h->m_alloc) h->spec_valid = false;
+  if (m > h->m_alloc) h->spec_valid = h->z0_valid = false;
   TRY(ensure_krylov(h, m));
   const int nbd = (int)((n + 256 * kGsTile - 1) / (256 * kGsTile));
   double bn2;
@@ -1446,7 +1642,10 @@ int fgmres(vfs_poisson *h, const vfs_solve_opts &o, vfs_solve_stats *st) {
   }
   // step 0 enqueued by the learned guess (V_0 = the guess's residual)
   const bool resume = o.warm_start == 2 && h->r0_valid && h->spec_valid && spec_matches(o, h->spec_opts);
+  // Z_0 formed by the guess's judge (one V-cycle of the installed residual)
+  const bool have_z0 = !resume && o.warm_start == 2 && h->r0_valid && h->z0_valid && spec_matches(o, h->z0_opts);
   h->spec_valid = false;
+  h->z0_valid = false;
   if (resume) {
     beta = h->r0_norm;
   } else if (o.warm_start == 2 && h->r0_valid) {  // residual formed by the guess
@@ -1493,7 +1692,7 @@ int fgmres(vfs_poisson *h, const vfs_solve_opts &o, vfs_solve_stats *st) {
       if (h->phase) cudaEventRecord(h->phev[0], h->stream);
       const bool pre = resume && it == 0 && jj == 0;  // enqueued by the guess
       const int hb = pre ? kSpecHb : 0;
-      if (!pre) TRY(arnoldi_enqueue(h, jj, nbd, o, 0));
+      if (!pre) TRY(arnoldi_enqueue(h, jj, nbd, o, 0, have_z0 && it == 0 && jj == 0));
       const auto t2 = h->phase ? std::chrono::steady_clock::now() : t0;
       TRY(sync(h));
       const auto t3 = h->phase ? std::chrono::steady_clock::now() : t0;
@@ -1747,7 +1946,7 @@ int vfs_poisson_set_nvert(vfs_poisson *h, const double *nvert) {
   h->have_nvert = true;
   h->have_rhs = false;
   h->r0_valid = false;
-  h->op_version++;  // stored history images belong to the previous operator
+  h->op_version++;  // stored history images belong to the previous assembly
   return VFS_OK;
 }
 
@@ -2026,6 +2225,7 @@ int guess_buffers(vfs_poisson *h) {
     TRY(dalloc(h, &h->gof[1], n));
     TRY(dalloc(h, &h->rprev, n));
     TRY(dalloc(h, &h->rlearn, n));
+    TRY(dalloc(h, &h->gnet, n));
     TRY(dalloc(h, &h->prev32, n));
     const char *e = getenv("VFS_GUESS_SMOOTH");
     if (e) h->gsmooth = std::max(0, std::min(8, atoi(e)));
@@ -2111,9 +2311,11 @@ int vfs_poisson_set_history(vfs_poisson *h, int k) {
     h->hist_X[j] = h->hist_Y[j] = nullptr;
   }
   if (h->r0 == h->hist_r) h->r0_valid = false;
-  dfree(h, h->hist_x);
-  dfree(h, h->hist_r);
-  h->hist_x = h->hist_r = nullptr;
+  if (h->r0 == h->hist_er) h->r0_valid = false;
+  for (double **p : {&h->hist_x, &h->hist_r, &h->hist_ex, &h->hist_er, &h->hist_coef}) {
+    dfree(h, *p);
+    *p = nullptr;
+  }
   h->hist_cap = h->hist_cnt = h->hist_head = 0;
   const size_t n = h->box.n();
   for (int j = 0; j < k; j++) {
@@ -2123,9 +2325,11 @@ int vfs_poisson_set_history(vfs_poisson *h, int k) {
   if (k) {
     TRY(dalloc(h, &h->hist_x, n));
     TRY(dalloc(h, &h->hist_r, n));
+    TRY(dalloc(h, &h->hist_ex, n));
+    TRY(dalloc(h, &h->hist_er, n));
+    TRY(dalloc(h, &h->hist_coef, 2 * kHistMax));
   }
   h->hist_cap = k;
-  h->hist_op_version = h->op_version;
   return VFS_OK;
 }
 
@@ -2143,19 +2347,32 @@ int vfs_poisson_set_network_period(vfs_poisson *h, int period) {
   return VFS_OK;
 }
 
+int vfs_poisson_guess_report(vfs_poisson *h, int *chosen, double *rel_res, double *est) {
+  if (!h) return fail(VFS_EINVAL, "null handle");
+  if (h->guess_chosen < 0) return fail(VFS_ESTATE, "no guess installed yet");
+  if (chosen) *chosen = h->guess_chosen;
+  for (int q = 0; q < 3; q++) {
+    if (rel_res) rel_res[q] = h->guess_rel[q];
+    if (est) est[q] = h->guess_est[q];
+  }
+  return VFS_OK;
+}
+
 int vfs_poisson_history_guess(vfs_poisson *h, double *rel_res) {
   if (!h) return fail(VFS_EINVAL, "null handle");
   if (!h->have_rhs) return fail(VFS_ESTATE, "rhs must come before the guess");
   if (!h->hist_cnt) return fail(VFS_ESTATE, "no stored solution (vfs_poisson_set_history, then a solve)");
-  double rn, bn;
-  TRY(hist_project(h, &rn, &bn));
-  std::swap(h->x, h->hist_x);
-  h->r0 = h->hist_r;
-  h->r0_norm = rn;
-  h->r0_valid = true;
-  h->spec_valid = false;
-  h->spec_next = false;
-  if (rel_res) *rel_res = bn > 0. ? rn / bn : 0.;
+  h->r0_valid = h->spec_valid = h->spec_next = h->z0_valid = false;
+  GuessCand c[2];
+  int nc = 0;
+  double bn = 0.;
+  bool far = false;
+  TRY(history_candidates(h, c, &nc, &bn, &far));
+  int w = 0;
+  TRY(judge(h, c, nc, &w));
+  install_guess(h, c[w]);
+  guess_report(h, c, nc, w, bn);
+  if (rel_res) *rel_res = bn > 0. ? c[w].beta / bn : 0.;
   return sync(h);
 }
 
@@ -2163,24 +2380,33 @@ int vfs_poisson_learned_guess(vfs_poisson *h, vfs_unet *u, const double *phi_nm1
                               double kappa, int *chosen, double *rel_res) {
   if (!h || !u) return fail(VFS_EINVAL, "null argument");
   const Box b = h->box;
-  h->r0_valid = false;
-  h->spec_valid = false;
+  h->r0_valid = h->spec_valid = h->z0_valid = false;
   if (h->phase) cudaEventRecord(h->phev[0], h->stream);
-  // with a solution history the candidate the network must beat is its
-  // projection (never worse than the previous step's phi), not phi_{n-1}
+  // with a solution history the network's candidate competes with the
+  // projection and the extrapolation of the stored solutions
   const bool use_hist = h->hist_cnt > 0;
-  double r_hist = 0., b_hist = 0.;
-  if (use_hist) TRY(hist_project(h, &r_hist, &b_hist));
-  if (use_hist && h->net_wait > 0) {  // the network sits this call out
-    h->net_wait--;
-    std::swap(h->x, h->hist_x);
-    h->r0 = h->hist_r;
-    h->r0_norm = r_hist;
-    h->r0_valid = true;
+  GuessCand hc[2];
+  int nh = 0;
+  double bn_h = 0.;
+  bool far = false;
+  if (use_hist) {
+    if (!h->have_rhs) return fail(VFS_ESTATE, "rhs must come before the guess");
+    TRY(history_candidates(h, hc, &nh, &bn_h, &far));
+  }
+  // the network sits this call out: between its periodic runs while it
+  // loses, or when the projection's residual is below the extrapolation's
+  // by more than kNetGate (the network's correction of the extrapolation
+  // would have to cut its residual by more than the judge's gate)
+  if (use_hist && (far || h->net_wait > 0)) {
+    if (!far) h->net_wait--;
+    int w = 0;
+    TRY(judge(h, hc, nh, &w));
+    install_guess(h, hc[w]);
     h->spec_next = false;
-    if (chosen) *chosen = 0;
+    guess_report(h, hc, nh, w, bn_h);
+    if (chosen) *chosen = hc[w].code;
     if (rel_res) {
-      rel_res[0] = b_hist > 0. ? r_hist / b_hist : 0.;
+      rel_res[0] = bn_h > 0. ? hc[w].beta / bn_h : 0.;
       rel_res[1] = -1.;
     }
     return sync(h);
@@ -2316,11 +2542,11 @@ int vfs_poisson_learned_guess(vfs_poisson *h, vfs_unet *u, const double *phi_nm1
   }
   if (h->phase)
     fprintf(stderr, "vfs guess band weights: %.4g %.4g %.4g %.4g\n", bw.a[0], bw.a[1], bw.a[2], bw.a[3]);
-  // the plain solver judges: keep whichever of the learned guess and the
-  // previous step's phi has the smaller FP64 residual.  The fit predicts
-  // the learned one, ||r_ex||^2 - 2 alpha.g + alpha.G.alpha; when that is
-  // clearly above the previous step's the learned guess is not formed,
-  // otherwise it is composed and its FP64 residual decides.
+  // the candidates: the base (the history's projection, or the previous
+  // step's phi without a history), the extrapolation and, when a band
+  // weight is not 0, the network's correction of it; the fit predicts the
+  // last one's residual, ||r_ex||^2 - 2 alpha.g + alpha.G.alpha, and it is
+  // composed only when that could pass the judge's gate
   double r2 = nrm[0];
   {
     int q = 0;
@@ -2329,69 +2555,65 @@ int vfs_poisson_learned_guess(vfs_poisson *h, vfs_unet *u, const double *phi_nm1
       for (int v = u2; v < kGuessBands; v++, q++) r2 += (u2 == v ? 1. : 2.) * bw.a[u2] * bw.a[v] * gm[q];
     }
   }
-  const double r_prev = use_hist ? r_hist : std::sqrt(nrm[1]);
   const double nb = nrm[2] > 0. ? std::sqrt(nrm[2]) : 1.;
-  double r_learn = std::sqrt(std::max(r2, 0.));
-  bool learned = false;
-  bool weighted = false;
-  for (int u2 = 0; u2 < kGuessBands; u2++) weighted = weighted || bw.a[u2] != 0.;
-  if (!weighted) {
-    // all band weights 0: the learned guess is the extrapolation, whose
-    // residual the features step already formed
-    r_learn = std::sqrt(nrm[0]);
-    learned = r_learn < r_prev;
-    if (learned) {
-      // the extrapolation becomes the iterate and its residual the learned
-      // candidate's: the box vectors trade places (queued work holds the
-      // pointers it was launched with; none writes these buffers later)
-      std::swap(h->x, h->gex);
-      std::swap(h->r, h->rlearn);
-    }
-  } else if (r_learn < 1.1 * r_prev) {
-    LAUNCH(h, k_guess_compose, kRedBlocks, 256, b, h->rowtype0, h->gex, h->gof[cur], kappa, h->gsum, bw, h->x);
-    LAUNCH(h, k_residual64, box_grid(h->box), 128, h->box, h->A0, h->x, h->b, h->rlearn, h->partial);
-    double s2 = 0.;
-    const dim3 gr = box_grid(h->box);
-    TRY(reduce_read(h, (int)(gr.x * gr.y * gr.z), 1, &s2));
-    r_learn = std::sqrt(s2);
-    learned = r_learn < r_prev;
-  }
-  double r_prev64 = r_prev;
-  if (!learned && use_hist) {
-    // the projection stays: its residual is exact already
-    std::swap(h->x, h->hist_x);
-  } else if (!learned) {
-    // the previous step's phi stays: its FP64 residual is FGMRES's start
-    CUDA_TRY(cudaMemcpyAsync(h->x, h->Z[h->m_alloc - 1], n * 8, cudaMemcpyDeviceToDevice, h->stream));
+  GuessCand c[3];
+  int nc = 0;
+  if (use_hist && hc[0].code == 0) {
+    c[nc++] = hc[0];
+  } else if (!use_hist) {
+    // the previous step's phi: its FP64 residual
+    CUDA_TRY(cudaMemcpyAsync(h->x, h->Z[h->m_alloc - 1], b.n() * 8, cudaMemcpyDeviceToDevice, h->stream));
     const dim3 gr = box_grid(h->box);
     LAUNCH(h, k_residual64, gr, 128, h->box, h->A0, h->x, h->b, h->rprev, h->partial);
     double s2 = 0.;
     TRY(reduce_read(h, (int)(gr.x * gr.y * gr.z), 1, &s2));
-    r_prev64 = std::sqrt(s2);
+    c[nc++] = GuessCand{h->x, h->rprev, std::sqrt(s2), 0, nullptr, -1.};
   }
-  h->r0 = learned ? h->rlearn : (use_hist ? h->hist_r : h->rprev);
+  const int iex = nc;
+  c[nc++] = GuessCand{h->gex, h->r, std::sqrt(nrm[0]), 2, spec ? h->Z[0] : nullptr, -1.};
+  bool weighted = false;
+  for (int u2 = 0; u2 < kGuessBands; u2++) weighted = weighted || bw.a[u2] != 0.;
+  double bmin = c[0].beta;
+  for (int q = 1; q < nc; q++) bmin = std::min(bmin, c[q].beta);
+  int inet = -1;
+  double r_learn = std::sqrt(std::max(r2, 0.));
+  if (weighted && r_learn <= kJudgeGate * bmin) {
+    double *xl = h->gnet;
+    LAUNCH(h, k_guess_compose, kRedBlocks, 256, b, h->rowtype0, h->gex, h->gof[cur], kappa, h->gsum, bw, xl);
+    LAUNCH(h, k_residual64, box_grid(h->box), 128, h->box, h->A0, xl, h->b, h->rlearn, h->partial);
+    double s2 = 0.;
+    const dim3 gr = box_grid(h->box);
+    TRY(reduce_read(h, (int)(gr.x * gr.y * gr.z), 1, &s2));
+    r_learn = std::sqrt(s2);
+    inet = nc;
+    c[nc++] = GuessCand{xl, h->rlearn, r_learn, 1, nullptr, -1.};
+  }
+  int w = 0;
+  TRY(judge(h, c, nc, &w));
+  const bool learned = c[w].code == 1;
+  install_guess(h, c[w]);
   if (use_hist) h->net_wait = learned ? 0 : h->net_period - 1;
-  h->r0_norm = learned ? r_learn : r_prev64;
-  h->r0_valid = true;
-  // the speculative step holds when the installed iterate is the plain
-  // extrapolation (its residual and norm are the step's V_0 and beta)
-  h->spec_valid = spec && learned && !weighted;
-  h->spec_next = learned && !weighted;
-  if (chosen) *chosen = learned ? 1 : 0;
+  // the speculative step holds when the extrapolation is installed (its
+  // residual and norm are the step's V_0 and beta)
+  h->spec_valid = spec && w == iex;
+  h->spec_next = w == iex;
+  guess_report(h, c, nc, w, nb);
+  if (chosen) *chosen = c[w].code;
   if (rel_res) {
-    rel_res[0] = r_prev64 / nb;
-    rel_res[1] = r_learn / nb;
+    rel_res[0] = c[0].code == 0 ? c[0].beta / nb : -1.;
+    rel_res[1] = (inet >= 0 ? r_learn : c[iex].beta) / nb;
   }
   if (h->phase) {
-    fprintf(stderr, "vfs guess rel residuals: extrapolation %.4e fit %.4e learned %.4e previous %.4e\n",
-            std::sqrt(nrm[0]) / nb, std::sqrt(std::max(r2, 0.)) / nb, r_learn / nb, r_prev64 / nb);
+    fprintf(stderr, "vfs guess rel residuals: extrapolation %.4e fit %.4e learned %.4e base %.4e\n",
+            std::sqrt(nrm[0]) / nb, std::sqrt(std::max(r2, 0.)) / nb, r_learn / nb,
+            c[0].code == 0 ? c[0].beta / nb : -1.);
     cudaEventRecord(h->phev[3], h->stream);
     TRY(sync(h));
-    float a = 0.f, c = 0.f, d = 0.f;
+    float a = 0.f, c2 = 0.f, d = 0.f;
     cudaEventElapsedTime(&a, h->phev[0], h->phev[1]);
-    cudaEventElapsedTime(&c, h->phev[1], h->phev[2]);
+    cudaEventElapsedTime(&c2, h->phev[1], h->phev[2]);
     cudaEventElapsedTime(&d, h->phev[2], h->phev[3]);
-    fprintf(stderr, "vfs guess ms: features+residuals %.3f network %.3f prolong+weights+judge %.3f\n", a, c, d);
+    fprintf(stderr, "vfs guess ms: features+residuals %.3f network %.3f prolong+weights+judge %.3f\n", a, c2, d);
   }
   return sync(h);
 }

@@ -938,6 +938,33 @@ __global__ void __launch_bounds__(256) k_hist_combine(size_t n, HistPtrs X, Hist
   if (threadIdx.x == 0) partial[blockIdx.x] = s;
 }
 
+// Moments over the fluid cells of z, for the estimated error of a guess
+// (z = one V-cycle of its residual): pass 0 writes the block partials of
+// sum z (row 0) and of the cell count (row 1); pass 1 those of
+// sum (z - mean)^2 (row 0).
+__global__ void __launch_bounds__(256) k_fluid_moments(size_t n, const uint8_t *__restrict__ fluid,
+                                                       const double *__restrict__ z, double mean, int pass,
+                                                       double *partial) {
+  double s = 0., cnt = 0.;
+  for (size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (size_t)gridDim.x * blockDim.x) {
+    if (!fluid[q]) continue;
+    const double v = z[q];
+    if (pass == 0) {
+      s += v;
+      cnt += 1.;
+    } else {
+      const double d = v - mean;
+      s = fma(d, d, s);
+    }
+  }
+  s = block_sum(s);
+  if (threadIdx.x == 0) partial[blockIdx.x] = s;
+  if (pass == 0) {
+    cnt = block_sum(cnt);
+    if (threadIdx.x == 0) partial[gridDim.x + blockIdx.x] = cnt;
+  }
+}
+
 // a solve's iterate and its image into a history slot: Xs = x, Ys = b - r
 // (r = b - A x, the solve's final FP64 residual)
 __global__ void __launch_bounds__(256) k_hist_push(size_t n, const double *__restrict__ x,

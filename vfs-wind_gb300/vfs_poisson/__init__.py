@@ -41,7 +41,7 @@ EXPORTS = [
     "vfs_read_petsc_vec", "vfs_write_petsc_vec", "vfs_read_grid", "vfs_read_ucd", "vfs_poisson_set_levelset",
     "vfs_poisson_ibm_search_nodes", "vfs_poisson_ibm_nodes", "vfs_poisson_ibm_interpolate", "vfs_poisson_ib_bc",
     "vfs_poisson_set_history", "vfs_poisson_history_guess", "vfs_poisson_set_network_period",
-    "vfs_poisson_history_record",
+    "vfs_poisson_history_record", "vfs_poisson_guess_report",
 ]
 
 
@@ -159,6 +159,7 @@ def load(path=LIB_PATH):
     L.vfs_poisson_history_guess.argtypes = [vp, P(C.c_double)]
     L.vfs_poisson_set_network_period.argtypes = [vp, C.c_int]
     L.vfs_poisson_history_record.argtypes = [vp, C.c_int]
+    L.vfs_poisson_guess_report.argtypes = [vp, P(C.c_int), vp, vp]
     L.vfs_poisson_contra2cart.argtypes = [vp, dp, dp, C.c_int]
     L.vfs_poisson_set_levelset.argtypes = [vp, dp, dp, vp, C.c_int]
     L.vfs_read_petsc_vec.argtypes = [C.c_char_p, P(C.c_int64), vp]
@@ -456,8 +457,9 @@ class PoissonSolver:
         _check(load().vfs_poisson_set_history(self.h, int(k)))
 
     def history_guess(self):
-        """Install the history projection as the iterate (solve with
-        warm_start=2 next); returns its relative residual."""
+        """Install the history's projection or extrapolation, whichever the
+        judge prefers, as the iterate (solve with warm_start=2 next); returns
+        its relative residual (guess_report tells which)."""
         r = C.c_double()
         _check(load().vfs_poisson_history_guess(self.h, C.byref(r)))
         return r.value
@@ -469,10 +471,23 @@ class PoissonSolver:
     def set_network_period(self, period):
         _check(load().vfs_poisson_set_network_period(self.h, int(period)))
 
+    def guess_report(self):
+        """What the last guess installed: (chosen, rel_res[3], est[3]) with
+        codes 0 projection / previous phi, 1 network, 2 extrapolation, and
+        per code the relative residual and the estimated error (-1 where the
+        candidate was not formed or not rated)."""
+        ch = C.c_int()
+        rr = (C.c_double * 3)()
+        es = (C.c_double * 3)()
+        _check(load().vfs_poisson_guess_report(self.h, C.byref(ch), C.cast(rr, C.c_void_p), C.cast(es, C.c_void_p)))
+        return ch.value, list(rr), list(es)
+
     def learned_guess(self, unet, phi_nm1, phi_nm2, kappa):
-        """Install the better of the learned guess and phi_{n-1} as the
-        iterate; returns (chosen, [rel_res_prev, rel_res_learned]).  Solve
-        with warm_start=2 next."""
+        """Install the judge's choice among the base (history projection, or
+        phi_{n-1} without a history), the extrapolation and the network's
+        guess as the iterate; returns (chosen, [rel_res_base,
+        rel_res_network]) with chosen 0 base, 1 network, 2 extrapolation.
+        Solve with warm_start=2 next."""
         ch = C.c_int()
         rr = (C.c_double * 2)()
         _check(load().vfs_poisson_learned_guess(self.h, unet.u, _ptr(phi_nm1), _ptr(phi_nm2), float(kappa),

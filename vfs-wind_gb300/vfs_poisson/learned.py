@@ -106,8 +106,9 @@ def run_sequence(seq, solver, steps, opts, guess="prev", net=None, pool=None, st
     """Solve steps start..start+steps-1 of a sequence on `solver`.
 
     guess: "zero", "prev" (phi_{n-1}, the reference's warm start), "extrap"
-    (2 phi_{n-1} - phi_{n-2}) or "learned" (the network, judged against
-    phi_{n-1}).  With `pool`, every step with two predecessors adds a
+    (2 phi_{n-1} - phi_{n-2}) or "learned" (the library's judge among
+    phi_{n-1} or the history's projection, the extrapolation and the
+    network's guess).  With `pool`, every step with two predecessors adds a
     training sample.  Returns (history [phi_{n-1}, phi_n] as CUDA tensors,
     per-step records)."""
     import torch

@@ -1362,6 +1362,9 @@ int hist_extrap(vfs_poisson *h, double *rnorm) {
     *rnorm = std::sqrt(std::max(rr, 0.));
     return VFS_OK;
   }
+  // cells without a dof under the current mask (a body moved over them)
+  // drop the old solutions' values there, as a warm start from phi does
+  LAUNCH(h, k_mask_box, lin_grid(n), 256, n, h->rowtype0, h->hist_ex);
   return residual_norm(h, h->hist_ex, h->hist_er, rnorm);
 }
 

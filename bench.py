@@ -486,19 +486,37 @@ def run_ours(args):
     p2_h = torch.empty(shape, dtype=torch.float64).pin_memory()
     out_h = torch.empty(shape, dtype=torch.float64).pin_memory()
     host = (u_h.numpy(), p1_h.numpy(), p2_h.numpy(), out_h.numpy())
-    ms_e2e, h2d = [], []
+    ms_e2e, h2d, its_e2e = [], [], []
     for r in range(1 + max(3, args.steps // 4)):
         u_h.copy_(step_inputs(n))
         p1_h.copy_(hist[-1])
         p2_h.copy_(hist[-2])
-        _, _, t_e, _, rr_e = arm_learned(None, hist, host=host)
+        _, st_e, t_e, _, rr_e = arm_learned(None, hist, host=host)
         if r:  # the first repetition warms the host path up
             ms_e2e.append(t_e)
+            its_e2e.append(st_e.iterations)
             # phi_{n-1} and phi_{n-2} are read only when the network runs
             h2d.append(u_h.numel() * 8 + (2 * p1_h.numel() * 8 if rr_e[1] >= 0 else 0))
         hist = [hist[-1], out_h.to(hist[-1].device)]
         n += 1
+    e2e_range = [min(ms_e2e), max(ms_e2e)]
     ms_e2e = statistics.mean(ms_e2e)
+    # the host link on its own: the step's input and output copies alone
+    u_d = torch.empty(tuple(u.shape), dtype=torch.float64, device=u.device)
+    link = []
+    for _ in range(3):
+        torch.cuda.synchronize()
+        e0.record(stream)
+        u_d.copy_(u_h, non_blocking=True)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        t_in = e0.elapsed_time(e1)
+        e0.record(stream)
+        out_h.copy_(hist[-1], non_blocking=True)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        link.append((u_h.numel() * 8 / t_in / 1e6, out_h.numel() * 8 / e0.elapsed_time(e1) / 1e6))
+    del u_d
 
     hbm, peak_kind = peaks()
     achieved = pbytes / (pms * 1e-3) / 1e9 if pms > 0 else None
@@ -523,7 +541,9 @@ def run_ours(args):
                       "extrapolation of the newest two) and the learned network's correction of the extrapolation "
                       "(run on every n-th step while it loses), chosen by estimated error (one V-cycle of each "
                       "residual within 32x of the smallest, fluid mean removed; the winner's V-cycle starts FGMRES)",
-            "iterations": statistics.mean(its_b),
+            "iterations": statistics.mean(its_b), "e2e_iterations": statistics.mean(its_e2e),
+            "e2e_ms_range": e2e_range,
+            "host_link_gbs": {"h2d": max(a for a, _ in link), "d2h": max(b for _, b in link)},
             "guess_chosen": {name: sum(1 for r in reports if r[0] == code)
                              for code, name in ((0, "projection"), (1, "network"), (2, "extrapolation"))},
             "network_evaluations": sum(1 for r in rel_learned if r >= 0),

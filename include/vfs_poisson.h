@@ -222,6 +222,23 @@ int vfs_poisson_projection(vfs_poisson *h, double *ucont, double dt, double st, 
  * blanked cell (the "Maxdiv" diagnostic). */
 int vfs_poisson_divergence(vfs_poisson *h, const double *ucont, double *maxdiv);
 
+/* FullyBlocked (Source/poisson.c:1909-1993) on the nvert of the last
+ * vfs_poisson_set_nvert: *multinullspace = 1 when every interior (i, j)
+ * column has a cell with nvert > 0.1 somewhere in k (boundary layers
+ * included), so that the operator of the -poisson -1 path has a null space
+ * per side of the blocking; ksk[my][mx] (int32, host or device; may be NULL)
+ * receives the first such k per column (KSKE[2 (j mx + i)]; -1 for none and
+ * on the boundary columns, where the reference leaves the entry unset). */
+int vfs_poisson_fully_blocked(vfs_poisson *h, int *multinullspace, int32_t *ksk);
+/* PoissonNullSpaceFunction_original (Source/poisson.c:757-943), the null
+ * space removal of the -poisson -1 multigrid solve, on a DA-layout array x
+ * (host or device, in place): the mean over the interior cells with nvert
+ * < 0.1 is removed (with multiple null spaces separately below and above
+ * each column's first blocked k); then the boundary layers and the cells with
+ * nvert > 0.1 are set to 0.  The sums are reduced in another order than the
+ * reference's loops (agreement to rounding). */
+int vfs_poisson_nullspace_original(vfs_poisson *h, double *x);
+
 /* ---- inspection entry points (parity tests, drop-in diagnostics) ---- */
 
 /* Number of pressure dofs (reduced_p_size) and, if gid != NULL, the dof id

@@ -92,6 +92,9 @@ def lib():
         L.or_contra2cart.argtypes = [P(Dims), dp, dp, dp, dp, dp, dp, C.c_int]
         L.or_remove_nullspace_scale.argtypes = [P(Dims), dp, ip, dp, dp, C.c_int]
         L.or_remove_nullspace.argtypes = [P(Dims), dp, ip, dp, C.c_int]
+        L.or_fully_blocked.argtypes = [P(Dims), dp, ip]
+        L.or_fully_blocked.restype = C.c_int
+        L.or_nullspace_original.argtypes = [P(Dims), dp, ip, C.c_int, dp]
         L.or_convert_phi2_phi.argtypes = [P(Dims), dp, dp, dp]
         L.or_update_pressure.argtypes = [P(Dims), dp, dp, dp]
         L.or_projection.argtypes = [P(Dims), dp, dp, P(Metrics), C.c_double, C.c_double, C.c_double, dp]
@@ -277,6 +280,24 @@ def remove_nullspace(d, nvert, gid, phi2, bctype3=0):
     lib().or_remove_nullspace(C.byref(d), _dp(np.ascontiguousarray(nvert, np.float64)),
                               _ip(np.ascontiguousarray(gid, np.int32).ravel()), _dp(p), bctype3)
     return p
+
+
+def fully_blocked(d, nvert):
+    """FullyBlocked: (multi, ksk[my, mx]) -- the first blocked k of every
+    interior column (-1 where none)."""
+    ksk = np.zeros((d.my, d.mx), np.int32)
+    multi = lib().or_fully_blocked(C.byref(d), _dp(np.ascontiguousarray(nvert, np.float64)), _ip(ksk))
+    return bool(multi), ksk
+
+
+def nullspace_original(d, nvert, x, ksk=None, multi=None):
+    """PoissonNullSpaceFunction_original on a DA-layout copy of x."""
+    if ksk is None:
+        multi, ksk = fully_blocked(d, nvert)
+    out = np.ascontiguousarray(x, np.float64).copy()
+    lib().or_nullspace_original(C.byref(d), _dp(np.ascontiguousarray(nvert, np.float64)),
+                                _ip(np.ascontiguousarray(ksk, np.int32)), int(bool(multi)), _dp(out))
+    return out
 
 
 def convert_phi2_phi(d, nvert, phi2):

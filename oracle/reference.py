@@ -63,6 +63,8 @@ def lib():
         L.vr_projection.argtypes = [vp, C.c_double, C.c_double]
         L.vr_divergence.argtypes = [vp, C.POINTER(C.c_double)]
         L.vr_volume_flux.argtypes = [vp, C.c_int, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]
+        L.vr_fully_blocked.argtypes = [vp, C.POINTER(C.c_int), vp]
+        L.vr_nullspace_original.argtypes = [vp, vp, C.c_long]
         _lib = L
     return _lib
 
@@ -172,6 +174,22 @@ class Block:
         v = C.c_double()
         lib().vr_divergence(self.h, C.byref(v))
         return v.value
+
+    def fully_blocked(self):
+        """FullyBlocked: (multi, ksk[my, mx]) with -1 where KSKE is unset."""
+        m = C.c_int()
+        ksk = np.zeros((self.dims[1], self.dims[0]), np.int32)
+        lib().vr_fully_blocked(self.h, C.byref(m), ksk.ctypes.data)
+        return bool(m.value), ksk
+
+    def nullspace_original(self, x):
+        """PoissonNullSpaceFunction_original on a copy of the DA array x
+        (after fully_blocked)."""
+        a = np.ascontiguousarray(x, np.float64).copy()
+        rc = lib().vr_nullspace_original(self.h, a.ctypes.data, a.size)
+        if rc != 0:
+            raise RuntimeError(f"vr_nullspace_original = {rc}")
+        return a
 
     def volume_flux(self, immersed_variant=True, flg=0):
         f, a = C.c_double(), C.c_double()

@@ -36,6 +36,7 @@ PetscErrorCode MyNvertRestriction(UserCtx *user_h, UserCtx *user_c);
 PetscErrorCode VolumeFlux(UserCtx *user, Vec lUcor, PetscReal *ibm_Flux, PetscReal *ibm_Area);
 PetscErrorCode VolumeFlux(UserCtx *user, PetscReal *ibm_Flux, PetscReal *ibm_Area, PetscInt flg);
 PetscErrorCode Divergence(UserCtx *user);
+PetscErrorCode PoissonNullSpaceFunction_original(MatNullSpace nsp, Vec X, void *ctx);
 
 namespace {
 
@@ -190,6 +191,7 @@ void *vr_create(int mx, int my, int mz, const int *per, const int *bctype, const
 void vr_destroy(void *h) {
   Ctx *c = (Ctx *)h;
   if (!c) return;
+  free(c->u->KSKE);
   for (Vec v : c->owned) {
     VecDestroy(v);
     VecDestroy(v);
@@ -381,6 +383,35 @@ int vr_volume_flux(void *h, int immersed_variant, int flg, double *flux, double 
     VolumeFlux(c->u, c->u->Ucont, flux, area);
   }
   immersed = old;
+  return 0;
+}
+
+// FullyBlocked (Source/poisson.c:1909-1993) on the current Nvert: the
+// multiple-null-space flag and KSKE[2 (j mx + i)] per interior column in
+// ksk[j mx + i] (-1 where the reference leaves the entry unset).
+int vr_fully_blocked(void *h, int *multi, int *ksk) {
+  Ctx *c = (Ctx *)h;
+  const DALocalInfo &i = c->u->info;
+  const int n = 2 * i.mx * i.my;
+  if (!c->u->KSKE) c->u->KSKE = (PetscInt *)malloc(sizeof(PetscInt) * n);
+  for (int q = 0; q < n; q++) c->u->KSKE[q] = -1;
+  FullyBlocked(c->u);
+  *multi = c->u->multinullspace ? 1 : 0;
+  for (int q = 0; q < i.mx * i.my; q++) ksk[q] = c->u->KSKE[2 * q];
+  return 0;
+}
+
+// PoissonNullSpaceFunction_original (Source/poisson.c:757-943) on a
+// DA-natural array x (through the global Phi vector), with the flag and
+// KSKE of the last vr_fully_blocked.
+int vr_nullspace_original(void *h, double *x, long n) {
+  Ctx *c = (Ctx *)h;
+  int m = 0;
+  double *d = vfs_shim_vec_data(c->u->Phi, &m);
+  if (m != n) return -3;
+  memcpy(d, x, sizeof(double) * (size_t)n);
+  PoissonNullSpaceFunction_original(nullptr, c->u->Phi, c->u);
+  memcpy(x, d, sizeof(double) * (size_t)n);
   return 0;
 }
 

@@ -664,6 +664,70 @@ void or_remove_nullspace_scale(const or_dims *d, const double *nvert, const int 
       }
 }
 
+/* FullyBlocked (Source/poisson.c:1909-1993): for every interior (i, j)
+ * column the first k (boundary layers included) whose nvert exceeds 0.1, in
+ * ksk[j * mx + i] (-1 for a column with none, and on the boundary columns);
+ * returns the multiple-null-space flag: every interior column is blocked. */
+int or_fully_blocked(const or_dims *d, const double *nvert, int *ksk)
+{
+  const int mx = d->mx, my = d->my, mz = d->mz;
+  int multi = 1;
+  for (int q = 0; q < mx * my; q++) ksk[q] = -1;
+  for (int j = 1; j < my - 1; j++)
+    for (int i = 1; i < mx - 1; i++) {
+      for (int k = 0; k < mz; k++)
+        if (nvert[IX(d, i, j, k)] > 0.1) { ksk[j * mx + i] = k; break; }
+      if (ksk[j * mx + i] < 0) multi = 0;
+    }
+  return multi;
+}
+
+/* PoissonNullSpaceFunction_original (Source/poisson.c:757-943) on a
+ * DA-layout vector x: the mean over the interior cells with nvert < 0.1 is
+ * removed (with multi, separately below and above each column's first
+ * blocked k, ksk from or_fully_blocked, summed in the reference's j-i-k
+ * order); then the boundary layers and the cells with nvert > 0.1 are set
+ * to 0. */
+void or_nullspace_original(const or_dims *d, const double *nvert, const int *ksk, int multi, double *x)
+{
+  const int mx = d->mx, my = d->my, mz = d->mz;
+  if (!multi) {
+    double sum = 0, num = 0;
+    for (int k = 1; k < mz - 1; k++)
+      for (int j = 1; j < my - 1; j++)
+        for (int i = 1; i < mx - 1; i++)
+          if (nvert[IX(d, i, j, k)] < 0.1) { sum += x[IX(d, i, j, k)]; num++; }
+    sum = sum / (-1.0 * num);
+    for (int k = 1; k < mz - 1; k++)
+      for (int j = 1; j < my - 1; j++)
+        for (int i = 1; i < mx - 1; i++)
+          if (nvert[IX(d, i, j, k)] < 0.1) x[IX(d, i, j, k)] += sum;
+  } else {
+    for (int above = 0; above < 2; above++) {
+      double sum = 0, num = 0;
+      for (int j = 1; j < my - 1; j++)
+        for (int i = 1; i < mx - 1; i++)
+          for (int k = 1; k < mz - 1; k++) {
+            const int in = above ? k >= ksk[j * mx + i] : k < ksk[j * mx + i];
+            if (in && nvert[IX(d, i, j, k)] < 0.1) { sum += x[IX(d, i, j, k)]; num++; }
+          }
+      sum /= -num;
+      for (int j = 1; j < my - 1; j++)
+        for (int i = 1; i < mx - 1; i++)
+          for (int k = 1; k < mz - 1; k++) {
+            const int in = above ? k >= ksk[j * mx + i] : k < ksk[j * mx + i];
+            if (in && nvert[IX(d, i, j, k)] < 0.1) x[IX(d, i, j, k)] += sum;
+          }
+    }
+  }
+  for (int k = 0; k < mz; k++)
+    for (int j = 0; j < my; j++)
+      for (int i = 0; i < mx; i++) {
+        const int bnd = i == 0 || i == mx - 1 || j == 0 || j == my - 1 || k == 0 || k == mz - 1;
+        if (bnd || nvert[IX(d, i, j, k)] > 0.1) x[IX(d, i, j, k)] = 0.;
+      }
+}
+
 /* Remove_Nullspace (Source/poisson_hypre.c:202-263). */
 void or_remove_nullspace(const or_dims *d, const double *nvert, const int *gid, double *phi2,
                          int bctype3)

@@ -73,6 +73,8 @@ void or_poisson_rhs2_hypre(const or_dims *d, const double *nvert, const int *gid
                            double *b);
 void or_remove_nullspace_scale(const or_dims *d, const double *nvert, const int *gid,
                                const double *aj, double *b, int bctype3);
+int or_fully_blocked(const or_dims *d, const double *nvert, int *ksk);
+void or_nullspace_original(const or_dims *d, const double *nvert, const int *ksk, int multi, double *x);
 void or_remove_nullspace(const or_dims *d, const double *nvert, const int *gid,
                          double *phi2, int bctype3);
 void or_convert_phi2_phi(const or_dims *d, const double *nvert, const double *phi2,

@@ -18,7 +18,10 @@ oracle/refshim/ (oracle/reference.py).  Recorded per case:
   * UpdatePressure of a seeded P, Projection of Ucont with that Phi, and the
     Divergence maximum after it;
   * VolumeFlux, the immersed variant (flg 0) and the immersed == 0 variant,
-    on the input Ucont.
+    on the input Ucont;
+  * FullyBlocked (the first blocked k of every column and the multiple
+    null space flag) and PoissonNullSpaceFunction_original of a seeded
+    array (the -poisson -1 path's null-space removal).
 
 The CPU tests check the oracle's restatement against these, the GPU tests
 check the CUDA library against them.  Needs the reference sources (the
@@ -43,16 +46,24 @@ def cases():
     """The fixture grids: a periodic channel, the curvilinear cylinder, two
     towers with both periodic DA directions, and a cylinder with the
     explicit-copy i/j periodic flags and fractional IB values (nvert 0.5:
-    dofs with identity rows)."""
+    dofs with identity rows), and a channel cut by a solid k-slab (every
+    column blocked: the multiple null space of FullyBlocked)."""
     c4 = CF.cylinder(10, 8, 10, seed=7)
     c4.nvert = np.where(c4.nvert == 1.0, 0.5, c4.nvert)
     c4.set_periodic((1, 1, 0, 0, 0, 0))
     c4.name = "cylinder_ijper_frac"
+    c5 = CF.channel(8, 8, 8)
+    nv = c5.nvert.copy()
+    nv[5] = 1.0
+    c5.nvert = CF.sync_periodic_ghosts(nv, c5.periodic)
+    c5.ucont = CF._mask_faces(c5.ucont, c5.nvert)
+    c5.name = "channel_slab"
     return {
         "channel_8": CF.channel(8, 8, 8),
         "cylinder_12": CF.cylinder(12, 8, 12),
         "towers_10": CF.towers(10, 8, 10, radius=0.12, array=(2, 1)),
         "cylinder_ijper_frac_10": c4,
+        "channel_slab_8": c5,
     }
 
 
@@ -121,6 +132,11 @@ def reference_outputs(case, seed):
     B.projection()
     out["ucont_proj"] = B.get("ucont", 3)
     out["maxdiv_proj"] = np.array([B.divergence()])
+    multi, ksk = B.fully_blocked()
+    out["multinull"] = np.array([int(multi)], np.int32)
+    out["ksk"] = ksk
+    out["ns_x"] = rng.standard_normal(case.nvert.shape)
+    out["ns_out"] = B.nullspace_original(out["ns_x"])
     B.close()
     return out
 

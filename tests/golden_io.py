@@ -69,3 +69,7 @@ def check_oracle(case, g):
     u_ib, flux, area = O.volume_flux(d, case.nvert, met, case.ucont, flg=0)
     np.testing.assert_array_equal(u_ib, g["vflux_ib_ucont"])
     np.testing.assert_array_equal([flux, area], g["vflux_ib"])
+    multi, ksk = O.fully_blocked(d, case.nvert)
+    assert int(multi) == int(g["multinull"][0])
+    np.testing.assert_array_equal(ksk, g["ksk"])
+    np.testing.assert_array_equal(O.nullspace_original(d, case.nvert, g["ns_x"], ksk, multi), g["ns_out"])

@@ -9,6 +9,8 @@ library, called through its C ABI, must reproduce them:
     VolumeFlux overloads;
   * to 1e-12 of the largest entry where the library reduces in another
     order: the right-hand sides (the mean removals) and the VolumeFlux sums;
+  * to 1e-12 of the largest entry as well: PoissonNullSpaceFunction_original
+    (its means); FullyBlocked bit for bit;
   * the solve: phi within 1e-6 relative L2 of the phi the reference makes
     from an exact inner solve (Remove_Nullspace + Convert_Phi2_Phi), with the
     true FP64 residual of the reference's own matrix <= 1e-8.
@@ -116,3 +118,23 @@ def test_solve_against_reference_phi(golden, precision):
     fl = _dof(g, (case.nvert < 0.1).astype(np.float64)) > 0
     ref = _dof(g, g["phi"])
     assert np.linalg.norm((phi2 - ref)[fl]) / np.linalg.norm(ref[fl]) <= 1e-6
+
+
+def test_fully_blocked_and_nullspace_original(golden):
+    """FullyBlocked bit for bit (the first blocked k per column and the
+    multiple-null-space flag, which the channel cut by a solid slab sets),
+    and PoissonNullSpaceFunction_original of the fixture's seeded array to
+    1e-12 of its largest entry (its means are reduced in another order), on
+    host and on device arrays."""
+    import torch
+    case, g, s = golden
+    multi, ksk = s.fully_blocked()
+    assert int(multi) == int(g["multinull"][0])
+    np.testing.assert_array_equal(ksk, g["ksk"])
+    tol = 1e-12 * np.abs(g["ns_x"]).max()
+    x = g["ns_x"].copy()
+    s.nullspace_original(x)
+    np.testing.assert_allclose(x, g["ns_out"], rtol=0, atol=tol)
+    xd = torch.from_numpy(g["ns_x"].copy()).cuda()
+    s.nullspace_original(xd)
+    np.testing.assert_allclose(xd.cpu().numpy(), g["ns_out"], rtol=0, atol=tol)

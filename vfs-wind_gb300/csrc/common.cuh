@@ -93,7 +93,9 @@ struct LevelSet {
 // Parity-split row layout of the multigrid level operators and line
 // factors: within each (j, k) row the even-i cells come first, then the odd
 // ones, so that the columns of one checkerboard colour ((i + k) parity) are
-// contiguous and coalesce.  Vectors (x, b, r) keep the natural layout.
+// contiguous and coalesce.  Vectors (x, b, r) keep the natural layout, except
+// the finest FP32 level's x and right-hand side under the checkerboard
+// smoother, which use this layout too (whole sectors per colour).
 __host__ __device__ inline int split_pos(int i, int nx) { return (i & 1) ? ((nx + 1) >> 1) + (i >> 1) : (i >> 1); }
 __host__ __device__ inline int split_cell(int p, int nx) {
   const int nh = (nx + 1) >> 1;
@@ -127,21 +129,30 @@ struct Nbr {
 
 // Linear indices of the 19 stencil points of (i,j,k) in slot order (32-bit:
 // the library rejects grids whose 19 operator planes reach 2^32 entries).
-__device__ inline void stencil_index(const Box &b, int i, int j, int k, uint32_t idx[NSLOT]) {
+// SPLIT: the vector is stored in the parity-split row layout (the finest
+// FP32 level's x and right-hand side), so each column index i goes through
+// split_pos.
+template <bool SPLIT>
+__device__ inline void stencil_index_t(const Box &b, int i, int j, int k, uint32_t idx[NSLOT]) {
   Nbr q(b, i, j, k);
   const uint32_t nx = b.nx, sl = (uint32_t)b.nx * b.ny;
   const uint32_t r0 = (uint32_t)k * sl, rm = (uint32_t)q.km * sl, rp = (uint32_t)q.kp * sl;
   const uint32_t j0 = (uint32_t)j * nx, jm = (uint32_t)q.jm * nx, jp = (uint32_t)q.jp * nx;
-  idx[CP] = r0 + j0 + i;
-  idx[EP] = r0 + j0 + q.ip;  idx[WP] = r0 + j0 + q.im;
-  idx[NP] = r0 + jp + i;     idx[SP] = r0 + jm + i;
-  idx[TP] = rp + j0 + i;     idx[BP] = rm + j0 + i;
-  idx[NE] = r0 + jp + q.ip;  idx[SE] = r0 + jm + q.ip;
-  idx[NW] = r0 + jp + q.im;  idx[SW] = r0 + jm + q.im;
-  idx[TN] = rp + jp + i;     idx[BN] = rm + jp + i;
-  idx[TS] = rp + jm + i;     idx[BS] = rm + jm + i;
-  idx[TE] = rp + j0 + q.ip;  idx[BE] = rm + j0 + q.ip;
-  idx[TW] = rp + j0 + q.im;  idx[BW] = rm + j0 + q.im;
+  const uint32_t ci = SPLIT ? split_pos(i, b.nx) : i, ce = SPLIT ? split_pos(q.ip, b.nx) : q.ip,
+                 cw = SPLIT ? split_pos(q.im, b.nx) : q.im;
+  idx[CP] = r0 + j0 + ci;
+  idx[EP] = r0 + j0 + ce;  idx[WP] = r0 + j0 + cw;
+  idx[NP] = r0 + jp + ci;  idx[SP] = r0 + jm + ci;
+  idx[TP] = rp + j0 + ci;  idx[BP] = rm + j0 + ci;
+  idx[NE] = r0 + jp + ce;  idx[SE] = r0 + jm + ce;
+  idx[NW] = r0 + jp + cw;  idx[SW] = r0 + jm + cw;
+  idx[TN] = rp + jp + ci;  idx[BN] = rm + jp + ci;
+  idx[TS] = rp + jm + ci;  idx[BS] = rm + jm + ci;
+  idx[TE] = rp + j0 + ce;  idx[BE] = rm + j0 + ce;
+  idx[TW] = rp + j0 + cw;  idx[BW] = rm + j0 + cw;
+}
+__device__ inline void stencil_index(const Box &b, int i, int j, int k, uint32_t idx[NSLOT]) {
+  stencil_index_t<false>(b, i, j, k, idx);
 }
 
 // ---- deterministic reductions: fixed-shape block trees ----

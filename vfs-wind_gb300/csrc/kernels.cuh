@@ -49,6 +49,11 @@ __global__ void k_rhs(Grid g, Box b, const double *nvert, const double *ucont, c
 __global__ void k_reduce_rows(const double *partial, int nb, int nrow, double *out);
 __global__ void k_rhs_nullspace(Grid g, Box b, const double *nvert, const double *aj, const double *sums,
                                 double *rhs);
+__global__ void k_fully_blocked(Grid g, const double *nvert, int *ksk, int *unblocked);
+__global__ void k_nullspace_sums(Grid g, const double *nvert, const int *ksk, int multi, const double *x,
+                                 double *partial);
+__global__ void k_nullspace_apply(Grid g, const double *nvert, const int *ksk, int multi, double shift0,
+                                  double shift1, double *x);
 __global__ void k_mean_partial(Box b, const uint8_t *fluid, const double *x, double *partial);
 __global__ void k_shift_fluid(Box b, const uint8_t *fluid, const double *sums, double *x);
 __global__ void k_fluid_mask(Grid g, Box b, const double *nvert, uint8_t *fluid);
@@ -72,6 +77,8 @@ __global__ void k_restrict_f64(Box bf, Box bc, int cx, int cy, int cz, const dou
                                const uint8_t *blank_c, double *out);
 __global__ void k_prolong_f32(Box bf, Box bc, int cx, int cy, int cz, const float *xc, const uint8_t *blank_c,
                               const uint8_t *blank_f, float *xf, int add);
+__global__ void k_prolong_f32_split(Box bf, Box bc, int cx, int cy, int cz, const float *xc, const uint8_t *blank_c,
+                              const uint8_t *blank_f, float *xf, int add);
 __global__ void k_prolong_f64(Box bf, Box bc, int cx, int cy, int cz, const double *xc, const uint8_t *blank_c,
                               const uint8_t *blank_f, double *xf, int add);
 
@@ -93,6 +100,10 @@ TYPED_DECL(double, f64)
 __global__ void k_pack16(size_t n, const double *A, __half2 *C, float *D);
 __global__ void k_residual16(Box b, const __half2 *C, const float *D, const float *x, const float *rhs, float *r,
                              int color);
+__global__ void k_residual16_split(Box b, const __half2 *C, const float *D, const float *x, const float *rhs, float *r,
+                             int color);
+__global__ void k_line_tri_f32_split(Box b, const float *r, const float *Asp, const float *inv, const float *cp, float *x,
+                                     float omega, int zg, int color);
 // Checkerboard zebra colour with the residual formed in the line kernel:
 // _oz counts the launch's colour as zero (its loads are masked), _z every x
 // (r = rhs).
@@ -144,9 +155,10 @@ __global__ void k_gs_update(size_t n, int nv, const double *const *Q, const doub
 __global__ void k_axpy_multi(size_t n, int nv, const double *const *Z, const double *coef, double *x);
 __global__ void k_scale_to(size_t n, const double *v, double s, const double *sinv, const double *scale,
                            double *out);
-__global__ void k_scale_to32(size_t n, const double *v, float s, const float *sinv, const float *scale, float *out);
+__global__ void k_scale_to32(size_t n, const double *v, float s, const float *sinv, const float *scale, float *out,
+                             int split_nx);
 __global__ void k_reduce_norm(const double *partial, int nb, double *out, float *out32);
-__global__ void k_to64(size_t n, const float *x32, const double *x64, double *out);
+__global__ void k_to64(size_t n, const float *x32, const double *x64, double *out, int split_nx);
 __global__ void k_sumsq(size_t n, const double *x, double *partial);
 // history projection of the initial guess (at most kHistMax solutions)
 constexpr int kHistMax = 8;

@@ -64,6 +64,12 @@ __global__ void k_mask_box(size_t n, const uint8_t *rowtype, double *x) {
   size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (c < n && rowtype[c] == 0) x[c] = 0.;
 }
+// zero x off the fluid rows: cells without a dof and identity rows (whose
+// solution is 0: their right-hand side is 0)
+__global__ void k_mask_fluid(size_t n, const uint8_t *rowtype, double *x) {
+  size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c < n && rowtype[c] != 1) x[c] = 0.;
+}
 // ---- learned initial guess: features, training target, composition ----
 // sums[0..2]: fluid sums of squares of planes 0..2, sums[3]: fluid count.
 __device__ inline void block_add(double v, double *dst) {
@@ -498,6 +504,11 @@ struct vfs_poisson {
   // installed residual divided by its norm, under the options z0_opts
   bool z0_valid = false;
   vfs_solve_opts z0_opts{};
+  // FullyBlocked of the current nvert: first blocked k per (i, j) column
+  // (device, mx * my) and the multiple-null-space flag (-1: not formed)
+  int *ksk = nullptr, *ksk_count = nullptr;
+  int multinull = -1;
+  uint64_t ksk_version = 0;
   // what the last guess installed (vfs_poisson_guess_report)
   int guess_chosen = -1;
   double guess_rel[3] = {-1., -1., -1.}, guess_est[3] = {-1., -1., -1.};
@@ -936,13 +947,17 @@ struct Prec;
 template <>
 struct Prec<float> {
   static constexpr auto sweep = k_line_sweep_f32;
-  static void residual(vfs_poisson *h, Level &l, dim3 g, const float *x, const float *bb, float *r, int color) {
-    LAUNCH(h, k_residual16, g, 128, l.b, l.C16, l.D32, x, bb, r, color);
+  static void residual(vfs_poisson *h, Level &l, dim3 g, const float *x, const float *bb, float *r, int color,
+                       bool split) {
+    if (split) LAUNCH(h, k_residual16_split, g, 128, l.b, l.C16, l.D32, x, bb, r, color);
+    else LAUNCH(h, k_residual16, g, 128, l.b, l.C16, l.D32, x, bb, r, color);
   }
   static constexpr auto restrict_ = k_restrict_f32;
   static constexpr auto prolong = k_prolong_f32;
+  static constexpr auto prolong_split = k_prolong_f32_split;
   static constexpr auto coarsest = k_coarsest_f32;
   static constexpr auto tri = k_line_tri_f32;
+  static constexpr auto tri_split = k_line_tri_f32_split;
   static void fused(vfs_poisson *h, Level &l, dim3 g, dim3 blk, size_t sm, const float *xo, const float *xn,
                     const float *bb, float *xd, float omega, bool own_zero, bool both_zero, int color) {
     const auto kern = both_zero ? k_line_fused16_z : own_zero ? k_line_fused16_oz : k_line_fused16;
@@ -959,13 +974,16 @@ struct Prec<float> {
 template <>
 struct Prec<double> {
   static constexpr auto sweep = k_line_sweep_f64;
-  static void residual(vfs_poisson *h, Level &l, dim3 g, const double *x, const double *bb, double *r, int color) {
+  static void residual(vfs_poisson *h, Level &l, dim3 g, const double *x, const double *bb, double *r, int color,
+                       bool) {
     LAUNCH(h, k_residual_f64, g, 128, l.b, l.A64, x, bb, r, color);
   }
   static constexpr auto restrict_ = k_restrict_f64;
   static constexpr auto prolong = k_prolong_f64;
+  static constexpr auto prolong_split = k_prolong_f64;  // (the FP64 V-cycle keeps natural vectors)
   static constexpr auto coarsest = k_coarsest_f64;
   static constexpr auto tri = k_line_tri_f64;
+  static constexpr auto tri_split = k_line_tri_f64;
   // no FP64 variant of the fused sweep (smoother 4 runs smoother 3's kernels)
   static void fused(vfs_poisson *, Level &, dim3, dim3, size_t, const double *, const double *, const double *,
                     double *, double, bool, bool, int) {}
@@ -998,6 +1016,16 @@ constexpr size_t kFusedMaxCells = size_t(1) << 20;
 template <typename T>
 bool fused_level(const Level &l, int smoother) {
   return smoother == 4 && std::is_same<T, float>::value && l.b.n() <= kFusedMaxCells;
+}
+// The finest FP32 level under the two-kernel checkerboard sweep keeps x and
+// its right-hand side in the parity-split row layout: each colour's launches
+// then read and write whole sectors of them (natural vectors give every
+// other float of a sector).  The residual handed to the restriction stays
+// natural, so the coarser levels are unaffected.
+template <typename T>
+bool split_level(const vfs_poisson *h, int li, int smoother) {
+  return std::is_same<T, float>::value && li == 0 && h->L.size() > 1 && smoother >= 3 &&
+         !fused_level<T>(h->L[0], smoother);
 }
 
 template <typename T>
@@ -1054,14 +1082,14 @@ void smooth(vfs_poisson *h, Level &l, int li, int smoother, bool zero_guess, T o
               zero_guess ? 1 : 0);
     std::swap(x, t);
   } else if (smoother == 1) {
-    if (!zero_guess) Prec<T>::residual(h, l, box_grid(l.b), x, bb, r, -1);
+    if (!zero_guess) Prec<T>::residual(h, l, box_grid(l.b), x, bb, r, -1, false);
     LAUNCH_SM(h, Prec<T>::tri, lg, lb, lsm, l.b, zero_guess ? bb : r, Asp, Prec<T>::inv(l), Prec<T>::cp(l), x,
               omega, zero_guess ? 1 : 0, -1);
   } else if (smoother == 2) {
     if (zero_guess) cudaMemsetAsync(x, 0, l.b.n() * sizeof(T), h->stream);
     for (int color = 0; color < 2; color++) {
       const bool skip_res = zero_guess && color == 0;  // x = 0: r = rhs
-      if (!skip_res) Prec<T>::residual(h, l, box_grid(l.b), x, bb, r, color);
+      if (!skip_res) Prec<T>::residual(h, l, box_grid(l.b), x, bb, r, color, false);
       LAUNCH_SM(h, Prec<T>::tri, lg, lb, lsm, l.b, skip_res ? bb : r, Asp, Prec<T>::inv(l), Prec<T>::cp(l), x,
                 omega, 0, color);
     }
@@ -1080,11 +1108,13 @@ void smooth(vfs_poisson *h, Level &l, int li, int smoother, bool zero_guess, T o
     if (zero_guess) cudaMemsetAsync(x, 0, l.b.n() * sizeof(T), h->stream);
     const int nh = (l.b.nx + 1) / 2;
     dim3 cg((nh + TI - 1) / TI, l.b.nz), rg((nh + 127) / 128, l.b.ny, l.b.nz);
+    const bool split = split_level<T>(h, li, smoother);
     for (int color = 0; color < 2; color++) {
       const bool skip_res = zero_guess && color == 0;
-      if (!skip_res) Prec<T>::residual(h, l, rg, x, bb, r, 2 + color);
-      LAUNCH_SM(h, Prec<T>::tri, cg, lb, lsm, l.b, skip_res ? bb : r, Asp, Prec<T>::inv(l), Prec<T>::cp(l), x,
-                omega, 0, (skip_res ? 4 : 2) + color);
+      if (!skip_res) Prec<T>::residual(h, l, rg, x, bb, r, 2 + color, split);
+      const auto tri = split ? Prec<T>::tri_split : Prec<T>::tri;
+      LAUNCH_SM(h, tri, cg, lb, lsm, l.b, skip_res ? bb : r, Asp, Prec<T>::inv(l), Prec<T>::cp(l), x, omega, 0,
+                (skip_res ? 4 : 2) + color);
     }
   }
   prof_end(h, li);
@@ -1107,17 +1137,17 @@ void vcycle(vfs_poisson *h, int li, int nu1, int nu2, T omega, int smoother) {
     // residual is zero up to rounding: form the first colour's only
     const int nh = (l.b.nx + 1) / 2;
     cudaMemsetAsync(r, 0, l.b.n() * sizeof(T), h->stream);
-    Prec<T>::residual(h, l, dim3((nh + 127) / 128, l.b.ny, l.b.nz), x, bb, r, 6);
+    Prec<T>::residual(h, l, dim3((nh + 127) / 128, l.b.ny, l.b.nz), x, bb, r, 6, split_level<T>(h, li, smoother));
   } else {
-    Prec<T>::residual(h, l, box_grid(l.b), x, bb, r, -1);
+    Prec<T>::residual(h, l, box_grid(l.b), x, bb, r, -1, split_level<T>(h, li, smoother));
   }
   Level &q = h->L[li + 1];
   LAUNCH(h, Prec<T>::restrict_, box_grid(q.b), 128, l.b, q.b, l.cx, l.cy, l.cz, r, Prec<T>::w(l), q.blank,
          Prec<T>::v(q)[1]);
   vcycle<T>(h, li + 1, nu1, nu2, omega, smoother);
-  LAUNCH(h, Prec<T>::prolong, dim3((l.b.nx + 127) / 128, (l.b.ny + 1) / 2, l.b.nz), 128, l.b, q.b, l.cx, l.cy,
-         l.cz, (const T *)Prec<T>::xfinal(q), q.blank,
-         l.blank, x, 1);
+  const auto prolong = split_level<T>(h, li, smoother) ? Prec<T>::prolong_split : Prec<T>::prolong;
+  LAUNCH(h, prolong, dim3((l.b.nx + 127) / 128, (l.b.ny + 1) / 2, l.b.nz), 128, l.b, q.b, l.cx, l.cy, l.cz,
+         (const T *)Prec<T>::xfinal(q), q.blank, l.blank, x, 1);
   for (int s = 0; s < nu2; s++) smooth<T>(h, l, li, smoother, false, omega, x, t, bb, r);
   Prec<T>::xfinal(l) = x;
 }
@@ -1169,13 +1199,14 @@ int precondition(vfs_poisson *h, const double *v, double s, const double *sinv64
   Level &l0 = h->L[0];
   const size_t n = h->box.n();
   if (o.precision == 0) {
-    LAUNCH(h, k_scale_to32, lin_grid(n), 256, n, v, (float)s, sinv32, h->scale32, l0.v32[1]);
+    const int snx = split_level<float>(h, 0, o.smoother) ? l0.b.nx : 0;
+    LAUNCH(h, k_scale_to32, lin_grid(n), 256, n, v, (float)s, sinv32, h->scale32, l0.v32[1], snx);
     TRY(run_vcycle<float>(h, o));
-    LAUNCH(h, k_to64, lin_grid(n), 256, n, (const float *)l0.xfinal32, (const double *)nullptr, z);
+    LAUNCH(h, k_to64, lin_grid(n), 256, n, (const float *)l0.xfinal32, (const double *)nullptr, z, snx);
   } else {
     LAUNCH(h, k_scale_to, kRedBlocks, 256, n, v, s, sinv64, h->scale, l0.v64[1]);
     TRY(run_vcycle<double>(h, o));
-    LAUNCH(h, k_to64, lin_grid(n), 256, n, (const float *)nullptr, (const double *)l0.xfinal64, z);
+    LAUNCH(h, k_to64, lin_grid(n), 256, n, (const float *)nullptr, (const double *)l0.xfinal64, z, 0);
   }
   return VFS_OK;
 }
@@ -1362,9 +1393,9 @@ int hist_extrap(vfs_poisson *h, double *rnorm) {
     *rnorm = std::sqrt(std::max(rr, 0.));
     return VFS_OK;
   }
-  // cells without a dof under the current mask (a body moved over them)
-  // drop the old solutions' values there, as a warm start from phi does
-  LAUNCH(h, k_mask_box, lin_grid(n), 256, n, h->rowtype0, h->hist_ex);
+  // cells that are no fluid rows under the current mask (a body moved over
+  // them) drop the old solutions' values: 0 is their solution
+  LAUNCH(h, k_mask_fluid, lin_grid(n), 256, n, h->rowtype0, h->hist_ex);
   return residual_norm(h, h->hist_ex, h->hist_er, rnorm);
 }
 
@@ -2348,6 +2379,54 @@ int vfs_poisson_set_network_period(vfs_poisson *h, int period) {
   h->net_period = period;
   h->net_wait = 0;
   return VFS_OK;
+}
+
+int vfs_poisson_fully_blocked(vfs_poisson *h, int *multinullspace, int32_t *ksk) {
+  if (!h) return fail(VFS_EINVAL, "null handle");
+  if (!h->have_nvert) return fail(VFS_ESTATE, "set_nvert must come first");
+  const Grid &g = h->g;
+  const size_t nc = (size_t)g.mx * g.my;
+  if (!h->ksk) {
+    TRY(dalloc(h, &h->ksk, nc));
+    TRY(dalloc(h, &h->ksk_count, 1));
+  }
+  if (h->multinull < 0 || h->ksk_version != h->op_version) {
+    CUDA_TRY(cudaMemsetAsync(h->ksk_count, 0, sizeof(int), h->stream));
+    LAUNCH(h, k_fully_blocked, dim3((g.mx + 127) / 128, g.my), 128, g, (const double *)h->nvert, h->ksk, h->ksk_count);
+    int cnt = 0;
+    CUDA_TRY(cudaMemcpyAsync(h->hbuf, h->ksk_count, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    TRY(sync(h));
+    memcpy(&cnt, h->hbuf, sizeof(int));
+    h->multinull = cnt == 0 ? 1 : 0;
+    h->ksk_version = h->op_version;
+  }
+  if (multinullspace) *multinullspace = h->multinull;
+  if (ksk) {
+    CUDA_TRY(cudaMemcpyAsync(ksk, h->ksk, nc * sizeof(int32_t),
+                             is_device_ptr(ksk) ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, h->stream));
+    TRY(sync(h));
+  }
+  return VFS_OK;
+}
+
+int vfs_poisson_nullspace_original(vfs_poisson *h, double *x) {
+  if (!h || !x) return fail(VFS_EINVAL, "null argument");
+  TRY(vfs_poisson_fully_blocked(h, nullptr, nullptr));
+  const Grid &g = h->g;
+  const size_t N = g.n();
+  const bool dev = is_device_ptr(x);
+  double *xd = dev ? x : h->stage;
+  if (!dev) TRY(upload(h, xd, x, N));
+  LAUNCH(h, k_nullspace_sums, kRedBlocks, 256, g, (const double *)h->nvert, (const int *)h->ksk, h->multinull,
+         (const double *)xd, h->partial);
+  double sm[4];
+  TRY(reduce_read(h, kRedBlocks, 4, sm));
+  // the reference's shift per region: sum / (-num) (poisson.c:813, 840, 865)
+  const double s0 = sm[0] / (-1.0 * sm[1]), s1 = h->multinull ? sm[2] / (-1.0 * sm[3]) : 0.;
+  LAUNCH(h, k_nullspace_apply, da_grid(g), 128, g, (const double *)h->nvert, (const int *)h->ksk, h->multinull, s0,
+         s1, xd);
+  if (!dev) TRY(download(h, x, xd, N));
+  return sync(h);
 }
 
 int vfs_poisson_guess_report(vfs_poisson *h, int *chosen, double *rel_res, double *est) {

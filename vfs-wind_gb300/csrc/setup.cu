@@ -601,6 +601,58 @@ __global__ void k_rhs_nullspace(Grid g, Box b, const double *__restrict__ nvert,
   }
 }
 
+// FullyBlocked (Source/poisson.c:1909-1993): per interior (i, j) column the
+// first k (boundary layers included) with nvert > 0.1 into ksk[j mx + i]
+// (-1 for none and on the boundary columns), and the count of interior
+// columns without one (the multiple-null-space flag is that count == 0).
+__global__ void k_fully_blocked(Grid g, const double *__restrict__ nvert, int *ksk, int *unblocked) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y;
+  if (i >= g.mx) return;
+  int first = -1;
+  if (i >= 1 && i < g.mx - 1 && j >= 1 && j < g.my - 1) {
+    for (int k = 0; k < g.mz; k++)
+      if (nvert[g.at(i, j, k)] > 0.1) { first = k; break; }
+    if (first < 0) atomicAdd(unblocked, 1);
+  }
+  ksk[(size_t)j * g.mx + i] = first;
+}
+
+// PoissonNullSpaceFunction_original (Source/poisson.c:757-943), first pass:
+// block partials over the interior cells with nvert < 0.1 of the sum of x
+// and the count, one pair of rows per region (multi: k below the column's
+// first blocked k, then k at or above it; else the whole interior).
+__global__ void k_nullspace_sums(Grid g, const double *__restrict__ nvert, const int *__restrict__ ksk, int multi,
+                                 const double *__restrict__ x, double *partial) {
+  double s[2] = {0., 0.}, c[2] = {0., 0.};
+  const size_t n = (size_t)(g.mx - 2) * (g.my - 2) * (g.mz - 2);
+  for (size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (size_t)gridDim.x * blockDim.x) {
+    const int i = 1 + (int)(q % (size_t)(g.mx - 2));
+    const size_t r = q / (size_t)(g.mx - 2);
+    const int j = 1 + (int)(r % (size_t)(g.my - 2)), k = 1 + (int)(r / (size_t)(g.my - 2));
+    const size_t t = g.at(i, j, k);
+    if (!(nvert[t] < 0.1)) continue;
+    const int reg = multi && k >= ksk[(size_t)j * g.mx + i] ? 1 : 0;
+    s[reg] += x[t];
+    c[reg] += 1.;
+  }
+  for (int q = 0; q < 4; q++) {
+    const double v = block_sum(q == 0 ? s[0] : q == 1 ? c[0] : q == 2 ? s[1] : c[1]);
+    if (threadIdx.x == 0) partial[(size_t)q * gridDim.x + blockIdx.x] = v;
+  }
+}
+// second pass: x += shift of its region on the interior cells with nvert <
+// 0.1; the boundary layers and the cells with nvert > 0.1 become 0
+__global__ void k_nullspace_apply(Grid g, const double *__restrict__ nvert, const int *__restrict__ ksk, int multi,
+                                  double shift0, double shift1, double *x) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y, k = blockIdx.z;
+  if (i >= g.mx) return;
+  const size_t t = g.at(i, j, k);
+  const bool bnd = i == 0 || i == g.mx - 1 || j == 0 || j == g.my - 1 || k == 0 || k == g.mz - 1;
+  const double nv = nvert[t];
+  if (!bnd && nv < 0.1) x[t] += multi && k >= ksk[(size_t)j * g.mx + i] ? shift1 : shift0;
+  if (bnd || nv > 0.1) x[t] = 0.;
+}
+
 // Remove_Nullspace (Source/poisson_hypre.c:202-263) on a box vector: sum and
 // count over nvert < 0.1
 __global__ void k_mean_partial(Box b, const uint8_t *fluid, const double *x, double *partial) {
@@ -909,7 +961,9 @@ __device__ __forceinline__ void restrict_body(Box bf, Box bc, int cx, int cy, in
 
 // MyInterpolation (poisson.c:527-670, GridInterpolation macro :474-507),
 // added onto the fine vector (the V-cycle correction).  add = 0 writes.
-template <typename T>
+// FSPLIT: the fine vector is in the parity-split row layout (the finest
+// FP32 level under the checkerboard smoother); blank flags stay natural.
+template <typename T, bool FSPLIT = false>
 __device__ __forceinline__ void prolong_body(Box bf, Box bc, int cx, int cy, int cz, const T *__restrict__ xc,
                                              const uint8_t *__restrict__ blank_c, const uint8_t *__restrict__ blank_f,
                                              T *xf, int add) {
@@ -923,7 +977,7 @@ __device__ __forceinline__ void prolong_body(Box bf, Box bc, int cx, int cy, int
   int ic, kc, ia, ka;
   if (!cx) { ic = I; ia = 0; } else { ic = (I + 1) / 2; ia = (I - 2 * ic) == 0 ? 1 : -1; if (I == 1 || I == mx - 2) ia = 0; }
   if (!cz) { kc = K; ka = 0; } else { kc = (K + 1) / 2; ka = (K - 2 * kc) == 0 ? 1 : -1; if (K == 1 || K == mz - 2) ka = 0; }
-  size_t c[2];
+  size_t c[2], cf[2];
   bool valid[2];
   int ja[2];
   uint8_t bf0[2], ni[2], nj[2], nk[2];
@@ -934,6 +988,7 @@ __device__ __forceinline__ void prolong_body(Box bf, Box bc, int cx, int cy, int
     valid[r] = j < bf.ny;
     if (!valid[r]) continue;
     c[r] = bf.at(i, j, k);
+    cf[r] = FSPLIT ? c[r] - i + split_pos(i, bf.nx) : c[r];
     const int J = j + 1;
     int jc;
     if (!cy) { jc = J; ja[r] = 0; } else { jc = (J + 1) / 2; ja[r] = (J - 2 * jc) == 0 ? 1 : -1; if (J == 1 || J == my - 2) ja[r] = 0; }
@@ -953,12 +1008,12 @@ __device__ __forceinline__ void prolong_body(Box bf, Box bc, int cx, int cy, int
       const int a = q & 1, bb = (q >> 1) & 1, cc = q >> 2;
       X[r][a][bb][cc] = xc[base + a * oi + bb * oj + cc * ok];
     }
-    xold[r] = add ? xf[c[r]] : (T)0;
+    xold[r] = add ? xf[cf[r]] : (T)0;
   }
 #pragma unroll
   for (int r = 0; r < 2; r++) {
     if (!valid[r]) continue;
-    if (bf0[r]) { if (!add) xf[c[r]] = (T)0; continue; }
+    if (bf0[r]) { if (!add) xf[cf[r]] = (T)0; continue; }
     // the reference zeroes an offset whose coarse neighbour is blank; an
     // offset already 0 reads the centre (its test reads the centre cell,
     // which an unblanked fine cell's parent is not).  Collapse the zeroed
@@ -973,8 +1028,8 @@ __device__ __forceinline__ void prolong_body(Box bf, Box bc, int cx, int cy, int
     for (int q = 0; q < 4; q++) X[r][q & 1][q >> 1][1] = zk ? X[r][q & 1][q >> 1][0] : X[r][q & 1][q >> 1][1];
     T v = (X[r][0][0][0] * (T)9 + X[r][0][1][0] * (T)3 + X[r][1][0][0] * (T)3 + X[r][1][1][0]) * (T)3. / (T)64. +
           (X[r][0][0][1] * (T)9 + X[r][0][1][1] * (T)3 + X[r][1][0][1] * (T)3 + X[r][1][1][1]) / (T)64.;
-    if (add) xf[c[r]] = xold[r] + v;
-    else xf[c[r]] = v;
+    if (add) xf[cf[r]] = xold[r] + v;
+    else xf[cf[r]] = v;
   }
 }
 
@@ -989,6 +1044,10 @@ __global__ void k_restrict_f64(Box bf, Box bc, int cx, int cy, int cz, const dou
 __global__ void k_prolong_f32(Box bf, Box bc, int cx, int cy, int cz, const float *xc, const uint8_t *blank_c,
                               const uint8_t *blank_f, float *xf, int add) {
   prolong_body<float>(bf, bc, cx, cy, cz, xc, blank_c, blank_f, xf, add);
+}
+__global__ void k_prolong_f32_split(Box bf, Box bc, int cx, int cy, int cz, const float *xc, const uint8_t *blank_c,
+                                    const uint8_t *blank_f, float *xf, int add) {
+  prolong_body<float, true>(bf, bc, cx, cy, cz, xc, blank_c, blank_f, xf, add);
 }
 __global__ void k_prolong_f64(Box bf, Box bc, int cx, int cy, int cz, const double *xc, const uint8_t *blank_c,
                               const uint8_t *blank_f, double *xf, int add) {

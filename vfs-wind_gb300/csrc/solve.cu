@@ -69,17 +69,19 @@ __global__ void k_pack16(size_t n, const double *__restrict__ A, __half2 *__rest
 // r = rhs - D (s x_c + sum_q c_q (x_q - x_c)): rounding the couplings to half
 // perturbs each one by at most 2^-11 relative and leaves the row sums (the
 // constant null space of the Neumann rows) exact.  44 operator bytes per row
-// instead of 76.  Colours and layouts as in residual_body.
-__global__ void __launch_bounds__(128) k_residual16(Box b, const __half2 *__restrict__ C,
-                                                    const float *__restrict__ D, const float *__restrict__ x,
-                                                    const float *__restrict__ rhs, float *__restrict__ r, int color) {
+// instead of 76.  Colours and layouts as in residual_body; SPLIT: x and rhs
+// in the parity-split row layout (r written as the colour selects).
+template <bool SPLIT>
+__device__ __forceinline__ void residual16_body(Box b, const __half2 *__restrict__ C, const float *__restrict__ D,
+                                                const float *__restrict__ x, const float *__restrict__ rhs,
+                                                float *__restrict__ r, int color) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y, k = blockIdx.z;
   int p;
   if (!colour_row(b, color, t, k, p)) return;
   const int i = split_cell(p, b.nx);
   uint32_t idx[NSLOT];
-  stencil_index(b, i, j, k, idx);
-  const uint32_t n = (uint32_t)b.n(), c = idx[CP], cs = c - i + p;
+  stencil_index_t<SPLIT>(b, i, j, k, idx);
+  const uint32_t n = (uint32_t)b.n(), c = idx[CP], row = c - (SPLIT ? p : i), cs = row + p, cn = row + i;
   const float xc = __ldg(&x[c]);
   float s = 0.f;
 #pragma unroll
@@ -90,7 +92,18 @@ __global__ void __launch_bounds__(128) k_residual16(Box b, const __half2 *__rest
   }
   const float2 f = __half22float2(__ldcs(&C[9 * n + cs]));
   s = fmaf(f.x, xc, s);
-  r[color == 2 || color == 3 ? cs : c] = rhs[c] - __ldcs(&D[cs]) * s;
+  r[color == 2 || color == 3 ? cs : cn] = rhs[SPLIT ? cs : cn] - __ldcs(&D[cs]) * s;
+}
+__global__ void __launch_bounds__(128) k_residual16(Box b, const __half2 *__restrict__ C,
+                                                    const float *__restrict__ D, const float *__restrict__ x,
+                                                    const float *__restrict__ rhs, float *__restrict__ r, int color) {
+  residual16_body<false>(b, C, D, x, rhs, r, color);
+}
+__global__ void __launch_bounds__(128) k_residual16_split(Box b, const __half2 *__restrict__ C,
+                                                          const float *__restrict__ D, const float *__restrict__ x,
+                                                          const float *__restrict__ rhs, float *__restrict__ r,
+                                                          int color) {
+  residual16_body<true>(b, C, D, x, rhs, r, color);
 }
 
 // FP64 y = A x on the unscaled operator.
@@ -398,7 +411,7 @@ __device__ __forceinline__ bool line_column(const Box &b, int color, int t, int 
 // column's threads walk split positions, so operator and factor loads
 // coalesce; x is natural.  Same chunked recurrences and scans as
 // line_sweep_body; only 5 words per cell are streamed.
-template <typename T, int M>
+template <typename T, int M, bool SPLIT = false>
 __device__ __forceinline__ void line_tri_body(Box b, const T *__restrict__ r, const T *__restrict__ Asp,
                                               const T *__restrict__ inv, const T *__restrict__ cp, T *x, T omega,
                                               int zero_guess, int color) {
@@ -411,8 +424,10 @@ __device__ __forceinline__ void line_tri_body(Box b, const T *__restrict__ r, co
   const int ny = b.ny, j0 = ty * M;
   const int cnt = valid ? max(0, min(M, ny - j0)) : 0;
   const uint32_t sj = b.nx;
-  const uint32_t cS = valid ? (uint32_t)b.at(pp, 0, k) : 0u;                     // operator / factor index
-  const uint32_t cX = valid ? (uint32_t)b.at(split_cell(pp, b.nx), 0, k) : 0u;  // natural index
+  const uint32_t cS = valid ? (uint32_t)b.at(pp, 0, k) : 0u;  // operator / factor index
+  // x (and a right-hand side used as r, colours 4/5) at the split position
+  // when the level's vectors are split, else natural
+  const uint32_t cX = SPLIT ? cS : (valid ? (uint32_t)b.at(split_cell(pp, b.nx), 0, k) : 0u);
   const uint32_t cR = (color == 2 || color == 3) ? cS : cX;
   // every load of the chunk up front (one memory round trip): the line
   // coefficients, factors, residual and the x being corrected
@@ -856,11 +871,20 @@ __global__ void k_scale_to(size_t n, const double *__restrict__ v, double s, con
 // The same into the FP32 V-cycle's right-hand side, with the products in
 // FP32 (the result is rounded to FP32 anyway and FP64 arithmetic is the
 // scarce pipe), one element per thread.
+// split_nx > 0: out is in the parity-split row layout of rows of split_nx
+// cells (the finest FP32 level's right-hand side under the checkerboard
+// smoother).
 __global__ void __launch_bounds__(256) k_scale_to32(size_t n, const double *__restrict__ v, float s,
                                                     const float *__restrict__ sinv, const float *__restrict__ scale,
-                                                    float *__restrict__ out) {
+                                                    float *__restrict__ out, int split_nx) {
   const size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (c < n) out[c] = (float)v[c] * ((sinv ? s * sinv[0] : s) * scale[c]);
+  if (c >= n) return;
+  size_t o = c;
+  if (split_nx > 0) {
+    const uint32_t i = (uint32_t)(c % (uint32_t)split_nx);
+    o = c - i + split_pos((int)i, split_nx);
+  }
+  out[o] = (float)v[c] * ((sinv ? s * sinv[0] : s) * scale[c]);
 }
 // ||V||^2 from the block partials into out[0], 1/||V|| into out[1] and
 // out32[0] (0 for a zero vector); one block
@@ -876,10 +900,18 @@ __global__ void k_reduce_norm(const double *partial, int nb, double *out, float 
   }
 }
 // out = x (the V-cycle's result in FP32 or FP64, widened), one element per thread
+// split_nx > 0: x32 is in the parity-split row layout (rows of split_nx)
 __global__ void __launch_bounds__(256) k_to64(size_t n, const float *__restrict__ x32,
-                                              const double *__restrict__ x64, double *__restrict__ out) {
+                                              const double *__restrict__ x64, double *__restrict__ out,
+                                              int split_nx) {
   const size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (c < n) out[c] = x32 ? (double)x32[c] : x64[c];
+  if (c >= n) return;
+  size_t o = c;
+  if (x32 && split_nx > 0) {
+    const uint32_t i = (uint32_t)(c % (uint32_t)split_nx);
+    o = c - i + split_pos((int)i, split_nx);
+  }
+  out[c] = x32 ? (double)x32[o] : x64[c];
 }
 __global__ void k_sumsq(size_t n, const double *__restrict__ x, double *partial) {
   double s = 0.;
@@ -1001,5 +1033,11 @@ __global__ void __launch_bounds__(256) k_hist_push(size_t n, const double *__res
 TYPED(float, f32, kLineMaxThreads, 1)
 TYPED(double, f64, kLineMaxThreads, 1)
 #undef TYPED
+// the finest FP32 level with x and the right-hand side in the split layout
+__global__ void __launch_bounds__(kLineMaxThreads, 1) k_line_tri_f32_split(Box b, const float *r, const float *Asp,
+                                                                          const float *inv, const float *cp, float *x,
+                                                                          float omega, int zg, int color) {
+  line_tri_body<float, kLineChunk, true>(b, r, Asp, inv, cp, x, omega, zg, color);
+}
 
 }  // namespace vfs

@@ -41,7 +41,8 @@ EXPORTS = [
     "vfs_read_petsc_vec", "vfs_write_petsc_vec", "vfs_read_grid", "vfs_read_ucd", "vfs_poisson_set_levelset",
     "vfs_poisson_ibm_search_nodes", "vfs_poisson_ibm_nodes", "vfs_poisson_ibm_interpolate", "vfs_poisson_ib_bc",
     "vfs_poisson_set_history", "vfs_poisson_history_guess", "vfs_poisson_set_network_period",
-    "vfs_poisson_history_record", "vfs_poisson_guess_report",
+    "vfs_poisson_history_record", "vfs_poisson_guess_report", "vfs_poisson_fully_blocked",
+    "vfs_poisson_nullspace_original",
 ]
 
 
@@ -160,6 +161,8 @@ def load(path=LIB_PATH):
     L.vfs_poisson_set_network_period.argtypes = [vp, C.c_int]
     L.vfs_poisson_history_record.argtypes = [vp, C.c_int]
     L.vfs_poisson_guess_report.argtypes = [vp, P(C.c_int), vp, vp]
+    L.vfs_poisson_fully_blocked.argtypes = [vp, P(C.c_int), vp]
+    L.vfs_poisson_nullspace_original.argtypes = [vp, vp]
     L.vfs_poisson_contra2cart.argtypes = [vp, dp, dp, C.c_int]
     L.vfs_poisson_set_levelset.argtypes = [vp, dp, dp, vp, C.c_int]
     L.vfs_read_petsc_vec.argtypes = [C.c_char_p, P(C.c_int64), vp]
@@ -470,6 +473,20 @@ class PoissonSolver:
 
     def set_network_period(self, period):
         _check(load().vfs_poisson_set_network_period(self.h, int(period)))
+
+    def fully_blocked(self):
+        """FullyBlocked: (multinullspace, ksk[my, mx]) -- the first k of every
+        interior column with nvert > 0.1 (-1 where none)."""
+        m = C.c_int()
+        ksk = np.zeros(self._shape()[1:], np.int32)
+        _check(load().vfs_poisson_fully_blocked(self.h, C.byref(m), _ptr(ksk, True)))
+        return bool(m.value), ksk
+
+    def nullspace_original(self, x):
+        """PoissonNullSpaceFunction_original on x (DA layout, in place for a
+        CUDA tensor; a numpy array is changed in place too)."""
+        _check(load().vfs_poisson_nullspace_original(self.h, _ptr(x, True)))
+        return x
 
     def guess_report(self):
         """What the last guess installed: (chosen, rel_res[3], est[3]) with

@@ -487,7 +487,7 @@ def run_ours(args):
     out_h = torch.empty(shape, dtype=torch.float64).pin_memory()
     host = (u_h.numpy(), p1_h.numpy(), p2_h.numpy(), out_h.numpy())
     ms_e2e, h2d, its_e2e = [], [], []
-    for r in range(1 + max(3, args.steps // 4)):
+    for r in range(1 + max(5, args.steps // 2)):
         u_h.copy_(step_inputs(n))
         p1_h.copy_(hist[-1])
         p2_h.copy_(hist[-2])

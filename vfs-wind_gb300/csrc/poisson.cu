@@ -525,6 +525,10 @@ struct vfs_poisson {
   bool spec_next = false, spec_valid = false;
   vfs_solve_opts spec_opts{};
   std::vector<Level> L;
+  // the hierarchy's build parameters (a new mask with the same ones refills
+  // the levels in place)
+  int hier_cmax = -1;
+  bool hier_ls = false;
   bool have_grid = false, have_nvert = false, have_rhs = false, have_phi = false;
   // graphs of the V-cycle per precision and parameters they were built for
   cudaGraphExec_t gexec[2] = {nullptr, nullptr};
@@ -848,20 +852,23 @@ LevelSet level_set(const vfs_poisson *h, const Level &l) {
   return ls;
 }
 
-// Operator, masks and line factors of one level (assembled from its metrics).
+// Operator, masks and line factors of one level (assembled from its
+// metrics) into its buffers, allocated on the first build.
 int build_level_operator(vfs_poisson *h, Level &l) {
   const size_t n = l.b.n();
-  TRY(dalloc(h, &l.A64, n * NSLOT));
-  TRY(dalloc(h, &l.A32, n * NSLOT));
-  TRY(dalloc(h, &l.C16, n * 10));
-  TRY(dalloc(h, &l.D32, n));
-  TRY(dalloc(h, &l.rowtype, n));
-  TRY(dalloc(h, &l.blank, n));
-  TRY(dalloc(h, &l.w64, n));
-  TRY(dalloc(h, &l.w32, n));
-  TRY(dalloc(h, &l.inv64, n)); TRY(dalloc(h, &l.cp64, n));
-  TRY(dalloc(h, &l.inv32, n)); TRY(dalloc(h, &l.cp32, n));
-  for (int q = 0; q < 4; q++) { TRY(dalloc(h, &l.v64[q], n)); TRY(dalloc(h, &l.v32[q], n)); }
+  if (!l.A64) {
+    TRY(dalloc(h, &l.A64, n * NSLOT));
+    TRY(dalloc(h, &l.A32, n * NSLOT));
+    TRY(dalloc(h, &l.C16, n * 10));
+    TRY(dalloc(h, &l.D32, n));
+    TRY(dalloc(h, &l.rowtype, n));
+    TRY(dalloc(h, &l.blank, n));
+    TRY(dalloc(h, &l.w64, n));
+    TRY(dalloc(h, &l.w32, n));
+    TRY(dalloc(h, &l.inv64, n)); TRY(dalloc(h, &l.cp64, n));
+    TRY(dalloc(h, &l.inv32, n)); TRY(dalloc(h, &l.cp32, n));
+    for (int q = 0; q < 4; q++) { TRY(dalloc(h, &l.v64[q], n)); TRY(dalloc(h, &l.v32[q], n)); }
+  }
   LAUNCH(h, k_assemble, box_grid(l.b), 128, l.g, l.b, l.nvert, l.met, 1, 0, 1, l.A64, l.rowtype, level_set(h, l));
   LAUNCH(h, k_level_masks, lin_grid(n), 256, l.g, l.b, l.nvert, l.blank, l.w64, l.w32, (double *)nullptr,
          (const double *)nullptr);
@@ -872,7 +879,37 @@ int build_level_operator(vfs_poisson *h, Level &l) {
   return VFS_OK;
 }
 
+// A new mask on the hierarchy's grid: the levels' shapes, coarsening,
+// coordinates and metrics do not depend on nvert, so every level keeps its
+// buffers; its mask is restricted again and its operator, line factors and
+// packed copy are refilled in place.  Only the coarsest level's dense
+// inverse (its size follows the dof count) is formed anew, and the V-cycle
+// graphs (which hold that count) are captured again at their next use.
+int refresh_hierarchy(vfs_poisson *h) {
+  drop_graphs(h);
+  h->L[0].nvert = h->nvert;
+  h->L[0].rho = h->ls_rho;
+  h->L[0].level = h->ls_level;
+  for (size_t li = 1; li < h->L.size(); li++) {
+    Level &f = h->L[li - 1], &q = h->L[li];
+    LAUNCH(h, k_nvert_restrict, da_grid(q.g), 128, f.g, q.g, f.cx, f.cy, f.cz, f.nvert, h->stage);
+    LAUNCH(h, k_nvert_fill, da_grid(q.g), 128, q.g, h->stage, q.nvert);
+    if (h->ls_on) {
+      LAUNCH(h, k_cellfield_restrict, da_grid(q.g), 128, f.g, q.g, f.cx, f.cy, f.cz, f.rho, q.rho);
+      LAUNCH(h, k_cellfield_restrict, da_grid(q.g), 128, f.g, q.g, f.cx, f.cy, f.cz, f.level, q.level);
+    }
+  }
+  for (Level &l : h->L) TRY(build_level_operator(h, l));
+  Level &c = h->L.back();
+  dfree(h, c.didx); dfree(h, c.dmap); dfree(h, c.dinv);
+  c.didx = c.dmap = nullptr;
+  c.dinv = nullptr;
+  TRY(build_coarsest(h, c));
+  return sync(h);
+}
+
 int build_hierarchy(vfs_poisson *h, int coarsest_max) {
+  if (!h->L.empty() && h->hier_cmax == coarsest_max && h->hier_ls == (h->ls_on != 0)) return refresh_hierarchy(h);
   for (size_t li = 0; li < h->L.size(); li++) free_level(h, h->L[li], li == 0);
   h->L.clear();
   drop_graphs(h);
@@ -932,12 +969,11 @@ int build_hierarchy(vfs_poisson *h, int coarsest_max) {
     }
     TRY(build_level_operator(h, l));
     TRY(sync(h));
-    if (li > 0) {  // coarse metrics are only needed for the assembly
-      free_metrics(h, l.met);
-      l.own_met = false;
-    }
+    // the coarse metrics stay for the assembly of later masks
   }
   TRY(build_coarsest(h, h->L.back()));
+  h->hier_cmax = coarsest_max;
+  h->hier_ls = h->ls_on != 0;
   return VFS_OK;
 }
 
@@ -1921,6 +1957,7 @@ void vfs_poisson_destroy(vfs_poisson *h) {
 
 int vfs_poisson_set_grid(vfs_poisson *h, const double *coor, const double *const *fm) {
   if (!h || !coor) return fail(VFS_EINVAL, "null argument");
+  h->hier_cmax = -1;  // new coordinates: the next mask builds the hierarchy afresh
   const size_t N = h->g.n();
   TRY(upload(h, h->coor, coor, 3 * N));
   TRY(form_metrics(h, h->g, h->coor, h->met));

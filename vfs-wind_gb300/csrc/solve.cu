@@ -923,44 +923,58 @@ __global__ void k_sumsq(size_t n, const double *__restrict__ x, double *partial)
 
 // ---- history projection of the initial guess ----
 // Block partials (grid-stride, fixed block count: deterministic) of the dot
-// products v . Y_j for j < k and of v . v: row j of `partial` holds v . Y_j,
-// row k holds v . v.
-__global__ void __launch_bounds__(256) k_hist_dots(size_t n, HistPtrs Y, int k, const double *__restrict__ v,
-                                                   double *partial) {
-  double s[kHistMax + 1];
+// products v . Y_j for j < K and of v . v: row j of `partial` holds v . Y_j,
+// row K holds v . v.  K is a template argument, so that no FMA of an
+// unused slot is issued on the FP64 pipe.
+template <int K>
+__device__ __forceinline__ void hist_dots_body(size_t n, const HistPtrs &Y, const double *__restrict__ v,
+                                               double *partial) {
+  double s[K + 1];
 #pragma unroll
-  for (int j = 0; j <= kHistMax; j++) s[j] = 0.;
+  for (int j = 0; j <= K; j++) s[j] = 0.;
   for (size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (size_t)gridDim.x * blockDim.x) {
     const double vc = v[c];
 #pragma unroll
-    for (int j = 0; j < kHistMax; j++)
-      if (j < k) s[j] = fma(vc, __ldg(&Y.p[j][c]), s[j]);
-    s[kHistMax] = fma(vc, vc, s[kHistMax]);
+    for (int j = 0; j < K; j++) s[j] = fma(vc, __ldg(&Y.p[j][c]), s[j]);
+    s[K] = fma(vc, vc, s[K]);
   }
-  for (int j = 0; j <= k; j++) {
-    const double t = block_sum(j < k ? s[j] : s[kHistMax]);
+#pragma unroll
+  for (int j = 0; j <= K; j++) {
+    const double t = block_sum(s[j]);
     if (threadIdx.x == 0) partial[(size_t)j * gridDim.x + blockIdx.x] = t;
+  }
+}
+__global__ void __launch_bounds__(256, 8) k_hist_dots(size_t n, HistPtrs Y, int k, const double *__restrict__ v,
+                                                   double *partial) {
+  switch (k) {
+    case 1: hist_dots_body<1>(n, Y, v, partial); break;
+    case 2: hist_dots_body<2>(n, Y, v, partial); break;
+    case 3: hist_dots_body<3>(n, Y, v, partial); break;
+    case 4: hist_dots_body<4>(n, Y, v, partial); break;
+    case 5: hist_dots_body<5>(n, Y, v, partial); break;
+    case 6: hist_dots_body<6>(n, Y, v, partial); break;
+    case 7: hist_dots_body<7>(n, Y, v, partial); break;
+    default: hist_dots_body<kHistMax>(n, Y, v, partial); break;
   }
 }
 
 // x = sum_j c_j X_j and r = b - sum_j c_j Y_j (Y_j = A X_j), with the block
 // partials of ||r||^2.  coefficients in `c` (device, k values).
-__global__ void __launch_bounds__(256) k_hist_combine(size_t n, HistPtrs X, HistPtrs Y, int k,
-                                                      const double *__restrict__ c, const double *__restrict__ b,
-                                                      double *__restrict__ x, double *__restrict__ r,
-                                                      double *partial) {
-  double cj[kHistMax];
+template <int K>
+__device__ __forceinline__ void hist_combine_body(size_t n, const HistPtrs &X, const HistPtrs &Y,
+                                                  const double *__restrict__ c, const double *__restrict__ b,
+                                                  double *__restrict__ x, double *__restrict__ r, double *partial) {
+  double cj[K];
 #pragma unroll
-  for (int j = 0; j < kHistMax; j++) cj[j] = j < k ? c[j] : 0.;
+  for (int j = 0; j < K; j++) cj[j] = c[j];
   double s = 0.;
   for (size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (size_t)gridDim.x * blockDim.x) {
     double xv = 0., yv = 0.;
 #pragma unroll
-    for (int j = 0; j < kHistMax; j++)
-      if (j < k) {
-        xv = fma(cj[j], __ldg(&X.p[j][q]), xv);
-        yv = fma(cj[j], __ldg(&Y.p[j][q]), yv);
-      }
+    for (int j = 0; j < K; j++) {
+      xv = fma(cj[j], __ldg(&X.p[j][q]), xv);
+      yv = fma(cj[j], __ldg(&Y.p[j][q]), yv);
+    }
     const double rv = b[q] - yv;
     x[q] = xv;
     r[q] = rv;
@@ -968,6 +982,21 @@ __global__ void __launch_bounds__(256) k_hist_combine(size_t n, HistPtrs X, Hist
   }
   s = block_sum(s);
   if (threadIdx.x == 0) partial[blockIdx.x] = s;
+}
+__global__ void __launch_bounds__(256, 8) k_hist_combine(size_t n, HistPtrs X, HistPtrs Y, int k,
+                                                      const double *__restrict__ c, const double *__restrict__ b,
+                                                      double *__restrict__ x, double *__restrict__ r,
+                                                      double *partial) {
+  switch (k) {
+    case 1: hist_combine_body<1>(n, X, Y, c, b, x, r, partial); break;
+    case 2: hist_combine_body<2>(n, X, Y, c, b, x, r, partial); break;
+    case 3: hist_combine_body<3>(n, X, Y, c, b, x, r, partial); break;
+    case 4: hist_combine_body<4>(n, X, Y, c, b, x, r, partial); break;
+    case 5: hist_combine_body<5>(n, X, Y, c, b, x, r, partial); break;
+    case 6: hist_combine_body<6>(n, X, Y, c, b, x, r, partial); break;
+    case 7: hist_combine_body<7>(n, X, Y, c, b, x, r, partial); break;
+    default: hist_combine_body<kHistMax>(n, X, Y, c, b, x, r, partial); break;
+  }
 }
 
 // Moments over the fluid cells of z, for the estimated error of a guess

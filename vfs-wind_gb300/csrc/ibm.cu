@@ -116,30 +116,38 @@ __device__ int point_cell(const double p[3], int ip, int jp, int kp, const HashB
   return -1;
 }
 
-__global__ void k_ibm_classify(Grid g, const double *__restrict__ cent, int ibi, HashBox H,
-                               const int *__restrict__ col_start, const int *__restrict__ col_tri,
-                               const int *__restrict__ col_kmax, const double *__restrict__ tv,
-                               const double *__restrict__ nf, const double *__restrict__ s_tab, double *nvert,
-                               int *failed) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x + 1, j = blockIdx.y + 1, k = blockIdx.z + 1;
-  if (i >= g.mx - 1) return;
+// Classification of one body (ibm_search_advanced, ibm.c:92-325) as a
+// copying pass over every DA point: boundary points take src unchanged,
+// interior points whose centre lies in the body's hash box the larger of
+// their value and the ray-parity test (4 inside), body 0 first clearing
+// every value below 5 (src may be dst: each point reads and writes only
+// itself).
+__global__ void k_ibm_classify_from(Grid g, const double *__restrict__ cent, int ibi, HashBox H,
+                                    const int *__restrict__ col_start, const int *__restrict__ col_tri,
+                                    const int *__restrict__ col_kmax, const double *__restrict__ tv,
+                                    const double *__restrict__ nf, const double *__restrict__ s_tab, const double *src,
+                                    double *dst, int *failed) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y, k = blockIdx.z;
+  if (i >= g.mx) return;
   const size_t t = g.at(i, j, k);
-  double nv = nvert[t];
-  if (ibi == 0 && nv < 5.) nv = 0;
-  const double p[3] = {cent[t * 3], cent[t * 3 + 1], cent[t * 3 + 2]};
-  if (p[0] > H.xmin && p[0] < H.xmax && p[1] > H.ymin && p[1] < H.ymax && p[2] > H.zmin && p[2] < H.zmax) {
-    const int ic = (int)floor((p[0] - H.xmin) / H.dcx);
-    const int jc = (int)floor((p[1] - H.ymin) / H.dcy);
-    const int kc = (int)floor((p[2] - H.zmin) / H.dcz);
-    int val = point_cell(p, ic, jc, kc, H, col_start, col_tri, col_kmax, tv, nf, s_tab);
-    if (val < 0) {
-      atomicAdd(failed, 1);
-      val = 0;
+  double nv = src[t];
+  if (i >= 1 && i < g.mx - 1 && j >= 1 && j < g.my - 1 && k >= 1 && k < g.mz - 1) {
+    if (ibi == 0 && nv < 5.) nv = 0;
+    const double p[3] = {cent[t * 3], cent[t * 3 + 1], cent[t * 3 + 2]};
+    if (p[0] > H.xmin && p[0] < H.xmax && p[1] > H.ymin && p[1] < H.ymax && p[2] > H.zmin && p[2] < H.zmax) {
+      const int ic = (int)floor((p[0] - H.xmin) / H.dcx);
+      const int jc = (int)floor((p[1] - H.ymin) / H.dcy);
+      const int kc = (int)floor((p[2] - H.zmin) / H.dcz);
+      int val = point_cell(p, ic, jc, kc, H, col_start, col_tri, col_kmax, tv, nf, s_tab);
+      if (val < 0) {
+        atomicAdd(failed, 1);
+        val = 0;
+      }
+      nv = nv > val ? nv : (double)val;
+      if (nv < 0) nv = 0;
     }
-    nv = nv > val ? nv : (double)val;
-    if (nv < 0) nv = 0;
   }
-  nvert[t] = nv;
+  dst[t] = nv;
 }
 
 // near-boundary dilation over every DA point (ibm.c:326-348); a parallel pass
@@ -167,11 +175,8 @@ __global__ void k_ibm_dilate(Grid g, const double *src, double *dst) {
 }
 
 // back to 3 / 1 and the wall rows of bctype -1 / -2 (ibm.c:514-543)
-__global__ void k_ibm_finish(Grid g, int b0, int b1, int b2, int b3, int b4, int b5, double *nvert) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x + 1, j = blockIdx.y + 1, k = blockIdx.z + 1;
-  if (i >= g.mx - 1) return;
-  const size_t t = g.at(i, j, k);
-  double v = nvert[t];
+__device__ __forceinline__ double ibm_finish_value(const Grid &g, int b0, int b1, int b2, int b3, int b4, int b5,
+                                                   int i, int j, int k, double v) {
   if ((int)(v + 0.5) == 2) v = 1;
   if ((int)(v + 0.5) == 4) v = 3;
   for (int q = -1; q >= -2; q--) {
@@ -182,7 +187,40 @@ __global__ void k_ibm_finish(Grid g, int b0, int b1, int b2, int b3, int b4, int
     if (b4 == q && k == 1) v = 1;
     if (b5 == q && k == g.mz - 2) v = 1;
   }
-  nvert[t] = v;
+  return v;
+}
+__global__ void k_ibm_finish(Grid g, int b0, int b1, int b2, int b3, int b4, int b5, double *nvert) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x + 1, j = blockIdx.y + 1, k = blockIdx.z + 1;
+  if (i >= g.mx - 1) return;
+  const size_t t = g.at(i, j, k);
+  nvert[t] = ibm_finish_value(g, b0, b1, b2, b3, b4, b5, i, j, k, nvert[t]);
+}
+// the dilation and the finishing pass in one (the search without IB node
+// records, where nothing reads the dilated marks in between): every DA
+// point of dst gets the dilation of src, the interior points then their
+// finished value
+__global__ void k_ibm_dilate_finish(Grid g, int b0, int b1, int b2, int b3, int b4, int b5,
+                                    const double *__restrict__ src, double *__restrict__ dst) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y, k = blockIdx.z;
+  if (i >= g.mx) return;
+  const size_t t = g.at(i, j, k);
+  double v = src[t];
+  if (v < 0) v = 0;
+  if ((int)(v + 0.5) != 4) {
+    const int ip = i < g.mx - 1 ? i + 1 : i, im = i > 0 ? i - 1 : i;
+    const int jp = j < g.my - 1 ? j + 1 : j, jm = j > 0 ? j - 1 : j;
+    const int kp = k < g.mz - 1 ? k + 1 : k, km = k > 0 ? k - 1 : k;
+    for (int kk = km; kk <= kp; kk++)
+      for (int jj = jm; jj <= jp; jj++)
+        for (int ii = im; ii <= ip; ii++) {
+          double w = src[g.at(ii, jj, kk)];
+          if (w < 0) w = 0;
+          if ((int)(w + 0.5) == 4) v = v > 2 ? v : 2;
+        }
+  }
+  if (i >= 1 && i < g.mx - 1 && j >= 1 && j < g.my - 1 && k >= 1 && k < g.mz - 1)
+    v = ibm_finish_value(g, b0, b1, b2, b3, b4, b5, i, j, k, v);
+  dst[t] = v;
 }
 
 // ---- IB interpolation records (ibm.c:373-508) ----
@@ -532,23 +570,28 @@ int ibm_search_impl(vfs_poisson *h, int ibi, int n_v, const double *xyz, int n_e
   std::vector<double> s_tab(kMaxTries + 1, 0.);
   for (int q = 1; q <= kMaxTries; q++) s_tab[q] = glibc_rand_first((unsigned)q) / ((double)2147483647 + 1) - 0.5;
 
-  // device copies (freed before returning)
+  // device copies in the handle's search buffers (grown on demand)
   const size_t N = g.n();
-  void *buf[9] = {};
-  auto cleanup = [&]() {
-    for (void *p : buf)
-      if (p) cudaFree(p);
-  };
+  void **buf = cx.scratch->buf;
   size_t sizes[9] = {col_start.size() * 4, std::max<size_t>(col_tri.size(), 1) * 4,
                      std::max<size_t>(col_kmax.size(), 1) * 4, tv.size() * 8, nf.size() * 8, s_tab.size() * 8,
                      N * 8, N * 8, 4};
-  for (int q = 0; q < 9; q++)
-    if (cudaMalloc(&buf[q], sizes[q]) != cudaSuccess) {
-      cudaGetLastError();
-      cleanup();
-      return fail(VFS_ENOMEM, "device allocation for the surface search failed");
-    }
   cudaStream_t st = cx.stream;
+  for (int q = 0; q < 9; q++)
+    if (cx.scratch->cap[q] < sizes[q]) {
+      if (buf[q]) {
+        cudaStreamSynchronize(st);
+        cudaFree(buf[q]);
+      }
+      buf[q] = nullptr;
+      cx.scratch->cap[q] = 0;
+      if (cudaMalloc(&buf[q], sizes[q]) != cudaSuccess) {
+        cudaGetLastError();
+        buf[q] = nullptr;
+        return fail(VFS_ENOMEM, "device allocation for the surface search failed");
+      }
+      cx.scratch->cap[q] = sizes[q];
+    }
   const void *host[6] = {col_start.data(), col_tri.data(), col_kmax.data(), tv.data(), nf.data(), s_tab.data()};
   size_t hsz[6] = {col_start.size() * 4, col_tri.size() * 4, col_kmax.size() * 4, tv.size() * 8, nf.size() * 8,
                    s_tab.size() * 8};
@@ -556,11 +599,37 @@ int ibm_search_impl(vfs_poisson *h, int ibi, int n_v, const double *xyz, int n_e
     if (hsz[q]) cudaMemcpyAsync(buf[q], host[q], hsz[q], cudaMemcpyHostToDevice, st);
   double *dnv = (double *)buf[6], *dtmp = (double *)buf[7];
   int *dfail = (int *)buf[8];
-  cudaMemcpyAsync(dnv, nvert, N * 8, on_device(nvert) ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, st);
+  const bool dev = on_device(nvert);
+  int b[6] = {0, 0, 0, 0, 0, 0};
+  if (bctype)
+    for (int q = 0; q < 6; q++) b[q] = bctype[q];
+  // the classification reads nvert where it lies (a host array is staged)
+  const double *src = nvert;
+  if (!dev) {
+    cudaMemcpyAsync(dtmp, nvert, N * 8, cudaMemcpyHostToDevice, st);
+    src = dtmp;
+  }
   cudaMemsetAsync(dfail, 0, 4, st);
   dim3 gi((g.mx - 2 + 127) / 128, g.my - 2, g.mz - 2), gd((g.mx + 127) / 128, g.my, g.mz);
-  k_ibm_classify<<<gi, 128, 0, st>>>(g, cx.cent, ibi, H, (int *)buf[0], (int *)buf[1], (int *)buf[2],
-                                     (double *)buf[3], (double *)buf[4], (double *)buf[5], dnv, dfail);
+  k_ibm_classify_from<<<gd, 128, 0, st>>>(g, cx.cent, ibi, H, (int *)buf[0], (int *)buf[1], (int *)buf[2],
+                                          (double *)buf[3], (double *)buf[4], (double *)buf[5], src, dnv, dfail);
+  if (!want_nodes) {
+    // dilation and finish in one pass, straight into a device nvert
+    double *out = dev ? nvert : dtmp;
+    k_ibm_dilate_finish<<<gd, 128, 0, st>>>(g, b[0], b[1], b[2], b[3], b[4], b[5], dnv, out);
+    *cx.launches += 2;
+    int nfail = 0;
+    if (!dev) cudaMemcpyAsync(nvert, dtmp, N * 8, cudaMemcpyDeviceToHost, st);
+    cudaMemcpyAsync(&nfail, dfail, 4, cudaMemcpyDeviceToHost, st);
+    cudaError_t e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      return fail(VFS_ECUDA, std::string("surface search: ") + cudaGetErrorString(e));
+    }
+    if (n_failed) *n_failed = nfail;
+    if (n_nodes) *n_nodes = 0;
+    return VFS_OK;
+  }
   k_ibm_dilate<<<gd, 128, 0, st>>>(g, dnv, dtmp);
   int nodes_found = 0;
   if (want_nodes) {  // the IB nodes (marked 2) and their interpolation records
@@ -610,7 +679,6 @@ int ibm_search_impl(vfs_poisson *h, int ibi, int n_v, const double *xyz, int n_e
       cudaGetLastError();
       if (body.nodes) cudaFree(body.nodes);
       if (body.tri) cudaFree(body.tri);
-      cleanup();
       return fail(VFS_ECUDA, "IB node records: allocation or launch failed");
     }
     auto &B = *cx.bodies;
@@ -619,16 +687,12 @@ int ibm_search_impl(vfs_poisson *h, int ibi, int n_v, const double *xyz, int n_e
     if (B[ibi].tri) cudaFree(B[ibi].tri);
     B[ibi] = body;
   }
-  int b[6] = {0, 0, 0, 0, 0, 0};
-  if (bctype)
-    for (int q = 0; q < 6; q++) b[q] = bctype[q];
   k_ibm_finish<<<gi, 128, 0, st>>>(g, b[0], b[1], b[2], b[3], b[4], b[5], dtmp);
   *cx.launches += 3;
   int nfail = 0;
   cudaMemcpyAsync(nvert, dtmp, N * 8, on_device(nvert) ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, st);
   cudaMemcpyAsync(&nfail, dfail, 4, cudaMemcpyDeviceToHost, st);
   cudaError_t e = cudaStreamSynchronize(st);
-  cleanup();
   if (e != cudaSuccess) {
     cudaGetLastError();
     return fail(VFS_ECUDA, std::string("surface search: ") + cudaGetErrorString(e));

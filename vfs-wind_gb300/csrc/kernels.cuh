@@ -182,12 +182,19 @@ struct IbmBody {
   vfs_ibm_node *nodes = nullptr;
   int *tri = nullptr;
 };
+// device buffers of the surface search, kept by the handle and grown on
+// demand (no allocation or free, and so no device synchronisation, per body)
+struct IbmScratch {
+  void *buf[9] = {};
+  size_t cap[9] = {};
+};
 struct IbmContext {
   cudaStream_t stream;
   Grid g;
   const double *cent;
   int64_t *launches;
   std::vector<IbmBody> *bodies;
+  IbmScratch *scratch;
 };
 // ibm.cu: the IB interpolation and IB_BC kernels (launched by poisson.cu)
 __global__ void k_ibm_apply(Grid g, const vfs_ibm_node *nodes, int n_nodes, const int *tri, const double *u_surf,

@@ -470,6 +470,7 @@ struct vfs_poisson {
   int gsmooth = 2;  // binomial passes over the prolonged correction
   std::vector<IbmBody> ibm_bodies;  // IB node records per body (ibm.cu)
   double *ibm_work = nullptr;        // 5 N words + the surface velocities (allocated on first use)
+  IbmScratch ibm_scratch;            // the surface search's buffers
   size_t ibm_work_len = 0;
   // residual of the iterate installed by the learned guess, handed to the
   // next solve (warm_start 2) so that it does not form it again
@@ -1838,6 +1839,7 @@ int ibm_context(vfs_poisson *h, IbmContext *c) {
   c->cent = h->met.cent;
   c->launches = &h->launches;
   c->bodies = &h->ibm_bodies;
+  c->scratch = &h->ibm_scratch;
   return VFS_OK;
 }
 }  // namespace vfs
@@ -1936,6 +1938,8 @@ void vfs_poisson_destroy(vfs_poisson *h) {
   drop_graphs(h);
   for (void *p : h->allocs) cudaFree(p);
   h->allocs.clear();
+  for (void *p : h->ibm_scratch.buf)
+    if (p) cudaFree(p);
   for (auto &b : h->ibm_bodies) {
     if (b.nodes) cudaFree(b.nodes);
     if (b.tri) cudaFree(b.tri);

@@ -99,6 +99,10 @@ typedef struct {
                          Gram-Schmidt in one pass (PETSc GMRES's default
                          refinement "never"), 1 classical Gram-Schmidt
                          with delayed reorthogonalisation (DCGS2)          */
+  int nu2_near;       /* post sweeps for a solve whose initial residual is
+                         within 32x of rtol (default 4; 0: nu2): one
+                         stronger V-cycle then often finishes it, where
+                         nu2 sweeps would need a second iteration          */
 } vfs_solve_opts;
 
 typedef struct {

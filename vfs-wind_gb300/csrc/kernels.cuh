@@ -55,9 +55,10 @@ __global__ void k_nullspace_sums(Grid g, const double *nvert, const int *ksk, in
 __global__ void k_nullspace_apply(Grid g, const double *nvert, const int *ksk, int multi, double shift0,
                                   double shift1, double *x);
 __global__ void k_mean_partial(Box b, const uint8_t *fluid, const double *x, double *partial);
-__global__ void k_shift_fluid(Box b, const uint8_t *fluid, const double *sums, double *x);
 __global__ void k_fluid_mask(Grid g, Box b, const double *nvert, uint8_t *fluid);
-__global__ void k_box_to_da_phi(Grid g, Box b, const double *nvert, const double *x, double *phi);
+__global__ void k_mean_shift(double *sums);
+__global__ void k_box_to_da_phi(Grid g, Box b, const double *nvert, const double *x, double *phi,
+                                const double *shift);
 __global__ void k_da_to_box(Grid g, Box b, const double *da, double *x);
 __global__ void k_box_to_da(Grid g, Box b, const double *x, double *da);
 __global__ void k_update_pressure(Grid g, const double *nvert, const double *phi, double *p);

@@ -532,10 +532,18 @@ struct vfs_poisson {
   bool hier_ls = false;
   bool have_grid = false, have_nvert = false, have_rhs = false, have_phi = false;
   // graphs of the V-cycle per precision and parameters they were built for
-  cudaGraphExec_t gexec[2] = {nullptr, nullptr};
-  int64_t gnodes[2] = {0, 0};
-  int gparams[2][4] = {{-1, -1, -1, -1}, {-1, -1, -1, -1}};
-  double gomega[2] = {0, 0};
+  // captured V-cycles per precision, a few parameter sets each (least
+  // recently used one replaced)
+  struct GraphSlot {
+    cudaGraphExec_t exec = nullptr;
+    int64_t nodes = 0;
+    int params[4] = {-1, -1, -1, -1};
+    double omega = 0.;
+    uint64_t used = 0;
+  };
+  static constexpr int kGraphSlots = 4;
+  GraphSlot gslot[2][kGraphSlots];
+  uint64_t gclock = 0;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   bool own_stream = true;
   // live timing of the level-0 line sweeps (the dominant kernel)
@@ -834,9 +842,10 @@ void free_level(vfs_poisson *h, Level &l, bool level0) {
 
 void drop_graphs(vfs_poisson *h) {
   for (int p = 0; p < 2; p++) {
-    if (h->gexec[p]) cudaGraphExecDestroy(h->gexec[p]);
-    h->gexec[p] = nullptr;
-    h->gparams[p][0] = -1;
+    for (auto &g : h->gslot[p]) {
+      if (g.exec) cudaGraphExecDestroy(g.exec);
+      g = vfs_poisson::GraphSlot{};
+    }
   }
 }
 
@@ -1198,33 +1207,37 @@ int run_vcycle(vfs_poisson *h, const vfs_solve_opts &o) {
     vcycle<T>(h, 0, o.nu1, o.nu2, (T)o.omega, o.smoother);
     return VFS_OK;
   }
-  if (!h->gexec[p] || h->gparams[p][0] != o.nu1 || h->gparams[p][1] != o.nu2 || h->gomega[p] != o.omega ||
-      h->gparams[p][2] != (int)h->prof || h->gparams[p][3] != o.smoother) {
+  const int key[4] = {o.nu1, o.nu2, (int)h->prof, o.smoother};
+  vfs_poisson::GraphSlot *slot = nullptr, *victim = &h->gslot[p][0];
+  for (auto &g : h->gslot[p]) {
+    if (g.exec && g.omega == o.omega && std::equal(key, key + 4, g.params)) { slot = &g; break; }
+    if (!g.exec || (victim->exec && g.used < victim->used)) victim = &g;
+  }
+  if (!slot) {
+    slot = victim;
     h->pcount = 0;
-    if (h->gexec[p]) cudaGraphExecDestroy(h->gexec[p]);
-    h->gexec[p] = nullptr;
+    if (slot->exec) cudaGraphExecDestroy(slot->exec);
+    *slot = vfs_poisson::GraphSlot{};
     cudaGraph_t graph;
     int64_t before = h->launches;
     CUDA_TRY(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
     vcycle<T>(h, 0, o.nu1, o.nu2, (T)o.omega, o.smoother);
     CUDA_TRY(cudaStreamEndCapture(h->stream, &graph));
-    h->gnodes[p] = h->launches - before;
+    slot->nodes = h->launches - before;
     h->launches = before;
-    cudaError_t e = cudaGraphInstantiate(&h->gexec[p], graph, 0);
+    cudaError_t e = cudaGraphInstantiate(&slot->exec, graph, 0);
     cudaGraphDestroy(graph);
     if (e != cudaSuccess) {
       cudaGetLastError();
-      h->gexec[p] = nullptr;
+      slot->exec = nullptr;
       return fail(VFS_ECUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
     }
-    h->gparams[p][0] = o.nu1;
-    h->gparams[p][1] = o.nu2;
-    h->gparams[p][2] = (int)h->prof;
-    h->gparams[p][3] = o.smoother;
-    h->gomega[p] = o.omega;
+    std::copy(key, key + 4, slot->params);
+    slot->omega = o.omega;
   }
-  CUDA_TRY(cudaGraphLaunch(h->gexec[p], h->stream));
-  h->launches += h->gnodes[p];
+  slot->used = ++h->gclock;
+  CUDA_TRY(cudaGraphLaunch(slot->exec, h->stream));
+  h->launches += slot->nodes;
   return VFS_OK;
 }
 
@@ -1664,6 +1677,10 @@ int arnoldi_enqueue(vfs_poisson *h, int jj, int nbd, const vfs_solve_opts &o, in
   return VFS_OK;
 }
 
+// A solve whose initial residual is within this factor of rtol runs its
+// V-cycles with opts.nu2_near post sweeps.
+constexpr double kNearStart = 32.;
+
 // The options of a solve that may resume from the speculative step 0: the
 // same preconditioner and orthogonalisation.
 bool spec_matches(const vfs_solve_opts &a, const vfs_solve_opts &b) {
@@ -1688,7 +1705,10 @@ bool spec_matches(const vfs_solve_opts &a, const vfs_solve_opts &b) {
 // again; column j enters with the norm of the once-projected vector, which
 // gives the residual estimate of the convergence test.  One host read-back
 // per step.
-int fgmres(vfs_poisson *h, const vfs_solve_opts &o, vfs_solve_stats *st) {
+int fgmres(vfs_poisson *h, const vfs_solve_opts &oin, vfs_solve_stats *st) {
+  // the options of this solve: nu2_near post sweeps when it starts within
+  // kNearStart x rtol (set once the initial residual is known)
+  vfs_solve_opts o = oin;
   const size_t n = h->box.n();
   const int m = o.restart;
   // a larger basis is allocated afresh: the speculative step's vectors go
@@ -1730,6 +1750,7 @@ int fgmres(vfs_poisson *h, const vfs_solve_opts &o, vfs_solve_stats *st) {
   }
   rel = beta / bn;
   st->initial_rel_residual = rel;
+  if (o.nu2_near > 0 && rel <= kNearStart * o.rtol) o.nu2 = o.nu2_near;
   // rotate the formed column j by rotations 0..j-1, form rotation j and
   // apply it to the right-hand side gv
   auto rotate = [&](int j) {
@@ -1863,6 +1884,7 @@ void vfs_poisson_default_opts(vfs_solve_opts *o) {
   o->warm_start = 0;
   o->smoother = 4;
   o->orth = 0;
+  o->nu2_near = 4;
 }
 
 int vfs_poisson_create(const vfs_grid_desc *gd, vfs_poisson **out) {
@@ -2262,12 +2284,15 @@ int vfs_poisson_solve(vfs_poisson *h, double *phi, const vfs_solve_opts *opts, v
   TRY(fgmres(h, o, &st));
   if (h->hist_cap && h->hist_record && st.initial_rel_residual > 0. && st.rel_residual <= o.rtol)
     TRY(hist_push(h));
-  if (h->desc.bctype3 != -10 && !(h->ls_on && h->ls_bc5 == 4)) {  // Remove_Nullspace of phi (:604-608)
+  // Remove_Nullspace of phi (:604-608), its shift applied by the DA output
+  const bool shift = h->desc.bctype3 != -10 && !(h->ls_on && h->ls_bc5 == 4);
+  if (shift) {
     LAUNCH(h, k_mean_partial, kRedBlocks, 256, h->box, h->fluid, h->x, h->partial);
     LAUNCH(h, k_reduce_rows, 2, 1024, h->partial, kRedBlocks, 2, h->red);
-    LAUNCH(h, k_shift_fluid, kRedBlocks, 256, h->box, h->fluid, h->red, h->x);
+    LAUNCH(h, k_mean_shift, 1, 32, h->red);
   }
-  LAUNCH(h, k_box_to_da_phi, da_grid(h->g), 128, h->g, h->box, h->nvert, h->x, h->phi_da);
+  LAUNCH(h, k_box_to_da_phi, da_grid(h->g), 128, h->g, h->box, h->nvert, h->x, h->phi_da,
+         shift ? (const double *)h->red + 2 : nullptr);
   if (phi) TRY(download(h, phi, h->phi_da, h->g.n()));
   CUDA_TRY(cudaEventRecord(h->ev1, h->stream));
   TRY(sync(h));

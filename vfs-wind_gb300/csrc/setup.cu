@@ -664,12 +664,6 @@ __global__ void k_mean_partial(Box b, const uint8_t *fluid, const double *x, dou
   double tc = block_sum(cnt);
   if (threadIdx.x == 0) { partial[blockIdx.x] = ts; partial[gridDim.x + blockIdx.x] = tc; }
 }
-__global__ void k_shift_fluid(Box b, const uint8_t *fluid, const double *sums, double *x) {
-  const double val = -sums[0] / sums[1];
-  const size_t n = b.n();
-  for (size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (size_t)gridDim.x * blockDim.x)
-    if (fluid[c]) x[c] += val;
-}
 __global__ void k_fluid_mask(Grid g, Box b, const double *nvert, uint8_t *fluid) {
   size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= b.n()) return;
@@ -679,16 +673,30 @@ __global__ void k_fluid_mask(Grid g, Box b, const double *nvert, uint8_t *fluid)
   fluid[c] = nvert[g.at(i, j, k)] < 0.1 ? 1 : 0;
 }
 
+// Remove_Nullspace's shift from the fluid sum and count (sums[0], sums[1]):
+// sums[2] = -sum / count, as k_shift_fluid forms it
+__global__ void k_mean_shift(double *sums) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) sums[2] = -sums[0] / sums[1];
+}
+
 // Convert_Phi2_Phi (Source/poisson.c:98-186): box phi -> DA phi, zero on
 // non-dof cells and non-periodic ghosts, partner values on periodic ghosts.
-__global__ void k_box_to_da_phi(Grid g, Box b, const double *nvert, const double *x, double *phi) {
+// With `shift` (device, one value), Remove_Nullspace's x += shift on the
+// fluid cells (nvert < 0.1) is applied on the way (x itself is left as is).
+__global__ void k_box_to_da_phi(Grid g, Box b, const double *nvert, const double *x, double *phi,
+                                const double *shift) {
   int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y, k = blockIdx.z;
   if (i >= g.mx) return;
   int a, bb, c, fi, fj, fk;
   g.remap(i, j, k, a, bb, c, fi, fj, fk);
   double v = 0.;
-  if (a >= 1 && a < g.mx - 1 && bb >= 1 && bb < g.my - 1 && c >= 1 && c < g.mz - 1)
-    if (!((int)nvert[g.at(a, bb, c)] > kThr)) v = x[b.at(a - 1, bb - 1, c - 1)];
+  if (a >= 1 && a < g.mx - 1 && bb >= 1 && bb < g.my - 1 && c >= 1 && c < g.mz - 1) {
+    const double nv = nvert[g.at(a, bb, c)];
+    if (!((int)nv > kThr)) {
+      v = x[b.at(a - 1, bb - 1, c - 1)];
+      if (shift && nv < 0.1) v += shift[0];
+    }
+  }
   phi[g.at(i, j, k)] = v;
 }
 // DA -> box copy of the interior (warm start / inspection input)

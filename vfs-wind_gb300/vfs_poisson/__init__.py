@@ -64,7 +64,8 @@ class GridDesc(C.Structure):
 class SolveOpts(C.Structure):
     _fields_ = [("rtol", C.c_double), ("max_it", C.c_int), ("restart", C.c_int), ("precision", C.c_int),
                 ("nu1", C.c_int), ("nu2", C.c_int), ("omega", C.c_double), ("use_graphs", C.c_int),
-                ("coarsest_max", C.c_int), ("warm_start", C.c_int), ("smoother", C.c_int), ("orth", C.c_int)]
+                ("coarsest_max", C.c_int), ("warm_start", C.c_int), ("smoother", C.c_int), ("orth", C.c_int),
+                ("nu2_near", C.c_int)]
 
 
 class UNetBatch(C.Structure):

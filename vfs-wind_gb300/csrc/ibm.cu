@@ -126,7 +126,7 @@ __global__ void k_ibm_classify_from(Grid g, const double *__restrict__ cent, int
                                     const int *__restrict__ col_start, const int *__restrict__ col_tri,
                                     const int *__restrict__ col_kmax, const double *__restrict__ tv,
                                     const double *__restrict__ nf, const double *__restrict__ s_tab, const double *src,
-                                    double *dst, int *failed) {
+                                    double *dst, uint8_t *is4, int *failed) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y, k = blockIdx.z;
   if (i >= g.mx) return;
   const size_t t = g.at(i, j, k);
@@ -148,6 +148,10 @@ __global__ void k_ibm_classify_from(Grid g, const double *__restrict__ cent, int
     }
   }
   dst[t] = nv;
+  // the dilation's test of this point as a neighbour, (int)(max(v, 0) + 0.5)
+  // == 4, once here instead of in each of its 27 neighbours (integer loads
+  // there; FP64 arithmetic is the scarce pipe)
+  if (is4) is4[t] = (int)((nv < 0 ? 0. : nv) + 0.5) == 4;
 }
 
 // near-boundary dilation over every DA point (ibm.c:326-348); a parallel pass
@@ -200,23 +204,22 @@ __global__ void k_ibm_finish(Grid g, int b0, int b1, int b2, int b3, int b4, int
 // point of dst gets the dilation of src, the interior points then their
 // finished value
 __global__ void k_ibm_dilate_finish(Grid g, int b0, int b1, int b2, int b3, int b4, int b5,
-                                    const double *__restrict__ src, double *__restrict__ dst) {
+                                    const double *__restrict__ src, const uint8_t *__restrict__ is4,
+                                    double *__restrict__ dst) {
   int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y, k = blockIdx.z;
   if (i >= g.mx) return;
   const size_t t = g.at(i, j, k);
   double v = src[t];
   if (v < 0) v = 0;
-  if ((int)(v + 0.5) != 4) {
+  if (!is4[t]) {
     const int ip = i < g.mx - 1 ? i + 1 : i, im = i > 0 ? i - 1 : i;
     const int jp = j < g.my - 1 ? j + 1 : j, jm = j > 0 ? j - 1 : j;
     const int kp = k < g.mz - 1 ? k + 1 : k, km = k > 0 ? k - 1 : k;
+    bool near = false;
     for (int kk = km; kk <= kp; kk++)
       for (int jj = jm; jj <= jp; jj++)
-        for (int ii = im; ii <= ip; ii++) {
-          double w = src[g.at(ii, jj, kk)];
-          if (w < 0) w = 0;
-          if ((int)(w + 0.5) == 4) v = v > 2 ? v : 2;
-        }
+        for (int ii = im; ii <= ip; ii++) near |= is4[g.at(ii, jj, kk)] != 0;
+    if (near) v = v > 2 ? v : 2;
   }
   if (i >= 1 && i < g.mx - 1 && j >= 1 && j < g.my - 1 && k >= 1 && k < g.mz - 1)
     v = ibm_finish_value(g, b0, b1, b2, b3, b4, b5, i, j, k, v);
@@ -573,11 +576,11 @@ int ibm_search_impl(vfs_poisson *h, int ibi, int n_v, const double *xyz, int n_e
   // device copies in the handle's search buffers (grown on demand)
   const size_t N = g.n();
   void **buf = cx.scratch->buf;
-  size_t sizes[9] = {col_start.size() * 4, std::max<size_t>(col_tri.size(), 1) * 4,
-                     std::max<size_t>(col_kmax.size(), 1) * 4, tv.size() * 8, nf.size() * 8, s_tab.size() * 8,
-                     N * 8, N * 8, 4};
+  size_t sizes[10] = {col_start.size() * 4, std::max<size_t>(col_tri.size(), 1) * 4,
+                      std::max<size_t>(col_kmax.size(), 1) * 4, tv.size() * 8, nf.size() * 8, s_tab.size() * 8,
+                      N * 8, N * 8, 4, N};
   cudaStream_t st = cx.stream;
-  for (int q = 0; q < 9; q++)
+  for (int q = 0; q < 10; q++)
     if (cx.scratch->cap[q] < sizes[q]) {
       if (buf[q]) {
         cudaStreamSynchronize(st);
@@ -611,12 +614,14 @@ int ibm_search_impl(vfs_poisson *h, int ibi, int n_v, const double *xyz, int n_e
   }
   cudaMemsetAsync(dfail, 0, 4, st);
   dim3 gi((g.mx - 2 + 127) / 128, g.my - 2, g.mz - 2), gd((g.mx + 127) / 128, g.my, g.mz);
+  uint8_t *dis4 = (uint8_t *)buf[9];
   k_ibm_classify_from<<<gd, 128, 0, st>>>(g, cx.cent, ibi, H, (int *)buf[0], (int *)buf[1], (int *)buf[2],
-                                          (double *)buf[3], (double *)buf[4], (double *)buf[5], src, dnv, dfail);
+                                          (double *)buf[3], (double *)buf[4], (double *)buf[5], src, dnv,
+                                          want_nodes ? nullptr : dis4, dfail);
   if (!want_nodes) {
     // dilation and finish in one pass, straight into a device nvert
     double *out = dev ? nvert : dtmp;
-    k_ibm_dilate_finish<<<gd, 128, 0, st>>>(g, b[0], b[1], b[2], b[3], b[4], b[5], dnv, out);
+    k_ibm_dilate_finish<<<gd, 128, 0, st>>>(g, b[0], b[1], b[2], b[3], b[4], b[5], dnv, dis4, out);
     *cx.launches += 2;
     int nfail = 0;
     if (!dev) cudaMemcpyAsync(nvert, dtmp, N * 8, cudaMemcpyDeviceToHost, st);

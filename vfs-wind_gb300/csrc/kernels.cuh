@@ -186,8 +186,8 @@ struct IbmBody {
 // device buffers of the surface search, kept by the handle and grown on
 // demand (no allocation or free, and so no device synchronisation, per body)
 struct IbmScratch {
-  void *buf[9] = {};
-  size_t cap[9] = {};
+  void *buf[10] = {};
+  size_t cap[10] = {};
 };
 struct IbmContext {
   cudaStream_t stream;

@@ -536,6 +536,7 @@ struct vfs_poisson {
   // recently used one replaced)
   struct GraphSlot {
     cudaGraphExec_t exec = nullptr;
+    void *xfinal0 = nullptr;  // where this V-cycle leaves the finest level's x
     int64_t nodes = 0;
     int params[4] = {-1, -1, -1, -1};
     double omega = 0.;
@@ -1234,7 +1235,11 @@ int run_vcycle(vfs_poisson *h, const vfs_solve_opts &o) {
     }
     std::copy(key, key + 4, slot->params);
     slot->omega = o.omega;
+    slot->xfinal0 = Prec<T>::xfinal(h->L[0]);
   }
+  // the buffer holding the result depends on the captured sweeps (the fused
+  // ones swap x and t): each graph's own
+  Prec<T>::xfinal(h->L[0]) = static_cast<T *>(slot->xfinal0);
   slot->used = ++h->gclock;
   CUDA_TRY(cudaGraphLaunch(slot->exec, h->stream));
   h->launches += slot->nodes;

@@ -284,3 +284,30 @@ def test_contra2cart_bitexact(pair, zero_solid):
     u_o = O.contra2cart(d, case.nvert, met, case.ucont, ucat0, zero_solid=bool(zero_solid))
     u_g = s.contra2cart(case.ucont, ucat0.copy(), zero_solid=bool(zero_solid))
     np.testing.assert_array_equal(u_g, u_o)
+
+
+def test_nullspace_scale_quotient_bitexact(cuda_lib):
+    """Remove_Nullspace_Scale's per-cell quotient (-sum aj) / sum_aj is formed
+    from a reciprocal with two Markstein corrections instead of a division;
+    it must give the division's bits.  With integer fluxes and aj on a grid of
+    1/256 (aj given as a metric of set_grid) every sum is exact in any order,
+    so the right-hand side must equal the oracle's (plain division) bit for
+    bit on every cell, across many numerators and two denominators."""
+    import vfs_poisson as V
+    for seed in (5, 6):
+        case = CF.channel(32, 24, 32)
+        rng = np.random.default_rng(seed)
+        u = rng.integers(-40, 41, case.ucont.shape).astype(np.float64)
+        aj = rng.integers(128, 512, case.nvert.shape) / 256.0
+        d = O.dims_of(case)
+        lhs = O.poisson_lhs(d, case.nvert, O.form_metrics(d, case.coor))
+        s = V.PoissonSolver.from_case(case)
+        try:
+            s.set_grid(case.coor, [None] * 12 + [aj])
+            s.set_nvert(case.nvert)
+            s.rhs(u)
+            b_lib = O.from_da(d, lhs["gid"], s.rhs_array())
+        finally:
+            s.close()
+        b_ref = O.rhs(d, case.nvert, lhs["gid"], u, aj)
+        np.testing.assert_array_equal(b_lib, b_ref)

@@ -41,6 +41,8 @@ __global__ void k_zero_solid(Grid g, const double *nvert, double *ucat);
 __global__ void k_cellfield_restrict(Grid gh, Grid gc, int cx, int cy, int cz, const double *fh, double *fc);
 __global__ void k_assemble(Grid g, Box b, const double *nvert, MetricPtrs m, int scale, int filter, int split, double *A,
                            uint8_t *rowtype, LevelSet ls);
+__global__ void k_assemble_fine(Grid g, Box b, const double *nvert, MetricPtrs m, double *A0, uint8_t *rowtype0,
+                                double *A1, uint8_t *rowtype1, LevelSet ls);
 __global__ void k_projection_coef(Grid g, Box b, MetricPtrs m, double *pc);
 __global__ void k_level_masks(Grid g, Box b, const double *nvert, uint8_t *blank, double *w64, float *w32,
                               double *aj_box, const double *aj_da);

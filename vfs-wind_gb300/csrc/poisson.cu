@@ -864,8 +864,9 @@ LevelSet level_set(const vfs_poisson *h, const Level &l) {
 }
 
 // Operator, masks and line factors of one level (assembled from its
-// metrics) into its buffers, allocated on the first build.
-int build_level_operator(vfs_poisson *h, Level &l) {
+// metrics, unless `assembled`: the fine level's operator formed together
+// with the FGMRES operator) into its buffers, allocated on the first build.
+int build_level_operator(vfs_poisson *h, Level &l, bool assembled = false) {
   const size_t n = l.b.n();
   if (!l.A64) {
     TRY(dalloc(h, &l.A64, n * NSLOT));
@@ -880,7 +881,8 @@ int build_level_operator(vfs_poisson *h, Level &l) {
     TRY(dalloc(h, &l.inv32, n)); TRY(dalloc(h, &l.cp32, n));
     for (int q = 0; q < 4; q++) { TRY(dalloc(h, &l.v64[q], n)); TRY(dalloc(h, &l.v32[q], n)); }
   }
-  LAUNCH(h, k_assemble, box_grid(l.b), 128, l.g, l.b, l.nvert, l.met, 1, 0, 1, l.A64, l.rowtype, level_set(h, l));
+  if (!assembled)
+    LAUNCH(h, k_assemble, box_grid(l.b), 128, l.g, l.b, l.nvert, l.met, 1, 0, 1, l.A64, l.rowtype, level_set(h, l));
   LAUNCH(h, k_level_masks, lin_grid(n), 256, l.g, l.b, l.nvert, l.blank, l.w64, l.w32, (double *)nullptr,
          (const double *)nullptr);
   LAUNCH(h, k_line_lu_f64, dim3((l.b.nx + 127) / 128, l.b.nz), 128, l.b, l.A64, l.inv64, l.cp64);
@@ -910,7 +912,7 @@ int refresh_hierarchy(vfs_poisson *h) {
       LAUNCH(h, k_cellfield_restrict, da_grid(q.g), 128, f.g, q.g, f.cx, f.cy, f.cz, f.level, q.level);
     }
   }
-  for (Level &l : h->L) TRY(build_level_operator(h, l));
+  for (size_t li = 0; li < h->L.size(); li++) TRY(build_level_operator(h, h->L[li], li == 0));
   Level &c = h->L.back();
   dfree(h, c.didx); dfree(h, c.dmap); dfree(h, c.dinv);
   c.didx = c.dmap = nullptr;
@@ -919,8 +921,14 @@ int refresh_hierarchy(vfs_poisson *h) {
   return sync(h);
 }
 
+// a new mask refills the existing hierarchy (its level-0 operator then
+// assembled by vfs_poisson_set_nvert together with the FGMRES operator)
+bool hierarchy_refills(const vfs_poisson *h, int coarsest_max) {
+  return !h->L.empty() && h->hier_cmax == coarsest_max && h->hier_ls == (h->ls_on != 0);
+}
+
 int build_hierarchy(vfs_poisson *h, int coarsest_max) {
-  if (!h->L.empty() && h->hier_cmax == coarsest_max && h->hier_ls == (h->ls_on != 0)) return refresh_hierarchy(h);
+  if (hierarchy_refills(h, coarsest_max)) return refresh_hierarchy(h);
   for (size_t li = 0; li < h->L.size(); li++) free_level(h, h->L[li], li == 0);
   h->L.clear();
   drop_graphs(h);
@@ -2024,7 +2032,13 @@ int vfs_poisson_set_nvert(vfs_poisson *h, const double *nvert) {
     fls.rho = h->ls_rho; fls.level = h->ls_level; fls.on = 1;
     fls.bc3 = h->ls_bc3; fls.bc4 = h->ls_bc4; fls.bc5 = h->ls_bc5;
   }
-  LAUNCH(h, k_assemble, box_grid(h->box), 128, h->g, h->box, h->nvert, h->met, 0, 1, 0, h->A0, h->rowtype0, fls);
+  vfs_solve_opts o;
+  vfs_poisson_default_opts(&o);
+  if (hierarchy_refills(h, o.coarsest_max))  // both fine operators from one evaluation of each row
+    LAUNCH(h, k_assemble_fine, box_grid(h->box), 128, h->g, h->box, h->nvert, h->met, h->A0, h->rowtype0,
+           h->L[0].A64, h->L[0].rowtype, fls);
+  else
+    LAUNCH(h, k_assemble, box_grid(h->box), 128, h->g, h->box, h->nvert, h->met, 0, 1, 0, h->A0, h->rowtype0, fls);
   uint8_t *blank;
   double *w64;
   float *w32;
@@ -2040,8 +2054,6 @@ int vfs_poisson_set_nvert(vfs_poisson *h, const double *nvert) {
   TRY(sync(h));
   dfree(h, blank); dfree(h, w64); dfree(h, w32);
   h->ndof = tot;
-  vfs_solve_opts o;
-  vfs_poisson_default_opts(&o);
   TRY(build_hierarchy(h, o.coarsest_max));
   CUDA_TRY(cudaMemsetAsync(h->x, 0, n * 8, h->stream));
   TRY(sync(h));

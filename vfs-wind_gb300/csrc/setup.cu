@@ -447,6 +447,43 @@ __global__ void k_assemble(Grid g, Box b, const double *__restrict__ nvert, Metr
   rowtype[cr] = 1;
 }
 
+// The fine level's two assemblies from one evaluation of each row: the
+// unscaled operator with the reference's insertion filter in the natural
+// layout (A0, the FGMRES operator: k_assemble scale 0, filter 1, split 0)
+// and the aj-scaled one without the filter in the parity-split layout (A1,
+// the finest multigrid level: scale 1, filter 0, split 1); the same values
+// as the two k_assemble passes.
+__global__ void k_assemble_fine(Grid g, Box b, const double *__restrict__ nvert, MetricPtrs m, double *A0,
+                                uint8_t *rowtype0, double *A1, uint8_t *rowtype1, LevelSet ls) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y, k = blockIdx.z;
+  if (i >= b.nx) return;
+  const size_t n = b.n(), c0 = b.at(i, j, k), c1 = b.at(split_pos(i, b.nx), j, k);
+  const int I = i + 1, J = j + 1, K = k + 1;
+  const size_t t = g.at(I, J, K);
+  const bool dof = is_dof_cell(g, nvert, I, J, K);
+  if ((nvert[t] > 0.1 && dof) || nvert[t] > kThr) {  // identity row (poisson.c:1158-1160) or no row
+    const bool ident = nvert[t] > 0.1 && dof;
+    for (int s = 0; s < NSLOT; s++) {
+      const double v = ident && s == CP ? 1.0 : 0.0;
+      A0[s * n + c0] = v;
+      A1[s * n + c1] = v;
+    }
+    rowtype0[c0] = rowtype1[c0] = ident ? 2 : 0;
+    return;
+  }
+  double v[NSLOT];
+  assemble_row(g, nvert, m, I, J, K, v, ls);
+  const double a = m.aj[t];
+  for (int s = 0; s < NSLOT; s++) {
+    int di, dj, dk;
+    slot_offset(s, di, dj, dk);
+    const bool col = s == CP || has_dof(g, nvert, I + di, J + dj, K + dk);
+    A0[s * n + c0] = col && (s == CP || fabs(v[s]) > 1.e-10) ? v[s] : 0.0;
+    A1[s * n + c1] = col ? v[s] * a : 0.0;
+  }
+  rowtype0[c0] = rowtype1[c0] = 1;
+}
+
 // Per-face dot products S = a.b of the projection and the face aj, so that
 // Projection can form (dpdc*S)*aj exactly as poisson.c:2828-2950 does.
 __global__ void k_projection_coef(Grid g, Box b, MetricPtrs m, double *pc) {
@@ -489,6 +526,7 @@ __global__ void k_rhs(Grid g, Box b, const double *__restrict__ nvert, const dou
                       double *partial) {
   double sb = 0, sa = 0;
   const size_t n = b.n();
+  const double f = -1.0 / dt * st * coeff;  // the reference's factor, formed once
   for (size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (size_t)gridDim.x * blockDim.x) {
     int i, j, k;
     box_ijk(b, c, i, j, k);
@@ -507,7 +545,7 @@ __global__ void k_rhs(Grid g, Box b, const double *__restrict__ nvert, const dou
       if (k == 1 && g.pz) val += U(i, j, g.mz - 2, 2);
       else val += U(i, j, k - 1, 2);
 #undef U
-      val *= -1.0 / dt * st * coeff;
+      val *= f;
       sb += val;
       sa += aj[t];
     }
@@ -585,9 +623,26 @@ __global__ void k_reduce_rows(const double *partial, int nb, int nrow, double *o
   if (threadIdx.x == 0) out[r] = s;
 }
 
+// The reference's per-cell quotient (-sum aj) / sum_aj, correctly rounded
+// (the bits of the division) in five FP64 operations instead of a division
+// per cell: y = RN(1 / sum_aj) once, q = RN(a y), then two of Markstein's
+// corrections q <- RN(q + RN(a - q sum_aj) y) with the exact FMA remainder
+// (P. Markstein, IBM J. Res. Dev. 34 (1990) 111-119; a start within 1 ulp
+// and y correctly rounded give the correctly rounded quotient, and the
+// first correction brings RN(a y) within 1 ulp).  A sum_aj without a finite
+// reciprocal takes the division.
+__device__ __forceinline__ double div_rn(double a, double d, double y) {
+  if (!isfinite(y)) return a / d;
+  double q = a * y;
+  double r = fma(-q, d, a);
+  q = fma(r, y, q);
+  r = fma(-q, d, a);
+  return fma(r, y, q);
+}
+
 __global__ void k_rhs_nullspace(Grid g, Box b, const double *__restrict__ nvert, const double *__restrict__ aj,
                                 const double *sums, double *rhs) {
-  const double sum = sums[0], sum_aj = sums[1];
+  const double sum = sums[0], sum_aj = sums[1], y = 1.0 / sum_aj;
   const size_t n = b.n();
   for (size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (size_t)gridDim.x * blockDim.x) {
     int i, j, k;
@@ -595,7 +650,7 @@ __global__ void k_rhs_nullspace(Grid g, Box b, const double *__restrict__ nvert,
     i++; j++; k++;
     size_t t = g.at(i, j, k);
     if (nvert[t] < 0.1) {
-      double val = -sum * aj[t] / sum_aj;
+      const double val = div_rn(-sum * aj[t], sum_aj, y);
       rhs[c] += val;
     }
   }

@@ -537,8 +537,8 @@ def run_ours(args):
             "mask_update_ms": statistics.mean(m[0] for m in mask_ms) if mask_ms else None,
             "mask_classify_ms": statistics.mean(m[1] for m in mask_ms) if mask_ms else None,
             "solver": "FGMRES(20) with one-pass classical Gram-Schmidt, FP64 residual, operator apply and Krylov; FP32 geometric "
-                      "V-cycle (zebra j-line Gauss-Seidel over checkerboard columns, 1+2 sweeps, 1+4 when the solve "
-                      "starts within 32x of rtol; finest-level x and rhs in the parity-split layout; residual couplings "
+                      "V-cycle (zebra j-line Gauss-Seidel over checkerboard columns, 1+2 sweeps; finest-level x and rhs "
+                      "in the parity-split layout; residual couplings "
                       "stored in half precision, difference form, formed inside the line kernel on the levels of at "
                       "most 2^20 cells; dense projected solve on a 192-cell coarsest level); initial guess: candidates "
                       "from the solution history (least-squares projection over the solutions of the current operator, "

@@ -100,9 +100,11 @@ typedef struct {
                          refinement "never"), 1 classical Gram-Schmidt
                          with delayed reorthogonalisation (DCGS2)          */
   int nu2_near;       /* post sweeps for a solve whose initial residual is
-                         within 32x of rtol (default 4; 0: nu2): one
-                         stronger V-cycle then often finishes it, where
-                         nu2 sweeps would need a second iteration          */
+                         within 32x of rtol (default 0: nu2).  4 finishes
+                         more such solves in one V-cycle; over a sequence
+                         warm-started from the solution history it saved
+                         no time (the history of solves that stop just
+                         under rtol guesses less well)                     */
 } vfs_solve_opts;
 
 typedef struct {

@@ -1897,7 +1897,7 @@ void vfs_poisson_default_opts(vfs_solve_opts *o) {
   o->warm_start = 0;
   o->smoother = 4;
   o->orth = 0;
-  o->nu2_near = 4;
+  o->nu2_near = 0;
 }
 
 int vfs_poisson_create(const vfs_grid_desc *gd, vfs_poisson **out) {

@@ -502,6 +502,7 @@ def run_ours(args):
         hist = [hist[-1], out_h.to(hist[-1].device)]
         n += 1
     e2e_range = [min(ms_e2e), max(ms_e2e)]
+    e2e_samples = [[round(t, 3), i] for t, i in zip(ms_e2e, its_e2e)]
     ms_e2e = statistics.mean(ms_e2e)
     # the host link on its own: the step's input and output copies alone
     u_d = torch.empty(tuple(u.shape), dtype=torch.float64, device=u.device)
@@ -546,7 +547,7 @@ def run_ours(args):
                       "(run on every n-th step while it loses), chosen by estimated error (one V-cycle of each "
                       "residual within 32x of the smallest, fluid mean removed; the winner's V-cycle starts FGMRES)",
             "iterations": statistics.mean(its_b), "e2e_iterations": statistics.mean(its_e2e),
-            "e2e_ms_range": e2e_range,
+            "e2e_ms_range": e2e_range, "e2e_samples_ms_iterations": e2e_samples,
             "host_link_gbs": {"h2d": max(a for a, _ in link), "d2h": max(b for _, b in link)},
             "guess_chosen": {name: sum(1 for r in reports if r[0] == code)
                              for code, name in ((0, "projection"), (1, "network"), (2, "extrapolation"))},

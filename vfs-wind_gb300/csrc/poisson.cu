@@ -1159,17 +1159,20 @@ void smooth(vfs_poisson *h, Level &l, int li, int smoother, bool zero_guess, T o
     std::swap(x, t);
   } else {
     // zebra by checkerboard columns: colour (i + k) % 2 == c; the colour's
-    // residuals go to split positions (r of the natural rhs when x = 0)
-    if (zero_guess) cudaMemsetAsync(x, 0, l.b.n() * sizeof(T), h->stream);
+    // residuals go to split positions (r of the natural rhs when x = 0).
+    // From a zero guess the first colour's line kernel does not read x; on
+    // a split level it also writes the other colour's zeros (no clearing
+    // pass), elsewhere x is cleared first.
+    const bool split = split_level<T>(h, li, smoother);
+    if (zero_guess && !split) cudaMemsetAsync(x, 0, l.b.n() * sizeof(T), h->stream);
     const int nh = (l.b.nx + 1) / 2;
     dim3 cg((nh + TI - 1) / TI, l.b.nz), rg((nh + 127) / 128, l.b.ny, l.b.nz);
-    const bool split = split_level<T>(h, li, smoother);
     for (int color = 0; color < 2; color++) {
       const bool skip_res = zero_guess && color == 0;
       if (!skip_res) Prec<T>::residual(h, l, rg, x, bb, r, 2 + color, split);
       const auto tri = split ? Prec<T>::tri_split : Prec<T>::tri;
-      LAUNCH_SM(h, tri, cg, lb, lsm, l.b, skip_res ? bb : r, Asp, Prec<T>::inv(l), Prec<T>::cp(l), x, omega, 0,
-                (skip_res ? 4 : 2) + color);
+      LAUNCH_SM(h, tri, cg, lb, lsm, l.b, skip_res ? bb : r, Asp, Prec<T>::inv(l), Prec<T>::cp(l), x, omega,
+                skip_res ? (split ? 2 : 1) : 0, (skip_res ? 4 : 2) + color);
     }
   }
   prof_end(h, li);

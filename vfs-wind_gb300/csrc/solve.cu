@@ -429,6 +429,18 @@ __device__ __forceinline__ void line_tri_body(Box b, const T *__restrict__ r, co
   // when the level's vectors are split, else natural
   const uint32_t cX = SPLIT ? cS : (valid ? (uint32_t)b.at(split_cell(pp, b.nx), 0, k) : 0u);
   const uint32_t cR = (color == 2 || color == 3) ? cS : cX;
+  if (SPLIT && zero_guess == 2 && color >= 2) {
+    // the first colour of a sweep from a zero guess: the other colour's
+    // half of each row (the same column t there) starts at 0 too, so that
+    // no separate clearing pass is needed
+    const int par = (color + k) & 1, nh = (b.nx + 1) >> 1;
+    const int po = par ? t : nh + t;
+    if (t < (par ? nh : b.nx - nh)) {
+      const uint32_t co = (uint32_t)b.at(po, 0, k);
+      for (int q = 0; q < M; q++)
+        if (j0 + q < ny) x[co + (uint32_t)(j0 + q) * sj] = (T)0;
+    }
+  }
   // every load of the chunk up front (one memory round trip): the line
   // coefficients, factors, residual and the x being corrected
   T y[M], av[M], ivv[M], cv[M], xv[M];

@@ -325,7 +325,10 @@ int vfs_divergence_noalloc(const vfs_grid_desc *g, const double *ucont, const do
  * until one meets no doubled intersection; *n_failed (may be NULL) counts
  * the cells that gave up, which stay 0 before the dilation.  The result is
  * bit-identical to the reference's loops.  nvert is not installed as the
- * solver's blanking: pass it to vfs_poisson_set_nvert. */
+ * solver's blanking: pass it to vfs_poisson_set_nvert.  Bodies are searched
+ * in order from ibi == 0 on the same array, as the reference's loop over the
+ * bodies does: a later body then changes only its box of cells (and their
+ * neighbours), which is all it passes over. */
 int vfs_poisson_ibm_search(vfs_poisson *h, int ibi, int n_v, const double *xyz, int n_elmt, const int32_t *tri,
                            const int *bctype, double *nvert, int *n_failed);
 

@@ -13,6 +13,7 @@
 // its triangles sorted by the top hash cell they reach, so that the search
 // of a cell is the prefix of its column list with top cell >= kc: the same
 // triangle set without a per-thread "already searched" bitmap.
+#include <climits>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -126,9 +127,9 @@ __global__ void k_ibm_classify_from(Grid g, const double *__restrict__ cent, int
                                     const int *__restrict__ col_start, const int *__restrict__ col_tri,
                                     const int *__restrict__ col_kmax, const double *__restrict__ tv,
                                     const double *__restrict__ nf, const double *__restrict__ s_tab, const double *src,
-                                    double *dst, uint8_t *is4, int *failed) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y, k = blockIdx.z;
-  if (i >= g.mx) return;
+                                    double *dst, uint8_t *is4, int *failed, int3 lo, int3 hi) {
+  const int i = lo.x + blockIdx.x * blockDim.x + threadIdx.x, j = lo.y + blockIdx.y, k = lo.z + blockIdx.z;
+  if (i >= hi.x) return;
   const size_t t = g.at(i, j, k);
   double nv = src[t];
   if (i >= 1 && i < g.mx - 1 && j >= 1 && j < g.my - 1 && k >= 1 && k < g.mz - 1) {
@@ -152,6 +153,20 @@ __global__ void k_ibm_classify_from(Grid g, const double *__restrict__ cent, int
   // == 4, once here instead of in each of its 27 neighbours (integer loads
   // there; FP64 arithmetic is the scarce pipe)
   if (is4) is4[t] = (int)((nv < 0 ? 0. : nv) + 0.5) == 4;
+}
+
+// index box of the interior cells whose centre lies strictly inside the
+// body's hash box (the cells the classification can change): atomic
+// min / max into box[0..2] / box[3..5]
+__global__ void k_ibm_box(Grid g, const double *__restrict__ cent, HashBox H, int *box) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x + 1, j = blockIdx.y + 1, k = blockIdx.z + 1;
+  if (i >= g.mx - 1) return;
+  const size_t t = g.at(i, j, k);
+  const double p0 = cent[t * 3], p1 = cent[t * 3 + 1], p2 = cent[t * 3 + 2];
+  if (p0 > H.xmin && p0 < H.xmax && p1 > H.ymin && p1 < H.ymax && p2 > H.zmin && p2 < H.zmax) {
+    atomicMin(&box[0], i); atomicMin(&box[1], j); atomicMin(&box[2], k);
+    atomicMax(&box[3], i); atomicMax(&box[4], j); atomicMax(&box[5], k);
+  }
 }
 
 // near-boundary dilation over every DA point (ibm.c:326-348); a parallel pass
@@ -205,9 +220,9 @@ __global__ void k_ibm_finish(Grid g, int b0, int b1, int b2, int b3, int b4, int
 // finished value
 __global__ void k_ibm_dilate_finish(Grid g, int b0, int b1, int b2, int b3, int b4, int b5,
                                     const double *__restrict__ src, const uint8_t *__restrict__ is4,
-                                    double *__restrict__ dst) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y, k = blockIdx.z;
-  if (i >= g.mx) return;
+                                    double *__restrict__ dst, int3 lo, int3 hi) {
+  int i = lo.x + blockIdx.x * blockDim.x + threadIdx.x, j = lo.y + blockIdx.y, k = lo.z + blockIdx.z;
+  if (i >= hi.x) return;
   const size_t t = g.at(i, j, k);
   double v = src[t];
   if (v < 0) v = 0;
@@ -576,11 +591,11 @@ int ibm_search_impl(vfs_poisson *h, int ibi, int n_v, const double *xyz, int n_e
   // device copies in the handle's search buffers (grown on demand)
   const size_t N = g.n();
   void **buf = cx.scratch->buf;
-  size_t sizes[10] = {col_start.size() * 4, std::max<size_t>(col_tri.size(), 1) * 4,
+  size_t sizes[11] = {col_start.size() * 4, std::max<size_t>(col_tri.size(), 1) * 4,
                       std::max<size_t>(col_kmax.size(), 1) * 4, tv.size() * 8, nf.size() * 8, s_tab.size() * 8,
-                      N * 8, N * 8, 4, N};
+                      N * 8, N * 8, 4, N, 6 * 4};
   cudaStream_t st = cx.stream;
-  for (int q = 0; q < 10; q++)
+  for (int q = 0; q < 11; q++)
     if (cx.scratch->cap[q] < sizes[q]) {
       if (buf[q]) {
         cudaStreamSynchronize(st);
@@ -615,13 +630,60 @@ int ibm_search_impl(vfs_poisson *h, int ibi, int n_v, const double *xyz, int n_e
   cudaMemsetAsync(dfail, 0, 4, st);
   dim3 gi((g.mx - 2 + 127) / 128, g.my - 2, g.mz - 2), gd((g.mx + 127) / 128, g.my, g.mz);
   uint8_t *dis4 = (uint8_t *)buf[9];
+  const int3 all_lo = make_int3(0, 0, 0), all_hi = make_int3(g.mx, g.my, g.mz);
+  if (!want_nodes && ibi > 0) {
+    // A body after the first changes only the cells whose centre lies in its
+    // hash box and, by the dilation, their neighbours: the earlier bodies'
+    // marks are finished (no 2 or 4 is left) and the wall rows' rule gives
+    // what it gave before.  So both passes run on that index box, grown by
+    // one cell for the dilation and by one more for the copy it reads.
+    int init[6] = {INT_MAX, INT_MAX, INT_MAX, INT_MIN, INT_MIN, INT_MIN}, bx[6];
+    int *dbox = (int *)buf[10];
+    cudaMemcpyAsync(dbox, init, sizeof(init), cudaMemcpyHostToDevice, st);
+    k_ibm_box<<<gi, 128, 0, st>>>(g, cx.cent, H, dbox);
+    cudaMemcpyAsync(bx, dbox, sizeof(bx), cudaMemcpyDeviceToHost, st);
+    *cx.launches += 1;
+    cudaError_t eb = cudaStreamSynchronize(st);
+    if (eb != cudaSuccess) {
+      cudaGetLastError();
+      return fail(VFS_ECUDA, std::string("surface search: ") + cudaGetErrorString(eb));
+    }
+    if (n_failed) *n_failed = 0;
+    if (n_nodes) *n_nodes = 0;
+    if (bx[0] > bx[3]) return VFS_OK;  // no cell centre in the body's box: nothing changes
+    auto grow = [&](int m) {
+      return std::make_pair(make_int3(std::max(bx[0] - m, 0), std::max(bx[1] - m, 0), std::max(bx[2] - m, 0)),
+                            make_int3(std::min(bx[3] + m + 1, g.mx), std::min(bx[4] + m + 1, g.my),
+                                      std::min(bx[5] + m + 1, g.mz)));
+    };
+    const auto r2 = grow(2), r1 = grow(1);
+    auto grid_of = [](int3 lo, int3 hi) { return dim3((hi.x - lo.x + 127) / 128, hi.y - lo.y, hi.z - lo.z); };
+    if (!dev) cudaMemcpyAsync(dtmp, nvert, N * 8, cudaMemcpyHostToDevice, st);
+    cudaMemsetAsync(dfail, 0, 4, st);
+    k_ibm_classify_from<<<grid_of(r2.first, r2.second), 128, 0, st>>>(
+        g, cx.cent, ibi, H, (int *)buf[0], (int *)buf[1], (int *)buf[2], (double *)buf[3], (double *)buf[4],
+        (double *)buf[5], dev ? nvert : dtmp, dnv, dis4, dfail, r2.first, r2.second);
+    k_ibm_dilate_finish<<<grid_of(r1.first, r1.second), 128, 0, st>>>(g, b[0], b[1], b[2], b[3], b[4], b[5], dnv,
+                                                                      dis4, dev ? nvert : dtmp, r1.first, r1.second);
+    *cx.launches += 2;
+    int nfail = 0;
+    if (!dev) cudaMemcpyAsync(nvert, dtmp, N * 8, cudaMemcpyDeviceToHost, st);
+    cudaMemcpyAsync(&nfail, dfail, 4, cudaMemcpyDeviceToHost, st);
+    cudaError_t e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      return fail(VFS_ECUDA, std::string("surface search: ") + cudaGetErrorString(e));
+    }
+    if (n_failed) *n_failed = nfail;
+    return VFS_OK;
+  }
   k_ibm_classify_from<<<gd, 128, 0, st>>>(g, cx.cent, ibi, H, (int *)buf[0], (int *)buf[1], (int *)buf[2],
                                           (double *)buf[3], (double *)buf[4], (double *)buf[5], src, dnv,
-                                          want_nodes ? nullptr : dis4, dfail);
+                                          want_nodes ? nullptr : dis4, dfail, all_lo, all_hi);
   if (!want_nodes) {
     // dilation and finish in one pass, straight into a device nvert
     double *out = dev ? nvert : dtmp;
-    k_ibm_dilate_finish<<<gd, 128, 0, st>>>(g, b[0], b[1], b[2], b[3], b[4], b[5], dnv, dis4, out);
+    k_ibm_dilate_finish<<<gd, 128, 0, st>>>(g, b[0], b[1], b[2], b[3], b[4], b[5], dnv, dis4, out, all_lo, all_hi);
     *cx.launches += 2;
     int nfail = 0;
     if (!dev) cudaMemcpyAsync(nvert, dtmp, N * 8, cudaMemcpyDeviceToHost, st);

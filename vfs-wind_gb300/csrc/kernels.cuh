@@ -188,8 +188,8 @@ struct IbmBody {
 // device buffers of the surface search, kept by the handle and grown on
 // demand (no allocation or free, and so no device synchronisation, per body)
 struct IbmScratch {
-  void *buf[10] = {};
-  size_t cap[10] = {};
+  void *buf[11] = {};
+  size_t cap[11] = {};
 };
 struct IbmContext {
   cudaStream_t stream;

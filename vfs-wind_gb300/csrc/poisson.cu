@@ -912,13 +912,21 @@ int refresh_hierarchy(vfs_poisson *h) {
       LAUNCH(h, k_cellfield_restrict, da_grid(q.g), 128, f.g, q.g, f.cx, f.cy, f.cz, f.level, q.level);
     }
   }
+  const auto t0 = std::chrono::steady_clock::now();
   for (size_t li = 0; li < h->L.size(); li++) TRY(build_level_operator(h, h->L[li], li == 0));
+  if (h->phase) TRY(sync(h));
+  const auto t1 = std::chrono::steady_clock::now();
   Level &c = h->L.back();
   dfree(h, c.didx); dfree(h, c.dmap); dfree(h, c.dinv);
   c.didx = c.dmap = nullptr;
   c.dinv = nullptr;
   TRY(build_coarsest(h, c));
-  return sync(h);
+  TRY(sync(h));
+  if (h->phase)
+    fprintf(stderr, "vfs refill ms: level operators %.3f coarsest %.3f\n",
+            std::chrono::duration<double, std::milli>(t1 - t0).count(),
+            std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t1).count());
+  return VFS_OK;
 }
 
 // a new mask refills the existing hierarchy (its level-0 operator then
@@ -2021,6 +2029,7 @@ int vfs_poisson_set_nvert(vfs_poisson *h, const double *nvert) {
   if (!h || !nvert) return fail(VFS_EINVAL, "null argument");
   if (!h->have_grid) return fail(VFS_ESTATE, "set_grid must come before set_nvert");
   const size_t N = h->g.n(), n = h->box.n();
+  const auto tp0 = std::chrono::steady_clock::now();
   TRY(upload(h, h->nvert, nvert, N));
   // setup_lidx2: dof numbering in k-j-i order
   const int nblk = (int)((n + 1023) / 1024);
@@ -2057,7 +2066,12 @@ int vfs_poisson_set_nvert(vfs_poisson *h, const double *nvert) {
   TRY(sync(h));
   dfree(h, blank); dfree(h, w64); dfree(h, w32);
   h->ndof = tot;
+  const auto tp1 = std::chrono::steady_clock::now();
   TRY(build_hierarchy(h, o.coarsest_max));
+  if (h->phase)
+    fprintf(stderr, "vfs set_nvert ms: numbering+fine operators+masks %.3f hierarchy %.3f\n",
+            std::chrono::duration<double, std::milli>(tp1 - tp0).count(),
+            std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - tp1).count());
   CUDA_TRY(cudaMemsetAsync(h->x, 0, n * 8, h->stream));
   TRY(sync(h));
   h->have_nvert = true;

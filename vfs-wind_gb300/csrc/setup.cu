@@ -226,8 +226,12 @@ __device__ inline double ls_mean(double A, double B) { return 2.0 * A * B / (A +
 // One row of the operator, accumulated in the reference's statement order.
 // With a level set (ls.on) every face coefficient is divided by the face
 // density and the Dirichlet top / bottom rows of poisson.c:1295-1554 apply.
-__device__ void assemble_row(const Grid &g, const double *nvert, const MetricPtrs &m, int i, int j, int k,
-                             double v[NSLOT], const LevelSet &ls) {
+template <bool LS>
+__device__ void assemble_row_t(const Grid &g, const double *nvert, const MetricPtrs &m, int i, int j, int k,
+                               double v[NSLOT], const LevelSet &ls) {
+  // a face coefficient divided by the face density: without a level set
+  // the density is exactly 1 and the division (exact there) is not issued
+#define DR(x) (LS ? (x) / r : (x))
   const int mx = g.mx, my = g.my, mz = g.mz;
   const bool ip = g.px, jp = g.py, kp = g.pz;
   const double thr = kThr;
@@ -239,55 +243,55 @@ __device__ void assemble_row(const Grid &g, const double *nvert, const MetricPtr
   if (NV(i + 1, j, k) < thr && (i != mx - 2 || ip)) {  // poisson.c:1167-1230
     r = ls.on ? ls_mean(RHO(i + 1, j, k), RHO(i, j, k)) : 1.0;
     double g0 = G(0, i, j, k), g1 = G(1, i, j, k), g2 = G(2, i, j, k);
-    v[CP] -= g0 / r; v[EP] += g0 / r;
+    v[CP] -= DR(g0); v[EP] += DR(g0);
     if ((j == my - 2 && !jp) || NV(i, j + 1, k) + NV(i + 1, j + 1, k) > thr) {
       if (NV(i, j - 1, k) + NV(i + 1, j - 1, k) < thr && j != 1) {
-        v[CP] += g1 * 0.5 / r; v[EP] += g1 * 0.5 / r; v[SP] -= g1 * 0.5 / r; v[SE] -= g1 * 0.5 / r;
+        v[CP] += DR(g1 * 0.5); v[EP] += DR(g1 * 0.5); v[SP] -= DR(g1 * 0.5); v[SE] -= DR(g1 * 0.5);
       }
     } else if ((j == 1 && !jp) || NV(i, j - 1, k) + NV(i + 1, j - 1, k) > thr) {
       if (NV(i, j + 1, k) + NV(i + 1, j + 1, k) < thr) {
-        v[NP] += g1 * 0.5 / r; v[NE] += g1 * 0.5 / r; v[CP] -= g1 * 0.5 / r; v[EP] -= g1 * 0.5 / r;
+        v[NP] += DR(g1 * 0.5); v[NE] += DR(g1 * 0.5); v[CP] -= DR(g1 * 0.5); v[EP] -= DR(g1 * 0.5);
       }
     } else {
-      v[NP] += g1 * 0.25 / r; v[NE] += g1 * 0.25 / r; v[SP] -= g1 * 0.25 / r; v[SE] -= g1 * 0.25 / r;
+      v[NP] += DR(g1 * 0.25); v[NE] += DR(g1 * 0.25); v[SP] -= DR(g1 * 0.25); v[SE] -= DR(g1 * 0.25);
     }
     if ((k == mz - 2 && !kp) || NV(i, j, k + 1) + NV(i + 1, j, k + 1) > thr) {
       if (NV(i, j, k - 1) + NV(i + 1, j, k - 1) < thr && k != 1) {
-        v[CP] += g2 * 0.5 / r; v[EP] += g2 * 0.5 / r; v[BP] -= g2 * 0.5 / r; v[BE] -= g2 * 0.5 / r;
+        v[CP] += DR(g2 * 0.5); v[EP] += DR(g2 * 0.5); v[BP] -= DR(g2 * 0.5); v[BE] -= DR(g2 * 0.5);
       }
     } else if ((k == 1 && !kp) || NV(i, j, k - 1) + NV(i + 1, j, k - 1) > thr) {
       if (NV(i, j, k + 1) + NV(i + 1, j, k + 1) < thr) {
-        v[TP] += g2 * 0.5 / r; v[TE] += g2 * 0.5 / r; v[CP] -= g2 * 0.5 / r; v[EP] -= g2 * 0.5 / r;
+        v[TP] += DR(g2 * 0.5); v[TE] += DR(g2 * 0.5); v[CP] -= DR(g2 * 0.5); v[EP] -= DR(g2 * 0.5);
       }
     } else {
-      v[TP] += g2 * 0.25 / r; v[TE] += g2 * 0.25 / r; v[BP] -= g2 * 0.25 / r; v[BE] -= g2 * 0.25 / r;
+      v[TP] += DR(g2 * 0.25); v[TE] += DR(g2 * 0.25); v[BP] -= DR(g2 * 0.25); v[BE] -= DR(g2 * 0.25);
     }
   }
   if (NV(i - 1, j, k) < thr && (i != 1 || ip)) {  // poisson.c:1233-1293
     r = ls.on ? ls_mean(RHO(i - 1, j, k), RHO(i, j, k)) : 1.0;
     double g0 = G(0, i - 1, j, k), g1 = G(1, i - 1, j, k), g2 = G(2, i - 1, j, k);
-    v[CP] -= g0 / r; v[WP] += g0 / r;
+    v[CP] -= DR(g0); v[WP] += DR(g0);
     if ((j == my - 2 && !jp) || NV(i, j + 1, k) + NV(i - 1, j + 1, k) > thr) {
       if (NV(i, j - 1, k) + NV(i - 1, j - 1, k) < thr && j != 1) {
-        v[CP] -= g1 * 0.5 / r; v[WP] -= g1 * 0.5 / r; v[SP] += g1 * 0.5 / r; v[SW] += g1 * 0.5 / r;
+        v[CP] -= DR(g1 * 0.5); v[WP] -= DR(g1 * 0.5); v[SP] += DR(g1 * 0.5); v[SW] += DR(g1 * 0.5);
       }
     } else if ((j == 1 && !jp) || NV(i, j - 1, k) + NV(i - 1, j - 1, k) > thr) {
       if (NV(i, j + 1, k) + NV(i - 1, j + 1, k) < thr) {
-        v[NP] -= g1 * 0.5 / r; v[NW] -= g1 * 0.5 / r; v[CP] += g1 * 0.5 / r; v[WP] += g1 * 0.5 / r;
+        v[NP] -= DR(g1 * 0.5); v[NW] -= DR(g1 * 0.5); v[CP] += DR(g1 * 0.5); v[WP] += DR(g1 * 0.5);
       }
     } else {
-      v[NP] -= g1 * 0.25 / r; v[NW] -= g1 * 0.25 / r; v[SP] += g1 * 0.25 / r; v[SW] += g1 * 0.25 / r;
+      v[NP] -= DR(g1 * 0.25); v[NW] -= DR(g1 * 0.25); v[SP] += DR(g1 * 0.25); v[SW] += DR(g1 * 0.25);
     }
     if ((k == mz - 2 && !kp) || NV(i, j, k + 1) + NV(i - 1, j, k + 1) > thr) {
       if (NV(i, j, k - 1) + NV(i - 1, j, k - 1) < thr && k != 1) {
-        v[CP] -= g2 * 0.5 / r; v[WP] -= g2 * 0.5 / r; v[BP] += g2 * 0.5 / r; v[BW] += g2 * 0.5 / r;
+        v[CP] -= DR(g2 * 0.5); v[WP] -= DR(g2 * 0.5); v[BP] += DR(g2 * 0.5); v[BW] += DR(g2 * 0.5);
       }
     } else if ((k == 1 && !kp) || NV(i, j, k - 1) + NV(i - 1, j, k - 1) > thr) {
       if (NV(i, j, k + 1) + NV(i - 1, j, k + 1) < thr) {
-        v[TP] -= g2 * 0.5 / r; v[TW] -= g2 * 0.5 / r; v[CP] += g2 * 0.5 / r; v[WP] += g2 * 0.5 / r;
+        v[TP] -= DR(g2 * 0.5); v[TW] -= DR(g2 * 0.5); v[CP] += DR(g2 * 0.5); v[WP] += DR(g2 * 0.5);
       }
     } else {
-      v[TP] -= g2 * 0.25 / r; v[TW] -= g2 * 0.25 / r; v[BP] += g2 * 0.25 / r; v[BW] += g2 * 0.25 / r;
+      v[TP] -= DR(g2 * 0.25); v[TW] -= DR(g2 * 0.25); v[BP] += DR(g2 * 0.25); v[BW] += DR(g2 * 0.25);
     }
   }
   if (NV(i, j + 1, k) < thr && (j != my - 2 || jp || (ls.on && ls.bc3 == 4 && j == my - 2))) {  // poisson.c:1296-1361
@@ -295,27 +299,27 @@ __device__ void assemble_row(const Grid &g, const double *nvert, const MetricPtr
     double g3 = G(3, i, j, k), g4 = G(4, i, j, k), g5 = G(5, i, j, k);
     if ((i == mx - 2 && !ip) || NV(i + 1, j, k) + NV(i + 1, j + 1, k) > thr) {
       if (NV(i - 1, j, k) + NV(i - 1, j + 1, k) < thr && i != 1) {
-        v[CP] += g3 * 0.5 / r; v[NP] += g3 * 0.5 / r; v[WP] -= g3 * 0.5 / r; v[NW] -= g3 * 0.5 / r;
+        v[CP] += DR(g3 * 0.5); v[NP] += DR(g3 * 0.5); v[WP] -= DR(g3 * 0.5); v[NW] -= DR(g3 * 0.5);
       }
     } else if ((i == 1 && !ip) || NV(i - 1, j, k) + NV(i - 1, j + 1, k) > thr) {
       if (NV(i + 1, j, k) + NV(i + 1, j + 1, k) < thr) {
-        v[EP] += g3 * 0.5 / r; v[NE] += g3 * 0.5 / r; v[CP] -= g3 * 0.5 / r; v[NP] -= g3 * 0.5 / r;
+        v[EP] += DR(g3 * 0.5); v[NE] += DR(g3 * 0.5); v[CP] -= DR(g3 * 0.5); v[NP] -= DR(g3 * 0.5);
       }
     } else {
-      v[EP] += g3 * 0.25 / r; v[NE] += g3 * 0.25 / r; v[WP] -= g3 * 0.25 / r; v[NW] -= g3 * 0.25 / r;
+      v[EP] += DR(g3 * 0.25); v[NE] += DR(g3 * 0.25); v[WP] -= DR(g3 * 0.25); v[NW] -= DR(g3 * 0.25);
     }
-    if (ls.on && ls.bc3 == 4 && j == my - 2) v[CP] -= g4 / 0.5 / r;  // zero Dirichlet pressure, :1328
-    else { v[CP] -= g4 / r; v[NP] += g4 / r; }
+    if (ls.on && ls.bc3 == 4 && j == my - 2) v[CP] -= DR(g4 / 0.5);  // zero Dirichlet pressure, :1328
+    else { v[CP] -= DR(g4); v[NP] += DR(g4); }
     if ((k == mz - 2 && !kp) || NV(i, j, k + 1) + NV(i, j + 1, k + 1) > thr) {
       if (NV(i, j, k - 1) + NV(i, j + 1, k - 1) < thr && k != 1) {
-        v[CP] += g5 * 0.5 / r; v[NP] += g5 * 0.5 / r; v[BP] -= g5 * 0.5 / r; v[BN] -= g5 * 0.5 / r;
+        v[CP] += DR(g5 * 0.5); v[NP] += DR(g5 * 0.5); v[BP] -= DR(g5 * 0.5); v[BN] -= DR(g5 * 0.5);
       }
     } else if ((k == 1 && !kp) || NV(i, j, k - 1) + NV(i, j + 1, k - 1) > thr) {
       if (NV(i, j, k + 1) + NV(i, j + 1, k + 1) < thr) {
-        v[TP] += g5 * 0.5 / r; v[TN] += g5 * 0.5 / r; v[CP] -= g5 * 0.5 / r; v[NP] -= g5 * 0.5 / r;
+        v[TP] += DR(g5 * 0.5); v[TN] += DR(g5 * 0.5); v[CP] -= DR(g5 * 0.5); v[NP] -= DR(g5 * 0.5);
       }
     } else {
-      v[TP] += g5 * 0.25 / r; v[TN] += g5 * 0.25 / r; v[BP] -= g5 * 0.25 / r; v[BN] -= g5 * 0.25 / r;
+      v[TP] += DR(g5 * 0.25); v[TN] += DR(g5 * 0.25); v[BP] -= DR(g5 * 0.25); v[BN] -= DR(g5 * 0.25);
     }
   }
   if (NV(i, j - 1, k) < thr && (j != 1 || jp)) {  // poisson.c:1364-1422
@@ -323,26 +327,26 @@ __device__ void assemble_row(const Grid &g, const double *nvert, const MetricPtr
     double g3 = G(3, i, j - 1, k), g4 = G(4, i, j - 1, k), g5 = G(5, i, j - 1, k);
     if ((i == mx - 2 && !ip) || NV(i + 1, j, k) + NV(i + 1, j - 1, k) > thr) {
       if (NV(i - 1, j, k) + NV(i - 1, j - 1, k) < thr && i != 1) {
-        v[CP] -= g3 * 0.5 / r; v[SP] -= g3 * 0.5 / r; v[WP] += g3 * 0.5 / r; v[SW] += g3 * 0.5 / r;
+        v[CP] -= DR(g3 * 0.5); v[SP] -= DR(g3 * 0.5); v[WP] += DR(g3 * 0.5); v[SW] += DR(g3 * 0.5);
       }
     } else if ((i == 1 && !ip) || NV(i - 1, j, k) + NV(i - 1, j - 1, k) > thr) {
       if (NV(i + 1, j, k) + NV(i + 1, j - 1, k) < thr) {
-        v[EP] -= g3 * 0.5 / r; v[SE] -= g3 * 0.5 / r; v[CP] += g3 * 0.5 / r; v[SP] += g3 * 0.5 / r;
+        v[EP] -= DR(g3 * 0.5); v[SE] -= DR(g3 * 0.5); v[CP] += DR(g3 * 0.5); v[SP] += DR(g3 * 0.5);
       }
     } else {
-      v[EP] -= g3 * 0.25 / r; v[SE] -= g3 * 0.25 / r; v[WP] += g3 * 0.25 / r; v[SW] += g3 * 0.25 / r;
+      v[EP] -= DR(g3 * 0.25); v[SE] -= DR(g3 * 0.25); v[WP] += DR(g3 * 0.25); v[SW] += DR(g3 * 0.25);
     }
-    v[CP] -= g4 / r; v[SP] += g4 / r;
+    v[CP] -= DR(g4); v[SP] += DR(g4);
     if ((k == mz - 2 && !kp) || NV(i, j, k + 1) + NV(i, j - 1, k + 1) > thr) {
       if (NV(i, j, k - 1) + NV(i, j - 1, k - 1) < thr && k != 1) {
-        v[CP] -= g5 * 0.5 / r; v[SP] -= g5 * 0.5 / r; v[BP] += g5 * 0.5 / r; v[BS] += g5 * 0.5 / r;
+        v[CP] -= DR(g5 * 0.5); v[SP] -= DR(g5 * 0.5); v[BP] += DR(g5 * 0.5); v[BS] += DR(g5 * 0.5);
       }
     } else if ((k == 1 && !kp) || NV(i, j, k - 1) + NV(i, j - 1, k - 1) > thr) {
       if (NV(i, j, k + 1) + NV(i, j - 1, k + 1) < thr) {
-        v[TP] -= g5 * 0.5 / r; v[TS] -= g5 * 0.5 / r; v[CP] += g5 * 0.5 / r; v[SP] += g5 * 0.5 / r;
+        v[TP] -= DR(g5 * 0.5); v[TS] -= DR(g5 * 0.5); v[CP] += DR(g5 * 0.5); v[SP] += DR(g5 * 0.5);
       }
     } else {
-      v[TP] -= g5 * 0.25 / r; v[TS] -= g5 * 0.25 / r; v[BP] += g5 * 0.25 / r; v[BS] += g5 * 0.25 / r;
+      v[TP] -= DR(g5 * 0.25); v[TS] -= DR(g5 * 0.25); v[BP] += DR(g5 * 0.25); v[BS] += DR(g5 * 0.25);
     }
   }
   if (NV(i, j, k + 1) < thr && (k != mz - 2 || kp || (ls.on && ls.bc5 == 4 && k == mz - 2))) {  // poisson.c:1425-1491
@@ -350,28 +354,28 @@ __device__ void assemble_row(const Grid &g, const double *nvert, const MetricPtr
     double g6 = G(6, i, j, k), g7 = G(7, i, j, k), g8 = G(8, i, j, k);
     if ((i == mx - 2 && !ip) || NV(i + 1, j, k) + NV(i + 1, j, k + 1) > thr) {
       if (NV(i - 1, j, k) + NV(i - 1, j, k + 1) < thr && i != 1) {
-        v[CP] += g6 * 0.5 / r; v[TP] += g6 * 0.5 / r; v[WP] -= g6 * 0.5 / r; v[TW] -= g6 * 0.5 / r;
+        v[CP] += DR(g6 * 0.5); v[TP] += DR(g6 * 0.5); v[WP] -= DR(g6 * 0.5); v[TW] -= DR(g6 * 0.5);
       }
     } else if ((i == 1 && !ip) || NV(i - 1, j, k) + NV(i - 1, j, k + 1) > thr) {
       if (NV(i + 1, j, k) + NV(i + 1, j, k + 1) < thr) {
-        v[EP] += g6 * 0.5 / r; v[TE] += g6 * 0.5 / r; v[CP] -= g6 * 0.5 / r; v[TP] -= g6 * 0.5 / r;
+        v[EP] += DR(g6 * 0.5); v[TE] += DR(g6 * 0.5); v[CP] -= DR(g6 * 0.5); v[TP] -= DR(g6 * 0.5);
       }
     } else {
-      v[EP] += g6 * 0.25 / r; v[TE] += g6 * 0.25 / r; v[WP] -= g6 * 0.25 / r; v[TW] -= g6 * 0.25 / r;
+      v[EP] += DR(g6 * 0.25); v[TE] += DR(g6 * 0.25); v[WP] -= DR(g6 * 0.25); v[TW] -= DR(g6 * 0.25);
     }
     if ((j == my - 2 && !jp) || NV(i, j + 1, k) + NV(i, j + 1, k + 1) > thr) {
       if (NV(i, j - 1, k) + NV(i, j - 1, k + 1) < thr && j != 1) {
-        v[CP] += g7 * 0.5 / r; v[TP] += g7 * 0.5 / r; v[SP] -= g7 * 0.5 / r; v[TS] -= g7 * 0.5 / r;
+        v[CP] += DR(g7 * 0.5); v[TP] += DR(g7 * 0.5); v[SP] -= DR(g7 * 0.5); v[TS] -= DR(g7 * 0.5);
       }
     } else if ((j == 1 && !jp) || NV(i, j - 1, k) + NV(i, j - 1, k + 1) > thr) {
       if (NV(i, j + 1, k) + NV(i, j + 1, k + 1) < thr) {
-        v[NP] += g7 * 0.5 / r; v[TN] += g7 * 0.5 / r; v[CP] -= g7 * 0.5 / r; v[TP] -= g7 * 0.5 / r;
+        v[NP] += DR(g7 * 0.5); v[TN] += DR(g7 * 0.5); v[CP] -= DR(g7 * 0.5); v[TP] -= DR(g7 * 0.5);
       }
     } else {
-      v[NP] += g7 * 0.25 / r; v[TN] += g7 * 0.25 / r; v[SP] -= g7 * 0.25 / r; v[TS] -= g7 * 0.25 / r;
+      v[NP] += DR(g7 * 0.25); v[TN] += DR(g7 * 0.25); v[SP] -= DR(g7 * 0.25); v[TS] -= DR(g7 * 0.25);
     }
-    if (ls.on && ls.bc5 == 4 && k == mz - 2) v[CP] -= g8 / 0.5 / r;  // :1482-1484
-    else { v[CP] -= g8 / r; v[TP] += g8 / r; }
+    if (ls.on && ls.bc5 == 4 && k == mz - 2) v[CP] -= DR(g8 / 0.5);  // :1482-1484
+    else { v[CP] -= DR(g8); v[TP] += DR(g8); }
   }
   if (NV(i, j, k - 1) < thr &&
       (k != 1 || kp || (ls.on && ls.bc4 == 5000 && k == 1 && ls.level[g.at(i, j, k)] < 0))) {  // poisson.c:1494-1561
@@ -379,32 +383,38 @@ __device__ void assemble_row(const Grid &g, const double *nvert, const MetricPtr
     double g6 = G(6, i, j, k - 1), g7 = G(7, i, j, k - 1), g8 = G(8, i, j, k - 1);
     if ((i == mx - 2 && !ip) || NV(i + 1, j, k) + NV(i + 1, j, k - 1) > thr) {
       if (NV(i - 1, j, k) + NV(i - 1, j, k - 1) < thr && i != 1) {
-        v[CP] -= g6 * 0.5 / r; v[BP] -= g6 * 0.5 / r; v[WP] += g6 * 0.5 / r; v[BW] += g6 * 0.5 / r;
+        v[CP] -= DR(g6 * 0.5); v[BP] -= DR(g6 * 0.5); v[WP] += DR(g6 * 0.5); v[BW] += DR(g6 * 0.5);
       }
     } else if ((i == 1 && !ip) || NV(i - 1, j, k) + NV(i - 1, j, k - 1) > thr) {
       if (NV(i + 1, j, k) + NV(i + 1, j, k - 1) < thr) {
-        v[EP] -= g6 * 0.5 / r; v[BE] -= g6 * 0.5 / r; v[CP] += g6 * 0.5 / r; v[BP] += g6 * 0.5 / r;
+        v[EP] -= DR(g6 * 0.5); v[BE] -= DR(g6 * 0.5); v[CP] += DR(g6 * 0.5); v[BP] += DR(g6 * 0.5);
       }
     } else {
-      v[EP] -= g6 * 0.25 / r; v[BE] -= g6 * 0.25 / r; v[WP] += g6 * 0.25 / r; v[BW] += g6 * 0.25 / r;
+      v[EP] -= DR(g6 * 0.25); v[BE] -= DR(g6 * 0.25); v[WP] += DR(g6 * 0.25); v[BW] += DR(g6 * 0.25);
     }
     if ((j == my - 2 && !jp) || NV(i, j + 1, k) + NV(i, j + 1, k - 1) > thr) {
       if (NV(i, j - 1, k) + NV(i, j - 1, k - 1) < thr && j != 1) {
-        v[CP] -= g7 * 0.5 / r; v[BP] -= g7 * 0.5 / r; v[SP] += g7 * 0.5 / r; v[BS] += g7 * 0.5 / r;
+        v[CP] -= DR(g7 * 0.5); v[BP] -= DR(g7 * 0.5); v[SP] += DR(g7 * 0.5); v[BS] += DR(g7 * 0.5);
       }
     } else if ((j == 1 && !jp) || NV(i, j - 1, k) + NV(i, j - 1, k - 1) > thr) {
       if (NV(i, j + 1, k) + NV(i, j + 1, k - 1) < thr) {
-        v[NP] -= g7 * 0.5 / r; v[BN] -= g7 * 0.5 / r; v[CP] += g7 * 0.5 / r; v[BP] += g7 * 0.5 / r;
+        v[NP] -= DR(g7 * 0.5); v[BN] -= DR(g7 * 0.5); v[CP] += DR(g7 * 0.5); v[BP] += DR(g7 * 0.5);
       }
     } else {
-      v[NP] -= g7 * 0.25 / r; v[BN] -= g7 * 0.25 / r; v[SP] += g7 * 0.25 / r; v[BS] += g7 * 0.25 / r;
+      v[NP] -= DR(g7 * 0.25); v[BN] -= DR(g7 * 0.25); v[SP] += DR(g7 * 0.25); v[BS] += DR(g7 * 0.25);
     }
-    if (ls.on && ls.bc4 == 5 && k == 1) v[CP] -= g8 / 0.5 / r;  // :1552-1554
-    else { v[CP] -= g8 / r; v[BP] += g8 / r; }
+    if (ls.on && ls.bc4 == 5 && k == 1) v[CP] -= DR(g8 / 0.5);  // :1552-1554
+    else { v[CP] -= DR(g8); v[BP] += DR(g8); }
   }
 #undef RHO
 #undef NV
 #undef G
+#undef DR
+}
+__device__ void assemble_row(const Grid &g, const double *nvert, const MetricPtrs &m, int i, int j, int k,
+                             double v[NSLOT], const LevelSet &ls) {
+  if (ls.on) assemble_row_t<true>(g, nvert, m, i, j, k, v, ls);
+  else assemble_row_t<false>(g, nvert, m, i, j, k, v, ls);
 }
 
 // Assemble one level's operator into 19 box-layout planes.  filter: the

@@ -314,7 +314,10 @@ def run_ours(args):
     plain = V.default_opts(precision=1, rtol=1e-8, warm_start=1)
     mixed = V.default_opts(precision=0, rtol=1e-8, warm_start=2)
 
-    # 1. the plain solver generates the training data (steps 0 .. T+1)
+    # 1. the plain solver generates the training data (steps 0 .. T+1); its
+    # converged solutions also fill the solution history, so that the timed
+    # steps start from a full history whatever the warm-up count
+    s.set_history(args.history)
     t0 = time.time()
     pool = LG.SamplePool((nx, ny, nz), args.train_samples)
     hist, _ = LG.run_sequence(seq, s, args.train_samples + 2, plain, guess="prev", pool=pool)
@@ -333,7 +336,6 @@ def run_ours(args):
 
     # 3. held-out steps: every arm on the same right-hand sides and history;
     # only the learned arm's solves enter the solution history
-    s.set_history(args.history)
     s.set_network_period(args.network_period)
 
     state = {"nv": nv}

@@ -15,10 +15,15 @@ struct MetricPtrs {
   double *icsi, *ieta, *izet, *iaj;
   double *jcsi, *jeta, *jzet, *jaj;
   double *kcsi, *keta, *kzet, *kaj;
+  // the operator's nine face coefficients per DA point (g11 g21 g31 at i
+  // faces, g12 g22 g32 at j faces, g13 g23 g33 at k faces), formed once per
+  // grid by k_face_coef; null: formed in the assembly
+  double *gface;
 };
 
 // setup.cu (compiled without FMA contraction)
 __global__ void k_metrics_cell(Grid g, const double *coor, MetricPtrs m);
+__global__ void k_face_coef(Grid g, MetricPtrs m, double *gface);
 __global__ void k_metrics_mirror(Grid g, MetricPtrs m, int dir);
 __global__ void k_metrics_periodic(Grid g, MetricPtrs m, int faces);
 __global__ void k_metrics_face(Grid g, MetricPtrs m, int dir);

@@ -521,6 +521,9 @@ struct vfs_poisson {
   // options are the ones the step used; otherwise the step is dropped.
   cudaStream_t side = nullptr;
   cudaEvent_t ev_feat = nullptr;
+  // the solve's copy of phi to a host array, beside the history push
+  cudaStream_t dl_stream = nullptr;
+  cudaEvent_t dl_ev[2] = {nullptr, nullptr};
   double *spartial = nullptr, *sred = nullptr;  // side-stream reductions
   bool spec_enable = true;                      // VFS_GUESS_SPECULATE=0 turns it off
   bool spec_next = false, spec_valid = false;
@@ -644,11 +647,21 @@ int alloc_metrics(vfs_poisson *h, const Grid &g, MetricPtrs &m) {
   double **sca[] = {&m.aj, &m.iaj, &m.jaj, &m.kaj};
   for (auto p : vec) { TRY(dalloc(h, p, 3 * n)); CUDA_TRY(cudaMemsetAsync(*p, 0, 3 * n * 8, h->stream)); }
   for (auto p : sca) { TRY(dalloc(h, p, n)); CUDA_TRY(cudaMemsetAsync(*p, 0, n * 8, h->stream)); }
+  m.gface = nullptr;  // formed by face_coef once the metrics are final
+  return VFS_OK;
+}
+// the operator's face coefficients of a grid's final metrics (every later
+// assembly reads them instead of forming them from the metrics)
+int face_coef(vfs_poisson *h, const Grid &g, MetricPtrs &m) {
+  if (!m.gface) TRY(dalloc(h, &m.gface, 9 * g.n()));
+  MetricPtrs src = m;
+  src.gface = nullptr;
+  LAUNCH(h, k_face_coef, da_grid(g), 128, g, src, m.gface);
   return VFS_OK;
 }
 void free_metrics(vfs_poisson *h, MetricPtrs &m) {
   double *all[] = {m.cent, m.csi, m.eta, m.zet, m.icsi, m.ieta, m.izet, m.jcsi, m.jeta, m.jzet,
-                   m.kcsi, m.keta, m.kzet, m.aj, m.iaj, m.jaj, m.kaj};
+                   m.kcsi, m.keta, m.kzet, m.aj, m.iaj, m.jaj, m.kaj, m.gface};
   for (auto p : all) dfree(h, p);
   m = MetricPtrs{};
 }
@@ -993,6 +1006,7 @@ int build_hierarchy(vfs_poisson *h, int coarsest_max) {
       TRY(alloc_metrics(h, l.g, l.met));
       l.own_met = true;
       TRY(form_metrics(h, l.g, l.coor, l.met));
+      TRY(face_coef(h, l.g, l.met));
     }
     TRY(build_level_operator(h, l));
     TRY(sync(h));
@@ -2000,6 +2014,9 @@ void vfs_poisson_destroy(vfs_poisson *h) {
     if (h->phev[q]) cudaEventDestroy(h->phev[q]);
   if (h->ev_feat) cudaEventDestroy(h->ev_feat);
   if (h->side) cudaStreamDestroy(h->side);
+  for (cudaEvent_t e : h->dl_ev)
+    if (e) cudaEventDestroy(e);
+  if (h->dl_stream) cudaStreamDestroy(h->dl_stream);
   if (h->stream && h->own_stream) cudaStreamDestroy(h->stream);
   cudaGetLastError();
   delete h;
@@ -2018,6 +2035,7 @@ int vfs_poisson_set_grid(vfs_poisson *h, const double *coor, const double *const
     for (int q = 0; q < 9; q++) if (fm[q]) TRY(upload(h, vec[q], fm[q], 3 * N));
     for (int q = 0; q < 4; q++) if (fm[9 + q]) TRY(upload(h, sca[q], fm[9 + q], N));
   }
+  TRY(face_coef(h, h->g, h->met));
   LAUNCH(h, k_projection_coef, box_grid(h->box), 128, h->g, h->box, h->met, h->pc);
   TRY(sync(h));
   h->have_grid = true;
@@ -2316,8 +2334,6 @@ int vfs_poisson_solve(vfs_poisson *h, double *phi, const vfs_solve_opts *opts, v
     CUDA_TRY(cudaMemsetAsync(h->x, 0, n * 8, h->stream));
   }
   TRY(fgmres(h, o, &st));
-  if (h->hist_cap && h->hist_record && st.initial_rel_residual > 0. && st.rel_residual <= o.rtol)
-    TRY(hist_push(h));
   // Remove_Nullspace of phi (:604-608), its shift applied by the DA output
   const bool shift = h->desc.bctype3 != -10 && !(h->ls_on && h->ls_bc5 == 4);
   if (shift) {
@@ -2327,7 +2343,26 @@ int vfs_poisson_solve(vfs_poisson *h, double *phi, const vfs_solve_opts *opts, v
   }
   LAUNCH(h, k_box_to_da_phi, da_grid(h->g), 128, h->g, h->box, h->nvert, h->x, h->phi_da,
          shift ? (const double *)h->red + 2 : nullptr);
-  if (phi) TRY(download(h, phi, h->phi_da, h->g.n()));
+  // phi to a host array on a side stream, while the solution enters the
+  // history on the handle's stream (it reads x, b and the residual, not
+  // phi); the handle's stream waits for the copy before the call returns
+  const bool host_out = phi && !is_device_ptr(phi);
+  if (host_out) {
+    if (!h->dl_stream) {
+      CUDA_TRY(cudaStreamCreateWithFlags(&h->dl_stream, cudaStreamNonBlocking));
+      CUDA_TRY(cudaEventCreateWithFlags(&h->dl_ev[0], cudaEventDisableTiming));
+      CUDA_TRY(cudaEventCreateWithFlags(&h->dl_ev[1], cudaEventDisableTiming));
+    }
+    CUDA_TRY(cudaEventRecord(h->dl_ev[0], h->stream));
+    CUDA_TRY(cudaStreamWaitEvent(h->dl_stream, h->dl_ev[0], 0));
+    CUDA_TRY(cudaMemcpyAsync(phi, h->phi_da, h->g.n() * sizeof(double), cudaMemcpyDeviceToHost, h->dl_stream));
+    CUDA_TRY(cudaEventRecord(h->dl_ev[1], h->dl_stream));
+  } else if (phi) {
+    TRY(download(h, phi, h->phi_da, h->g.n()));
+  }
+  if (h->hist_cap && h->hist_record && st.initial_rel_residual > 0. && st.rel_residual <= o.rtol)
+    TRY(hist_push(h));
+  if (host_out) CUDA_TRY(cudaStreamWaitEvent(h->stream, h->dl_ev[1], 0));
   CUDA_TRY(cudaEventRecord(h->ev1, h->stream));
   TRY(sync(h));
   float ms = 0.f;

@@ -201,10 +201,7 @@ __global__ void k_gid_da(Grid g, Box b, const int *gid_box, int *gid_da) {
 // PoissonLHSNew (Source/poisson.c:977-1688), level set off (r = 1)
 // --------------------------------------------------------------------------
 // g11..g33 at a face with the periodic source remap of poisson.c:1102-1138
-__device__ inline double gface(const Grid &g, const MetricPtrs &m, int q, int i, int j, int k) {
-  int a, b, c, fi, fj, fk;
-  g.remap(i, j, k, a, b, c, fi, fj, fk);
-  size_t s = g.at(a, b, c);
+__device__ inline double gface_at(const MetricPtrs &m, int q, size_t s) {
   const double *X, *Y, *AJ;
   switch (q) {
     case 0: X = m.icsi; Y = m.icsi; AJ = m.iaj; break;
@@ -218,6 +215,21 @@ __device__ inline double gface(const Grid &g, const MetricPtrs &m, int q, int i,
     default: X = m.kzet; Y = m.kzet; AJ = m.kaj; break;
   }
   return (X[s * 3] * Y[s * 3] + X[s * 3 + 1] * Y[s * 3 + 1] + X[s * 3 + 2] * Y[s * 3 + 2]) * AJ[s];
+}
+__device__ inline double gface(const Grid &g, const MetricPtrs &m, int q, int i, int j, int k) {
+  int a, b, c, fi, fj, fk;
+  g.remap(i, j, k, a, b, c, fi, fj, fk);
+  const size_t s = g.at(a, b, c);
+  return m.gface ? m.gface[(size_t)q * g.n() + s] : gface_at(m, q, s);
+}
+// the nine face coefficients of every DA point, as gface forms them (no FMA
+// contraction in this unit: the same bits)
+__global__ void k_face_coef(Grid g, MetricPtrs m, double *out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y, k = blockIdx.z;
+  if (i >= g.mx) return;
+  const size_t s = g.at(i, j, k), n = g.n();
+#pragma unroll
+  for (int q = 0; q < 9; q++) out[(size_t)q * n + s] = gface_at(m, q, s);
 }
 
 // mean (Source/level.c:2276-2280): the harmonic mean of two densities

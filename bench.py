@@ -398,11 +398,18 @@ def run_ours(args):
             s.rhs(u)
             ch, rr = s.learned_guess(net, h[-1], h[-2], net.kappa)
         else:
+            w0 = time.perf_counter()
             s.rhs(host[0])
+            w1 = time.perf_counter()
             ch, rr = s.learned_guess(net, host[1], host[2], net.kappa)
+            w2 = time.perf_counter()
         _, st = s.solve(phi, opts=mixed)
         e1.record(stream)
         torch.cuda.synchronize()
+        if host is not None:  # host-side phases of an end-to-end repetition (diagnostics)
+            w3 = time.perf_counter()
+            print(f"e2e repetition: rhs {1e3 * (w1 - w0):.2f} ms, guess {1e3 * (w2 - w1):.2f} ms, "
+                  f"solve {1e3 * (w3 - w2):.2f} ms, device {e0.elapsed_time(e1):.2f} ms", file=sys.stderr)
         return phi, st, e0.elapsed_time(e1), ch, rr
 
     n = args.train_samples + 2

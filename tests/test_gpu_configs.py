@@ -123,6 +123,41 @@ def test_line_block_width_changes_no_bit(cuda_lib, precision):
     np.testing.assert_array_equal(outs[0][0], outs[1][0])
 
 
+def _solver_with_pdl(case, on):
+    import vfs_poisson as V
+    old = os.environ.get("VFS_PDL")
+    try:
+        os.environ["VFS_PDL"] = "1" if on else "0"
+        return V.PoissonSolver.from_case(case)
+    finally:
+        if old is None:
+            os.environ.pop("VFS_PDL", None)
+        else:
+            os.environ["VFS_PDL"] = old
+
+
+@pytest.mark.parametrize("precision,smoother,graphs", [
+    (0, 4, 1), (0, 4, 0), (0, 3, 1), (0, 2, 1), (0, 1, 1), (0, 0, 1), (1, 3, 1), (1, 3, 0)])
+def test_dependent_launch_changes_no_bit(cuda_lib, precision, smoother, graphs):
+    """The V-cycle's kernels launched with programmatic stream serialization
+    (each may start during its predecessor's last wave and waits for it
+    before reading its results) give the same bits as ordinary launches,
+    for every smoother, with and without the V-cycle's CUDA graph."""
+    case = _tall(192, 32, 32)
+    outs = []
+    for on in (False, True):
+        s = _solver_with_pdl(case, on)
+        try:
+            s.rhs(case.ucont)
+            phi, st = s.solve(precision=precision, rtol=1e-10, max_it=60, smoother=smoother, use_graphs=graphs)
+            outs.append((phi, st.iterations, st.rel_residual))
+        finally:
+            s.close()
+    assert outs[0][1] == outs[1][1]
+    assert outs[0][2] == outs[1][2]
+    np.testing.assert_array_equal(outs[0][0], outs[1][0])
+
+
 @pytest.mark.parametrize("precision", [0, 1], ids=["fp32mg", "fp64mg"])
 def test_long_lines_vs_oracle(cuda_lib, precision):
     """A 24x256x24 grid (256-cell j-lines: 8-column blocks in FP32) solves

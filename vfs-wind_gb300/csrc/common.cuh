@@ -75,6 +75,20 @@ __device__ __forceinline__ double divergence_cell(const Grid &g, const double *_
   return v;
 }
 
+// Programmatic dependent launch (PTX griddepcontrol, sm_90 and later).  The
+// V-cycle's kernels are launched with programmatic stream serialization, so
+// a kernel's blocks may start while the previous kernel in the stream is
+// still running its last wave.  pdl_trigger lets the next kernel start once
+// every block of this one has started; pdl_wait blocks until the previous
+// kernel has completed and its writes are visible.  A kernel reads only
+// data that no kernel of the V-cycle writes (operator planes, line factors,
+// blank flags) before pdl_wait, and writes nothing before it.  Every
+// thread of such a kernel executes pdl_wait, so a kernel completes only
+// after its predecessor has, and the chain stays ordered.  Launched without
+// the attribute, both are no-ops.
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
 // Cells of a j-line handled by one thread of the line smoother; a line of
 // ny cells uses ceil(ny / kLineChunk) threads per column.
 constexpr int kLineChunk = 8;

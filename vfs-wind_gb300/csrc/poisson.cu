@@ -481,6 +481,10 @@ struct vfs_poisson {
   double *ls_rho = nullptr, *ls_level = nullptr;
   int ls_on = 0, ls_bc3 = 0, ls_bc4 = 0, ls_bc5 = 0;
   int line_cols_cap = 0;  // cap on the line kernels' columns per block (0: none)
+  // V-cycle kernels start during their predecessor's last wave (programmatic
+  // dependent launch; VFS_PDL=0 at create turns it off); pdl_prev: the last
+  // operation issued on the stream was such a kernel
+  bool pdl = true, pdl_prev = false;
   // history of converged solutions for the initial guess: the last hist_cap
   // solutions X_j (FGMRES iterates before the mean removal) and their images
   // Y_j = A X_j (b - r of the solves that produced them) under the operator
@@ -639,6 +643,34 @@ dim3 guess_grid(const Box &b) { return dim3((b.nx + 127) / 128, (b.ny + kGuessRo
     kern<<<(grid), (block), (smem), (h)->stream>>>(__VA_ARGS__);   \
     (h)->launches++;                                               \
   } while (0)
+
+// A kernel of the V-cycle.  When the previous operation on the stream was
+// one too, the launch carries programmatic stream serialization: its blocks
+// may start as the previous kernel's last blocks run, load the level's
+// operator planes and wait (griddepcontrol.wait) for that kernel's results.
+// Only kernels that wait before reading anything the V-cycle writes go
+// through here.  A memset or an event in between (vmemset, the profiling
+// events) makes the next launch an ordinary one.
+template <typename... P, typename... A>
+void launch_v(vfs_poisson *h, void (*kern)(P...), dim3 grid, dim3 block, size_t smem, A &&...args) {
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = h->stream;
+  cfg.attrs = at;
+  cfg.numAttrs = h->pdl && h->pdl_prev ? 1 : 0;
+  cudaLaunchKernelEx(&cfg, kern, std::forward<A>(args)...);
+  h->pdl_prev = true;
+  h->launches++;
+}
+void vmemset(vfs_poisson *h, void *p, size_t bytes) {
+  cudaMemsetAsync(p, 0, bytes, h->stream);
+  h->pdl_prev = false;
+}
 
 int alloc_metrics(vfs_poisson *h, const Grid &g, MetricPtrs &m) {
   size_t n = g.n();
@@ -1026,8 +1058,8 @@ struct Prec<float> {
   static constexpr auto sweep = k_line_sweep_f32;
   static void residual(vfs_poisson *h, Level &l, dim3 g, const float *x, const float *bb, float *r, int color,
                        bool split) {
-    if (split) LAUNCH(h, k_residual16_split, g, 128, l.b, l.C16, l.D32, x, bb, r, color);
-    else LAUNCH(h, k_residual16, g, 128, l.b, l.C16, l.D32, x, bb, r, color);
+    if (split) launch_v(h, k_residual16_split, g, 128, 0, l.b, l.C16, l.D32, x, bb, r, color);
+    else launch_v(h, k_residual16, g, 128, 0, l.b, l.C16, l.D32, x, bb, r, color);
   }
   static constexpr auto restrict_ = k_restrict_f32;
   static constexpr auto prolong = k_prolong_f32;
@@ -1038,8 +1070,8 @@ struct Prec<float> {
   static void fused(vfs_poisson *h, Level &l, dim3 g, dim3 blk, size_t sm, const float *xo, const float *xn,
                     const float *bb, float *xd, float omega, bool own_zero, bool both_zero, int color) {
     const auto kern = both_zero ? k_line_fused16_z : own_zero ? k_line_fused16_oz : k_line_fused16;
-    LAUNCH_SM(h, kern, g, blk, sm, l.b, l.C16, l.D32, xo, xn, bb, l.A32 + (size_t)SP * l.b.n(), l.inv32, l.cp32, xd,
-              omega, color);
+    launch_v(h, kern, g, blk, sm, l.b, l.C16, l.D32, xo, xn, bb, l.A32 + (size_t)SP * l.b.n(), l.inv32, l.cp32, xd,
+             omega, color);
   }
   static float *A(Level &l) { return l.A32; }
   static float *inv(Level &l) { return l.inv32; }
@@ -1053,7 +1085,7 @@ struct Prec<double> {
   static constexpr auto sweep = k_line_sweep_f64;
   static void residual(vfs_poisson *h, Level &l, dim3 g, const double *x, const double *bb, double *r, int color,
                        bool) {
-    LAUNCH(h, k_residual_f64, g, 128, l.b, l.A64, x, bb, r, color);
+    launch_v(h, k_residual_f64, g, 128, 0, l.b, l.A64, x, bb, r, color);
   }
   static constexpr auto restrict_ = k_restrict_f64;
   static constexpr auto prolong = k_prolong_f64;
@@ -1109,6 +1141,7 @@ template <typename T>
 void prof_begin(vfs_poisson *h, int li, bool zero_guess, int smoother) {
   if (!h->prof || li != 0 || h->pcount >= 16) return;
   cudaEventRecord(h->pev[0][h->pcount], h->stream);
+  h->pdl_prev = false;
   const double R = std::is_same<T, float>::value ? 14.0 : 22.0;
   double words = zero_guess ? (smoother >= 2 ? 0.5 * (5.0 + R + 6.0) : 5.0)
                             : (smoother == 0 ? 22.0 : R + 6.0);
@@ -1121,6 +1154,7 @@ void prof_begin(vfs_poisson *h, int li, bool zero_guess, int smoother) {
 void prof_end(vfs_poisson *h, int li) {
   if (!h->prof || li != 0 || h->pcount >= 16) return;
   cudaEventRecord(h->pev[1][h->pcount], h->stream);
+  h->pdl_prev = false;
   h->pcount++;
 }
 
@@ -1155,20 +1189,20 @@ void smooth(vfs_poisson *h, Level &l, int li, int smoother, bool zero_guess, T o
   T *Asp = Prec<T>::A(l) + (size_t)SP * l.b.n();
   prof_begin<T>(h, li, zero_guess, smoother);
   if (smoother == 0) {
-    LAUNCH_SM(h, Prec<T>::sweep, lg, lb, lsm, l.b, Prec<T>::A(l), Prec<T>::inv(l), Prec<T>::cp(l), x, bb, t, omega,
-              zero_guess ? 1 : 0);
+    launch_v(h, Prec<T>::sweep, lg, lb, lsm, l.b, Prec<T>::A(l), Prec<T>::inv(l), Prec<T>::cp(l), x, bb, t, omega,
+             zero_guess ? 1 : 0);
     std::swap(x, t);
   } else if (smoother == 1) {
     if (!zero_guess) Prec<T>::residual(h, l, box_grid(l.b), x, bb, r, -1, false);
-    LAUNCH_SM(h, Prec<T>::tri, lg, lb, lsm, l.b, zero_guess ? bb : r, Asp, Prec<T>::inv(l), Prec<T>::cp(l), x,
-              omega, zero_guess ? 1 : 0, -1);
+    launch_v(h, Prec<T>::tri, lg, lb, lsm, l.b, zero_guess ? bb : r, Asp, Prec<T>::inv(l), Prec<T>::cp(l), x,
+             omega, zero_guess ? 1 : 0, -1);
   } else if (smoother == 2) {
-    if (zero_guess) cudaMemsetAsync(x, 0, l.b.n() * sizeof(T), h->stream);
+    if (zero_guess) vmemset(h, x, l.b.n() * sizeof(T));
     for (int color = 0; color < 2; color++) {
       const bool skip_res = zero_guess && color == 0;  // x = 0: r = rhs
       if (!skip_res) Prec<T>::residual(h, l, box_grid(l.b), x, bb, r, color, false);
-      LAUNCH_SM(h, Prec<T>::tri, lg, lb, lsm, l.b, skip_res ? bb : r, Asp, Prec<T>::inv(l), Prec<T>::cp(l), x,
-                omega, 0, color);
+      launch_v(h, Prec<T>::tri, lg, lb, lsm, l.b, skip_res ? bb : r, Asp, Prec<T>::inv(l), Prec<T>::cp(l), x,
+               omega, 0, color);
     }
   } else if (fused_level<T>(l, smoother)) {
     // checkerboard zebra, residual in the line kernel: the first colour reads
@@ -1186,15 +1220,15 @@ void smooth(vfs_poisson *h, Level &l, int li, int smoother, bool zero_guess, T o
     // a split level it also writes the other colour's zeros (no clearing
     // pass), elsewhere x is cleared first.
     const bool split = split_level<T>(h, li, smoother);
-    if (zero_guess && !split) cudaMemsetAsync(x, 0, l.b.n() * sizeof(T), h->stream);
+    if (zero_guess && !split) vmemset(h, x, l.b.n() * sizeof(T));
     const int nh = (l.b.nx + 1) / 2;
     dim3 cg((nh + TI - 1) / TI, l.b.nz), rg((nh + 127) / 128, l.b.ny, l.b.nz);
     for (int color = 0; color < 2; color++) {
       const bool skip_res = zero_guess && color == 0;
       if (!skip_res) Prec<T>::residual(h, l, rg, x, bb, r, 2 + color, split);
       const auto tri = split ? Prec<T>::tri_split : Prec<T>::tri;
-      LAUNCH_SM(h, tri, cg, lb, lsm, l.b, skip_res ? bb : r, Asp, Prec<T>::inv(l), Prec<T>::cp(l), x, omega,
-                skip_res ? (split ? 2 : 1) : 0, (skip_res ? 4 : 2) + color);
+      launch_v(h, tri, cg, lb, lsm, l.b, skip_res ? bb : r, Asp, Prec<T>::inv(l), Prec<T>::cp(l), x, omega,
+               skip_res ? (split ? 2 : 1) : 0, (skip_res ? 4 : 2) + color);
     }
   }
   prof_end(h, li);
@@ -1206,28 +1240,29 @@ void vcycle(vfs_poisson *h, int li, int nu1, int nu2, T omega, int smoother) {
   T **v = Prec<T>::v(l);
   T *x = v[0], *bb = v[1], *r = v[2], *t = v[3];
   if (li == (int)h->L.size() - 1) {
-    LAUNCH(h, Prec<T>::coarsest, (int)((l.b.n() + 7) / 8), 256, l.nd, l.dmap, l.didx, l.dinv, bb, x, (int)l.b.n());
+    launch_v(h, Prec<T>::coarsest, (int)((l.b.n() + 7) / 8), 256, 0, l.nd, l.dmap, l.didx, l.dinv, bb, x,
+             (int)l.b.n());
     Prec<T>::xfinal(l) = x;
     return;
   }
-  if (nu1 == 0) cudaMemsetAsync(x, 0, l.b.n() * sizeof(T), h->stream);
+  if (nu1 == 0) vmemset(h, x, l.b.n() * sizeof(T));
   for (int s = 0; s < nu1; s++) smooth<T>(h, l, li, smoother, s == 0, omega, x, t, bb, r);
   if ((smoother == 3 || smoother == 4) && nu1 > 0 && omega == (T)1) {
     // the second colour's lines were just solved exactly (omega 1), so its
     // residual is zero up to rounding: form the first colour's only
     const int nh = (l.b.nx + 1) / 2;
-    cudaMemsetAsync(r, 0, l.b.n() * sizeof(T), h->stream);
+    vmemset(h, r, l.b.n() * sizeof(T));
     Prec<T>::residual(h, l, dim3((nh + 127) / 128, l.b.ny, l.b.nz), x, bb, r, 6, split_level<T>(h, li, smoother));
   } else {
     Prec<T>::residual(h, l, box_grid(l.b), x, bb, r, -1, split_level<T>(h, li, smoother));
   }
   Level &q = h->L[li + 1];
-  LAUNCH(h, Prec<T>::restrict_, box_grid(q.b), 128, l.b, q.b, l.cx, l.cy, l.cz, r, Prec<T>::w(l), q.blank,
-         Prec<T>::v(q)[1]);
+  launch_v(h, Prec<T>::restrict_, box_grid(q.b), 128, 0, l.b, q.b, l.cx, l.cy, l.cz, r, Prec<T>::w(l), q.blank,
+           Prec<T>::v(q)[1]);
   vcycle<T>(h, li + 1, nu1, nu2, omega, smoother);
   const auto prolong = split_level<T>(h, li, smoother) ? Prec<T>::prolong_split : Prec<T>::prolong;
-  LAUNCH(h, prolong, dim3((l.b.nx + 127) / 128, (l.b.ny + 1) / 2, l.b.nz), 128, l.b, q.b, l.cx, l.cy, l.cz,
-         (const T *)Prec<T>::xfinal(q), q.blank, l.blank, x, 1);
+  launch_v(h, prolong, dim3((l.b.nx + 127) / 128, (l.b.ny + 1) / 2, l.b.nz), 128, 0, l.b, q.b, l.cx, l.cy, l.cz,
+           (const T *)Prec<T>::xfinal(q), q.blank, l.blank, x, 1);
   for (int s = 0; s < nu2; s++) smooth<T>(h, l, li, smoother, false, omega, x, t, bb, r);
   Prec<T>::xfinal(l) = x;
 }
@@ -1236,6 +1271,7 @@ void vcycle(vfs_poisson *h, int li, int nu1, int nu2, T omega, int smoother) {
 template <typename T>
 int run_vcycle(vfs_poisson *h, const vfs_solve_opts &o) {
   const int p = std::is_same<T, float>::value ? 0 : 1;
+  h->pdl_prev = false;  // the V-cycle's first kernel waits for all earlier work
   if (!o.use_graphs || h->prof) {  // live kernel timing runs the V-cycle without a graph
     h->pcount = 0;
     vcycle<T>(h, 0, o.nu1, o.nu2, (T)o.omega, o.smoother);
@@ -1964,6 +2000,8 @@ int vfs_poisson_create(const vfs_grid_desc *gd, vfs_poisson **out) {
     h->spec_enable = !(sp && sp[0] == '0');
     const char *lc = getenv("VFS_LINE_COLUMNS");
     h->line_cols_cap = lc ? atoi(lc) : 0;
+    const char *pd = getenv("VFS_PDL");
+    h->pdl = !(pd && pd[0] == '0');
   }
   const size_t N = h->g.n(), n = h->box.n();
   int rc;

@@ -1031,6 +1031,8 @@ template <typename T>
 __device__ __forceinline__ void restrict_body(Box bf, Box bc, int cx, int cy, int cz, const T *__restrict__ rf,
                                               const T *__restrict__ wf, const uint8_t *__restrict__ blank_c,
                                               T *bc_out) {
+  pdl_trigger();
+  pdl_wait();
   int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y, k = blockIdx.z;
   if (i >= bc.nx) return;
   size_t cc = bc.at(i, j, k);
@@ -1052,6 +1054,8 @@ template <typename T, bool FSPLIT = false>
 __device__ __forceinline__ void prolong_body(Box bf, Box bc, int cx, int cy, int cz, const T *__restrict__ xc,
                                              const uint8_t *__restrict__ blank_c, const uint8_t *__restrict__ blank_f,
                                              T *xf, int add) {
+  pdl_trigger();
+  pdl_wait();
   // a thread takes rows j = blockIdx.y and blockIdx.y + gridDim.y of column
   // i (when inside the box): all the loads of both cells first, then both
   // results

@@ -35,6 +35,8 @@ __device__ __forceinline__ bool colour_row(const Box &b, int color, int t, int k
 template <typename T>
 __device__ __forceinline__ void residual_body(Box b, const T *__restrict__ A, const T *__restrict__ x,
                                               const T *__restrict__ rhs, T *__restrict__ r, int color) {
+  pdl_trigger();
+  pdl_wait();
   const int t = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y, k = blockIdx.z;
   int p;
   if (!colour_row(b, color, t, k, p)) return;
@@ -70,29 +72,41 @@ __global__ void k_pack16(size_t n, const double *__restrict__ A, __half2 *__rest
 // perturbs each one by at most 2^-11 relative and leaves the row sums (the
 // constant null space of the Neumann rows) exact.  44 operator bytes per row
 // instead of 76.  Colours and layouts as in residual_body; SPLIT: x and rhs
-// in the parity-split row layout (r written as the colour selects).
+// in the parity-split row layout (r written as the colour selects).  The
+// operator's 44 bytes per row are loaded before pdl_wait (no kernel of the
+// V-cycle writes them), x and rhs after it.
 template <bool SPLIT>
 __device__ __forceinline__ void residual16_body(Box b, const __half2 *__restrict__ C, const float *__restrict__ D,
                                                 const float *__restrict__ x, const float *__restrict__ rhs,
                                                 float *__restrict__ r, int color) {
+  pdl_trigger();
   const int t = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y, k = blockIdx.z;
   int p;
-  if (!colour_row(b, color, t, k, p)) return;
+  const bool ok = colour_row(b, color, t, k, p);
+  if (!ok) p = 0;  // (a row without a cell of the colour loads nothing)
   const int i = split_cell(p, b.nx);
   uint32_t idx[NSLOT];
   stencil_index_t<SPLIT>(b, i, j, k, idx);
   const uint32_t n = (uint32_t)b.n(), c = idx[CP], row = c - (SPLIT ? p : i), cs = row + p, cn = row + i;
+  __half2 hc[10];
+  float d = 0.f;
+  if (ok) {
+#pragma unroll
+    for (int m = 0; m < 10; m++) hc[m] = __ldcs(&C[m * n + cs]);
+    d = __ldcs(&D[cs]);
+  }
+  pdl_wait();
+  if (!ok) return;
   const float xc = __ldg(&x[c]);
   float s = 0.f;
 #pragma unroll
   for (int m = 0; m < 9; m++) {
-    const float2 f = __half22float2(__ldcs(&C[m * n + cs]));
+    const float2 f = __half22float2(hc[m]);
     s = fmaf(f.x, __ldg(&x[idx[2 * m + 1]]) - xc, s);
     s = fmaf(f.y, __ldg(&x[idx[2 * m + 2]]) - xc, s);
   }
-  const float2 f = __half22float2(__ldcs(&C[9 * n + cs]));
-  s = fmaf(f.x, xc, s);
-  r[color == 2 || color == 3 ? cs : cn] = rhs[SPLIT ? cs : cn] - __ldcs(&D[cs]) * s;
+  s = fmaf(__low2float(hc[9]), xc, s);
+  r[color == 2 || color == 3 ? cs : cn] = rhs[SPLIT ? cs : cn] - d * s;
 }
 __global__ void __launch_bounds__(128) k_residual16(Box b, const __half2 *__restrict__ C,
                                                     const float *__restrict__ D, const float *__restrict__ x,
@@ -203,6 +217,8 @@ __device__ __forceinline__ void line_sweep_body(Box b, const T *__restrict__ A, 
                                                 const T *__restrict__ cp, const T *__restrict__ x,
                                                 const T *__restrict__ rhs, T *__restrict__ xo, T omega,
                                                 int zero_guess) {
+  pdl_trigger();
+  pdl_wait();
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int tx = threadIdx.x, ty = threadIdx.y, TI = blockDim.x, P = blockDim.y;
   T *sA = (T *)smem_raw, *sB = sA + P * TI;
@@ -415,6 +431,7 @@ template <typename T, int M, bool SPLIT = false>
 __device__ __forceinline__ void line_tri_body(Box b, const T *__restrict__ r, const T *__restrict__ Asp,
                                               const T *__restrict__ inv, const T *__restrict__ cp, T *x, T omega,
                                               int zero_guess, int color) {
+  pdl_trigger();
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int tx = threadIdx.x, ty = threadIdx.y, TI = blockDim.x, P = blockDim.y;
   T *sA = (T *)smem_raw, *sB = sA + P * TI;
@@ -429,6 +446,21 @@ __device__ __forceinline__ void line_tri_body(Box b, const T *__restrict__ r, co
   // when the level's vectors are split, else natural
   const uint32_t cX = SPLIT ? cS : (valid ? (uint32_t)b.at(split_cell(pp, b.nx), 0, k) : 0u);
   const uint32_t cR = (color == 2 || color == 3) ? cS : cX;
+  // the line coefficients and factors first (no kernel of the V-cycle
+  // writes them), then, once the previous kernel has completed, the
+  // residual and the x being corrected: each chunk's loads in one memory
+  // round trip
+  T y[M], av[M], ivv[M], cv[M], xv[M];
+#pragma unroll
+  for (int q = 0; q < M; q++) {
+    const int j = j0 + q;
+    const uint32_t o = (uint32_t)j * sj;
+    const bool in = q < cnt;
+    av[q] = in && j > 0 ? __ldcs(&Asp[cS + o]) : (T)0;
+    ivv[q] = in ? __ldcs(&inv[cS + o]) : (T)0;
+    cv[q] = in && j < ny - 1 ? __ldcs(&cp[cS + o]) : (T)0;
+  }
+  pdl_wait();
   if (SPLIT && zero_guess == 2 && color >= 2) {
     // the first colour of a sweep from a zero guess: the other colour's
     // half of each row (the same column t there) starts at 0 too, so that
@@ -441,17 +473,10 @@ __device__ __forceinline__ void line_tri_body(Box b, const T *__restrict__ r, co
         if (j0 + q < ny) x[co + (uint32_t)(j0 + q) * sj] = (T)0;
     }
   }
-  // every load of the chunk up front (one memory round trip): the line
-  // coefficients, factors, residual and the x being corrected
-  T y[M], av[M], ivv[M], cv[M], xv[M];
 #pragma unroll
   for (int q = 0; q < M; q++) {
-    const int j = j0 + q;
-    const uint32_t o = (uint32_t)j * sj;
+    const uint32_t o = (uint32_t)(j0 + q) * sj;
     const bool in = q < cnt;
-    av[q] = in && j > 0 ? __ldcs(&Asp[cS + o]) : (T)0;
-    ivv[q] = in ? __ldcs(&inv[cS + o]) : (T)0;
-    cv[q] = in && j < ny - 1 ? __ldcs(&cp[cS + o]) : (T)0;
     y[q] = in ? __ldcs(&r[cR + o]) : (T)0;
     xv[q] = in && !zero_guess ? x[cX + o] : (T)0;
   }
@@ -486,6 +511,8 @@ __device__ __forceinline__ void line_fused16_body(Box b, const __half2 *__restri
                                                   const float *xo, const float *xn, const float *__restrict__ rhs,
                                                   const float *__restrict__ Asp, const float *__restrict__ inv,
                                                   const float *__restrict__ cp, float *xd, float omega, int color) {
+  pdl_trigger();
+  pdl_wait();  // (a wait after the factor loads would cost the kernel spills)
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int tx = threadIdx.x, ty = threadIdx.y, TI = blockDim.x, P = blockDim.y;
   float *sA = (float *)smem_raw, *sB = sA + P * TI;
@@ -595,6 +622,8 @@ template <typename T>
 __device__ __forceinline__ void coarsest_body(int nd, const int *__restrict__ dmap, const int *__restrict__ didx,
                                               const double *__restrict__ dinv, const T *__restrict__ rhs, T *x,
                                               int n) {
+  pdl_trigger();
+  pdl_wait();
   __shared__ double sb[1024];
   for (int q = threadIdx.x; q < nd; q += blockDim.x) sb[q] = (double)rhs[didx[q]];
   __syncthreads();

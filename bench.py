@@ -77,7 +77,10 @@ def parse():
     ap.add_argument("--train-samples", type=int, default=None,
                     help="plain-solver samples before the held-out steps (default 16; rotor: 148, steps 0-149)")
     ap.add_argument("--train-steps", type=int, default=3000)
-    ap.add_argument("--history", type=int, default=6, help="solutions kept for the history projection (0: off)")
+    ap.add_argument("--history", type=int, default=None,
+                    help="solutions kept for the history projection (0: off; default 10 for the static towers, "
+                         "2 for the moving bodies, whose operator changes every step so that only the newest two "
+                         "enter a guess)")
     ap.add_argument("--network-period", type=int, default=8,
                     help="while its candidate loses, the network runs on every n-th guess")
     a = ap.parse_args()
@@ -317,6 +320,8 @@ def run_ours(args):
     # 1. the plain solver generates the training data (steps 0 .. T+1); its
     # converged solutions also fill the solution history, so that the timed
     # steps start from a full history whatever the warm-up count
+    if args.history is None:
+        args.history = 2 if seq.moving else 10
     s.set_history(args.history)
     t0 = time.time()
     pool = LG.SamplePool((nx, ny, nz), args.train_samples)

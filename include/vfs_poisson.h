@@ -455,13 +455,17 @@ int64_t vfs_unet_kernel_launches(vfs_unet *u);
 /* Initial guess from a history of solutions (no counterpart in the
  * reference, which restarts from the previous step's Phi2,
  * poisson_hypre.c:577).  The handle keeps the last k converged solutions
- * X_j (1 <= k <= 8; 0 turns it off) and their images A X_j (b - r of the
+ * X_j (1 <= k <= 12; 0 turns it off) and their images A X_j (b - r of the
  * solves that produced them) under the operator assembly current when each
- * was stored.  vfs_poisson_history_guess, after vfs_poisson_rhs, forms two
+ * was stored, as the newest solution and the differences of consecutive
+ * ones.  vfs_poisson_history_guess, after vfs_poisson_rhs, forms two
  * candidates:
  *   - the projection x = sum_j c_j X_j over the solutions of the current
  *     assembly, with c minimising ||b - sum_j c_j A X_j||_2 (Fischer's
- *     projection for successive right-hand sides, CMAME 163 (1998) 193-204);
+ *     projection for successive right-hand sides, CMAME 163 (1998) 193-204),
+ *     solved by normal equations in the difference basis, whose Gram entries
+ *     are formed from the differences themselves (the raw images of
+ *     successive solutions are too nearly parallel for normal equations);
  *     never above the previous step's phi in residual;
  *   - the extrapolation 2 X_0 - X_1 of the newest two solutions (its
  *     residual from the stored images, or by an operator apply when a moving

@@ -79,6 +79,40 @@ def test_projection_exact_and_never_worse(cuda_lib, seq):
         s.close()
 
 
+def test_projection_reaches_least_squares(cuda_lib, seq):
+    """With 10 stored solutions the projection's residual is the least-squares
+    optimum over the images of the stored solutions (numpy lstsq with the
+    oracle's operator) within 1 %: the basis of the newest solution and the
+    differences of consecutive ones keeps the directions that normal
+    equations on the nearly parallel images themselves would lose."""
+    import vfs_poisson as V
+    case0, d, met, lhs, _ = seq
+    A = O.csr(lhs)
+    us = [CF._mask_faces(CF._fourier_ucont(np.random.default_rng(1003), NX, NY, NZ, shift=0.5 * t), case0.nvert)
+          for t in range(13)]
+    s = V.PoissonSolver.from_case(case0)
+    try:
+        s.set_history(10)
+        X = []
+        for step, u in enumerate(us[:-1]):
+            s.rhs(u)
+            if step:
+                s.history_guess()
+            phi, st = s.solve(opts=V.default_opts(rtol=1e-10, warm_start=2 if step else 0))
+            assert st.rel_residual <= 1e-10
+            X.append(O.from_da(d, lhs["gid"], phi))
+        s.rhs(us[-1])
+        s.history_guess()
+        ch, rels, _ = s.guess_report()
+        b2 = O.rhs(d, case0.nvert, lhs["gid"], us[-1], met["aj"])
+        Y = np.stack([A @ x for x in X[-10:]], 1)
+        c, *_ = np.linalg.lstsq(Y, b2, rcond=None)
+        r_ls = np.linalg.norm(b2 - Y @ c) / np.linalg.norm(b2)
+        assert rels[0] <= 1.01 * r_ls, (rels[0], r_ls)
+    finally:
+        s.close()
+
+
 def test_projection_after_new_operator(cuda_lib, seq):
     import vfs_poisson as V
     case0, d, met, lhs, us = seq

@@ -1,13 +1,15 @@
 """Numpy model of the history projection of the initial guess (CPU).
 
 The library's projection (vfs_poisson_history_guess) solves the normal
-equations of min ||b - sum_j c_j A X_j|| by a Cholesky factorisation taken
-newest solution first, dropping a vector whose pivot falls below 1e-13 of its
-Gram diagonal.  This model restates that step and checks it on an advected
-towers sequence solved by the oracle's CPU solver: the projection is never
-worse than the previous step's phi, it tracks a QR least-squares solution
-where the Gram matrix is well conditioned, and over 6 solutions it cuts the
-initial residual of the sequence by more than 1000x.
+equations of min ||b - sum_j c_j A X_j|| in the basis of the newest image
+Y_0 and the differences Y_0 - Y_1, Y_1 - Y_2, ... (Gram entries formed from
+the difference vectors), by a Cholesky factorisation in that order that
+drops a vector whose pivot falls below 1e-13 of its Gram diagonal.  This
+model restates that step and checks it on an advected towers sequence solved
+by the oracle's CPU solver: the projection is never worse than the previous
+step's phi, it reaches the least-squares optimum of a QR solution over the
+same solutions up to 8 of them, and over 6 solutions it cuts the initial
+residual of the sequence by more than 1000x.
 """
 import numpy as np
 import pytest
@@ -51,7 +53,7 @@ def sequence():
     A = O.csr(lhs).tocsr()
     mg = bench.cpu_solver(d, case0.coor, case0.nvert, met)
     bs, xs = [], []
-    for s in range(10):
+    for s in range(12):
         u = CF._mask_faces(CF._fourier_ucont(np.random.default_rng(1003), nx, ny, nz, shift=0.5 * s), case0.nvert)
         b2 = O.rhs(d, case0.nvert, lhs["gid"], u, met["aj"])
         x, st = mg.solve(O.to_da(d, lhs["gid"], b2), rtol=1e-10, max_it=100, nu1=1, nu2=2, omega=1.0,
@@ -65,23 +67,28 @@ def _rel(A, b, x):
     return np.linalg.norm(b - A @ x) / np.linalg.norm(b)
 
 
-@pytest.mark.parametrize("k", [2, 4, 6])
+def difference_basis(V):
+    """V_0, V_0 - V_1, V_1 - V_2, ... of vectors given newest first."""
+    return [V[0]] + [V[i] - V[i + 1] for i in range(len(V) - 1)]
+
+
+@pytest.mark.parametrize("k", [2, 4, 6, 8])
 def test_projection_model(sequence, k):
     A, bs, xs = sequence
-    n = 9
+    n = 11
     b = bs[n]
-    X = [xs[n - 1 - i] for i in range(k)]          # slot i: i-th newest
+    X = [xs[n - 1 - i] for i in range(k)]          # i-th newest
     Y = [A @ x for x in X]
-    G = np.array([[yi @ yj for yj in Y] for yi in Y])
-    g = np.array([y @ b for y in Y])
+    BX, BY = difference_basis(X), difference_basis(Y)
+    G = np.array([[yi @ yj for yj in BY] for yi in BY])
+    g = np.array([y @ b for y in BY])
     c = greedy_projection(G, g, list(range(k)))
-    xg = sum(ci * xi for ci, xi in zip(c, X))
+    xg = sum(ci * xi for ci, xi in zip(c, BX))
     r_proj = _rel(A, b, xg)
     r_prev = _rel(A, b, xs[n - 1])
     assert r_proj <= r_prev * (1 + 1e-9)
     cq, *_ = np.linalg.lstsq(np.stack(Y, 1), b, rcond=None)
     r_ls = _rel(A, b, np.stack(X, 1) @ cq)
-    if k <= 4:
-        assert r_proj <= 1.01 * r_ls
-    if k == 6:
+    assert r_proj <= 1.01 * r_ls, (k, r_proj, r_ls)
+    if k >= 6:
         assert r_proj < 1e-3 * r_prev, (r_proj, r_prev)

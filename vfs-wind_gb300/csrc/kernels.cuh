@@ -168,15 +168,23 @@ __global__ void k_scale_to32(size_t n, const double *v, float s, const float *si
 __global__ void k_reduce_norm(const double *partial, int nb, double *out, float *out32);
 __global__ void k_to64(size_t n, const float *x32, const double *x64, double *out, int split_nx);
 __global__ void k_sumsq(size_t n, const double *x, double *partial);
-// history projection of the initial guess (at most kHistMax solutions)
-constexpr int kHistMax = 8;
+// history projection of the initial guess (at most kHistMax solutions:
+// the newest and the differences of consecutive ones)
+constexpr int kHistMax = 12;
 struct HistPtrs {
   const double *p[kHistMax];
 };
-__global__ void k_hist_dots(size_t n, HistPtrs Y, int k, const double *v, double *partial);
-__global__ void k_hist_combine(size_t n, HistPtrs X, HistPtrs Y, int k, const double *c, const double *b, double *x,
-                               double *r, double *partial);
-__global__ void k_hist_push(size_t n, const double *x, const double *b, const double *r, double *Xs, double *Ys);
+// v . Y_j (j < k) and v . v as block partials (row j, row k)
+void launch_hist_dots(cudaStream_t st, int blocks, size_t n, const HistPtrs &Y, int k, const double *v,
+                      double *partial);
+// x = sum_j c_j X_j, r = b - sum_j c_j Y_j and the partials of ||r||^2
+void launch_hist_combine(cudaStream_t st, int blocks, size_t n, const HistPtrs &X, const HistPtrs &Y, int k,
+                         const double *c, const double *b, double *x, double *r, double *partial);
+// a converged solve into the newest solution and a difference slot, with
+// the new Gram entries as block partials (rows as in hist_push_body)
+void launch_hist_push(cudaStream_t st, int blocks, size_t n, const double *x, const double *b, const double *r,
+                      double *Xn, double *Yn, double *dX, double *dY, const HistPtrs &E, int m, bool first,
+                      double *partial);
 __global__ void k_fluid_moments(size_t n, const uint8_t *fluid, const double *z, double mean, int pass,
                                 double *partial);
 

@@ -485,16 +485,23 @@ struct vfs_poisson {
   // dependent launch; VFS_PDL=0 at create turns it off); pdl_prev: the last
   // operation issued on the stream was such a kernel
   bool pdl = true, pdl_prev = false;
-  // history of converged solutions for the initial guess: the last hist_cap
-  // solutions X_j (FGMRES iterates before the mean removal) and their images
-  // Y_j = A X_j (b - r of the solves that produced them) under the operator
-  // assembly hist_ver[j], a ring with the newest at hist_head - 1, and the
-  // Gram matrix G_ij = Y_i . Y_j (host).  The projection uses the slots of
-  // the current assembly only; the extrapolation uses the newest two.
+  // history of the last hist_cnt (at most hist_cap) converged solutions for
+  // the initial guess, held as the newest one X_n (the FGMRES iterate before
+  // the mean removal) with its image Y_n = A X_n (b - r of its solve), stored
+  // under the operator assembly hist_vn, and the differences of consecutive
+  // solutions before it, D_j = X_j - X_{j-1} with images E_j = Y_j - Y_{j-1},
+  // in a ring of hist_cap - 1 slots with the newest at hist_head - 1.
+  // hist_ver[j]: the assembly both ends of D_j were stored under (kHistMixed
+  // when they differ).  Gram entries (host): hist_Gnn = Y_n . Y_n,
+  // hist_Gn[j] = Y_n . E_j, hist_G[i][j] = E_i . E_j.  The projection uses
+  // the basis Y_n, E_newest, ... of the current assembly; the extrapolation
+  // X_n + D_newest = 2 X_n - X_{n-1}.
   int hist_cap = 0, hist_cnt = 0, hist_head = 0;
+  double *hist_Xn = nullptr, *hist_Yn = nullptr;
+  uint64_t hist_vn = 0;
   double *hist_X[kHistMax] = {}, *hist_Y[kHistMax] = {};
   uint64_t hist_ver[kHistMax] = {};
-  double hist_G[kHistMax][kHistMax] = {};
+  double hist_Gnn = 0., hist_Gn[kHistMax] = {}, hist_G[kHistMax][kHistMax] = {};
   double *hist_x = nullptr, *hist_r = nullptr;    // the projection and its residual
   double *hist_ex = nullptr, *hist_er = nullptr;  // the extrapolation and its residual
   double *hist_coef = nullptr;                    // combination coefficients (device)
@@ -1385,56 +1392,87 @@ HistPtrs hist_ptrs(double *const *a, int k) {
   return p;
 }
 
-// row and column s of the Gram matrix: Y_s . Y_j for the stored slots
-int hist_gram_row(vfs_poisson *h, int s) {
-  const int k = h->hist_cnt;
-  LAUNCH(h, k_hist_dots, kRedBlocks, 256, h->box.n(), hist_ptrs(h->hist_Y, k), k, (const double *)h->hist_Y[s],
-         h->partial);
-  double d[kHistMax + 1];
-  TRY(reduce_read(h, kRedBlocks, k + 1, d));
-  for (int j = 0; j < k; j++) h->hist_G[s][j] = h->hist_G[j][s] = d[j];
-  h->hist_G[s][s] = d[k];
-  return VFS_OK;
-}
+constexpr uint64_t kHistMixed = ~uint64_t(0);
 
-// slot of the i-th newest stored solution
+// difference slot of the i-th newest difference
 int hist_slot(const vfs_poisson *h, int i) {
-  return ((h->hist_head - 1 - i) % h->hist_cap + h->hist_cap) % h->hist_cap;
+  const int nd = h->hist_cap - 1;
+  return ((h->hist_head - 1 - i) % nd + nd) % nd;
 }
 
-// the slots stored under the current operator assembly, newest first (a
-// moving mask makes the older images stale: they are not recomputed)
+// the projection's basis under the current operator assembly: Y_n, then the
+// differences whose ends both belong to it, newest first (their slots in
+// sl); returns its size, 0 when the newest solution is of another assembly
+// (a moving mask makes the stored images stale: they are not recomputed)
 int hist_fresh(const vfs_poisson *h, int *sl) {
-  int nf = 0;
-  for (int i = 0; i < h->hist_cnt; i++) {
+  if (!h->hist_cnt || h->hist_vn != h->op_version) return 0;
+  int nf = 1;
+  for (int i = 0; i < h->hist_cnt - 1; i++) {
     const int q = hist_slot(h, i);
-    if (h->hist_ver[q] == h->op_version) sl[nf++] = q;
+    if (h->hist_ver[q] != h->op_version) break;
+    sl[nf++ - 1] = q;
   }
   return nf;
 }
 
 // store a converged solve: the iterate x and its image b - r (V_0 holds the
-// solve's final FP64 residual r = b - A x) under the current assembly
+// solve's final FP64 residual r = b - A x) under the current assembly, as
+// the new X_n, Y_n and, from the second solve on, the difference from the
+// previous newest in the ring (over the oldest difference when it is full)
 int hist_push(vfs_poisson *h) {
   if (!h->hist_cap) return VFS_OK;
-  const int s = h->hist_head;
-  LAUNCH(h, k_hist_push, kRedBlocks, 256, h->box.n(), (const double *)h->x, (const double *)h->b,
-         (const double *)h->V[0], h->hist_X[s], h->hist_Y[s]);
-  h->hist_ver[s] = h->op_version;
-  h->hist_head = (s + 1) % h->hist_cap;
+  const size_t n = h->box.n();
+  HistPtrs E{};
+  if (h->hist_cnt == 0 || h->hist_cap == 1) {
+    launch_hist_push(h->stream, kRedBlocks, n, h->x, h->b, h->V[0], h->hist_Xn, h->hist_Yn, nullptr, nullptr, E, 0,
+                     true, h->partial);
+    h->launches++;
+    TRY(reduce_read(h, kRedBlocks, 1, &h->hist_Gnn));
+    h->hist_vn = h->op_version;
+    h->hist_cnt = 1;
+    return VFS_OK;
+  }
+  const int s = h->hist_head, nd = h->hist_cap - 1;
+  // the differences that stay: all stored ones but the slot written now
+  const int keep = std::min(h->hist_cnt - 1, nd - 1);
+  int win[kHistMax];
+  for (int i = 0; i < keep; i++) {
+    win[i] = hist_slot(h, i);
+    E.p[i] = h->hist_Y[win[i]];
+  }
+  launch_hist_push(h->stream, kRedBlocks, n, h->x, h->b, h->V[0], h->hist_Xn, h->hist_Yn, h->hist_X[s],
+                   h->hist_Y[s], E, keep, false, h->partial);
+  h->launches++;
+  double d[kHistMax + 3];
+  TRY(reduce_read(h, kRedBlocks, keep + 3, d));
+  const double ee = d[keep], ye = d[keep + 1];
+  for (int i = 0; i < keep; i++) {
+    h->hist_G[s][win[i]] = h->hist_G[win[i]][s] = d[i];
+    h->hist_Gn[win[i]] += d[i];  // Y_new . E_j = Y_old . E_j + E_new . E_j
+  }
+  h->hist_G[s][s] = ee;
+  h->hist_Gn[s] = ye + ee;
+  h->hist_Gnn = d[keep + 2];
+  h->hist_ver[s] = h->hist_vn == h->op_version ? h->op_version : kHistMixed;
+  h->hist_vn = h->op_version;
+  h->hist_head = (s + 1) % nd;
   if (h->hist_cnt < h->hist_cap) h->hist_cnt++;
-  return hist_gram_row(h, s);
+  return VFS_OK;
 }
 
-// the projection x = X c, r = b - Y c minimising ||b - Y c|| over the
-// stored images of the current assembly: normal equations G c = Y^T b by a
-// Cholesky factorisation taken newest first, where a vector whose pivot
-// falls below 1e-13 of its Gram diagonal adds nothing new and keeps the
-// coefficient 0 (the images of successive solutions are nearly parallel).
-// The newest solution alone is in the span, so the result's residual is
+// the projection x = X c, r = b - Y c minimising ||b - Y c|| over the span of
+// the stored images of the current assembly, in the basis Y_n, E_newest, ...:
+// normal equations G c = B^T b by a Cholesky factorisation in that order,
+// where a vector whose pivot falls below 1e-13 of its Gram diagonal adds
+// nothing new and keeps the coefficient 0.  The images of successive
+// solutions are nearly parallel; their differences are not, and their Gram
+// entries were formed from the differences themselves, so that the
+// factorisation resolves the directions a least-squares fit by orthogonal
+// factors resolves (the raw images' Gram matrix loses them from about eight
+// solutions on).  Y_n alone is in the span, so the result's residual is
 // never above the previous step's phi's.  *rext receives the residual norm
-// of the extrapolation 2 X_0 - X_1 of the newest two solutions, predicted
-// from the Gram matrix when both are of the current assembly (else -1).
+// of the extrapolation 2 X_n - X_{n-1}, predicted from the Gram entries when
+// both solutions are of the current assembly (else -1).
 int hist_project(vfs_poisson *h, double *rnorm, double *bnorm, double *rext) {
   int sl[kHistMax];
   const int k = hist_fresh(h, sl);
@@ -1442,25 +1480,35 @@ int hist_project(vfs_poisson *h, double *rnorm, double *bnorm, double *rext) {
   if (k == 0) return fail(VFS_ESTATE, "no stored solution of the current operator");
   const size_t n = h->box.n();
   double *Xp[kHistMax], *Yp[kHistMax];
-  for (int i = 0; i < k; i++) {
-    Xp[i] = h->hist_X[sl[i]];
-    Yp[i] = h->hist_Y[sl[i]];
+  Xp[0] = h->hist_Xn;
+  Yp[0] = h->hist_Yn;
+  for (int i = 1; i < k; i++) {
+    Xp[i] = h->hist_X[sl[i - 1]];
+    Yp[i] = h->hist_Y[sl[i - 1]];
   }
-  LAUNCH(h, k_hist_dots, kRedBlocks, 256, n, hist_ptrs(Yp, k), k, (const double *)h->b, h->partial);
+  launch_hist_dots(h->stream, kRedBlocks, n, hist_ptrs(Yp, k), k, h->b, h->partial);
+  h->launches++;
   double g[kHistMax + 1];
   TRY(reduce_read(h, kRedBlocks, k + 1, g));
+  // the basis Gram matrix
+  double G[kHistMax][kHistMax];
+  G[0][0] = h->hist_Gnn;
+  for (int i = 1; i < k; i++) {
+    G[0][i] = G[i][0] = h->hist_Gn[sl[i - 1]];
+    for (int j = 1; j < k; j++) G[i][j] = h->hist_G[sl[i - 1]][sl[j - 1]];
+  }
   int ord[kHistMax], na = 0;
   double L[kHistMax][kHistMax] = {};
   for (int i = 0; i < k; i++) {
     double row[kHistMax];
     for (int q = 0; q < na; q++) {
-      double v = h->hist_G[sl[i]][sl[ord[q]]];
+      double v = G[i][ord[q]];
       for (int t = 0; t < q; t++) v -= row[t] * L[q][t];
       row[q] = v / L[q][q];
     }
-    double piv = h->hist_G[sl[i]][sl[i]];
+    double piv = G[i][i];
     for (int t = 0; t < na; t++) piv -= row[t] * row[t];
-    if (!(piv > 1e-13 * h->hist_G[sl[i]][sl[i]])) continue;
+    if (!(piv > 1e-13 * G[i][i])) continue;
     for (int t = 0; t < na; t++) L[na][t] = row[t];
     L[na][na] = std::sqrt(piv);
     ord[na++] = i;
@@ -1479,38 +1527,40 @@ int hist_project(vfs_poisson *h, double *rnorm, double *bnorm, double *rext) {
   for (int p = 0; p < na; p++) c[ord[p]] = cc[p];
   for (int j = 0; j < k; j++) h->hbuf[kHistStage + j] = c[j];
   CUDA_TRY(cudaMemcpyAsync(h->hist_coef, h->hbuf + kHistStage, k * 8, cudaMemcpyHostToDevice, h->stream));
-  LAUNCH(h, k_hist_combine, kRedBlocks, 256, n, hist_ptrs(Xp, k), hist_ptrs(Yp, k), k,
-         (const double *)h->hist_coef, (const double *)h->b, h->hist_x, h->hist_r, h->partial);
+  launch_hist_combine(h->stream, kRedBlocks, n, hist_ptrs(Xp, k), hist_ptrs(Yp, k), k, h->hist_coef, h->b,
+                      h->hist_x, h->hist_r, h->partial);
+  h->launches++;
   double rr;
   TRY(reduce_read(h, kRedBlocks, 1, &rr));
   *rnorm = std::sqrt(std::max(rr, 0.));
   *bnorm = std::sqrt(std::max(g[k], 0.));
-  if (k >= 2 && sl[0] == hist_slot(h, 0) && sl[1] == hist_slot(h, 1)) {
-    const double G00 = h->hist_G[sl[0]][sl[0]], G01 = h->hist_G[sl[0]][sl[1]], G11 = h->hist_G[sl[1]][sl[1]];
-    const double e2 = g[k] - 2. * (2. * g[0] - g[1]) + 4. * G00 - 4. * G01 + G11;
+  if (k >= 2 && sl[0] == hist_slot(h, 0)) {
+    // ||b - Y_n - E_newest||^2
+    const double e2 = g[k] - 2. * (g[0] + g[1]) + G[0][0] + 2. * G[0][1] + G[1][1];
     *rext = std::sqrt(std::max(e2, 0.));
   }
   return VFS_OK;
 }
 
-// the extrapolation 2 X_0 - X_1 of the newest two stored solutions (X_0
-// alone when one is stored) into hist_ex, and its FP64 residual into
 // hist_er: from the stored images when both belong to the current
 // assembly, otherwise by an operator apply
 int hist_extrap(vfs_poisson *h, double *rnorm) {
   const int k = std::min(h->hist_cnt, 2);
   if (k == 0) return fail(VFS_ESTATE, "no stored solution");
   const size_t n = h->box.n();
-  const int s0 = hist_slot(h, 0), s1 = hist_slot(h, k - 1);
-  double *Xp[2] = {h->hist_X[s0], h->hist_X[s1]}, *Yp[2] = {h->hist_Y[s0], h->hist_Y[s1]};
-  const bool fresh = h->hist_ver[s0] == h->op_version && h->hist_ver[s1] == h->op_version;
-  h->hbuf[kHistStage + kHistMax] = k > 1 ? 2. : 1.;
-  h->hbuf[kHistStage + kHistMax + 1] = -1.;
+  // X_n + D_newest (X_n alone with one stored solution)
+  const int s0 = k > 1 ? hist_slot(h, 0) : 0;
+  double *Xp[2] = {h->hist_Xn, k > 1 ? h->hist_X[s0] : nullptr};
+  double *Yp[2] = {h->hist_Yn, k > 1 ? h->hist_Y[s0] : nullptr};
+  const bool fresh = h->hist_vn == h->op_version && (k == 1 || h->hist_ver[s0] == h->op_version);
+  h->hbuf[kHistStage + kHistMax] = 1.;
+  h->hbuf[kHistStage + kHistMax + 1] = 1.;
   CUDA_TRY(cudaMemcpyAsync(h->hist_coef + kHistMax, h->hbuf + kHistStage + kHistMax, 2 * 8, cudaMemcpyHostToDevice,
                            h->stream));
   // (with stale images the combination's residual is formed again below)
-  LAUNCH(h, k_hist_combine, kRedBlocks, 256, n, hist_ptrs(Xp, k), hist_ptrs(Yp, k), k,
-         (const double *)(h->hist_coef + kHistMax), (const double *)h->b, h->hist_ex, h->hist_er, h->partial);
+  launch_hist_combine(h->stream, kRedBlocks, n, hist_ptrs(Xp, k), hist_ptrs(Yp, k), k, h->hist_coef + kHistMax,
+                      h->b, h->hist_ex, h->hist_er, h->partial);
+  h->launches++;
   if (fresh) {
     double rr;
     TRY(reduce_read(h, kRedBlocks, 1, &rr));
@@ -2519,17 +2569,19 @@ int vfs_poisson_set_history(vfs_poisson *h, int k) {
   }
   if (h->r0 == h->hist_r) h->r0_valid = false;
   if (h->r0 == h->hist_er) h->r0_valid = false;
-  for (double **p : {&h->hist_x, &h->hist_r, &h->hist_ex, &h->hist_er, &h->hist_coef}) {
+  for (double **p : {&h->hist_Xn, &h->hist_Yn, &h->hist_x, &h->hist_r, &h->hist_ex, &h->hist_er, &h->hist_coef}) {
     dfree(h, *p);
     *p = nullptr;
   }
   h->hist_cap = h->hist_cnt = h->hist_head = 0;
   const size_t n = h->box.n();
-  for (int j = 0; j < k; j++) {
+  for (int j = 0; j + 1 < k; j++) {  // k - 1 difference slots
     TRY(dalloc(h, &h->hist_X[j], n));
     TRY(dalloc(h, &h->hist_Y[j], n));
   }
   if (k) {
+    TRY(dalloc(h, &h->hist_Xn, n));
+    TRY(dalloc(h, &h->hist_Yn, n));
     TRY(dalloc(h, &h->hist_x, n));
     TRY(dalloc(h, &h->hist_r, n));
     TRY(dalloc(h, &h->hist_ex, n));

@@ -985,18 +985,13 @@ __device__ __forceinline__ void hist_dots_body(size_t n, const HistPtrs &Y, cons
     if (threadIdx.x == 0) partial[(size_t)j * gridDim.x + blockIdx.x] = t;
   }
 }
-__global__ void __launch_bounds__(256, 8) k_hist_dots(size_t n, HistPtrs Y, int k, const double *__restrict__ v,
-                                                   double *partial) {
-  switch (k) {
-    case 1: hist_dots_body<1>(n, Y, v, partial); break;
-    case 2: hist_dots_body<2>(n, Y, v, partial); break;
-    case 3: hist_dots_body<3>(n, Y, v, partial); break;
-    case 4: hist_dots_body<4>(n, Y, v, partial); break;
-    case 5: hist_dots_body<5>(n, Y, v, partial); break;
-    case 6: hist_dots_body<6>(n, Y, v, partial); break;
-    case 7: hist_dots_body<7>(n, Y, v, partial); break;
-    default: hist_dots_body<kHistMax>(n, Y, v, partial); break;
-  }
+// one kernel per basis size: up to 7 vectors the accumulators fit the 32
+// registers of 8 resident blocks; larger sizes get 64 (4 blocks) instead of
+// spilling
+template <int K>
+__global__ void __launch_bounds__(256, K <= 7 ? 8 : 4) k_hist_dots(size_t n, HistPtrs Y,
+                                                                  const double *__restrict__ v, double *partial) {
+  hist_dots_body<K>(n, Y, v, partial);
 }
 
 // x = sum_j c_j X_j and r = b - sum_j c_j Y_j (Y_j = A X_j), with the block
@@ -1024,20 +1019,13 @@ __device__ __forceinline__ void hist_combine_body(size_t n, const HistPtrs &X, c
   s = block_sum(s);
   if (threadIdx.x == 0) partial[blockIdx.x] = s;
 }
-__global__ void __launch_bounds__(256, 8) k_hist_combine(size_t n, HistPtrs X, HistPtrs Y, int k,
-                                                      const double *__restrict__ c, const double *__restrict__ b,
-                                                      double *__restrict__ x, double *__restrict__ r,
-                                                      double *partial) {
-  switch (k) {
-    case 1: hist_combine_body<1>(n, X, Y, c, b, x, r, partial); break;
-    case 2: hist_combine_body<2>(n, X, Y, c, b, x, r, partial); break;
-    case 3: hist_combine_body<3>(n, X, Y, c, b, x, r, partial); break;
-    case 4: hist_combine_body<4>(n, X, Y, c, b, x, r, partial); break;
-    case 5: hist_combine_body<5>(n, X, Y, c, b, x, r, partial); break;
-    case 6: hist_combine_body<6>(n, X, Y, c, b, x, r, partial); break;
-    case 7: hist_combine_body<7>(n, X, Y, c, b, x, r, partial); break;
-    default: hist_combine_body<kHistMax>(n, X, Y, c, b, x, r, partial); break;
-  }
+template <int K>
+__global__ void __launch_bounds__(256, K <= 8 ? 8 : 4) k_hist_combine(size_t n, HistPtrs X, HistPtrs Y,
+                                                                     const double *__restrict__ c,
+                                                                     const double *__restrict__ b,
+                                                                     double *__restrict__ x, double *__restrict__ r,
+                                                                     double *partial) {
+  hist_combine_body<K>(n, X, Y, c, b, x, r, partial);
 }
 
 // Moments over the fluid cells of z, for the estimated error of a guess
@@ -1067,14 +1055,95 @@ __global__ void __launch_bounds__(256) k_fluid_moments(size_t n, const uint8_t *
   }
 }
 
-// a solve's iterate and its image into a history slot: Xs = x, Ys = b - r
-// (r = b - A x, the solve's final FP64 residual)
-__global__ void __launch_bounds__(256) k_hist_push(size_t n, const double *__restrict__ x,
-                                                   const double *__restrict__ b, const double *__restrict__ r,
-                                                   double *__restrict__ Xs, double *__restrict__ Ys) {
+// A converged solve into the history: its iterate x and image y = b - r
+// (r = b - A x, the solve's final FP64 residual).  FIRST: x and y become
+// the newest solution Xn, Yn, and row 0 of `partial` gets the block
+// partials of y . y.  Otherwise the differences from the previous newest,
+// dx = x - Xn and e = y - Yn, go to a difference slot (dX, dY), x and y
+// replace Xn and Yn, and the rows get e . E_j for the M other differences
+// E_j of the window (rows 0..M-1), e . e (row M), Yn_old . e (row M + 1)
+// and y . y (row M + 2).  The differences are formed per cell before any
+// product, so that their Gram entries carry rounding relative to their own
+// size, not to the size of the nearly parallel solutions.
+template <int M, bool FIRST>
+__device__ __forceinline__ void hist_push_body(size_t n, const double *__restrict__ x, const double *__restrict__ b,
+                                               const double *__restrict__ r, double *Xn, double *Yn,
+                                               double *__restrict__ dX, double *__restrict__ dY, const HistPtrs &E,
+                                               double *partial) {
+  constexpr int R = FIRST ? 1 : M + 3;
+  double s[R];
+#pragma unroll
+  for (int j = 0; j < R; j++) s[j] = 0.;
   for (size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (size_t)gridDim.x * blockDim.x) {
-    Xs[q] = x[q];
-    Ys[q] = b[q] - r[q];
+    const double xv = x[q], y = b[q] - r[q];
+    if (FIRST) {
+      Xn[q] = xv;
+      Yn[q] = y;
+      s[0] = fma(y, y, s[0]);
+      continue;
+    }
+    const double xo = Xn[q], yo = Yn[q], e = y - yo;
+    dX[q] = xv - xo;
+    dY[q] = e;
+    Xn[q] = xv;
+    Yn[q] = y;
+#pragma unroll
+    for (int j = 0; j < M; j++) s[j] = fma(e, __ldg(&E.p[j][q]), s[j]);
+    s[M] = fma(e, e, s[M]);
+    s[M + 1] = fma(yo, e, s[M + 1]);
+    s[M + 2] = fma(y, y, s[M + 2]);
+  }
+#pragma unroll
+  for (int j = 0; j < R; j++) {
+    const double t = block_sum(s[j]);
+    if (threadIdx.x == 0) partial[(size_t)j * gridDim.x + blockIdx.x] = t;
+  }
+}
+template <int M, bool FIRST>
+__global__ void __launch_bounds__(256, FIRST || M <= 1 ? 8 : 4) k_hist_push(size_t n, const double *__restrict__ x,
+                                                                         const double *__restrict__ b,
+                                                                         const double *__restrict__ r, double *Xn,
+                                                                         double *Yn, double *dX, double *dY,
+                                                                         HistPtrs E, double *partial) {
+  hist_push_body<M, FIRST>(n, x, b, r, Xn, Yn, dX, dY, E, partial);
+}
+
+// Host launches of the history kernels for a basis of k vectors (push: m
+// other differences in the window); sizes outside 1..kHistMax (0..kHistMax-2
+// for m) launch nothing.
+void launch_hist_dots(cudaStream_t st, int blocks, size_t n, const HistPtrs &Y, int k, const double *v,
+                      double *partial) {
+  switch (k) {
+#define VFS_K(K) \
+  case K: k_hist_dots<K><<<blocks, 256, 0, st>>>(n, Y, v, partial); break;
+    VFS_K(1) VFS_K(2) VFS_K(3) VFS_K(4) VFS_K(5) VFS_K(6) VFS_K(7) VFS_K(8) VFS_K(9) VFS_K(10) VFS_K(11) VFS_K(12)
+#undef VFS_K
+    default: break;
+  }
+}
+void launch_hist_combine(cudaStream_t st, int blocks, size_t n, const HistPtrs &X, const HistPtrs &Y, int k,
+                         const double *c, const double *b, double *x, double *r, double *partial) {
+  switch (k) {
+#define VFS_K(K) \
+  case K: k_hist_combine<K><<<blocks, 256, 0, st>>>(n, X, Y, c, b, x, r, partial); break;
+    VFS_K(1) VFS_K(2) VFS_K(3) VFS_K(4) VFS_K(5) VFS_K(6) VFS_K(7) VFS_K(8) VFS_K(9) VFS_K(10) VFS_K(11) VFS_K(12)
+#undef VFS_K
+    default: break;
+  }
+}
+void launch_hist_push(cudaStream_t st, int blocks, size_t n, const double *x, const double *b, const double *r,
+                      double *Xn, double *Yn, double *dX, double *dY, const HistPtrs &E, int m, bool first,
+                      double *partial) {
+  if (first) {
+    k_hist_push<0, true><<<blocks, 256, 0, st>>>(n, x, b, r, Xn, Yn, dX, dY, E, partial);
+    return;
+  }
+  switch (m) {
+#define VFS_M(M) \
+  case M: k_hist_push<M, false><<<blocks, 256, 0, st>>>(n, x, b, r, Xn, Yn, dX, dY, E, partial); break;
+    VFS_M(0) VFS_M(1) VFS_M(2) VFS_M(3) VFS_M(4) VFS_M(5) VFS_M(6) VFS_M(7) VFS_M(8) VFS_M(9) VFS_M(10)
+#undef VFS_M
+    default: break;
   }
 }
 

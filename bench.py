@@ -78,7 +78,7 @@ def parse():
                     help="plain-solver samples before the held-out steps (default 16; rotor: 148, steps 0-149)")
     ap.add_argument("--train-steps", type=int, default=3000)
     ap.add_argument("--history", type=int, default=None,
-                    help="solutions kept for the history projection (0: off; default 10 for the static towers, "
+                    help="solutions kept for the history projection (0: off; default 8 for the static towers, "
                          "2 for the moving bodies, whose operator changes every step so that only the newest two "
                          "enter a guess)")
     ap.add_argument("--network-period", type=int, default=8,
@@ -321,7 +321,7 @@ def run_ours(args):
     # converged solutions also fill the solution history, so that the timed
     # steps start from a full history whatever the warm-up count
     if args.history is None:
-        args.history = 2 if seq.moving else 10
+        args.history = 2 if seq.moving else 8
     s.set_history(args.history)
     t0 = time.time()
     pool = LG.SamplePool((nx, ny, nz), args.train_samples)

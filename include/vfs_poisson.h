@@ -482,7 +482,10 @@ int64_t vfs_unet_kernel_launches(vfs_unet *u);
  * V-cycle then becomes the solve's first preconditioned vector, so the
  * judging costs one V-cycle per losing candidate.  rel_res gets
  * ||b - A x|| / ||b|| of the installed guess.  Each converged solve appends
- * its solution.  Memory: 2 k + 4 box-sized FP64 vectors. */
+ * its solution.  Memory: 2 k + 4 box-sized FP64 vectors.  Up to about 8
+ * solutions for sequences solved to rtol 1e-8 by about one V-cycle per
+ * step: a fit over more reaches the stored solutions' own errors, and the
+ * solutions then drift from step to step while every residual meets rtol. */
 int vfs_poisson_set_history(vfs_poisson *h, int k);
 int vfs_poisson_history_guess(vfs_poisson *h, double *rel_res);
 /* Whether converged solves append to the history (default 1): 0 lets a

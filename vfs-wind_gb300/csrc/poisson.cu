@@ -1525,6 +1525,13 @@ int hist_project(vfs_poisson *h, double *rnorm, double *bnorm, double *rext) {
     cc[p] = v / L[p][p];
   }
   for (int p = 0; p < na; p++) c[ord[p]] = cc[p];
+  if (h->phase) {
+    // the coefficients of the stored solutions themselves: X_n gets c_0 + c_1,
+    // X_{n-m} gets c_{m+1} - c_m (D_m = X_{n-m+1} - X_{n-m})
+    double s1 = 0.;
+    for (int m = 0; m < k; m++) s1 += std::fabs((m == 0 ? c[0] : -c[m]) + (m + 1 < k ? c[m + 1] : 0.));
+    fprintf(stderr, "vfs history: basis %d, used %d, sum |c| over the solutions %.3g\n", k, na, s1);
+  }
   for (int j = 0; j < k; j++) h->hbuf[kHistStage + j] = c[j];
   CUDA_TRY(cudaMemcpyAsync(h->hist_coef, h->hbuf + kHistStage, k * 8, cudaMemcpyHostToDevice, h->stream));
   launch_hist_combine(h->stream, kRedBlocks, n, hist_ptrs(Xp, k), hist_ptrs(Yp, k), k, h->hist_coef, h->b,

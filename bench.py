@@ -38,6 +38,7 @@ rank runs an independent replica (weak scaling) and rank 0 reports.
 from __future__ import annotations
 
 import argparse
+import gc
 import json
 import os
 import statistics
@@ -425,6 +426,12 @@ def run_ours(args):
         hist = [hist[-1], pa]
         n += 1
     barrier()
+    # Python's cyclic collector is run before the timed steps and paused
+    # during them (and during the end-to-end repetitions): a full collection
+    # of this process's heap takes milliseconds and would idle the GPU
+    # between two calls of the timed step
+    gc.collect()
+    gc.disable()
     clocks = ClockSampler(local)
     clocks.start()
     ms_a, ms_b, its_a, its_b, chosen, rel_prev, rel_learned, launches = [], [], [], [], [], [], [], 0
@@ -452,6 +459,7 @@ def run_ours(args):
         hist = [hist[-1], pa]
         n += 1
     ck = clocks.stop()
+    gc.enable()
     barrier()
     ms_b_mean = statistics.mean(ms_b)
     ms_a_mean = statistics.mean(ms_a)
@@ -503,6 +511,8 @@ def run_ours(args):
     out_h = torch.empty(shape, dtype=torch.float64).pin_memory()
     host = (u_h.numpy(), p1_h.numpy(), p2_h.numpy(), out_h.numpy())
     ms_e2e, h2d, its_e2e = [], [], []
+    gc.collect()
+    gc.disable()
     for r in range(1 + max(5, args.steps // 2)):
         u_h.copy_(step_inputs(n))
         p1_h.copy_(hist[-1])
@@ -515,6 +525,7 @@ def run_ours(args):
             h2d.append(u_h.numel() * 8 + (2 * p1_h.numel() * 8 if rr_e[1] >= 0 else 0))
         hist = [hist[-1], out_h.to(hist[-1].device)]
         n += 1
+    gc.enable()
     e2e_range = [min(ms_e2e), max(ms_e2e)]
     e2e_samples = [[round(t, 3), i] for t, i in zip(ms_e2e, its_e2e)]
     ms_e2e = statistics.mean(ms_e2e)
@@ -583,6 +594,7 @@ def run_ours(args):
                          "data_seconds": round(t_data, 2), "loss_first": losses[0] if losses else None,
                          "loss_last50": float(np.mean(losses[-50:])) if losses else None},
             "l2": "inputs larger than L2 (finest-level operator: 0.55 GB packed, 0.96 GB in FP32, 1.9 GB in FP64)",
+            "python_gc": "collected before, and paused during, the timed steps and the end-to-end repetitions",
             "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
         },
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",

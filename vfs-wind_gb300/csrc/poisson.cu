@@ -2428,7 +2428,10 @@ int vfs_poisson_solve(vfs_poisson *h, double *phi, const vfs_solve_opts *opts, v
   } else if (!o.warm_start) {
     CUDA_TRY(cudaMemsetAsync(h->x, 0, n * 8, h->stream));
   }
+  const auto tf0 = std::chrono::steady_clock::now();
   TRY(fgmres(h, o, &st));
+  const auto tf1 = std::chrono::steady_clock::now();
+  if (h->phase) cudaEventRecord(h->phev[0], h->stream);
   // Remove_Nullspace of phi (:604-608), its shift applied by the DA output
   const bool shift = h->desc.bctype3 != -10 && !(h->ls_on && h->ls_bc5 == 4);
   if (shift) {
@@ -2451,15 +2454,31 @@ int vfs_poisson_solve(vfs_poisson *h, double *phi, const vfs_solve_opts *opts, v
     CUDA_TRY(cudaEventRecord(h->dl_ev[0], h->stream));
     CUDA_TRY(cudaStreamWaitEvent(h->dl_stream, h->dl_ev[0], 0));
     CUDA_TRY(cudaMemcpyAsync(phi, h->phi_da, h->g.n() * sizeof(double), cudaMemcpyDeviceToHost, h->dl_stream));
+    if (h->phase) cudaEventRecord(h->phev[2], h->dl_stream);
     CUDA_TRY(cudaEventRecord(h->dl_ev[1], h->dl_stream));
   } else if (phi) {
     TRY(download(h, phi, h->phi_da, h->g.n()));
   }
   if (h->hist_cap && h->hist_record && st.initial_rel_residual > 0. && st.rel_residual <= o.rtol)
     TRY(hist_push(h));
+  if (h->phase) cudaEventRecord(h->phev[1], h->stream);
+  const auto tf2 = std::chrono::steady_clock::now();
   if (host_out) CUDA_TRY(cudaStreamWaitEvent(h->stream, h->dl_ev[1], 0));
   CUDA_TRY(cudaEventRecord(h->ev1, h->stream));
   TRY(sync(h));
+  if (h->phase) {
+    // host: the FGMRES call, the tail's launches (with the push's Gram read)
+    // and the final wait; device: from the end of FGMRES to the end of the
+    // push and of the host copy
+    const auto tf3 = std::chrono::steady_clock::now();
+    float a = 0.f, c = -1.f;
+    cudaEventElapsedTime(&a, h->phev[0], h->phev[1]);
+    if (host_out) cudaEventElapsedTime(&c, h->phev[0], h->phev[2]);
+    fprintf(stderr, "vfs solve tail ms: host fgmres %.3f tail %.3f wait %.3f; device to push end %.3f, to copy end %.3f\n",
+            std::chrono::duration<double, std::milli>(tf1 - tf0).count(),
+            std::chrono::duration<double, std::milli>(tf2 - tf1).count(),
+            std::chrono::duration<double, std::milli>(tf3 - tf2).count(), a, c);
+  }
   float ms = 0.f;
   cudaEventElapsedTime(&ms, h->ev0, h->ev1);
   st.ms_total = ms;

@@ -3,7 +3,7 @@
 learned guess + FP32 V-cycle in FP64 refinement vs the plain FP64 GPU solver.
 
 Workload: the 256x192x256 curvilinear wind-farm-like grid with a 3x2 array of
-tower cylinders (configuration 3: geometric 1.03 wall stretching, amplitude
+tower cylinders (geometric 1.03 wall stretching, amplitude
 0.02), run as a time sequence: the seeded Fourier-mode Ucont advects by 0.5
 cells per step in x, the towers (closed triangulated surfaces classified by
 the library's immersed-boundary search) stay put.  One step is one
@@ -55,12 +55,13 @@ for _p in (os.path.join(REPO, "vfs-wind_gb300"), os.path.join(REPO, "oracle"), R
 METRIC = "ms per Poisson solve to 1e-8 rel. residual: learned+FP32/FP64 vs plain FP64 GPU"
 def workload(nx, ny, nz, kind="towers"):
     if kind == "rotor":
-        return (f"rotor {nx}x{ny}x{nz} sequence (config 4: curvilinear grid of config 2, 3-rod rotor rotating "
+        return (f"rotor {nx}x{ny}x{nz} sequence (curvilinear grid: tanh wall stretching, sinusoidal node "
+                "perturbation of amplitude 0.05; 3-rod rotor rotating "
                 "2 deg/step; Fourier Ucont advected 0.5 cells/step; steps 0-149 train, 150-199 held out)")
     if kind == "farm":
-        return (f"farm {nx}x{ny}x{nz} sequence (config 5 grid: geometric 1.02 wall stretching, amplitude 0.02, "
+        return (f"farm {nx}x{ny}x{nz} sequence (geometric 1.02 wall stretching, amplitude 0.02, "
                 "4x3 towers with 3-rod rotors rotating 2 deg/step; Fourier Ucont advected 0.5 cells/step)")
-    return (f"towers {nx}x{ny}x{nz} sequence (config 3 grid: geometric 1.03 wall stretching, amplitude 0.02, "
+    return (f"towers {nx}x{ny}x{nz} sequence (geometric 1.03 wall stretching, amplitude 0.02, "
             "3x2 tower cylinders; Fourier Ucont advected 0.5 cells/step)")
 
 

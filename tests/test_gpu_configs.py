@@ -1,8 +1,8 @@
 """Solves at the stated configuration sizes and on long j-lines, against the
 oracle (marked gpu).
 
-  * configuration 1 (64x64x64 channel) and configuration 2 (128x96x128
-    curvilinear grid with the cylinder), both precisions of the V-cycle:
+  * the 64x64x64 channel and the 128x96x128 curvilinear grid with the
+    cylinder, both precisions of the V-cycle:
     the true FP64 relative residual of the returned phi is <= 1e-8 (the
     oracle's operator and right-hand side), phi is within 1e-6 relative L2
     of the oracle's CPU solve to 1e-11 (both with the fluid mean removed,

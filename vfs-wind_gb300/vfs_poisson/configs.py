@@ -180,7 +180,7 @@ def _fourier_ucont(rng, nx, ny, nz, modes=32, kmax=8, noise=0.1, shift=0.0):
 
 
 def channel(nx=64, ny=64, nz=64, seed=1001):
-    """Config 1: Cartesian channel, tanh wall stretching (beta 1.5) in y,
+    """The channel: Cartesian, tanh wall stretching (beta 1.5) in y,
     periodic x and z (periodic DA), Neumann y walls, no body."""
     rng = np.random.default_rng(seed)
     coor = _nodes(nx, ny, nz, lambda e: _tanh_stretch(e, 1.5), 0.0)
@@ -190,7 +190,7 @@ def channel(nx=64, ny=64, nz=64, seed=1001):
 
 
 def cylinder(nx=128, ny=96, nz=128, seed=1002, amp=0.05):
-    """Config 2: curvilinear grid (amplitude 0.05, tanh beta 2 in eta),
+    """The cylinder case: curvilinear grid (amplitude 0.05, tanh beta 2 in eta),
     periodic x, vertical cylinder of radius 0.1 at the domain centre."""
     rng = np.random.default_rng(seed)
     coor = _nodes(nx, ny, nz, lambda e: _tanh_stretch(e, 2.0), amp)
@@ -203,7 +203,7 @@ def cylinder(nx=128, ny=96, nz=128, seed=1002, amp=0.05):
 
 def towers(nx=256, ny=192, nz=256, seed=1003, amp=0.02, ratio=1.03, array=(3, 2),
            radius=0.02, physical=True):
-    """Config 3: wind-farm-like grid, geometric wall stretching (ratio 1.03)
+    """The towers: wind-farm-like grid, geometric wall stretching (ratio 1.03)
     in y, perturbation amplitude 0.02, periodic x and z, a 3x2 array of
     vertical tower cylinders (radius 0.02, 0.25 streamwise and 0.3 spanwise
     spacing); Fourier-mode Ucont plus noise."""
@@ -244,7 +244,7 @@ def rotor_mask(coor, centre, angle_deg, rods=3, rod_radius_cells=3, rod_length_c
 
 
 def rotor(nx=192, ny=128, nz=192, step=0, seed=1004, amp=0.05):
-    """Config 4: config-2 geometry with a 3-rod rotor (radius 3 cells,
+    """The rotor: the cylinder case's geometry with a 3-rod rotor (radius 3 cells,
     length 30 cells) rotating 2 degrees per step about a z-axis hub at the
     domain centre; Fourier RHS advected 0.5 cells per step in x."""
     rng = np.random.default_rng(seed)

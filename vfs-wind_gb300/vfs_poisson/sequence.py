@@ -106,7 +106,7 @@ class _Sequence:
 
 
 class RotorSequence(_Sequence):
-    """Config 4: 192x128x192, the cylinder case's curvilinear grid (tanh
+    """The rotor: 192x128x192, the cylinder case's curvilinear grid (tanh
     beta 2 in eta, amplitude 0.05, periodic x), a 3-rod rotor (radius 3
     cells, length 30 cells) rotating 2 degrees per step about a z-axis hub at
     the domain centre, Fourier fluxes advected 0.5 cells per step in x."""
@@ -142,7 +142,7 @@ class TowerSequence(_Sequence):
 
 
 class FarmSequence(_Sequence):
-    """Configuration 5: 512x256x512, geometric 1.02 wall stretching,
+    """The wind farm: 512x256x512, geometric 1.02 wall stretching,
     amplitude 0.02, periodic x and z; a 4x3 array of towers (the towers
     case's radius 0.02 and 0.25 streamwise spacing, 0.3 spanwise, filling the
     domain) from below the wall to the hub height 0.5, each carrying a 3-rod

@@ -65,6 +65,22 @@ def test_rotor_rods(cuda_lib, angle):
     _assert_same(g, o, fails)
 
 
+@pytest.mark.parametrize("kind", ["towers", "rotor"])
+def test_later_bodies_on_odd_grids(cuda_lib, kind):
+    """Bodies after the first search only the index box of their hash box,
+    found through bounds of the cell centres over 8x8x8 blocks: grids whose
+    sizes are no multiple of 8 end in partial blocks."""
+    if kind == "towers":
+        c = CF.towers(37, 21, 43, radius=0.05)
+        surfs = CF.tower_surfaces(radius=0.05, height=0.6)
+    else:
+        c = CF.rotor(29, 19, 35)
+        surfs = CF.rotor_surfaces(angle_deg=21.0)
+    g, o, fails = _run_both(c, surfs)
+    _assert_same(g, o, fails)
+    assert (g == 3).sum() > 0
+
+
 @pytest.mark.parametrize("which", ["side", "cap"])
 def test_duplicated_triangles_give_up(cuda_lib, which):
     # a surface with repeated triangles: every ray through them meets a

@@ -158,14 +158,68 @@ __global__ void k_ibm_classify_from(Grid g, const double *__restrict__ cent, int
 // index box of the interior cells whose centre lies strictly inside the
 // body's hash box (the cells the classification can change): atomic
 // min / max into box[0..2] / box[3..5]
-__global__ void k_ibm_box(Grid g, const double *__restrict__ cent, HashBox H, int *box) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x + 1, j = blockIdx.y + 1, k = blockIdx.z + 1;
-  if (i >= g.mx - 1) return;
-  const size_t t = g.at(i, j, k);
-  const double p0 = cent[t * 3], p1 = cent[t * 3 + 1], p2 = cent[t * 3 + 2];
-  if (p0 > H.xmin && p0 < H.xmax && p1 > H.ymin && p1 < H.ymax && p2 > H.zmin && p2 < H.zmax) {
-    atomicMin(&box[0], i); atomicMin(&box[1], j); atomicMin(&box[2], k);
-    atomicMax(&box[3], i); atomicMax(&box[4], j); atomicMax(&box[5], k);
+// The search of a body after the first needs the index box of the interior
+// cells whose centre lies strictly inside its hash box.  The centres are
+// bounded per block of 8x8x8 interior cells once per grid (k_cent_blocks);
+// a block whose bounds miss the hash box holds no such cell, so only the
+// cells of the other blocks are tested, with the same strict comparisons.
+constexpr int kCentBlock = 8;
+__global__ void __launch_bounds__(512) k_cent_blocks(Grid g, const double *__restrict__ cent, int nbx, int nby,
+                                                     double *bbox) {
+  const int b = blockIdx.x;
+  const int bi = b % nbx, bj = (b / nbx) % nby, bk = b / (nbx * nby);
+  const int i = 1 + bi * kCentBlock + (threadIdx.x & 7), j = 1 + bj * kCentBlock + ((threadIdx.x >> 3) & 7),
+            k = 1 + bk * kCentBlock + (threadIdx.x >> 6);
+  double lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+  if (i < g.mx - 1 && j < g.my - 1 && k < g.mz - 1) {
+    const size_t t = g.at(i, j, k);
+    for (int q = 0; q < 3; q++) lo[q] = hi[q] = cent[t * 3 + q];
+  }
+  for (int q = 0; q < 3; q++)
+    for (int o = 16; o > 0; o >>= 1) {
+      lo[q] = fmin(lo[q], __shfl_xor_sync(0xffffffffu, lo[q], o));
+      hi[q] = fmax(hi[q], __shfl_xor_sync(0xffffffffu, hi[q], o));
+    }
+  __shared__ double sh[16][6];
+  const int w = threadIdx.x >> 5;
+  if ((threadIdx.x & 31) == 0)
+    for (int q = 0; q < 3; q++) { sh[w][q] = lo[q]; sh[w][3 + q] = hi[q]; }
+  __syncthreads();
+  if (threadIdx.x < 6) {
+    double v = sh[0][threadIdx.x];
+    for (int u = 1; u < 16; u++) v = threadIdx.x < 3 ? fmin(v, sh[u][threadIdx.x]) : fmax(v, sh[u][threadIdx.x]);
+    bbox[(size_t)b * 6 + threadIdx.x] = v;
+  }
+}
+
+// One thread tests one block's bounds; a warp then walks the cells of each
+// of its blocks that meet the hash box (box: atomic min/max of i, j, k).
+__global__ void __launch_bounds__(256) k_ibm_box_blocks(Grid g, const double *__restrict__ cent,
+                                                        const double *__restrict__ bbox, int nbx, int nby,
+                                                        int nblocks, HashBox H, int *box) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x, lane = threadIdx.x & 31;
+  bool hit = false;
+  if (b < nblocks) {
+    const double *q = bbox + (size_t)b * 6;
+    hit = q[3] > H.xmin && q[0] < H.xmax && q[4] > H.ymin && q[1] < H.ymax && q[5] > H.zmin && q[2] < H.zmax;
+  }
+  unsigned m = __ballot_sync(0xffffffffu, hit);
+  while (m) {
+    const int src = __ffs(m) - 1;
+    m &= m - 1;
+    const int bb = b - lane + src;
+    const int bi = bb % nbx, bj = (bb / nbx) % nby, bk = bb / (nbx * nby);
+    for (int c = lane; c < kCentBlock * kCentBlock * kCentBlock; c += 32) {
+      const int i = 1 + bi * kCentBlock + (c & 7), j = 1 + bj * kCentBlock + ((c >> 3) & 7),
+                k = 1 + bk * kCentBlock + (c >> 6);
+      if (i >= g.mx - 1 || j >= g.my - 1 || k >= g.mz - 1) continue;
+      const size_t t = g.at(i, j, k);
+      const double p0 = cent[t * 3], p1 = cent[t * 3 + 1], p2 = cent[t * 3 + 2];
+      if (p0 > H.xmin && p0 < H.xmax && p1 > H.ymin && p1 < H.ymax && p2 > H.zmin && p2 < H.zmax) {
+        atomicMin(&box[0], i); atomicMin(&box[1], j); atomicMin(&box[2], k);
+        atomicMax(&box[3], i); atomicMax(&box[4], j); atomicMax(&box[5], k);
+      }
+    }
   }
 }
 
@@ -639,8 +693,31 @@ int ibm_search_impl(vfs_poisson *h, int ibi, int n_v, const double *xyz, int n_e
     // one cell for the dilation and by one more for the copy it reads.
     int init[6] = {INT_MAX, INT_MAX, INT_MAX, INT_MIN, INT_MIN, INT_MIN}, bx[6];
     int *dbox = (int *)buf[10];
+    const int nbx = (g.mx - 2 + kCentBlock - 1) / kCentBlock, nby = (g.my - 2 + kCentBlock - 1) / kCentBlock,
+              nbz = (g.mz - 2 + kCentBlock - 1) / kCentBlock, nblocks = nbx * nby * nbz;
+    IbmScratch &sc = *cx.scratch;
+    if (!sc.bbox_valid) {
+      const size_t need = (size_t)nblocks * 6 * 8;
+      if (sc.bbox_cap < need) {
+        if (sc.bbox) {
+          cudaStreamSynchronize(st);
+          cudaFree(sc.bbox);
+        }
+        sc.bbox = nullptr;
+        sc.bbox_cap = 0;
+        if (cudaMalloc(&sc.bbox, need) != cudaSuccess) {
+          cudaGetLastError();
+          sc.bbox = nullptr;
+          return fail(VFS_ENOMEM, "device allocation for the surface search failed");
+        }
+        sc.bbox_cap = need;
+      }
+      k_cent_blocks<<<nblocks, 512, 0, st>>>(g, cx.cent, nbx, nby, sc.bbox);
+      *cx.launches += 1;
+      sc.bbox_valid = true;
+    }
     cudaMemcpyAsync(dbox, init, sizeof(init), cudaMemcpyHostToDevice, st);
-    k_ibm_box<<<gi, 128, 0, st>>>(g, cx.cent, H, dbox);
+    k_ibm_box_blocks<<<(nblocks + 255) / 256, 256, 0, st>>>(g, cx.cent, sc.bbox, nbx, nby, nblocks, H, dbox);
     cudaMemcpyAsync(bx, dbox, sizeof(bx), cudaMemcpyDeviceToHost, st);
     *cx.launches += 1;
     cudaError_t eb = cudaStreamSynchronize(st);

@@ -203,6 +203,11 @@ struct IbmBody {
 struct IbmScratch {
   void *buf[11] = {};
   size_t cap[11] = {};
+  // bounds of the cell centres over blocks of 8x8x8 interior cells (6
+  // doubles each), formed by the first search after the grid was set
+  double *bbox = nullptr;
+  size_t bbox_cap = 0;
+  bool bbox_valid = false;
 };
 struct IbmContext {
   cudaStream_t stream;

@@ -2095,6 +2095,7 @@ void vfs_poisson_destroy(vfs_poisson *h) {
   h->allocs.clear();
   for (void *p : h->ibm_scratch.buf)
     if (p) cudaFree(p);
+  if (h->ibm_scratch.bbox) cudaFree(h->ibm_scratch.bbox);
   for (auto &b : h->ibm_bodies) {
     if (b.nodes) cudaFree(b.nodes);
     if (b.tri) cudaFree(b.tri);
@@ -2120,6 +2121,7 @@ void vfs_poisson_destroy(vfs_poisson *h) {
 int vfs_poisson_set_grid(vfs_poisson *h, const double *coor, const double *const *fm) {
   if (!h || !coor) return fail(VFS_EINVAL, "null argument");
   h->hier_cmax = -1;  // new coordinates: the next mask builds the hierarchy afresh
+  h->ibm_scratch.bbox_valid = false;  // and the next search bounds the new centres
   const size_t N = h->g.n();
   TRY(upload(h, h->coor, coor, 3 * N));
   TRY(form_metrics(h, h->g, h->coor, h->met));

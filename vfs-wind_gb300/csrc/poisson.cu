@@ -823,13 +823,18 @@ int build_coarsest(vfs_poisson *h, Level &l) {
     double piv = M[(size_t)c * nd + c];
     double ip = piv != 0. ? 1. / piv : 0.;
     for (int q = 0; q < nd; q++) { M[(size_t)c * nd + q] *= ip; I[(size_t)c * nd + q] *= ip; }
+    const double *__restrict__ mc = &M[(size_t)c * nd];
+    const double *__restrict__ ic = &I[(size_t)c * nd];
     for (int r = 0; r < nd; r++) {
       if (r == c) continue;
       double f = M[(size_t)r * nd + c];
       if (f == 0.) continue;
+      // distinct rows: the restrict pointers let the compiler vectorise
+      double *__restrict__ mr = &M[(size_t)r * nd];
+      double *__restrict__ ir = &I[(size_t)r * nd];
       for (int q = 0; q < nd; q++) {
-        M[(size_t)r * nd + q] -= f * M[(size_t)c * nd + q];
-        I[(size_t)r * nd + q] -= f * I[(size_t)c * nd + q];
+        mr[q] -= f * mc[q];
+        ir[q] -= f * ic[q];
       }
     }
   }
@@ -2166,20 +2171,14 @@ int vfs_poisson_set_nvert(vfs_poisson *h, const double *nvert) {
            h->L[0].A64, h->L[0].rowtype, fls);
   else
     LAUNCH(h, k_assemble, box_grid(h->box), 128, h->g, h->box, h->nvert, h->met, 0, 1, 0, h->A0, h->rowtype0, fls);
-  uint8_t *blank;
-  double *w64;
-  float *w32;
-  TRY(dalloc(h, &blank, n));
-  TRY(dalloc(h, &w64, n));
-  TRY(dalloc(h, &w32, n));
-  LAUNCH(h, k_level_masks, lin_grid(n), 256, h->g, h->box, h->nvert, blank, w64, w32, h->aj_box,
-         (const double *)h->met.aj);
+  // aj at the box cells for the row scale (each level forms its own masks)
+  LAUNCH(h, k_level_masks, lin_grid(n), 256, h->g, h->box, h->nvert, (uint8_t *)nullptr, (double *)nullptr,
+         (float *)nullptr, h->aj_box, (const double *)h->met.aj);
   LAUNCH(h, k_row_scale, lin_grid(n), 256, n, h->rowtype0, h->aj_box, h->scale);
   LAUNCH(h, k_cast_planes_f32, kRedBlocks, 256, h->scale, h->scale32, n);
   int tot = 0;
   CUDA_TRY(cudaMemcpyAsync(&tot, h->total, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
   TRY(sync(h));
-  dfree(h, blank); dfree(h, w64); dfree(h, w32);
   h->ndof = tot;
   const auto tp1 = std::chrono::steady_clock::now();
   TRY(build_hierarchy(h, o.coarsest_max));

@@ -532,10 +532,10 @@ __global__ void k_level_masks(Grid g, Box b, const double *nvert, uint8_t *blank
   int i, j, k;
   box_ijk(b, c, i, j, k);
   double nv = nvert[g.at(i + 1, j + 1, k + 1)];
-  blank[c] = nv > 0.1 ? 1 : 0;
   double w = 1 - nv > 0. ? 1 - nv : 0.;
-  w64[c] = w;
-  w32[c] = (float)w;
+  if (blank) blank[c] = nv > 0.1 ? 1 : 0;  // (null outputs are skipped)
+  if (w64) w64[c] = w;
+  if (w32) w32[c] = (float)w;
   if (aj_box) aj_box[c] = aj_da[g.at(i + 1, j + 1, k + 1)];
 }
 

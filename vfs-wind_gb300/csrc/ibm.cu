@@ -192,24 +192,26 @@ __global__ void __launch_bounds__(512) k_cent_blocks(Grid g, const double *__res
   }
 }
 
-// One thread tests one block's bounds; a warp then walks the cells of each
-// of its blocks that meet the hash box (box: atomic min/max of i, j, k).
-__global__ void __launch_bounds__(256) k_ibm_box_blocks(Grid g, const double *__restrict__ cent,
-                                                        const double *__restrict__ bbox, int nbx, int nby,
-                                                        int nblocks, HashBox H, int *box) {
-  const int b = blockIdx.x * blockDim.x + threadIdx.x, lane = threadIdx.x & 31;
-  bool hit = false;
-  if (b < nblocks) {
-    const double *q = bbox + (size_t)b * 6;
-    hit = q[3] > H.xmin && q[0] < H.xmax && q[4] > H.ymin && q[1] < H.ymax && q[5] > H.zmin && q[2] < H.zmax;
-  }
-  unsigned m = __ballot_sync(0xffffffffu, hit);
-  while (m) {
-    const int src = __ffs(m) - 1;
-    m &= m - 1;
-    const int bb = b - lane + src;
+// One thread tests one block's bounds and lists the block when they meet
+// the hash box (box[6]: the count); then every thread block of a fixed grid
+// takes listed blocks in turn and tests their cells, two per thread (box[0..5]:
+// atomic min/max of i, j, k), so that a large box's blocks spread over the
+// whole GPU.
+__global__ void __launch_bounds__(256) k_ibm_box_hits(const double *__restrict__ bbox, int nblocks, HashBox H,
+                                                      int *box, int *hits) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= nblocks) return;
+  const double *q = bbox + (size_t)b * 6;
+  if (q[3] > H.xmin && q[0] < H.xmax && q[4] > H.ymin && q[1] < H.ymax && q[5] > H.zmin && q[2] < H.zmax)
+    hits[atomicAdd(&box[6], 1)] = b;
+}
+__global__ void __launch_bounds__(256) k_ibm_box_cells(Grid g, const double *__restrict__ cent, int nbx, int nby,
+                                                       HashBox H, const int *__restrict__ hits, int *box) {
+  const int nh = *(volatile int *)&box[6];
+  for (int w = blockIdx.x; w < nh; w += gridDim.x) {
+    const int bb = hits[w];
     const int bi = bb % nbx, bj = (bb / nbx) % nby, bk = bb / (nbx * nby);
-    for (int c = lane; c < kCentBlock * kCentBlock * kCentBlock; c += 32) {
+    for (int c = threadIdx.x; c < kCentBlock * kCentBlock * kCentBlock; c += blockDim.x) {
       const int i = 1 + bi * kCentBlock + (c & 7), j = 1 + bj * kCentBlock + ((c >> 3) & 7),
                 k = 1 + bk * kCentBlock + (c >> 6);
       if (i >= g.mx - 1 || j >= g.my - 1 || k >= g.mz - 1) continue;
@@ -647,7 +649,7 @@ int ibm_search_impl(vfs_poisson *h, int ibi, int n_v, const double *xyz, int n_e
   void **buf = cx.scratch->buf;
   size_t sizes[11] = {col_start.size() * 4, std::max<size_t>(col_tri.size(), 1) * 4,
                       std::max<size_t>(col_kmax.size(), 1) * 4, tv.size() * 8, nf.size() * 8, s_tab.size() * 8,
-                      N * 8, N * 8, 4, N, 6 * 4};
+                      N * 8, N * 8, 4, N, 7 * 4};
   cudaStream_t st = cx.stream;
   for (int q = 0; q < 11; q++)
     if (cx.scratch->cap[q] < sizes[q]) {
@@ -691,7 +693,7 @@ int ibm_search_impl(vfs_poisson *h, int ibi, int n_v, const double *xyz, int n_e
     // marks are finished (no 2 or 4 is left) and the wall rows' rule gives
     // what it gave before.  So both passes run on that index box, grown by
     // one cell for the dilation and by one more for the copy it reads.
-    int init[6] = {INT_MAX, INT_MAX, INT_MAX, INT_MIN, INT_MIN, INT_MIN}, bx[6];
+    int init[7] = {INT_MAX, INT_MAX, INT_MAX, INT_MIN, INT_MIN, INT_MIN, 0}, bx[6];
     int *dbox = (int *)buf[10];
     const int nbx = (g.mx - 2 + kCentBlock - 1) / kCentBlock, nby = (g.my - 2 + kCentBlock - 1) / kCentBlock,
               nbz = (g.mz - 2 + kCentBlock - 1) / kCentBlock, nblocks = nbx * nby * nbz;
@@ -716,10 +718,25 @@ int ibm_search_impl(vfs_poisson *h, int ibi, int n_v, const double *xyz, int n_e
       *cx.launches += 1;
       sc.bbox_valid = true;
     }
+    if (sc.hits_cap < (size_t)nblocks * 4) {
+      if (sc.hits) {
+        cudaStreamSynchronize(st);
+        cudaFree(sc.hits);
+      }
+      sc.hits = nullptr;
+      sc.hits_cap = 0;
+      if (cudaMalloc(&sc.hits, (size_t)nblocks * 4) != cudaSuccess) {
+        cudaGetLastError();
+        sc.hits = nullptr;
+        return fail(VFS_ENOMEM, "device allocation for the surface search failed");
+      }
+      sc.hits_cap = (size_t)nblocks * 4;
+    }
     cudaMemcpyAsync(dbox, init, sizeof(init), cudaMemcpyHostToDevice, st);
-    k_ibm_box_blocks<<<(nblocks + 255) / 256, 256, 0, st>>>(g, cx.cent, sc.bbox, nbx, nby, nblocks, H, dbox);
+    k_ibm_box_hits<<<(nblocks + 255) / 256, 256, 0, st>>>(sc.bbox, nblocks, H, dbox, sc.hits);
+    k_ibm_box_cells<<<152 * 4, 256, 0, st>>>(g, cx.cent, nbx, nby, H, sc.hits, dbox);
     cudaMemcpyAsync(bx, dbox, sizeof(bx), cudaMemcpyDeviceToHost, st);
-    *cx.launches += 1;
+    *cx.launches += 2;
     cudaError_t eb = cudaStreamSynchronize(st);
     if (eb != cudaSuccess) {
       cudaGetLastError();

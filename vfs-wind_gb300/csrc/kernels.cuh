@@ -208,6 +208,8 @@ struct IbmScratch {
   double *bbox = nullptr;
   size_t bbox_cap = 0;
   bool bbox_valid = false;
+  int *hits = nullptr;  // the blocks that meet a body's hash box
+  size_t hits_cap = 0;
 };
 struct IbmContext {
   cudaStream_t stream;

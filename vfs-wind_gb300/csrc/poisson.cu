@@ -2101,6 +2101,7 @@ void vfs_poisson_destroy(vfs_poisson *h) {
   for (void *p : h->ibm_scratch.buf)
     if (p) cudaFree(p);
   if (h->ibm_scratch.bbox) cudaFree(h->ibm_scratch.bbox);
+  if (h->ibm_scratch.hits) cudaFree(h->ibm_scratch.hits);
   for (auto &b : h->ibm_bodies) {
     if (b.nodes) cudaFree(b.nodes);
     if (b.tri) cudaFree(b.tri);

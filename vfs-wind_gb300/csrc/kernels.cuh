@@ -48,6 +48,11 @@ __global__ void k_assemble(Grid g, Box b, const double *nvert, MetricPtrs m, int
                            uint8_t *rowtype, LevelSet ls);
 __global__ void k_assemble_fine(Grid g, Box b, const double *nvert, MetricPtrs m, double *A0, uint8_t *rowtype0,
                                 double *A1, uint8_t *rowtype1, LevelSet ls);
+__global__ void k_assemble_fine_rows(Grid g, Box b, const double *nvert, MetricPtrs m, double *A0, uint8_t *rowtype0,
+                                     double *A1, uint8_t *rowtype1, LevelSet ls, const int *rows, const int *nrows);
+__global__ void k_mask_changed(size_t N, const double *a, const double *b, uint8_t *chg);
+__global__ void k_dilate_axis(Grid g, int axis, int R, const uint8_t *src, uint8_t *dst);
+__global__ void k_list_rows(Grid g, Box b, const uint8_t *flag, int *rows, int *nrows, uint8_t *colflag);
 __global__ void k_projection_coef(Grid g, Box b, MetricPtrs m, double *pc);
 __global__ void k_level_masks(Grid g, Box b, const double *nvert, uint8_t *blank, double *w64, float *w32,
                               double *aj_box, const double *aj_da);
@@ -93,7 +98,7 @@ __global__ void k_prolong_f64(Box bf, Box bc, int cx, int cy, int cz, const doub
 // solve.cu (hot loop kernels)
 #define TYPED_DECL(T, S)                                                                                 \
   __global__ void k_residual_##S(Box b, const T *A, const T *x, const T *rhs, T *r, int color);          \
-  __global__ void k_line_lu_##S(Box b, const double *A64, T *inv, T *cp);                                \
+  __global__ void k_line_lu_##S(Box b, const double *A64, T *inv, T *cp, const uint8_t *colflag);        \
   __global__ void k_line_sweep_##S(Box b, const T *A, const T *inv, const T *cp, const T *x, const T *rhs, \
                                    T *xo, T omega, int zero_guess);                                      \
   __global__ void k_line_tri_##S(Box b, const T *r, const T *Asp, const T *inv, const T *cp, T *x, T omega,  \
@@ -106,6 +111,8 @@ TYPED_DECL(double, f64)
 #undef TYPED_DECL
 
 __global__ void k_pack16(size_t n, const double *A, __half2 *C, float *D);
+__global__ void k_pack16_rows(Box b, const double *A, __half2 *C, float *D, float *A32, const int *rows,
+                              const int *nrows);
 __global__ void k_residual16(Box b, const __half2 *C, const float *D, const float *x, const float *rhs, float *r,
                              int color);
 __global__ void k_residual16_split(Box b, const __half2 *C, const float *D, const float *x, const float *rhs, float *r,

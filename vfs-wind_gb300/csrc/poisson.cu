@@ -485,6 +485,15 @@ struct vfs_poisson {
   // dependent launch; VFS_PDL=0 at create turns it off); pdl_prev: the last
   // operation issued on the stream was such a kernel
   bool pdl = true, pdl_prev = false;
+  // incremental refill of the finest level on a new mask (VFS_INCREMENTAL=0
+  // at create turns it off): the mask the hierarchy was last filled with
+  // (nvert_prev after the swap), the changed DA points, the rows to refill
+  // (natural box indices, count on the device) and their j-columns;
+  // inc_rows: the level-0 refill in progress uses that list
+  bool inc_enable = true, nvert_prev_valid = false, inc_rows = false;
+  double *nvert_prev = nullptr;
+  uint8_t *chg_a = nullptr, *chg_b = nullptr, *colflag = nullptr;
+  int *rows = nullptr, *nrows = nullptr;
   // history of the last hist_cnt (at most hist_cap) converged solutions for
   // the initial guess, held as the newest one X_n (the FGMRES iterate before
   // the mean removal) with its image Y_n = A X_n (b - r of its solve), stored
@@ -942,10 +951,18 @@ int build_level_operator(vfs_poisson *h, Level &l, bool assembled = false) {
     LAUNCH(h, k_assemble, box_grid(l.b), 128, l.g, l.b, l.nvert, l.met, 1, 0, 1, l.A64, l.rowtype, level_set(h, l));
   LAUNCH(h, k_level_masks, lin_grid(n), 256, l.g, l.b, l.nvert, l.blank, l.w64, l.w32, (double *)nullptr,
          (const double *)nullptr);
-  LAUNCH(h, k_line_lu_f64, dim3((l.b.nx + 127) / 128, l.b.nz), 128, l.b, l.A64, l.inv64, l.cp64);
-  LAUNCH(h, k_line_lu_f32, dim3((l.b.nx + 127) / 128, l.b.nz), 128, l.b, l.A64, l.inv32, l.cp32);
-  LAUNCH(h, k_cast_planes_f32, kRedBlocks, 256, l.A64, l.A32, n * NSLOT);
-  LAUNCH(h, k_pack16, kRedBlocks, 256, n, l.A64, l.C16, l.D32);
+  // the finest level of an incremental refill: only the listed rows'
+  // copies and the j-columns that hold one are formed again
+  const uint8_t *cols = assembled && h->inc_rows ? h->colflag : nullptr;
+  LAUNCH(h, k_line_lu_f64, dim3((l.b.nx + 127) / 128, l.b.nz), 128, l.b, l.A64, l.inv64, l.cp64, cols);
+  LAUNCH(h, k_line_lu_f32, dim3((l.b.nx + 127) / 128, l.b.nz), 128, l.b, l.A64, l.inv32, l.cp32, cols);
+  if (cols) {
+    LAUNCH(h, k_pack16_rows, kRedBlocks, 256, l.b, (const double *)l.A64, l.C16, l.D32, l.A32, (const int *)h->rows,
+           (const int *)h->nrows);
+  } else {
+    LAUNCH(h, k_cast_planes_f32, kRedBlocks, 256, l.A64, l.A32, n * NSLOT);
+    LAUNCH(h, k_pack16, kRedBlocks, 256, n, l.A64, l.C16, l.D32);
+  }
   return VFS_OK;
 }
 
@@ -2064,6 +2081,8 @@ int vfs_poisson_create(const vfs_grid_desc *gd, vfs_poisson **out) {
     h->line_cols_cap = lc ? atoi(lc) : 0;
     const char *pd = getenv("VFS_PDL");
     h->pdl = !(pd && pd[0] == '0');
+    const char *inc = getenv("VFS_INCREMENTAL");
+    h->inc_enable = !(inc && inc[0] == '0');
   }
   const size_t N = h->g.n(), n = h->box.n();
   int rc;
@@ -2128,6 +2147,7 @@ int vfs_poisson_set_grid(vfs_poisson *h, const double *coor, const double *const
   if (!h || !coor) return fail(VFS_EINVAL, "null argument");
   h->hier_cmax = -1;  // new coordinates: the next mask builds the hierarchy afresh
   h->ibm_scratch.bbox_valid = false;  // and the next search bounds the new centres
+  h->nvert_prev_valid = false;        // and the next mask fills every row
   const size_t N = h->g.n();
   TRY(upload(h, h->coor, coor, 3 * N));
   TRY(form_metrics(h, h->g, h->coor, h->met));
@@ -2151,6 +2171,24 @@ int vfs_poisson_set_nvert(vfs_poisson *h, const double *nvert) {
   if (!h->have_grid) return fail(VFS_ESTATE, "set_grid must come before set_nvert");
   const size_t N = h->g.n(), n = h->box.n();
   const auto tp0 = std::chrono::steady_clock::now();
+  vfs_solve_opts o;
+  vfs_poisson_default_opts(&o);
+  const bool refills = hierarchy_refills(h, o.coarsest_max);
+  // a new mask on a filled hierarchy without a level set refills only the
+  // finest-level rows next to the changed points; the mask it was filled
+  // with is kept (two buffers, swapped) to find them
+  const bool incremental = refills && h->inc_enable && !h->ls_on && h->nvert_prev_valid;
+  h->nvert_prev_valid = false;
+  h->inc_rows = false;
+  if (h->inc_enable && !h->nvert_prev) {
+    TRY(dalloc(h, &h->nvert_prev, N));
+    TRY(dalloc(h, &h->chg_a, N));
+    TRY(dalloc(h, &h->chg_b, N));
+    TRY(dalloc(h, &h->colflag, (size_t)h->box.nx * h->box.nz));
+    TRY(dalloc(h, &h->rows, n));
+    TRY(dalloc(h, &h->nrows, 1));
+  }
+  if (incremental) std::swap(h->nvert, h->nvert_prev);
   TRY(upload(h, h->nvert, nvert, N));
   // setup_lidx2: dof numbering in k-j-i order
   const int nblk = (int)((n + 1023) / 1024);
@@ -2165,12 +2203,21 @@ int vfs_poisson_set_nvert(vfs_poisson *h, const double *nvert) {
     fls.rho = h->ls_rho; fls.level = h->ls_level; fls.on = 1;
     fls.bc3 = h->ls_bc3; fls.bc4 = h->ls_bc4; fls.bc5 = h->ls_bc5;
   }
-  vfs_solve_opts o;
-  vfs_poisson_default_opts(&o);
-  if (hierarchy_refills(h, o.coarsest_max))  // both fine operators from one evaluation of each row
+  if (incremental) {
+    LAUNCH(h, k_mask_changed, kRedBlocks, 256, N, (const double *)h->nvert, (const double *)h->nvert_prev, h->chg_a);
+    LAUNCH(h, k_dilate_axis, kRedBlocks, 256, h->g, 0, 2, (const uint8_t *)h->chg_a, h->chg_b);
+    LAUNCH(h, k_dilate_axis, kRedBlocks, 256, h->g, 1, 2, (const uint8_t *)h->chg_b, h->chg_a);
+    LAUNCH(h, k_dilate_axis, kRedBlocks, 256, h->g, 2, 2, (const uint8_t *)h->chg_a, h->chg_b);
+    CUDA_TRY(cudaMemsetAsync(h->nrows, 0, sizeof(int), h->stream));
+    CUDA_TRY(cudaMemsetAsync(h->colflag, 0, (size_t)h->box.nx * h->box.nz, h->stream));
+    LAUNCH(h, k_list_rows, kRedBlocks, 256, h->g, h->box, (const uint8_t *)h->chg_b, h->rows, h->nrows, h->colflag);
+    LAUNCH(h, k_assemble_fine_rows, kRedBlocks, 256, h->g, h->box, h->nvert, h->met, h->A0, h->rowtype0,
+           h->L[0].A64, h->L[0].rowtype, fls, (const int *)h->rows, (const int *)h->nrows);
+    h->inc_rows = true;
+  } else if (refills) {  // both fine operators from one evaluation of each row
     LAUNCH(h, k_assemble_fine, box_grid(h->box), 128, h->g, h->box, h->nvert, h->met, h->A0, h->rowtype0,
            h->L[0].A64, h->L[0].rowtype, fls);
-  else
+  } else
     LAUNCH(h, k_assemble, box_grid(h->box), 128, h->g, h->box, h->nvert, h->met, 0, 1, 0, h->A0, h->rowtype0, fls);
   // aj at the box cells for the row scale (each level forms its own masks)
   LAUNCH(h, k_level_masks, lin_grid(n), 256, h->g, h->box, h->nvert, (uint8_t *)nullptr, (double *)nullptr,
@@ -2183,6 +2230,8 @@ int vfs_poisson_set_nvert(vfs_poisson *h, const double *nvert) {
   h->ndof = tot;
   const auto tp1 = std::chrono::steady_clock::now();
   TRY(build_hierarchy(h, o.coarsest_max));
+  h->inc_rows = false;
+  h->nvert_prev_valid = h->inc_enable;  // nvert now holds the mask every row was filled with
   if (h->phase)
     fprintf(stderr, "vfs set_nvert ms: numbering+fine operators+masks %.3f hierarchy %.3f\n",
             std::chrono::duration<double, std::milli>(tp1 - tp0).count(),

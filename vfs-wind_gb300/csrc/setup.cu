@@ -475,10 +475,9 @@ __global__ void k_assemble(Grid g, Box b, const double *__restrict__ nvert, Metr
 // and the aj-scaled one without the filter in the parity-split layout (A1,
 // the finest multigrid level: scale 1, filter 0, split 1); the same values
 // as the two k_assemble passes.
-__global__ void k_assemble_fine(Grid g, Box b, const double *__restrict__ nvert, MetricPtrs m, double *A0,
-                                uint8_t *rowtype0, double *A1, uint8_t *rowtype1, LevelSet ls) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y, k = blockIdx.z;
-  if (i >= b.nx) return;
+__device__ __forceinline__ void assemble_fine_cell(const Grid &g, const Box &b, const double *__restrict__ nvert,
+                                                   const MetricPtrs &m, double *A0, uint8_t *rowtype0, double *A1,
+                                                   uint8_t *rowtype1, const LevelSet &ls, int i, int j, int k) {
   const size_t n = b.n(), c0 = b.at(i, j, k), c1 = b.at(split_pos(i, b.nx), j, k);
   const int I = i + 1, J = j + 1, K = k + 1;
   const size_t t = g.at(I, J, K);
@@ -504,6 +503,69 @@ __global__ void k_assemble_fine(Grid g, Box b, const double *__restrict__ nvert,
     A1[s * n + c1] = col ? v[s] * a : 0.0;
   }
   rowtype0[c0] = rowtype1[c0] = 1;
+}
+__global__ void k_assemble_fine(Grid g, Box b, const double *__restrict__ nvert, MetricPtrs m, double *A0,
+                                uint8_t *rowtype0, double *A1, uint8_t *rowtype1, LevelSet ls) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y, k = blockIdx.z;
+  if (i >= b.nx) return;
+  assemble_fine_cell(g, b, nvert, m, A0, rowtype0, A1, rowtype1, ls, i, j, k);
+}
+// the same rows, only those listed (natural box indices rows[0 .. *nrows))
+__global__ void k_assemble_fine_rows(Grid g, Box b, const double *__restrict__ nvert, MetricPtrs m, double *A0,
+                                     uint8_t *rowtype0, double *A1, uint8_t *rowtype1, LevelSet ls,
+                                     const int *__restrict__ rows, const int *__restrict__ nrows) {
+  const int nr = *nrows;
+  for (int w = blockIdx.x * blockDim.x + threadIdx.x; w < nr; w += gridDim.x * blockDim.x) {
+    int i, j, k;
+    box_ijk(b, (size_t)rows[w], i, j, k);
+    assemble_fine_cell(g, b, nvert, m, A0, rowtype0, A1, rowtype1, ls, i, j, k);
+  }
+}
+
+// ---- incremental refill of the finest level on a new mask ----
+// A row of the operator reads nvert within one point of its own (the
+// one-sided differences and the neighbours' dof tests), where a periodic
+// ghost neighbour's dof test reads its interior partner.  The rows to refill
+// are those within two points of a point whose value changed, the periodic
+// partners of ghost points included; every other row is the same as before.
+__global__ void k_mask_changed(size_t N, const double *__restrict__ a, const double *__restrict__ b,
+                               uint8_t *__restrict__ chg) {
+  for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < N; t += (size_t)gridDim.x * blockDim.x)
+    chg[t] = a[t] != b[t] ? 1 : 0;
+}
+// dilation by R points along one axis (0: i, 1: j, 2: k) of the DA points,
+// a ghost point of a periodic axis also standing for its interior partner
+__global__ void k_dilate_axis(Grid g, int axis, int R, const uint8_t *__restrict__ src, uint8_t *__restrict__ dst) {
+  const size_t N = g.n();
+  for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < N; t += (size_t)gridDim.x * blockDim.x) {
+    const int i = (int)(t % g.mx), j = (int)((t / g.mx) % g.my), k = (int)(t / ((size_t)g.mx * g.my));
+    const int x = axis == 0 ? i : axis == 1 ? j : k, m = axis == 0 ? g.mx : axis == 1 ? g.my : g.mz;
+    const bool per = axis == 0 ? g.px : axis == 1 ? g.py : g.pz;
+    uint8_t f = 0;
+    for (int d = -R; d <= R && !f; d++) {
+      const int q = min(max(x + d, 0), m - 1);
+      const int qa = per && q == 0 ? m - 2 : per && q == m - 1 ? 1 : q;
+      for (int u = 0; u < 2; u++) {
+        const int qq = u ? qa : q;
+        const size_t s = axis == 0 ? g.at(qq, j, k) : axis == 1 ? g.at(i, qq, k) : g.at(i, j, qq);
+        f |= src[s];
+      }
+    }
+    dst[t] = f;
+  }
+}
+// the interior rows at flagged points (natural box indices, in no order)
+// and the j-columns that hold one
+__global__ void k_list_rows(Grid g, Box b, const uint8_t *__restrict__ flag, int *rows, int *nrows,
+                            uint8_t *colflag) {
+  const size_t n = b.n();
+  for (size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (size_t)gridDim.x * blockDim.x) {
+    int i, j, k;
+    box_ijk(b, c, i, j, k);
+    if (!flag[g.at(i + 1, j + 1, k + 1)]) continue;
+    rows[atomicAdd(nrows, 1)] = (int)c;
+    colflag[(size_t)k * b.nx + i] = 1;
+  }
 }
 
 // Per-face dot products S = a.b of the projection and the face aj, so that

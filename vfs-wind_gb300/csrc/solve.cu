@@ -54,16 +54,33 @@ __device__ __forceinline__ void residual_body(Box b, const T *__restrict__ A, co
 // diagonal; half2 plane m < 9 holds the couplings of slots 2m+1 and 2m+2
 // divided by D, plane 9 the row sum divided by D (0 for the Neumann rows).
 // Rows without a dof get D = 0 and zero couplings.
+__device__ __forceinline__ void pack16_row(size_t n, const double *__restrict__ A, __half2 *__restrict__ C,
+                                           float *__restrict__ D, size_t c) {
+  const double d = A[CP * n + c];
+  const double inv = d != 0. ? 1. / d : 0.;
+  double sum = d;
+  for (int q = 1; q < NSLOT; q++) sum += A[q * n + c];
+  for (int m = 0; m < 9; m++)
+    C[m * n + c] = __halves2half2(__double2half(A[(2 * m + 1) * n + c] * inv), __double2half(A[(2 * m + 2) * n + c] * inv));
+  C[9 * n + c] = __halves2half2(__double2half(sum * inv), __double2half(0.));
+  D[c] = (float)d;
+}
 __global__ void k_pack16(size_t n, const double *__restrict__ A, __half2 *__restrict__ C, float *__restrict__ D) {
-  for (size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (size_t)gridDim.x * blockDim.x) {
-    const double d = A[CP * n + c];
-    const double inv = d != 0. ? 1. / d : 0.;
-    double sum = d;
-    for (int q = 1; q < NSLOT; q++) sum += A[q * n + c];
-    for (int m = 0; m < 9; m++)
-      C[m * n + c] = __halves2half2(__double2half(A[(2 * m + 1) * n + c] * inv), __double2half(A[(2 * m + 2) * n + c] * inv));
-    C[9 * n + c] = __halves2half2(__double2half(sum * inv), __double2half(0.));
-    D[c] = (float)d;
+  for (size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (size_t)gridDim.x * blockDim.x)
+    pack16_row(n, A, C, D, c);
+}
+// The finest level's packed copy and FP32 planes of the listed rows only
+// (natural box indices; the level's operator is stored split).
+__global__ void k_pack16_rows(Box b, const double *__restrict__ A, __half2 *__restrict__ C, float *__restrict__ D,
+                              float *__restrict__ A32, const int *__restrict__ rows, const int *__restrict__ nrows) {
+  const size_t n = b.n();
+  const int nr = *nrows;
+  for (int w = blockIdx.x * blockDim.x + threadIdx.x; w < nr; w += gridDim.x * blockDim.x) {
+    int i, j, k;
+    box_ijk(b, (size_t)rows[w], i, j, k);
+    const size_t c = b.at(split_pos(i, b.nx), j, k);
+    pack16_row(n, A, C, D, c);
+    for (int q = 0; q < NSLOT; q++) A32[q * n + c] = (float)A[q * n + c];
   }
 }
 
@@ -176,9 +193,11 @@ __global__ void __launch_bounds__(256) k_residual64(Box b, const double *__restr
 // operator, computed in FP64 and stored in T.  Rows without a dof get an
 // identity line entry.  The j-periodic wrap couplings stay off the line.
 template <typename T>
-__device__ __forceinline__ void line_lu_body(Box b, const double *__restrict__ A, T *inv, T *cp) {
+__device__ __forceinline__ void line_lu_body(Box b, const double *__restrict__ A, T *inv, T *cp,
+                                             const uint8_t *__restrict__ colflag) {
   int i = blockIdx.x * blockDim.x + threadIdx.x, k = blockIdx.y;
   if (i >= b.nx) return;
+  if (colflag && !colflag[(size_t)k * b.nx + i]) return;  // (a column left as it was)
   const size_t n = b.n();
   double cprev = 0.;
   const int p = split_pos(i, b.nx);
@@ -1152,7 +1171,9 @@ void launch_hist_push(cudaStream_t st, int blocks, size_t n, const double *x, co
                                                         int color) {                                       \
     residual_body<T>(b, A, x, rhs, r, color);                                                              \
   }                                                                                                        \
-  __global__ void k_line_lu_##S(Box b, const double *A64, T *inv, T *cp) { line_lu_body<T>(b, A64, inv, cp); } \
+  __global__ void k_line_lu_##S(Box b, const double *A64, T *inv, T *cp, const uint8_t *colflag) {            \
+    line_lu_body<T>(b, A64, inv, cp, colflag);                                                            \
+  }                                                                                                        \
   __global__ void __launch_bounds__(768, 1) k_line_sweep_##S(Box b, const T *A, const T *inv, const T *cp,      \
                                                            const T *x, const T *rhs, T *xo, T omega, int zg) { \
     line_sweep_body<T, kLineChunk>(b, A, inv, cp, x, rhs, xo, omega, zg);                                   \

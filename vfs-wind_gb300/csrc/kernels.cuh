@@ -48,6 +48,8 @@ __global__ void k_assemble(Grid g, Box b, const double *nvert, MetricPtrs m, int
                            uint8_t *rowtype, LevelSet ls);
 __global__ void k_assemble_fine(Grid g, Box b, const double *nvert, MetricPtrs m, double *A0, uint8_t *rowtype0,
                                 double *A1, uint8_t *rowtype1, LevelSet ls);
+__global__ void k_assemble_rows(Grid g, Box b, const double *nvert, MetricPtrs m, int scale, int filter, int split,
+                                double *A, uint8_t *rowtype, LevelSet ls, const int *rows, const int *nrows);
 __global__ void k_assemble_fine_rows(Grid g, Box b, const double *nvert, MetricPtrs m, double *A0, uint8_t *rowtype0,
                                      double *A1, uint8_t *rowtype1, LevelSet ls, const int *rows, const int *nrows);
 __global__ void k_mask_changed(size_t N, const double *a, const double *b, uint8_t *chg);

@@ -413,6 +413,7 @@ struct Level {
   Box b{};
   int cx = 0, cy = 0, cz = 0;
   double *coor = nullptr, *nvert = nullptr;
+  double *nvert_prev = nullptr;  // the restricted mask of the previous fill (coarse levels, incremental refill)
   MetricPtrs met{};
   bool own_met = false;
   double *A64 = nullptr;
@@ -898,7 +899,7 @@ int build_coarsest(vfs_poisson *h, Level &l) {
 }
 
 void free_level(vfs_poisson *h, Level &l, bool level0) {
-  if (!level0) { dfree(h, l.coor); dfree(h, l.nvert); dfree(h, l.rho); dfree(h, l.level); }
+  if (!level0) { dfree(h, l.coor); dfree(h, l.nvert); dfree(h, l.nvert_prev); dfree(h, l.rho); dfree(h, l.level); }
   if (l.own_met) free_metrics(h, l.met);
   dfree(h, l.A64); dfree(h, l.A32); dfree(h, l.C16); dfree(h, l.D32); dfree(h, l.rowtype); dfree(h, l.blank);
   dfree(h, l.inv64); dfree(h, l.cp64); dfree(h, l.w64); dfree(h, l.inv32); dfree(h, l.cp32); dfree(h, l.w32);
@@ -947,13 +948,16 @@ int build_level_operator(vfs_poisson *h, Level &l, bool assembled = false) {
     TRY(dalloc(h, &l.inv32, n)); TRY(dalloc(h, &l.cp32, n));
     for (int q = 0; q < 4; q++) { TRY(dalloc(h, &l.v64[q], n)); TRY(dalloc(h, &l.v32[q], n)); }
   }
-  if (!assembled)
+  if (!assembled && h->inc_rows)
+    LAUNCH(h, k_assemble_rows, kRedBlocks, 256, l.g, l.b, l.nvert, l.met, 1, 0, 1, l.A64, l.rowtype, level_set(h, l),
+           (const int *)h->rows, (const int *)h->nrows);
+  else if (!assembled)
     LAUNCH(h, k_assemble, box_grid(l.b), 128, l.g, l.b, l.nvert, l.met, 1, 0, 1, l.A64, l.rowtype, level_set(h, l));
   LAUNCH(h, k_level_masks, lin_grid(n), 256, l.g, l.b, l.nvert, l.blank, l.w64, l.w32, (double *)nullptr,
          (const double *)nullptr);
-  // the finest level of an incremental refill: only the listed rows'
-  // copies and the j-columns that hold one are formed again
-  const uint8_t *cols = assembled && h->inc_rows ? h->colflag : nullptr;
+  // a level of an incremental refill: only the listed rows' copies and the
+  // j-columns that hold one are formed again
+  const uint8_t *cols = h->inc_rows ? h->colflag : nullptr;
   LAUNCH(h, k_line_lu_f64, dim3((l.b.nx + 127) / 128, l.b.nz), 128, l.b, l.A64, l.inv64, l.cp64, cols);
   LAUNCH(h, k_line_lu_f32, dim3((l.b.nx + 127) / 128, l.b.nz), 128, l.b, l.A64, l.inv32, l.cp32, cols);
   if (cols) {
@@ -977,8 +981,15 @@ int refresh_hierarchy(vfs_poisson *h) {
   h->L[0].nvert = h->nvert;
   h->L[0].rho = h->ls_rho;
   h->L[0].level = h->ls_level;
+  // an incremental refill keeps each coarse level's previous mask to find
+  // the rows to refill there too
+  const bool incremental = h->inc_rows;
   for (size_t li = 1; li < h->L.size(); li++) {
     Level &f = h->L[li - 1], &q = h->L[li];
+    if (incremental) {
+      if (!q.nvert_prev) TRY(dalloc(h, &q.nvert_prev, q.g.n()));
+      std::swap(q.nvert, q.nvert_prev);
+    }
     LAUNCH(h, k_nvert_restrict, da_grid(q.g), 128, f.g, q.g, f.cx, f.cy, f.cz, f.nvert, h->stage);
     LAUNCH(h, k_nvert_fill, da_grid(q.g), 128, q.g, h->stage, q.nvert);
     if (h->ls_on) {
@@ -987,14 +998,42 @@ int refresh_hierarchy(vfs_poisson *h) {
     }
   }
   const auto t0 = std::chrono::steady_clock::now();
-  for (size_t li = 0; li < h->L.size(); li++) TRY(build_level_operator(h, h->L[li], li == 0));
+  for (size_t li = 0; li < h->L.size(); li++) {
+    Level &l = h->L[li];
+    if (li > 0 && incremental) {
+      // the rows of this level within two points of a changed restricted
+      // mask value (the list buffers of the finest level, consumed by its
+      // launches above, are reused in stream order)
+      LAUNCH(h, k_mask_changed, kRedBlocks, 256, l.g.n(), (const double *)l.nvert, (const double *)l.nvert_prev,
+             h->chg_a);
+      LAUNCH(h, k_dilate_axis, kRedBlocks, 256, l.g, 0, 2, (const uint8_t *)h->chg_a, h->chg_b);
+      LAUNCH(h, k_dilate_axis, kRedBlocks, 256, l.g, 1, 2, (const uint8_t *)h->chg_b, h->chg_a);
+      LAUNCH(h, k_dilate_axis, kRedBlocks, 256, l.g, 2, 2, (const uint8_t *)h->chg_a, h->chg_b);
+      CUDA_TRY(cudaMemsetAsync(h->nrows, 0, sizeof(int), h->stream));
+      CUDA_TRY(cudaMemsetAsync(h->colflag, 0, (size_t)l.b.nx * l.b.nz, h->stream));
+      LAUNCH(h, k_list_rows, kRedBlocks, 256, l.g, l.b, (const uint8_t *)h->chg_b, h->rows, h->nrows, h->colflag);
+    }
+    TRY(build_level_operator(h, l, li == 0));
+  }
+  h->inc_rows = false;
   if (h->phase) TRY(sync(h));
   const auto t1 = std::chrono::steady_clock::now();
   Level &c = h->L.back();
-  dfree(h, c.didx); dfree(h, c.dmap); dfree(h, c.dinv);
-  c.didx = c.dmap = nullptr;
-  c.dinv = nullptr;
-  TRY(build_coarsest(h, c));
+  // an incremental refill that listed no row of the coarsest level (the
+  // last list formed above) leaves its operator, and so its inverse, as it was
+  bool same = false;
+  if (incremental && c.dinv) {
+    int nr = -1;
+    CUDA_TRY(cudaMemcpyAsync(&nr, h->nrows, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    TRY(sync(h));
+    same = nr == 0;
+  }
+  if (!same) {
+    dfree(h, c.didx); dfree(h, c.dmap); dfree(h, c.dinv);
+    c.didx = c.dmap = nullptr;
+    c.dinv = nullptr;
+    TRY(build_coarsest(h, c));
+  }
   TRY(sync(h));
   if (h->phase)
     fprintf(stderr, "vfs refill ms: level operators %.3f coarsest %.3f\n",

@@ -435,10 +435,9 @@ __device__ void assemble_row(const Grid &g, const double *nvert, const MetricPtr
 // multigrid levels; split: store rows in the parity-split row layout of the
 // multigrid levels (rowtype stays natural).  Slots whose column has no dof
 // are zero (idx < 0).
-__global__ void k_assemble(Grid g, Box b, const double *__restrict__ nvert, MetricPtrs m, int scale,
-                           int filter, int split, double *A, uint8_t *rowtype, LevelSet ls) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y, k = blockIdx.z;
-  if (i >= b.nx) return;
+__device__ __forceinline__ void assemble_cell(const Grid &g, const Box &b, const double *__restrict__ nvert,
+                                              const MetricPtrs &m, int scale, int filter, int split, double *A,
+                                              uint8_t *rowtype, const LevelSet &ls, int i, int j, int k) {
   const size_t n = b.n(), c = split ? b.at(split_pos(i, b.nx), j, k) : b.at(i, j, k);
   const size_t cr = b.at(i, j, k);
   const int I = i + 1, J = j + 1, K = k + 1;
@@ -467,6 +466,23 @@ __global__ void k_assemble(Grid g, Box b, const double *__restrict__ nvert, Metr
     A[s * n + c] = keep ? v[s] : 0.0;
   }
   rowtype[cr] = 1;
+}
+__global__ void k_assemble(Grid g, Box b, const double *__restrict__ nvert, MetricPtrs m, int scale,
+                           int filter, int split, double *A, uint8_t *rowtype, LevelSet ls) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y, k = blockIdx.z;
+  if (i >= b.nx) return;
+  assemble_cell(g, b, nvert, m, scale, filter, split, A, rowtype, ls, i, j, k);
+}
+// the same rows, only those listed (natural box indices rows[0 .. *nrows))
+__global__ void k_assemble_rows(Grid g, Box b, const double *__restrict__ nvert, MetricPtrs m, int scale,
+                                int filter, int split, double *A, uint8_t *rowtype, LevelSet ls,
+                                const int *__restrict__ rows, const int *__restrict__ nrows) {
+  const int nr = *nrows;
+  for (int w = blockIdx.x * blockDim.x + threadIdx.x; w < nr; w += gridDim.x * blockDim.x) {
+    int i, j, k;
+    box_ijk(b, (size_t)rows[w], i, j, k);
+    assemble_cell(g, b, nvert, m, scale, filter, split, A, rowtype, ls, i, j, k);
+  }
 }
 
 // The fine level's two assemblies from one evaluation of each row: the

@@ -155,9 +155,6 @@ __global__ void k_ibm_classify_from(Grid g, const double *__restrict__ cent, int
   if (is4) is4[t] = (int)((nv < 0 ? 0. : nv) + 0.5) == 4;
 }
 
-// index box of the interior cells whose centre lies strictly inside the
-// body's hash box (the cells the classification can change): atomic
-// min / max into box[0..2] / box[3..5]
 // The search of a body after the first needs the index box of the interior
 // cells whose centre lies strictly inside its hash box.  The centres are
 // bounded per block of 8x8x8 interior cells once per grid (k_cent_blocks);

@@ -24,11 +24,27 @@ def _mask(s, case, x0):
     return CF.sync_periodic_ghosts(nv, case.periodic)
 
 
+def _solver(case, incremental):
+    import os
+    import vfs_poisson as V
+    old = os.environ.get("VFS_INCREMENTAL")
+    try:
+        os.environ["VFS_INCREMENTAL"] = "1" if incremental else "0"
+        return V.PoissonSolver(*case.dims, periodic=case.periodic)
+    finally:
+        if old is None:
+            os.environ.pop("VFS_INCREMENTAL", None)
+        else:
+            os.environ["VFS_INCREMENTAL"] = old
+
+
+@pytest.mark.parametrize("incremental", [True, False], ids=["incremental", "full"])
 @pytest.mark.parametrize("xs", [(0.03, 0.97, 0.5, 0.03), (0.5, 0.52, 0.5)], ids=["seam", "interior"])
-def test_incremental_refill_matches_fresh(cuda_lib, xs):
+def test_refill_matches_fresh(cuda_lib, xs, incremental):
+    """(With VFS_INCREMENTAL=0 every row is refilled; both must match.)"""
     import vfs_poisson as V
     case = CF.towers(40, 24, 40, radius=0.05)
-    moved = V.PoissonSolver(*case.dims, periodic=case.periodic)
+    moved = _solver(case, incremental)
     try:
         moved.set_grid(case.coor)
         for step, x0 in enumerate(xs):

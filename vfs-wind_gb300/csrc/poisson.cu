@@ -1006,9 +1006,9 @@ int refresh_hierarchy(vfs_poisson *h) {
       // launches above, are reused in stream order)
       LAUNCH(h, k_mask_changed, kRedBlocks, 256, l.g.n(), (const double *)l.nvert, (const double *)l.nvert_prev,
              h->chg_a);
-      LAUNCH(h, k_dilate_axis, kRedBlocks, 256, l.g, 0, 2, (const uint8_t *)h->chg_a, h->chg_b);
-      LAUNCH(h, k_dilate_axis, kRedBlocks, 256, l.g, 1, 2, (const uint8_t *)h->chg_b, h->chg_a);
-      LAUNCH(h, k_dilate_axis, kRedBlocks, 256, l.g, 2, 2, (const uint8_t *)h->chg_a, h->chg_b);
+      LAUNCH(h, k_dilate_axis, da_grid(l.g), 128, l.g, 0, 2, (const uint8_t *)h->chg_a, h->chg_b);
+      LAUNCH(h, k_dilate_axis, da_grid(l.g), 128, l.g, 1, 2, (const uint8_t *)h->chg_b, h->chg_a);
+      LAUNCH(h, k_dilate_axis, da_grid(l.g), 128, l.g, 2, 2, (const uint8_t *)h->chg_a, h->chg_b);
       CUDA_TRY(cudaMemsetAsync(h->nrows, 0, sizeof(int), h->stream));
       CUDA_TRY(cudaMemsetAsync(h->colflag, 0, (size_t)l.b.nx * l.b.nz, h->stream));
       LAUNCH(h, k_list_rows, kRedBlocks, 256, l.g, l.b, (const uint8_t *)h->chg_b, h->rows, h->nrows, h->colflag);
@@ -2244,9 +2244,9 @@ int vfs_poisson_set_nvert(vfs_poisson *h, const double *nvert) {
   }
   if (incremental) {
     LAUNCH(h, k_mask_changed, kRedBlocks, 256, N, (const double *)h->nvert, (const double *)h->nvert_prev, h->chg_a);
-    LAUNCH(h, k_dilate_axis, kRedBlocks, 256, h->g, 0, 2, (const uint8_t *)h->chg_a, h->chg_b);
-    LAUNCH(h, k_dilate_axis, kRedBlocks, 256, h->g, 1, 2, (const uint8_t *)h->chg_b, h->chg_a);
-    LAUNCH(h, k_dilate_axis, kRedBlocks, 256, h->g, 2, 2, (const uint8_t *)h->chg_a, h->chg_b);
+    LAUNCH(h, k_dilate_axis, da_grid(h->g), 128, h->g, 0, 2, (const uint8_t *)h->chg_a, h->chg_b);
+    LAUNCH(h, k_dilate_axis, da_grid(h->g), 128, h->g, 1, 2, (const uint8_t *)h->chg_b, h->chg_a);
+    LAUNCH(h, k_dilate_axis, da_grid(h->g), 128, h->g, 2, 2, (const uint8_t *)h->chg_a, h->chg_b);
     CUDA_TRY(cudaMemsetAsync(h->nrows, 0, sizeof(int), h->stream));
     CUDA_TRY(cudaMemsetAsync(h->colflag, 0, (size_t)h->box.nx * h->box.nz, h->stream));
     LAUNCH(h, k_list_rows, kRedBlocks, 256, h->g, h->box, (const uint8_t *)h->chg_b, h->rows, h->nrows, h->colflag);

@@ -551,24 +551,23 @@ __global__ void k_mask_changed(size_t N, const double *__restrict__ a, const dou
 }
 // dilation by R points along one axis (0: i, 1: j, 2: k) of the DA points,
 // a ghost point of a periodic axis also standing for its interior partner
+// (one thread per DA point of a (mx, my, mz) launch: no index divisions)
 __global__ void k_dilate_axis(Grid g, int axis, int R, const uint8_t *__restrict__ src, uint8_t *__restrict__ dst) {
-  const size_t N = g.n();
-  for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < N; t += (size_t)gridDim.x * blockDim.x) {
-    const int i = (int)(t % g.mx), j = (int)((t / g.mx) % g.my), k = (int)(t / ((size_t)g.mx * g.my));
-    const int x = axis == 0 ? i : axis == 1 ? j : k, m = axis == 0 ? g.mx : axis == 1 ? g.my : g.mz;
-    const bool per = axis == 0 ? g.px : axis == 1 ? g.py : g.pz;
-    uint8_t f = 0;
-    for (int d = -R; d <= R && !f; d++) {
-      const int q = min(max(x + d, 0), m - 1);
-      const int qa = per && q == 0 ? m - 2 : per && q == m - 1 ? 1 : q;
-      for (int u = 0; u < 2; u++) {
-        const int qq = u ? qa : q;
-        const size_t s = axis == 0 ? g.at(qq, j, k) : axis == 1 ? g.at(i, qq, k) : g.at(i, j, qq);
-        f |= src[s];
-      }
+  const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y, k = blockIdx.z;
+  if (i >= g.mx) return;
+  const int x = axis == 0 ? i : axis == 1 ? j : k, m = axis == 0 ? g.mx : axis == 1 ? g.my : g.mz;
+  const bool per = axis == 0 ? g.px : axis == 1 ? g.py : g.pz;
+  uint8_t f = 0;
+  for (int d = -R; d <= R && !f; d++) {
+    const int q = min(max(x + d, 0), m - 1);
+    const int qa = per && q == 0 ? m - 2 : per && q == m - 1 ? 1 : q;
+    for (int u = 0; u < 2; u++) {
+      const int qq = u ? qa : q;
+      const size_t s = axis == 0 ? g.at(qq, j, k) : axis == 1 ? g.at(i, qq, k) : g.at(i, j, qq);
+      f |= src[s];
     }
-    dst[t] = f;
   }
+  dst[g.at(i, j, k)] = f;
 }
 // the interior rows at flagged points (natural box indices, in no order)
 // and the j-columns that hold one
